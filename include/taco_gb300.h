@@ -1,0 +1,105 @@
+/* libtacogb — the GB300 (sm_103a) implementation of taco's sparse hot path behind a C ABI.
+ *
+ * Two layers are exported:
+ *
+ *  1. taco's kernel ABI.  For each of the three statements
+ *       SpMV   y(i)   = A(i,j) * x(j)     A {Dense,Sparse} (CSR), x, y {Dense}
+ *       SpMM   C(i,k) = A(i,j) * B(j,k)   A CSR, B and C {Dense,Dense} row-major
+ *       SpGEMM C(i,k) = A(i,j) * B(j,k)   A, B, C CSR
+ *     the library exports `assemble`, `compute` and `evaluate` with the signature taco's code
+ *     generator emits (int f(taco_tensor_t* result, taco_tensor_t* operand...), result first,
+ *     operands in TensorBase::getArguments order — src/tensor.cpp:779-806,
+ *     src/codegen/codegen_c.cpp:591-630) and the packed `_shim_` form that
+ *     ir::Module::callFuncPackedRaw resolves with dlsym (src/codegen/module.cpp:178-218).
+ *     Names carry a pattern prefix here; the per-pattern objects libtacogb_<pattern>.so export
+ *     the unprefixed names (assemble, compute, evaluate, _shim_*) exactly as a taco-compiled
+ *     module does.
+ *
+ *     Memory: operand arrays may be host memory (malloc, as taco allocates without CUDA),
+ *     pinned host memory, managed memory (taco's CUDA build, cudaMallocManaged —
+ *     src/cuda.cpp:54-63) or device memory.  Host arrays are staged to the GPU inside the call.
+ *     Result arrays allocated by `assemble`/`evaluate` use malloc when the operands are host
+ *     memory and cudaMallocManaged otherwise, matching the allocator taco frees them with
+ *     (src/storage/array.cpp:22-33).  Calls are synchronous, like taco's generated CUDA
+ *     (cudaDeviceSynchronize after each launch, src/codegen/codegen_cuda.cpp:609).
+ *
+ *  2. A device-pointer layer (tacogb_spmv, tacogb_spmm, tacogb_spgemm_*) on a caller stream,
+ *     which the taco ABI forwards to and which may be captured in CUDA graphs.
+ *
+ * Errors: every function returns 0 on success and a TACOGB_ERR_* code otherwise; the message
+ * is available from tacogb_last_error().  Generated taco CUDA exits the process on a CUDA
+ * error (src/codegen/codegen_cuda.cpp:58-67); this library never does.
+ */
+#ifndef TACO_GB300_H
+#define TACO_GB300_H
+
+#include <stdint.h>
+#include "taco_gb300_tensor.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TACOGB_OK 0
+#define TACOGB_ERR_ARG 1       /* invalid argument, unsupported format or type */
+#define TACOGB_ERR_CUDA 2      /* CUDA runtime error */
+#define TACOGB_ERR_OVERFLOW 3  /* a result does not fit taco's int32 positions */
+#define TACOGB_ERR_TIMEOUT 4   /* a bounded device-side wait gave up */
+#define TACOGB_ERR_ALLOC 5     /* allocation failed */
+
+/* Value types (taco's csize in bits: 64 -> F64, 32 -> F32; 16 -> BF16 is an extension). */
+#define TACOGB_F64 0
+#define TACOGB_F32 1
+#define TACOGB_BF16 2
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* tacogb_last_error(void);
+/* Library version string. */
+const char* tacogb_version(void);
+
+/* Number of kernels this library has launched in this process. */
+long long tacogb_launch_count(void);
+/* Per-kernel device timing: between begin and end every launch is bracketed by CUDA events on
+ * its stream.  end() waits for the events and writes, per distinct kernel name (64-byte slots
+ * in `names`), the summed milliseconds and the launch count; returns the number of kernels. */
+void tacogb_profile_begin(void);
+int tacogb_profile_end(int32_t max_kernels, char* names, double* total_ms, int32_t* launches);
+
+/* ------------------------------------------------------------------ device layer -------- */
+
+/* A CSR matrix in device (or managed) memory: {Dense,Sparse} with int32 pos/crd. */
+typedef struct tacogb_csr {
+  int32_t rows, cols;
+  int64_t nnz;
+  const int32_t* pos;  /* rows+1 */
+  const int32_t* crd;  /* nnz, sorted within each row */
+  const void* vals;    /* nnz values of type vtype */
+  int32_t vtype;       /* TACOGB_F64 or TACOGB_F32 */
+} tacogb_csr;
+
+/* SpMV kernel variants.  TACOGB_VARIANT_AUTO lets the library choose (tuning database, cost
+ * model, then a structural rule). */
+#define TACOGB_VARIANT_AUTO (-1)
+
+/* y = A x.  F64 values: x, y FP64.  F32 values: x, y FP32 with compensated (TwoSum/TwoProduct)
+ * row accumulation.  Replaces the generated compute of y(i)=A(i,j)*x(j)
+ * (src/lower/lowerer_impl_imperative.cpp:1304 + src/index_notation/transformations.cpp:1982). */
+int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, void* stream);
+int tacogb_spmv_variant_count(void);
+const char* tacogb_spmv_variant_name(int32_t variant);
+
+/* ------------------------------------------------------------------ taco kernel ABI ----- */
+
+/* y(i) = A(i,j) * x(j).  Replaces the generated assemble/compute/evaluate of that statement
+ * (taco "y(i) = A(i,j) * x(j)" -f=A:ds; generated text at the lowering cited above). */
+int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x);
+int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x);
+int tacogb_spmv_evaluate(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x);
+int _shim_tacogb_spmv_assemble(void** args);
+int _shim_tacogb_spmv_compute(void** args);
+int _shim_tacogb_spmv_evaluate(void** args);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

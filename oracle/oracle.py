@@ -1,0 +1,146 @@
+"""ORACLE — test infrastructure only (tests/, __graft_entry__.smoke(), bench.py's CPU-baseline
+leg).  The taco_gb300 product never imports this module.
+
+Two CPU checkers, both over plain numpy arrays:
+  * liboracle.so       — the C restatement in oracle/taco_oracle.c (always built);
+  * libtacoref_*.so    — taco's own generated C (oracle/_ref/gen/*.c, emitted by taco's CLI
+                         through oracle/Makefile.ref), compiled with taco's JIT flags; present
+                         wherever oracle/_ref/gen travelled.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+GEN_DIR = os.path.join(REF_DIR, "gen")
+P = ctypes.c_void_p
+I32 = ctypes.c_int32
+I64 = ctypes.c_int64
+
+
+def _run(cmd, cwd=None):
+    r = subprocess.run(cmd, cwd=cwd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed: %s\n%s" % (" ".join(cmd), r.stdout))
+
+
+def build(reference_root="/root/reference"):
+    """Compiles the C restatement; compiles taco's generated C when it is available, first
+    regenerating it from the reference tree when that tree exists."""
+    src = os.path.join(HERE, "taco_oracle.c")
+    out = os.path.join(HERE, "liboracle.so")
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        _run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", out])
+    root = os.path.dirname(HERE)
+    if os.path.isdir(os.path.join(reference_root, "src")):
+        _run(["make", "-s", "-f", "oracle/Makefile.ref", "-j8", "REF=" + reference_root], cwd=root)
+    elif os.path.isdir(GEN_DIR):
+        _run(["make", "-s", "-f", "oracle/Makefile.ref", "lib", "REF=/nonexistent"], cwd=root)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        L.oracle_spmv_f64.argtypes = [I32, P, P, P, P, P]
+        L.oracle_spmm_f64.argtypes = [I32, I32, P, P, P, P, P]
+        L.oracle_spgemm_assemble.restype = I64
+        L.oracle_spgemm_assemble.argtypes = [I32, I32, P, P, P, P, P, ctypes.POINTER(P)]
+        L.oracle_spgemm_compute.argtypes = [I32, I32, P, P, P, P, P, P, P, P, P]
+        L.oracle_free.argtypes = [P]
+        L.oracle_num_threads.restype = I32
+        L.oracle_set_num_threads.argtypes = [I32]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data
+
+
+def spmv(pos, crd, vals, x):
+    y = np.empty(len(pos) - 1, dtype=np.float64)
+    lib().oracle_spmv_f64(len(pos) - 1, _p(pos), _p(crd), _p(vals), _p(x), _p(y))
+    return y
+
+
+def spmm(pos, crd, vals, B):
+    rows, N = len(pos) - 1, B.shape[1]
+    C = np.empty((rows, N), dtype=np.float64)
+    lib().oracle_spmm_f64(rows, N, _p(pos), _p(crd), _p(vals), _p(np.ascontiguousarray(B)), _p(C))
+    return C
+
+
+def spgemm(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, K):
+    """(Cpos, Ccrd, Cvals) of A*B with taco's structure: every structural product kept,
+    columns sorted per row."""
+    rows = len(Apos) - 1
+    Cpos = np.empty(rows + 1, dtype=np.int32)
+    crd_ptr = P()
+    nnz = lib().oracle_spgemm_assemble(rows, K, _p(Apos), _p(Acrd), _p(Bpos), _p(Bcrd), _p(Cpos),
+                                       ctypes.byref(crd_ptr))
+    if nnz < 0:
+        raise OverflowError("nnz(C) exceeds int32")
+    Ccrd = np.ctypeslib.as_array(ctypes.cast(crd_ptr, ctypes.POINTER(ctypes.c_int32)),
+                                 shape=(max(nnz, 1),))[:nnz].copy()
+    lib().oracle_free(crd_ptr)
+    Cvals = np.empty(nnz, dtype=np.float64)
+    if vals_given := (Avals is not None and Bvals is not None):
+        lib().oracle_spgemm_compute(rows, K, _p(Apos), _p(Acrd), _p(Avals), _p(Bpos), _p(Bcrd),
+                                    _p(Bvals), _p(Cpos), _p(Ccrd), _p(Cvals))
+    return Cpos, Ccrd, (Cvals if vals_given else None)
+
+
+def set_threads(n):
+    lib().oracle_set_num_threads(n)
+
+
+def threads():
+    return lib().oracle_num_threads()
+
+
+# ------------------------------------------------------------ taco's generated code --------
+
+def ref_available(pattern):
+    return os.path.exists(os.path.join(REF_DIR, "libtacoref_%s.so" % pattern))
+
+
+_ref = {}
+
+
+def ref_lib(pattern):
+    """taco's generated C for pattern (spmv, spmm, spgemm) as compiled by Makefile.ref; exports
+    taco's own assemble/compute/evaluate(taco_tensor_t*...)."""
+    if pattern not in _ref:
+        path = os.path.join(REF_DIR, "libtacoref_%s.so" % pattern)
+        L = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
+        for fn in ("assemble", "compute", "evaluate"):
+            getattr(L, fn).argtypes = [P, P, P]
+            getattr(L, fn).restype = ctypes.c_int
+        _ref[pattern] = L
+    return _ref[pattern]
+
+
+def ref_set_threads(n):
+    """OpenMP thread count and static schedule for taco's generated code, as
+    Module::callFuncPackedRaw sets them (src/codegen/module.cpp:190-215)."""
+    import ctypes.util
+    for name in ("libgomp.so.1", ctypes.util.find_library("gomp")):
+        if not name:
+            continue
+        try:
+            g = ctypes.CDLL(name)
+            g.omp_set_num_threads(int(n))
+            g.omp_set_schedule(1, 0)  # omp_sched_static, default chunk
+            return
+        except OSError:
+            continue

@@ -1,0 +1,153 @@
+/* ORACLE — test infrastructure only.  Nothing in the taco_gb300 product links or calls this
+ * file; only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it, and only
+ * as the checker (or as the timed CPU port).
+ *
+ * A plain-C restatement of the code taco generates for the three hot-path statements, each
+ * function following the loop nest taco's lowering emits:
+ *
+ *   SpMV   y(i) = A(i,j) * x(j), A {Dense,Sparse}
+ *          generated `compute`: a row loop (src/lower/lowerer_impl_imperative.cpp:1304,
+ *          lowerForallPosition over A2_pos/A2_crd), the reduction scalar `tjy_val` introduced by
+ *          scalarPromote (src/index_notation/transformations.cpp:1982), and the OpenMP pragma
+ *          emitted for the outer loop (src/codegen/codegen_c.cpp:393-446).
+ *   SpMM   C(i,k) = A(i,j) * B(j,k), B and C dense row-major
+ *          generated `compute`: zero C, then for i, for p in row i, for k: C[i*N+k] += A[p]*B[j*N+k]
+ *          (same lowering, dense k loop; flat int32 index i*N+k as the generated code uses).
+ *   SpGEMM C(i,k) = A(i,j) * B(j,k), all CSR
+ *          workspace form forall(i, where(forall(k, C(i,k)=w(k)), forall(j,k, w(k) += A*B))) made by
+ *          insertTemporaries (src/index_notation/transformations.cpp:2083); the dense accelerator
+ *          arrays w_already_set/w_index_list (src/lower/lowerer_impl_imperative.cpp:2197), the
+ *          per-row qsort of the index list, and compressed appends
+ *          (src/lower/mode_format_compressed.cpp:107-213).  `assemble` builds pos/crd; `compute`
+ *          fills vals, initialising w[k] with the first product and adding later products in
+ *          A-row order.
+ *
+ * The SpGEMM functions are also given in a row-parallel two-pass form (per-row counts, scan,
+ * fill), the shape taco's scheduleSpGEMMCPU produces through lowerAssemble
+ * (test/tests-scheduling-eval.cpp:68-94, src/lower/lowerer_impl_imperative.cpp:2616-2781); its
+ * output is identical to the serial form.
+ *
+ * Compiled with -O2 -fopenmp -ffp-contract=off: products and sums are rounded separately, in
+ * the written order.
+ */
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+
+int oracle_num_threads(void) { return omp_get_max_threads(); }
+void oracle_set_num_threads(int n) { omp_set_num_threads(n); }
+
+/* y(i) = A(i,j) * x(j) */
+void oracle_spmv_f64(int32_t rows, const int32_t* pos, const int32_t* crd, const double* vals,
+                     const double* x, double* y) {
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < rows; i++) {
+    double t = 0.0;
+    for (int32_t p = pos[i]; p < pos[i + 1]; p++) t += vals[p] * x[crd[p]];
+    y[i] = t;
+  }
+}
+
+/* C(i,k) = A(i,j) * B(j,k), B: rowsB x N row-major, C: rows x N row-major */
+void oracle_spmm_f64(int32_t rows, int32_t N, const int32_t* pos, const int32_t* crd,
+                     const double* vals, const double* B, double* C) {
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < (int64_t)rows * N; q++) C[q] = 0.0;
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < rows; i++) {
+    double* c = C + (int64_t)i * N;
+    for (int32_t p = pos[i]; p < pos[i + 1]; p++) {
+      const double a = vals[p];
+      const double* b = B + (int64_t)crd[p] * N;
+      for (int32_t k = 0; k < N; k++) c[k] = c[k] + a * b[k];
+    }
+  }
+}
+
+static int cmp_i32(const void* a, const void* b) {
+  int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+  return (x > y) - (x < y);
+}
+
+/* Row i's sorted distinct output columns into list; returns the count.  `set` is all-zero on
+ * entry and on exit. */
+static int32_t spgemm_row_cols(int32_t i, const int32_t* Apos, const int32_t* Acrd,
+                               const int32_t* Bpos, const int32_t* Bcrd, char* set,
+                               int32_t* list) {
+  int32_t cnt = 0;
+  for (int32_t p = Apos[i]; p < Apos[i + 1]; p++) {
+    int32_t j = Acrd[p];
+    for (int32_t q = Bpos[j]; q < Bpos[j + 1]; q++) {
+      int32_t k = Bcrd[q];
+      if (!set[k]) { set[k] = 1; list[cnt++] = k; }
+    }
+  }
+  qsort(list, (size_t)cnt, sizeof(int32_t), cmp_i32);
+  for (int32_t t = 0; t < cnt; t++) set[list[t]] = 0;
+  return cnt;
+}
+
+/* Symbolic phase.  Writes Cpos[0..rows]; returns nnz(C) and a malloc'd crd in *Ccrd_out, or
+ * -1 when nnz(C) exceeds int32. */
+int64_t oracle_spgemm_assemble(int32_t rows, int32_t K, const int32_t* Apos, const int32_t* Acrd,
+                               const int32_t* Bpos, const int32_t* Bcrd, int32_t* Cpos,
+                               int32_t** Ccrd_out) {
+  int32_t* cnt = (int32_t*)malloc(sizeof(int32_t) * ((size_t)rows + 1));
+#pragma omp parallel
+  {
+    char* set = (char*)calloc((size_t)K, 1);
+    int32_t* list = (int32_t*)malloc(sizeof(int32_t) * (size_t)(K > 0 ? K : 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int32_t i = 0; i < rows; i++) cnt[i] = spgemm_row_cols(i, Apos, Acrd, Bpos, Bcrd, set, list);
+    free(set);
+    free(list);
+  }
+  int64_t acc = 0;
+  Cpos[0] = 0;
+  for (int32_t i = 0; i < rows; i++) {
+    acc += cnt[i];
+    if (acc > INT32_MAX) { free(cnt); *Ccrd_out = NULL; return -1; }
+    Cpos[i + 1] = (int32_t)acc;
+  }
+  free(cnt);
+  int32_t* Ccrd = (int32_t*)malloc(sizeof(int32_t) * (size_t)(acc > 0 ? acc : 1));
+#pragma omp parallel
+  {
+    char* set = (char*)calloc((size_t)K, 1);
+#pragma omp for schedule(dynamic, 64)
+    for (int32_t i = 0; i < rows; i++) spgemm_row_cols(i, Apos, Acrd, Bpos, Bcrd, set, Ccrd + Cpos[i]);
+    free(set);
+  }
+  *Ccrd_out = Ccrd;
+  return acc;
+}
+
+/* Numeric phase over the pattern from oracle_spgemm_assemble. */
+void oracle_spgemm_compute(int32_t rows, int32_t K, const int32_t* Apos, const int32_t* Acrd,
+                           const double* Avals, const int32_t* Bpos, const int32_t* Bcrd,
+                           const double* Bvals, const int32_t* Cpos, const int32_t* Ccrd,
+                           double* Cvals) {
+#pragma omp parallel
+  {
+    char* set = (char*)calloc((size_t)K, 1);
+    double* w = (double*)malloc(sizeof(double) * (size_t)(K > 0 ? K : 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int32_t i = 0; i < rows; i++) {
+      for (int32_t p = Apos[i]; p < Apos[i + 1]; p++) {
+        int32_t j = Acrd[p];
+        for (int32_t q = Bpos[j]; q < Bpos[j + 1]; q++) {
+          int32_t k = Bcrd[q];
+          double prod = Avals[p] * Bvals[q];
+          if (!set[k]) { set[k] = 1; w[k] = prod; }
+          else w[k] = w[k] + prod;
+        }
+      }
+      for (int32_t t = Cpos[i]; t < Cpos[i + 1]; t++) { Cvals[t] = w[Ccrd[t]]; set[Ccrd[t]] = 0; }
+    }
+    free(set);
+    free(w);
+  }
+}
+
+void oracle_free(void* p) { free(p); }

@@ -1,0 +1,70 @@
+"""taco_gb300 — taco's sparse hot path (CSR SpMV, SpMM, two-phase SpGEMM) as hand-written
+sm_103a CUDA behind taco's kernel ABI.
+
+Python here is plumbing for tests and benchmarks: the product is libtacogb.so
+(include/taco_gb300.h) and the per-pattern drop-in modules.  Device memory comes from torch.
+"""
+import ctypes
+
+from . import _native
+from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBError, check,
+                      lib)
+
+__all__ = ["CsrMatrix", "spmv", "spmv_variants", "lib", "check", "TacoGBError",
+           "TACOGB_F64", "TACOGB_F32", "TACOGB_BF16", "VARIANT_AUTO"]
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+_VTYPE = {8: TACOGB_F64, 4: TACOGB_F32}
+
+
+class CsrMatrix:
+    """A CSR matrix resident on the GPU (torch int32 pos/crd, float64 or float32 vals)."""
+
+    def __init__(self, pos, crd, vals, cols):
+        import torch
+        assert pos.dtype == torch.int32 and crd.dtype == torch.int32
+        assert pos.is_cuda and crd.is_cuda and vals.is_cuda
+        self.pos, self.crd, self.vals = pos, crd, vals
+        self.rows = pos.numel() - 1
+        self.cols = cols
+        self.nnz = crd.numel()
+        self.vtype = _VTYPE[vals.element_size()]
+
+    @classmethod
+    def from_numpy(cls, pos, crd, vals, cols, device="cuda", dtype=None):
+        import torch
+        v = torch.from_numpy(vals)
+        if dtype is not None:
+            v = v.to(dtype)
+        return cls(torch.from_numpy(pos).to(device), torch.from_numpy(crd).to(device),
+                   v.to(device), cols)
+
+    def as_csr(self):
+        c = _native.Csr()
+        c.rows, c.cols, c.nnz = self.rows, self.cols, self.nnz
+        c.pos, c.crd, c.vals = self.pos.data_ptr(), self.crd.data_ptr(), self.vals.data_ptr()
+        c.vtype = self.vtype
+        return c
+
+
+def spmv(A, x, y=None, variant=VARIANT_AUTO, stream=None):
+    """y = A x on the GPU through tacogb_spmv (FP64, or FP32 with compensated accumulation)."""
+    import torch
+    if y is None:
+        y = torch.empty(A.rows, dtype=x.dtype, device=x.device)
+    c = A.as_csr()
+    check(lib().tacogb_spmv(ctypes.byref(c), x.data_ptr(), y.data_ptr(), variant,
+                            _stream_ptr(stream)), "tacogb_spmv")
+    return y
+
+
+def spmv_variants():
+    L = lib()
+    return [L.tacogb_spmv_variant_name(i).decode() for i in range(L.tacogb_spmv_variant_count())]

@@ -1,0 +1,128 @@
+"""ctypes bindings of libtacogb (include/taco_gb300.h) and libtacogb_gen
+(include/taco_gb300_gen.h).
+
+The shared objects are built in-tree by taco_gb300.build; loading fails loudly when they are
+missing — there is no Python or CPU fallback for any kernel.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBDIR = os.path.join(HERE, "lib")
+
+TACOGB_F64, TACOGB_F32, TACOGB_BF16 = 0, 1, 2
+VARIANT_AUTO = -1
+
+
+class TacoTensor(ctypes.Structure):
+    """taco_tensor_t (include/taco/taco_tensor_t.h:13-23 in taco)."""
+    _fields_ = [
+        ("order", ctypes.c_int32),
+        ("dimensions", ctypes.POINTER(ctypes.c_int32)),
+        ("csize", ctypes.c_int32),
+        ("mode_ordering", ctypes.POINTER(ctypes.c_int32)),
+        ("mode_types", ctypes.POINTER(ctypes.c_int)),
+        ("indices", ctypes.POINTER(ctypes.POINTER(ctypes.c_void_p))),
+        ("vals", ctypes.c_void_p),
+        ("fill_value", ctypes.c_void_p),
+        ("vals_size", ctypes.c_int32),
+    ]
+
+
+class Csr(ctypes.Structure):
+    """tacogb_csr: a CSR matrix in device memory."""
+    _fields_ = [
+        ("rows", ctypes.c_int32),
+        ("cols", ctypes.c_int32),
+        ("nnz", ctypes.c_int64),
+        ("pos", ctypes.c_void_p),
+        ("crd", ctypes.c_void_p),
+        ("vals", ctypes.c_void_p),
+        ("vtype", ctypes.c_int32),
+    ]
+
+
+class GenSpec(ctypes.Structure):
+    """tacogb_gen_spec."""
+    _fields_ = [
+        ("rows", ctypes.c_int32), ("cols", ctypes.c_int32), ("kind", ctypes.c_int32),
+        ("len_lo", ctypes.c_int32), ("len_hi", ctypes.c_int32),
+        ("mean", ctypes.c_double), ("len_max", ctypes.c_int32),
+        ("band", ctypes.c_int32), ("band_len", ctypes.c_int32), ("grid", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+_lib = None
+_gen = None
+
+P = ctypes.c_void_p
+I32 = ctypes.c_int32
+I64 = ctypes.c_int64
+
+# name -> (restype, argtypes); every symbol declared in include/taco_gb300.h
+SIGNATURES = {
+    "tacogb_last_error": (ctypes.c_char_p, []),
+    "tacogb_version": (ctypes.c_char_p, []),
+    "tacogb_launch_count": (ctypes.c_longlong, []),
+    "tacogb_profile_begin": (None, []),
+    "tacogb_profile_end": (I32, [I32, P, P, P]),
+    "tacogb_spmv": (I32, [ctypes.POINTER(Csr), P, P, I32, P]),
+    "tacogb_spmv_variant_count": (I32, []),
+    "tacogb_spmv_variant_name": (ctypes.c_char_p, [I32]),
+    "tacogb_spmv_assemble": (I32, [P, P, P]),
+    "tacogb_spmv_compute": (I32, [P, P, P]),
+    "tacogb_spmv_evaluate": (I32, [P, P, P]),
+    "_shim_tacogb_spmv_assemble": (I32, [P]),
+    "_shim_tacogb_spmv_compute": (I32, [P]),
+    "_shim_tacogb_spmv_evaluate": (I32, [P]),
+}
+
+GEN_SIGNATURES = {
+    "tacogb_gen_pos": (I64, [ctypes.POINTER(GenSpec), P]),
+    "tacogb_gen_fill": (I32, [ctypes.POINTER(GenSpec), P, P, P]),
+    "tacogb_gen_dense": (None, [ctypes.c_uint64, I64, P]),
+    "tacogb_gen_powerlaw_scale": (ctypes.c_double, [ctypes.c_double, I32]),
+    "tacogb_gen_batch_spec": (None, [ctypes.c_uint64, I32, I32, I32, ctypes.POINTER(GenSpec)]),
+}
+
+
+def _bind(lib, sigs):
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def lib():
+    """The loaded libtacogb (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        path = os.path.join(LIBDIR, "libtacogb.so")
+        if not os.path.exists(path):
+            raise RuntimeError("libtacogb.so is not built (run taco_gb300.build.build())")
+        _lib = ctypes.CDLL(path)
+        _bind(_lib, SIGNATURES)
+    return _lib
+
+
+def gen():
+    global _gen
+    if _gen is None:
+        path = os.path.join(LIBDIR, "libtacogb_gen.so")
+        if not os.path.exists(path):
+            raise RuntimeError("libtacogb_gen.so is not built (run taco_gb300.build.build())")
+        _gen = ctypes.CDLL(path)
+        _bind(_gen, GEN_SIGNATURES)
+    return _gen
+
+
+class TacoGBError(RuntimeError):
+    pass
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = lib().tacogb_last_error().decode()
+        raise TacoGBError("%s failed (code %d): %s" % (what, rc, msg))
+    return rc

@@ -1,0 +1,424 @@
+// The C-ABI layer of libtacogb: error state, per-device scratch arena, and taco's kernel ABI
+// (assemble / compute / evaluate over taco_tensor_t, plus the packed _shim_ forms) forwarding to
+// the device-pointer layer.
+//
+// taco_tensor_t handling follows what taco's generated code reads from the struct
+// (src/codegen/codegen.cpp:232-350 unpack text): dimensions[m], indices[m][0]/[1] for a
+// compressed mode, vals; csize is in bits (src/storage/storage.cpp:61-63).
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace tacogb {
+
+// ------------------------------------------------------------------ errors ----------------
+
+namespace {
+thread_local char g_err[512] = "";
+thread_local int g_code = 0;
+}  // namespace
+
+void set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  g_code = code;
+}
+int last_code() { return g_code ? g_code : TACOGB_ERR_CUDA; }
+
+// ------------------------------------------------------------------ profiling -------------
+
+namespace {
+struct ProfRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::vector<ProfRec> g_prof;
+std::vector<cudaEvent_t> g_event_pool;
+size_t g_event_next = 0;
+long long g_launches = 0;
+
+cudaEvent_t pool_event() {
+  if (g_event_next == g_event_pool.size()) {
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    g_event_pool.push_back(e);
+  }
+  return g_event_pool[g_event_next++];
+}
+}  // namespace
+
+void prof_before(const char* name, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_launches++;
+  if (!g_prof_on) return;
+  ProfRec r{name, pool_event(), nullptr};
+  cudaEventRecord(r.a, st);
+  g_prof.push_back(r);
+}
+
+void prof_after(cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  if (!g_prof_on || g_prof.empty()) return;
+  g_prof.back().b = pool_event();
+  cudaEventRecord(g_prof.back().b, st);
+}
+
+// ------------------------------------------------------------------ device state ----------
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+constexpr int kScratchSlots = 4;
+
+struct DeviceState {
+  int sms = 0;
+  void* scratch[kScratchSlots] = {};
+  size_t scratch_cap[kScratchSlots] = {};
+  // staging buffers for host-memory operands of the taco ABI
+  std::vector<void*> stage;
+  std::vector<size_t> stage_cap;
+  cudaStream_t stream = nullptr;
+};
+
+std::mutex g_mu;
+DeviceState g_dev[kMaxDevices];
+
+DeviceState* current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) return nullptr;
+  return &g_dev[d];
+}
+
+}  // namespace
+
+int sm_count() {
+  DeviceState* ds = current_device();
+  if (!ds) return 148;
+  if (ds->sms == 0) {
+    int d = 0, v = 0;
+    cudaGetDevice(&d);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, d);
+    ds->sms = v > 0 ? v : 148;
+  }
+  return ds->sms;
+}
+
+void* scratch(size_t bytes, int slot) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState* ds = current_device();
+  if (!ds || slot < 0 || slot >= kScratchSlots) {
+    set_error(TACOGB_ERR_ARG, "scratch: no device or bad slot");
+    return nullptr;
+  }
+  if (bytes == 0) bytes = 256;
+  if (ds->scratch_cap[slot] < bytes) {
+    size_t cap = bytes + bytes / 4;
+    if (ds->scratch[slot]) cudaFree(ds->scratch[slot]);
+    ds->scratch[slot] = nullptr;
+    ds->scratch_cap[slot] = 0;
+    cudaError_t e = cudaMalloc(&ds->scratch[slot], cap);
+    if (e != cudaSuccess) {
+      set_error(TACOGB_ERR_ALLOC, "scratch: cudaMalloc(%zu) failed: %s", cap, cudaGetErrorString(e));
+      return nullptr;
+    }
+    ds->scratch_cap[slot] = cap;
+  }
+  return ds->scratch[slot];
+}
+
+namespace {
+
+// Device staging buffer `slot` with room for `bytes` (for host-resident taco operands).
+void* stage_buffer(int slot, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState* ds = current_device();
+  if (!ds) return nullptr;
+  if ((int)ds->stage.size() <= slot) {
+    ds->stage.resize(slot + 1, nullptr);
+    ds->stage_cap.resize(slot + 1, 0);
+  }
+  if (bytes == 0) bytes = 16;
+  if (ds->stage_cap[slot] < bytes) {
+    if (ds->stage[slot]) cudaFree(ds->stage[slot]);
+    ds->stage[slot] = nullptr;
+    ds->stage_cap[slot] = 0;
+    if (cudaMalloc(&ds->stage[slot], bytes) != cudaSuccess) {
+      set_error(TACOGB_ERR_ALLOC, "staging: cudaMalloc(%zu) failed", bytes);
+      return nullptr;
+    }
+    ds->stage_cap[slot] = bytes;
+  }
+  return ds->stage[slot];
+}
+
+cudaStream_t lib_stream() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState* ds = current_device();
+  if (!ds) return nullptr;
+  if (!ds->stream) cudaStreamCreateWithFlags(&ds->stream, cudaStreamNonBlocking);
+  return ds->stream;
+}
+
+// True when the GPU can dereference p directly (device or managed memory).
+bool device_accessible(const void* p) {
+  if (!p) return true;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// An operand array as seen by the kernels: either the caller's pointer (device-accessible) or
+// a staging copy.
+struct Operand {
+  const void* host = nullptr;
+  void* dev = nullptr;
+  size_t bytes = 0;
+  bool staged = false;
+};
+
+int stage_in(Operand& o, const void* p, size_t bytes, int slot, cudaStream_t st) {
+  o.host = p;
+  o.bytes = bytes;
+  if (device_accessible(p)) {
+    o.dev = const_cast<void*>(p);
+    return 0;
+  }
+  o.dev = stage_buffer(slot, bytes);
+  if (!o.dev) return TACOGB_ERR_ALLOC;
+  o.staged = true;
+  if (bytes) TACOGB_CUDA_TRY(cudaMemcpyAsync(o.dev, p, bytes, cudaMemcpyHostToDevice, st));
+  return 0;
+}
+
+int value_type_of_csize(int32_t csize) {
+  switch (csize) {
+    case 64: return TACOGB_F64;
+    case 32: return TACOGB_F32;
+    case 16: return TACOGB_BF16;
+  }
+  return -1;
+}
+
+size_t value_bytes(int vt) { return vt == TACOGB_F64 ? 8 : vt == TACOGB_F32 ? 4 : 2; }
+
+// Reads an int32 that may live in host, managed or device memory.
+int read_i32(const int32_t* p, int32_t* out) {
+  if (!device_accessible(p)) {
+    *out = *p;
+    return 0;
+  }
+  cudaPointerAttributes at;
+  cudaPointerGetAttributes(&at, p);
+  if (at.type == cudaMemoryTypeManaged) {
+    TACOGB_CUDA_TRY(cudaDeviceSynchronize());
+    *out = *p;
+    return 0;
+  }
+  TACOGB_CUDA_TRY(cudaMemcpy(out, p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// Allocation for a result array, with the allocator taco releases it with
+// (src/storage/array.cpp:22-33): cudaMallocManaged when the operands are GPU memory (taco's
+// CUDA build), malloc otherwise.
+void* alloc_result(size_t bytes, bool managed) {
+  if (bytes == 0) bytes = 1;
+  if (managed) {
+    void* p = nullptr;
+    if (cudaMallocManaged(&p, bytes) != cudaSuccess) {
+      set_error(TACOGB_ERR_ALLOC, "cudaMallocManaged(%zu) failed", bytes);
+      return nullptr;
+    }
+    return p;
+  }
+  void* p = malloc(bytes);
+  if (!p) set_error(TACOGB_ERR_ALLOC, "malloc(%zu) failed", bytes);
+  return p;
+}
+
+// ------------------------------------------------------------ struct validation -----------
+
+int check_dense_vector(const taco_tensor_t* t, const char* name) {
+  TACOGB_CHECK_ARG(t != nullptr, "%s: null tensor", name);
+  TACOGB_CHECK_ARG(t->order == 1, "%s: expected order 1, got %d", name, t->order);
+  TACOGB_CHECK_ARG(t->mode_types == nullptr || t->mode_types[0] == taco_mode_dense,
+                   "%s: expected a {Dense} vector", name);
+  TACOGB_CHECK_ARG(t->dimensions != nullptr, "%s: null dimensions", name);
+  return 0;
+}
+
+int check_dense_matrix(const taco_tensor_t* t, const char* name) {
+  TACOGB_CHECK_ARG(t != nullptr, "%s: null tensor", name);
+  TACOGB_CHECK_ARG(t->order == 2, "%s: expected order 2, got %d", name, t->order);
+  TACOGB_CHECK_ARG(t->mode_types == nullptr ||
+                       (t->mode_types[0] == taco_mode_dense && t->mode_types[1] == taco_mode_dense),
+                   "%s: expected {Dense,Dense}", name);
+  TACOGB_CHECK_ARG(t->mode_ordering == nullptr ||
+                       (t->mode_ordering[0] == 0 && t->mode_ordering[1] == 1),
+                   "%s: expected row-major mode ordering {0,1}", name);
+  TACOGB_CHECK_ARG(t->dimensions != nullptr, "%s: null dimensions", name);
+  return 0;
+}
+
+int check_csr(const taco_tensor_t* t, const char* name) {
+  TACOGB_CHECK_ARG(t != nullptr, "%s: null tensor", name);
+  TACOGB_CHECK_ARG(t->order == 2, "%s: expected order 2, got %d", name, t->order);
+  TACOGB_CHECK_ARG(t->mode_types != nullptr && t->mode_types[0] == taco_mode_dense &&
+                       t->mode_types[1] == taco_mode_sparse,
+                   "%s: expected CSR {Dense,Sparse}", name);
+  TACOGB_CHECK_ARG(t->mode_ordering == nullptr ||
+                       (t->mode_ordering[0] == 0 && t->mode_ordering[1] == 1),
+                   "%s: expected mode ordering {0,1} (CSR, not CSC)", name);
+  TACOGB_CHECK_ARG(t->dimensions != nullptr && t->indices != nullptr && t->indices[1] != nullptr,
+                   "%s: missing dimensions or indices", name);
+  return 0;
+}
+
+}  // namespace
+}  // namespace tacogb
+
+using namespace tacogb;
+
+// =================================================================== exported ==============
+
+extern "C" {
+
+const char* tacogb_last_error(void) { return g_err; }
+
+long long tacogb_launch_count(void) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  return g_launches;
+}
+
+void tacogb_profile_begin(void) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.clear();
+  g_event_next = 0;
+  g_prof_on = true;
+}
+
+int tacogb_profile_end(int32_t max_kernels, char* names, double* total_ms, int32_t* launches) {
+  std::vector<ProfRec> recs;
+  {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof_on = false;
+    recs.swap(g_prof);
+  }
+  int n = 0;
+  for (const ProfRec& r : recs) {
+    if (!r.b) continue;
+    if (cudaEventSynchronize(r.b) != cudaSuccess) {
+      set_error(TACOGB_ERR_CUDA, "profile: event synchronize failed");
+      return -TACOGB_ERR_CUDA;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    int k = 0;
+    while (k < n && strncmp(names + 64 * k, r.name, 63) != 0) k++;
+    if (k == n) {
+      if (n == max_kernels) continue;
+      strncpy(names + 64 * n, r.name, 63);
+      names[64 * n + 63] = 0;
+      total_ms[n] = 0.0;
+      launches[n] = 0;
+      n++;
+    }
+    total_ms[k] += ms;
+    launches[k] += 1;
+  }
+  return n;
+}
+const char* tacogb_version(void) { return "taco_gb300 0.1 (sm_103a)"; }
+
+int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, void* stream) {
+  return spmv_run(A, x, y, variant, (cudaStream_t)stream);
+}
+int tacogb_spmv_variant_count(void) { return spmv_variant_count(); }
+const char* tacogb_spmv_variant_name(int32_t v) { return spmv_variant_name(v); }
+
+// ---------------------------------------------------------------- SpMV taco ABI -----------
+
+int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
+  if (int rc = check_dense_vector(y, "spmv result y")) return rc;
+  if (int rc = check_csr(A, "spmv operand A")) return rc;
+  const int vt = value_type_of_csize(y->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spmv: unsupported csize %d", y->csize);
+  const bool managed = device_accessible(A->vals) && A->vals != nullptr;
+  void* p = alloc_result((size_t)y->dimensions[0] * value_bytes(vt), managed);
+  if (!p) return TACOGB_ERR_ALLOC;
+  y->vals = (uint8_t*)p;
+  return 0;
+}
+
+int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
+  if (int rc = check_dense_vector(y, "spmv result y")) return rc;
+  if (int rc = check_csr(A, "spmv operand A")) return rc;
+  if (int rc = check_dense_vector(x, "spmv operand x")) return rc;
+  const int vt = value_type_of_csize(A->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spmv: unsupported csize %d", A->csize);
+  TACOGB_CHECK_ARG(x->csize == A->csize && y->csize == A->csize,
+                   "spmv: operand component sizes differ (%d, %d, %d)", y->csize, A->csize,
+                   x->csize);
+  const int32_t rows = A->dimensions[0], cols = A->dimensions[1];
+  TACOGB_CHECK_ARG(y->dimensions[0] == rows, "spmv: y has %d rows, A has %d", y->dimensions[0], rows);
+  TACOGB_CHECK_ARG(x->dimensions[0] == cols, "spmv: x has %d rows, A has %d columns",
+                   x->dimensions[0], cols);
+  TACOGB_CHECK_ARG(y->vals != nullptr, "spmv: result values not assembled");
+  const int32_t* pos = (const int32_t*)A->indices[1][0];
+  const int32_t* crd = (const int32_t*)A->indices[1][1];
+  TACOGB_CHECK_ARG(pos != nullptr, "spmv: null pos");
+  int32_t nnz = 0;
+  if (int rc = read_i32(pos + rows, &nnz)) return rc;
+  TACOGB_CHECK_ARG(nnz >= 0, "spmv: negative nnz");
+  const size_t vb = value_bytes(vt);
+
+  cudaStream_t st = lib_stream();
+  Operand opos, ocrd, ovals, ox;
+  if (int rc = stage_in(opos, pos, ((size_t)rows + 1) * 4, 0, st)) return rc;
+  if (int rc = stage_in(ocrd, crd, (size_t)nnz * 4, 1, st)) return rc;
+  if (int rc = stage_in(ovals, A->vals, (size_t)nnz * vb, 2, st)) return rc;
+  if (int rc = stage_in(ox, x->vals, (size_t)cols * vb, 3, st)) return rc;
+  void* ydev = y->vals;
+  const bool y_staged = !device_accessible(y->vals);
+  if (y_staged) {
+    ydev = stage_buffer(4, (size_t)rows * vb);
+    if (!ydev) return TACOGB_ERR_ALLOC;
+  }
+  tacogb_csr csr{rows, cols, nnz, (const int32_t*)opos.dev, (const int32_t*)ocrd.dev, ovals.dev, vt};
+  if (int rc = spmv_run(&csr, ox.dev, ydev, TACOGB_VARIANT_AUTO, st)) return rc;
+  if (y_staged && rows)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(y->vals, ydev, (size_t)rows * vb, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int tacogb_spmv_evaluate(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
+  if (int rc = tacogb_spmv_assemble(y, A, x)) return rc;
+  return tacogb_spmv_compute(y, A, x);
+}
+
+int _shim_tacogb_spmv_assemble(void** a) {
+  return tacogb_spmv_assemble((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+int _shim_tacogb_spmv_compute(void** a) {
+  return tacogb_spmv_compute((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+int _shim_tacogb_spmv_evaluate(void** a) {
+  return tacogb_spmv_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+
+}  // extern "C"

@@ -1,0 +1,66 @@
+"""Generates the golden fixtures in tests/golden/ by running taco's own generated C code.
+
+The generated code comes from taco's CLI built from the reference sources by
+oracle/Makefile.ref (taco "y(i) = A(i,j) * x(j)" -f=A:ds -write-source=..., etc.) and is
+compiled with taco's JIT flags.  Run from the repository root where the reference tree exists:
+
+    python tests/golden/make_golden.py
+
+Each fixture stores its inputs and taco's outputs, so the tests that read it need neither the
+reference nor the generator.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from taco_gb300 import build as B  # noqa: E402
+from taco_gb300 import workloads as W  # noqa: E402
+from tests import helpers as H  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def save(name, **arrays):
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrays)
+    print("wrote", name, {k: v.shape for k, v in arrays.items()})
+
+
+def spmv_cases():
+    (pos, crd, vals, _), _ = H.taco_rand_csr(1021 // 10, 1039 // 10, 0.3)
+    x = W.dense(11, 1039 // 10)
+    save("spmv_taco_rand", pos=pos, crd=crd, vals=vals, x=x, y=H.ref_spmv(pos, crd, vals, x))
+
+    s = W.spec(1024, kind=W.UNIFORM, len_lo=4, len_hi=28, seed=W.SEED_BASE + 101)
+    pos, crd, vals = W.generate(s)
+    x = W.dense(12, s.cols)
+    save("spmv_uniform", pos=pos, crd=crd, vals=vals, x=x, y=H.ref_spmv(pos, crd, vals, x))
+
+    s = W.spec(1024, kind=W.POWERLAW, mean=24.0, len_max=1024, seed=W.SEED_BASE + 102)
+    pos, crd, vals = W.generate(s)
+    x = W.dense(13, s.cols)
+    save("spmv_powerlaw", pos=pos, crd=crd, vals=vals, x=x, y=H.ref_spmv(pos, crd, vals, x))
+
+    # mostly empty rows, one dense row, rows of length 1
+    rng = np.random.default_rng(14)
+    rows, cols = 3000, 700
+    lens = np.zeros(rows, np.int32)
+    lens[rng.choice(rows, 200, replace=False)] = 1
+    lens[1234] = cols
+    lens[rows - 1] = 3
+    pos = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    crd = np.concatenate([np.sort(rng.choice(cols, l, replace=False)) for l in lens if l > 0]).astype(np.int32)
+    vals = rng.uniform(-1, 1, len(crd))
+    x = W.dense(15, cols)
+    save("spmv_empty_rows", pos=pos, crd=crd, vals=vals, x=x, y=H.ref_spmv(pos, crd, vals, x))
+
+
+if __name__ == "__main__":
+    B.build()
+    O.build()
+    assert O.ref_available("spmv"), "taco's generated code is not built (oracle/Makefile.ref)"
+    spmv_cases()

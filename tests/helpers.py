@@ -1,0 +1,69 @@
+"""Shared test helpers: taco's own randomized test inputs, error norms, and the taco-generated
+reference kernels driven through taco_tensor_t."""
+import ctypes
+import ctypes.util
+
+import numpy as np
+
+from oracle import oracle as O
+from taco_gb300 import taco as T
+
+_libc = ctypes.CDLL(ctypes.util.find_library("c"))
+_libc.rand.restype = ctypes.c_int
+RAND_MAX = 2147483647  # glibc
+
+
+def taco_rand_csr(rows, cols, sparsity, seed=75883, dense_b_cols=None, b_sparse=False):
+    """The inputs of taco's randomized scheduling tests (test/tests-scheduling-eval.cpp:549-662,
+    843-889): srand(seed); A(i,j) inserted when rand_float < SPARSITY with value
+    (double)(int)(rand_float*3/SPARSITY); then B filled by the same draw, densely or sparsely.
+    rand_float is (float)rand()/(float)RAND_MAX, evaluated in single precision."""
+    _libc.srand(seed)
+    sp = np.float32(sparsity)
+
+    def draw():
+        return np.float32(_libc.rand()) / np.float32(RAND_MAX)
+
+    def fill(nr, nc, sparse):
+        pos = [0]
+        crd, vals = [], []
+        dense = np.zeros((nr, nc))
+        for i in range(nr):
+            for j in range(nc):
+                r = draw()
+                if (not sparse) or r < sp:
+                    v = float(int(np.float32(np.float32(r * np.float32(3)) / sp)))
+                    crd.append(j)
+                    vals.append(v)
+                    dense[i, j] = v
+            pos.append(len(crd))
+        return (np.array(pos, np.int32), np.array(crd, np.int32), np.array(vals, np.float64),
+                dense)
+
+    A = fill(rows, cols, True)
+    B = None
+    if dense_b_cols is not None:
+        B = fill(cols, dense_b_cols, b_sparse)
+    return A, B
+
+
+def normwise(approx, exact):
+    """||approx - exact||_2 / ||exact||_2 (0 when both are zero)."""
+    a = np.asarray(approx, dtype=np.float64).ravel()
+    e = np.asarray(exact, dtype=np.float64).ravel()
+    den = np.linalg.norm(e)
+    num = np.linalg.norm(a - e)
+    return num / den if den > 0 else num
+
+
+def ref_spmv(pos, crd, vals, x, threads=1):
+    """taco's generated SpMV (assemble + compute) on host arrays."""
+    L = O.ref_lib("spmv")
+    O.ref_set_threads(threads)
+    rows, cols = len(pos) - 1, len(x)
+    A = T.csr(pos, crd, vals, [rows, cols])
+    X = T.dense(x, [cols])
+    y = np.empty(rows, dtype=np.float64)
+    Y = T.dense(y, [rows])
+    assert L.compute(Y.ptr, A.ptr, X.ptr) == 0
+    return y

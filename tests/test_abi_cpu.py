@@ -1,0 +1,94 @@
+"""The C-ABI libraries load without a GPU and export every symbol their headers declare; the
+generators are deterministic and produce valid CSR."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import taco_gb300 as tg
+from taco_gb300 import _native as N
+from taco_gb300 import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header):
+    """Function names declared in include/<header> (C declarations ending in ');')."""
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w\s\*]*?\b(\w+)\s*\([^;{]*\)\s*;", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_libtacogb_exports_header():
+    names = declared("taco_gb300.h")
+    assert "tacogb_spmv" in names and "_shim_tacogb_spmv_compute" in names
+    L = ctypes.CDLL(os.path.join(N.LIBDIR, "libtacogb.so"))
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert set(names) <= set(N.SIGNATURES), "bindings miss %s" % (set(names) - set(N.SIGNATURES))
+
+
+def test_libtacogb_gen_exports_header():
+    names = declared("taco_gb300_gen.h")
+    L = ctypes.CDLL(os.path.join(N.LIBDIR, "libtacogb_gen.so"))
+    assert all(hasattr(L, n) for n in names)
+
+
+@pytest.mark.parametrize("pattern", ["spmv"])
+def test_dropin_modules_export_taco_names(pattern):
+    L = ctypes.CDLL(os.path.join(N.LIBDIR, "libtacogb_%s.so" % pattern))
+    for n in ("assemble", "compute", "evaluate", "_shim_assemble", "_shim_compute",
+              "_shim_evaluate"):
+        assert hasattr(L, n)
+
+
+def test_version_and_error_without_gpu():
+    assert tg.lib().tacogb_version().startswith(b"taco_gb300")
+    assert tg.lib().tacogb_spmv_variant_count() >= 2
+
+
+def test_generator_deterministic_and_valid():
+    s = W.spmv_powerlaw(rows=50000)
+    p1, c1, v1 = W.generate(s)
+    p2, c2, v2 = W.generate(s)
+    assert np.array_equal(p1, p2) and np.array_equal(c1, c2) and np.array_equal(v1, v2)
+    assert p1[0] == 0 and np.all(np.diff(p1) >= 1)
+    for i in range(0, 50000, 997):
+        row = c1[p1[i]:p1[i + 1]]
+        assert np.all(np.diff(row) > 0) and row.min() >= 0 and row.max() < s.cols
+    assert np.all(np.abs(v1) < 1.0)
+
+
+def test_generator_fingerprint():
+    """Bytes of a small power-law matrix are fixed: the golden fixtures and the benchmark
+    depend on the generator staying bit-identical across machines."""
+    s = W.spec(777, kind=W.POWERLAW, mean=24.0, len_max=777, seed=12345)
+    pos, crd, vals = W.generate(s)
+    h = (int(pos.astype(np.int64).sum()), int((crd.astype(np.int64) * np.arange(len(crd))).sum() % 1000003),
+         float(np.round(vals.sum(), 9)))
+    expect_path = os.path.join(ROOT, "tests", "golden", "gen_fingerprint.txt")
+    got = "%d %d %.9f" % h
+    assert open(expect_path).read().strip() == got
+
+
+def test_powerlaw_calibration():
+    for mean, kmax in ((24.0, 20000), (32.0, 10000)):
+        c = W.powerlaw_scale(mean, kmax)
+        assert 3.0 < c < 7.0
+    s = W.spmv_powerlaw(rows=400000)
+    pos, _, _ = W.generate(s, values=False)
+    assert abs(pos[-1] / 400000 - 24.0) < 1.0
+
+
+def test_banded_and_poisson_structure():
+    pos, crd, _ = W.generate(W.spmv_banded(rows=1000))
+    for i in (0, 10, 500, 999):
+        row = crd[pos[i]:pos[i + 1]]
+        assert len(row) == min(32, min(1000, i + 32) - max(0, i - 32))
+        assert row.min() >= i - 32 and row.max() < i + 32
+    pos, crd, vals = W.generate(W.spgemm_poisson(grid=512))
+    assert pos[-1] == 1308672
+    assert set(np.unique(vals)) == {-1.0, 4.0}

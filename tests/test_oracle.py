@@ -1,0 +1,80 @@
+"""The oracle is pinned before it is trusted: against taco's own known-answer tests, against
+taco's generated code run here on the same inputs, and against the committed golden fixtures
+(made by tests/golden/make_golden.py from taco's generated code)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from taco_gb300 import workloads as W
+from tests.helpers import normwise, ref_spmv, taco_rand_csr
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _csr_from_dense(D):
+    pos, crd, vals = [0], [], []
+    for row in D:
+        nz = np.nonzero(row)[0]
+        crd += list(nz)
+        vals += list(row[nz])
+        pos.append(len(crd))
+    return np.array(pos, np.int32), np.array(crd, np.int32), np.array(vals, np.float64)
+
+
+# d33a, d3b, d33b of test/test_tensors.cpp:89-94, 205-227
+D33A = np.array([[0, 2, 0], [0, 0, 0], [3, 0, 4]], dtype=np.float64)
+D33B = np.array([[10, 20, 0], [0, 0, 0], [0, 30, 0]], dtype=np.float64)
+D3B = np.array([2, 0, 3], dtype=np.float64)
+
+
+def test_spmv_kat():
+    """expr_storage spmv: d33a(i,k) * d3b(k) = {0,0,18} (test/tests-expr_storage.cpp:873-937)."""
+    pos, crd, vals = _csr_from_dense(D33A)
+    assert list(O.spmv(pos, crd, vals, D3B)) == [0, 0, 18]
+
+
+def test_matmul_kat():
+    """matrix_mul: d33a * d33b = {0,0,0, 0,0,0, 30,180,0} (test/tests-expr_storage.cpp:996-1035),
+    as SpMM (dense B) and as SpGEMM (CSR B)."""
+    pos, crd, vals = _csr_from_dense(D33A)
+    C = O.spmm(pos, crd, vals, D33B)
+    assert list(C.ravel()) == [0, 0, 0, 0, 0, 0, 30, 180, 0]
+    bp, bc, bv = _csr_from_dense(D33B)
+    Cp, Cc, Cv = O.spgemm(pos, crd, vals, bp, bc, bv, 3)
+    # row 0 meets only the empty row 1 of B; row 2 = 3*B(0,:) + 4*B(2,:) -> cols {0,1}
+    assert list(Cp) == [0, 0, 0, 2] and list(Cc) == [0, 1] and list(Cv) == [30, 180]
+
+
+@pytest.mark.skipif(not O.ref_available("spmv"), reason="taco generated code not built here")
+@pytest.mark.parametrize("sparsity", [0.01, 0.1, 0.3])
+def test_spmv_oracle_vs_taco_generated(sparsity):
+    (pos, crd, vals, _), _ = taco_rand_csr(1021 // 10, 1039 // 10, sparsity)
+    x = W.dense(5, 1039 // 10)
+    y_ref = ref_spmv(pos, crd, vals, x, threads=1)
+    y = O.spmv(pos, crd, vals, x)
+    # same left-to-right loop; -ffast-math may reassociate taco's reduction
+    assert normwise(y, y_ref) <= 1e-15
+
+
+@pytest.mark.skipif(not O.ref_available("spmv"), reason="taco generated code not built here")
+def test_spmv_oracle_vs_taco_generated_powerlaw():
+    s = W.spmv_powerlaw(rows=20000)
+    pos, crd, vals = W.generate(s)
+    x = W.dense(7, s.cols)
+    assert normwise(O.spmv(pos, crd, vals, x), ref_spmv(pos, crd, vals, x, threads=4)) <= 1e-14
+
+
+def _golden(name):
+    path = os.path.join(GOLDEN, name)
+    if not os.path.exists(path):
+        pytest.fail("missing golden fixture %s" % name)
+    return np.load(path)
+
+
+@pytest.mark.parametrize("case", ["spmv_taco_rand", "spmv_uniform", "spmv_powerlaw", "spmv_empty_rows"])
+def test_oracle_matches_golden_spmv(case):
+    g = _golden(case + ".npz")
+    y = O.spmv(g["pos"], g["crd"], g["vals"], g["x"])
+    assert normwise(y, g["y"]) <= 1e-14

@@ -1,0 +1,210 @@
+"""SpMV parity on the GPU: every kernel variant against the oracle (taco's loop restated in C)
+and against golden fixtures produced by taco's generated code.
+
+Bars: FP64 values within 1e-12 normwise relative error (summation order only); the FP32
+compensated path within 1e-6 of the FP64 oracle on the FP64 inputs, and within 1e-7 of the FP64
+oracle evaluated on the FP32-rounded inputs (what compensation buys over plain FP32 sums).
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import taco_gb300 as tg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from taco_gb300 import taco as T  # noqa: E402
+from taco_gb300 import workloads as W  # noqa: E402
+from tests.helpers import normwise  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+F64_TOL = 1e-12
+F32_TOL = 1e-6
+F32_COMP_TOL = 1e-7
+
+
+def variants():
+    return list(range(tg.lib().tacogb_spmv_variant_count()))
+
+
+def run_dev(pos, crd, vals, x, variant, dtype=torch.float64):
+    A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x), dtype=dtype)
+    xd = torch.from_numpy(x).to("cuda", dtype)
+    y = tg.spmv(A, xd, variant=variant)
+    torch.cuda.synchronize()
+    return y.double().cpu().numpy()
+
+
+@pytest.mark.parametrize("case", ["spmv_taco_rand", "spmv_uniform", "spmv_powerlaw",
+                                  "spmv_empty_rows"])
+@pytest.mark.parametrize("variant", variants())
+def test_golden_f64(case, variant):
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    y = run_dev(g["pos"], g["crd"], g["vals"], g["x"], variant)
+    assert normwise(y, g["y"]) <= F64_TOL
+
+
+@pytest.mark.parametrize("case", ["spmv_uniform", "spmv_powerlaw", "spmv_empty_rows"])
+@pytest.mark.parametrize("variant", variants())
+def test_golden_f32_compensated(case, variant):
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    y = run_dev(g["pos"], g["crd"], g["vals"], g["x"], variant, torch.float32)
+    assert normwise(y, g["y"]) <= F32_TOL
+    v32 = g["vals"].astype(np.float32).astype(np.float64)
+    x32 = g["x"].astype(np.float32).astype(np.float64)
+    assert normwise(y, O.spmv(g["pos"], g["crd"], v32, x32)) <= F32_COMP_TOL
+
+
+def _edge_matrices():
+    rng = np.random.default_rng(3)
+    out = {}
+    out["empty_matrix"] = (np.zeros(1, np.int32), np.zeros(0, np.int32), np.zeros(0), 5)
+    out["no_nonzeros"] = (np.zeros(1001, np.int32), np.zeros(0, np.int32), np.zeros(0), 17)
+    out["one_row"] = (np.array([0, 3], np.int32), np.array([0, 4, 9], np.int32),
+                      np.array([1.0, -2.0, 0.5]), 10)
+    # one row spanning many merge tiles, surrounded by short rows
+    cols = 50000
+    lens = np.ones(4000, np.int32)
+    lens[1999] = cols
+    pos = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    crd = np.concatenate([np.arange(cols) if l == cols else rng.choice(cols, 1) for l in lens])
+    out["long_row"] = (pos, crd.astype(np.int32), rng.uniform(-1, 1, len(crd)), cols)
+    # every row length 1
+    n = 70001
+    out["unit_rows"] = (np.arange(n + 1, dtype=np.int32), rng.integers(0, n, n).astype(np.int32),
+                        rng.uniform(-1, 1, n), n)
+    # two very long rows back to back, then empties
+    lens = np.zeros(300, np.int32)
+    lens[0], lens[1] = 30000, 29999
+    pos = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    crd = np.concatenate([np.arange(30000), np.arange(29999)]).astype(np.int32)
+    out["two_long_rows"] = (pos, crd, rng.uniform(-1, 1, len(crd)), 30000)
+    return out
+
+
+EDGE = _edge_matrices()
+
+
+@pytest.mark.parametrize("name", sorted(EDGE))
+@pytest.mark.parametrize("variant", variants())
+def test_edge_cases(name, variant):
+    pos, crd, vals, cols = EDGE[name]
+    x = W.dense(21, cols)
+    y_ref = O.spmv(pos, crd, vals, x)
+    y = run_dev(pos, crd, vals, x, variant)
+    assert y.shape == y_ref.shape
+    assert normwise(y, y_ref) <= F64_TOL
+    y32 = run_dev(pos, crd, vals, x, variant, torch.float32)
+    assert normwise(y32, y_ref) <= F32_TOL
+
+
+@pytest.mark.parametrize("variant", variants())
+def test_powerlaw_medium(variant):
+    s = W.spmv_powerlaw(rows=200000)
+    pos, crd, vals = W.generate(s)
+    x = W.dense(22, s.cols)
+    assert normwise(run_dev(pos, crd, vals, x, variant), O.spmv(pos, crd, vals, x)) <= F64_TOL
+
+
+@pytest.fixture(scope="module")
+def full_powerlaw():
+    s = W.spmv_powerlaw()
+    pos, crd, vals = W.generate(s)
+    x = W.dense(23, s.cols)
+    return pos, crd, vals, x
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_full_size_powerlaw(full_powerlaw, dtype):
+    """4,194,304^2 power-law (~1.0e8 nnz): the merge path against the oracle at full size,
+    deterministic across runs, and linear in x."""
+    pos, crd, vals, x = full_powerlaw
+    y_ref = O.spmv(pos, crd, vals, x)
+    A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x), dtype=dtype)
+    xd = torch.from_numpy(x).to("cuda", dtype)
+    y1 = tg.spmv(A, xd, variant=1)
+    y2 = tg.spmv(A, xd, variant=1)
+    torch.cuda.synchronize()
+    assert torch.equal(y1, y2)
+    tol = F64_TOL if dtype == torch.float64 else F32_TOL
+    assert normwise(y1.double().cpu().numpy(), y_ref) <= tol
+    z = torch.from_numpy(W.dense(24, len(x))).to("cuda", dtype)
+    lhs = tg.spmv(A, 2 * xd - z, variant=1)
+    rhs = 2 * y1 - tg.spmv(A, z, variant=1)
+    assert normwise(lhs.double().cpu().numpy(), rhs.double().cpu().numpy()) <= 10 * tol
+
+
+def test_full_size_banded():
+    s = W.spmv_banded()
+    pos, crd, vals = W.generate(s)
+    x = W.dense(25, s.cols)
+    y_ref = O.spmv(pos, crd, vals, x)
+    for variant in (1, 6):
+        assert normwise(run_dev(pos, crd, vals, x, variant), y_ref) <= F64_TOL
+
+
+# ------------------------------------------------------------------ taco ABI ---------------
+
+D33A = (np.array([0, 1, 1, 3], np.int32), np.array([1, 0, 2], np.int32), np.array([2.0, 3.0, 4.0]))
+D3B = np.array([2.0, 0.0, 3.0])
+
+
+def _abi(fn_name, y, A, x, lib=None):
+    L = lib or tg.lib()
+    return getattr(L, fn_name)(y.ptr, A.ptr, x.ptr)
+
+
+def test_abi_kat_host_memory():
+    """expr_storage spmv KAT through tacogb_spmv_evaluate with malloc'd (host) operands."""
+    A = T.csr(*D33A, [3, 3])
+    X = T.dense(D3B, [3])
+    Y = T.dense_result([3])
+    assert _abi("tacogb_spmv_evaluate", Y, A, X) == 0
+    y = np.ctypeslib.as_array(ctypes.cast(Y.vals_ptr, ctypes.POINTER(ctypes.c_double)), (3,))
+    assert list(y) == [0.0, 0.0, 18.0]
+
+
+def test_abi_host_and_device_memory():
+    g = np.load(os.path.join(GOLDEN, "spmv_powerlaw.npz"))
+    rows, cols = len(g["pos"]) - 1, len(g["x"])
+    # host arrays: staged inside compute
+    y = np.zeros(rows)
+    Y, A, X = T.dense(y, [rows]), T.csr(g["pos"], g["crd"], g["vals"], [rows, cols]), T.dense(g["x"], [cols])
+    assert _abi("tacogb_spmv_compute", Y, A, X) == 0
+    assert normwise(y, g["y"]) <= F64_TOL
+    # device arrays: used in place
+    dev = {k: torch.from_numpy(g[k]).cuda() for k in ("pos", "crd", "vals", "x")}
+    yd = torch.zeros(rows, dtype=torch.float64, device="cuda")
+    Yd, Ad, Xd = (T.dense(yd, [rows]), T.csr(dev["pos"], dev["crd"], dev["vals"], [rows, cols]),
+                  T.dense(dev["x"], [cols]))
+    assert _abi("tacogb_spmv_compute", Yd, Ad, Xd) == 0
+    assert normwise(yd.cpu().numpy(), g["y"]) <= F64_TOL
+
+
+def test_dropin_module_symbols():
+    """libtacogb_spmv.so exports taco's unprefixed names; compute through _shim_compute."""
+    L = ctypes.CDLL(os.path.join(os.path.dirname(tg.__file__), "lib", "libtacogb_spmv.so"))
+    A = T.csr(*D33A, [3, 3])
+    X = T.dense(D3B, [3])
+    y = np.zeros(3)
+    Y = T.dense(y, [3])
+    args = (ctypes.c_void_p * 3)(Y.ptr, A.ptr, X.ptr)
+    L._shim_compute.argtypes = [ctypes.c_void_p]
+    assert L._shim_compute(args) == 0
+    assert list(y) == [0.0, 0.0, 18.0]
+
+
+def test_abi_rejects_csc_and_mismatch():
+    pos, crd, vals = D33A
+    A = T.TacoTensor([3, 3], [T.MODE_DENSE, T.MODE_SPARSE], vals=vals,
+                     index_arrays={1: (pos, crd)}, mode_ordering=[1, 0])
+    Y, X = T.dense(np.zeros(3), [3]), T.dense(D3B, [3])
+    rc = _abi("tacogb_spmv_compute", Y, A, X)
+    assert rc == 1  # TACOGB_ERR_ARG
+    assert b"CSC" in tg.lib().tacogb_last_error()
+    Y4, A3 = T.dense(np.zeros(4), [4]), T.csr(*D33A, [3, 3])
+    rc = _abi("tacogb_spmv_compute", Y4, A3, X)
+    assert rc != 0 and b"rows" in tg.lib().tacogb_last_error()
