@@ -4,275 +4,382 @@
 // A2_pos/A2_crd with a promoted scalar accumulator (src/lower/lowerer_impl_imperative.cpp:1304,
 // src/index_notation/transformations.cpp:1982), and the GPU schedules of
 // test/tests-scheduling-eval.cpp:193-247 (thread-per-row, warp-per-row, nnz-split with
-// atomics + taco_binarySearchBeforeBlock, src/codegen/codegen_cuda.cpp:110-125).
+// atomics after taco_binarySearchBeforeBlock, src/codegen/codegen_cuda.cpp:110-125).
 //
-// Two kernel families:
+// GB300 facts that shape the kernels (measured on the part): FP64 FMA issues at ~1.6 lanes per
+// clock per SM and a DFMA warp instruction costs the same with 1 or 32 lanes active, while FP32
+// FMA issues at ~118 lanes per clock per SM.  HBM delivers about two nonzeros (12 bytes each)
+// per SM clock, so an FP64 SpMV that spends more than one full-warp FP64 instruction per 32
+// nonzeros is FP64-bound, not HBM-bound.
 //
-//  merge  Merge-path over the sequence (row ends, nonzeros): tile t owns merge items
-//         [t*TILE, (t+1)*TILE), so every CTA does the same work whatever the row-length skew.
-//         The CTA stages its nonzeros (vals and the gathered x[crd]) and its row ends in shared
-//         memory with coalesced loads, then each thread walks IPT consecutive merge items and
-//         accumulates with one FMA per nonzero.  A row split across threads is summed from
-//         per-thread carries in shared memory; a row split across tiles gets its earlier part
-//         from a tile carry-out that a fix-up kernel adds.  No atomics on values: results are
-//         deterministic.  On GB300 the FP64 pipe issues about as many DFMA per clock as HBM
-//         delivers nonzeros, so this family spends one FP64 op per nonzero plus one per
-//         thread-boundary crossing, and no FP64 shuffle trees.
-//  vector G lanes per row (G = 1 is thread-per-row, G = 32 is warp-per-row); lanes stride the
-//         row with coalesced loads and combine with a shuffle butterfly.  Cheapest for short
-//         regular rows; its log2(G) FP64 adds per row make it lose on long rows.
+// Kernel families:
 //
-// FP64 values accumulate in FP64.  FP32 values accumulate with TwoProduct + TwoSum
-// compensation (CompF32) and round once at the end.
+//  wmerge  Merge-path over the sequence (row ends, nonzeros).  A scatter kernel writes the
+//          merge coordinate of every CTA tile (one thread per row, no search chains).  A CTA
+//          stages its tile's crd, vals and row ends in shared memory with coalesced loads; each
+//          lane then walks IPT consecutive merge items, gathers x and accumulates; rows split
+//          across lanes are joined by a segmented shuffle scan (all lanes active), rows split
+//          across warps by one thread over eight warp carries, rows split across tiles by a
+//          fix-up kernel over tile carry-outs.  Row results are staged in shared memory and
+//          written coalesced.  No atomics: results are deterministic.
+//          Accumulation policies:
+//            native  FP64 DFMA (FP64 values), or TwoProduct/TwoSum-compensated FP32 (FP32
+//                    values);
+//            df      FP64 values evaluated in double-float on the FP32 pipe: each double is
+//                    split with integer operations into hi+lo floats (46 significant bits),
+//                    products by TwoProduct, sums by TwoSum; a tile whose values fall outside
+//                    [2^-40, 2^40) (or are non-finite) is recomputed with native DFMA.  Error
+//                    about 1e-14 relative, far inside the 1e-12 parity bar, at FP32-pipe cost.
+//  vector  G lanes per row (G = 1 is thread-per-row, G = 32 is warp-per-row); lanes stride the
+//          row with coalesced loads and combine with a shuffle butterfly.  Cheapest for short
+//          regular rows in FP32; its log2(G) FP64 adds per row cost full warp instructions.
 
 #include <cstdio>
+#include <type_traits>
 
 #include "common.cuh"
 #include "kernels.h"
 
 namespace tacogb {
 
-// ------------------------------------------------------------------ accumulators ----------
+// ------------------------------------------------------------------ policies -------------
 
-template <typename V> struct Acc;
-
-template <> struct Acc<double> {
-  double v;
-  __device__ __forceinline__ void zero() { v = 0.0; }
-  __device__ __forceinline__ void add_prod(double a, double b) { v = __fma_rn(a, b, v); }
-  __device__ __forceinline__ void add(const Acc& o) { v = __dadd_rn(v, o.v); }
-  __device__ __forceinline__ void add_value(double o) { v = __dadd_rn(v, o); }
-  __device__ __forceinline__ double result() const { return v; }
-  __device__ __forceinline__ void shfl_xor_add(int m) {
-    v = __dadd_rn(v, __shfl_xor_sync(0xffffffffu, v, m));
-  }
+struct DF {  // double-float value hi + lo
+  float h, l;
 };
 
-template <> struct Acc<float> {
-  CompF32 c;
-  __device__ __forceinline__ void zero() { c.zero(); }
-  __device__ __forceinline__ void add_prod(float a, float b) { c.add_prod(a, b); }
-  __device__ __forceinline__ void add(const Acc& o) { c.add(o.c); }
-  __device__ __forceinline__ void add_value(float o) {
-    CompF32 t;
-    t.hi = o;
-    t.lo = 0.f;
-    c.add(t);
-  }
-  __device__ __forceinline__ float result() const { return c.result(); }
-  __device__ __forceinline__ void shfl_xor_add(int m) {
-    CompF32 o;
-    o.hi = __shfl_xor_sync(0xffffffffu, c.hi, m);
-    o.lo = __shfl_xor_sync(0xffffffffu, c.lo, m);
-    c.add(o);
-  }
-};
-
-template <typename V>
-__device__ __forceinline__ V ld_stream(const V* p);
-template <>
-__device__ __forceinline__ double ld_stream<double>(const double* p) { return ld_stream_f64(p); }
-template <>
-__device__ __forceinline__ float ld_stream<float>(const float* p) { return ld_stream_f32(p); }
-
-// ------------------------------------------------------------------ merge path ------------
-
-// Coordinate (rows ended, nonzeros consumed) of merge diagonal t*tile_items over the row ends
-// pos[1..n] and the nonzero indices 0..nnz-1.  Row end r sorts before nonzero k iff
-// pos[r+1] <= k.
-__global__ void spmv_merge_partition(const int32_t* __restrict__ pos, int32_t n, int64_t nnz,
-                                     int64_t tile_items, int32_t num_tiles,
-                                     int2* __restrict__ part) {
-  int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t > num_tiles) return;
-  int64_t total = (int64_t)n + nnz;
-  int64_t d = (int64_t)t * tile_items;
-  if (d > total) d = total;
-  int64_t lo = d - nnz > 0 ? d - nnz : 0;
-  int64_t hi = d < (int64_t)n ? d : (int64_t)n;
-  while (lo < hi) {
-    int64_t mid = (lo + hi) >> 1;
-    if ((int64_t)__ldg(pos + mid + 1) <= d - mid - 1) lo = mid + 1; else hi = mid;
-  }
-  part[t] = make_int2((int)lo, (int)(d - lo));
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  float t = __fadd_rn(__fadd_rn(a.l, b.l), e);
+  DF r;
+  r.h = __fadd_rn(s, t);
+  r.l = __fsub_rn(t, __fsub_rn(r.h, s));
+  return r;
 }
 
-template <typename V, int BLOCK, int IPT>
-struct MergeSmem {
-  static constexpr int TILE = BLOCK * IPT;
-  static constexpr int LONG_RUN = 16;                 // carries summed serially up to this
-  static constexpr int MAX_JOBS = BLOCK / LONG_RUN + 2;  // disjoint runs longer than LONG_RUN
-  V v[TILE];
-  V x[TILE];
-  int32_t re[TILE];
-  int32_t crow[BLOCK];
-  Acc<V> cval[BLOCK];
-  Acc<V> job_first[MAX_JOBS];
-  int32_t job_a[MAX_JOBS], job_b[MAX_JOBS], job_dst[MAX_JOBS];
-  int32_t njobs;
+// Splits a double into hi + lo floats with integer operations only (no FP64 instruction):
+// hi takes the sign, exponent and top 23 mantissa bits; lo the next 23 bits of the remainder.
+// |v - (hi + lo)| < 2^-46 |v|.  Returns false when |v| is outside [2^-40, 2^40) and v != 0
+// (including inf/nan), where the representation would lose precision.
+__device__ __forceinline__ bool split_df(double v, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned int bh = (unsigned int)(b >> 32);
+  const unsigned int e = (bh >> 20) & 0x7FFu;
+  const unsigned int sign = bh & 0x80000000u;
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  const bool zero = (b << 1) == 0ull;
+  const bool ok = (e - 983u) < 80u;  // 2^-40 <= |v| < 2^40
+  const unsigned int ee = ok ? e : 1023u;
+  hi = __int_as_float((int)(sign | ((ee - 896u) << 23) | (unsigned int)(m >> 29)));
+  const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull) >> 6;  // next 23 bits
+  const float r = __fsub_rn(__int_as_float((int)(0x4B000000u | rem)), 8388608.0f);
+  const float scale = __int_as_float((int)((ee - 1069u + 127u) << 23));  // 2^(e-1069)
+  lo = __int_as_float(__float_as_int(__fmul_rn(r, scale)) | (int)sign);
+  if (zero) {
+    hi = 0.f;
+    lo = 0.f;
+  }
+  return ok || zero;
+}
+
+// FP64 values, FP64 accumulation.
+struct PolNative64 {
+  using Val = double;
+  using Out = double;
+  using Acc = double;
+  static constexpr bool kChecked = false;
+  __device__ static Acc zero() { return 0.0; }
+  __device__ static bool madd(Acc& acc, Val a, Val x) {
+    acc = __fma_rn(a, x, acc);
+    return true;
+  }
+  __device__ static Acc add(Acc a, Acc b) { return __dadd_rn(a, b); }
+  __device__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+  __device__ static Acc shfl_xor(Acc a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
+  __device__ static Out out(Acc a) { return a; }
+  __device__ static double to_double(Acc a) { return a; }
 };
 
-template <typename V, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK, 4)
-spmv_merge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
-                  const V* __restrict__ vals, const V* __restrict__ x, V* __restrict__ y,
-                  const int2* __restrict__ part, int32_t* __restrict__ carry_row,
-                  Acc<V>* __restrict__ carry_val) {
-  using S = MergeSmem<V, BLOCK, IPT>;
+// FP64 values, double-float accumulation on the FP32 pipe.
+struct PolDF64 {
+  using Val = double;
+  using Out = double;
+  using Acc = DF;
+  static constexpr bool kChecked = true;
+  __device__ static Acc zero() { return DF{0.f, 0.f}; }
+  __device__ static bool madd(Acc& acc, Val a, Val x) {
+    float ah, al, xh, xl;
+    const bool ok = split_df(a, ah, al) & split_df(x, xh, xl);
+    DF p;
+    p.h = __fmul_rn(ah, xh);
+    const float pe = __fmaf_rn(ah, xh, -p.h);
+    const float pc = __fmaf_rn(ah, xl, __fmul_rn(al, xh));
+    p.l = __fadd_rn(pe, pc);
+    acc = df_add(acc, p);
+    return ok;
+  }
+  __device__ static Acc add(Acc a, Acc b) { return df_add(a, b); }
+  __device__ static Acc shfl_up(Acc a, int d) {
+    return DF{__shfl_up_sync(0xffffffffu, a.h, d), __shfl_up_sync(0xffffffffu, a.l, d)};
+  }
+  __device__ static Acc shfl_xor(Acc a, int m) {
+    return DF{__shfl_xor_sync(0xffffffffu, a.h, m), __shfl_xor_sync(0xffffffffu, a.l, m)};
+  }
+  __device__ static Out out(Acc a) { return __dadd_rn((double)a.h, (double)a.l); }
+  __device__ static double to_double(Acc a) { return out(a); }
+};
+
+// FP32 values, TwoProduct/TwoSum-compensated FP32 accumulation.
+struct PolComp32 {
+  using Val = float;
+  using Out = float;
+  using Acc = DF;
+  static constexpr bool kChecked = false;
+  __device__ static Acc zero() { return DF{0.f, 0.f}; }
+  __device__ static bool madd(Acc& acc, Val a, Val x) {
+    DF p;
+    p.h = __fmul_rn(a, x);
+    p.l = __fmaf_rn(a, x, -p.h);
+    acc = df_add(acc, p);
+    return true;
+  }
+  __device__ static Acc add(Acc a, Acc b) { return df_add(a, b); }
+  __device__ static Acc shfl_up(Acc a, int d) {
+    return DF{__shfl_up_sync(0xffffffffu, a.h, d), __shfl_up_sync(0xffffffffu, a.l, d)};
+  }
+  __device__ static Acc shfl_xor(Acc a, int m) {
+    return DF{__shfl_xor_sync(0xffffffffu, a.h, m), __shfl_xor_sync(0xffffffffu, a.l, m)};
+  }
+  __device__ static Out out(Acc a) { return __fadd_rn(a.h, a.l); }
+  __device__ static double to_double(Acc a) { return (double)a.h + (double)a.l; }
+};
+
+// ------------------------------------------------------------------ partition -------------
+
+// Merge coordinate of every tile boundary D = b*tile_items: the (rows ended, nonzeros consumed)
+// point of the merge path over (row ends, nonzeros).  Row i owns the diagonals
+// [pos[i]+i, pos[i+1]+i]; a boundary D inside them sits at (i, D-i).  One thread per row, so
+// the cost is one coalesced read of pos.  part[tiles] = (n, nnz).
+__global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t n,
+                                        int64_t nnz, int64_t tile_items, int32_t tiles,
+                                        int2* __restrict__ part) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == n) {
+    part[tiles] = make_int2(n, (int)nnz);
+    return;
+  }
+  const int64_t lo = (int64_t)__ldg(pos + i) + i;
+  const int64_t hi = (int64_t)__ldg(pos + i + 1) + i;
+  for (int64_t b = (lo + tile_items - 1) / tile_items; b * tile_items <= hi && b < tiles; b++)
+    part[b] = make_int2((int)i, (int)(b * tile_items - i));
+}
+
+int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_items,
+                    int32_t tiles, int2* part, cudaStream_t st) {
+  const int64_t threads = (int64_t)n + 1;
+  TACOGB_LAUNCH("merge_partition_scatter", st,
+                merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                    pos, n, nnz, tile_items, tiles, part));
+  return 0;
+}
+
+// ------------------------------------------------------------------ wmerge ----------------
+
+constexpr int kWmBlock = 256;
+constexpr int kWmWarps = kWmBlock / 32;
+
+template <class P, int IPT>
+struct WmSmem {
+  static constexpr int ITEMS = kWmBlock * IPT;
+  int32_t crd[ITEMS];
+  typename P::Val val[ITEMS];
+  int32_t re[ITEMS];  // global nonzero index of each row end in the tile
+  double y[ITEMS];    // row results (policy accumulator, 8 bytes for every policy)
+  int32_t wkey[kWmWarps];
+  double wval[kWmWarps];  // warp carries (policy accumulator)
+};
+
+// Tile-local merge coordinate of diagonal d (rows ended, nonzeros consumed).
+__device__ __forceinline__ void tile_search(const int32_t* s_re, int rn, int kn, int k0, int d,
+                                            int& row, int& k) {
+  int lo = max(d - kn, 0), hi = min(d, rn);
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (s_re[mid] <= k0 + d - mid - 1) lo = mid + 1; else hi = mid;
+  }
+  row = lo;
+  k = d - lo;
+}
+
+template <class A>
+__device__ __forceinline__ A& as_acc(double& slot) {
+  static_assert(sizeof(A) == sizeof(double), "accumulator must be 8 bytes");
+  return *reinterpret_cast<A*>(&slot);
+}
+
+// Walks this lane's merge items with policy P, joins lanes and warps, and leaves every row
+// result of the tile in s.y; the part of the row still open at the tile end is returned in
+// `carry` (thread 0).  Returns false when a checked policy met a value it cannot represent.
+template <class P, class S>
+__device__ __forceinline__ bool wm_tile(S& s, const typename P::Val* __restrict__ x, int rn,
+                                        int kn, int k0, int ipt, typename P::Acc& carry) {
+  using Acc = typename P::Acc;
+  using Val = typename P::Val;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int items = rn + kn;
+  const int ds = min(tid * ipt, items), de = min(ds + ipt, items);
+  int row, ks, row_e, ke;
+  tile_search(s.re, rn, kn, k0, ds, row, ks);
+  tile_search(s.re, rn, kn, k0, de, row_e, ke);
+  const int cnt = ke - ks;
+
+  bool ok = true;
+  Acc acc = P::zero(), first = P::zero();
+  int first_row = -1;
+  constexpr int CH = 8;
+  for (int c = 0; c < ipt; c += CH) {
+    Val xv[CH], vv[CH];
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+      if (c + j < cnt) {
+        vv[j] = s.val[ks + c + j];
+        xv[j] = __ldg(x + s.crd[ks + c + j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+      while (row < row_e && s.re[row] <= k0 + ks + c + j) {
+        if (first_row < 0) {
+          first_row = row;
+          first = acc;
+        } else {
+          as_acc<Acc>(s.y[row]) = acc;
+        }
+        acc = P::zero();
+        row++;
+      }
+      if (c + j < cnt) ok &= P::madd(acc, vv[j], xv[j]);
+    }
+  }
+  while (row < row_e) {
+    if (first_row < 0) {
+      first_row = row;
+      first = acc;
+    } else {
+      as_acc<Acc>(s.y[row]) = acc;
+    }
+    acc = P::zero();
+    row++;
+  }
+
+  // Segmented inclusive scan of lane carries keyed by the open row (keys are non-decreasing
+  // along the lanes, so equal keys are contiguous).
+  const int key = row_e;
+  Acc sc = acc;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const Acc o = P::shfl_up(sc, d);
+    const int ko = __shfl_up_sync(0xffffffffu, key, d);
+    if (lane >= d && ko == key) sc = P::add(o, sc);
+  }
+  const Acc prev = P::shfl_up(sc, 1);
+  const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+  if (first_row >= 0) {
+    Acc tot = first;
+    if (lane > 0 && kprev == first_row) tot = P::add(prev, first);
+    as_acc<Acc>(s.y[first_row]) = tot;
+  }
+  if (lane == 31) {
+    s.wkey[warp] = key;
+    as_acc<Acc>(s.wval[warp]) = sc;
+  }
+  __syncthreads();
+  // Warps in order: a run of equal open-row keys adds into the row where it ends (a later
+  // warp's first row) or, for the final run, becomes the tile carry-out.
+  if (tid == 0) {
+    int rk = s.wkey[0];
+    Acc rv = as_acc<Acc>(s.wval[0]);
+    for (int w = 1; w <= kWmWarps; w++) {
+      if (w < kWmWarps && s.wkey[w] == rk) {
+        rv = P::add(rv, as_acc<Acc>(s.wval[w]));
+        continue;
+      }
+      if (rk < rn) as_acc<Acc>(s.y[rk]) = P::add(rv, as_acc<Acc>(s.y[rk]));
+      else carry = rv;
+      if (w < kWmWarps) {
+        rk = s.wkey[w];
+        rv = as_acc<Acc>(s.wval[w]);
+      }
+    }
+  }
+  return ok;
+}
+
+template <class P, int IPT>
+__global__ void __launch_bounds__(kWmBlock, 2)
+spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+                   const typename P::Val* __restrict__ vals, const typename P::Val* __restrict__ x,
+                   typename P::Out* __restrict__ y, const int2* __restrict__ part, int32_t n,
+                   int32_t* __restrict__ carry_row, double* __restrict__ carry_val) {
+  using S = WmSmem<P, IPT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S& s = *reinterpret_cast<S*>(smem_raw);
-
   const int tid = threadIdx.x;
   const int tile = blockIdx.x;
   const int2 c0 = part[tile], c1 = part[tile + 1];
   const int r0 = c0.x, k0 = c0.y;
   const int rn = c1.x - c0.x, kn = c1.y - c0.y;
-  if (tid == 0) s.njobs = 0;
 
-  for (int j = tid; j < rn; j += BLOCK) s.re[j] = __ldg(pos + r0 + 1 + j);
-  {
-    int32_t cc[IPT];
-    V vv[IPT];
-#pragma unroll
-    for (int j = 0; j < IPT; j++) {
-      int idx = tid + j * BLOCK;
-      if (idx < kn) {
-        cc[j] = ld_stream_i32(crd + k0 + idx);
-        vv[j] = ld_stream<V>(vals + k0 + idx);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < IPT; j++) {
-      int idx = tid + j * BLOCK;
-      if (idx < kn) {
-        s.v[idx] = vv[j];
-        s.x[idx] = __ldg(x + cc[j]);
-      }
-    }
+  for (int i = tid; i < kn; i += kWmBlock) {
+    s.crd[i] = ld_stream_i32(crd + k0 + i);
+    s.val[i] = vals[k0 + i];
   }
+  for (int i = tid; i < rn; i += kWmBlock) s.re[i] = __ldg(pos + r0 + 1 + i);
   __syncthreads();
 
-  // This thread's start on the tile-local merge path.
-  const int items = rn + kn;
-  const int dt = min(tid * IPT, items);
-  int lo = max(dt - kn, 0), hi = min(dt, rn);
-  while (lo < hi) {
-    int mid = (lo + hi) >> 1;
-    if (s.re[mid] <= k0 + dt - mid - 1) lo = mid + 1; else hi = mid;
-  }
-  int row = lo, k = dt - lo;
-
-  Acc<V> acc, first;
-  acc.zero();
-  first.zero();
-  int first_row = -1;
-#pragma unroll
-  for (int it = 0; it < IPT; it++) {
-    if (row < rn && s.re[row] <= k0 + k) {
-      if (first_row < 0) {
-        first_row = row;
-        first = acc;
-      } else {
-        y[r0 + row] = acc.result();
-      }
-      acc.zero();
-      row++;
-    } else if (k < kn) {
-      acc.add_prod(s.v[k], s.x[k]);
-      k++;
-    }
-  }
-  s.crow[tid] = r0 + row;  // row still open after this thread's items (n past the end)
-  s.cval[tid] = acc;
-  __syncthreads();
-
-  // s.crow is non-decreasing in thread order, so the threads that ended inside one row form a
-  // contiguous run; lower_bound finds its first thread.
-  auto run_start = [&](int target, int limit) {
-    int a = 0, b = limit;
-    while (a < b) {
-      int m = (a + b) >> 1;
-      if (s.crow[m] < target) a = m + 1; else b = m;
-    }
-    return a;
-  };
-  auto push_job = [&](int a, int b, int dst, const Acc<V>& f) {
-    int slot = atomicAdd(&s.njobs, 1);
-    s.job_a[slot] = a;
-    s.job_b[slot] = b;
-    s.job_dst[slot] = dst;
-    s.job_first[slot] = f;
-  };
-
-  // First completed row of this thread: its carries from the preceding threads plus `first`.
-  if (first_row >= 0) {
-    const int fr = r0 + first_row;
-    const int a = run_start(fr, tid);
-    if (tid - a <= S::LONG_RUN) {
-      Acc<V> tot;
-      tot.zero();
-      for (int t = a; t < tid; t++) tot.add(s.cval[t]);
-      tot.add(first);
-      y[fr] = tot.result();
+  double carry_d = 0.0;
+  bool native = !P::kChecked;
+  if constexpr (P::kChecked) {
+    typename P::Acc carry = P::zero();
+    const bool ok = wm_tile<P>(s, x, rn, kn, k0, IPT, carry);
+    if (__syncthreads_and(ok)) {
+      for (int i = tid; i < rn; i += kWmBlock) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
+      carry_d = P::to_double(carry);
     } else {
-      push_job(a, tid - 1, fr, first);
+      native = true;
     }
   }
-  // Tile carry-out: the run of threads whose open row is still open at the tile end.
-  if (tid == BLOCK - 1) {
-    const int cr = r0 + rn;
-    const int a = run_start(cr, BLOCK - 1);
-    Acc<V> zero;
-    zero.zero();
-    if (BLOCK - a <= S::LONG_RUN) {
-      Acc<V> tot;
-      tot.zero();
-      for (int t = a; t < BLOCK; t++) tot.add(s.cval[t]);
-      carry_row[tile] = cr;
-      carry_val[tile] = tot;
-    } else {
-      push_job(a, BLOCK - 1, -1, zero);
-    }
+  if (native) {
+    using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
+    typename Q::Acc carry = Q::zero();
+    wm_tile<Q>(s, (const typename Q::Val*)x, rn, kn, k0, IPT, carry);
+    __syncthreads();
+    for (int i = tid; i < rn; i += kWmBlock)
+      y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
+    carry_d = Q::to_double(carry);
   }
-  __syncthreads();
-
-  const int warp = tid >> 5, lane = tid & 31;
-  const int njobs = s.njobs;
-  for (int job = warp; job < njobs; job += BLOCK / 32) {
-    const int a = s.job_a[job], b = s.job_b[job];
-    Acc<V> part;
-    part.zero();
-    for (int t = a + lane; t <= b; t += 32) part.add(s.cval[t]);
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) part.shfl_xor_add(m);
-    if (lane == 0) {
-      part.add(s.job_first[job]);
-      const int dst = s.job_dst[job];
-      if (dst >= 0) {
-        y[dst] = part.result();
-      } else {
-        carry_row[tile] = r0 + rn;
-        carry_val[tile] = part;
-      }
-    }
+  if (tid == 0) {
+    carry_row[tile] = r0 + rn;
+    carry_val[tile] = carry_d;
   }
 }
 
 // Adds the tile carry-outs to the rows that continue into later tiles.  Tiles carrying the same
 // row are consecutive; the first tile of each run sums the run in tile order.
-template <typename V>
-__global__ void spmv_merge_fixup(const int32_t* __restrict__ carry_row,
-                                 const Acc<V>* __restrict__ carry_val, int32_t num_tiles,
-                                 V* __restrict__ y, int32_t n) {
-  int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= num_tiles) return;
+template <typename Out>
+__global__ void spmv_carry_fixup(const int32_t* __restrict__ carry_row,
+                                 const double* __restrict__ carry_val, int32_t tiles,
+                                 Out* __restrict__ y, int32_t n) {
+  const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tiles) return;
   const int32_t r = carry_row[t];
   if (r >= n) return;
   if (t > 0 && carry_row[t - 1] == r) return;
-  Acc<V> tot = carry_val[t];
-  for (int32_t u = t + 1; u < num_tiles && carry_row[u] == r; u++) tot.add(carry_val[u]);
-  tot.add_value(y[r]);
-  y[r] = tot.result();
+  double tot = carry_val[t];
+  for (int32_t u = t + 1; u < tiles && carry_row[u] == r; u++) tot += carry_val[u];
+  y[r] = (Out)((double)y[r] + tot);
 }
 
 // ------------------------------------------------------------------ vector ----------------
@@ -282,24 +389,25 @@ __global__ void __launch_bounds__(256)
 spmv_vector_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                    const V* __restrict__ vals, const V* __restrict__ x, V* __restrict__ y,
                    int32_t n) {
+  using P = typename std::conditional<sizeof(V) == 8, PolNative64, PolComp32>::type;
   const int lane = threadIdx.x & (G - 1);
-  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t gtid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t gid = gtid / G;
   const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
   // Every lane of a warp runs the same number of outer iterations so that the shuffles below
   // always see the full warp.
-  const int64_t warp_first = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll) / G;
+  const int64_t warp_first = (gtid & ~31ll) / G;
   for (int64_t base = warp_first; base < n; base += ngroups) {
     const int64_t row = base + (gid - warp_first);
-    Acc<V> acc;
-    acc.zero();
+    typename P::Acc acc = P::zero();
     if (row < n) {
       const int32_t p1 = __ldg(pos + row + 1);
       for (int32_t p = __ldg(pos + row) + lane; p < p1; p += G)
-        acc.add_prod(ld_stream<V>(vals + p), __ldg(x + ld_stream_i32(crd + p)));
+        P::madd(acc, vals[p], __ldg(x + ld_stream_i32(crd + p)));
     }
 #pragma unroll
-    for (int m = G / 2; m >= 1; m >>= 1) acc.shfl_xor_add(m);
-    if (row < n && lane == 0) y[row] = acc.result();
+    for (int m = G / 2; m >= 1; m >>= 1) acc = P::add(acc, P::shfl_xor(acc, m));
+    if (row < n && lane == 0) y[row] = P::out(acc);
   }
 }
 
@@ -309,48 +417,48 @@ namespace {
 
 struct SpmvVariant {
   const char* name;
-  int family;  // 0 merge, 1 vector
-  int param;   // IPT for merge, G for vector
+  int family;  // 0 wmerge native, 1 wmerge double-float, 2 vector
+  int param;   // IPT for wmerge, G for vector
 };
 
 const SpmvVariant kSpmvVariants[] = {
-    {"merge_ipt5", 0, 5},   {"merge_ipt7", 0, 7},   {"merge_ipt11", 0, 11},
-    {"vector_g1", 1, 1},    {"vector_g2", 1, 2},    {"vector_g4", 1, 4},
-    {"vector_g8", 1, 8},    {"vector_g16", 1, 16},  {"vector_g32", 1, 32},
+    {"wmerge_ipt8", 0, 8},      {"wmerge_ipt16", 0, 16}, {"wmerge_df_ipt8", 1, 8},
+    {"wmerge_df_ipt16", 1, 16}, {"vector_g1", 2, 1},     {"vector_g2", 2, 2},
+    {"vector_g4", 2, 4},        {"vector_g8", 2, 8},     {"vector_g16", 2, 16},
+    {"vector_g32", 2, 32},
 };
 constexpr int kNumSpmvVariants = sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]);
-constexpr int kMergeBlock = 256;
 
-template <typename V, int IPT>
-int launch_merge(const tacogb_csr* A, const V* x, V* y, cudaStream_t st) {
-  using S = MergeSmem<V, kMergeBlock, IPT>;
-  const int64_t tile_items = S::TILE;
+template <class P, int IPT>
+int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
+                  cudaStream_t st) {
+  using S = WmSmem<P, IPT>;
+  const int64_t tile_items = S::ITEMS;
   const int64_t total = (int64_t)A->rows + A->nnz;
   const int64_t tiles64 = (total + tile_items - 1) / tile_items;
   if (tiles64 == 0) return 0;
   TACOGB_CHECK_ARG(tiles64 < (1ll << 31), "SpMV: too many merge tiles");
   const int32_t tiles = (int32_t)tiles64;
-  const size_t part_bytes = ((size_t)tiles + 1) * sizeof(int2);
-  const size_t crow_bytes = (size_t)tiles * sizeof(int32_t);
-  const size_t cval_bytes = (size_t)tiles * sizeof(Acc<V>);
-  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + 256, 0);
+  const size_t part_bytes = (((size_t)tiles + 1) * sizeof(int2) + 255) & ~(size_t)255;
+  const size_t crow_bytes = ((size_t)tiles * sizeof(int32_t) + 255) & ~(size_t)255;
+  const size_t cval_bytes = (size_t)tiles * sizeof(double);
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes, 0);
   if (!ws) return last_code();
   int2* part = (int2*)ws;
   int32_t* crow = (int32_t*)(ws + part_bytes);
-  Acc<V>* cval = (Acc<V>*)(ws + ((part_bytes + crow_bytes + 15) & ~(size_t)15));
+  double* cval = (double*)(ws + part_bytes + crow_bytes);
 
-  TACOGB_LAUNCH("spmv_merge_partition", st,
-                spmv_merge_partition<<<(tiles + 1 + 255) / 256, 256, 0, st>>>(
-                    A->pos, A->rows, A->nnz, tile_items, tiles, part));
-  auto kern = spmv_merge_kernel<V, kMergeBlock, IPT>;
+  if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
+  auto kern = spmv_wmerge_kernel<P, IPT>;
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(S)));
-  TACOGB_LAUNCH("spmv_merge_kernel", st,
-                kern<<<tiles, kMergeBlock, sizeof(S), st>>>(A->pos, A->crd, (const V*)A->vals, x,
-                                                           y, part, crow, cval));
-  TACOGB_LAUNCH("spmv_merge_fixup", st,
-                spmv_merge_fixup<V><<<(tiles + 255) / 256, 256, 0, st>>>(crow, cval, tiles, y,
-                                                                         A->rows));
+  TACOGB_LAUNCH("spmv_wmerge_kernel", st,
+                kern<<<tiles, kWmBlock, sizeof(S), st>>>(A->pos, A->crd,
+                                                        (const typename P::Val*)A->vals, x, y,
+                                                        part, A->rows, crow, cval));
+  TACOGB_LAUNCH("spmv_carry_fixup", st,
+                spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(
+                    crow, cval, tiles, y, A->rows));
   return 0;
 }
 
@@ -370,21 +478,23 @@ int launch_vector(const tacogb_csr* A, const V* x, V* y, cudaStream_t st) {
 template <typename V>
 int spmv_typed(const tacogb_csr* A, const V* x, V* y, int variant, cudaStream_t st) {
   const SpmvVariant& v = kSpmvVariants[variant];
+  using Native = typename std::conditional<sizeof(V) == 8, PolNative64, PolComp32>::type;
+  using Dbl = typename std::conditional<sizeof(V) == 8, PolDF64, PolComp32>::type;
   if (v.family == 0) {
-    switch (v.param) {
-      case 5: return launch_merge<V, 5>(A, x, y, st);
-      case 7: return launch_merge<V, 7>(A, x, y, st);
-      case 11: return launch_merge<V, 11>(A, x, y, st);
-    }
-  } else {
-    switch (v.param) {
-      case 1: return launch_vector<V, 1>(A, x, y, st);
-      case 2: return launch_vector<V, 2>(A, x, y, st);
-      case 4: return launch_vector<V, 4>(A, x, y, st);
-      case 8: return launch_vector<V, 8>(A, x, y, st);
-      case 16: return launch_vector<V, 16>(A, x, y, st);
-      case 32: return launch_vector<V, 32>(A, x, y, st);
-    }
+    if (v.param == 8) return launch_wmerge<Native, 8>(A, x, y, st);
+    return launch_wmerge<Native, 16>(A, x, y, st);
+  }
+  if (v.family == 1) {
+    if (v.param == 8) return launch_wmerge<Dbl, 8>(A, x, y, st);
+    return launch_wmerge<Dbl, 16>(A, x, y, st);
+  }
+  switch (v.param) {
+    case 1: return launch_vector<V, 1>(A, x, y, st);
+    case 2: return launch_vector<V, 2>(A, x, y, st);
+    case 4: return launch_vector<V, 4>(A, x, y, st);
+    case 8: return launch_vector<V, 8>(A, x, y, st);
+    case 16: return launch_vector<V, 16>(A, x, y, st);
+    case 32: return launch_vector<V, 32>(A, x, y, st);
   }
   set_error(TACOGB_ERR_ARG, "SpMV: bad variant %d", variant);
   return TACOGB_ERR_ARG;
@@ -398,11 +508,9 @@ const char* spmv_variant_name(int v) {
 }
 
 // Structural rule used when neither a tuning record nor the cost model gives a choice: the
-// merge family is robust to any skew; regular short rows go to thread/sub-warp per row.
-int spmv_default_variant(const tacogb_csr* A) {
-  (void)A;
-  return 1;  // merge_ipt7
-}
+// merge family is robust to any skew, and for FP64 values the double-float policy keeps the
+// kernel off GB300's narrow FP64 pipe.
+int spmv_default_variant(const tacogb_csr* A) { return A->vtype == TACOGB_F64 ? 3 : 1; }
 
 int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStream_t st) {
   TACOGB_CHECK_ARG(A != nullptr && x != nullptr && y != nullptr, "SpMV: null argument");

@@ -125,7 +125,7 @@ def test_full_size_powerlaw(full_powerlaw, dtype):
     y_ref = O.spmv(pos, crd, vals, x)
     A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x), dtype=dtype)
     xd = torch.from_numpy(x).to("cuda", dtype)
-    y1 = tg.spmv(A, xd, variant=1)
+    y1 = tg.spmv(A, xd, variant=1)  # wmerge_ipt16, native accumulation
     y2 = tg.spmv(A, xd, variant=1)
     torch.cuda.synchronize()
     assert torch.equal(y1, y2)
@@ -137,12 +137,38 @@ def test_full_size_powerlaw(full_powerlaw, dtype):
     assert normwise(lhs.double().cpu().numpy(), rhs.double().cpu().numpy()) <= 10 * tol
 
 
+def test_full_size_powerlaw_double_float(full_powerlaw):
+    """The default FP64 variant (double-float on the FP32 pipe) at full size."""
+    pos, crd, vals, x = full_powerlaw
+    y_ref = O.spmv(pos, crd, vals, x)
+    A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x))
+    xd = torch.from_numpy(x).cuda()
+    y = tg.spmv(A, xd).cpu().numpy()
+    err = normwise(y, y_ref)
+    assert err <= F64_TOL
+    assert err <= 1e-13  # 46-bit significands: far inside the bar
+
+
 def test_full_size_banded():
     s = W.spmv_banded()
     pos, crd, vals = W.generate(s)
     x = W.dense(25, s.cols)
     y_ref = O.spmv(pos, crd, vals, x)
-    for variant in (1, 6):
+    for variant in (1, 3, 6):
+        assert normwise(run_dev(pos, crd, vals, x, variant), y_ref) <= F64_TOL
+
+
+@pytest.mark.parametrize("scale", [2.0 ** 60, 2.0 ** -60, 1e300])
+def test_double_float_falls_back_outside_range(scale):
+    """Tiles holding values outside [2^-40, 2^40) are recomputed with native DFMA."""
+    s = W.spmv_powerlaw(rows=60000)
+    pos, crd, vals = W.generate(s)
+    vals = vals.copy()
+    vals[len(vals) // 3: len(vals) // 3 + 5000] *= scale
+    x = W.dense(26, s.cols)
+    x[:100] *= 1e-20  # some x out of range too
+    y_ref = O.spmv(pos, crd, vals, x)
+    for variant in (2, 3):
         assert normwise(run_dev(pos, crd, vals, x, variant), y_ref) <= F64_TOL
 
 
