@@ -1,20 +1,24 @@
 """Benchmark of taco_gb300's sparse hot path on one GB300 (or N replicas under torchrun).
 
-Default workload: FP64 CSR SpMV y(i) = A(i,j) * x(j) on the 4,194,304 x 4,194,304 power-law
-matrix (Zipf(2) row lengths scaled to mean 24, clipped to [1, 20000]; ~1.0e8 nnz; columns
-uniform, sorted; values U(-1,1)).  One step = one SpMV over the whole matrix.
+Default workload (the headline): FP64 CSR SpMV y(i) = A(i,j) * x(j) on the 4,194,304 x
+4,194,304 power-law matrix (Zipf(2) row lengths scaled to mean 24, clipped to [1, 20000];
+~1.0e8 nnz; columns uniform, sorted; values U(-1,1)).  One step = one SpMV over the matrix.
+`--workload spmm_powerlaw --n 64|256 --dtype f64|f32|bf16` measures SpMM C = A B on the
+1,048,576^2 power-law matrix (mean 32, max 10,000) with a dense row-major B.
 
-  value  algorithmic GB/s of the device path (inputs resident in HBM), bytes model
-         B = nnz*(4+8) + 4*(rows+1) + 8*cols (x once) + 8*rows (y)
-  e2e    the same metric through taco's kernel ABI (tacogb_spmv_compute on taco_tensor_t with
-         pinned host arrays): every step copies pos/crd/vals/x to the GPU and y back
+  value  algorithmic GB/s of the device path (inputs resident in HBM):
+           SpMV  B = nnz*(4+s_v) + 4*(rows+1) + s_x*cols (x once) + s_y*rows (y)
+           SpMM  B = nnz*(4+s_a) + 4*(rows+1) + s_b*cols*N (B once) + s_c*rows*N (C)
+         (SpMM also reports the gather model, B read once per nonzero, and GFLOP/s)
+  e2e    the same metric through taco's kernel ABI (tacogb_<op>_compute on taco_tensor_t with
+         pinned host arrays): every step copies the operands to the GPU and the result back
   roofline  the dominant kernel's algorithmic bytes / its mean event-timed duration, against
          the measured HBM copy bandwidth
   cpu_baseline  taco's own generated C for the statement (oracle/_ref, compiled with taco's JIT
          flags, OpenMP over all host cores), or the C restatement when that is absent
 
 `--impl reference` times taco's generated CPU code alone (rank 0) and prints its line.
-Working set (1.29 GB) is larger than L2 (129 MB): no flush between steps.
+Every working set is larger than L2 (129 MB): no flush between steps.
 """
 import argparse
 import ctypes
@@ -31,6 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
+ESZ = {"f64": 8, "f32": 4, "bf16": 2}
 
 
 def parse():
@@ -40,12 +45,16 @@ def parse():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="spmv_powerlaw",
-                   choices=["spmv_powerlaw", "spmv_banded", "spmv_small"])
-    p.add_argument("--dtype", default="f64", choices=["f64", "f32"])
+                   choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw"])
+    p.add_argument("--dtype", default="f64", choices=["f64", "f32", "bf16"])
+    p.add_argument("--n", type=int, default=64, help="dense columns of B for SpMM")
     p.add_argument("--variant", type=int, default=-1)
     p.add_argument("--e2e-steps", type=int, default=30)
     p.add_argument("--no-cpu", action="store_true")
-    return p.parse_args()
+    a = p.parse_args()
+    if a.workload.startswith("spmv") and a.dtype == "bf16":
+        p.error("bf16 applies to SpMM's dense operand only")
+    return a
 
 
 def dist_env():
@@ -53,20 +62,9 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
-def workload_spec(name):
-    from taco_gb300 import workloads as W
-    return {"spmv_powerlaw": W.spmv_powerlaw, "spmv_banded": W.spmv_banded,
-            "spmv_small": W.spmv_small}[name]()
-
-
-def bytes_model(rows, cols, nnz, sv=8, sx=8, sy=8):
-    return nnz * (4 + sv) + 4 * (rows + 1) + sx * cols + sy * rows
-
-
 def measured_peak():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
-        with open(path) as f:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
@@ -84,15 +82,162 @@ def ncu_traffic(kernel, workload):
     return None
 
 
+# ----------------------------------------------------------------------------- workloads
+
+class SpmvOp:
+    pattern = "spmv"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        self.spec = {"spmv_powerlaw": W.spmv_powerlaw, "spmv_banded": W.spmv_banded,
+                     "spmv_small": W.spmv_small}[args.workload]()
+        s = self.spec
+        self.pos, self.crd, self.vals = W.generate(s)
+        self.x = W.dense(23, s.cols)
+        self.rows, self.cols, self.nnz = s.rows, s.cols, len(self.crd)
+        e = ESZ[args.dtype]
+        self.bytes = self.nnz * (4 + e) + 4 * (self.rows + 1) + e * self.cols + e * self.rows
+        self.flops = 2 * self.nnz
+        self.metric = "spmv_%s_hbm_gbs" % args.dtype
+        self.workload = "%s_%d" % (args.workload, self.rows)
+
+    def device(self, torch, tg):
+        dt = torch.float64 if self.args.dtype == "f64" else torch.float32
+        A = tg.CsrMatrix.from_numpy(self.pos, self.crd, self.vals, self.cols, dtype=dt)
+        xd = torch.from_numpy(self.x).to("cuda", dt)
+        yd = torch.empty(self.rows, dtype=dt, device="cuda")
+        csr = A.as_csr()
+        L, v = tg.lib(), self.args.variant
+        keep = (A, xd, yd, csr)
+
+        def step(sp):
+            rc = L.tacogb_spmv(ctypes.byref(csr), xd.data_ptr(), yd.data_ptr(), v, sp)
+            if rc:
+                raise RuntimeError(L.tacogb_last_error().decode())
+        return step, keep
+
+    def abi(self, torch, tg, T):
+        dt = torch.float64 if self.args.dtype == "f64" else torch.float32
+        e = ESZ[self.args.dtype]
+        hp, hc = torch.from_numpy(self.pos).pin_memory(), torch.from_numpy(self.crd).pin_memory()
+        hv = torch.from_numpy(self.vals).to(dt).pin_memory()
+        hx = torch.from_numpy(self.x).to(dt).pin_memory()
+        hy = torch.empty(self.rows, dtype=dt).pin_memory()
+        At = T.csr(hp, hc, hv, [self.rows, self.cols])
+        Xt, Yt = T.dense(hx, [self.cols]), T.dense(hy, [self.rows])
+        L = tg.lib()
+        keep = (hp, hc, hv, hx, hy, At, Xt, Yt)
+
+        def step():
+            tg.check(L.tacogb_spmv_compute(Yt.ptr, At.ptr, Xt.ptr), "tacogb_spmv_compute")
+        h2d = (self.rows + 1) * 4 + self.nnz * (4 + e) + self.cols * e
+        return step, keep, h2d, self.rows * e, "tacogb_spmv_compute(taco_tensor_t*) on pinned host arrays"
+
+    def cpu(self):
+        """(kind, one-step callable, keep-alive) for taco's generated code or the port."""
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        y = np.empty(self.rows)
+        if O.ref_available("spmv"):
+            L = O.ref_lib("spmv")
+            At = T.csr(self.pos, self.crd, self.vals, [self.rows, self.cols])
+            Xt, Yt = T.dense(self.x, [self.cols]), T.dense(y, [self.rows])
+            return "reference", lambda: L.compute(Yt.ptr, At.ptr, Xt.ptr), (At, Xt, Yt, y)
+        lib = O.lib()
+        p, c, v, x = self.pos, self.crd, self.vals, self.x
+        return "port", lambda: lib.oracle_spmv_f64(self.rows, p.ctypes.data, c.ctypes.data,
+                                                   v.ctypes.data, x.ctypes.data, y.ctypes.data), y
+
+
+class SpmmOp:
+    pattern = "spmm"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        s = self.spec = W.spmm_powerlaw()
+        self.pos, self.crd, self.vals = W.generate(s)
+        self.N = args.n
+        self.B = W.dense(29, s.cols * self.N).reshape(s.cols, self.N)
+        self.rows, self.cols, self.nnz = s.rows, s.cols, len(self.crd)
+        sa = 8 if args.dtype == "f64" else 4
+        sb = ESZ[args.dtype]
+        sc = 8 if args.dtype == "f64" else 4
+        self.bytes = (self.nnz * (4 + sa) + 4 * (self.rows + 1) + sb * self.cols * self.N
+                      + sc * self.rows * self.N)
+        self.gather_bytes = (self.nnz * (4 + sa) + 4 * (self.rows + 1) + sb * self.nnz * self.N
+                             + sc * self.rows * self.N)
+        self.flops = 2 * self.nnz * self.N
+        self.metric = "spmm_%s_n%d_hbm_gbs" % (args.dtype, self.N)
+        self.workload = "%s_%d_n%d" % (args.workload, self.rows, self.N)
+
+    def _types(self, torch):
+        a = torch.float64 if self.args.dtype == "f64" else torch.float32
+        b = {"f64": torch.float64, "f32": torch.float32, "bf16": torch.bfloat16}[self.args.dtype]
+        return a, b
+
+    def device(self, torch, tg):
+        at, bt = self._types(torch)
+        A = tg.CsrMatrix.from_numpy(self.pos, self.crd, self.vals, self.cols, dtype=at)
+        Bd = torch.from_numpy(self.B).to("cuda", bt)
+        Cd = torch.empty(self.rows, self.N, dtype=at, device="cuda")
+        csr = A.as_csr()
+        L, v = tg.lib(), self.args.variant
+        btype = {"f64": 0, "f32": 1, "bf16": 2}[self.args.dtype]
+        keep = (A, Bd, Cd, csr)
+
+        def step(sp):
+            rc = L.tacogb_spmm(ctypes.byref(csr), self.N, Bd.data_ptr(), btype, Cd.data_ptr(), v, sp)
+            if rc:
+                raise RuntimeError(L.tacogb_last_error().decode())
+        return step, keep
+
+    def abi(self, torch, tg, T):
+        at, bt = self._types(torch)
+        hp, hc = torch.from_numpy(self.pos).pin_memory(), torch.from_numpy(self.crd).pin_memory()
+        hv = torch.from_numpy(self.vals).to(at).pin_memory()
+        hb = torch.from_numpy(self.B).to(bt).pin_memory()
+        hcm = torch.empty(self.rows, self.N, dtype=at).pin_memory()
+        At = T.csr(hp, hc, hv, [self.rows, self.cols])
+        Bt, Ct = T.dense(hb, [self.cols, self.N]), T.dense(hcm, [self.rows, self.N])
+        L = tg.lib()
+        keep = (hp, hc, hv, hb, hcm, At, Bt, Ct)
+
+        def step():
+            tg.check(L.tacogb_spmm_compute(Ct.ptr, At.ptr, Bt.ptr), "tacogb_spmm_compute")
+        sa, sb = (8 if self.args.dtype == "f64" else 4), ESZ[self.args.dtype]
+        h2d = (self.rows + 1) * 4 + self.nnz * (4 + sa) + self.cols * self.N * sb
+        return step, keep, h2d, self.rows * self.N * sa, "tacogb_spmm_compute(taco_tensor_t*) on pinned host arrays"
+
+    def cpu(self):
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        C = np.empty((self.rows, self.N))
+        if O.ref_available("spmm"):
+            L = O.ref_lib("spmm")
+            At = T.csr(self.pos, self.crd, self.vals, [self.rows, self.cols])
+            Bt, Ct = T.dense(self.B, [self.cols, self.N]), T.dense(C, [self.rows, self.N])
+            return "reference", lambda: L.compute(Ct.ptr, At.ptr, Bt.ptr), (At, Bt, Ct, C)
+        lib = O.lib()
+        p, c, v, B = self.pos, self.crd, self.vals, self.B
+        return "port", lambda: lib.oracle_spmm_f64(self.rows, self.N, p.ctypes.data, c.ctypes.data,
+                                                   v.ctypes.data, B.ctypes.data, C.ctypes.data), C
+
+
+def make_op(args):
+    return SpmmOp(args) if args.workload.startswith("spmm") else SpmvOp(args)
+
+
+# ----------------------------------------------------------------------------- clocks
+
 class ClockSampler:
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
-        self.proc = None
-        self.out = None
+        self.index, self.proc, self.out = index, None, None
 
     def start(self):
         try:
@@ -133,28 +278,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(pos, crd, vals, x, reps=None, budget_s=8.0):
-    """taco's generated SpMV (or the C restatement) on all host cores."""
+# ----------------------------------------------------------------------------- CPU legs
+
+def time_cpu(op, budget_s=8.0, reps=None):
+    """Median seconds of one step of taco's generated code (or the port) on all host cores."""
     from oracle import oracle as O
-    from taco_gb300 import taco as T
-    rows, cols = len(pos) - 1, len(x)
     ncores = os.cpu_count() or 1
-    y = np.empty(rows)
-    if O.ref_available("spmv"):
-        kind = "reference"
-        L = O.ref_lib("spmv")
-        O.ref_set_threads(ncores)
-        At, Xt, Yt = T.csr(pos, crd, vals, [rows, cols]), T.dense(x, [cols]), T.dense(y, [rows])
-
-        def once():
-            L.compute(Yt.ptr, At.ptr, Xt.ptr)
-    else:
-        kind = "port"
-        O.set_threads(ncores)
-
-        def once():
-            O.lib().oracle_spmv_f64(rows, pos.ctypes.data, crd.ctypes.data, vals.ctypes.data,
-                                    x.ctypes.data, y.ctypes.data)
+    O.ref_set_threads(ncores)
+    O.set_threads(ncores)
+    kind, once, keep = op.cpu()
     for _ in range(3):
         once()
     times = []
@@ -164,52 +296,51 @@ def cpu_baseline(pos, crd, vals, x, reps=None, budget_s=8.0):
         t0 = time.perf_counter()
         once()
         times.append(time.perf_counter() - t0)
-    t = float(np.median(times))
-    return kind, ncores, t, len(times)
+    del keep
+    return kind, ncores, float(np.median(times)), len(times)
 
 
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
         return
-    s = workload_spec(args.workload)
-    from taco_gb300 import workloads as W
     from oracle import oracle as O
+    from taco_gb300 import build as Bd
+    Bd.build()
     O.build()
-    pos, crd, vals = W.generate(s)
-    x = W.dense(23, s.cols)
-    nnz = len(crd)
-    B = bytes_model(s.rows, s.cols, nnz)
-    kind, cores, _, _ = cpu_baseline(pos, crd, vals, x, reps=args.warmup)
-    # timed: exactly K steps
-    from taco_gb300 import taco as T
-    y = np.empty(s.rows)
-    if kind == "reference":
-        L = O.ref_lib("spmv")
-        At, Xt, Yt = T.csr(pos, crd, vals, [s.rows, s.cols]), T.dense(x, [s.cols]), T.dense(y, [s.rows])
-        step = lambda: L.compute(Yt.ptr, At.ptr, Xt.ptr)  # noqa: E731
-    else:
-        step = lambda: O.lib().oracle_spmv_f64(s.rows, pos.ctypes.data, crd.ctypes.data,  # noqa: E731
-                                               vals.ctypes.data, x.ctypes.data, y.ctypes.data)
-    steps = max(1, min(args.steps, 200))
+    op = make_op(args)
+    ncores = os.cpu_count() or 1
+    O.ref_set_threads(ncores)
+    O.set_threads(ncores)
+    kind, once, keep = op.cpu()
+    for _ in range(max(3, args.warmup)):
+        once()
+    steps = max(1, args.steps)
     t0 = time.perf_counter()
     for _ in range(steps):
-        step()
+        once()
+        if time.perf_counter() - t0 > 120.0:  # keep the reference arm within a few minutes
+            steps = _ + 1
+            break
     dt = time.perf_counter() - t0
-    v = B * steps / dt / 1e9
-    out = {"metric": "spmv_fp64_hbm_gbs", "value": v, "unit": "GB/s", "impl": "reference",
+    v = op.bytes * steps / dt / 1e9
+    code = ("taco generated C, -O3 -ffast-math -std=c99 -fopenmp" if kind == "reference"
+            else "C restatement of taco's loop, -O2 -fopenmp")
+    out = {"metric": op.metric, "value": v, "unit": "GB/s", "impl": "reference",
            "n_gpus": world, "steps": steps, "warmup": args.warmup,
            "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": "%s_%d" % (args.workload, s.rows), "rows": s.rows,
-                      "nnz": nnz, "bytes_per_step": B,
-                      "code": "taco generated C, -O3 -ffast-math -fopenmp" if kind == "reference"
-                      else "C restatement of taco's loop, -O2 -fopenmp"},
-           "cpu_baseline": {"value": v, "unit": "GB/s", "cores": cores, "kind": kind,
-                            "sample": "whole matrix per step, %d steps" % steps},
-           "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+           "config": {"workload": op.workload, "rows": op.rows, "nnz": op.nnz,
+                      "bytes_per_step": op.bytes, "code": code, "threads": ncores},
+           "cpu_baseline": {"value": v, "unit": "GB/s", "cores": ncores, "kind": kind,
+                            "sample": "whole workload per step, %d steps" % steps},
+           "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "gflops": op.flops * steps / dt / 1e9}
     print(json.dumps(out), flush=True)
+    del keep
 
+
+# ----------------------------------------------------------------------------- main
 
 def main():
     args = parse()
@@ -226,30 +357,14 @@ def main():
     Bd.build()
     import taco_gb300 as tg
     from taco_gb300 import taco as T
-    from taco_gb300 import workloads as W
     L = tg.lib()
 
-    s = workload_spec(args.workload)
-    pos, crd, vals = W.generate(s)
-    x = W.dense(23, s.cols)
-    nnz = len(crd)
-    dt = torch.float64 if args.dtype == "f64" else torch.float32
-    esz = 8 if args.dtype == "f64" else 4
-    A = tg.CsrMatrix.from_numpy(pos, crd, vals, s.cols, dtype=dt)
-    xd = torch.from_numpy(x).to("cuda", dt)
-    yd = torch.empty(s.rows, dtype=dt, device="cuda")
-    B = bytes_model(s.rows, s.cols, nnz, esz, esz, esz)
+    op = make_op(args)
     stream = torch.cuda.current_stream()
-    csr = A.as_csr()
     sp = ctypes.c_void_p(stream.cuda_stream)
-
-    def step():
-        rc = L.tacogb_spmv(ctypes.byref(csr), xd.data_ptr(), yd.data_ptr(), args.variant, sp)
-        if rc:
-            raise RuntimeError(L.tacogb_last_error().decode())
-
+    step, keep = op.device(torch, tg)
     for _ in range(max(3, args.warmup)):
-        step()
+        step(sp)
     torch.cuda.synchronize()
 
     sampler = ClockSampler(local_rank) if rank == 0 else None
@@ -264,24 +379,26 @@ def main():
     L.tacogb_profile_begin()
     e0.record(stream)
     for _ in range(args.steps):
-        step()
+        step(sp)
     e1.record(stream)
     torch.cuda.synchronize()
     launches = L.tacogb_launch_count() - launches0
     names = ctypes.create_string_buffer(64 * 16)
-    tot = (ctypes.c_double * 16)()
-    cnt = (ctypes.c_int32 * 16)()
+    tot, cnt = (ctypes.c_double * 16)(), (ctypes.c_int32 * 16)()
     nk = L.tacogb_profile_end(16, names, tot, cnt)
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop() if sampler else None
+    status = ctypes.c_int32(0)
+    L.tacogb_device_status(ctypes.byref(status))
+    if status.value:
+        raise RuntimeError("device status %d after the timed region" % status.value)
     ms = e0.elapsed_time(e1)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    ms_step = ms / args.steps
-    value = B * args.steps * world / (ms / 1e3) / 1e9
+    value = op.bytes * args.steps * world / (ms / 1e3) / 1e9
 
     kernels = {}
     for k in range(nk):
@@ -290,59 +407,55 @@ def main():
     dom = max(kernels, key=lambda k: kernels[k][0])
     dom_ms = kernels[dom][0] / kernels[dom][1]
     peak, peak_kind = measured_peak()
-    achieved = B / (dom_ms / 1e3) / 1e9
-    traffic = ncu_traffic(dom, "%s_%s" % (args.workload, args.dtype))
+    achieved = op.bytes / (dom_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
+                "frac": achieved / peak,
+                "traffic": ncu_traffic(dom, "%s_%s" % (op.workload, args.dtype)),
                 "kernel": dom, "kernel_ms": dom_ms, "peak_source": peak_kind,
                 "kernel_share": kernels[dom][0] / sum(v[0] for v in kernels.values())}
+    del keep
 
-    # e2e through the taco kernel ABI with pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
-        hp = torch.from_numpy(pos).pin_memory()
-        hc = torch.from_numpy(crd).pin_memory()
-        hv = torch.from_numpy(vals).to(dt).pin_memory()
-        hx = torch.from_numpy(x).to(dt).pin_memory()
-        hy = torch.empty(s.rows, dtype=dt).pin_memory()
-        At = T.csr(hp, hc, hv, [s.rows, s.cols])
-        Xt, Yt = T.dense(hx, [s.cols]), T.dense(hy, [s.rows])
+        astep, akeep, h2d, d2h, api = op.abi(torch, tg, T)
         for _ in range(2):
-            tg.check(L.tacogb_spmv_compute(Yt.ptr, At.ptr, Xt.ptr), "spmv_compute")
+            astep()
         if world > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            tg.check(L.tacogb_spmv_compute(Yt.ptr, At.ptr, Xt.ptr), "spmv_compute")
+            astep()
         e2e_s = time.perf_counter() - t0
         if world > 1:
             t = torch.tensor([e2e_s], device="cuda")
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             e2e_s = float(t.item())
-        h2d = (s.rows + 1) * 4 + nnz * (4 + esz) + s.cols * esz
-        e2e = {"value": B * args.e2e_steps * world / e2e_s / 1e9, "unit": "GB/s",
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": s.rows * esz,
-               "steps": args.e2e_steps, "ms_per_step": e2e_s / args.e2e_steps * 1e3,
-               "api": "tacogb_spmv_compute(taco_tensor_t*) on pinned host arrays"}
+        e2e = {"value": op.bytes * args.e2e_steps * world / e2e_s / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "steps": args.e2e_steps, "ms_per_step": e2e_s / args.e2e_steps * 1e3, "api": api}
+        del akeep
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        kind, cores, t, reps = cpu_baseline(pos, crd, vals, x)
-        cpu = {"value": B / t / 1e9, "unit": "GB/s", "cores": cores, "kind": kind,
-               "sample": "whole matrix, median of %d reps" % reps, "ms_per_step": t * 1e3}
+        kind, cores, t, reps = time_cpu(op)
+        cpu = {"value": op.bytes / t / 1e9, "unit": "GB/s", "cores": cores, "kind": kind,
+               "sample": "whole workload, median of %d reps" % reps, "ms_per_step": t * 1e3}
 
     if rank == 0:
-        variant = args.variant if args.variant >= 0 else -1
-        out = {"metric": "spmv_%s_hbm_gbs" % args.dtype, "value": value, "unit": "GB/s",
+        names_v = (tg.spmv_variants() if op.pattern == "spmv" else tg.spmm_variants())
+        config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
+                  "bytes_per_step": op.bytes,
+                  "variant": "auto" if args.variant < 0 else names_v[args.variant],
+                  "l2": "inputs larger than L2 (%.2f GB per step), no flush" % (op.bytes / 1e9),
+                  "parallelism": "replicas" if world > 1 else "single"}
+        if op.pattern == "spmm":
+            config["n"] = op.N
+            config["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9
+        out = {"metric": op.metric, "value": value, "unit": "GB/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-               "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
-               "config": {"workload": "%s_%d" % (args.workload, s.rows), "rows": s.rows,
-                          "cols": s.cols, "nnz": nnz, "bytes_per_step": B,
-                          "variant": "auto" if variant < 0 else tg.spmv_variants()[variant],
-                          "l2": "inputs larger than L2 (%.2f GB per step), no flush" % (B / 1e9),
-                          "parallelism": "replicas" if world > 1 else "single"},
-               "pct_of_peak": value / peak,
+               "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": args.dtype, "data": "synthetic", "config": config,
+               "pct_of_peak": value / peak, "gflops": op.flops * args.steps * world / (ms / 1e3) / 1e9,
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clocks,
                "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kernels.items()}}

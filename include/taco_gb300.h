@@ -57,6 +57,11 @@ const char* tacogb_last_error(void);
 /* Library version string. */
 const char* tacogb_version(void);
 
+/* Reads and clears this device's status word: bit 1 = a bounded device-side wait (an mbarrier
+ * on an asynchronous copy) gave up.  The taco-ABI entry points check it themselves and return
+ * TACOGB_ERR_TIMEOUT; stream-ordered callers of the device layer check it when they sync. */
+int tacogb_device_status(int32_t* status);
+
 /* Number of kernels this library has launched in this process. */
 long long tacogb_launch_count(void);
 /* Per-kernel device timing: between begin and end every launch is bracketed by CUDA events on
@@ -88,6 +93,16 @@ int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, vo
 int tacogb_spmv_variant_count(void);
 const char* tacogb_spmv_variant_name(int32_t variant);
 
+/* C = A B with B (rows = A->cols) x N and C (A->rows x N) dense row-major.
+ * Types: A F64 with B F64 -> C FP64; A F32 with B F32 -> C FP32; A F32 with B BF16 -> C FP32
+ * (BF16 dense operand, FP32 accumulation).  Replaces the generated compute of
+ * C(i,k)=A(i,j)*B(j,k) with A {Dense,Sparse} (src/lower/lowerer_impl_imperative.cpp:1304, dense
+ * k loop) and the GPU schedules of test/tests-scheduling-eval.cpp:249-370. */
+int tacogb_spmm(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C,
+                int32_t variant, void* stream);
+int tacogb_spmm_variant_count(void);
+const char* tacogb_spmm_variant_name(int32_t variant);
+
 /* ------------------------------------------------------------------ taco kernel ABI ----- */
 
 /* y(i) = A(i,j) * x(j).  Replaces the generated assemble/compute/evaluate of that statement
@@ -98,6 +113,16 @@ int tacogb_spmv_evaluate(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x);
 int _shim_tacogb_spmv_assemble(void** args);
 int _shim_tacogb_spmv_compute(void** args);
 int _shim_tacogb_spmv_evaluate(void** args);
+
+/* C(i,k) = A(i,j) * B(j,k), A CSR, B and C {Dense,Dense} row-major.  Replaces the generated
+ * assemble/compute/evaluate of taco "C(i,k) = A(i,j) * B(j,k)" -f=A:ds (same lowering as
+ * tacogb_spmm).  csize 64/64 -> FP64; 32/32 -> FP32; A 32 with B 16 -> BF16 B (extension). */
+int tacogb_spmm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
+int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
+int tacogb_spmm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
+int _shim_tacogb_spmm_assemble(void** args);
+int _shim_tacogb_spmm_compute(void** args);
+int _shim_tacogb_spmm_evaluate(void** args);
 
 #ifdef __cplusplus
 }

@@ -10,7 +10,7 @@ from . import _native
 from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBError, check,
                       lib)
 
-__all__ = ["CsrMatrix", "spmv", "spmv_variants", "lib", "check", "TacoGBError",
+__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "lib", "check", "TacoGBError",
            "TACOGB_F64", "TACOGB_F32", "TACOGB_BF16", "VARIANT_AUTO"]
 
 
@@ -63,6 +63,28 @@ def spmv(A, x, y=None, variant=VARIANT_AUTO, stream=None):
     check(lib().tacogb_spmv(ctypes.byref(c), x.data_ptr(), y.data_ptr(), variant,
                             _stream_ptr(stream)), "tacogb_spmv")
     return y
+
+
+_BTYPE = {8: TACOGB_F64, 4: TACOGB_F32, 2: TACOGB_BF16}
+
+
+def spmm(A, B, C=None, variant=VARIANT_AUTO, stream=None):
+    """C = A B on the GPU through tacogb_spmm.  B is a (A.cols x N) row-major torch tensor of
+    float64 (A FP64), float32 or bfloat16 (A FP32); C is float64 or float32 accordingly."""
+    import torch
+    N = B.shape[1]
+    if C is None:
+        C = torch.empty(A.rows, N, dtype=torch.float64 if A.vtype == TACOGB_F64 else torch.float32,
+                        device=B.device)
+    c = A.as_csr()
+    check(lib().tacogb_spmm(ctypes.byref(c), N, B.data_ptr(), _BTYPE[B.element_size()],
+                            C.data_ptr(), variant, _stream_ptr(stream)), "tacogb_spmm")
+    return C
+
+
+def spmm_variants():
+    L = lib()
+    return [L.tacogb_spmm_variant_name(i).decode() for i in range(L.tacogb_spmm_variant_count())]
 
 
 def spmv_variants():

@@ -64,6 +64,7 @@ I64 = ctypes.c_int64
 SIGNATURES = {
     "tacogb_last_error": (ctypes.c_char_p, []),
     "tacogb_version": (ctypes.c_char_p, []),
+    "tacogb_device_status": (I32, [ctypes.POINTER(I32)]),
     "tacogb_launch_count": (ctypes.c_longlong, []),
     "tacogb_profile_begin": (None, []),
     "tacogb_profile_end": (I32, [I32, P, P, P]),
@@ -76,6 +77,15 @@ SIGNATURES = {
     "_shim_tacogb_spmv_assemble": (I32, [P]),
     "_shim_tacogb_spmv_compute": (I32, [P]),
     "_shim_tacogb_spmv_evaluate": (I32, [P]),
+    "tacogb_spmm": (I32, [ctypes.POINTER(Csr), I32, P, I32, P, I32, P]),
+    "tacogb_spmm_variant_count": (I32, []),
+    "tacogb_spmm_variant_name": (ctypes.c_char_p, [I32]),
+    "tacogb_spmm_assemble": (I32, [P, P, P]),
+    "tacogb_spmm_compute": (I32, [P, P, P]),
+    "tacogb_spmm_evaluate": (I32, [P, P, P]),
+    "_shim_tacogb_spmm_assemble": (I32, [P]),
+    "_shim_tacogb_spmm_compute": (I32, [P]),
+    "_shim_tacogb_spmm_evaluate": (I32, [P]),
 }
 
 GEN_SIGNATURES = {

@@ -20,8 +20,8 @@ INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "lib", "obj")
 
-CU_SOURCES = ["abi.cu", "spmv.cu"]
-PATTERNS = ["spmv"]
+CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu"]
+PATTERNS = ["spmv", "spmm"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -89,6 +89,7 @@ struct DeviceState {
   std::vector<void*> stage;
   std::vector<size_t> stage_cap;
   cudaStream_t stream = nullptr;
+  int* status = nullptr;  // device status word (see device_status())
 };
 
 std::mutex g_mu;
@@ -137,7 +138,36 @@ void* scratch(size_t bytes, int slot) {
   return ds->scratch[slot];
 }
 
+int* device_status() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState* ds = current_device();
+  if (!ds) return nullptr;
+  if (!ds->status) {
+    if (cudaMalloc(&ds->status, 256) != cudaSuccess) {
+      ds->status = nullptr;
+      set_error(TACOGB_ERR_ALLOC, "device status: cudaMalloc failed");
+      return nullptr;
+    }
+    cudaMemset(ds->status, 0, 256);
+  }
+  return ds->status;
+}
+
 namespace {
+
+// Reads and clears the device status word; TACOGB_ERR_TIMEOUT when a bounded wait gave up.
+int consume_device_status() {
+  int* st = device_status();
+  if (!st) return TACOGB_ERR_ALLOC;
+  int h = 0;
+  TACOGB_CUDA_TRY(cudaMemcpy(&h, st, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    TACOGB_CUDA_TRY(cudaMemset(st, 0, sizeof(int)));
+    set_error(TACOGB_ERR_TIMEOUT, "a bounded device-side wait timed out (status %d)", h);
+    return TACOGB_ERR_TIMEOUT;
+  }
+  return 0;
+}
 
 // Device staging buffer `slot` with room for `bytes` (for host-resident taco operands).
 void* stage_buffer(int slot, size_t bytes) {
@@ -299,6 +329,16 @@ extern "C" {
 
 const char* tacogb_last_error(void) { return g_err; }
 
+int tacogb_device_status(int32_t* status) {
+  int* st = device_status();
+  if (!st) return TACOGB_ERR_ALLOC;
+  int h = 0;
+  TACOGB_CUDA_TRY(cudaMemcpy(&h, st, sizeof(int), cudaMemcpyDeviceToHost));
+  TACOGB_CUDA_TRY(cudaMemset(st, 0, sizeof(int)));
+  if (status) *status = h;
+  return 0;
+}
+
 long long tacogb_launch_count(void) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   return g_launches;
@@ -349,6 +389,13 @@ int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, vo
 }
 int tacogb_spmv_variant_count(void) { return spmv_variant_count(); }
 const char* tacogb_spmv_variant_name(int32_t v) { return spmv_variant_name(v); }
+
+int tacogb_spmm(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C,
+                int32_t variant, void* stream) {
+  return spmm_run(A, N, B, btype, C, variant, (cudaStream_t)stream);
+}
+int tacogb_spmm_variant_count(void) { return spmm_variant_count(); }
+const char* tacogb_spmm_variant_name(int32_t v) { return spmm_variant_name(v); }
 
 // ---------------------------------------------------------------- SpMV taco ABI -----------
 
@@ -403,7 +450,7 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   if (y_staged && rows)
     TACOGB_CUDA_TRY(cudaMemcpyAsync(y->vals, ydev, (size_t)rows * vb, cudaMemcpyDeviceToHost, st));
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
-  return 0;
+  return consume_device_status();
 }
 
 int tacogb_spmv_evaluate(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
@@ -419,6 +466,81 @@ int _shim_tacogb_spmv_compute(void** a) {
 }
 int _shim_tacogb_spmv_evaluate(void** a) {
   return tacogb_spmv_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+
+// ---------------------------------------------------------------- SpMM taco ABI -----------
+
+int tacogb_spmm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = check_dense_matrix(C, "spmm result C")) return rc;
+  if (int rc = check_csr(A, "spmm operand A")) return rc;
+  const int vt = value_type_of_csize(C->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spmm: unsupported result csize %d",
+                   C->csize);
+  const bool managed = device_accessible(A->vals) && A->vals != nullptr;
+  void* p = alloc_result((size_t)C->dimensions[0] * (size_t)C->dimensions[1] * value_bytes(vt),
+                         managed);
+  if (!p) return TACOGB_ERR_ALLOC;
+  C->vals = (uint8_t*)p;
+  return 0;
+}
+
+int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = check_dense_matrix(C, "spmm result C")) return rc;
+  if (int rc = check_csr(A, "spmm operand A")) return rc;
+  if (int rc = check_dense_matrix(B, "spmm operand B")) return rc;
+  const int at = value_type_of_csize(A->csize), bt = value_type_of_csize(B->csize);
+  const int ct = value_type_of_csize(C->csize);
+  TACOGB_CHECK_ARG((at == TACOGB_F64 && bt == TACOGB_F64 && ct == TACOGB_F64) ||
+                       (at == TACOGB_F32 && (bt == TACOGB_F32 || bt == TACOGB_BF16) &&
+                        ct == TACOGB_F32),
+                   "spmm: unsupported component sizes (C %d, A %d, B %d)", C->csize, A->csize,
+                   B->csize);
+  const int32_t rows = A->dimensions[0], cols = A->dimensions[1], N = B->dimensions[1];
+  TACOGB_CHECK_ARG(B->dimensions[0] == cols, "spmm: B has %d rows, A has %d columns",
+                   B->dimensions[0], cols);
+  TACOGB_CHECK_ARG(C->dimensions[0] == rows && C->dimensions[1] == N,
+                   "spmm: C is %dx%d, expected %dx%d rows", C->dimensions[0], C->dimensions[1],
+                   rows, N);
+  TACOGB_CHECK_ARG(C->vals != nullptr, "spmm: result values not assembled");
+  const int32_t* pos = (const int32_t*)A->indices[1][0];
+  const int32_t* crd = (const int32_t*)A->indices[1][1];
+  TACOGB_CHECK_ARG(pos != nullptr, "spmm: null pos");
+  int32_t nnz = 0;
+  if (int rc = read_i32(pos + rows, &nnz)) return rc;
+  cudaStream_t st = lib_stream();
+  Operand opos, ocrd, ovals, ob;
+  if (int rc = stage_in(opos, pos, ((size_t)rows + 1) * 4, 0, st)) return rc;
+  if (int rc = stage_in(ocrd, crd, (size_t)nnz * 4, 1, st)) return rc;
+  if (int rc = stage_in(ovals, A->vals, (size_t)nnz * value_bytes(at), 2, st)) return rc;
+  if (int rc = stage_in(ob, B->vals, (size_t)cols * N * value_bytes(bt), 3, st)) return rc;
+  const size_t cbytes = (size_t)rows * N * value_bytes(ct);
+  void* cdev = C->vals;
+  const bool c_staged = !device_accessible(C->vals);
+  if (c_staged) {
+    cdev = stage_buffer(4, cbytes);
+    if (!cdev) return TACOGB_ERR_ALLOC;
+  }
+  tacogb_csr csr{rows, cols, nnz, (const int32_t*)opos.dev, (const int32_t*)ocrd.dev, ovals.dev, at};
+  if (int rc = spmm_run(&csr, N, ob.dev, bt, cdev, TACOGB_VARIANT_AUTO, st)) return rc;
+  if (c_staged && cbytes)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(C->vals, cdev, cbytes, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return consume_device_status();
+}
+
+int tacogb_spmm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = tacogb_spmm_assemble(C, A, B)) return rc;
+  return tacogb_spmm_compute(C, A, B);
+}
+
+int _shim_tacogb_spmm_assemble(void** a) {
+  return tacogb_spmm_assemble((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+int _shim_tacogb_spmm_compute(void** a) {
+  return tacogb_spmm_compute((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+int _shim_tacogb_spmm_evaluate(void** a) {
+  return tacogb_spmm_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
 }
 
 }  // extern "C"

@@ -65,6 +65,72 @@ int sm_count();
 // capture; calls on one device are serialised by the caller's stream order.
 void* scratch(size_t bytes, int slot);
 
+// Per-device status word (device memory, zero when healthy).  Kernels that wait on an mbarrier
+// or a flag set bit TACOGB_DEV_TIMEOUT when a bounded wait gives up; the taco-ABI entry points
+// check it after synchronising, tacogb_device_status() reads and clears it.
+constexpr int TACOGB_DEV_TIMEOUT = 1;
+int* device_status();
+
+// ---------------------------------------------------------------- TMA / mbarrier ----------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Arrive on `bar` and announce `bytes` of asynchronous copies that will complete on it.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Bulk (non-tensor) TMA copy global -> this CTA's shared memory, completing on `bar`.
+// dst, src 16-byte aligned; bytes a positive multiple of 16.
+__device__ __forceinline__ void tma_load_bulk(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// Waits for phase `phase` of `bar` at most ~max_iters polls (with back-off); false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase,
+                                                  uint32_t max_iters = (1u << 20)) {
+  for (uint32_t it = 0; it < max_iters; it++) {
+    if (mbar_try_wait(bar, phase)) return true;
+    if (it > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+// Waits for the copies of `bar`; on timeout records TACOGB_DEV_TIMEOUT and waits once more
+// (again bounded) so that no copy is still writing this CTA's shared memory when it exits.
+__device__ __forceinline__ bool mbar_wait_or_flag(uint64_t* bar, uint32_t phase, int* status) {
+  if (mbar_wait_bounded(bar, phase)) return true;
+  atomicOr(status, TACOGB_DEV_TIMEOUT);
+  mbar_wait_bounded(bar, phase);
+  return false;
+}
+
 // ---------------------------------------------------------------- device helpers ---------
 
 __device__ __forceinline__ double ldg_f64(const double* p) { return __ldg(p); }

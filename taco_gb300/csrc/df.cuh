@@ -1,0 +1,67 @@
+// Double-float arithmetic for FP64 values on GB300's FP32 pipe.
+//
+// A double v is carried as an unevaluated sum hi + lo of two floats.  split_df builds the pair
+// with integer operations only (no FP64 instruction), keeping 46 significant bits; products
+// use the FMA-exact TwoProduct of the hi parts plus rounded cross terms; sums use Knuth's
+// TwoSum followed by a fast renormalisation.  Relative error of one multiply-add is about
+// 2^-46, so sums of random-sign terms stay near 1e-14 relative, inside taco-parity's 1e-12.
+// The representation needs |v| in [2^-40, 2^40) (or v == 0); split_df reports other values so
+// that callers fall back to native FP64.
+#pragma once
+
+#include "common.cuh"
+
+namespace tacogb {
+
+struct DF {  // double-float value hi + lo
+  float h, l;
+};
+
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  float t = __fadd_rn(__fadd_rn(a.l, b.l), e);
+  DF r;
+  r.h = __fadd_rn(s, t);
+  r.l = __fsub_rn(t, __fsub_rn(r.h, s));
+  return r;
+}
+
+// Splits a double into hi + lo floats with integer operations only (no FP64 instruction):
+// hi takes the sign, exponent and top 23 mantissa bits; lo the next 23 bits of the remainder.
+// |v - (hi + lo)| < 2^-46 |v|.  Returns false when |v| is outside [2^-40, 2^40) and v != 0
+// (including inf/nan), where the representation would lose precision.
+__device__ __forceinline__ bool split_df(double v, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned int bh = (unsigned int)(b >> 32);
+  const unsigned int e = (bh >> 20) & 0x7FFu;
+  const unsigned int sign = bh & 0x80000000u;
+  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  const bool zero = (b << 1) == 0ull;
+  const bool ok = (e - 983u) < 80u;  // 2^-40 <= |v| < 2^40
+  const unsigned int ee = ok ? e : 1023u;
+  hi = __int_as_float((int)(sign | ((ee - 896u) << 23) | (unsigned int)(m >> 29)));
+  const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull) >> 6;  // next 23 bits
+  const float r = __fsub_rn(__int_as_float((int)(0x4B000000u | rem)), 8388608.0f);
+  const float scale = __int_as_float((int)((ee - 1069u + 127u) << 23));  // 2^(e-1069)
+  lo = __int_as_float(__float_as_int(__fmul_rn(r, scale)) | (int)sign);
+  if (zero) {
+    hi = 0.f;
+    lo = 0.f;
+  }
+  return ok || zero;
+}
+
+// (hi + lo) * (a_hi + a_lo) for two split doubles, relative error about 2^-46.
+__device__ __forceinline__ DF df_mul(float ah, float al, float bh, float bl) {
+  DF p;
+  p.h = __fmul_rn(ah, bh);
+  const float pe = __fmaf_rn(ah, bh, -p.h);
+  const float pc = __fmaf_rn(ah, bl, __fmul_rn(al, bh));
+  p.l = __fadd_rn(pe, pc);
+  return p;
+}
+
+__device__ __forceinline__ double df_to_double(DF a) { return __dadd_rn((double)a.h, (double)a.l); }
+
+}  // namespace tacogb

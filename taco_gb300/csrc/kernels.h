@@ -12,4 +12,15 @@ const char* spmv_variant_name(int v);
 int spmv_default_variant(const tacogb_csr* A);
 int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStream_t st);
 
+// Merge-path tile boundaries (spmv.cu): part[0..tiles] = (rows ended, nonzeros consumed) at
+// diagonals b*tile_items; rows shorter than snap_len are never split (0 = split anywhere).
+int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_items,
+                    int32_t tiles, int2* part, cudaStream_t st, int32_t snap_len = 0);
+
+// SpMM (spmm.cu)
+int spmm_variant_count();
+const char* spmm_variant_name(int v);
+int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,
+             cudaStream_t st);
+
 }  // namespace tacogb

@@ -38,50 +38,12 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "df.cuh"
 #include "kernels.h"
 
 namespace tacogb {
 
 // ------------------------------------------------------------------ policies -------------
-
-struct DF {  // double-float value hi + lo
-  float h, l;
-};
-
-__device__ __forceinline__ DF df_add(DF a, DF b) {
-  float s, e;
-  two_sum(a.h, b.h, s, e);
-  float t = __fadd_rn(__fadd_rn(a.l, b.l), e);
-  DF r;
-  r.h = __fadd_rn(s, t);
-  r.l = __fsub_rn(t, __fsub_rn(r.h, s));
-  return r;
-}
-
-// Splits a double into hi + lo floats with integer operations only (no FP64 instruction):
-// hi takes the sign, exponent and top 23 mantissa bits; lo the next 23 bits of the remainder.
-// |v - (hi + lo)| < 2^-46 |v|.  Returns false when |v| is outside [2^-40, 2^40) and v != 0
-// (including inf/nan), where the representation would lose precision.
-__device__ __forceinline__ bool split_df(double v, float& hi, float& lo) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-  const unsigned int bh = (unsigned int)(b >> 32);
-  const unsigned int e = (bh >> 20) & 0x7FFu;
-  const unsigned int sign = bh & 0x80000000u;
-  const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  const bool zero = (b << 1) == 0ull;
-  const bool ok = (e - 983u) < 80u;  // 2^-40 <= |v| < 2^40
-  const unsigned int ee = ok ? e : 1023u;
-  hi = __int_as_float((int)(sign | ((ee - 896u) << 23) | (unsigned int)(m >> 29)));
-  const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFull) >> 6;  // next 23 bits
-  const float r = __fsub_rn(__int_as_float((int)(0x4B000000u | rem)), 8388608.0f);
-  const float scale = __int_as_float((int)((ee - 1069u + 127u) << 23));  // 2^(e-1069)
-  lo = __int_as_float(__float_as_int(__fmul_rn(r, scale)) | (int)sign);
-  if (zero) {
-    hi = 0.f;
-    lo = 0.f;
-  }
-  return ok || zero;
-}
 
 // FP64 values, FP64 accumulation.
 struct PolNative64 {
@@ -157,31 +119,39 @@ struct PolComp32 {
 
 // ------------------------------------------------------------------ partition -------------
 
-// Merge coordinate of every tile boundary D = b*tile_items: the (rows ended, nonzeros consumed)
+// Merge coordinate of every tile boundary D = b*2^shift: the (rows ended, nonzeros consumed)
 // point of the merge path over (row ends, nonzeros).  Row i owns the diagonals
 // [pos[i]+i, pos[i+1]+i]; a boundary D inside them sits at (i, D-i).  One thread per row, so
 // the cost is one coalesced read of pos.  part[tiles] = (n, nnz).
+// With snap_len > 0 a boundary inside a row shorter than snap_len moves to that row's end
+// (i+1, pos[i+1]), so that only rows of snap_len or more nonzeros are split between tiles;
+// snap_len < tile size keeps every short row within one boundary, so coordinates stay monotone.
 __global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t n,
-                                        int64_t nnz, int64_t tile_items, int32_t tiles,
-                                        int2* __restrict__ part) {
+                                        int64_t nnz, int shift, int32_t tiles,
+                                        int32_t snap_len, int2* __restrict__ part) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i > n) return;
   if (i == n) {
     part[tiles] = make_int2(n, (int)nnz);
     return;
   }
-  const int64_t lo = (int64_t)__ldg(pos + i) + i;
-  const int64_t hi = (int64_t)__ldg(pos + i + 1) + i;
-  for (int64_t b = (lo + tile_items - 1) / tile_items; b * tile_items <= hi && b < tiles; b++)
-    part[b] = make_int2((int)i, (int)(b * tile_items - i));
+  const int32_t p0 = __ldg(pos + i), p1 = __ldg(pos + i + 1);
+  const int64_t lo = (int64_t)p0 + i;
+  const int64_t hi = (int64_t)p1 + i;
+  const bool snap = (p1 - p0) < snap_len;
+  for (int64_t b = (lo + (1ll << shift) - 1) >> shift; (b << shift) <= hi && b < tiles; b++)
+    part[b] = snap ? make_int2((int)i + 1, p1) : make_int2((int)i, (int)((b << shift) - i));
 }
 
 int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_items,
-                    int32_t tiles, int2* part, cudaStream_t st) {
+                    int32_t tiles, int2* part, cudaStream_t st, int32_t snap_len) {
+  int shift = 0;
+  while ((1ll << shift) < tile_items) shift++;
+  TACOGB_CHECK_ARG((1ll << shift) == tile_items, "merge tiles must be a power of two");
   const int64_t threads = (int64_t)n + 1;
   TACOGB_LAUNCH("merge_partition_scatter", st,
                 merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                    pos, n, nnz, tile_items, tiles, part));
+                    pos, n, nnz, shift, tiles, snap_len, part));
   return 0;
 }
 
@@ -192,14 +162,84 @@ constexpr int kWmWarps = kWmBlock / 32;
 
 template <class P, int IPT>
 struct WmSmem {
+  using Val = typename P::Val;
   static constexpr int ITEMS = kWmBlock * IPT;
-  int32_t crd[ITEMS];
-  typename P::Val val[ITEMS];
-  int32_t re[ITEMS];  // global nonzero index of each row end in the tile
-  double y[ITEMS];    // row results (policy accumulator, 8 bytes for every policy)
+  static constexpr int VPAD = 16 / sizeof(Val);  // values per 16 bytes
+  // Staged arrays keep room for the 16-byte alignment slack of the bulk copies.
+  alignas(16) int32_t crd[ITEMS + 8];
+  alignas(16) Val val[ITEMS + 2 * VPAD];
+  alignas(16) int32_t re[ITEMS + 8];  // global nonzero index of each row end (pos entries)
+  double y[ITEMS];                     // row results (policy accumulator, 8 bytes)
   int32_t wkey[kWmWarps];
   double wval[kWmWarps];  // warp carries (policy accumulator)
+  uint64_t bar;
 };
+
+// Stages a tile's crd[k0,k1), vals[k0,k1) and row ends pos[r0+1, r0+1+rn) in shared memory.
+// With TMA, one thread issues three bulk copies over the 16-byte-aligned spans inside the
+// arrays and every thread waits on the mbarrier (bounded); the sub-16-byte tails at the array
+// ends are loaded by plain loads.  Without TMA (unaligned base pointers), each thread issues
+// its IPT loads before storing any of them.  Returns the shared-memory base pointers for
+// tile-local indices.
+template <bool TMA, class P, int IPT>
+__device__ __forceinline__ void wm_stage(WmSmem<P, IPT>& s, const int32_t* __restrict__ pos,
+                                         const int32_t* __restrict__ crd,
+                                         const typename P::Val* __restrict__ vals, int32_t n,
+                                         int32_t nnz, int r0, int rn, int k0, int kn,
+                                         int* status, const int32_t*& scrd,
+                                         const typename P::Val*& sval, const int32_t*& sre) {
+  using Val = typename P::Val;
+  using S = WmSmem<P, IPT>;
+  const int tid = threadIdx.x;
+  const int k1 = k0 + kn;
+  if constexpr (TMA) {
+    constexpr int VP = S::VPAD;
+    const int a = k0 & ~3, b = max(a, min((k1 + 3) & ~3, nnz & ~3));
+    const int av = k0 & ~(VP - 1), bv = max(av, min((k1 + VP - 1) & ~(VP - 1), nnz & ~(VP - 1)));
+    const int q0 = r0 + 1, q1 = r0 + 1 + rn;  // pos indices of the row ends
+    const int ar = q0 & ~3, br = max(ar, min((q1 + 3) & ~3, (n + 1) & ~3));
+    if (tid == 0) mbar_init(&s.bar, 1);
+    __syncthreads();
+    if (tid == 0) {
+      mbar_arrive_expect_tx(&s.bar, (uint32_t)((b - a) * 4 + (bv - av) * (int)sizeof(Val) +
+                                               (br - ar) * 4));
+      if (b > a) tma_load_bulk(s.crd, crd + a, (uint32_t)(b - a) * 4, &s.bar);
+      if (bv > av) tma_load_bulk(s.val, vals + av, (uint32_t)(bv - av) * sizeof(Val), &s.bar);
+      if (br > ar) tma_load_bulk(s.re, pos + ar, (uint32_t)(br - ar) * 4, &s.bar);
+    }
+    for (int i = max(b, k0) + tid; i < k1; i += kWmBlock) s.crd[i - a] = crd[i];
+    for (int i = max(bv, k0) + tid; i < k1; i += kWmBlock) s.val[i - av] = vals[i];
+    for (int i = max(br, q0) + tid; i < q1; i += kWmBlock) s.re[i - ar] = __ldg(pos + i);
+    mbar_wait_or_flag(&s.bar, 0, status);
+    scrd = s.crd + (k0 - a);
+    sval = s.val + (k0 - av);
+    sre = s.re + (q0 - ar);
+  } else {
+    int32_t cc[IPT];
+    Val vv[IPT];
+#pragma unroll
+    for (int j = 0; j < IPT; j++) {
+      const int i = tid + j * kWmBlock;
+      if (i < kn) {
+        cc[j] = ld_stream_i32(crd + k0 + i);
+        vv[j] = vals[k0 + i];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < IPT; j++) {
+      const int i = tid + j * kWmBlock;
+      if (i < kn) {
+        s.crd[i] = cc[j];
+        s.val[i] = vv[j];
+      }
+    }
+    for (int i = tid; i < rn; i += kWmBlock) s.re[i] = __ldg(pos + r0 + 1 + i);
+    scrd = s.crd;
+    sval = s.val;
+    sre = s.re;
+  }
+  __syncthreads();
+}
 
 // Tile-local merge coordinate of diagonal d (rows ended, nonzeros consumed).
 __device__ __forceinline__ void tile_search(const int32_t* s_re, int rn, int kn, int k0, int d,
@@ -223,16 +263,17 @@ __device__ __forceinline__ A& as_acc(double& slot) {
 // result of the tile in s.y; the part of the row still open at the tile end is returned in
 // `carry` (thread 0).  Returns false when a checked policy met a value it cannot represent.
 template <class P, class S>
-__device__ __forceinline__ bool wm_tile(S& s, const typename P::Val* __restrict__ x, int rn,
-                                        int kn, int k0, int ipt, typename P::Acc& carry) {
+__device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typename P::Val* sval,
+                                        const int32_t* sre, const typename P::Val* __restrict__ x,
+                                        int rn, int kn, int k0, int ipt, typename P::Acc& carry) {
   using Acc = typename P::Acc;
   using Val = typename P::Val;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int items = rn + kn;
   const int ds = min(tid * ipt, items), de = min(ds + ipt, items);
   int row, ks, row_e, ke;
-  tile_search(s.re, rn, kn, k0, ds, row, ks);
-  tile_search(s.re, rn, kn, k0, de, row_e, ke);
+  tile_search(sre, rn, kn, k0, ds, row, ks);
+  tile_search(sre, rn, kn, k0, de, row_e, ke);
   const int cnt = ke - ks;
 
   bool ok = true;
@@ -244,13 +285,13 @@ __device__ __forceinline__ bool wm_tile(S& s, const typename P::Val* __restrict_
 #pragma unroll
     for (int j = 0; j < CH; j++) {
       if (c + j < cnt) {
-        vv[j] = s.val[ks + c + j];
-        xv[j] = __ldg(x + s.crd[ks + c + j]);
+        vv[j] = sval[ks + c + j];
+        xv[j] = __ldg(x + scrd[ks + c + j]);
       }
     }
 #pragma unroll
     for (int j = 0; j < CH; j++) {
-      while (row < row_e && s.re[row] <= k0 + ks + c + j) {
+      while (row < row_e && sre[row] <= k0 + ks + c + j) {
         if (first_row < 0) {
           first_row = row;
           first = acc;
@@ -317,12 +358,13 @@ __device__ __forceinline__ bool wm_tile(S& s, const typename P::Val* __restrict_
   return ok;
 }
 
-template <class P, int IPT>
+template <class P, int IPT, bool TMA>
 __global__ void __launch_bounds__(kWmBlock, 2)
 spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                    const typename P::Val* __restrict__ vals, const typename P::Val* __restrict__ x,
                    typename P::Out* __restrict__ y, const int2* __restrict__ part, int32_t n,
-                   int32_t* __restrict__ carry_row, double* __restrict__ carry_val) {
+                   int32_t nnz, int32_t* __restrict__ carry_row, double* __restrict__ carry_val,
+                   int* status) {
   using S = WmSmem<P, IPT>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S& s = *reinterpret_cast<S*>(smem_raw);
@@ -332,18 +374,16 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   const int r0 = c0.x, k0 = c0.y;
   const int rn = c1.x - c0.x, kn = c1.y - c0.y;
 
-  for (int i = tid; i < kn; i += kWmBlock) {
-    s.crd[i] = ld_stream_i32(crd + k0 + i);
-    s.val[i] = vals[k0 + i];
-  }
-  for (int i = tid; i < rn; i += kWmBlock) s.re[i] = __ldg(pos + r0 + 1 + i);
-  __syncthreads();
+  const int32_t* scrd;
+  const typename P::Val* sval;
+  const int32_t* sre;
+  wm_stage<TMA, P, IPT>(s, pos, crd, vals, n, nnz, r0, rn, k0, kn, status, scrd, sval, sre);
 
   double carry_d = 0.0;
   bool native = !P::kChecked;
   if constexpr (P::kChecked) {
     typename P::Acc carry = P::zero();
-    const bool ok = wm_tile<P>(s, x, rn, kn, k0, IPT, carry);
+    const bool ok = wm_tile<P>(s, scrd, sval, sre, x, rn, kn, k0, IPT, carry);
     if (__syncthreads_and(ok)) {
       for (int i = tid; i < rn; i += kWmBlock) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
       carry_d = P::to_double(carry);
@@ -354,7 +394,8 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   if (native) {
     using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
     typename Q::Acc carry = Q::zero();
-    wm_tile<Q>(s, (const typename Q::Val*)x, rn, kn, k0, IPT, carry);
+    wm_tile<Q>(s, scrd, (const typename Q::Val*)sval, sre, (const typename Q::Val*)x, rn, kn, k0,
+               IPT, carry);
     __syncthreads();
     for (int i = tid; i < rn; i += kWmBlock)
       y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
@@ -448,14 +489,19 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
   int32_t* crow = (int32_t*)(ws + part_bytes);
   double* cval = (double*)(ws + part_bytes + crow_bytes);
 
+  int* status = device_status();
+  if (!status) return last_code();
   if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
-  auto kern = spmv_wmerge_kernel<P, IPT>;
+  // Bulk copies need 16-byte aligned sources: true for every allocator the library meets
+  // (cudaMalloc, cudaMallocManaged, torch); sliced pointers take the register-staged kernel.
+  const bool tma = (((uintptr_t)A->pos | (uintptr_t)A->crd | (uintptr_t)A->vals) & 15) == 0;
+  auto kern = tma ? spmv_wmerge_kernel<P, IPT, true> : spmv_wmerge_kernel<P, IPT, false>;
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(S)));
   TACOGB_LAUNCH("spmv_wmerge_kernel", st,
-                kern<<<tiles, kWmBlock, sizeof(S), st>>>(A->pos, A->crd,
-                                                        (const typename P::Val*)A->vals, x, y,
-                                                        part, A->rows, crow, cval));
+                kern<<<tiles, kWmBlock, sizeof(S), st>>>(
+                    A->pos, A->crd, (const typename P::Val*)A->vals, x, y, part, A->rows,
+                    (int32_t)A->nnz, crow, cval, status));
   TACOGB_LAUNCH("spmv_carry_fixup", st,
                 spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(
                     crow, cval, tiles, y, A->rows));
@@ -513,8 +559,10 @@ const char* spmv_variant_name(int v) {
 int spmv_default_variant(const tacogb_csr* A) { return A->vtype == TACOGB_F64 ? 3 : 1; }
 
 int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStream_t st) {
-  TACOGB_CHECK_ARG(A != nullptr && x != nullptr && y != nullptr, "SpMV: null argument");
+  TACOGB_CHECK_ARG(A != nullptr, "SpMV: null matrix");
   TACOGB_CHECK_ARG(A->rows >= 0 && A->cols >= 0 && A->nnz >= 0, "SpMV: negative size");
+  TACOGB_CHECK_ARG(A->rows == 0 || y != nullptr, "SpMV: null y");
+  TACOGB_CHECK_ARG(A->nnz == 0 || x != nullptr, "SpMV: null x");
   TACOGB_CHECK_ARG(A->nnz <= INT32_MAX, "SpMV: nnz exceeds int32 positions");
   TACOGB_CHECK_ARG(A->rows == 0 || A->pos != nullptr, "SpMV: null pos");
   TACOGB_CHECK_ARG(A->nnz == 0 || (A->crd != nullptr && A->vals != nullptr),

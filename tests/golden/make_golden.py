@@ -59,8 +59,23 @@ def spmv_cases():
     save("spmv_empty_rows", pos=pos, crd=crd, vals=vals, x=x, y=H.ref_spmv(pos, crd, vals, x))
 
 
+def spmm_cases():
+    # taco's spmmCPU inputs (test/tests-scheduling-eval.cpp:549-598): 102x103 CSR at 0.3,
+    # dense 103x128 B, both from srand(75883)
+    (pos, crd, vals, _), (_, _, _, Bd) = H.taco_rand_csr(1021 // 10, 1039 // 10, 0.3,
+                                                          dense_b_cols=128)
+    save("spmm_taco_rand", pos=pos, crd=crd, vals=vals, B=Bd, C=H.ref_spmm(pos, crd, vals, Bd))
+
+    s = W.spec(512, kind=W.POWERLAW, mean=32.0, len_max=512, seed=W.SEED_BASE + 103)
+    pos, crd, vals = W.generate(s)
+    B = W.dense(16, s.cols * 64).reshape(s.cols, 64)
+    save("spmm_powerlaw_n64", pos=pos, crd=crd, vals=vals, B=B, C=H.ref_spmm(pos, crd, vals, B))
+
+
 if __name__ == "__main__":
     B.build()
     O.build()
     assert O.ref_available("spmv"), "taco's generated code is not built (oracle/Makefile.ref)"
     spmv_cases()
+    assert O.ref_available("spmm")
+    spmm_cases()

@@ -51,6 +51,8 @@ def normwise(approx, exact):
     """||approx - exact||_2 / ||exact||_2 (0 when both are zero)."""
     a = np.asarray(approx, dtype=np.float64).ravel()
     e = np.asarray(exact, dtype=np.float64).ravel()
+    scale = max(np.max(np.abs(e)) if e.size else 0.0, 1e-300)
+    a, e = a / scale, e / scale  # no overflow in the squares
     den = np.linalg.norm(e)
     num = np.linalg.norm(a - e)
     return num / den if den > 0 else num
@@ -67,3 +69,15 @@ def ref_spmv(pos, crd, vals, x, threads=1):
     Y = T.dense(y, [rows])
     assert L.compute(Y.ptr, A.ptr, X.ptr) == 0
     return y
+
+
+def ref_spmm(pos, crd, vals, B, threads=1):
+    """taco's generated SpMM compute (C(i,k) = A(i,j) * B(j,k), dense row-major B, C)."""
+    L = O.ref_lib("spmm")
+    O.ref_set_threads(threads)
+    rows, cols, N = len(pos) - 1, B.shape[0], B.shape[1]
+    B = np.ascontiguousarray(B)
+    C = np.empty((rows, N), dtype=np.float64)
+    At, Bt, Ct = T.csr(pos, crd, vals, [rows, cols]), T.dense(B, [cols, N]), T.dense(C, [rows, N])
+    assert L.compute(Ct.ptr, At.ptr, Bt.ptr) == 0
+    return C
