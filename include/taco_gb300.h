@@ -103,6 +103,24 @@ int tacogb_spmm(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, vo
 int tacogb_spmm_variant_count(void);
 const char* tacogb_spmm_variant_name(int32_t variant);
 
+/* Two-phase C = A B with A, B, C CSR ({Dense,Sparse}, int32 pos/crd).  Keeps taco's result
+ * structure exactly: every structural product (no numerical-zero dropping), columns sorted per
+ * row; each value is the A-row-ordered sum of its products with separately rounded multiplies
+ * and adds (taco's serial loop order).  Replaces the generated assemble/compute of
+ * C(i,k)=A(i,j)*B(j,k) over the workspace form of src/index_notation/transformations.cpp:2083
+ * (dense accelerator src/lower/lowerer_impl_imperative.cpp:2197, appends
+ * src/lower/mode_format_compressed.cpp:107-213).
+ *   symbolic  writes Cpos[0..A->rows] (device) and returns nnz(C) (synchronises the stream);
+ *             TACOGB_ERR_OVERFLOW when nnz(C) exceeds int32.
+ *   fill      writes the sorted columns Ccrd[0..nnz(C)) for that Cpos.
+ *   numeric   writes Cvals (A's value type; A and B share it) for that pattern. */
+int tacogb_spgemm_symbolic(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos,
+                           int64_t* nnzC, void* stream);
+int tacogb_spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
+                       int32_t* Ccrd, void* stream);
+int tacogb_spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
+                          const int32_t* Ccrd, void* Cvals, void* stream);
+
 /* ------------------------------------------------------------------ taco kernel ABI ----- */
 
 /* y(i) = A(i,j) * x(j).  Replaces the generated assemble/compute/evaluate of that statement
@@ -123,6 +141,19 @@ int tacogb_spmm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
 int _shim_tacogb_spmm_assemble(void** args);
 int _shim_tacogb_spmm_compute(void** args);
 int _shim_tacogb_spmm_evaluate(void** args);
+
+/* C(i,k) = A(i,j) * B(j,k), all CSR.  assemble allocates and fills C's pos and crd and
+ * allocates its vals (taco's generated assemble, which leaves vals for compute); compute fills
+ * vals over the assembled pattern; evaluate does both.  Result arrays come from malloc for
+ * host operands and cudaMallocManaged for GPU operands (taco's allocator choice,
+ * src/storage/array.cpp:22-33); taco owns them afterwards (pos/crd UserOwns, vals Free,
+ * src/tensor.cpp:263-292). */
+int tacogb_spgemm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
+int tacogb_spgemm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
+int tacogb_spgemm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B);
+int _shim_tacogb_spgemm_assemble(void** args);
+int _shim_tacogb_spgemm_compute(void** args);
+int _shim_tacogb_spgemm_evaluate(void** args);
 
 #ifdef __cplusplus
 }

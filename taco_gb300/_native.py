@@ -86,6 +86,16 @@ SIGNATURES = {
     "_shim_tacogb_spmm_assemble": (I32, [P]),
     "_shim_tacogb_spmm_compute": (I32, [P]),
     "_shim_tacogb_spmm_evaluate": (I32, [P]),
+    "tacogb_spgemm_symbolic": (I32, [ctypes.POINTER(Csr), ctypes.POINTER(Csr), P,
+                                      ctypes.POINTER(I64), P]),
+    "tacogb_spgemm_fill": (I32, [ctypes.POINTER(Csr), ctypes.POINTER(Csr), P, P, P]),
+    "tacogb_spgemm_numeric": (I32, [ctypes.POINTER(Csr), ctypes.POINTER(Csr), P, P, P, P]),
+    "tacogb_spgemm_assemble": (I32, [P, P, P]),
+    "tacogb_spgemm_compute": (I32, [P, P, P]),
+    "tacogb_spgemm_evaluate": (I32, [P, P, P]),
+    "_shim_tacogb_spgemm_assemble": (I32, [P]),
+    "_shim_tacogb_spgemm_compute": (I32, [P]),
+    "_shim_tacogb_spgemm_evaluate": (I32, [P]),
 }
 
 GEN_SIGNATURES = {

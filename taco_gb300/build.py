@@ -20,13 +20,13 @@ INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "lib", "obj")
 
-CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu"]
-PATTERNS = ["spmv", "spmm"]
+CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu", "spgemm.cu"]
+PATTERNS = ["spmv", "spmm", "spgemm"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-    "--expt-relaxed-constexpr", "-I" + INC, "-I" + CSRC,
+    "--expt-relaxed-constexpr", "--extended-lambda", "-I" + INC, "-I" + CSRC,
 ]
 
 

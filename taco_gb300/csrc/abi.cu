@@ -397,6 +397,19 @@ int tacogb_spmm(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, vo
 int tacogb_spmm_variant_count(void) { return spmm_variant_count(); }
 const char* tacogb_spmm_variant_name(int32_t v) { return spmm_variant_name(v); }
 
+int tacogb_spgemm_symbolic(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos,
+                           int64_t* nnzC, void* stream) {
+  return spgemm_symbolic(A, B, Cpos, nnzC, (cudaStream_t)stream);
+}
+int tacogb_spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
+                       int32_t* Ccrd, void* stream) {
+  return spgemm_fill(A, B, Cpos, Ccrd, (cudaStream_t)stream);
+}
+int tacogb_spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
+                          const int32_t* Ccrd, void* Cvals, void* stream) {
+  return spgemm_numeric(A, B, Cpos, Ccrd, Cvals, (cudaStream_t)stream);
+}
+
 // ---------------------------------------------------------------- SpMV taco ABI -----------
 
 int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
@@ -541,6 +554,115 @@ int _shim_tacogb_spmm_compute(void** a) {
 }
 int _shim_tacogb_spmm_evaluate(void** a) {
   return tacogb_spmm_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+
+// ---------------------------------------------------------------- SpGEMM taco ABI ---------
+
+namespace {
+
+// Device views of a CSR taco_tensor_t; host arrays are staged into slots base..base+2.
+int csr_operand(const taco_tensor_t* T, int base, bool with_vals, cudaStream_t st,
+                tacogb_csr& out) {
+  const int32_t rows = T->dimensions[0], cols = T->dimensions[1];
+  const int32_t* pos = (const int32_t*)T->indices[1][0];
+  const int32_t* crd = (const int32_t*)T->indices[1][1];
+  TACOGB_CHECK_ARG(pos != nullptr, "spgemm: null pos");
+  int32_t nnz = 0;
+  if (int rc = read_i32(pos + rows, &nnz)) return rc;
+  const int vt = value_type_of_csize(T->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spgemm: unsupported csize %d", T->csize);
+  Operand op, oc, ov;
+  if (int rc = stage_in(op, pos, ((size_t)rows + 1) * 4, base, st)) return rc;
+  if (int rc = stage_in(oc, crd, (size_t)nnz * 4, base + 1, st)) return rc;
+  if (with_vals) {
+    if (int rc = stage_in(ov, T->vals, (size_t)nnz * value_bytes(vt), base + 2, st)) return rc;
+  }
+  out = tacogb_csr{rows, cols, nnz, (const int32_t*)op.dev, (const int32_t*)oc.dev,
+                   with_vals ? ov.dev : nullptr, vt};
+  return 0;
+}
+
+int check_spgemm(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = check_csr(C, "spgemm result C")) return rc;
+  if (int rc = check_csr(A, "spgemm operand A")) return rc;
+  if (int rc = check_csr(B, "spgemm operand B")) return rc;
+  TACOGB_CHECK_ARG(A->dimensions[1] == B->dimensions[0], "spgemm: A has %d columns, B has %d rows",
+                   A->dimensions[1], B->dimensions[0]);
+  TACOGB_CHECK_ARG(C->dimensions[0] == A->dimensions[0] && C->dimensions[1] == B->dimensions[1],
+                   "spgemm: C is %dx%d, expected %dx%d", C->dimensions[0], C->dimensions[1],
+                   A->dimensions[0], B->dimensions[1]);
+  TACOGB_CHECK_ARG(A->csize == B->csize && C->csize == A->csize,
+                   "spgemm: component sizes differ (C %d, A %d, B %d)", C->csize, A->csize,
+                   B->csize);
+  return 0;
+}
+
+}  // namespace
+
+int tacogb_spgemm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = check_spgemm(C, A, B)) return rc;
+  cudaStream_t st = lib_stream();
+  tacogb_csr a, b;
+  if (int rc = csr_operand(A, 0, false, st, a)) return rc;
+  if (int rc = csr_operand(B, 3, false, st, b)) return rc;
+  const int32_t rows = a.rows;
+  const bool managed = device_accessible(A->indices[1][0]);
+  int32_t* dpos = (int32_t*)stage_buffer(6, ((size_t)rows + 1) * 4);
+  if (!dpos) return TACOGB_ERR_ALLOC;
+  int64_t nnz = 0;
+  if (int rc = spgemm_symbolic(&a, &b, dpos, &nnz, st)) return rc;
+  int32_t* dcrd = (int32_t*)stage_buffer(7, (size_t)nnz * 4);
+  if (!dcrd) return TACOGB_ERR_ALLOC;
+  if (int rc = spgemm_fill(&a, &b, dpos, dcrd, st)) return rc;
+  int32_t* pos = (int32_t*)alloc_result(((size_t)rows + 1) * 4, managed);
+  int32_t* crd = (int32_t*)alloc_result((size_t)nnz * 4, managed);
+  void* vals = alloc_result((size_t)nnz * value_bytes(a.vtype), managed);
+  if (!pos || !crd || !vals) return TACOGB_ERR_ALLOC;
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, dpos, ((size_t)rows + 1) * 4, cudaMemcpyDefault, st));
+  if (nnz) TACOGB_CUDA_TRY(cudaMemcpyAsync(crd, dcrd, (size_t)nnz * 4, cudaMemcpyDefault, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  C->indices[1][0] = (uint8_t*)pos;
+  C->indices[1][1] = (uint8_t*)crd;
+  C->vals = (uint8_t*)vals;
+  return consume_device_status();
+}
+
+int tacogb_spgemm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = check_spgemm(C, A, B)) return rc;
+  TACOGB_CHECK_ARG(C->indices[1][0] != nullptr && C->indices[1][1] != nullptr && C->vals != nullptr,
+                   "spgemm: result not assembled");
+  cudaStream_t st = lib_stream();
+  tacogb_csr a, b, c;
+  if (int rc = csr_operand(A, 0, true, st, a)) return rc;
+  if (int rc = csr_operand(B, 3, true, st, b)) return rc;
+  if (int rc = csr_operand(C, 6, false, st, c)) return rc;
+  const size_t vbytes = (size_t)c.nnz * value_bytes(a.vtype);
+  void* dvals = C->vals;
+  const bool staged = !device_accessible(C->vals);
+  if (staged) {
+    dvals = stage_buffer(9, vbytes);
+    if (!dvals) return TACOGB_ERR_ALLOC;
+  }
+  if (int rc = spgemm_numeric(&a, &b, c.pos, c.crd, dvals, st)) return rc;
+  if (staged && vbytes)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(C->vals, dvals, vbytes, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return consume_device_status();
+}
+
+int tacogb_spgemm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = tacogb_spgemm_assemble(C, A, B)) return rc;
+  return tacogb_spgemm_compute(C, A, B);
+}
+
+int _shim_tacogb_spgemm_assemble(void** a) {
+  return tacogb_spgemm_assemble((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+int _shim_tacogb_spgemm_compute(void** a) {
+  return tacogb_spgemm_compute((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+int _shim_tacogb_spgemm_evaluate(void** a) {
+  return tacogb_spgemm_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
 }
 
 }  // extern "C"

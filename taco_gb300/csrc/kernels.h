@@ -23,4 +23,12 @@ const char* spmm_variant_name(int v);
 int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,
              cudaStream_t st);
 
+// SpGEMM (spgemm.cu)
+int spgemm_symbolic(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int64_t* nnzC,
+                    cudaStream_t st);
+int spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos, int32_t* Ccrd,
+                cudaStream_t st);
+int spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
+                   const int32_t* Ccrd, void* Cvals, cudaStream_t st);
+
 }  // namespace tacogb

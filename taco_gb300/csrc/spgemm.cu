@@ -1,0 +1,670 @@
+// Two-phase CSR x CSR SpGEMM for sm_103a: C(i,k) = A(i,j) * B(j,k), all operands CSR.
+//
+// Replaces the assemble and compute functions taco generates for this statement through the
+// workspace form forall(i, where(forall(k, C(i,k) = w(k)), forall(j,k, w(k) += A(i,j)*B(j,k))))
+// (src/index_notation/transformations.cpp:2083, dense accelerator arrays from
+// src/lower/lowerer_impl_imperative.cpp:2197, compressed appends from
+// src/lower/mode_format_compressed.cpp:107-213) and its parallel two-pass form
+// (test/tests-scheduling-eval.cpp:68-94 -> lowerAssemble,
+// src/lower/lowerer_impl_imperative.cpp:2616-2781).  taco has no GPU schedule for SpGEMM.
+//
+// Semantics kept exactly: every structural product is kept (no numerical-zero dropping), the
+// columns of each row are sorted ascending, and each output value is the sum of its products in
+// A-row order, the first product initialising it — the order of taco's serial loop.  Products
+// and sums are separately rounded (no FMA), so values are bit-identical to taco's generated
+// code when that code is compiled without FMA contraction.
+//
+// Work decomposition: per row, the product count P_i = sum of B-row lengths over A's row.  Rows
+// are binned by P_i; each bin runs expand-sort-compress (ESC) on (column, sequence) keys:
+//   bin 1  P <= 32     one warp per row, keys in registers, warp bitonic sort by shuffles
+//   bin 2  P <= 256    one warp per row, bitonic sort in the warp's shared-memory slice
+//   bin 3  P <= 4096   one CTA per row, bitonic sort in shared memory
+//   bin 4  P >  4096   one CTA per row over a dense per-CTA accumulator in global scratch
+//                      (column bitmap for the pattern, stamp + value arrays for the numbers)
+// Phases: symbolic count -> device exclusive scan -> (caller allocates) -> crd fill; numeric.
+// Bin lists are built with per-bin atomic counters; the order of rows inside a list does not
+// affect any result.
+
+#include <cstdio>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace tacogb {
+
+namespace {
+
+constexpr int kBins = 5;  // 0: empty rows, 1..4 as above
+constexpr int kBin1 = 32, kBin2 = 256, kBin3 = 4096;
+constexpr int kDenseSlots = 64;  // concurrent CTAs of the dense (bin 4) path
+
+__device__ __forceinline__ int bin_of(int64_t p) {
+  return p == 0 ? 0 : p <= kBin1 ? 1 : p <= kBin2 ? 2 : p <= kBin3 ? 3 : 4;
+}
+
+// P_i per row, and the row appended to its bin's list (warp-aggregated atomics per bin).
+__global__ void spgemm_bin_rows(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
+                                const int32_t* __restrict__ Bpos, int32_t n,
+                                int64_t* __restrict__ prod, int32_t* __restrict__ bin_cnt,
+                                int32_t* __restrict__ bin_rows) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int b = -1;
+  if (i < n) {
+    int64_t p = 0;
+    for (int32_t q = __ldg(Apos + i); q < __ldg(Apos + i + 1); q++) {
+      const int32_t j = __ldg(Acrd + q);
+      p += __ldg(Bpos + j + 1) - __ldg(Bpos + j);
+    }
+    prod[i] = p;
+    b = bin_of(p);
+  }
+  const int lane = threadIdx.x & 31;
+  for (int bb = 0; bb < kBins; bb++) {
+    const unsigned m = __ballot_sync(0xffffffffu, b == bb);
+    if (!m) continue;
+    int base = 0;
+    const int leader = __ffs(m) - 1;
+    if (lane == leader) base = atomicAdd(bin_cnt + bb, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (b == bb) bin_rows[(int64_t)bb * n + base + __popc(m & ((1u << lane) - 1))] = (int32_t)i;
+  }
+}
+
+// Sorts 64-bit keys (and payloads) of one warp, one per lane, ascending; invalid lanes hold
+// UINT64_MAX.
+template <typename V>
+__device__ __forceinline__ void warp_bitonic(uint64_t& key, V& val) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint64_t ok = __shfl_xor_sync(0xffffffffu, key, j);
+      const V ov = __shfl_xor_sync(0xffffffffu, val, j);
+      const bool up = (lane & k) == 0;
+      const bool lower = (lane & j) == 0;
+      const bool take = lower == up ? ok < key : ok > key;
+      if (take) {
+        key = ok;
+        val = ov;
+      }
+    }
+  }
+}
+
+// Bitonic sort of cap (power of two) keys/payloads in shared memory by `nthreads` threads
+// starting at thread index `t0`; `sync` synchronises those threads.
+template <typename V, typename Sync>
+__device__ __forceinline__ void smem_bitonic(uint64_t* key, V* val, int cap, int t, int nthreads,
+                                             Sync sync) {
+  for (int k = 2; k <= cap; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int idx = t; idx < cap / 2; idx += nthreads) {
+        const int i = 2 * idx - (idx & (j - 1));
+        const int p = i + j;
+        const bool up = (i & k) == 0;
+        const uint64_t a = key[i], b = key[p];
+        if ((a > b) == up) {
+          key[i] = b;
+          key[p] = a;
+          const V tv = val[i];
+          val[i] = val[p];
+          val[p] = tv;
+        }
+      }
+      sync();
+    }
+  }
+}
+
+template <typename V> __device__ __forceinline__ V mul_rn(V a, V b);
+template <> __device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
+template <typename V> __device__ __forceinline__ V add_rn(V a, V b);
+template <> __device__ __forceinline__ double add_rn<double>(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ float add_rn<float>(float a, float b) { return __fadd_rn(a, b); }
+
+__device__ __forceinline__ uint64_t esc_key(int32_t col, int32_t seq) {
+  return ((uint64_t)(uint32_t)col << 32) | (uint32_t)seq;
+}
+__device__ __forceinline__ int32_t key_col(uint64_t k) { return (int32_t)(k >> 32); }
+
+// MODE 0: count unique columns -> cnt[row]; 1: write sorted columns at Cpos[row];
+// 2: write values (sum of products in sequence order) at Cpos[row].
+template <int MODE, typename V>
+__device__ __forceinline__ void esc_emit_warp(const uint64_t* key, const V* val, int P, int row,
+                                              const int32_t* __restrict__ Cpos,
+                                              int32_t* __restrict__ cnt,
+                                              int32_t* __restrict__ Ccrd, V* __restrict__ Cvals) {
+  const int lane = threadIdx.x & 31;
+  int base = 0;
+  const int out0 = (MODE == 0) ? 0 : Cpos[row];
+  for (int c = 0; c < P; c += 32) {
+    const int e = c + lane;
+    const bool head = e < P && (e == 0 || key_col(key[e]) != key_col(key[e - 1]));
+    const unsigned m = __ballot_sync(0xffffffffu, head);
+    if (MODE != 0 && head) {
+      const int rank = base + __popc(m & ((1u << lane) - 1));
+      if (MODE == 1) {
+        Ccrd[out0 + rank] = key_col(key[e]);
+      } else {
+        V s = val[e];
+        for (int f = e + 1; f < P && key_col(key[f]) == key_col(key[e]); f++) s = add_rn(s, val[f]);
+        Cvals[out0 + rank] = s;
+      }
+    }
+    base += __popc(m);
+  }
+  if (MODE == 0 && lane == 0) cnt[row] = base;
+}
+
+// Expands row `row`'s products into (key, value) slots [0, P) of a buffer, strided over
+// `nthreads` threads starting at `t`.
+template <bool VALS, typename V>
+__device__ __forceinline__ void esc_expand(const int32_t* __restrict__ Apos,
+                                           const int32_t* __restrict__ Acrd,
+                                           const V* __restrict__ Avals,
+                                           const int32_t* __restrict__ Bpos,
+                                           const int32_t* __restrict__ Bcrd,
+                                           const V* __restrict__ Bvals, int row, uint64_t* key,
+                                           V* val, int t, int nthreads) {
+  // Walk A's row; each thread handles products strided over the concatenated B rows.
+  int seq0 = 0;
+  for (int32_t q = __ldg(Apos + row); q < __ldg(Apos + row + 1); q++) {
+    const int32_t j = __ldg(Acrd + q);
+    const int32_t b0 = __ldg(Bpos + j), len = __ldg(Bpos + j + 1) - b0;
+    V a = V();
+    if (VALS) a = Avals[q];
+    for (int u = t; u < len; u += nthreads) {
+      key[seq0 + u] = esc_key(__ldg(Bcrd + b0 + u), seq0 + u);
+      if (VALS) val[seq0 + u] = mul_rn(a, Bvals[b0 + u]);
+    }
+    seq0 += len;
+  }
+}
+
+// ---- bin 1: P <= 32, one warp per row, registers -----------------------------------------
+
+template <int MODE, typename V>
+__global__ void __launch_bounds__(256)
+spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
+            const V* __restrict__ Avals, const int32_t* __restrict__ Bpos,
+            const int32_t* __restrict__ Bcrd, const V* __restrict__ Bvals,
+            const int32_t* __restrict__ rows, const int32_t* __restrict__ count,
+            const int32_t* __restrict__ Cpos, int32_t* __restrict__ cnt,
+            int32_t* __restrict__ Ccrd, V* __restrict__ Cvals) {
+  const int lane = threadIdx.x & 31;
+  const int nr = *count;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nr;
+       w += (gridDim.x * blockDim.x) >> 5) {
+    const int row = rows[w];
+    // lane l takes product l: find its A nonzero by walking the row (<= 32 products)
+    uint64_t key = ~0ull;
+    V val = V();
+    int seq0 = 0;
+    for (int32_t q = __ldg(Apos + row); q < __ldg(Apos + row + 1); q++) {
+      const int32_t j = __ldg(Acrd + q);
+      const int32_t b0 = __ldg(Bpos + j), len = __ldg(Bpos + j + 1) - b0;
+      const int u = lane - seq0;
+      if (u >= 0 && u < len) {
+        key = esc_key(__ldg(Bcrd + b0 + u), lane);
+        if (MODE == 2) val = mul_rn(Avals[q], Bvals[b0 + u]);
+      }
+      seq0 += len;
+    }
+    warp_bitonic(key, val);
+    const int P = seq0;
+    const uint64_t prevk = __shfl_up_sync(0xffffffffu, key, 1);
+    const bool valid = lane < P;
+    const bool head = valid && (lane == 0 || key_col(prevk) != key_col(key));
+    const unsigned m = __ballot_sync(0xffffffffu, head);
+    if (MODE == 0) {
+      if (lane == 0) cnt[row] = __popc(m);
+    } else {
+      // run sums in sequence order: lane-serial accumulation along each run
+      V s = val;
+      if (MODE == 2) {
+        // walk forward within the run from each head
+        for (int d = 1; d < 32; d++) {
+          const uint64_t kd = __shfl_down_sync(0xffffffffu, key, d);
+          const V vd = __shfl_down_sync(0xffffffffu, val, d);
+          const bool same = (lane + d < P) && key_col(kd) == key_col(key);
+          const bool any = __any_sync(0xffffffffu, head && same);
+          if (!any) break;
+          if (head && same) s = add_rn(s, vd);
+        }
+      }
+      if (head) {
+        const int rank = __popc(m & ((1u << lane) - 1));
+        const int o = Cpos[row] + rank;
+        if (MODE == 1) Ccrd[o] = key_col(key);
+        else Cvals[o] = s;
+      }
+    }
+  }
+}
+
+// ---- bin 2: P <= 256, one warp per row, shared memory -------------------------------------
+
+template <int MODE, typename V>
+__global__ void __launch_bounds__(256)
+spgemm_bin2(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
+            const V* __restrict__ Avals, const int32_t* __restrict__ Bpos,
+            const int32_t* __restrict__ Bcrd, const V* __restrict__ Bvals,
+            const int32_t* __restrict__ rows, const int32_t* __restrict__ count,
+            const int64_t* __restrict__ prod, const int32_t* __restrict__ Cpos,
+            int32_t* __restrict__ cnt, int32_t* __restrict__ Ccrd, V* __restrict__ Cvals) {
+  __shared__ uint64_t s_key[8][kBin2];
+  __shared__ V s_val[8][kBin2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint64_t* key = s_key[warp];
+  V* val = s_val[warp];
+  const int nr = *count;
+  for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nr;
+       w += (gridDim.x * blockDim.x) >> 5) {
+    const int row = rows[w];
+    const int P = (int)prod[row];
+    int cap = 32;
+    while (cap < P) cap <<= 1;
+    esc_expand<MODE == 2>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, lane, 32);
+    for (int e = P + lane; e < cap; e += 32) key[e] = ~0ull;
+    __syncwarp();
+    smem_bitonic(key, val, cap, lane, 32, [] __device__() { __syncwarp(); });
+    esc_emit_warp<MODE>(key, val, P, row, Cpos, cnt, Ccrd, Cvals);
+    __syncwarp();
+  }
+}
+
+// ---- bin 3: P <= 4096, one CTA per row, shared memory -------------------------------------
+
+template <int MODE, typename V>
+__global__ void __launch_bounds__(256)
+spgemm_bin3(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
+            const V* __restrict__ Avals, const int32_t* __restrict__ Bpos,
+            const int32_t* __restrict__ Bcrd, const V* __restrict__ Bvals,
+            const int32_t* __restrict__ rows, const int32_t* __restrict__ count,
+            const int64_t* __restrict__ prod, const int32_t* __restrict__ Cpos,
+            int32_t* __restrict__ cnt, int32_t* __restrict__ Ccrd, V* __restrict__ Cvals) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* key = reinterpret_cast<uint64_t*>(smem_raw);
+  V* val = reinterpret_cast<V*>(key + kBin3);
+  __shared__ int32_t s_wcount[8];
+  const int nr = *count;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int w = blockIdx.x; w < nr; w += gridDim.x) {
+    const int row = rows[w];
+    const int P = (int)prod[row];
+    int cap = 32;
+    while (cap < P) cap <<= 1;
+    esc_expand<MODE == 2>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, tid, 256);
+    for (int e = P + tid; e < cap; e += 256) key[e] = ~0ull;
+    __syncthreads();
+    smem_bitonic(key, val, cap, tid, 256, [] __device__() { __syncthreads(); });
+    // heads: per-thread chunks of ELEMS consecutive slots, block prefix over chunk counts
+    constexpr int ELEMS = kBin3 / 256;
+    const int e0 = tid * ELEMS;
+    int local = 0;
+    for (int e = e0; e < e0 + ELEMS && e < P; e++)
+      local += (e == 0 || key_col(key[e]) != key_col(key[e - 1]));
+    // block exclusive scan of `local`
+    int incl = local;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int o = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += o;
+    }
+    if (lane == 31) s_wcount[warp] = incl;
+    __syncthreads();
+    int wbase = 0;
+    for (int x = 0; x < warp; x++) wbase += s_wcount[x];
+    int rank = wbase + incl - local;
+    if (MODE == 0) {
+      if (tid == 255) cnt[row] = wbase + incl;
+    } else {
+      const int o0 = Cpos[row];
+      for (int e = e0; e < e0 + ELEMS && e < P; e++) {
+        if (e == 0 || key_col(key[e]) != key_col(key[e - 1])) {
+          if (MODE == 1) {
+            Ccrd[o0 + rank] = key_col(key[e]);
+          } else {
+            V s = val[e];
+            for (int f = e + 1; f < P && key_col(key[f]) == key_col(key[e]); f++) s = add_rn(s, val[f]);
+            Cvals[o0 + rank] = s;
+          }
+          rank++;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---- bin 4: P > 4096, one CTA per row, dense accumulator in global scratch -----------------
+//
+// Per CTA slot: a column bitmap (K bits) and, for values, a stamp (int32 per column, the row
+// that last touched it) and an accumulator (V per column).  A's row is walked in order; the
+// threads split each B row, whose columns are distinct, so every column's products are added
+// in A-row order without atomics.  The pattern is read back by scanning the bitmap words in
+// column order, which yields sorted columns directly.
+
+template <int MODE, typename V>
+__global__ void __launch_bounds__(256)
+spgemm_bin4(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
+            const V* __restrict__ Avals, const int32_t* __restrict__ Bpos,
+            const int32_t* __restrict__ Bcrd, const V* __restrict__ Bvals,
+            const int32_t* __restrict__ rows, const int32_t* __restrict__ count, int32_t K,
+            uint32_t* __restrict__ bitmap_all, int32_t* __restrict__ stamp_all,
+            V* __restrict__ acc_all, const int32_t* __restrict__ Cpos,
+            int32_t* __restrict__ cnt, int32_t* __restrict__ Ccrd, V* __restrict__ Cvals) {
+  const int nr = *count;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int words = (K + 31) >> 5;
+  uint32_t* bitmap = bitmap_all + (int64_t)blockIdx.x * words;
+  int32_t* stamp = stamp_all + (int64_t)blockIdx.x * K;
+  V* acc = acc_all + (int64_t)blockIdx.x * K;
+  __shared__ int32_t s_wcount[8];
+  __shared__ int32_t s_base;
+  for (int w = blockIdx.x; w < nr; w += gridDim.x) {
+    const int row = rows[w];
+    for (int32_t q = __ldg(Apos + row); q < __ldg(Apos + row + 1); q++) {
+      const int32_t j = __ldg(Acrd + q);
+      const int32_t b0 = __ldg(Bpos + j), b1 = __ldg(Bpos + j + 1);
+      V a = V();
+      if (MODE == 2) a = Avals[q];
+      for (int32_t u = b0 + tid; u < b1; u += 256) {
+        const int32_t k = __ldg(Bcrd + u);
+        if (MODE == 2) {
+          const V pr = mul_rn(a, Bvals[u]);
+          if (stamp[k] != row) {
+            stamp[k] = row;
+            acc[k] = pr;
+          } else {
+            acc[k] = add_rn(acc[k], pr);
+          }
+        } else {
+          atomicOr(bitmap + (k >> 5), 1u << (k & 31));
+        }
+      }
+      __syncthreads();  // B rows of later A nonzeros may hit the same columns
+    }
+    if (MODE == 2) {
+      // the pattern is known: gather accumulated values in column order
+      for (int32_t t = Cpos[row] + tid; t < Cpos[row + 1]; t += 256) Cvals[t] = acc[Ccrd[t]];
+      __syncthreads();
+      continue;
+    }
+    // scan the bitmap in column order (chunks of 256 words)
+    if (tid == 0) s_base = 0;
+    __syncthreads();
+    for (int c = 0; c < words; c += 256) {
+      const int wi = c + tid;
+      const uint32_t bits = wi < words ? bitmap[wi] : 0u;
+      const int pc = __popc(bits);
+      int incl = pc;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += o;
+      }
+      if (lane == 31) s_wcount[warp] = incl;
+      __syncthreads();
+      int wbase = 0, total = 0;
+      for (int x = 0; x < 8; x++) {
+        if (x < warp) wbase += s_wcount[x];
+        total += s_wcount[x];
+      }
+      if (MODE == 1 && bits) {
+        int r = s_base + wbase + incl - pc;
+        const int o0 = Cpos[row];
+        uint32_t bb = bits;
+        while (bb) {
+          const int bit = __ffs(bb) - 1;
+          Ccrd[o0 + r++] = (wi << 5) + bit;
+          bb &= bb - 1;
+        }
+      }
+      if (wi < words) bitmap[wi] = 0u;  // leave the slot clean for the next row
+      __syncthreads();
+      if (tid == 0) s_base += total;
+      __syncthreads();
+    }
+    if (MODE == 0 && tid == 0) cnt[row] = s_base;
+    __syncthreads();
+  }
+}
+
+// ---- exclusive scan of row counts into pos (int32, overflow-checked) -----------------------
+
+constexpr int kScanChunk = 4096;
+
+__global__ void scan_block_sums(const int32_t* __restrict__ cnt, int32_t n,
+                                int64_t* __restrict__ sums) {
+  __shared__ int64_t s[256];
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk;
+  int64_t t = 0;
+  for (int e = threadIdx.x; e < kScanChunk; e += 256)
+    if (base + e < n) t += cnt[base + e];
+  s[threadIdx.x] = t;
+  __syncthreads();
+  for (int d = 128; d > 0; d >>= 1) {
+    if (threadIdx.x < d) s[threadIdx.x] += s[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = s[0];
+}
+
+__global__ void scan_sums_exclusive(int64_t* __restrict__ sums, int32_t nblocks,
+                                    int32_t* __restrict__ total_overflow) {
+  if (threadIdx.x != 0) return;
+  int64_t acc = 0;
+  for (int b = 0; b < nblocks; b++) {
+    const int64_t v = sums[b];
+    sums[b] = acc;
+    acc += v;
+  }
+  sums[nblocks] = acc;
+  *total_overflow = acc > INT32_MAX ? 1 : 0;
+}
+
+__global__ void scan_write_pos(const int32_t* __restrict__ cnt, int32_t n,
+                               const int64_t* __restrict__ sums, int32_t* __restrict__ pos) {
+  __shared__ int64_t s_warp[8];
+  const int64_t base = (int64_t)blockIdx.x * kScanChunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int PER = kScanChunk / 256;
+  const int64_t e0 = base + (int64_t)threadIdx.x * PER;
+  int64_t local[PER];
+  int64_t t = 0;
+#pragma unroll
+  for (int e = 0; e < PER; e++) {
+    local[e] = t;
+    t += (e0 + e < n) ? cnt[e0 + e] : 0;
+  }
+  int64_t incl = t;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int64_t o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += o;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  int64_t wb = 0;
+  for (int x = 0; x < warp; x++) wb += s_warp[x];
+  const int64_t off = sums[blockIdx.x] + wb + incl - t;
+#pragma unroll
+  for (int e = 0; e < PER; e++)
+    if (e0 + e < n) pos[e0 + e] = (int32_t)(off + local[e]);
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) pos[n] = (int32_t)sums[gridDim.x];
+}
+
+// ---- host orchestration -------------------------------------------------------------------
+
+struct Plan {
+  int64_t* prod;
+  int32_t* bin_cnt;   // kBins counters
+  int32_t* bin_rows;  // kBins * n
+  int32_t* cnt;       // per-row unique counts (symbolic)
+  int64_t* sums;      // scan block sums
+  int32_t* flag;      // overflow flag
+  int32_t h_cnt[kBins];
+};
+
+// Bins the rows of A*B and reads the bin sizes back (one small synchronising copy).
+int make_plan(const tacogb_csr* A, const tacogb_csr* B, Plan& pl, cudaStream_t st) {
+  const int64_t n = A->rows;
+  const int64_t nblocks = (n + kScanChunk - 1) / kScanChunk;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t off = 0;
+  const size_t o_prod = off; off += al(sizeof(int64_t) * (n + 1));
+  const size_t o_bc = off; off += al(sizeof(int32_t) * kBins);
+  const size_t o_br = off; off += al(sizeof(int32_t) * kBins * (n + 1));
+  const size_t o_cnt = off; off += al(sizeof(int32_t) * (n + 1));
+  const size_t o_sums = off; off += al(sizeof(int64_t) * (nblocks + 2));
+  const size_t o_flag = off; off += al(sizeof(int32_t) * 4);
+  unsigned char* ws = (unsigned char*)scratch(off, 2);
+  if (!ws) return last_code();
+  pl.prod = (int64_t*)(ws + o_prod);
+  pl.bin_cnt = (int32_t*)(ws + o_bc);
+  pl.bin_rows = (int32_t*)(ws + o_br);
+  pl.cnt = (int32_t*)(ws + o_cnt);
+  pl.sums = (int64_t*)(ws + o_sums);
+  pl.flag = (int32_t*)(ws + o_flag);
+  TACOGB_CUDA_TRY(cudaMemsetAsync(pl.bin_cnt, 0, sizeof(int32_t) * kBins, st));
+  TACOGB_CUDA_TRY(cudaMemsetAsync(pl.cnt, 0, sizeof(int32_t) * (n + 1), st));
+  if (n > 0)
+    TACOGB_LAUNCH("spgemm_bin_rows", st,
+                  spgemm_bin_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                      A->pos, A->crd, B->pos, (int32_t)n, pl.prod, pl.bin_cnt, pl.bin_rows));
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(pl.h_cnt, pl.bin_cnt, sizeof(pl.h_cnt), cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return 0;
+}
+
+template <int MODE, typename V>
+int run_bins(const tacogb_csr* A, const tacogb_csr* B, const Plan& pl, const int32_t* Cpos,
+             int32_t* Ccrd, V* Cvals, cudaStream_t st) {
+  const int64_t n = A->rows;
+  const V* Av = (const V*)A->vals;
+  const V* Bv = (const V*)B->vals;
+  const int sms = sm_count();
+  auto rows_of = [&](int b) { return pl.bin_rows + (int64_t)b * n; };
+  auto grid = [](int64_t items, int64_t cap) { return (unsigned)(items < cap ? items : cap); };
+  if (pl.h_cnt[1] > 0)
+    TACOGB_LAUNCH("spgemm_bin1", st,
+                  (spgemm_bin1<MODE, V><<<grid((pl.h_cnt[1] + 7) / 8, sms * 8), 256, 0, st>>>(
+                      A->pos, A->crd, Av, B->pos, B->crd, Bv, rows_of(1), pl.bin_cnt + 1, Cpos,
+                      pl.cnt, Ccrd, Cvals)));
+  if (pl.h_cnt[2] > 0)
+    TACOGB_LAUNCH("spgemm_bin2", st,
+                  (spgemm_bin2<MODE, V><<<grid((pl.h_cnt[2] + 7) / 8, sms * 4), 256, 0, st>>>(
+                      A->pos, A->crd, Av, B->pos, B->crd, Bv, rows_of(2), pl.bin_cnt + 2, pl.prod,
+                      Cpos, pl.cnt, Ccrd, Cvals)));
+  if (pl.h_cnt[3] > 0) {
+    const size_t smem3 = (size_t)kBin3 * (sizeof(uint64_t) + sizeof(V));
+    TACOGB_CUDA_TRY(cudaFuncSetAttribute(spgemm_bin3<MODE, V>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem3));
+    TACOGB_LAUNCH("spgemm_bin3", st,
+                  (spgemm_bin3<MODE, V><<<grid(pl.h_cnt[3], sms * 2), 256, smem3, st>>>(
+                      A->pos, A->crd, Av, B->pos, B->crd, Bv, rows_of(3), pl.bin_cnt + 3, pl.prod,
+                      Cpos, pl.cnt, Ccrd, Cvals)));
+  }
+  if (pl.h_cnt[4] > 0) {
+    // dense per-slot scratch: bitmap for the pattern, stamps + accumulators for values
+    const int64_t K = B->cols;
+    const int slots = (int)(pl.h_cnt[4] < kDenseSlots ? pl.h_cnt[4] : kDenseSlots);
+    const size_t words = (size_t)((K + 31) / 32);
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t bm_bytes = al(sizeof(uint32_t) * words * slots);
+    const size_t st_bytes = MODE == 2 ? al(sizeof(int32_t) * K * slots) : 0;
+    const size_t acc_bytes = MODE == 2 ? al(sizeof(V) * K * slots) : 0;
+    unsigned char* ws = (unsigned char*)scratch(bm_bytes + st_bytes + acc_bytes, 3);
+    if (!ws) return last_code();
+    uint32_t* bitmap = (uint32_t*)ws;
+    int32_t* stamp = (int32_t*)(ws + bm_bytes);
+    V* acc = (V*)(ws + bm_bytes + st_bytes);
+    TACOGB_CUDA_TRY(cudaMemsetAsync(bitmap, 0, bm_bytes, st));
+    if (MODE == 2) TACOGB_CUDA_TRY(cudaMemsetAsync(stamp, 0xFF, st_bytes, st));
+    TACOGB_LAUNCH("spgemm_bin4", st,
+                  (spgemm_bin4<MODE, V><<<slots, 256, 0, st>>>(
+                      A->pos, A->crd, Av, B->pos, B->crd, Bv, rows_of(4), pl.bin_cnt + 4,
+                      (int32_t)K, bitmap, MODE == 2 ? stamp : nullptr, MODE == 2 ? acc : nullptr,
+                      Cpos, pl.cnt, Ccrd, Cvals)));
+  }
+  return 0;
+}
+
+int check_pair(const tacogb_csr* A, const tacogb_csr* B) {
+  TACOGB_CHECK_ARG(A != nullptr && B != nullptr, "SpGEMM: null matrix");
+  TACOGB_CHECK_ARG(A->cols == B->rows, "SpGEMM: A has %d columns, B has %d rows", A->cols,
+                   B->rows);
+  TACOGB_CHECK_ARG(A->rows >= 0 && B->cols >= 0, "SpGEMM: negative size");
+  TACOGB_CHECK_ARG(A->rows == 0 || A->pos != nullptr, "SpGEMM: null A pos");
+  TACOGB_CHECK_ARG(B->rows == 0 || B->pos != nullptr, "SpGEMM: null B pos");
+  TACOGB_CHECK_ARG(A->nnz <= INT32_MAX && B->nnz <= INT32_MAX, "SpGEMM: nnz exceeds int32");
+  return 0;
+}
+
+}  // namespace
+
+int spgemm_symbolic(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int64_t* nnzC,
+                    cudaStream_t st) {
+  if (int rc = check_pair(A, B)) return rc;
+  TACOGB_CHECK_ARG(Cpos != nullptr && nnzC != nullptr, "SpGEMM: null output");
+  const int64_t n = A->rows;
+  if (n == 0) {
+    TACOGB_CUDA_TRY(cudaMemsetAsync(Cpos, 0, sizeof(int32_t), st));
+    TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+    *nnzC = 0;
+    return 0;
+  }
+  Plan pl;
+  if (int rc = make_plan(A, B, pl, st)) return rc;
+  if (int rc = run_bins<0, double>(A, B, pl, nullptr, nullptr, nullptr, st)) return rc;
+  const int64_t nblocks = (n + kScanChunk - 1) / kScanChunk;
+  TACOGB_LAUNCH("spgemm_scan_sums", st,
+                scan_block_sums<<<(unsigned)nblocks, 256, 0, st>>>(pl.cnt, (int32_t)n, pl.sums));
+  TACOGB_LAUNCH("spgemm_scan_top", st,
+                scan_sums_exclusive<<<1, 32, 0, st>>>(pl.sums, (int32_t)nblocks, pl.flag));
+  TACOGB_LAUNCH("spgemm_scan_pos", st,
+                scan_write_pos<<<(unsigned)nblocks, 256, 0, st>>>(pl.cnt, (int32_t)n, pl.sums,
+                                                                  Cpos));
+  int64_t total = 0;
+  int32_t flag = 0;
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(&total, pl.sums + nblocks, sizeof(int64_t),
+                                  cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(&flag, pl.flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (flag) {
+    set_error(TACOGB_ERR_OVERFLOW, "SpGEMM: nnz(C) = %lld exceeds int32 positions",
+              (long long)total);
+    return TACOGB_ERR_OVERFLOW;
+  }
+  *nnzC = total;
+  return 0;
+}
+
+int spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos, int32_t* Ccrd,
+                cudaStream_t st) {
+  if (int rc = check_pair(A, B)) return rc;
+  if (A->rows == 0) return 0;
+  Plan pl;
+  if (int rc = make_plan(A, B, pl, st)) return rc;
+  return run_bins<1, double>(A, B, pl, Cpos, Ccrd, nullptr, st);
+}
+
+int spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
+                   const int32_t* Ccrd, void* Cvals, cudaStream_t st) {
+  if (int rc = check_pair(A, B)) return rc;
+  TACOGB_CHECK_ARG(A->vtype == B->vtype && (A->vtype == TACOGB_F64 || A->vtype == TACOGB_F32),
+                   "SpGEMM: A and B need the same value type (F64 or F32)");
+  if (A->rows == 0) return 0;
+  TACOGB_CHECK_ARG(A->nnz == 0 || A->vals != nullptr, "SpGEMM: null A values");
+  TACOGB_CHECK_ARG(B->nnz == 0 || B->vals != nullptr, "SpGEMM: null B values");
+  Plan pl;
+  if (int rc = make_plan(A, B, pl, st)) return rc;
+  if (A->vtype == TACOGB_F64)
+    return run_bins<2, double>(A, B, pl, Cpos, const_cast<int32_t*>(Ccrd), (double*)Cvals, st);
+  return run_bins<2, float>(A, B, pl, Cpos, const_cast<int32_t*>(Ccrd), (float*)Cvals, st);
+}
+
+}  // namespace tacogb

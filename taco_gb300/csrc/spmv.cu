@@ -51,6 +51,7 @@ struct PolNative64 {
   using Out = double;
   using Acc = double;
   static constexpr bool kChecked = false;
+  static constexpr int kAcc = 1;  // joining accumulators at a row end would cost an FP64 add
   __device__ static Acc zero() { return 0.0; }
   __device__ static bool madd(Acc& acc, Val a, Val x) {
     acc = __fma_rn(a, x, acc);
@@ -69,6 +70,7 @@ struct PolDF64 {
   using Out = double;
   using Acc = DF;
   static constexpr bool kChecked = true;
+  static constexpr int kAcc = 2;  // interleaved accumulators halve the TwoSum dependency chain
   __device__ static Acc zero() { return DF{0.f, 0.f}; }
   __device__ static bool madd(Acc& acc, Val a, Val x) {
     float ah, al, xh, xl;
@@ -98,6 +100,7 @@ struct PolComp32 {
   using Out = float;
   using Acc = DF;
   static constexpr bool kChecked = false;
+  static constexpr int kAcc = 2;
   __device__ static Acc zero() { return DF{0.f, 0.f}; }
   __device__ static bool madd(Acc& acc, Val a, Val x) {
     DF p;
@@ -119,15 +122,17 @@ struct PolComp32 {
 
 // ------------------------------------------------------------------ partition -------------
 
-// Merge coordinate of every tile boundary D = b*2^shift: the (rows ended, nonzeros consumed)
-// point of the merge path over (row ends, nonzeros).  Row i owns the diagonals
-// [pos[i]+i, pos[i+1]+i]; a boundary D inside them sits at (i, D-i).  One thread per row, so
-// the cost is one coalesced read of pos.  part[tiles] = (n, nnz).
+// Merge coordinate of every tile boundary D = b*T: the (rows ended, nonzeros consumed) point of
+// the merge path over (row ends, nonzeros).  Row i owns the diagonals [pos[i]+i, pos[i+1]+i]; a
+// boundary D inside them sits at (i, D-i).  One thread per row, so the cost is one coalesced
+// read of pos.  part[tiles] = (n, nnz).  Diagonals stay below 2^32 (n and nnz are int32), so
+// the division is 32-bit.
 // With snap_len > 0 a boundary inside a row shorter than snap_len moves to that row's end
 // (i+1, pos[i+1]), so that only rows of snap_len or more nonzeros are split between tiles;
-// snap_len < tile size keeps every short row within one boundary, so coordinates stay monotone.
+// snap_len < T keeps every short row within one boundary, so coordinates stay monotone.
+// Boundary 0 never moves: the first tile starts at (0, 0).
 __global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t n,
-                                        int64_t nnz, int shift, int32_t tiles,
+                                        int64_t nnz, uint32_t T, int32_t tiles,
                                         int32_t snap_len, int2* __restrict__ part) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i > n) return;
@@ -136,28 +141,31 @@ __global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t
     return;
   }
   const int32_t p0 = __ldg(pos + i), p1 = __ldg(pos + i + 1);
-  const int64_t lo = (int64_t)p0 + i;
-  const int64_t hi = (int64_t)p1 + i;
+  const uint32_t lo = (uint32_t)p0 + (uint32_t)i;
+  const uint32_t hi = (uint32_t)p1 + (uint32_t)i;
   const bool snap = (p1 - p0) < snap_len;
-  for (int64_t b = (lo + (1ll << shift) - 1) >> shift; (b << shift) <= hi && b < tiles; b++)
-    part[b] = snap ? make_int2((int)i + 1, p1) : make_int2((int)i, (int)((b << shift) - i));
+  for (uint32_t b = lo / T + (lo % T != 0); (uint64_t)b * T <= hi && (int32_t)b < tiles; b++)
+    part[b] = (snap && b > 0) ? make_int2((int)i + 1, p1)
+                              : make_int2((int)i, (int)((uint64_t)b * T - (uint64_t)i));
 }
 
 int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_items,
                     int32_t tiles, int2* part, cudaStream_t st, int32_t snap_len) {
-  int shift = 0;
-  while ((1ll << shift) < tile_items) shift++;
-  TACOGB_CHECK_ARG((1ll << shift) == tile_items, "merge tiles must be a power of two");
+  TACOGB_CHECK_ARG(tile_items > 0 && tile_items < (1ll << 30), "bad merge tile size");
   const int64_t threads = (int64_t)n + 1;
   TACOGB_LAUNCH("merge_partition_scatter", st,
                 merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                    pos, n, nnz, shift, tiles, snap_len, part));
+                    pos, n, nnz, (uint32_t)tile_items, tiles, snap_len, part));
   return 0;
 }
 
 // ------------------------------------------------------------------ wmerge ----------------
 
-constexpr int kWmBlock = 256;
+// 128-thread CTAs with a small shared-memory footprint, so that many tiles are in flight per
+// SM and the hardware overlaps one tile's staging with another's arithmetic.  IPT is odd: a
+// lane's items start about IPT elements after its neighbour's, and an odd stride spreads the
+// lanes' shared-memory reads over all banks.
+constexpr int kWmBlock = 128;
 constexpr int kWmWarps = kWmBlock / 32;
 
 template <class P, int IPT>
@@ -277,9 +285,30 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
   const int cnt = ke - ks;
 
   bool ok = true;
-  Acc acc = P::zero(), first = P::zero();
+  constexpr int NA = P::kAcc;
+  Acc acc[NA], first = P::zero();
+#pragma unroll
+  for (int a = 0; a < NA; a++) acc[a] = P::zero();
   int first_row = -1;
-  constexpr int CH = 8;
+  // Joins the interleaved accumulators into acc[0] (a row's complete partial sum).
+  auto join = [&]() {
+#pragma unroll
+    for (int a = 1; a < NA; a++) {
+      acc[0] = P::add(acc[0], acc[a]);
+      acc[a] = P::zero();
+    }
+  };
+  auto emit = [&](int r) {
+    join();
+    if (first_row < 0) {
+      first_row = r;
+      first = acc[0];
+    } else {
+      as_acc<Acc>(s.y[r]) = acc[0];
+    }
+    acc[0] = P::zero();
+  };
+  constexpr int CH = 4;
   for (int c = 0; c < ipt; c += CH) {
     Val xv[CH], vv[CH];
 #pragma unroll
@@ -291,34 +320,18 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
     }
 #pragma unroll
     for (int j = 0; j < CH; j++) {
-      while (row < row_e && sre[row] <= k0 + ks + c + j) {
-        if (first_row < 0) {
-          first_row = row;
-          first = acc;
-        } else {
-          as_acc<Acc>(s.y[row]) = acc;
-        }
-        acc = P::zero();
-        row++;
-      }
-      if (c + j < cnt) ok &= P::madd(acc, vv[j], xv[j]);
+      while (row < row_e && sre[row] <= k0 + ks + c + j) emit(row++);
+      if (c + j < cnt) ok &= P::madd(acc[j % NA], vv[j], xv[j]);
     }
   }
-  while (row < row_e) {
-    if (first_row < 0) {
-      first_row = row;
-      first = acc;
-    } else {
-      as_acc<Acc>(s.y[row]) = acc;
-    }
-    acc = P::zero();
-    row++;
-  }
+  while (row < row_e) emit(row++);
+  join();
+  Acc accv = acc[0];
 
   // Segmented inclusive scan of lane carries keyed by the open row (keys are non-decreasing
   // along the lanes, so equal keys are contiguous).
   const int key = row_e;
-  Acc sc = acc;
+  Acc sc = accv;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const Acc o = P::shfl_up(sc, d);
@@ -359,7 +372,7 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
 }
 
 template <class P, int IPT, bool TMA>
-__global__ void __launch_bounds__(kWmBlock, 2)
+__global__ void __launch_bounds__(kWmBlock, 8)
 spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                    const typename P::Val* __restrict__ vals, const typename P::Val* __restrict__ x,
                    typename P::Out* __restrict__ y, const int2* __restrict__ part, int32_t n,
@@ -463,8 +476,8 @@ struct SpmvVariant {
 };
 
 const SpmvVariant kSpmvVariants[] = {
-    {"wmerge_ipt8", 0, 8},      {"wmerge_ipt16", 0, 16}, {"wmerge_df_ipt8", 1, 8},
-    {"wmerge_df_ipt16", 1, 16}, {"vector_g1", 2, 1},     {"vector_g2", 2, 2},
+    {"wmerge_ipt7", 0, 7},      {"wmerge_ipt11", 0, 11}, {"wmerge_df_ipt7", 1, 7},
+    {"wmerge_df_ipt11", 1, 11}, {"vector_g1", 2, 1},     {"vector_g2", 2, 2},
     {"vector_g4", 2, 4},        {"vector_g8", 2, 8},     {"vector_g16", 2, 16},
     {"vector_g32", 2, 32},
 };
@@ -527,12 +540,12 @@ int spmv_typed(const tacogb_csr* A, const V* x, V* y, int variant, cudaStream_t 
   using Native = typename std::conditional<sizeof(V) == 8, PolNative64, PolComp32>::type;
   using Dbl = typename std::conditional<sizeof(V) == 8, PolDF64, PolComp32>::type;
   if (v.family == 0) {
-    if (v.param == 8) return launch_wmerge<Native, 8>(A, x, y, st);
-    return launch_wmerge<Native, 16>(A, x, y, st);
+    if (v.param == 7) return launch_wmerge<Native, 7>(A, x, y, st);
+    return launch_wmerge<Native, 11>(A, x, y, st);
   }
   if (v.family == 1) {
-    if (v.param == 8) return launch_wmerge<Dbl, 8>(A, x, y, st);
-    return launch_wmerge<Dbl, 16>(A, x, y, st);
+    if (v.param == 7) return launch_wmerge<Dbl, 7>(A, x, y, st);
+    return launch_wmerge<Dbl, 11>(A, x, y, st);
   }
   switch (v.param) {
     case 1: return launch_vector<V, 1>(A, x, y, st);

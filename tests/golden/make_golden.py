@@ -72,6 +72,28 @@ def spmm_cases():
     save("spmm_powerlaw_n64", pos=pos, crd=crd, vals=vals, B=B, C=H.ref_spmm(pos, crd, vals, B))
 
 
+def spgemm_cases():
+    # taco's spgemm test inputs (test/tests-scheduling-eval.cpp:602-662): 100x100 A and B at
+    # sparsity 0.03 from srand(75883), CSR x CSR
+    (ap, ac, av, _), (bp, bc, bv, _) = H.taco_rand_csr(100, 100, 0.03, dense_b_cols=100,
+                                                         b_sparse=True)
+    cp, cc, cv = H.ref_spgemm((ap, ac, av, 100), (bp, bc, bv, 100))
+    save("spgemm_taco_rand", Apos=ap, Acrd=ac, Avals=av, Bpos=bp, Bcrd=bc, Bvals=bv,
+         Cpos=cp, Ccrd=cc, Cvals=cv, K=np.array([100]))
+
+    s = W.spgemm_random(rows=512)
+    ap, ac, av = W.generate(s)
+    cp, cc, cv = H.ref_spgemm((ap, ac, av, s.cols), (ap, ac, av, s.cols))
+    save("spgemm_random_512", Apos=ap, Acrd=ac, Avals=av, Bpos=ap, Bcrd=ac, Bvals=av,
+         Cpos=cp, Ccrd=cc, Cvals=cv, K=np.array([s.cols]))
+
+    s = W.spgemm_poisson(grid=32)
+    ap, ac, av = W.generate(s)
+    cp, cc, cv = H.ref_spgemm((ap, ac, av, s.cols), (ap, ac, av, s.cols))
+    save("spgemm_poisson_32", Apos=ap, Acrd=ac, Avals=av, Bpos=ap, Bcrd=ac, Bvals=av,
+         Cpos=cp, Ccrd=cc, Cvals=cv, K=np.array([s.cols]))
+
+
 if __name__ == "__main__":
     B.build()
     O.build()
@@ -79,3 +101,5 @@ if __name__ == "__main__":
     spmv_cases()
     assert O.ref_available("spmm")
     spmm_cases()
+    assert O.ref_available("spgemm")
+    spgemm_cases()

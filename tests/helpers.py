@@ -81,3 +81,25 @@ def ref_spmm(pos, crd, vals, B, threads=1):
     At, Bt, Ct = T.csr(pos, crd, vals, [rows, cols]), T.dense(B, [cols, N]), T.dense(C, [rows, N])
     assert L.compute(Ct.ptr, At.ptr, Bt.ptr) == 0
     return C
+
+
+def ref_spgemm(A, B, threads=1):
+    """taco's generated SpGEMM (assemble then compute) on host CSR arrays; A, B = (pos, crd,
+    vals, cols).  Returns (pos, crd, vals) of C copied out of the arrays taco allocated."""
+    import ctypes
+    L = O.ref_lib("spgemm")
+    O.ref_set_threads(threads)
+    (ap, ac, av, acols), (bp, bc, bv, bcols) = A, B
+    rows = len(ap) - 1
+    At, Bt = T.csr(ap, ac, av, [rows, acols]), T.csr(bp, bc, bv, [acols, bcols])
+    Ct = T.csr_result([rows, bcols])
+    assert L.assemble(Ct.ptr, At.ptr, Bt.ptr) == 0
+    assert L.compute(Ct.ptr, At.ptr, Bt.ptr) == 0
+    pos = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 0), ctypes.POINTER(ctypes.c_int32)),
+                                (rows + 1,)).copy()
+    nnz = int(pos[-1])
+    crd = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 1), ctypes.POINTER(ctypes.c_int32)),
+                                (max(nnz, 1),))[:nnz].copy()
+    vals = np.ctypeslib.as_array(ctypes.cast(Ct.vals_ptr, ctypes.POINTER(ctypes.c_double)),
+                                 (max(nnz, 1),))[:nnz].copy()
+    return pos, crd, vals

@@ -1,0 +1,172 @@
+"""Two-phase SpGEMM parity on the GPU.
+
+Bars: C's pos and crd bit-exact against taco's generated code (golden fixtures) and the oracle;
+values bit-exact too, because the GPU sums each column's products in taco's A-row order with
+separately rounded multiplies and adds (the golden values were produced by taco's generated C
+compiled without FMA contraction).  The normwise 1e-12 bar is asserted as well.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import taco_gb300 as tg  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from taco_gb300 import taco as T  # noqa: E402
+from taco_gb300 import workloads as W  # noqa: E402
+from tests.helpers import normwise  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _csr(pos, crd, vals, cols, dtype=torch.float64):
+    return tg.CsrMatrix.from_numpy(pos, crd, vals, cols, dtype=dtype)
+
+
+def gpu_spgemm(A, B, dtype=torch.float64):
+    """(pos, crd, vals) of A*B through tacogb_spgemm_symbolic/fill/numeric."""
+    (ap, ac, av, acols), (bp, bc, bv, bcols) = A, B
+    Ad, Bd = _csr(ap, ac, av, acols, dtype), _csr(bp, bc, bv, bcols, dtype)
+    a, b = Ad.as_csr(), Bd.as_csr()
+    L = tg.lib()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    Cpos = torch.empty(len(ap), dtype=torch.int32, device="cuda")
+    nnz = ctypes.c_int64(0)
+    tg.check(L.tacogb_spgemm_symbolic(ctypes.byref(a), ctypes.byref(b), Cpos.data_ptr(),
+                                      ctypes.byref(nnz), sp), "symbolic")
+    Ccrd = torch.empty(max(nnz.value, 1), dtype=torch.int32, device="cuda")
+    Cvals = torch.empty(max(nnz.value, 1), dtype=dtype, device="cuda")
+    tg.check(L.tacogb_spgemm_fill(ctypes.byref(a), ctypes.byref(b), Cpos.data_ptr(),
+                                  Ccrd.data_ptr(), sp), "fill")
+    tg.check(L.tacogb_spgemm_numeric(ctypes.byref(a), ctypes.byref(b), Cpos.data_ptr(),
+                                     Ccrd.data_ptr(), Cvals.data_ptr(), sp), "numeric")
+    torch.cuda.synchronize()
+    n = nnz.value
+    return (Cpos.cpu().numpy(), Ccrd[:n].cpu().numpy(), Cvals[:n].double().cpu().numpy())
+
+
+@pytest.mark.parametrize("case", ["spgemm_taco_rand", "spgemm_random_512", "spgemm_poisson_32"])
+def test_golden(case):
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    K = int(g["K"][0])
+    A = (g["Apos"], g["Acrd"], g["Avals"], len(g["Bpos"]) - 1)
+    B = (g["Bpos"], g["Bcrd"], g["Bvals"], K)
+    cp, cc, cv = gpu_spgemm(A, B)
+    assert np.array_equal(cp, g["Cpos"])
+    assert np.array_equal(cc, g["Ccrd"])
+    assert normwise(cv, g["Cvals"]) <= 1e-12
+    assert np.array_equal(cv, g["Cvals"])
+
+
+def _bins_matrix():
+    """Rows whose product counts fall in every bin: 0, <=32, <=256, <=4096, >4096."""
+    rng = np.random.default_rng(11)
+    n, K = 3000, 20000
+    # B: mostly short rows, a few long ones
+    blens = rng.integers(0, 6, n)
+    blens[:10] = 2500
+    bpos = np.concatenate([[0], np.cumsum(blens)]).astype(np.int32)
+    bcrd = np.concatenate([np.sort(rng.choice(K, l, replace=False)) for l in blens]).astype(np.int32)
+    bvals = rng.uniform(-1, 1, len(bcrd))
+    alens = rng.integers(0, 12, n)
+    alens[100:110] = 0
+    arows = []
+    for i, l in enumerate(alens):
+        if i in (7, 8):          # > 4096 products: several long B rows
+            arows.append(np.array([0, 1, 2, 3, 50, 60], dtype=np.int64))
+        elif i in (20, 21, 22):  # 2500 < P <= 4096
+            arows.append(np.array([4, 70, 80], dtype=np.int64))
+        else:
+            arows.append(np.sort(rng.choice(np.arange(10, n), l, replace=False)))
+    apos = np.concatenate([[0], np.cumsum([len(r) for r in arows])]).astype(np.int32)
+    acrd = np.concatenate(arows).astype(np.int32)
+    avals = rng.uniform(-1, 1, len(acrd))
+    return (apos, acrd, avals, n), (bpos, bcrd, bvals, K)
+
+
+def test_all_bins_against_oracle():
+    A, B = _bins_matrix()
+    ref = O.spgemm(A[0], A[1], A[2], B[0], B[1], B[2], B[3])
+    cp, cc, cv = gpu_spgemm(A, B)
+    assert np.array_equal(cp, ref[0]) and np.array_equal(cc, ref[1])
+    assert np.array_equal(cv, ref[2])
+
+
+def test_all_bins_float32():
+    A, B = _bins_matrix()
+    ref = O.spgemm(A[0], A[1], A[2], B[0], B[1], B[2], B[3])
+    cp, cc, cv = gpu_spgemm(A, B, torch.float32)
+    assert np.array_equal(cp, ref[0]) and np.array_equal(cc, ref[1])
+    assert normwise(cv, ref[2]) <= 1e-6
+
+
+@pytest.mark.parametrize("which", ["random", "poisson"])
+def test_full_size(which):
+    """262,144^2 with 8 uniform nonzeros per row, and the 512x512 Poisson stencil squared."""
+    s = W.spgemm_random() if which == "random" else W.spgemm_poisson()
+    p, c, v = W.generate(s)
+    A = (p, c, v, s.cols)
+    ref = O.spgemm(p, c, v, p, c, v, s.cols)
+    cp, cc, cv = gpu_spgemm(A, A)
+    assert np.array_equal(cp, ref[0]) and np.array_equal(cc, ref[1])
+    assert np.array_equal(cv, ref[2])
+    if which == "poisson":
+        assert cp[-1] == 3397636
+
+
+def test_empty_and_degenerate():
+    A = (np.zeros(5, np.int32), np.zeros(0, np.int32), np.zeros(0), 7)
+    B = (np.zeros(8, np.int32), np.zeros(0, np.int32), np.zeros(0), 3)
+    cp, cc, cv = gpu_spgemm(A, B)
+    assert list(cp) == [0] * 5 and len(cc) == 0
+
+
+def test_abi_assemble_compute_host_and_device():
+    g = np.load(os.path.join(GOLDEN, "spgemm_poisson_32.npz"))
+    n = len(g["Apos"]) - 1
+    for where in ("host", "device"):
+        arrs = {k: g[k] for k in ("Apos", "Acrd", "Avals")}
+        if where == "device":
+            arrs = {k: torch.from_numpy(v).cuda() for k, v in arrs.items()}
+        At = T.csr(arrs["Apos"], arrs["Acrd"], arrs["Avals"], [n, n])
+        Ct = T.csr_result([n, n])
+        assert tg.lib().tacogb_spgemm_assemble(Ct.ptr, At.ptr, At.ptr) == 0
+        assert tg.lib().tacogb_spgemm_compute(Ct.ptr, At.ptr, At.ptr) == 0
+        if where == "device":
+            torch.cuda.synchronize()  # managed results are host-readable after a sync
+        nnz = int(g["Cpos"][-1])
+        pos = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 0), ctypes.POINTER(ctypes.c_int32)), (n + 1,))
+        crd = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 1), ctypes.POINTER(ctypes.c_int32)), (nnz,))
+        vals = np.ctypeslib.as_array(ctypes.cast(Ct.vals_ptr, ctypes.POINTER(ctypes.c_double)), (nnz,))
+        assert np.array_equal(pos, g["Cpos"]) and np.array_equal(crd, g["Ccrd"])
+        assert np.array_equal(vals, g["Cvals"])
+
+
+def test_abi_matmul_kat_through_dropin_module():
+    """d33a * d33b (test/tests-expr_storage.cpp:996-1035) in CSR through libtacogb_spgemm.so's
+    _shim_evaluate: structural entries of row 2 are {0: 30, 1: 180}."""
+    L = ctypes.CDLL(os.path.join(os.path.dirname(tg.__file__), "lib", "libtacogb_spgemm.so"))
+    L._shim_evaluate.argtypes = [ctypes.c_void_p]
+    At = T.csr(np.array([0, 1, 1, 3], np.int32), np.array([1, 0, 2], np.int32),
+               np.array([2.0, 3.0, 4.0]), [3, 3])
+    Bt = T.csr(np.array([0, 2, 2, 3], np.int32), np.array([0, 1, 1], np.int32),
+               np.array([10.0, 20.0, 30.0]), [3, 3])
+    Ct = T.csr_result([3, 3])
+    args = (ctypes.c_void_p * 3)(Ct.ptr, At.ptr, Bt.ptr)
+    assert L._shim_evaluate(args) == 0
+    pos = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 0), ctypes.POINTER(ctypes.c_int32)), (4,))
+    crd = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 1), ctypes.POINTER(ctypes.c_int32)), (2,))
+    vals = np.ctypeslib.as_array(ctypes.cast(Ct.vals_ptr, ctypes.POINTER(ctypes.c_double)), (2,))
+    assert list(pos) == [0, 0, 0, 2] and list(crd) == [0, 1] and list(vals) == [30.0, 180.0]
+
+
+def test_abi_rejects_shape_mismatch():
+    At = T.csr(np.array([0, 1], np.int32), np.array([0], np.int32), np.array([1.0]), [1, 4])
+    Bt = T.csr(np.array([0, 0, 0], np.int32), np.zeros(0, np.int32), np.zeros(0), [2, 2])
+    Ct = T.csr_result([1, 2])
+    assert tg.lib().tacogb_spgemm_assemble(Ct.ptr, At.ptr, Bt.ptr) == 1
+    assert b"columns" in tg.lib().tacogb_last_error()
