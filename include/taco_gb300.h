@@ -93,6 +93,20 @@ int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, vo
 int tacogb_spmv_variant_count(void);
 const char* tacogb_spmv_variant_name(int32_t variant);
 
+/* y = A x like tacogb_spmv (merge-path kernel, default accumulation per value type), for
+ * callers that cannot allocate GPU memory during the call: code running under another
+ * framework's memory pool or allocator hooks, latency-critical paths where cudaMalloc/cudaFree
+ * may synchronise the device, and deployments with a fixed memory budget.  No counterpart in
+ * taco (taco's generated kernels allocate their outputs and never need scratch).
+ * It calls no cudaMalloc, cudaFree or other allocating routine: its temporary memory is a
+ * 4 MiB static device array that every GPU loading this library holds until the process exits,
+ * which bounds the problem to about 2.9e8 rows + nonzeros; larger problems are rejected with
+ * TACOGB_ERR_ARG and a message (use tacogb_spmv).  The first call on each device looks the
+ * array's address up (cudaGetSymbolAddress) and caches it, so make that first call before any
+ * stream capture.  All calls share the one array: calls that overlap on the GPU (different
+ * streams, or graphs replayed concurrently) race and must be serialised by the caller. */
+int tacogb_spmv_noalloc(const tacogb_csr* A, const void* x, void* y, void* stream);
+
 /* C = A B with B (rows = A->cols) x N and C (A->rows x N) dense row-major.
  * Types: A F64 with B F64 -> C FP64; A F32 with B F32 -> C FP32; A F32 with B BF16 -> C FP32
  * (BF16 dense operand, FP32 accumulation).  Replaces the generated compute of

@@ -67,6 +67,11 @@ void prof_before(const char* name, cudaStream_t st) {
   g_prof.push_back(r);
 }
 
+void count_launch() {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_launches++;
+}
+
 void prof_after(cudaStream_t st) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   if (!g_prof_on || g_prof.empty()) return;

@@ -48,6 +48,8 @@ inline int launch_check(const char* what) {
 // on its own stream so that per-kernel device time is measured where the kernel runs.
 void prof_before(const char* name, cudaStream_t st);
 void prof_after(cudaStream_t st);
+// Counts a launch without touching the profiling events (for paths that must not allocate).
+void count_launch();
 
 #define TACOGB_LAUNCH(name, st, ...)                                                    \
   do {                                                                                  \

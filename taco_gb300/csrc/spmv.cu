@@ -35,6 +35,7 @@
 //          regular rows in FP32; its log2(G) FP64 adds per row cost full warp instructions.
 
 #include <cstdio>
+#include <mutex>
 #include <type_traits>
 
 #include "common.cuh"
@@ -590,4 +591,126 @@ int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStrea
   return TACOGB_ERR_ARG;
 }
 
+// ------------------------------------------------------------ allocation-free SpMV --------
+//
+// Some callers cannot call cudaMalloc when they multiply: code that runs inside another
+// framework's memory pool or allocator hooks (where a foreign allocation breaks its accounting),
+// latency-critical or real-time paths (cudaMalloc and cudaFree can synchronise the device), and
+// deployments that fix their GPU memory budget up front.  For them, tacogb_spmv_noalloc runs the
+// merge-path SpMV with its temporary global memory (the tile partition and the tile carry-outs)
+// in a file-scope device array of kNoAllocScratchBytes, reserved on every GPU that loads this
+// library for as long as the process lives, instead of the library's grow-on-demand arena.
+
+namespace {
+constexpr size_t kNoAllocScratchBytes = (size_t)4 << 20;  // 4 MiB: ~2.9e8 merge items (rows + nnz)
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_spmv_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_base[64];  // device address of g_spmv_noalloc_scratch, per device
+
+// Device address of the static scratch on the current device.  In host code the array's name
+// is only a host-side stand-in, so the address is looked up once per device, with that device
+// current, and cached.
+int noalloc_base(void** out) {
+  int dev = 0;
+  TACOGB_CUDA_TRY(cudaGetDevice(&dev));
+  TACOGB_CHECK_ARG(dev >= 0 && dev < 64, "SpMV (no-alloc): device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_spmv_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      set_error(TACOGB_ERR_CUDA, "SpMV (no-alloc): cudaGetSymbolAddress failed: %s",
+                cudaGetErrorString(e));
+      return TACOGB_ERR_CUDA;
+    }
+    g_noalloc_base[dev] = p;
+  }
+  *out = g_noalloc_base[dev];
+  return 0;
+}
+
+constexpr int kNoAllocIpt = 11;
+constexpr int64_t kNoAllocTileItems = (int64_t)kWmBlock * kNoAllocIpt;
+
+// Bytes of scratch a call needs: tile partition, carry rows, carry values.
+struct NoAllocLayout {
+  int64_t tiles;
+  size_t part_bytes, crow_bytes, need;
+};
+
+NoAllocLayout noalloc_layout(const tacogb_csr* A) {
+  NoAllocLayout l;
+  l.tiles = ((int64_t)A->rows + A->nnz + kNoAllocTileItems - 1) / kNoAllocTileItems;
+  l.part_bytes = (((size_t)l.tiles + 1) * sizeof(int2) + 255) & ~(size_t)255;
+  l.crow_bytes = ((size_t)l.tiles * sizeof(int32_t) + 255) & ~(size_t)255;
+  l.need = l.part_bytes + l.crow_bytes + (size_t)l.tiles * sizeof(double);
+  return l;
+}
+
+template <class P>
+int launch_wmerge_noalloc(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
+                          const NoAllocLayout& l, cudaStream_t st) {
+  using S = WmSmem<P, kNoAllocIpt>;
+  static_assert(S::ITEMS == kNoAllocTileItems, "tile size");
+  if (l.tiles == 0) return 0;
+  void* base = nullptr;
+  if (int rc = noalloc_base(&base)) return rc;
+  const int32_t tiles = (int32_t)l.tiles;
+  unsigned char* ws = (unsigned char*)base;
+  int2* part = (int2*)ws;
+  int32_t* crow = (int32_t*)(ws + l.part_bytes);
+  double* cval = (double*)(ws + l.part_bytes + l.crow_bytes);
+  // Every entry of part, crow and cval is written before it is read, so the contents left by
+  // an earlier call need no clearing.
+  const int64_t threads = (int64_t)A->rows + 1;
+  count_launch();
+  merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+      A->pos, A->rows, A->nnz, (uint32_t)kNoAllocTileItems, tiles, 0, part);
+  if (int rc = launch_check("merge_partition_scatter")) return rc;
+  auto kern = spmv_wmerge_kernel<P, kNoAllocIpt, false>;
+  TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sizeof(S)));
+  count_launch();
+  kern<<<tiles, kWmBlock, sizeof(S), st>>>(A->pos, A->crd, (const typename P::Val*)A->vals, x, y,
+                                          part, A->rows, (int32_t)A->nnz, crow, cval, nullptr);
+  if (int rc = launch_check("spmv_wmerge_kernel")) return rc;
+  count_launch();
+  spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(crow, cval, tiles, y,
+                                                                          A->rows);
+  return launch_check("spmv_carry_fixup");
+}
+
+}  // namespace
+
 }  // namespace tacogb
+
+extern "C" int tacogb_spmv_noalloc(const tacogb_csr* A, const void* x, void* y, void* stream) {
+  using namespace tacogb;
+  TACOGB_CHECK_ARG(A != nullptr, "SpMV (no-alloc): null matrix");
+  TACOGB_CHECK_ARG(A->rows >= 0 && A->cols >= 0 && A->nnz >= 0, "SpMV (no-alloc): negative size");
+  TACOGB_CHECK_ARG(A->nnz <= INT32_MAX, "SpMV (no-alloc): nnz exceeds int32 positions");
+  const NoAllocLayout l = noalloc_layout(A);
+  if (l.need > kNoAllocScratchBytes) {
+    set_error(TACOGB_ERR_ARG,
+              "SpMV (no-alloc): %lld rows + %lld nonzeros need %zu bytes of scratch but the "
+              "static scratch holds %zu (about %lld rows + nonzeros at most); use tacogb_spmv",
+              (long long)A->rows, (long long)A->nnz, l.need, kNoAllocScratchBytes,
+              (long long)(kNoAllocScratchBytes / 20 * kNoAllocTileItems));
+    return TACOGB_ERR_ARG;
+  }
+  TACOGB_CHECK_ARG(A->vtype == TACOGB_F64 || A->vtype == TACOGB_F32,
+                   "SpMV (no-alloc): unsupported value type %d", A->vtype);
+  TACOGB_CHECK_ARG(A->rows == 0 || (A->pos != nullptr && y != nullptr),
+                   "SpMV (no-alloc): null pos or y");
+  TACOGB_CHECK_ARG(A->nnz == 0 || (A->crd != nullptr && A->vals != nullptr && x != nullptr),
+                   "SpMV (no-alloc): null crd, vals or x");
+  const cudaStream_t st = (cudaStream_t)stream;
+  if (A->vtype == TACOGB_F64)
+    return launch_wmerge_noalloc<PolDF64>(A, (const double*)x, (double*)y, l, st);
+  return launch_wmerge_noalloc<PolComp32>(A, (const float*)x, (float*)y, l, st);
+}
