@@ -46,18 +46,23 @@ namespace tacogb {
 
 // ------------------------------------------------------------------ policies -------------
 
-// FP64 values, FP64 accumulation.
+// Accumulation policies.  Val is the stored value type; SV/SX are the value and x element as
+// staged in shared memory; XG is the element type of the x array the kernel gathers from.
+
+// FP64 values, FP64 accumulation (DFMA).
 struct PolNative64 {
   using Val = double;
   using Out = double;
   using Acc = double;
+  using SV = double;
+  using SX = double;
+  using XG = double;
   static constexpr bool kChecked = false;
   static constexpr int kAcc = 1;  // joining accumulators at a row end would cost an FP64 add
   __device__ static Acc zero() { return 0.0; }
-  __device__ static bool madd(Acc& acc, Val a, Val x) {
-    acc = __fma_rn(a, x, acc);
-    return true;
-  }
+  __device__ static SV stage_val(Val v, bool&) { return v; }
+  __device__ static SX stage_x(XG x, bool&) { return x; }
+  __device__ static void madd(Acc& acc, SV a, SX x) { acc = __fma_rn(a, x, acc); }
   __device__ static Acc add(Acc a, Acc b) { return __dadd_rn(a, b); }
   __device__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
   __device__ static Acc shfl_xor(Acc a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
@@ -65,25 +70,24 @@ struct PolNative64 {
   __device__ static double to_double(Acc a) { return a; }
 };
 
-// FP64 values, double-float accumulation on the FP32 pipe.
+// FP64 values evaluated in double-float on the FP32 pipe; x arrives pre-split (DF per entry).
 struct PolDF64 {
   using Val = double;
   using Out = double;
   using Acc = DF;
+  using SV = DF;
+  using SX = DF;
+  using XG = DF;
   static constexpr bool kChecked = true;
   static constexpr int kAcc = 2;  // interleaved accumulators halve the TwoSum dependency chain
   __device__ static Acc zero() { return DF{0.f, 0.f}; }
-  __device__ static bool madd(Acc& acc, Val a, Val x) {
-    float ah, al, xh, xl;
-    const bool ok = split_df(a, ah, al) & split_df(x, xh, xl);
-    DF p;
-    p.h = __fmul_rn(ah, xh);
-    const float pe = __fmaf_rn(ah, xh, -p.h);
-    const float pc = __fmaf_rn(ah, xl, __fmul_rn(al, xh));
-    p.l = __fadd_rn(pe, pc);
-    acc = df_add(acc, p);
-    return ok;
+  __device__ static SV stage_val(Val v, bool& ok) {
+    DF d;
+    ok &= split_df(v, d.h, d.l);
+    return d;
   }
+  __device__ static SX stage_x(XG x, bool&) { return x; }
+  __device__ static void madd(Acc& acc, SV a, SX x) { acc = df_add(acc, df_mul(a.h, a.l, x.h, x.l)); }
   __device__ static Acc add(Acc a, Acc b) { return df_add(a, b); }
   __device__ static Acc shfl_up(Acc a, int d) {
     return DF{__shfl_up_sync(0xffffffffu, a.h, d), __shfl_up_sync(0xffffffffu, a.l, d)};
@@ -91,8 +95,8 @@ struct PolDF64 {
   __device__ static Acc shfl_xor(Acc a, int m) {
     return DF{__shfl_xor_sync(0xffffffffu, a.h, m), __shfl_xor_sync(0xffffffffu, a.l, m)};
   }
-  __device__ static Out out(Acc a) { return __dadd_rn((double)a.h, (double)a.l); }
-  __device__ static double to_double(Acc a) { return out(a); }
+  __device__ static Out out(Acc a) { return df_to_double(a); }
+  __device__ static double to_double(Acc a) { return df_to_double(a); }
 };
 
 // FP32 values, TwoProduct/TwoSum-compensated FP32 accumulation.
@@ -100,15 +104,19 @@ struct PolComp32 {
   using Val = float;
   using Out = float;
   using Acc = DF;
+  using SV = float;
+  using SX = float;
+  using XG = float;
   static constexpr bool kChecked = false;
   static constexpr int kAcc = 2;
   __device__ static Acc zero() { return DF{0.f, 0.f}; }
-  __device__ static bool madd(Acc& acc, Val a, Val x) {
+  __device__ static SV stage_val(Val v, bool&) { return v; }
+  __device__ static SX stage_x(XG x, bool&) { return x; }
+  __device__ static void madd(Acc& acc, SV a, SX x) {
     DF p;
     p.h = __fmul_rn(a, x);
     p.l = __fmaf_rn(a, x, -p.h);
     acc = df_add(acc, p);
-    return true;
   }
   __device__ static Acc add(Acc a, Acc b) { return df_add(a, b); }
   __device__ static Acc shfl_up(Acc a, int d) {
@@ -120,6 +128,28 @@ struct PolComp32 {
   __device__ static Out out(Acc a) { return __fadd_rn(a.h, a.l); }
   __device__ static double to_double(Acc a) { return (double)a.h + (double)a.l; }
 };
+
+// Double-float policy that gathers the FP64 x and splits each gathered entry while staging
+// (no pre-split buffer; more integer work per nonzero).
+struct PolDF64X : PolDF64 {
+  using XG = double;
+  __device__ static SX stage_x(XG x, bool& ok) {
+    DF d;
+    ok &= split_df(x, d.h, d.l);
+    return d;
+  }
+};
+
+// x split once per product for the double-float policy; flag set when some entry is outside
+// the double-float range (the product then runs every tile natively).
+__global__ void spmv_split_x(const double* __restrict__ x, DF* __restrict__ xdf, int32_t n,
+                             int* __restrict__ flag) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  DF d;
+  if (!split_df(__ldg(x + i), d.h, d.l)) *flag = 1;
+  xdf[i] = d;
+}
 
 // ------------------------------------------------------------------ partition -------------
 
@@ -174,11 +204,13 @@ struct WmSmem {
   using Val = typename P::Val;
   static constexpr int ITEMS = kWmBlock * IPT;
   static constexpr int VPAD = 16 / sizeof(Val);  // values per 16 bytes
-  // Staged arrays keep room for the 16-byte alignment slack of the bulk copies.
+  // Staged arrays keep room for the 16-byte alignment slack of the bulk copies.  val holds the
+  // raw values as copied, then (in place, same width) the policy's staged form.
   alignas(16) int32_t crd[ITEMS + 8];
   alignas(16) Val val[ITEMS + 2 * VPAD];
   alignas(16) int32_t re[ITEMS + 8];  // global nonzero index of each row end (pos entries)
-  double y[ITEMS];                     // row results (policy accumulator, 8 bytes)
+  alignas(8) double x[ITEMS];         // gathered x (policy's SX, at most 8 bytes)
+  double y[ITEMS];                    // row results (policy accumulator, 8 bytes)
   int32_t wkey[kWmWarps];
   double wval[kWmWarps];  // warp carries (policy accumulator)
   uint64_t bar;
@@ -188,15 +220,15 @@ struct WmSmem {
 // With TMA, one thread issues three bulk copies over the 16-byte-aligned spans inside the
 // arrays and every thread waits on the mbarrier (bounded); the sub-16-byte tails at the array
 // ends are loaded by plain loads.  Without TMA (unaligned base pointers), each thread issues
-// its IPT loads before storing any of them.  Returns the shared-memory base pointers for
+// its IPT loads before storing any of them.  Sets the shared-memory base pointers for
 // tile-local indices.
 template <bool TMA, class P, int IPT>
 __device__ __forceinline__ void wm_stage(WmSmem<P, IPT>& s, const int32_t* __restrict__ pos,
                                          const int32_t* __restrict__ crd,
                                          const typename P::Val* __restrict__ vals, int32_t n,
                                          int32_t nnz, int r0, int rn, int k0, int kn,
-                                         int* status, const int32_t*& scrd,
-                                         const typename P::Val*& sval, const int32_t*& sre) {
+                                         int* status, int32_t*& scrd, typename P::Val*& sval,
+                                         const int32_t*& sre) {
   using Val = typename P::Val;
   using S = WmSmem<P, IPT>;
   const int tid = threadIdx.x;
@@ -250,6 +282,47 @@ __device__ __forceinline__ void wm_stage(WmSmem<P, IPT>& s, const int32_t* __res
   __syncthreads();
 }
 
+template <typename T>
+__device__ __forceinline__ T ldg_xg(const T* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ DF ldg_xg<DF>(const DF* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return DF{v.x, v.y};
+}
+
+// Gathers x for every nonzero of the tile into s.x and converts the staged values to the
+// policy's form, all threads at once with IPT independent gathers each (so no lane waits on a
+// gather inside its walk).  Returns false when a checked policy met an unrepresentable value.
+template <class P, int IPT, class S>
+__device__ __forceinline__ bool wm_gather(S& s, const int32_t* scrd, typename P::Val* sval,
+                                          const typename P::XG* __restrict__ x, int kn) {
+  using XG = typename P::XG;
+  using SV = typename P::SV;
+  using SX = typename P::SX;
+  static_assert(sizeof(SV) == sizeof(typename P::Val), "staged values convert in place");
+  static_assert(sizeof(SX) <= sizeof(double), "staged x fits its slot");
+  const int tid = threadIdx.x;
+  SX* sx = reinterpret_cast<SX*>(s.x);
+  SV* sv = reinterpret_cast<SV*>(sval);
+  bool ok = true;
+  XG g[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    const int i = tid + j * kWmBlock;
+    if (i < kn) g[j] = ldg_xg(x + scrd[i]);
+  }
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    const int i = tid + j * kWmBlock;
+    if (i < kn) {
+      sx[i] = P::stage_x(g[j], ok);
+      sv[i] = P::stage_val(sval[i], ok);
+    }
+  }
+  __syncthreads();
+  return ok;
+}
+
 // Tile-local merge coordinate of diagonal d (rows ended, nonzeros consumed).
 __device__ __forceinline__ void tile_search(const int32_t* s_re, int rn, int kn, int k0, int d,
                                             int& row, int& k) {
@@ -268,39 +341,34 @@ __device__ __forceinline__ A& as_acc(double& slot) {
   return *reinterpret_cast<A*>(&slot);
 }
 
-// Walks this lane's merge items with policy P, joins lanes and warps, and leaves every row
-// result of the tile in s.y; the part of the row still open at the tile end is returned in
-// `carry` (thread 0).  Returns false when a checked policy met a value it cannot represent.
-template <class P, class S>
-__device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typename P::Val* sval,
-                                        const int32_t* sre, const typename P::Val* __restrict__ x,
-                                        int rn, int kn, int k0, int ipt, typename P::Acc& carry) {
+// Walks this lane's IPT merge items over the staged tile with policy P, joins lanes and warps,
+// and leaves every row result of the tile in s.y; the part of the row still open at the tile
+// end is returned in `carry` (thread 0).
+template <class P, int IPT, class S>
+__device__ __forceinline__ void wm_tile(S& s, const typename P::SV* sv, const int32_t* sre,
+                                        int rn, int kn, int k0, typename P::Acc& carry) {
   using Acc = typename P::Acc;
-  using Val = typename P::Val;
+  using SX = typename P::SX;
+  const SX* sx = reinterpret_cast<const SX*>(s.x);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int items = rn + kn;
-  const int ds = min(tid * ipt, items), de = min(ds + ipt, items);
+  const int ds = min(tid * IPT, items), de = min(ds + IPT, items);
   int row, ks, row_e, ke;
   tile_search(sre, rn, kn, k0, ds, row, ks);
   tile_search(sre, rn, kn, k0, de, row_e, ke);
   const int cnt = ke - ks;
 
-  bool ok = true;
   constexpr int NA = P::kAcc;
   Acc acc[NA], first = P::zero();
 #pragma unroll
   for (int a = 0; a < NA; a++) acc[a] = P::zero();
   int first_row = -1;
-  // Joins the interleaved accumulators into acc[0] (a row's complete partial sum).
-  auto join = [&]() {
+  auto emit = [&](int r) {
 #pragma unroll
     for (int a = 1; a < NA; a++) {
       acc[0] = P::add(acc[0], acc[a]);
       acc[a] = P::zero();
     }
-  };
-  auto emit = [&](int r) {
-    join();
     if (first_row < 0) {
       first_row = r;
       first = acc[0];
@@ -309,30 +377,19 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
     }
     acc[0] = P::zero();
   };
-  constexpr int CH = 4;
-  for (int c = 0; c < ipt; c += CH) {
-    Val xv[CH], vv[CH];
 #pragma unroll
-    for (int j = 0; j < CH; j++) {
-      if (c + j < cnt) {
-        vv[j] = sval[ks + c + j];
-        xv[j] = __ldg(x + scrd[ks + c + j]);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < CH; j++) {
-      while (row < row_e && sre[row] <= k0 + ks + c + j) emit(row++);
-      if (c + j < cnt) ok &= P::madd(acc[j % NA], vv[j], xv[j]);
-    }
+  for (int j = 0; j < IPT; j++) {
+    while (row < row_e && sre[row] <= k0 + ks + j) emit(row++);
+    if (j < cnt) P::madd(acc[j % NA], sv[ks + j], sx[ks + j]);
   }
   while (row < row_e) emit(row++);
-  join();
-  Acc accv = acc[0];
+#pragma unroll
+  for (int a = 1; a < NA; a++) acc[0] = P::add(acc[0], acc[a]);
 
   // Segmented inclusive scan of lane carries keyed by the open row (keys are non-decreasing
   // along the lanes, so equal keys are contiguous).
   const int key = row_e;
-  Acc sc = accv;
+  Acc sc = acc[0];
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const Acc o = P::shfl_up(sc, d);
@@ -369,13 +426,17 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
       }
     }
   }
-  return ok;
+  __syncthreads();
 }
 
+// xg: x in the policy's gather form (pre-split for the double-float policy); x64: the original
+// FP64 x for the native fallback (same as xg for unchecked policies); xflag: non-zero when x
+// has entries outside the double-float range.
 template <class P, int IPT, bool TMA>
 __global__ void __launch_bounds__(kWmBlock, 8)
 spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
-                   const typename P::Val* __restrict__ vals, const typename P::Val* __restrict__ x,
+                   const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
+                   const typename P::Val* __restrict__ x64, const int* __restrict__ xflag,
                    typename P::Out* __restrict__ y, const int2* __restrict__ part, int32_t n,
                    int32_t nnz, int32_t* __restrict__ carry_row, double* __restrict__ carry_val,
                    int* status) {
@@ -388,29 +449,33 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   const int r0 = c0.x, k0 = c0.y;
   const int rn = c1.x - c0.x, kn = c1.y - c0.y;
 
-  const int32_t* scrd;
-  const typename P::Val* sval;
+  int32_t* scrd;
+  typename P::Val* sval;
   const int32_t* sre;
   wm_stage<TMA, P, IPT>(s, pos, crd, vals, n, nnz, r0, rn, k0, kn, status, scrd, sval, sre);
 
   double carry_d = 0.0;
   bool native = !P::kChecked;
   if constexpr (P::kChecked) {
-    typename P::Acc carry = P::zero();
-    const bool ok = wm_tile<P>(s, scrd, sval, sre, x, rn, kn, k0, IPT, carry);
+    bool ok = (xflag == nullptr || *xflag == 0);
+    if (__syncthreads_and(ok)) ok = wm_gather<P, IPT>(s, scrd, sval, xg, kn);
     if (__syncthreads_and(ok)) {
+      typename P::Acc carry = P::zero();
+      wm_tile<P, IPT>(s, reinterpret_cast<const typename P::SV*>(sval), sre, rn, kn, k0, carry);
       for (int i = tid; i < rn; i += kWmBlock) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
       carry_d = P::to_double(carry);
     } else {
       native = true;
+      // the staged values were converted in place: restore the raw FP64 values
+      for (int i = tid; i < kn; i += kWmBlock) sval[i] = vals[k0 + i];
+      __syncthreads();
     }
   }
   if (native) {
     using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
+    wm_gather<Q, IPT>(s, scrd, (typename Q::Val*)sval, (const typename Q::XG*)x64, kn);
     typename Q::Acc carry = Q::zero();
-    wm_tile<Q>(s, scrd, (const typename Q::Val*)sval, sre, (const typename Q::Val*)x, rn, kn, k0,
-               IPT, carry);
-    __syncthreads();
+    wm_tile<Q, IPT>(s, reinterpret_cast<const typename Q::SV*>(sval), sre, rn, kn, k0, carry);
     for (int i = tid; i < rn; i += kWmBlock)
       y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
     carry_d = Q::to_double(carry);
@@ -472,15 +537,16 @@ namespace {
 
 struct SpmvVariant {
   const char* name;
-  int family;  // 0 wmerge native, 1 wmerge double-float, 2 vector
+  int family;  // 0 wmerge native, 1 wmerge double-float (x pre-split), 2 vector,
+               // 3 wmerge double-float (x split while staging)
   int param;   // IPT for wmerge, G for vector
 };
 
 const SpmvVariant kSpmvVariants[] = {
-    {"wmerge_ipt7", 0, 7},      {"wmerge_ipt11", 0, 11}, {"wmerge_df_ipt7", 1, 7},
-    {"wmerge_df_ipt11", 1, 11}, {"vector_g1", 2, 1},     {"vector_g2", 2, 2},
-    {"vector_g4", 2, 4},        {"vector_g8", 2, 8},     {"vector_g16", 2, 16},
-    {"vector_g32", 2, 32},
+    {"wmerge_ipt7", 0, 7},       {"wmerge_ipt11", 0, 11},     {"wmerge_df_ipt7", 1, 7},
+    {"wmerge_df_ipt11", 1, 11},  {"vector_g1", 2, 1},         {"vector_g2", 2, 2},
+    {"vector_g4", 2, 4},         {"vector_g8", 2, 8},         {"vector_g16", 2, 16},
+    {"vector_g32", 2, 32},       {"wmerge_dfx_ipt7", 3, 7},   {"wmerge_dfx_ipt11", 3, 11},
 };
 constexpr int kNumSpmvVariants = sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]);
 
@@ -494,17 +560,33 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
   if (tiles64 == 0) return 0;
   TACOGB_CHECK_ARG(tiles64 < (1ll << 31), "SpMV: too many merge tiles");
   const int32_t tiles = (int32_t)tiles64;
-  const size_t part_bytes = (((size_t)tiles + 1) * sizeof(int2) + 255) & ~(size_t)255;
-  const size_t crow_bytes = ((size_t)tiles * sizeof(int32_t) + 255) & ~(size_t)255;
-  const size_t cval_bytes = (size_t)tiles * sizeof(double);
-  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes, 0);
+  // x pre-split into double-float pairs when the policy gathers DF entries
+  constexpr bool presplit = std::is_same<typename P::XG, DF>::value;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
+  const size_t crow_bytes = al((size_t)tiles * sizeof(int32_t));
+  const size_t cval_bytes = al((size_t)tiles * sizeof(double));
+  const size_t xdf_bytes = presplit ? al((size_t)A->cols * sizeof(DF)) + 256 : 0;
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + xdf_bytes, 0);
   if (!ws) return last_code();
   int2* part = (int2*)ws;
   int32_t* crow = (int32_t*)(ws + part_bytes);
   double* cval = (double*)(ws + part_bytes + crow_bytes);
-
   int* status = device_status();
   if (!status) return last_code();
+  const typename P::XG* xg = (const typename P::XG*)x;
+  const int* xflag = nullptr;
+  if constexpr (presplit) {
+    int* flag = (int*)(ws + part_bytes + crow_bytes + cval_bytes);
+    DF* xdf = (DF*)((unsigned char*)flag + 256);
+    TACOGB_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    if (A->cols > 0)
+      TACOGB_LAUNCH("spmv_split_x", st,
+                    spmv_split_x<<<(A->cols + 255) / 256, 256, 0, st>>>((const double*)x, xdf,
+                                                                        A->cols, flag));
+    xg = (const typename P::XG*)xdf;
+    xflag = flag;
+  }
   if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
   // Bulk copies need 16-byte aligned sources: true for every allocator the library meets
   // (cudaMalloc, cudaMallocManaged, torch); sliced pointers take the register-staged kernel.
@@ -514,8 +596,8 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
                                        (int)sizeof(S)));
   TACOGB_LAUNCH("spmv_wmerge_kernel", st,
                 kern<<<tiles, kWmBlock, sizeof(S), st>>>(
-                    A->pos, A->crd, (const typename P::Val*)A->vals, x, y, part, A->rows,
-                    (int32_t)A->nnz, crow, cval, status));
+                    A->pos, A->crd, (const typename P::Val*)A->vals, xg, x, xflag, y, part,
+                    A->rows, (int32_t)A->nnz, crow, cval, status));
   TACOGB_LAUNCH("spmv_carry_fixup", st,
                 spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(
                     crow, cval, tiles, y, A->rows));
@@ -547,6 +629,11 @@ int spmv_typed(const tacogb_csr* A, const V* x, V* y, int variant, cudaStream_t 
   if (v.family == 1) {
     if (v.param == 7) return launch_wmerge<Dbl, 7>(A, x, y, st);
     return launch_wmerge<Dbl, 11>(A, x, y, st);
+  }
+  if (v.family == 3) {
+    using DblX = typename std::conditional<sizeof(V) == 8, PolDF64X, PolComp32>::type;
+    if (v.param == 7) return launch_wmerge<DblX, 7>(A, x, y, st);
+    return launch_wmerge<DblX, 11>(A, x, y, st);
   }
   switch (v.param) {
     case 1: return launch_vector<V, 1>(A, x, y, st);
@@ -676,8 +763,9 @@ int launch_wmerge_noalloc(const tacogb_csr* A, const typename P::Val* x, typenam
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(S)));
   count_launch();
-  kern<<<tiles, kWmBlock, sizeof(S), st>>>(A->pos, A->crd, (const typename P::Val*)A->vals, x, y,
-                                          part, A->rows, (int32_t)A->nnz, crow, cval, nullptr);
+  kern<<<tiles, kWmBlock, sizeof(S), st>>>(A->pos, A->crd, (const typename P::Val*)A->vals,
+                                          (const typename P::XG*)x, x, nullptr, y, part, A->rows,
+                                          (int32_t)A->nnz, crow, cval, nullptr);
   if (int rc = launch_check("spmv_wmerge_kernel")) return rc;
   count_launch();
   spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(crow, cval, tiles, y,
@@ -711,6 +799,6 @@ extern "C" int tacogb_spmv_noalloc(const tacogb_csr* A, const void* x, void* y, 
                    "SpMV (no-alloc): null crd, vals or x");
   const cudaStream_t st = (cudaStream_t)stream;
   if (A->vtype == TACOGB_F64)
-    return launch_wmerge_noalloc<PolDF64>(A, (const double*)x, (double*)y, l, st);
+    return launch_wmerge_noalloc<PolDF64X>(A, (const double*)x, (double*)y, l, st);
   return launch_wmerge_noalloc<PolComp32>(A, (const float*)x, (float*)y, l, st);
 }
