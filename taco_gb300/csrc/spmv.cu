@@ -34,6 +34,7 @@
 //          row with coalesced loads and combine with a shuffle butterfly.  Cheapest for short
 //          regular rows in FP32; its log2(G) FP64 adds per row cost full warp instructions.
 
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 #include <type_traits>
@@ -46,23 +47,22 @@ namespace tacogb {
 
 // ------------------------------------------------------------------ policies -------------
 
-// Accumulation policies.  Val is the stored value type; SV/SX are the value and x element as
-// staged in shared memory; XG is the element type of the x array the kernel gathers from.
+// Accumulation policies.  Val is the stored value type; XG is the element type of the x array
+// the kernel gathers from (pre-split double-float pairs for PolDF64).
 
 // FP64 values, FP64 accumulation (DFMA).
 struct PolNative64 {
   using Val = double;
   using Out = double;
   using Acc = double;
-  using SV = double;
-  using SX = double;
   using XG = double;
   static constexpr bool kChecked = false;
   static constexpr int kAcc = 1;  // joining accumulators at a row end would cost an FP64 add
   __device__ static Acc zero() { return 0.0; }
-  __device__ static SV stage_val(Val v, bool&) { return v; }
-  __device__ static SX stage_x(XG x, bool&) { return x; }
-  __device__ static void madd(Acc& acc, SV a, SX x) { acc = __fma_rn(a, x, acc); }
+  __device__ static bool madd(Acc& acc, Val a, XG x) {
+    acc = __fma_rn(a, x, acc);
+    return true;
+  }
   __device__ static Acc add(Acc a, Acc b) { return __dadd_rn(a, b); }
   __device__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
   __device__ static Acc shfl_xor(Acc a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
@@ -75,19 +75,16 @@ struct PolDF64 {
   using Val = double;
   using Out = double;
   using Acc = DF;
-  using SV = DF;
-  using SX = DF;
   using XG = DF;
   static constexpr bool kChecked = true;
   static constexpr int kAcc = 2;  // interleaved accumulators halve the TwoSum dependency chain
   __device__ static Acc zero() { return DF{0.f, 0.f}; }
-  __device__ static SV stage_val(Val v, bool& ok) {
-    DF d;
-    ok &= split_df(v, d.h, d.l);
-    return d;
+  __device__ static bool madd(Acc& acc, Val a, XG x) {
+    float ah, al;
+    const bool ok = split_df(a, ah, al);
+    acc = df_add(acc, df_mul(ah, al, x.h, x.l));
+    return ok;
   }
-  __device__ static SX stage_x(XG x, bool&) { return x; }
-  __device__ static void madd(Acc& acc, SV a, SX x) { acc = df_add(acc, df_mul(a.h, a.l, x.h, x.l)); }
   __device__ static Acc add(Acc a, Acc b) { return df_add(a, b); }
   __device__ static Acc shfl_up(Acc a, int d) {
     return DF{__shfl_up_sync(0xffffffffu, a.h, d), __shfl_up_sync(0xffffffffu, a.l, d)};
@@ -104,19 +101,16 @@ struct PolComp32 {
   using Val = float;
   using Out = float;
   using Acc = DF;
-  using SV = float;
-  using SX = float;
   using XG = float;
   static constexpr bool kChecked = false;
   static constexpr int kAcc = 2;
   __device__ static Acc zero() { return DF{0.f, 0.f}; }
-  __device__ static SV stage_val(Val v, bool&) { return v; }
-  __device__ static SX stage_x(XG x, bool&) { return x; }
-  __device__ static void madd(Acc& acc, SV a, SX x) {
+  __device__ static bool madd(Acc& acc, Val a, XG x) {
     DF p;
     p.h = __fmul_rn(a, x);
     p.l = __fmaf_rn(a, x, -p.h);
     acc = df_add(acc, p);
+    return true;
   }
   __device__ static Acc add(Acc a, Acc b) { return df_add(a, b); }
   __device__ static Acc shfl_up(Acc a, int d) {
@@ -133,10 +127,11 @@ struct PolComp32 {
 // (no pre-split buffer; more integer work per nonzero).
 struct PolDF64X : PolDF64 {
   using XG = double;
-  __device__ static SX stage_x(XG x, bool& ok) {
-    DF d;
-    ok &= split_df(x, d.h, d.l);
-    return d;
+  __device__ static bool madd(Acc& acc, Val a, XG x) {
+    float ah, al, xh, xl;
+    const bool ok = split_df(a, ah, al) & split_df(x, xh, xl);
+    acc = df_add(acc, df_mul(ah, al, xh, xl));
+    return ok;
   }
 };
 
@@ -204,12 +199,10 @@ struct WmSmem {
   using Val = typename P::Val;
   static constexpr int ITEMS = kWmBlock * IPT;
   static constexpr int VPAD = 16 / sizeof(Val);  // values per 16 bytes
-  // Staged arrays keep room for the 16-byte alignment slack of the bulk copies.  val holds the
-  // raw values as copied, then (in place, same width) the policy's staged form.
+  // Staged arrays keep room for the 16-byte alignment slack of the bulk copies.
   alignas(16) int32_t crd[ITEMS + 8];
   alignas(16) Val val[ITEMS + 2 * VPAD];
   alignas(16) int32_t re[ITEMS + 8];  // global nonzero index of each row end (pos entries)
-  alignas(8) double x[ITEMS];         // gathered x (policy's SX, at most 8 bytes)
   double y[ITEMS];                    // row results (policy accumulator, 8 bytes)
   int32_t wkey[kWmWarps];
   double wval[kWmWarps];  // warp carries (policy accumulator)
@@ -290,39 +283,6 @@ __device__ __forceinline__ DF ldg_xg<DF>(const DF* p) {
   return DF{v.x, v.y};
 }
 
-// Gathers x for every nonzero of the tile into s.x and converts the staged values to the
-// policy's form, all threads at once with IPT independent gathers each (so no lane waits on a
-// gather inside its walk).  Returns false when a checked policy met an unrepresentable value.
-template <class P, int IPT, class S>
-__device__ __forceinline__ bool wm_gather(S& s, const int32_t* scrd, typename P::Val* sval,
-                                          const typename P::XG* __restrict__ x, int kn) {
-  using XG = typename P::XG;
-  using SV = typename P::SV;
-  using SX = typename P::SX;
-  static_assert(sizeof(SV) == sizeof(typename P::Val), "staged values convert in place");
-  static_assert(sizeof(SX) <= sizeof(double), "staged x fits its slot");
-  const int tid = threadIdx.x;
-  SX* sx = reinterpret_cast<SX*>(s.x);
-  SV* sv = reinterpret_cast<SV*>(sval);
-  bool ok = true;
-  XG g[IPT];
-#pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    const int i = tid + j * kWmBlock;
-    if (i < kn) g[j] = ldg_xg(x + scrd[i]);
-  }
-#pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    const int i = tid + j * kWmBlock;
-    if (i < kn) {
-      sx[i] = P::stage_x(g[j], ok);
-      sv[i] = P::stage_val(sval[i], ok);
-    }
-  }
-  __syncthreads();
-  return ok;
-}
-
 // Tile-local merge coordinate of diagonal d (rows ended, nonzeros consumed).
 __device__ __forceinline__ void tile_search(const int32_t* s_re, int rn, int kn, int k0, int d,
                                             int& row, int& k) {
@@ -341,15 +301,18 @@ __device__ __forceinline__ A& as_acc(double& slot) {
   return *reinterpret_cast<A*>(&slot);
 }
 
-// Walks this lane's IPT merge items over the staged tile with policy P, joins lanes and warps,
-// and leaves every row result of the tile in s.y; the part of the row still open at the tile
-// end is returned in `carry` (thread 0).
+// Walks this lane's IPT merge items over the staged tile with policy P, gathering x in chunks
+// of CH independent loads inside the walk (other warps' arithmetic hides their latency), joins
+// lanes and warps, and leaves every row result of the tile in s.y; the part of the row still
+// open at the tile end is returned in `carry` (thread 0).  Returns false when a checked policy
+// met a value it cannot represent.
 template <class P, int IPT, class S>
-__device__ __forceinline__ void wm_tile(S& s, const typename P::SV* sv, const int32_t* sre,
+__device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typename P::Val* sval,
+                                        const int32_t* sre, const typename P::XG* __restrict__ x,
                                         int rn, int kn, int k0, typename P::Acc& carry) {
   using Acc = typename P::Acc;
-  using SX = typename P::SX;
-  const SX* sx = reinterpret_cast<const SX*>(s.x);
+  using Val = typename P::Val;
+  using XG = typename P::XG;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int items = rn + kn;
   const int ds = min(tid * IPT, items), de = min(ds + IPT, items);
@@ -358,6 +321,7 @@ __device__ __forceinline__ void wm_tile(S& s, const typename P::SV* sv, const in
   tile_search(sre, rn, kn, k0, de, row_e, ke);
   const int cnt = ke - ks;
 
+  bool ok = true;
   constexpr int NA = P::kAcc;
   Acc acc[NA], first = P::zero();
 #pragma unroll
@@ -377,10 +341,25 @@ __device__ __forceinline__ void wm_tile(S& s, const typename P::SV* sv, const in
     }
     acc[0] = P::zero();
   };
+  constexpr int CH = 4;
+#pragma unroll 1
+  for (int c = 0; c < IPT; c += CH) {
+    Val vv[CH];
+    XG xv[CH];
 #pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    while (row < row_e && sre[row] <= k0 + ks + j) emit(row++);
-    if (j < cnt) P::madd(acc[j % NA], sv[ks + j], sx[ks + j]);
+    for (int j = 0; j < CH; j++) {
+      if (c + j < cnt) {
+        vv[j] = sval[ks + c + j];
+        xv[j] = ldg_xg(x + scrd[ks + c + j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < CH; j++) {
+      if (c + j < IPT) {
+        while (row < row_e && sre[row] <= k0 + ks + c + j) emit(row++);
+        if (c + j < cnt) ok &= P::madd(acc[(c + j) % NA], vv[j], xv[j]);
+      }
+    }
   }
   while (row < row_e) emit(row++);
 #pragma unroll
@@ -427,6 +406,7 @@ __device__ __forceinline__ void wm_tile(S& s, const typename P::SV* sv, const in
     }
   }
   __syncthreads();
+  return ok;
 }
 
 // xg: x in the policy's gather form (pre-split for the double-float policy); x64: the original
@@ -458,24 +438,20 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   bool native = !P::kChecked;
   if constexpr (P::kChecked) {
     bool ok = (xflag == nullptr || *xflag == 0);
-    if (__syncthreads_and(ok)) ok = wm_gather<P, IPT>(s, scrd, sval, xg, kn);
+    typename P::Acc carry = P::zero();
+    if (__syncthreads_and(ok)) ok = wm_tile<P, IPT>(s, scrd, sval, sre, xg, rn, kn, k0, carry);
     if (__syncthreads_and(ok)) {
-      typename P::Acc carry = P::zero();
-      wm_tile<P, IPT>(s, reinterpret_cast<const typename P::SV*>(sval), sre, rn, kn, k0, carry);
       for (int i = tid; i < rn; i += kWmBlock) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
       carry_d = P::to_double(carry);
     } else {
       native = true;
-      // the staged values were converted in place: restore the raw FP64 values
-      for (int i = tid; i < kn; i += kWmBlock) sval[i] = vals[k0 + i];
-      __syncthreads();
     }
   }
   if (native) {
     using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
-    wm_gather<Q, IPT>(s, scrd, (typename Q::Val*)sval, (const typename Q::XG*)x64, kn);
     typename Q::Acc carry = Q::zero();
-    wm_tile<Q, IPT>(s, reinterpret_cast<const typename Q::SV*>(sval), sre, rn, kn, k0, carry);
+    wm_tile<Q, IPT>(s, scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64, rn,
+                    kn, k0, carry);
     for (int i = tid; i < rn; i += kWmBlock)
       y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
     carry_d = Q::to_double(carry);
@@ -483,6 +459,146 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   if (tid == 0) {
     carry_row[tile] = r0 + rn;
     carry_val[tile] = carry_d;
+  }
+}
+
+// ------------------------------------------------------------------ pmerge ----------------
+//
+// Persistent form of wmerge: CTA b owns the contiguous tile range [tiles*b/G, tiles*(b+1)/G).
+// Two shared-memory stages alternate: while the CTA walks tile t from one stage, the bulk copies
+// of tile t+1 land in the other, so DRAM latency leaves the critical path.  A row that runs from
+// one of the CTA's tiles into the next is chained through a register (carry_in, FP64), so only
+// one carry per CTA reaches the fix-up kernel.
+
+template <class P, int IPT>
+struct PmStage {
+  using Val = typename P::Val;
+  static constexpr int ITEMS = kWmBlock * IPT;
+  static constexpr int VPAD = 16 / sizeof(Val);
+  alignas(16) int32_t crd[ITEMS + 8];
+  alignas(16) Val val[ITEMS + 2 * VPAD];
+  alignas(16) int32_t re[ITEMS + 8];
+};
+
+template <class P, int IPT>
+struct PmSmem {
+  PmStage<P, IPT> st[2];
+  double y[kWmBlock * IPT];
+  int32_t wkey[kWmWarps];
+  double wval[kWmWarps];
+  uint64_t bar[2];
+};
+
+// Issues the copies of tile (r0, rn, k0, kn) into stage buf: thread 0 the bulk copies over the
+// 16-byte-aligned spans, every thread its share of the sub-16-byte tails at the array ends.
+// Returns the offsets of the tile's first crd/val/row-end element inside the stage.
+template <class P, int IPT>
+__device__ __forceinline__ int3 pm_issue(PmSmem<P, IPT>& s, int buf,
+                                         const int32_t* __restrict__ pos,
+                                         const int32_t* __restrict__ crd,
+                                         const typename P::Val* __restrict__ vals, int32_t n,
+                                         int32_t nnz, int r0, int rn, int k0, int kn) {
+  using Val = typename P::Val;
+  constexpr int VP = PmStage<P, IPT>::VPAD;
+  PmStage<P, IPT>& g = s.st[buf];
+  const int tid = threadIdx.x;
+  const int k1 = k0 + kn;
+  const int a = k0 & ~3, b = max(a, min((k1 + 3) & ~3, nnz & ~3));
+  const int av = k0 & ~(VP - 1), bv = max(av, min((k1 + VP - 1) & ~(VP - 1), nnz & ~(VP - 1)));
+  const int q0 = r0 + 1, q1 = r0 + 1 + rn;
+  const int ar = q0 & ~3, br = max(ar, min((q1 + 3) & ~3, (n + 1) & ~3));
+  if (tid == 0) {
+    // generic-proxy reads of this stage (the tile before last) precede the async overwrite
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(&s.bar[buf], (uint32_t)((b - a) * 4 + (bv - av) * (int)sizeof(Val) +
+                                                  (br - ar) * 4));
+    if (b > a) tma_load_bulk(g.crd, crd + a, (uint32_t)(b - a) * 4, &s.bar[buf]);
+    if (bv > av) tma_load_bulk(g.val, vals + av, (uint32_t)(bv - av) * sizeof(Val), &s.bar[buf]);
+    if (br > ar) tma_load_bulk(g.re, pos + ar, (uint32_t)(br - ar) * 4, &s.bar[buf]);
+  }
+  for (int i = max(b, k0) + tid; i < k1; i += kWmBlock) g.crd[i - a] = crd[i];
+  for (int i = max(bv, k0) + tid; i < k1; i += kWmBlock) g.val[i - av] = vals[i];
+  for (int i = max(br, q0) + tid; i < q1; i += kWmBlock) g.re[i - ar] = __ldg(pos + i);
+  return make_int3(k0 - a, k0 - av, q0 - ar);
+}
+
+template <class P, int IPT>
+__global__ void __launch_bounds__(kWmBlock, 6)
+spmv_pmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+                   const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
+                   const typename P::Val* __restrict__ x64, typename P::Out* __restrict__ y,
+                   const int2* __restrict__ part, int32_t n, int32_t nnz, int32_t tiles,
+                   int32_t* __restrict__ carry_row, double* __restrict__ carry_val,
+                   int* status) {
+  using S = PmSmem<P, IPT>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S& s = *reinterpret_cast<S*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int G = gridDim.x, cb = blockIdx.x;
+  const int t0 = (int)((int64_t)tiles * cb / G), t1 = (int)((int64_t)tiles * (cb + 1) / G);
+  if (tid == 0) {
+    mbar_init(&s.bar[0], 1);
+    mbar_init(&s.bar[1], 1);
+  }
+  __syncthreads();
+  double carry_in = 0.0;  // thread 0: part of the open row from this CTA's earlier tiles
+  int3 off_cur = make_int3(0, 0, 0), off_next = make_int3(0, 0, 0);
+  int2 c0 = part[t0], c1 = part[t0 < t1 ? t0 + 1 : t0];
+  if (t0 < t1) off_cur = pm_issue<P, IPT>(s, 0, pos, crd, vals, n, nnz, c0.x, c1.x - c0.x, c0.y,
+                                          c1.y - c0.y);
+  for (int t = t0, i = 0; t < t1; t++, i++) {
+    const int buf = i & 1;
+    const int r0 = c0.x, k0 = c0.y, rn = c1.x - c0.x, kn = c1.y - c0.y;
+    int2 n1 = c1;
+    if (t + 1 < t1) {
+      n1 = part[t + 2];
+      off_next = pm_issue<P, IPT>(s, buf ^ 1, pos, crd, vals, n, nnz, c1.x, n1.x - c1.x, c1.y,
+                                  n1.y - c1.y);
+    }
+    mbar_wait_or_flag(&s.bar[buf], (uint32_t)((i >> 1) & 1), status);
+    __syncthreads();
+    const PmStage<P, IPT>& g = s.st[buf];
+    const int32_t* scrd = g.crd + off_cur.x;
+    const typename P::Val* sval = g.val + off_cur.y;
+    const int32_t* sre = g.re + off_cur.z;
+
+    double carry_d = 0.0;
+    bool native = !P::kChecked;
+    if constexpr (P::kChecked) {
+      typename P::Acc carry = P::zero();
+      const bool ok = wm_tile<P, IPT>(s, scrd, sval, sre, xg, rn, kn, k0, carry);
+      if (__syncthreads_and(ok)) {
+        for (int q = tid; q < rn; q += kWmBlock) {
+          double v = P::to_double(as_acc<typename P::Acc>(s.y[q]));
+          if (q == 0) v += carry_in;
+          y[r0 + q] = (typename P::Out)v;
+        }
+        carry_d = P::to_double(carry);
+      } else {
+        native = true;
+      }
+    }
+    if (native) {
+      using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
+      typename Q::Acc carry = Q::zero();
+      wm_tile<Q, IPT>(s, scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64, rn,
+                      kn, k0, carry);
+      for (int q = tid; q < rn; q += kWmBlock) {
+        double v = Q::to_double(as_acc<typename Q::Acc>(s.y[q]));
+        if (q == 0) v += carry_in;
+        y[r0 + q] = (typename P::Out)v;
+      }
+      carry_d = Q::to_double(carry);
+    }
+    if (tid == 0) carry_in = (rn > 0) ? carry_d : carry_in + carry_d;
+    __syncthreads();  // this stage's readers are done before the next iteration reuses it
+    c0 = c1;
+    c1 = n1;
+    off_cur = off_next;
+  }
+  if (tid == 0) {
+    carry_row[cb] = (t0 < t1) ? part[t1].x : n;
+    carry_val[cb] = carry_in;
   }
 }
 
@@ -538,7 +654,8 @@ namespace {
 struct SpmvVariant {
   const char* name;
   int family;  // 0 wmerge native, 1 wmerge double-float (x pre-split), 2 vector,
-               // 3 wmerge double-float (x split while staging)
+               // 3 wmerge double-float (x split in the walk), 4 pmerge native,
+               // 5 pmerge double-float (x split in the walk)
   int param;   // IPT for wmerge, G for vector
 };
 
@@ -547,6 +664,7 @@ const SpmvVariant kSpmvVariants[] = {
     {"wmerge_df_ipt11", 1, 11},  {"vector_g1", 2, 1},         {"vector_g2", 2, 2},
     {"vector_g4", 2, 4},         {"vector_g8", 2, 8},         {"vector_g16", 2, 16},
     {"vector_g32", 2, 32},       {"wmerge_dfx_ipt7", 3, 7},   {"wmerge_dfx_ipt11", 3, 11},
+    {"pmerge_ipt7", 4, 7},       {"pmerge_dfx_ipt7", 5, 7},   {"pmerge_dfx_ipt11", 5, 11},
 };
 constexpr int kNumSpmvVariants = sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]);
 
@@ -604,6 +722,48 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
   return 0;
 }
 
+template <class P, int IPT>
+int launch_pmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
+                  cudaStream_t st) {
+  using S = PmSmem<P, IPT>;
+  const int64_t tile_items = (int64_t)kWmBlock * IPT;
+  const int64_t total = (int64_t)A->rows + A->nnz;
+  const int64_t tiles64 = (total + tile_items - 1) / tile_items;
+  if (tiles64 == 0) return 0;
+  TACOGB_CHECK_ARG(tiles64 < (1ll << 31) - 2, "SpMV: too many merge tiles");
+  const int32_t tiles = (int32_t)tiles64;
+  auto kern = spmv_pmerge_kernel<P, IPT>;
+  TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sizeof(S)));
+  int per_sm = 0;
+  TACOGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWmBlock,
+                                                                sizeof(S)));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t grid64 = std::min<int64_t>(tiles64, (int64_t)sm_count() * per_sm);
+  const int grid = (int)grid64;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
+  const size_t crow_bytes = al((size_t)grid * sizeof(int32_t));
+  const size_t cval_bytes = al((size_t)grid * sizeof(double));
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes, 0);
+  if (!ws) return last_code();
+  int2* part = (int2*)ws;
+  int32_t* crow = (int32_t*)(ws + part_bytes);
+  double* cval = (double*)(ws + part_bytes + crow_bytes);
+  int* status = device_status();
+  if (!status) return last_code();
+  if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
+  TACOGB_LAUNCH("spmv_pmerge_kernel", st,
+                kern<<<grid, kWmBlock, sizeof(S), st>>>(
+                    A->pos, A->crd, (const typename P::Val*)A->vals,
+                    (const typename P::XG*)x, x, y, part, A->rows, (int32_t)A->nnz, tiles, crow,
+                    cval, status));
+  TACOGB_LAUNCH("spmv_carry_fixup", st,
+                spmv_carry_fixup<typename P::Out><<<(grid + 255) / 256, 256, 0, st>>>(
+                    crow, cval, grid, y, A->rows));
+  return 0;
+}
+
 template <typename V, int G>
 int launch_vector(const tacogb_csr* A, const V* x, V* y, cudaStream_t st) {
   if (A->rows == 0) return 0;
@@ -630,10 +790,15 @@ int spmv_typed(const tacogb_csr* A, const V* x, V* y, int variant, cudaStream_t 
     if (v.param == 7) return launch_wmerge<Dbl, 7>(A, x, y, st);
     return launch_wmerge<Dbl, 11>(A, x, y, st);
   }
+  using DblX = typename std::conditional<sizeof(V) == 8, PolDF64X, PolComp32>::type;
   if (v.family == 3) {
-    using DblX = typename std::conditional<sizeof(V) == 8, PolDF64X, PolComp32>::type;
     if (v.param == 7) return launch_wmerge<DblX, 7>(A, x, y, st);
     return launch_wmerge<DblX, 11>(A, x, y, st);
+  }
+  if (v.family == 4) return launch_pmerge<Native, 7>(A, x, y, st);
+  if (v.family == 5) {
+    if (v.param == 7) return launch_pmerge<DblX, 7>(A, x, y, st);
+    return launch_pmerge<DblX, 11>(A, x, y, st);
   }
   switch (v.param) {
     case 1: return launch_vector<V, 1>(A, x, y, st);
