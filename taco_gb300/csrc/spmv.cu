@@ -35,6 +35,7 @@
 //          regular rows in FP32; its log2(G) FP64 adds per row cost full warp instructions.
 
 #include <algorithm>
+#include <climits>
 #include <cstdio>
 #include <mutex>
 #include <type_traits>
@@ -49,6 +50,37 @@ namespace tacogb {
 
 // Accumulation policies.  Val is the stored value type; XG is the element type of the x array
 // the kernel gathers from (pre-split double-float pairs for PolDF64).
+
+// Walk state.  A lane's items go through step<J> (J = item parity, a compile-time constant
+// after unrolling); take() returns the row's sum in the policy's accumulator type and resets.
+// The default keeps kAcc interleaved accumulators of type Acc, which shortens the dependency
+// chain of each one.
+template <class P, class AccT, int NA>
+struct InterleavedWalk {
+  struct State {
+    AccT a[NA];
+  };
+  __device__ static State init() {
+    State s;
+#pragma unroll
+    for (int i = 0; i < NA; i++) s.a[i] = P::zero();
+    return s;
+  }
+  template <int J>
+  __device__ static bool step(State& s, typename P::Val a, typename P::XG x) {
+    return P::madd(s.a[J % NA], a, x);
+  }
+  __device__ static AccT take(State& s) {
+    AccT v = s.a[0];
+    s.a[0] = P::zero();
+#pragma unroll
+    for (int i = 1; i < NA; i++) {
+      v = P::add(v, s.a[i]);
+      s.a[i] = P::zero();
+    }
+    return v;
+  }
+};
 
 // FP64 values, FP64 accumulation (DFMA).
 struct PolNative64 {
@@ -68,6 +100,7 @@ struct PolNative64 {
   __device__ static Acc shfl_xor(Acc a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
   __device__ static Out out(Acc a) { return a; }
   __device__ static double to_double(Acc a) { return a; }
+  using W = InterleavedWalk<PolNative64, Acc, kAcc>;
 };
 
 // FP64 values evaluated in double-float on the FP32 pipe; x arrives pre-split (DF per entry).
@@ -94,6 +127,7 @@ struct PolDF64 {
   }
   __device__ static Out out(Acc a) { return df_to_double(a); }
   __device__ static double to_double(Acc a) { return df_to_double(a); }
+  using W = InterleavedWalk<PolDF64, Acc, kAcc>;
 };
 
 // FP32 values, TwoProduct/TwoSum-compensated FP32 accumulation.
@@ -121,6 +155,7 @@ struct PolComp32 {
   }
   __device__ static Out out(Acc a) { return __fadd_rn(a.h, a.l); }
   __device__ static double to_double(Acc a) { return (double)a.h + (double)a.l; }
+  using W = InterleavedWalk<PolComp32, Acc, kAcc>;
 };
 
 // Double-float policy that gathers the FP64 x and splits each gathered entry while staging
@@ -133,6 +168,59 @@ struct PolDF64X : PolDF64 {
     acc = df_add(acc, df_mul(ah, al, xh, xl));
     return ok;
   }
+  using W = InterleavedWalk<PolDF64X, Acc, kAcc>;
+};
+
+// PolDF64X with four interleaved accumulators (shorter TwoSum chains, one more join per row).
+struct PolDF64X4 : PolDF64X {
+  static constexpr int kAcc = 4;
+  using W = InterleavedWalk<PolDF64X, Acc, kAcc>;
+};
+
+// FP64 values, both pipes at once: even items of a lane accumulate with DFMA on the FP64 pipe,
+// odd items in double-float on the FP32 pipe (x split on the fly); a row's two partial sums
+// join in FP64 at the row end, and the lane/warp/tile joins run in FP64.  Error is bounded by
+// the double-float half (about 2^-46 per product).
+struct PolHybrid {
+  using Val = double;
+  using Out = double;
+  using Acc = double;
+  using XG = double;
+  static constexpr bool kChecked = true;
+  __device__ static Acc zero() { return 0.0; }
+  __device__ static Acc add(Acc a, Acc b) { return __dadd_rn(a, b); }
+  __device__ static Acc shfl_up(Acc a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+  __device__ static Acc shfl_xor(Acc a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
+  __device__ static Out out(Acc a) { return a; }
+  __device__ static double to_double(Acc a) { return a; }
+  __device__ static bool madd(Acc& acc, Val a, XG x) {  // used by the vector family only
+    acc = __fma_rn(a, x, acc);
+    return true;
+  }
+  struct W {
+    struct State {
+      double n;
+      DF d;
+    };
+    __device__ static State init() { return State{0.0, DF{0.f, 0.f}}; }
+    template <int J>
+    __device__ static bool step(State& s, double a, double x) {
+      if (J == 0) {
+        s.n = __fma_rn(a, x, s.n);
+        return true;
+      }
+      float ah, al, xh, xl;
+      const bool ok = split_df(a, ah, al) & split_df(x, xh, xl);
+      s.d = df_add(s.d, df_mul(ah, al, xh, xl));
+      return ok;
+    }
+    __device__ static double take(State& s) {
+      const double v = __dadd_rn(s.n, df_to_double(s.d));
+      s.n = 0.0;
+      s.d = DF{0.f, 0.f};
+      return v;
+    }
+  };
 };
 
 // x split once per product for the double-float policy; flag set when some entry is outside
@@ -204,6 +292,7 @@ struct WmSmem {
   alignas(16) Val val[ITEMS + 2 * VPAD];
   alignas(16) int32_t re[ITEMS + 8];  // global nonzero index of each row end (pos entries)
   double y[ITEMS];                    // row results (policy accumulator, 8 bytes)
+  int2 lane_start[kWmBlock + 1];      // merge coordinate where each lane's walk starts
   int32_t wkey[kWmWarps];
   double wval[kWmWarps];  // warp carries (policy accumulator)
   uint64_t bar;
@@ -306,7 +395,7 @@ __device__ __forceinline__ A& as_acc(double& slot) {
 // lanes and warps, and leaves every row result of the tile in s.y; the part of the row still
 // open at the tile end is returned in `carry` (thread 0).  Returns false when a checked policy
 // met a value it cannot represent.
-template <class P, int IPT, class S>
+template <class P, int IPT, class S, int CH = 4>
 __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typename P::Val* sval,
                                         const int32_t* sre, const typename P::XG* __restrict__ x,
                                         int rn, int kn, int k0, typename P::Acc& carry) {
@@ -315,33 +404,38 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
   using XG = typename P::XG;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int items = rn + kn;
-  const int ds = min(tid * IPT, items), de = min(ds + IPT, items);
-  int row, ks, row_e, ke;
-  tile_search(sre, rn, kn, k0, ds, row, ks);
-  tile_search(sre, rn, kn, k0, de, row_e, ke);
+  // One merge-path search per thread: a lane's walk ends where the next lane's begins.
+  int row, ks;
+  tile_search(sre, rn, kn, k0, min(tid * IPT, items), row, ks);
+  s.lane_start[tid] = make_int2(row, ks);
+  if (tid == 0) {
+    int r, k;
+    tile_search(sre, rn, kn, k0, min(kWmBlock * IPT, items), r, k);
+    s.lane_start[kWmBlock] = make_int2(r, k);
+  }
+  __syncthreads();
+  const int row_e = s.lane_start[tid + 1].x, ke = s.lane_start[tid + 1].y;
   const int cnt = ke - ks;
+  // global nonzero index of the next row end (kept in a register; reloaded only at row ends)
+  int next_end = row < row_e ? sre[row] : INT_MAX;
 
   bool ok = true;
-  constexpr int NA = P::kAcc;
-  Acc acc[NA], first = P::zero();
-#pragma unroll
-  for (int a = 0; a < NA; a++) acc[a] = P::zero();
+  using Wk = typename P::W;
+  typename Wk::State st = Wk::init();
+  Acc first = P::zero();
   int first_row = -1;
   auto emit = [&](int r) {
-#pragma unroll
-    for (int a = 1; a < NA; a++) {
-      acc[0] = P::add(acc[0], acc[a]);
-      acc[a] = P::zero();
-    }
+    const Acc v = Wk::take(st);
     if (first_row < 0) {
       first_row = r;
-      first = acc[0];
+      first = v;
     } else {
-      as_acc<Acc>(s.y[r]) = acc[0];
+      as_acc<Acc>(s.y[r]) = v;
     }
-    acc[0] = P::zero();
+    row = r + 1;
+    next_end = row < row_e ? sre[row] : INT_MAX;
   };
-  constexpr int CH = 4;
+  static_assert(CH % 2 == 0, "item parity within a chunk must equal the parity of j");
 #pragma unroll 1
   for (int c = 0; c < IPT; c += CH) {
     Val vv[CH];
@@ -356,19 +450,20 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
 #pragma unroll
     for (int j = 0; j < CH; j++) {
       if (c + j < IPT) {
-        while (row < row_e && sre[row] <= k0 + ks + c + j) emit(row++);
-        if (c + j < cnt) ok &= P::madd(acc[(c + j) % NA], vv[j], xv[j]);
+        while (next_end <= k0 + ks + c + j) emit(row);
+        if (c + j < cnt)
+          ok &= (j & 1) ? Wk::template step<1>(st, vv[j], xv[j])
+                        : Wk::template step<0>(st, vv[j], xv[j]);
       }
     }
   }
-  while (row < row_e) emit(row++);
-#pragma unroll
-  for (int a = 1; a < NA; a++) acc[0] = P::add(acc[0], acc[a]);
+  while (row < row_e) emit(row);
+  const Acc accv = Wk::take(st);
 
   // Segmented inclusive scan of lane carries keyed by the open row (keys are non-decreasing
   // along the lanes, so equal keys are contiguous).
   const int key = row_e;
-  Acc sc = acc[0];
+  Acc sc = accv;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const Acc o = P::shfl_up(sc, d);
@@ -412,7 +507,7 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
 // xg: x in the policy's gather form (pre-split for the double-float policy); x64: the original
 // FP64 x for the native fallback (same as xg for unchecked policies); xflag: non-zero when x
 // has entries outside the double-float range.
-template <class P, int IPT, bool TMA>
+template <class P, int IPT, bool TMA, int CH = 4>
 __global__ void __launch_bounds__(kWmBlock, 8)
 spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                    const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
@@ -439,7 +534,7 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   if constexpr (P::kChecked) {
     bool ok = (xflag == nullptr || *xflag == 0);
     typename P::Acc carry = P::zero();
-    if (__syncthreads_and(ok)) ok = wm_tile<P, IPT>(s, scrd, sval, sre, xg, rn, kn, k0, carry);
+    if (__syncthreads_and(ok)) ok = wm_tile<P, IPT, S, CH>(s, scrd, sval, sre, xg, rn, kn, k0, carry);
     if (__syncthreads_and(ok)) {
       for (int i = tid; i < rn; i += kWmBlock) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
       carry_d = P::to_double(carry);
@@ -450,8 +545,8 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   if (native) {
     using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
     typename Q::Acc carry = Q::zero();
-    wm_tile<Q, IPT>(s, scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64, rn,
-                    kn, k0, carry);
+    wm_tile<Q, IPT, S, CH>(s, scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64,
+                           rn, kn, k0, carry);
     for (int i = tid; i < rn; i += kWmBlock)
       y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
     carry_d = Q::to_double(carry);
@@ -484,6 +579,7 @@ template <class P, int IPT>
 struct PmSmem {
   PmStage<P, IPT> st[2];
   double y[kWmBlock * IPT];
+  int2 lane_start[kWmBlock + 1];
   int32_t wkey[kWmWarps];
   double wval[kWmWarps];
   uint64_t bar[2];
@@ -655,7 +751,9 @@ struct SpmvVariant {
   const char* name;
   int family;  // 0 wmerge native, 1 wmerge double-float (x pre-split), 2 vector,
                // 3 wmerge double-float (x split in the walk), 4 pmerge native,
-               // 5 pmerge double-float (x split in the walk)
+               // 5 pmerge double-float (x split in the walk), 6 wmerge hybrid
+               // (DFMA and double-float items interleaved), 7 family 3 with 8-deep gathers,
+               // 8 family 3 with four accumulators, 9 both
   int param;   // IPT for wmerge, G for vector
 };
 
@@ -665,10 +763,13 @@ const SpmvVariant kSpmvVariants[] = {
     {"vector_g4", 2, 4},         {"vector_g8", 2, 8},         {"vector_g16", 2, 16},
     {"vector_g32", 2, 32},       {"wmerge_dfx_ipt7", 3, 7},   {"wmerge_dfx_ipt11", 3, 11},
     {"pmerge_ipt7", 4, 7},       {"pmerge_dfx_ipt7", 5, 7},   {"pmerge_dfx_ipt11", 5, 11},
+    {"wmerge_hyb_ipt7", 6, 7},   {"wmerge_hyb_ipt11", 6, 11},
+    {"wmerge_dfx_ipt7_c8", 7, 7}, {"wmerge_dfx4_ipt7", 8, 7}, {"wmerge_dfx_ipt5", 3, 5},
+    {"wmerge_dfx_ipt9", 3, 9},   {"wmerge_dfx4_ipt11_c8", 9, 11},
 };
 constexpr int kNumSpmvVariants = sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]);
 
-template <class P, int IPT>
+template <class P, int IPT, int CH = 4>
 int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
                   cudaStream_t st) {
   using S = WmSmem<P, IPT>;
@@ -709,7 +810,7 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
   // Bulk copies need 16-byte aligned sources: true for every allocator the library meets
   // (cudaMalloc, cudaMallocManaged, torch); sliced pointers take the register-staged kernel.
   const bool tma = (((uintptr_t)A->pos | (uintptr_t)A->crd | (uintptr_t)A->vals) & 15) == 0;
-  auto kern = tma ? spmv_wmerge_kernel<P, IPT, true> : spmv_wmerge_kernel<P, IPT, false>;
+  auto kern = tma ? spmv_wmerge_kernel<P, IPT, true, CH> : spmv_wmerge_kernel<P, IPT, false, CH>;
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(S)));
   TACOGB_LAUNCH("spmv_wmerge_kernel", st,
@@ -792,10 +893,23 @@ int spmv_typed(const tacogb_csr* A, const V* x, V* y, int variant, cudaStream_t 
   }
   using DblX = typename std::conditional<sizeof(V) == 8, PolDF64X, PolComp32>::type;
   if (v.family == 3) {
-    if (v.param == 7) return launch_wmerge<DblX, 7>(A, x, y, st);
-    return launch_wmerge<DblX, 11>(A, x, y, st);
+    switch (v.param) {
+      case 5: return launch_wmerge<DblX, 5>(A, x, y, st);
+      case 7: return launch_wmerge<DblX, 7>(A, x, y, st);
+      case 9: return launch_wmerge<DblX, 9>(A, x, y, st);
+      default: return launch_wmerge<DblX, 11>(A, x, y, st);
+    }
   }
+  using DblX4 = typename std::conditional<sizeof(V) == 8, PolDF64X4, PolComp32>::type;
+  if (v.family == 7) return launch_wmerge<DblX, 7, 8>(A, x, y, st);
+  if (v.family == 8) return launch_wmerge<DblX4, 7>(A, x, y, st);
+  if (v.family == 9) return launch_wmerge<DblX4, 11, 8>(A, x, y, st);
   if (v.family == 4) return launch_pmerge<Native, 7>(A, x, y, st);
+  if (v.family == 6) {
+    using Hyb = typename std::conditional<sizeof(V) == 8, PolHybrid, PolComp32>::type;
+    if (v.param == 7) return launch_wmerge<Hyb, 7>(A, x, y, st);
+    return launch_wmerge<Hyb, 11>(A, x, y, st);
+  }
   if (v.family == 5) {
     if (v.param == 7) return launch_pmerge<DblX, 7>(A, x, y, st);
     return launch_pmerge<DblX, 11>(A, x, y, st);
@@ -821,8 +935,11 @@ const char* spmv_variant_name(int v) {
 
 // Structural rule used when neither a tuning record nor the cost model gives a choice: the
 // merge family is robust to any skew, and for FP64 values the double-float policy keeps the
-// kernel off GB300's narrow FP64 pipe.
-int spmv_default_variant(const tacogb_csr* A) { return A->vtype == TACOGB_F64 ? 3 : 1; }
+// kernel off GB300's narrow FP64 pipe (IPT 7 measured fastest on the power-law workload).
+int spmv_default_variant(const tacogb_csr* A) {
+  (void)A;
+  return 10;  // wmerge_dfx_ipt7: double-float for FP64 values, compensated FP32 for FP32
+}
 
 int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStream_t st) {
   TACOGB_CHECK_ARG(A != nullptr, "SpMV: null matrix");

@@ -168,7 +168,7 @@ def test_double_float_falls_back_outside_range(scale):
     x = W.dense(26, s.cols)
     x[:100] *= 1e-20  # some x out of range too
     y_ref = O.spmv(pos, crd, vals, x)
-    for variant in (2, 3, 10, 11):
+    for variant in (2, 3, 10, 11, 13, 15, 16):
         assert normwise(run_dev(pos, crd, vals, x, variant), y_ref) <= F64_TOL
 
 
