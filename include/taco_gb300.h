@@ -107,6 +107,28 @@ const char* tacogb_spmv_variant_name(int32_t variant);
  * streams, or graphs replayed concurrently) race and must be serialised by the caller. */
 int tacogb_spmv_noalloc(const tacogb_csr* A, const void* x, void* y, void* stream);
 
+/* Batched SpMV: y_m = A_m x_m for count independent CSR matrices in one persistent launch.
+ * taco has no batched statement: a taco user calls the generated compute of y(i)=A(i,j)*x(j)
+ * once per matrix (TensorBase::compute, src/tensor.cpp:829-850); a plan replaces that loop.
+ * tacogb_batch_create validates every matrix (all of one value type, F64 or F32), cuts each into
+ * work units of the kind variants[m] names (tacogb_batch_variant_name; NULL = merge_ipt7 for
+ * all), uploads the work queue and captures the launches in a CUDA graph.  The pointers in
+ * mats, x and y are kept: the plan computes from whatever those device arrays hold when
+ * tacogb_batch_run is called.  precision 0 = the default accumulation (double-float on the FP32
+ * pipe for F64 values, with native FP64 for tiles outside its range; compensated FP32 for F32
+ * values), 1 = native FP64 (F64 values only).  Merge kinds need pos, crd and vals 16-byte
+ * aligned; a matrix whose arrays are not is planned with vector_g4.
+ * tacogb_batch_run launches the graph on stream (one graph launch; stream-ordered; one run of
+ * a plan at a time). */
+typedef struct tacogb_batch tacogb_batch;
+int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const* x,
+                        void* const* y, int32_t precision, const int32_t* variants,
+                        tacogb_batch** plan);
+int tacogb_batch_run(tacogb_batch* plan, void* stream);
+int tacogb_batch_destroy(tacogb_batch* plan);
+int tacogb_batch_variant_count(void);
+const char* tacogb_batch_variant_name(int32_t variant);
+
 /* C = A B with B (rows = A->cols) x N and C (A->rows x N) dense row-major.
  * Types: A F64 with B F64 -> C FP64; A F32 with B F32 -> C FP32; A F32 with B BF16 -> C FP32
  * (BF16 dense operand, FP32 accumulation).  Replaces the generated compute of

@@ -10,7 +10,8 @@ from . import _native
 from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBError, check,
                       lib)
 
-__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "lib", "check", "TacoGBError",
+__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "SpmvBatch",
+           "batch_variants", "lib", "check", "TacoGBError",
            "TACOGB_F64", "TACOGB_F32", "TACOGB_BF16", "VARIANT_AUTO"]
 
 
@@ -90,3 +91,41 @@ def spmm_variants():
 def spmv_variants():
     L = lib()
     return [L.tacogb_spmv_variant_name(i).decode() for i in range(L.tacogb_spmv_variant_count())]
+
+
+class SpmvBatch:
+    """A plan for y_m = A_m x_m over many CsrMatrix objects, run as one CUDA-graph launch
+    (tacogb_batch_create / tacogb_batch_run).  variants[m] names how matrix m is cut into work
+    units (an index into batch_variants()); precision 1 selects native FP64 accumulation."""
+
+    def __init__(self, mats, xs, ys, precision=0, variants=None):
+        n = len(mats)
+        if not (n == len(xs) == len(ys)):
+            raise ValueError("mats, xs and ys differ in length")
+        self._keep = (list(mats), list(xs), list(ys))
+        csr = (_native.Csr * n)(*[A.as_csr() for A in mats])
+        xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
+        yp = (ctypes.c_void_p * n)(*[y.data_ptr() for y in ys])
+        var = None if variants is None else (ctypes.c_int32 * n)(*[int(v) for v in variants])
+        self._h = ctypes.c_void_p()
+        check(lib().tacogb_batch_create(n, csr, xp, yp, precision, var, ctypes.byref(self._h)),
+              "tacogb_batch_create")
+
+    def run(self, stream=None):
+        check(lib().tacogb_batch_run(self._h, _stream_ptr(stream)), "tacogb_batch_run")
+
+    def close(self):
+        if self._h:
+            lib().tacogb_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_variants():
+    L = lib()
+    return [L.tacogb_batch_variant_name(i).decode() for i in range(L.tacogb_batch_variant_count())]

@@ -78,6 +78,11 @@ SIGNATURES = {
     "_shim_tacogb_spmv_assemble": (I32, [P]),
     "_shim_tacogb_spmv_compute": (I32, [P]),
     "_shim_tacogb_spmv_evaluate": (I32, [P]),
+    "tacogb_batch_create": (I32, [I32, ctypes.POINTER(Csr), P, P, I32, P, ctypes.POINTER(P)]),
+    "tacogb_batch_run": (I32, [P, P]),
+    "tacogb_batch_destroy": (I32, [P]),
+    "tacogb_batch_variant_count": (I32, []),
+    "tacogb_batch_variant_name": (ctypes.c_char_p, [I32]),
     "tacogb_spmm": (I32, [ctypes.POINTER(Csr), I32, P, I32, P, I32, P]),
     "tacogb_spmm_variant_count": (I32, []),
     "tacogb_spmm_variant_name": (ctypes.c_char_p, [I32]),

@@ -92,3 +92,29 @@ def test_banded_and_poisson_structure():
     pos, crd, vals = W.generate(W.spgemm_poisson(grid=512))
     assert pos[-1] == 1308672
     assert set(np.unique(vals)) == {-1.0, 4.0}
+
+
+def test_batch_plan_rejects_bad_arguments_without_gpu():
+    """tacogb_batch_create validates the whole batch on the host before touching the GPU."""
+    L = tg.lib()
+    assert [L.tacogb_batch_variant_name(i) for i in range(L.tacogb_batch_variant_count())] == \
+        [b"merge_ipt7", b"merge_ipt3", b"vector_g4", b"vector_g16"]
+    h = ctypes.c_void_p()
+    assert L.tacogb_batch_create(0, None, None, None, 0, None, ctypes.byref(h)) == 1
+    assert b"empty" in L.tacogb_last_error() and not h.value
+    mats = (N.Csr * 2)()
+    for m, vt in enumerate((tg.TACOGB_F64, tg.TACOGB_F32)):
+        mats[m].rows, mats[m].cols, mats[m].nnz, mats[m].vtype = 4, 4, 0, vt
+        mats[m].pos = 16  # never dereferenced on the host
+    ptrs = (ctypes.c_void_p * 2)(16, 16)
+    assert L.tacogb_batch_create(2, mats, ptrs, ptrs, 0, None, ctypes.byref(h)) == 1
+    assert b"value type" in L.tacogb_last_error()
+    mats[1].vtype = tg.TACOGB_F64
+    bad = (ctypes.c_int32 * 2)(0, 9)
+    assert L.tacogb_batch_create(2, mats, ptrs, ptrs, 0, bad, ctypes.byref(h)) == 1
+    assert b"variant 9" in L.tacogb_last_error()
+    assert L.tacogb_batch_create(2, mats, ptrs, ptrs, 3, None, ctypes.byref(h)) == 1
+    mats[0].rows = -1
+    assert L.tacogb_batch_create(2, mats, ptrs, ptrs, 0, None, ctypes.byref(h)) == 1
+    assert b"bad size" in L.tacogb_last_error()
+    assert L.tacogb_batch_run(None, None) == 1
