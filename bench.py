@@ -45,7 +45,11 @@ def parse():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="spmv_powerlaw",
-                   choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw"])
+                   choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
+                            "batched_spmv"])
+    p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
+    p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
+                   help="how batched_spmv picks each matrix's work-unit kind")
     p.add_argument("--dtype", default="f64", choices=["f64", "f32", "bf16"])
     p.add_argument("--n", type=int, default=64, help="dense columns of B for SpMM")
     p.add_argument("--variant", type=int, default=-1)
@@ -225,7 +229,101 @@ class SpmmOp:
                                                    v.ctypes.data, B.ctypes.data, C.ctypes.data), C
 
 
+class BatchOp:
+    """4,096 CSR matrices from the batch generator (rows log-uniform in [256, 262,144], square,
+    mean nnz/row in {2,...,64}, uniform / power-law / banded by index mod 3), y_m = A_m x_m for
+    all m per step.  Metric: GFLOP/s = sum_m 2*nnz_m per step."""
+    pattern = "batch"
+    unit = "GFLOP/s"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        self.count = args.batch_count
+        self.specs = [W.batch_spec(m) for m in range(self.count)]
+        self.rows = sum(s.rows for s in self.specs)
+        self.cols = self.rows
+        self.nnz = 0
+        self.metric = "batched_spmv_%s_gflops" % ("f32c" if args.dtype == "f32" else "f64")
+        self.workload = "batched_spmv_%d" % self.count
+
+    def upload(self, torch):
+        """Generates every matrix on the host and keeps it on the GPU: int32 pos/crd, FP64 and
+        FP32 values; x and y of all matrices are views into four flat buffers."""
+        from taco_gb300 import workloads as W
+        dev = {"pos": [], "crd": [], "v64": [], "v32": []}
+        nnz = []
+        for s in self.specs:
+            pos, crd, vals = W.generate(s)
+            dev["pos"].append(torch.from_numpy(pos).cuda())
+            dev["crd"].append(torch.from_numpy(crd).cuda())
+            v = torch.from_numpy(vals).cuda()
+            dev["v64"].append(v)
+            dev["v32"].append(v.float())
+            nnz.append(len(crd))
+        self.nnz = int(sum(nnz))
+        self.nnz_m = nnz
+        off = np.concatenate([[0], np.cumsum([s.rows for s in self.specs])])
+        self.off = off
+        x64 = torch.from_numpy(W.dense(41, int(off[-1]))).cuda()
+        dev["x64"], dev["x32"] = x64, x64.float()
+        dev["y64"] = torch.empty_like(x64)
+        dev["y32"] = torch.empty_like(dev["x32"])
+        e = ESZ["f32" if self.args.dtype == "f32" else "f64"]
+        self.bytes = self.nnz * (4 + e) + sum(4 * (s.rows + 1) + 2 * e * s.rows
+                                              for s in self.specs)
+        self.flops = 2 * self.nnz
+        return dev
+
+    def matrices(self, tg, dev, vals_key):
+        mats, xs, ys = [], [], []
+        xk, yk = ("x32", "y32") if vals_key == "v32" else ("x64", "y64")
+        for m, s in enumerate(self.specs):
+            mats.append(tg.CsrMatrix(dev["pos"][m], dev["crd"][m], dev[vals_key][m], s.cols))
+            a, b = int(self.off[m]), int(self.off[m + 1])
+            xs.append(dev[xk][a:b])
+            ys.append(dev[yk][a:b])
+        return mats, xs, ys
+
+    def cpu(self):
+        """taco's generated SpMV called once per matrix (each call OpenMP-parallel over rows) on
+        the first matrices of the batch up to about 4e8 nonzeros."""
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        from taco_gb300 import workloads as W
+        keep, calls, nnz, rows = [], [], 0, 0
+        ref = O.ref_available("spmv")
+        L = O.ref_lib("spmv") if ref else O.lib()
+        for m, s in enumerate(self.specs):
+            if nnz > 4e8:
+                break
+            pos, crd, vals = W.generate(s)
+            x, y = W.dense(41 + m, s.cols), np.empty(s.rows)
+            if ref:
+                At = T.csr(pos, crd, vals, [s.rows, s.cols])
+                Xt, Yt = T.dense(x, [s.cols]), T.dense(y, [s.rows])
+                keep.append((At, Xt, Yt, pos, crd, vals, x, y))
+                calls.append(lambda At=At, Xt=Xt, Yt=Yt: L.compute(Yt.ptr, At.ptr, Xt.ptr))
+            else:
+                keep.append((pos, crd, vals, x, y))
+                calls.append(lambda s=s, pos=pos, crd=crd, vals=vals, x=x, y=y: L.oracle_spmv_f64(
+                    s.rows, pos.ctypes.data, crd.ctypes.data, vals.ctypes.data, x.ctypes.data,
+                    y.ctypes.data))
+            nnz += len(crd)
+            rows += s.rows
+        self.cpu_units = 2 * nnz
+        self.cpu_sample = "first %d of %d matrices (%d rows, %d nnz), FP64" % (
+            len(calls), self.count, rows, nnz)
+
+        def once():
+            for c in calls:
+                c()
+        return ("reference" if ref else "port"), once, keep
+
+
 def make_op(args):
+    if args.workload == "batched_spmv":
+        return BatchOp(args)
     return SpmmOp(args) if args.workload.startswith("spmm") else SpmvOp(args)
 
 
@@ -323,21 +421,171 @@ def run_reference(args):
             steps = _ + 1
             break
     dt = time.perf_counter() - t0
-    v = op.bytes * steps / dt / 1e9
+    unit = getattr(op, "unit", "GB/s")
+    work = op.cpu_units if op.pattern == "batch" else op.bytes
+    sample = (op.cpu_sample if op.pattern == "batch" else "whole workload") + \
+        " per step, %d steps" % steps
+    v = work * steps / dt / 1e9
     code = ("taco generated C, -O3 -ffast-math -std=c99 -fopenmp" if kind == "reference"
             else "C restatement of taco's loop, -O2 -fopenmp")
-    out = {"metric": op.metric, "value": v, "unit": "GB/s", "impl": "reference",
+    out = {"metric": op.metric, "value": v, "unit": unit, "impl": "reference",
            "n_gpus": world, "steps": steps, "warmup": args.warmup,
            "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": op.workload, "rows": op.rows, "nnz": op.nnz,
-                      "bytes_per_step": op.bytes, "code": code, "threads": ncores},
-           "cpu_baseline": {"value": v, "unit": "GB/s", "cores": ncores, "kind": kind,
-                            "sample": "whole workload per step, %d steps" % steps},
-           "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-           "gflops": op.flops * steps / dt / 1e9}
+                      "work_per_step": work, "code": code, "threads": ncores},
+           "cpu_baseline": {"value": v, "unit": unit, "cores": ncores, "kind": kind,
+                            "sample": sample},
+           "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if op.pattern != "batch":
+        out["gflops"] = op.flops * steps / dt / 1e9
     print(json.dumps(out), flush=True)
     del keep
+
+
+# ----------------------------------------------------------------------------- batched
+
+def batch_variants_for(args, op, tg, dev):
+    """Per-matrix work-unit kinds: None (merge_ipt7 everywhere) or the autotuner's choice."""
+    if args.select == "default":
+        return None, "merge_ipt7 for every matrix"
+    from taco_gb300 import autotune as AT
+    mats, xs, ys = op.matrices(tg, dev, "v32")
+    if args.select == "exhaustive":
+        kinds, _ = AT.exhaustive_select(mats, xs, ys, precision=0)
+        return kinds, "exhaustive autotuner (per-matrix argmin of measured unit cycles)"
+    model = AT.load_model(os.path.join(ROOT, "taco_gb300", "data", "batch_mlp.npz"))
+    kinds = AT.learned_select(model, mats)
+    return kinds, "MLP cost model (argmin of predicted cycles over sparsity features)"
+
+
+def main_batch(args, torch, tg, T, L, rank, world):
+    """Batched SpMV: one graph launch per step over all matrices, against the same matrices
+    computed with one plain FP64 tacogb_spmv call per matrix."""
+    op = make_op(args)
+    dev = op.upload(torch)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    vkey = "v32" if args.dtype == "f32" else "v64"
+    kinds, how = batch_variants_for(args, op, tg, dev)
+    mats, xs, ys = op.matrices(tg, dev, vkey)
+    plan = tg.SpmvBatch(mats, xs, ys, precision=0, variants=kinds)
+    for _ in range(max(3, args.warmup)):
+        plan.run(stream)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = L.tacogb_launch_count()
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.run(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = L.tacogb_launch_count() - launches0
+    clocks = sampler.stop() if sampler else None
+    ms = e0.elapsed_time(e1) / args.steps
+    status = ctypes.c_int32(0)
+    L.tacogb_device_status(ctypes.byref(status))
+    if status.value:
+        raise RuntimeError("device status %d after the timed region" % status.value)
+    value = op.flops / (ms / 1e3) / 1e9
+
+    # plain FP64: one tacogb_spmv (native FP64 merge path) per matrix, issued from a host loop
+    m64, x64, y64 = op.matrices(tg, dev, "v64")
+    csrs = [A.as_csr() for A in m64]
+    native = tg.spmv_variants().index("wmerge_ipt7")
+
+    def per_matrix():
+        for c, x, y in zip(csrs, x64, y64):
+            rc = L.tacogb_spmv(ctypes.byref(c), x.data_ptr(), y.data_ptr(), native, sp)
+            if rc:
+                raise RuntimeError(L.tacogb_last_error().decode())
+    for _ in range(3):
+        per_matrix()
+    torch.cuda.synchronize()
+    k64 = max(2, min(args.steps, 10))
+    e0.record(stream)
+    for _ in range(k64):
+        per_matrix()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / k64
+
+    # error of every matrix's result against the FP64 result
+    plan.run(stream)
+    torch.cuda.synchronize()
+    yb = dev["y32" if vkey == "v32" else "y64"].double()
+    errs = []
+    for m in range(op.count):
+        a, b = int(op.off[m]), int(op.off[m + 1])
+        ref = dev["y64"][a:b]
+        den = float(ref.abs().max()) or 1.0
+        d = (yb[a:b] - ref) / den
+        nr = float(torch.linalg.vector_norm(ref / den))
+        errs.append(float(torch.linalg.vector_norm(d)) / nr if nr > 0 else 0.0)
+    max_err = max(errs)
+    del yb
+
+    # end to end: all x from pinned host memory, the graph, all y back to pinned host memory
+    xk = "x32" if vkey == "v32" else "x64"
+    yk = "y32" if vkey == "v32" else "y64"
+    hx = dev[xk].cpu().pin_memory()
+    hy = torch.empty_like(hx).pin_memory()
+    for _ in range(2):
+        dev[xk].copy_(hx, non_blocking=True)
+        plan.run(stream)
+        hy.copy_(dev[yk], non_blocking=True)
+    torch.cuda.synchronize()
+    ne = max(3, min(args.e2e_steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(ne):
+        dev[xk].copy_(hx, non_blocking=True)
+        plan.run(stream)
+        hy.copy_(dev[yk], non_blocking=True)
+        stream.synchronize()
+    e2e_s = (time.perf_counter() - t0) / ne
+    nbytes = hx.numel() * hx.element_size()
+    e2e = {"value": op.flops / e2e_s / 1e9, "unit": "GFLOP/s", "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes, "ms_per_step": e2e_s * 1e3, "steps": ne,
+           "api": "SpmvBatch.run (tacogb_batch_run) with x/y copied from/to pinned host memory; "
+                  "matrices resident"}
+
+    cpu = None
+    if not args.no_cpu:
+        kind, cores, t, reps = time_cpu(op, budget_s=10.0)
+        cpu = {"value": op.cpu_units / t / 1e9, "unit": "GFLOP/s", "cores": cores, "kind": kind,
+               "sample": op.cpu_sample + ", median of %d reps" % reps, "ms_per_step": t * 1e3}
+
+    peak, peak_kind = measured_peak()
+    achieved = op.bytes / (ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": ncu_traffic("batch_spmv_kernel", op.workload),
+                "kernel": "batch_spmv_kernel (graph: partition + persistent queue + fix-up)",
+                "kernel_ms": ms, "peak_source": peak_kind}
+    kinds_used = {}
+    for k in (kinds if kinds is not None else [0] * op.count):
+        nm = tg.batch_variants()[k]
+        kinds_used[nm] = kinds_used.get(nm, 0) + 1
+    out = {"metric": op.metric, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32c" if vkey == "v32" else "f64", "data": "synthetic",
+           "config": {"workload": op.workload, "matrices": op.count, "rows": op.rows,
+                      "nnz": op.nnz, "bytes_per_step": op.bytes, "selection": how,
+                      "kinds": kinds_used,
+                      "l2": "inputs larger than L2 (%.1f GB per step), no flush" % (op.bytes / 1e9)},
+           "fp64_per_matrix": {"gflops": op.flops / (ms64 / 1e3) / 1e9, "ms_per_step": ms64,
+                               "launch": "tacogb_spmv wmerge_ipt7 native FP64, one call per "
+                                         "matrix from a host loop", "steps": k64},
+           "speedup_vs_fp64_per_matrix": ms64 / ms,
+           "max_normwise_err_vs_fp64": max_err,
+           "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+           "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(out), flush=True)
+    plan.close()
 
 
 # ----------------------------------------------------------------------------- main
@@ -359,6 +607,9 @@ def main():
     from taco_gb300 import taco as T
     L = tg.lib()
 
+    if args.workload == "batched_spmv":
+        main_batch(args, torch, tg, T, L, rank, world)
+        return
     op = make_op(args)
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)

@@ -126,8 +126,56 @@ int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const
                         tacogb_batch** plan);
 int tacogb_batch_run(tacogb_batch* plan, void* stream);
 int tacogb_batch_destroy(tacogb_batch* plan);
+/* Cost of each matrix in the last run of the plan: the sum over its work units of the SM cycles
+ * the persistent kernel spent on each unit (read with clock64 by the unit's CTA).  Writes count
+ * entries to the host array cycles; synchronises stream.  The autotuner's measure. */
+int tacogb_batch_matrix_cycles(tacogb_batch* plan, int64_t* cycles, void* stream);
 int tacogb_batch_variant_count(void);
 const char* tacogb_batch_variant_name(int32_t variant);
+
+/* ---- batch autotuning: sparsity features and the MLP cost model (tuner.cu) ----
+ * The model predicts, for each batch work-unit kind, log2 of the SM cycles the kind spends per
+ * (row + nonzero) of a matrix; the selection is the argmin.  It changes only which kernel runs.
+ * Parameters: TACOGB_MLP_FEATURES inputs -> TACOGB_MLP_HIDDEN ReLU -> TACOGB_MLP_HIDDEN ReLU ->
+ * TACOGB_MLP_KINDS outputs, packed as W1[H][F] b1[H] W2[H][H] b2[H] W3[K][H] b3[K] (float).
+ * norm holds the feature means (F floats) then standard deviations (F floats); features are
+ * z-scored with it inside the kernels.  All pointers except tacogb_batch_features' are device
+ * pointers; calls are stream-ordered. */
+#define TACOGB_MLP_FEATURES 10
+#define TACOGB_MLP_HIDDEN 32
+#define TACOGB_MLP_KINDS 6
+int tacogb_mlp_param_count(void);
+/* Features of every matrix (device CSR arrays) into the host array feats (count x F, row-major):
+ * log2(rows+1), log2(nnz+1), log2(mean row length+1), std/mean of row lengths, log2(max+1),
+ * Gini of row lengths (histogram: exact below 2048, 16 bins per octave above), max |j-i|/cols,
+ * mean |j-i|/cols, fraction of empty rows, log2(cols+1).  Synchronises stream. */
+int tacogb_batch_features(int32_t count, const tacogb_csr* mats, float* feats, void* stream);
+/* Predictions (n x K; may be NULL) and argmin kinds (n; may be NULL) for n feature rows X. */
+int tacogb_mlp_predict(const float* params, const float* norm, const float* X, int32_t n,
+                       float* pred, int32_t* kinds, void* stream);
+/* Gradient of the masked mean squared error sum(M*(y-Y)^2)/sum(M) with respect to the
+ * parameters (grad: param_count floats) and the loss (one float; may be NULL).  Y, M: n x K. */
+int tacogb_mlp_grad(const float* params, const float* norm, const float* X, const float* Y,
+                    const float* M, int32_t n, float* grad, float* loss, void* stream);
+/* steps full-batch Adam steps (beta1 0.9, beta2 0.999, eps 1e-8, learning rate lr), numbered
+ * step0+1 .. step0+steps for bias correction; adam_state holds 2 x param_count floats (first and
+ * second moments, zero before the first step); losses (steps floats; may be NULL) receives the
+ * loss before each step.  Deterministic: the same inputs give the same parameters bit for bit. */
+int tacogb_mlp_train(float* params, const float* norm, const float* X, const float* Y,
+                     const float* M, int32_t n, int32_t steps, int32_t step0, float lr,
+                     float* adam_state, float* losses, void* stream);
+/* Exhaustive autotuner, the model's judge and fallback: plans the batch once per kind (every
+ * matrix with that kind), runs it reps times after one warm-up, keeps each matrix's minimum
+ * cycles (tacogb_batch_matrix_cycles) and writes the cheapest kind per matrix to the host array
+ * kinds; cycles (host, count x TACOGB_MLP_KINDS, may be NULL) receives the table.  x and y are
+ * written as in tacogb_batch_run.  Synchronises stream. */
+int tacogb_batch_autotune(int32_t count, const tacogb_csr* mats, const void* const* x,
+                          void* const* y, int32_t precision, int32_t reps, int32_t* kinds,
+                          int64_t* cycles, void* stream);
+/* Learned selection: tacogb_batch_features on the GPU, then tacogb_mlp_predict's argmin per
+ * matrix into the host array kinds (params and norm: device pointers).  Synchronises stream. */
+int tacogb_batch_select(int32_t count, const tacogb_csr* mats, const float* params,
+                        const float* norm, int32_t* kinds, void* stream);
 
 /* C = A B with B (rows = A->cols) x N and C (A->rows x N) dense row-major.
  * Types: A F64 with B F64 -> C FP64; A F32 with B F32 -> C FP32; A F32 with B BF16 -> C FP32

@@ -81,8 +81,16 @@ SIGNATURES = {
     "tacogb_batch_create": (I32, [I32, ctypes.POINTER(Csr), P, P, I32, P, ctypes.POINTER(P)]),
     "tacogb_batch_run": (I32, [P, P]),
     "tacogb_batch_destroy": (I32, [P]),
+    "tacogb_batch_matrix_cycles": (I32, [P, P, P]),
     "tacogb_batch_variant_count": (I32, []),
     "tacogb_batch_variant_name": (ctypes.c_char_p, [I32]),
+    "tacogb_mlp_param_count": (I32, []),
+    "tacogb_batch_features": (I32, [I32, ctypes.POINTER(Csr), P, P]),
+    "tacogb_mlp_predict": (I32, [P, P, P, I32, P, P, P]),
+    "tacogb_mlp_grad": (I32, [P, P, P, P, P, I32, P, P, P]),
+    "tacogb_mlp_train": (I32, [P, P, P, P, P, I32, I32, I32, ctypes.c_float, P, P, P]),
+    "tacogb_batch_autotune": (I32, [I32, ctypes.POINTER(Csr), P, P, I32, I32, P, P, P]),
+    "tacogb_batch_select": (I32, [I32, ctypes.POINTER(Csr), P, P, P, P]),
     "tacogb_spmm": (I32, [ctypes.POINTER(Csr), I32, P, I32, P, I32, P]),
     "tacogb_spmm_variant_count": (I32, []),
     "tacogb_spmm_variant_name": (ctypes.c_char_p, [I32]),

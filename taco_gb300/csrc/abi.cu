@@ -84,7 +84,7 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 4;
+constexpr int kScratchSlots = 5;  // spmv, spmm, spgemm x2, tuner
 
 struct DeviceState {
   int sms = 0;

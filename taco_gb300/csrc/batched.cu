@@ -28,11 +28,16 @@
 namespace tacogb {
 namespace {
 
-enum BatchKind { kMerge7 = 0, kMerge3 = 1, kVec4 = 2, kVec16 = 3 };
-constexpr int kNumBatchKinds = 4;
-const char* const kBatchKindNames[kNumBatchKinds] = {"merge_ipt7", "merge_ipt3", "vector_g4",
-                                                     "vector_g16"};
-constexpr int kVecRows = 128;  // rows per vector unit
+enum BatchKind { kMerge7 = 0, kMerge3 = 1, kVec2 = 2, kVec4 = 3, kVec8 = 4, kVec16 = 5 };
+constexpr int kNumBatchKinds = 6;
+const char* const kBatchKindNames[kNumBatchKinds] = {"merge_ipt7", "merge_ipt3", "vector_g2",
+                                                     "vector_g4", "vector_g8", "vector_g16"};
+__host__ __device__ __forceinline__ bool is_merge(int kind) { return kind <= kMerge3; }
+// Lanes per row of a vector kind, and rows per vector unit (every lane group takes 4 rows).
+__host__ __device__ __forceinline__ int vec_lanes(int kind) { return 2 << (kind - kVec2); }
+__host__ __device__ __forceinline__ int vec_rows(int kind) { return 4 * kWmBlock / vec_lanes(kind); }
+constexpr int kChunk = 4;  // units taken from the queue per atomic
+static_assert(kNumBatchKinds == TACOGB_MLP_KINDS, "the cost model predicts one output per kind");
 constexpr int kPartBlock = 256;
 
 struct BatchDesc {
@@ -72,7 +77,7 @@ __global__ void batch_partition(const BatchDesc* __restrict__ desc,
   __syncthreads();
   const BatchDesc& d = desc[s_m];
   const int64_t i = (int64_t)(blockIdx.x - d.blk0) * blockDim.x + threadIdx.x;
-  if (d.kind > kMerge3 || i > d.rows) return;
+  if (!is_merge(d.kind) || i > d.rows) return;
   int2* p = part + d.part0;
   if (i == d.rows) {
     p[d.units] = make_int2(d.rows, d.nnz);
@@ -85,17 +90,18 @@ __global__ void batch_partition(const BatchDesc* __restrict__ desc,
     p[b] = make_int2((int)i, (int)((uint64_t)b * T - (uint64_t)i));
 }
 
-// Rows [128*lu, 128*lu+128) of matrix d with G lanes per row.  Returns false when a checked
-// policy met a value it cannot represent (the caller redoes the unit natively).
+// Rows [R*lu, R*lu+R) of matrix d (R = 4*128/G) with G lanes per row and a shuffle butterfly.
+// Returns false when a checked policy met a value it cannot represent (the caller redoes the
+// unit natively).
 template <class P, int G>
 __device__ __forceinline__ bool batch_vector_unit(const BatchDesc& d, int lu,
                                                   const typename P::XG* __restrict__ x,
                                                   typename P::Out* __restrict__ y) {
   using Val = typename P::Val;
   const Val* __restrict__ vals = (const Val*)d.vals;
-  constexpr int GROUPS = kWmBlock / G;
+  constexpr int GROUPS = kWmBlock / G, R = 4 * GROUPS;
   const int g = threadIdx.x / G, lane = threadIdx.x % G;
-  const int rb = lu * kVecRows, re = min(d.rows, rb + kVecRows);
+  const int rb = lu * R, re = min(d.rows, rb + R);
   bool ok = true;
   for (int base = rb; base < re; base += GROUPS) {  // uniform trip count across the CTA
     const int row = base + g;
@@ -137,39 +143,63 @@ __device__ __forceinline__ void batch_vector_checked(const BatchDesc& d, int lu)
   }
 }
 
-// Persistent worker: CTAs take units from the queue until it runs dry.
+template <class P>
+__device__ __forceinline__ void batch_vector_any(const BatchDesc& d, int lu) {
+  switch (d.kind) {
+    case kVec2: batch_vector_checked<P, 2>(d, lu); break;
+    case kVec4: batch_vector_checked<P, 4>(d, lu); break;
+    case kVec8: batch_vector_checked<P, 8>(d, lu); break;
+    default: batch_vector_checked<P, 16>(d, lu); break;
+  }
+}
+
+// Persistent worker: CTAs take chunks of kChunk consecutive units from the queue until it runs
+// dry.  The next chunk's atomic is issued when a chunk starts and its result is only needed when
+// the chunk ends, so the queue round trip overlaps the work; within a chunk the matrix index
+// advances incrementally.  Thread 0 records each unit's duration in SM cycles (the autotuner's
+// cost measure: the CTA time a unit holds one of the resident slots).
 template <class P>
 __global__ void __launch_bounds__(kWmBlock, 8)
 batch_spmv_kernel(const BatchDesc* __restrict__ desc, const int32_t* __restrict__ unit_off,
                   int count, int32_t total, const int2* __restrict__ part,
                   int32_t* __restrict__ carry_row, double* __restrict__ carry_val,
-                  int* __restrict__ counter, int* status) {
+                  int* __restrict__ counter, long long* __restrict__ unit_cycles, int* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ int s_unit;
-  for (;;) {
-    if (threadIdx.x == 0) s_unit = atomicAdd(counter, 1);
-    __syncthreads();
-    const int u = s_unit;
-    __syncthreads();  // every thread holds u before thread 0 takes the next one
-    if (u >= total) break;
-    const int m = find_matrix(unit_off, count, u);
-    const BatchDesc d = desc[m];
-    const int lu = u - d.unit0;
-    if (d.kind == kMerge7 || d.kind == kMerge3) {
-      const int2* p = part + d.part0;
-      const int2 c0 = p[lu], c1 = p[lu + 1];
-      const double cd = d.kind == kMerge7 ? batch_merge_unit<P, 7>(smem_raw, d, c0, c1, status)
-                                          : batch_merge_unit<P, 3>(smem_raw, d, c0, c1, status);
-      if (threadIdx.x == 0) {
-        carry_row[u] = c1.x;
-        carry_val[u] = cd;
+  __shared__ int s_next;
+  if (threadIdx.x == 0) s_next = atomicAdd(counter, kChunk);
+  __syncthreads();
+  int c = s_next;
+  while (c < total) {
+    __syncthreads();  // every thread holds c before s_next is written again
+    int next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(counter, kChunk);
+    int m = find_matrix(unit_off, count, c);
+    const int cend = min(c + kChunk, total);
+    for (int u = c; u < cend; u++) {
+      const long long t0 = clock64();
+      while (u >= __ldg(unit_off + m + 1)) m++;
+      const BatchDesc d = desc[m];
+      const int lu = u - d.unit0;
+      if (is_merge(d.kind)) {
+        const int2* p = part + d.part0;
+        const int2 c0 = p[lu], c1 = p[lu + 1];
+        const double cd = d.kind == kMerge7 ? batch_merge_unit<P, 7>(smem_raw, d, c0, c1, status)
+                                            : batch_merge_unit<P, 3>(smem_raw, d, c0, c1, status);
+        if (threadIdx.x == 0) {
+          carry_row[u] = c1.x;
+          carry_val[u] = cd;
+        }
+      } else {
+        batch_vector_any<P>(d, lu);
+        if (threadIdx.x == 0) carry_row[u] = INT_MAX;
       }
-    } else {
-      if (d.kind == kVec4) batch_vector_checked<P, 4>(d, lu);
-      else batch_vector_checked<P, 16>(d, lu);
-      if (threadIdx.x == 0) carry_row[u] = INT_MAX;
+      if (threadIdx.x == 0) {
+        if (u == cend - 1) s_next = next;
+        unit_cycles[u] = clock64() - t0;
+      }
+      __syncthreads();  // shared memory is reused by the next unit; s_next is published
     }
-    __syncthreads();  // shared memory is reused by the next unit
+    c = s_next;
   }
 }
 
@@ -194,6 +224,20 @@ __global__ void batch_fixup(const BatchDesc* __restrict__ desc, const int32_t* _
   y[r] = (Out)((double)y[r] + tot);
 }
 
+// Per-matrix sum of the unit cycles of the last run (one warp per matrix).
+__global__ void batch_matrix_cycles(const BatchDesc* __restrict__ desc, int count,
+                                    const long long* __restrict__ unit_cycles,
+                                    long long* __restrict__ out) {
+  const int m = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (m >= count) return;
+  const BatchDesc& d = desc[m];
+  long long t = 0;
+  for (int u = lane; u < d.units; u += 32) t += unit_cycles[d.unit0 + u];
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) out[m] = t;
+}
+
 }  // namespace
 }  // namespace tacogb
 
@@ -212,6 +256,8 @@ struct tacogb_batch {
   int32_t* d_carry_row = nullptr;
   double* d_carry_val = nullptr;
   int* d_counter = nullptr;
+  long long* d_unit_cycles = nullptr;
+  long long* d_mat_cycles = nullptr;
   cudaStream_t cap = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -232,6 +278,8 @@ void batch_free(tacogb_batch* b) {
   cudaFree(b->d_carry_row);
   cudaFree(b->d_carry_val);
   cudaFree(b->d_counter);
+  cudaFree(b->d_unit_cycles);
+  cudaFree(b->d_mat_cycles);
   delete b;
 }
 
@@ -254,7 +302,7 @@ int batch_capture(tacogb_batch* b, int32_t total_blocks, int* status) {
   if (b->total_units > 0) {
     kern<<<grid, kWmBlock, smem, b->cap>>>(b->d_desc, b->d_unit_off, b->count, b->total_units,
                                            b->d_part, b->d_carry_row, b->d_carry_val,
-                                           b->d_counter, status);
+                                           b->d_counter, b->d_unit_cycles, status);
     b->kernels_per_run++;
   }
   batch_fixup<typename P::Out><<<(std::max(b->total_units, 1) + 255) / 256, 256, 0, b->cap>>>(
@@ -307,7 +355,7 @@ int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const
     int kind = variants ? variants[m] : kMerge7;
     TACOGB_CHECK_ARG(kind >= 0 && kind < kNumBatchKinds, "batch: matrix %d variant %d", m, kind);
     const bool aligned = (((uintptr_t)A.pos | (uintptr_t)A.crd | (uintptr_t)A.vals) & 15) == 0;
-    if (kind <= kMerge3 && !aligned) kind = kVec4;  // merge tiles are staged with bulk copies
+    if (is_merge(kind) && !aligned) kind = kVec4;  // merge tiles are staged with bulk copies
     BatchDesc& d = desc[m];
     d.pos = A.pos;
     d.crd = A.crd;
@@ -320,11 +368,11 @@ int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const
     d.kind = kind;
     d.tma = aligned;
     int64_t u = 0;
-    if (kind <= kMerge3) {
+    if (is_merge(kind)) {
       const int64_t T = kind_tile_items(kind);
       u = ((int64_t)A.rows + A.nnz + T - 1) / T;
     } else {
-      u = ((int64_t)A.rows + kVecRows - 1) / kVecRows;
+      u = ((int64_t)A.rows + vec_rows(kind) - 1) / vec_rows(kind);
     }
     d.unit0 = (int32_t)units;
     d.units = (int32_t)u;
@@ -333,7 +381,7 @@ int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const
     unit_off[m] = (int32_t)units;
     blk_off[m] = (int32_t)blocks;
     units += u;
-    if (kind <= kMerge3 && u > 0) {
+    if (is_merge(kind) && u > 0) {
       parts += u + 1;
       blocks += ((int64_t)A.rows + 1 + kPartBlock - 1) / kPartBlock;
     }
@@ -363,6 +411,11 @@ int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const
   if ((e = cudaMalloc(&b->d_carry_row, sizeof(int32_t) * std::max<int64_t>(units, 1))) != cudaSuccess) return fail(e, "carries");
   if ((e = cudaMalloc(&b->d_carry_val, sizeof(double) * std::max<int64_t>(units, 1))) != cudaSuccess) return fail(e, "carries");
   if ((e = cudaMalloc(&b->d_counter, sizeof(int))) != cudaSuccess) return fail(e, "queue");
+  if ((e = cudaMalloc(&b->d_unit_cycles, sizeof(long long) * std::max<int64_t>(units, 1))) != cudaSuccess)
+    return fail(e, "unit cycles");
+  if ((e = cudaMalloc(&b->d_mat_cycles, sizeof(long long) * count)) != cudaSuccess)
+    return fail(e, "matrix cycles");
+  cudaMemset(b->d_unit_cycles, 0, sizeof(long long) * std::max<int64_t>(units, 1));
   cudaMemcpy(b->d_desc, desc.data(), sizeof(BatchDesc) * count, cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_unit_off, unit_off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_blk_off, blk_off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice);
@@ -383,6 +436,19 @@ int tacogb_batch_run(tacogb_batch* b, void* stream) {
   TACOGB_CHECK_ARG(b != nullptr && b->exec != nullptr, "batch: null plan");
   TACOGB_CUDA_TRY(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
   for (int k = 0; k < b->kernels_per_run; k++) count_launch();
+  return 0;
+}
+
+int tacogb_batch_matrix_cycles(tacogb_batch* b, int64_t* cycles, void* stream) {
+  TACOGB_CHECK_ARG(b != nullptr && b->exec != nullptr && cycles != nullptr, "batch: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  batch_matrix_cycles<<<(b->count * 32 + 255) / 256, 256, 0, st>>>(b->d_desc, b->count,
+                                                                     b->d_unit_cycles, b->d_mat_cycles);
+  count_launch();
+  TACOGB_CUDA_TRY(cudaGetLastError());
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(cycles, b->d_mat_cycles, sizeof(long long) * b->count,
+                                  cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
   return 0;
 }
 

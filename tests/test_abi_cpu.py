@@ -98,7 +98,7 @@ def test_batch_plan_rejects_bad_arguments_without_gpu():
     """tacogb_batch_create validates the whole batch on the host before touching the GPU."""
     L = tg.lib()
     assert [L.tacogb_batch_variant_name(i) for i in range(L.tacogb_batch_variant_count())] == \
-        [b"merge_ipt7", b"merge_ipt3", b"vector_g4", b"vector_g16"]
+        [b"merge_ipt7", b"merge_ipt3", b"vector_g2", b"vector_g4", b"vector_g8", b"vector_g16"]
     h = ctypes.c_void_p()
     assert L.tacogb_batch_create(0, None, None, None, 0, None, ctypes.byref(h)) == 1
     assert b"empty" in L.tacogb_last_error() and not h.value

@@ -120,9 +120,9 @@ def test_unaligned_arrays_fall_back_to_vector_units(generated):
     planned as vector units for them and the results stay exact."""
     mats, xs, ys, refs = [], [], [], []
     for m, (pos, crd, vals, cols) in enumerate(generated[:6]):
-        p = torch.from_numpy(np.concatenate([[0], pos])).cuda()[1:]  # offset by 4 bytes
-        c = torch.from_numpy(np.concatenate([[0], crd])).cuda()[1:]
-        v = torch.from_numpy(np.concatenate([[0.0], vals])).cuda()[1:]
+        p = torch.from_numpy(np.concatenate([pos[:1], pos])).cuda()[1:]  # offset by 4 bytes
+        c = torch.from_numpy(np.concatenate([pos[:1], crd])).cuda()[1:]
+        v = torch.from_numpy(np.concatenate([vals[:1], vals])).cuda()[1:]
         mats.append(tg.CsrMatrix(p, c, v, cols))
         x = W.dense(200 + m, cols)
         xs.append(torch.from_numpy(x).cuda())
@@ -158,5 +158,5 @@ def test_double_float_out_of_range_tiles(generated):
     for t in sub[::2]:
         t[2] = t[2].copy()
         t[2][: max(1, len(t[2]) // 4)] *= 2.0 ** 70
-    ys, xs = _run([tuple(t) for t in sub], torch.float64, 0, [m % 4 for m in range(len(sub))])
+    ys, xs = _run([tuple(t) for t in sub], torch.float64, 0, [m % len(KINDS) for m in range(len(sub))])
     _check([tuple(t) for t in sub], ys, xs, F64_TOL)
