@@ -46,16 +46,19 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="spmv_powerlaw",
                    choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
-                            "batched_spmv"])
+                            "batched_spmv", "batched_spmm"])
     p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
     p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
                    help="how batched_spmv picks each matrix's work-unit kind")
     p.add_argument("--dtype", default="f64", choices=["f64", "f32", "bf16"])
-    p.add_argument("--n", type=int, default=64, help="dense columns of B for SpMM")
+    p.add_argument("--n", type=int, default=None,
+                   help="dense columns of B for SpMM (default 64; 32 for batched_spmm)")
     p.add_argument("--variant", type=int, default=-1)
     p.add_argument("--e2e-steps", type=int, default=30)
     p.add_argument("--no-cpu", action="store_true")
     a = p.parse_args()
+    if a.n is None:
+        a.n = 32 if a.workload == "batched_spmm" else 64
     if a.workload.startswith("spmv") and a.dtype == "bf16":
         p.error("bf16 applies to SpMM's dense operand only")
     return a
@@ -321,9 +324,85 @@ class BatchOp:
         return ("reference" if ref else "port"), once, keep
 
 
+class BatchSpmmOp(BatchOp):
+    """The batched_spmv matrices with a dense B_m (cols x N, row-major, U(-1,1)) per matrix:
+    C_m = A_m B_m for all m per step.  Metric: GFLOP/s = sum_m 2*N*nnz_m per step."""
+
+    def __init__(self, args):
+        super().__init__(args)
+        self.N = args.n
+        self.metric = "batched_spmm_n%d_%s_gflops" % (self.N, args.dtype if args.dtype != "f32"
+                                                          else "f32c")
+        self.workload = "batched_spmm_%d_n%d" % (self.count, self.N)
+
+    def upload(self, torch):
+        dev = super().upload(torch)
+        N, total = self.N, int(self.off[-1])
+        g = torch.Generator(device="cuda")
+        g.manual_seed(43)
+        dev["B64"] = torch.rand(total, N, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+        dev["Bl"] = dev["B64"].to(torch.bfloat16 if self.args.dtype == "bf16" else torch.float32)
+        dev["C64"] = torch.empty(total, N, dtype=torch.float64, device="cuda")
+        dev["Cl"] = torch.empty(total, N, dtype=torch.float32, device="cuda")
+        sa = 8 if self.args.dtype == "f64" else 4
+        sb = ESZ[self.args.dtype]
+        self.bytes = self.nnz * (4 + sa) + sum(4 * (s.rows + 1) + (sb + sa) * N * s.rows
+                                               for s in self.specs)
+        self.flops = 2 * N * self.nnz
+        return dev
+
+    def operands(self, tg, dev, low):
+        vk, bk, ck = ("v32", "Bl", "Cl") if low else ("v64", "B64", "C64")
+        mats, Bs, Cs = [], [], []
+        for m, s in enumerate(self.specs):
+            mats.append(tg.CsrMatrix(dev["pos"][m], dev["crd"][m], dev[vk][m], s.cols))
+            a, b = int(self.off[m]), int(self.off[m + 1])
+            Bs.append(dev[bk][a:b])
+            Cs.append(dev[ck][a:b])
+        return mats, Bs, Cs
+
+    def cpu(self):
+        """taco's generated SpMM called once per matrix on the first matrices of the batch up to
+        about 5e7 nonzeros (N = 32 dense columns)."""
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        from taco_gb300 import workloads as W
+        keep, calls, nnz, rows, N = [], [], 0, 0, self.N
+        ref = O.ref_available("spmm")
+        L = O.ref_lib("spmm") if ref else O.lib()
+        for m, s in enumerate(self.specs):
+            if nnz > 5e7:
+                break
+            pos, crd, vals = W.generate(s)
+            B = W.dense(41 + m, s.cols * N).reshape(s.cols, N)
+            C = np.empty((s.rows, N))
+            if ref:
+                At = T.csr(pos, crd, vals, [s.rows, s.cols])
+                Bt, Ct = T.dense(B, [s.cols, N]), T.dense(C, [s.rows, N])
+                keep.append((At, Bt, Ct, pos, crd, vals, B, C))
+                calls.append(lambda At=At, Bt=Bt, Ct=Ct: L.compute(Ct.ptr, At.ptr, Bt.ptr))
+            else:
+                keep.append((pos, crd, vals, B, C))
+                calls.append(lambda s=s, pos=pos, crd=crd, vals=vals, B=B, C=C: L.oracle_spmm_f64(
+                    s.rows, N, pos.ctypes.data, crd.ctypes.data, vals.ctypes.data, B.ctypes.data,
+                    C.ctypes.data))
+            nnz += len(crd)
+            rows += s.rows
+        self.cpu_units = 2 * N * nnz
+        self.cpu_sample = "first %d of %d matrices (%d rows, %d nnz, N=%d), FP64" % (
+            len(calls), self.count, rows, nnz, N)
+
+        def once():
+            for c in calls:
+                c()
+        return ("reference" if ref else "port"), once, keep
+
+
 def make_op(args):
     if args.workload == "batched_spmv":
         return BatchOp(args)
+    if args.workload == "batched_spmm":
+        return BatchSpmmOp(args)
     return SpmmOp(args) if args.workload.startswith("spmm") else SpmvOp(args)
 
 
@@ -588,6 +667,103 @@ def main_batch(args, torch, tg, T, L, rank, world):
     plan.close()
 
 
+def main_batch_spmm(args, torch, tg, L, rank):
+    """Batched SpMM: one graph launch per step over all matrices, against one plain FP64
+    tacogb_spmm call per matrix on the same matrices."""
+    op = make_op(args)
+    dev = op.upload(torch)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    low = args.dtype != "f64"
+    mats, Bs, Cs = op.operands(tg, dev, low)
+    plan = tg.SpmmBatch(mats, Bs, Cs, precision=0)
+    for _ in range(max(3, args.warmup)):
+        plan.run(stream)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(0) if rank == 0 else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = L.tacogb_launch_count()
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.run(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = L.tacogb_launch_count() - launches0
+    clocks = sampler.stop() if sampler else None
+    ms = e0.elapsed_time(e1) / args.steps
+    status = ctypes.c_int32(0)
+    L.tacogb_device_status(ctypes.byref(status))
+    if status.value:
+        raise RuntimeError("device status %d after the timed region" % status.value)
+
+    m64, B64, C64 = op.operands(tg, dev, False)
+    csrs = [A.as_csr() for A in m64]
+    native = tg.spmm_variants().index("merge_w512_native")
+
+    def per_matrix():
+        for c, B, C in zip(csrs, B64, C64):
+            rc = L.tacogb_spmm(ctypes.byref(c), op.N, B.data_ptr(), tg.TACOGB_F64, C.data_ptr(),
+                               native, sp)
+            if rc:
+                raise RuntimeError(L.tacogb_last_error().decode())
+    for _ in range(2):
+        per_matrix()
+    torch.cuda.synchronize()
+    k64 = max(2, min(args.steps, 5))
+    e0.record(stream)
+    for _ in range(k64):
+        per_matrix()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / k64
+
+    plan.run(stream)
+    torch.cuda.synchronize()
+    errs = []
+    key = "Cl" if low else "C64"
+    for m in range(op.count):
+        a, b = int(op.off[m]), int(op.off[m + 1])
+        ref = dev["C64"][a:b]
+        den = float(ref.abs().max()) if b > a else 0.0
+        if den == 0.0:
+            continue
+        d = (dev[key][a:b].double() - ref) / den
+        errs.append(float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref / den)))
+    max_err = max(errs) if errs else 0.0
+
+    cpu = None
+    if not args.no_cpu:
+        kind, cores, t, reps = time_cpu(op, budget_s=10.0)
+        cpu = {"value": op.cpu_units / t / 1e9, "unit": "GFLOP/s", "cores": cores, "kind": kind,
+               "sample": op.cpu_sample + ", median of %d reps" % reps, "ms_per_step": t * 1e3}
+    peak, peak_kind = measured_peak()
+    achieved = op.bytes / (ms / 1e3) / 1e9
+    out = {"metric": op.metric, "value": op.flops / (ms / 1e3) / 1e9, "unit": "GFLOP/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": {"f64": "f64", "f32": "f32c", "bf16": "bf16b_f32"}[args.dtype],
+           "data": "synthetic",
+           "config": {"workload": op.workload, "matrices": op.count, "rows": op.rows,
+                      "nnz": op.nnz, "n": op.N, "bytes_per_step": op.bytes,
+                      "l2": "inputs larger than L2 (%.1f GB per step), no flush" % (op.bytes / 1e9)},
+           "fp64_per_matrix": {"gflops": op.flops / (ms64 / 1e3) / 1e9, "ms_per_step": ms64,
+                               "launch": "tacogb_spmm merge_w512_native FP64, one call per "
+                                         "matrix from a host loop", "steps": k64},
+           "speedup_vs_fp64_per_matrix": ms64 / ms,
+           "max_normwise_err_vs_fp64": max_err,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak,
+                        "traffic": ncu_traffic("batch_spmm_kernel", op.workload),
+                        "kernel": "batch_spmm_kernel (graph: partition + queue + fix-up)",
+                        "kernel_ms": ms, "peak_source": peak_kind},
+           "cpu_baseline": cpu, "e2e": None, "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(out), flush=True)
+    plan.close()
+
+
 # ----------------------------------------------------------------------------- main
 
 def main():
@@ -609,6 +785,9 @@ def main():
 
     if args.workload == "batched_spmv":
         main_batch(args, torch, tg, T, L, rank, world)
+        return
+    if args.workload == "batched_spmm":
+        main_batch_spmm(args, torch, tg, L, rank)
         return
     op = make_op(args)
     stream = torch.cuda.current_stream()

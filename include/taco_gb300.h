@@ -124,6 +124,15 @@ typedef struct tacogb_batch tacogb_batch;
 int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const* x,
                         void* const* y, int32_t precision, const int32_t* variants,
                         tacogb_batch** plan);
+/* Batched SpMM: C_m = A_m B_m with B_m (A_m->cols x N) and C_m (A_m->rows x N) dense row-major,
+ * N shared by the batch; value types as tacogb_spmm (F64/F64, F32/F32, F32 values with BF16 B).
+ * Units are row-snapped merge tiles of 512 items; every warp of the persistent kernel takes
+ * units from the queue.  precision 0 = double-float (F64) or compensated FP32 accumulation,
+ * 1 = native FMA; BF16 B always accumulates in FP32.  Run, cost and destroy with the
+ * tacogb_batch_* calls below. */
+int tacogb_batch_spmm_create(int32_t count, const tacogb_csr* mats, int32_t N,
+                             const void* const* B, int32_t btype, void* const* C,
+                             int32_t precision, tacogb_batch** plan);
 int tacogb_batch_run(tacogb_batch* plan, void* stream);
 int tacogb_batch_destroy(tacogb_batch* plan);
 /* Cost of each matrix in the last run of the plan: the sum over its work units of the SM cycles

@@ -10,7 +10,7 @@ from . import _native
 from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBError, check,
                       lib)
 
-__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "SpmvBatch",
+__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "SpmvBatch", "SpmmBatch",
            "batch_variants", "lib", "check", "TacoGBError",
            "TACOGB_F64", "TACOGB_F32", "TACOGB_BF16", "VARIANT_AUTO"]
 
@@ -93,26 +93,19 @@ def spmv_variants():
     return [L.tacogb_spmv_variant_name(i).decode() for i in range(L.tacogb_spmv_variant_count())]
 
 
-class SpmvBatch:
-    """A plan for y_m = A_m x_m over many CsrMatrix objects, run as one CUDA-graph launch
-    (tacogb_batch_create / tacogb_batch_run).  variants[m] names how matrix m is cut into work
-    units (an index into batch_variants()); precision 1 selects native FP64 accumulation."""
-
-    def __init__(self, mats, xs, ys, precision=0, variants=None):
-        n = len(mats)
-        if not (n == len(xs) == len(ys)):
-            raise ValueError("mats, xs and ys differ in length")
-        self._keep = (list(mats), list(xs), list(ys))
-        csr = (_native.Csr * n)(*[A.as_csr() for A in mats])
-        xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
-        yp = (ctypes.c_void_p * n)(*[y.data_ptr() for y in ys])
-        var = None if variants is None else (ctypes.c_int32 * n)(*[int(v) for v in variants])
-        self._h = ctypes.c_void_p()
-        check(lib().tacogb_batch_create(n, csr, xp, yp, precision, var, ctypes.byref(self._h)),
-              "tacogb_batch_create")
+class _BatchPlan:
+    _h = None
 
     def run(self, stream=None):
         check(lib().tacogb_batch_run(self._h, _stream_ptr(stream)), "tacogb_batch_run")
+
+    def matrix_cycles(self, stream=None):
+        """Per-matrix SM cycles of the last run (the autotuner's cost measure)."""
+        import numpy as np
+        out = np.empty(self.count, dtype=np.int64)
+        check(lib().tacogb_batch_matrix_cycles(self._h, out.ctypes.data, _stream_ptr(stream)),
+              "tacogb_batch_matrix_cycles")
+        return out
 
     def close(self):
         if self._h:
@@ -124,6 +117,44 @@ class SpmvBatch:
             self.close()
         except Exception:
             pass
+
+
+class SpmvBatch(_BatchPlan):
+    """A plan for y_m = A_m x_m over many CsrMatrix objects, run as one CUDA-graph launch
+    (tacogb_batch_create / tacogb_batch_run).  variants[m] names how matrix m is cut into work
+    units (an index into batch_variants()); precision 1 selects native FP64 accumulation."""
+
+    def __init__(self, mats, xs, ys, precision=0, variants=None):
+        n = self.count = len(mats)
+        if not (n == len(xs) == len(ys)):
+            raise ValueError("mats, xs and ys differ in length")
+        self._keep = (list(mats), list(xs), list(ys))
+        csr = (_native.Csr * n)(*[A.as_csr() for A in mats])
+        xp = (ctypes.c_void_p * n)(*[x.data_ptr() for x in xs])
+        yp = (ctypes.c_void_p * n)(*[y.data_ptr() for y in ys])
+        var = None if variants is None else (ctypes.c_int32 * n)(*[int(v) for v in variants])
+        self._h = ctypes.c_void_p()
+        check(lib().tacogb_batch_create(n, csr, xp, yp, precision, var, ctypes.byref(self._h)),
+              "tacogb_batch_create")
+
+
+class SpmmBatch(_BatchPlan):
+    """A plan for C_m = A_m B_m over many CsrMatrix objects with dense row-major B_m (cols x N)
+    and C_m (rows x N), N shared, run as one CUDA-graph launch (tacogb_batch_spmm_create)."""
+
+    def __init__(self, mats, Bs, Cs, precision=0):
+        n = self.count = len(mats)
+        if not (n == len(Bs) == len(Cs)):
+            raise ValueError("mats, Bs and Cs differ in length")
+        N = int(Bs[0].shape[1])
+        self._keep = (list(mats), list(Bs), list(Cs))
+        csr = (_native.Csr * n)(*[A.as_csr() for A in mats])
+        bp = (ctypes.c_void_p * n)(*[b.data_ptr() for b in Bs])
+        cp = (ctypes.c_void_p * n)(*[c.data_ptr() for c in Cs])
+        self._h = ctypes.c_void_p()
+        check(lib().tacogb_batch_spmm_create(n, csr, N, bp, _BTYPE[Bs[0].element_size()], cp,
+                                             precision, ctypes.byref(self._h)),
+              "tacogb_batch_spmm_create")
 
 
 def batch_variants():

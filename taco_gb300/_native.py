@@ -79,6 +79,8 @@ SIGNATURES = {
     "_shim_tacogb_spmv_compute": (I32, [P]),
     "_shim_tacogb_spmv_evaluate": (I32, [P]),
     "tacogb_batch_create": (I32, [I32, ctypes.POINTER(Csr), P, P, I32, P, ctypes.POINTER(P)]),
+    "tacogb_batch_spmm_create": (I32, [I32, ctypes.POINTER(Csr), I32, P, I32, P, I32,
+                                        ctypes.POINTER(P)]),
     "tacogb_batch_run": (I32, [P, P]),
     "tacogb_batch_destroy": (I32, [P]),
     "tacogb_batch_matrix_cycles": (I32, [P, P, P]),

@@ -29,239 +29,9 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.h"
+#include "spmm_tile.cuh"
 
 namespace tacogb {
-
-// ------------------------------------------------------------------ vector I/O -----------
-
-template <int VEC>
-__device__ __forceinline__ void load_vec(const double* p, double (&o)[VEC]) {
-  if constexpr (VEC == 2) {
-    const double2 v = __ldg(reinterpret_cast<const double2*>(p));
-    o[0] = v.x;
-    o[1] = v.y;
-  } else {
-    static_assert(VEC == 1, "double vectors are 1 or 2 wide");
-    o[0] = __ldg(p);
-  }
-}
-
-template <int VEC>
-__device__ __forceinline__ void load_vec(const float* p, float (&o)[VEC]) {
-  if constexpr (VEC == 4) {
-    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
-    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-  } else if constexpr (VEC == 2) {
-    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
-    o[0] = v.x; o[1] = v.y;
-  } else {
-    static_assert(VEC == 1, "float vectors are 1, 2 or 4 wide");
-    o[0] = __ldg(p);
-  }
-}
-
-__device__ __forceinline__ float bf16_lo(unsigned int w) { return __uint_as_float(w << 16); }
-__device__ __forceinline__ float bf16_hi(unsigned int w) { return __uint_as_float(w & 0xFFFF0000u); }
-
-template <int VEC>
-__device__ __forceinline__ void load_vec(const __nv_bfloat16* p, float (&o)[VEC]) {
-  if constexpr (VEC == 8) {
-    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-    o[0] = bf16_lo(v.x); o[1] = bf16_hi(v.x); o[2] = bf16_lo(v.y); o[3] = bf16_hi(v.y);
-    o[4] = bf16_lo(v.z); o[5] = bf16_hi(v.z); o[6] = bf16_lo(v.w); o[7] = bf16_hi(v.w);
-  } else if constexpr (VEC == 4) {
-    const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
-    o[0] = bf16_lo(v.x); o[1] = bf16_hi(v.x); o[2] = bf16_lo(v.y); o[3] = bf16_hi(v.y);
-  } else if constexpr (VEC == 2) {
-    const unsigned int v = __ldg(reinterpret_cast<const unsigned int*>(p));
-    o[0] = bf16_lo(v); o[1] = bf16_hi(v);
-  } else {
-    static_assert(VEC == 1, "bf16 vectors are 1, 2, 4 or 8 wide");
-    o[0] = bf16_lo((unsigned int)__ldg(reinterpret_cast<const unsigned short*>(p)));
-  }
-}
-
-template <int VEC>
-__device__ __forceinline__ void store_vec(double* p, const double (&o)[VEC]) {
-  if constexpr (VEC == 2) *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
-  else p[0] = o[0];
-}
-
-template <int VEC>
-__device__ __forceinline__ void store_vec(float* p, const float (&o)[VEC]) {
-  if constexpr (VEC == 8) {
-    reinterpret_cast<float4*>(p)[0] = make_float4(o[0], o[1], o[2], o[3]);
-    reinterpret_cast<float4*>(p)[1] = make_float4(o[4], o[5], o[6], o[7]);
-  } else if constexpr (VEC == 4) {
-    *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
-  } else if constexpr (VEC == 2) {
-    *reinterpret_cast<float2*>(p) = make_float2(o[0], o[1]);
-  } else {
-    p[0] = o[0];
-  }
-}
-
-// ------------------------------------------------------------------ policies -------------
-
-struct MmNative64 {
-  using AV = double;  // A value
-  using BV = double;  // B element in memory
-  using BE = double;  // B element in registers
-  using Prep = double;
-  using Acc = double;
-  using Out = double;
-  static constexpr bool kChecked = false;
-  __device__ static Prep prep(AV a, bool&) { return a; }
-  __device__ static Prep shfl(Prep a, int src) { return __shfl_sync(0xffffffffu, a, src); }
-  __device__ static Acc zero() { return 0.0; }
-  __device__ static void madd(Acc& acc, Prep a, BE b, bool&) { acc = __fma_rn(a, b, acc); }
-  __device__ static Out out(Acc a) { return a; }
-  __device__ static double to_double(Acc a) { return a; }
-};
-
-struct MmDF64 {
-  using AV = double;
-  using BV = double;
-  using BE = double;
-  using Prep = DF;
-  using Acc = DF;
-  using Out = double;
-  static constexpr bool kChecked = true;
-  __device__ static Prep prep(AV a, bool& ok) {
-    DF p;
-    ok &= split_df(a, p.h, p.l);
-    return p;
-  }
-  __device__ static Prep shfl(Prep a, int src) {
-    return DF{__shfl_sync(0xffffffffu, a.h, src), __shfl_sync(0xffffffffu, a.l, src)};
-  }
-  __device__ static Acc zero() { return DF{0.f, 0.f}; }
-  __device__ static void madd(Acc& acc, Prep a, BE b, bool& ok) {
-    float bh, bl;
-    ok &= split_df(b, bh, bl);
-    acc = df_add(acc, df_mul(a.h, a.l, bh, bl));
-  }
-  __device__ static Out out(Acc a) { return df_to_double(a); }
-  __device__ static double to_double(Acc a) { return df_to_double(a); }
-};
-
-struct MmF32 {
-  using AV = float;
-  using BV = float;
-  using BE = float;
-  using Prep = float;
-  using Acc = float;
-  using Out = float;
-  static constexpr bool kChecked = false;
-  __device__ static Prep prep(AV a, bool&) { return a; }
-  __device__ static Prep shfl(Prep a, int src) { return __shfl_sync(0xffffffffu, a, src); }
-  __device__ static Acc zero() { return 0.f; }
-  __device__ static void madd(Acc& acc, Prep a, BE b, bool&) { acc = __fmaf_rn(a, b, acc); }
-  __device__ static Out out(Acc a) { return a; }
-  __device__ static double to_double(Acc a) { return (double)a; }
-};
-
-struct MmComp32 : MmF32 {
-  using Acc = DF;
-  __device__ static Acc zero() { return DF{0.f, 0.f}; }
-  __device__ static void madd(Acc& acc, Prep a, BE b, bool&) {
-    DF p;
-    p.h = __fmul_rn(a, b);
-    p.l = __fmaf_rn(a, b, -p.h);
-    acc = df_add(acc, p);
-  }
-  __device__ static Out out(Acc a) { return __fadd_rn(a.h, a.l); }
-  __device__ static double to_double(Acc a) { return (double)a.h + (double)a.l; }
-};
-
-struct MmBF16 : MmF32 {
-  using BV = __nv_bfloat16;
-};
-
-// ------------------------------------------------------------------ kernel ---------------
-
-constexpr int kMmBlock = 256;
-constexpr int kMmWarps = kMmBlock / 32;
-constexpr int kMmUnroll = 4;
-
-// One warp: rows of merge tile `tile`, columns [col0, col0+VEC) per lane.  Returns false when a
-// checked policy met an unrepresentable value (the caller then redoes the tile natively).
-template <class P, int VEC>
-__device__ __forceinline__ bool spmm_tile(const int32_t* __restrict__ pos,
-                                          const int32_t* __restrict__ crd,
-                                          const typename P::AV* __restrict__ vals,
-                                          const typename P::BV* __restrict__ B,
-                                          typename P::Out* __restrict__ C, int32_t n, int32_t N,
-                                          int2 c0, int2 c1, int tile, int col0, bool active,
-                                          int32_t* __restrict__ carry_row,
-                                          double* __restrict__ carry_val) {
-  using Acc = typename P::Acc;
-  using Prep = typename P::Prep;
-  using BE = typename P::BE;
-  const int lane = threadIdx.x & 31;
-  const int r0 = c0.x, k0 = c0.y, r1 = c1.x, k1 = c1.y;
-  bool ok = true;
-  bool carried = false;
-  for (int r = r0; r <= r1 && r < n; r++) {
-    const int ps = (r == r0) ? k0 : __ldg(pos + r);
-    const int pe = (r < r1) ? __ldg(pos + r + 1) : k1;
-    Acc acc[VEC];
-#pragma unroll
-    for (int v = 0; v < VEC; v++) acc[v] = P::zero();
-    for (int base = ps; base < pe; base += 32) {
-      const int cnt = min(32, pe - base);
-      int mc = 0;
-      Prep ma = Prep();
-      if (lane < cnt) {
-        mc = ld_stream_i32(crd + base + lane);
-        ma = P::prep(vals[base + lane], ok);
-      }
-      int j = 0;
-      for (; j + kMmUnroll <= cnt; j += kMmUnroll) {
-        BE b[kMmUnroll][VEC];
-#pragma unroll
-        for (int u = 0; u < kMmUnroll; u++) {
-          const int c = __shfl_sync(0xffffffffu, mc, j + u);
-          if (active) load_vec<VEC>(B + (int64_t)c * N + col0, b[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < kMmUnroll; u++) {
-          const Prep a = P::shfl(ma, j + u);
-          if (active) {
-#pragma unroll
-            for (int v = 0; v < VEC; v++) P::madd(acc[v], a, b[u][v], ok);
-          }
-        }
-      }
-      for (; j < cnt; j++) {
-        const int c = __shfl_sync(0xffffffffu, mc, j);
-        const Prep a = P::shfl(ma, j);
-        if (active) {
-          BE b[VEC];
-          load_vec<VEC>(B + (int64_t)c * N + col0, b);
-#pragma unroll
-          for (int v = 0; v < VEC; v++) P::madd(acc[v], a, b[v], ok);
-        }
-      }
-    }
-    if (r < r1) {
-      if (active) {
-        typename P::Out o[VEC];
-#pragma unroll
-        for (int v = 0; v < VEC; v++) o[v] = P::out(acc[v]);
-        store_vec<VEC>(C + (int64_t)r * N + col0, o);
-      }
-    } else if (pe > ps) {
-      carried = true;
-      if (active) {
-#pragma unroll
-        for (int v = 0; v < VEC; v++) carry_val[(int64_t)tile * N + col0 + v] = P::to_double(acc[v]);
-      }
-    }
-  }
-  if (lane == 0 && blockIdx.y == 0) carry_row[tile] = carried ? r1 : n;
-  return ok;
-}
 
 template <class P, int VEC>
 __global__ void __launch_bounds__(kMmBlock, 3)
