@@ -20,7 +20,8 @@ INC = os.path.join(ROOT, "include")
 LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "lib", "obj")
 
-CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu", "spgemm.cu", "batched.cu", "tuner.cu"]
+CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu", "spgemm.cu", "batched.cu", "batched_spmm.cu",
+              "tuner.cu"]
 PATTERNS = ["spmv", "spmm", "spgemm"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 NVCC_FLAGS = [

@@ -23,7 +23,7 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.h"
-#include "spmm_tile.cuh"
+#include "batched.cuh"
 #include "wmerge.cuh"
 
 namespace tacogb {
@@ -39,62 +39,12 @@ __host__ __device__ __forceinline__ int vec_lanes(int kind) { return 2 << (kind 
 __host__ __device__ __forceinline__ int vec_rows(int kind) { return 4 * kWmBlock / vec_lanes(kind); }
 constexpr int kChunk = 4;  // units taken from the queue per atomic
 static_assert(kNumBatchKinds == TACOGB_MLP_KINDS, "the cost model predicts one output per kind");
-constexpr int kPartBlock = 256;
 
-struct BatchDesc {
-  const int32_t* pos;
-  const int32_t* crd;
-  const void* vals;
-  const void* x;
-  void* y;
-  int32_t rows, cols, nnz, kind;
-  int32_t unit0, units;  // global unit range
-  int32_t part0;         // first merge-partition entry (merge kinds: units + 1 entries)
-  int32_t blk0;          // first block of the partition kernel (merge kinds)
-  int32_t tma;           // 1 when pos/crd/vals are 16-byte aligned (required by merge kinds)
-  int32_t tile;          // merge-tile items (0: not merge-partitioned)
-  int32_t snap;          // rows shorter than this are never split between tiles (0: none)
-};
-
-// Largest m in [0, count) with off[m] <= u.
-__device__ __forceinline__ int find_matrix(const int32_t* __restrict__ off, int count, int32_t u) {
-  int lo = 0, hi = count - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(off + mid) <= u) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
 
 __host__ __device__ __forceinline__ int64_t kind_tile_items(int kind) {
   return kind == kMerge7 ? (int64_t)kWmBlock * 7 : (int64_t)kWmBlock * 3;
 }
 
-// Merge-tile boundaries of every merge-kind matrix (the scatter partition of the single-matrix
-// path, one block range per matrix).
-__global__ void batch_partition(const BatchDesc* __restrict__ desc,
-                                const int32_t* __restrict__ blk_off, int count,
-                                int2* __restrict__ part) {
-  __shared__ int s_m;
-  if (threadIdx.x == 0) s_m = find_matrix(blk_off, count, blockIdx.x);
-  __syncthreads();
-  const BatchDesc& d = desc[s_m];
-  const int64_t i = (int64_t)(blockIdx.x - d.blk0) * blockDim.x + threadIdx.x;
-  if (d.tile == 0 || i > d.rows) return;
-  int2* p = part + d.part0;
-  if (i == d.rows) {
-    p[d.units] = make_int2(d.rows, d.nnz);
-    return;
-  }
-  const uint32_t T = (uint32_t)d.tile;
-  const int32_t p0 = __ldg(d.pos + i), p1 = __ldg(d.pos + i + 1);
-  const uint32_t lo = (uint32_t)p0 + (uint32_t)i;
-  const uint32_t hi = (uint32_t)p1 + (uint32_t)i;
-  const bool snap = (p1 - p0) < d.snap;
-  for (uint32_t b = lo / T + (lo % T != 0); (uint64_t)b * T <= hi && (int32_t)b < d.units; b++)
-    p[b] = (snap && b > 0) ? make_int2((int)i + 1, p1)
-                           : make_int2((int)i, (int)((uint64_t)b * T - (uint64_t)i));
-}
 
 // Rows [R*lu, R*lu+R) of matrix d (R = 4*128/G) with G lanes per row and a shuffle butterfly.
 // Returns false when a checked policy met a value it cannot represent (the caller redoes the
@@ -230,96 +180,6 @@ __global__ void batch_fixup(const BatchDesc* __restrict__ desc, const int32_t* _
   y[r] = (Out)((double)y[r] + tot);
 }
 
-// ------------------------------------------------------------------ batched SpMM ---------
-//
-// C_m = A_m B_m for every matrix (B_m: cols x N, C_m: rows x N, dense row-major).  Units are the
-// row-snapped merge tiles of the single-matrix SpMM (kMmBatchTile items; rows shorter than half a
-// tile are never split), and every warp is an independent worker that takes chunks of units from
-// the queue and runs the single-matrix warp tile on each, column tile by column tile.  Split
-// rows are fixed up in unit order.
-
-constexpr int kMmBatchBlock = 256;
-constexpr int kMmBatchTile = 512;
-constexpr int kMmChunk = 4;
-
-template <class P, int VEC>
-__device__ __forceinline__ void batch_spmm_unit(const BatchDesc& d, int32_t N, int2 c0, int2 c1,
-                                                int u, int32_t* carry_row, double* carry_val) {
-  using AV = typename P::AV;
-  using BV = typename P::BV;
-  using Out = typename P::Out;
-  const int lane = threadIdx.x & 31;
-  for (int ct = 0; ct < N; ct += 32 * VEC) {
-    const int col0 = ct + lane * VEC;
-    const bool active = col0 < N;
-    const bool ok = spmm_tile<P, VEC>(d.pos, d.crd, (const AV*)d.vals, (const BV*)d.x, (Out*)d.y,
-                                      d.rows, N, c0, c1, u, col0, active, carry_row, carry_val);
-    if constexpr (P::kChecked) {
-      if (!__all_sync(0xffffffffu, ok))
-        spmm_tile<MmNative64, VEC>(d.pos, d.crd, (const double*)d.vals, (const double*)d.x,
-                                   (double*)d.y, d.rows, N, c0, c1, u, col0, active, carry_row,
-                                   carry_val);
-    }
-  }
-}
-
-template <class P, int VEC>
-__global__ void __launch_bounds__(kMmBatchBlock, 3)
-batch_spmm_kernel(const BatchDesc* __restrict__ desc, const int32_t* __restrict__ unit_off,
-                  int count, int32_t total, int32_t N, const int2* __restrict__ part,
-                  int32_t* __restrict__ carry_row, double* __restrict__ carry_val,
-                  int32_t* __restrict__ unit_mat, int* __restrict__ counter,
-                  long long* __restrict__ unit_cycles) {
-  const int lane = threadIdx.x & 31;
-  int c = 0;
-  if (lane == 0) c = atomicAdd(counter, kMmChunk);
-  c = __shfl_sync(0xffffffffu, c, 0);
-  while (c < total) {
-    int next = 0;
-    if (lane == 0) next = atomicAdd(counter, kMmChunk);  // needed only when this chunk ends
-    int m = find_matrix(unit_off, count, c);
-    const int cend = min(c + kMmChunk, total);
-    for (int u = c; u < cend; u++) {
-      const long long t0 = clock64();
-      while (u >= __ldg(unit_off + m + 1)) m++;
-      const BatchDesc& d = desc[m];
-      const int lu = u - d.unit0;
-      const int2* p = part + d.part0;
-      batch_spmm_unit<P, VEC>(d, N, p[lu], p[lu + 1], u, carry_row, carry_val);
-      if (lane == 0) {
-        const int32_t r = carry_row[u];  // written by this lane inside the tile
-        carry_row[u] = r < d.rows ? r : -1;
-        unit_mat[u] = m;
-        unit_cycles[u] = clock64() - t0;
-      }
-    }
-    c = __shfl_sync(0xffffffffu, next, 0);
-  }
-}
-
-// One thread per (unit, column): the first unit of each run that ends inside the same row adds
-// the run's carries in unit order.  Resets the work queue for the next launch.
-template <typename Out>
-__global__ void batch_spmm_fixup(const BatchDesc* __restrict__ desc, int32_t total, int32_t N,
-                                 const int32_t* __restrict__ carry_row,
-                                 const double* __restrict__ carry_val,
-                                 const int32_t* __restrict__ unit_mat, int* __restrict__ counter) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx == 0) *counter = 0;
-  const int64_t u = idx / N;
-  const int32_t col = (int32_t)(idx % N);
-  if (u >= total) return;
-  const int32_t r = carry_row[u];
-  if (r < 0) return;
-  const int32_t m = unit_mat[u];
-  if (u > 0 && carry_row[u - 1] == r && unit_mat[u - 1] == m) return;
-  double tot = carry_val[u * N + col];
-  for (int64_t v = u + 1; v < total && carry_row[v] == r && unit_mat[v] == m; v++)
-    tot += carry_val[v * N + col];
-  Out* c = (Out*)desc[m].y + (int64_t)r * N + col;
-  *c = (Out)((double)*c + tot);
-}
-
 // Per-matrix sum of the unit cycles of the last run (one warp per matrix).
 __global__ void batch_matrix_cycles(const BatchDesc* __restrict__ desc, int count,
                                     const long long* __restrict__ unit_cycles,
@@ -339,29 +199,7 @@ __global__ void batch_matrix_cycles(const BatchDesc* __restrict__ desc, int coun
 
 // ================================================================= plan (C ABI) ==========
 
-struct tacogb_batch {
-  int device = 0;
-  int count = 0;
-  int vt = TACOGB_F64;
-  int32_t total_units = 0;
-  int kernels_per_run = 0;
-  tacogb::BatchDesc* d_desc = nullptr;
-  int32_t* d_unit_off = nullptr;
-  int32_t* d_blk_off = nullptr;
-  int2* d_part = nullptr;
-  int32_t* d_carry_row = nullptr;
-  double* d_carry_val = nullptr;
-  int* d_counter = nullptr;
-  long long* d_unit_cycles = nullptr;
-  long long* d_mat_cycles = nullptr;
-  int32_t* d_unit_mat = nullptr;  // SpMM plans: matrix of each unit
-  cudaStream_t cap = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-};
-
 namespace tacogb {
-namespace {
 
 void batch_free(tacogb_batch* b) {
   if (!b) return;
@@ -380,6 +218,53 @@ void batch_free(tacogb_batch* b) {
   cudaFree(b->d_unit_mat);
   delete b;
 }
+
+int batch_alloc(tacogb_batch* b, const BatchDesc* desc, const int32_t* unit_off,
+                const int32_t* blk_off, int64_t parts, int64_t carry_cols, bool with_unit_mat) {
+  const int count = b->count;
+  const int64_t u1 = std::max<int64_t>(b->total_units, 1);
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  alloc((void**)&b->d_desc, sizeof(BatchDesc) * count);
+  alloc((void**)&b->d_unit_off, sizeof(int32_t) * (count + 1));
+  alloc((void**)&b->d_blk_off, sizeof(int32_t) * (count + 1));
+  alloc((void**)&b->d_part, sizeof(int2) * std::max<int64_t>(parts, 1));
+  alloc((void**)&b->d_carry_row, sizeof(int32_t) * u1);
+  alloc((void**)&b->d_carry_val, sizeof(double) * u1 * carry_cols);
+  if (with_unit_mat) alloc((void**)&b->d_unit_mat, sizeof(int32_t) * u1);
+  alloc((void**)&b->d_counter, sizeof(int));
+  alloc((void**)&b->d_unit_cycles, sizeof(long long) * u1);
+  alloc((void**)&b->d_mat_cycles, sizeof(long long) * count);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error(TACOGB_ERR_ALLOC, "batch: allocating the plan: %s", cudaGetErrorString(e));
+    return TACOGB_ERR_ALLOC;
+  }
+  TACOGB_CUDA_TRY(cudaMemset(b->d_unit_cycles, 0, sizeof(long long) * u1));
+  TACOGB_CUDA_TRY(cudaMemset(b->d_counter, 0, sizeof(int)));
+  TACOGB_CUDA_TRY(cudaMemcpy(b->d_desc, desc, sizeof(BatchDesc) * count, cudaMemcpyHostToDevice));
+  TACOGB_CUDA_TRY(cudaMemcpy(b->d_unit_off, unit_off, sizeof(int32_t) * (count + 1),
+                             cudaMemcpyHostToDevice));
+  TACOGB_CUDA_TRY(cudaMemcpy(b->d_blk_off, blk_off, sizeof(int32_t) * (count + 1),
+                             cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int batch_end_capture(tacogb_batch* b) {
+  const cudaError_t le = cudaGetLastError();
+  const cudaError_t ce = cudaStreamEndCapture(b->cap, &b->graph);
+  if (le != cudaSuccess || ce != cudaSuccess) {
+    set_error(TACOGB_ERR_CUDA, "batch: graph capture failed: %s",
+              cudaGetErrorString(le != cudaSuccess ? le : ce));
+    return TACOGB_ERR_CUDA;
+  }
+  TACOGB_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  return 0;
+}
+
+namespace {
 
 template <class P>
 int batch_capture(tacogb_batch* b, int32_t total_blocks, int* status) {
@@ -407,60 +292,7 @@ int batch_capture(tacogb_batch* b, int32_t total_blocks, int* status) {
       b->d_desc, b->d_unit_off, b->count, b->total_units, b->d_carry_row, b->d_carry_val,
       b->d_counter);
   b->kernels_per_run++;
-  const cudaError_t le = cudaGetLastError();
-  const cudaError_t ce = cudaStreamEndCapture(b->cap, &b->graph);
-  if (le != cudaSuccess || ce != cudaSuccess) {
-    set_error(TACOGB_ERR_CUDA, "batch: graph capture failed: %s",
-              cudaGetErrorString(le != cudaSuccess ? le : ce));
-    return TACOGB_ERR_CUDA;
-  }
-  TACOGB_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
-  return 0;
-}
-
-template <class P, int VEC>
-int batch_capture_spmm(tacogb_batch* b, int32_t N, int32_t total_blocks) {
-  auto kern = batch_spmm_kernel<P, VEC>;
-  int per_sm = 0;
-  TACOGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMmBatchBlock, 0));
-  const int grid = sm_count() * std::max(per_sm, 1);
-  TACOGB_CUDA_TRY(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
-  TACOGB_CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
-  b->kernels_per_run = 0;
-  if (total_blocks > 0) {
-    batch_partition<<<total_blocks, kPartBlock, 0, b->cap>>>(b->d_desc, b->d_blk_off, b->count,
-                                                             b->d_part);
-    b->kernels_per_run++;
-  }
-  if (b->total_units > 0) {
-    kern<<<grid, kMmBatchBlock, 0, b->cap>>>(b->d_desc, b->d_unit_off, b->count, b->total_units,
-                                             N, b->d_part, b->d_carry_row, b->d_carry_val,
-                                             b->d_unit_mat, b->d_counter, b->d_unit_cycles);
-    b->kernels_per_run++;
-  }
-  const int64_t fix = std::max<int64_t>((int64_t)b->total_units * N, 1);
-  batch_spmm_fixup<typename P::Out><<<(unsigned)((fix + 255) / 256), 256, 0, b->cap>>>(
-      b->d_desc, b->total_units, N, b->d_carry_row, b->d_carry_val, b->d_unit_mat, b->d_counter);
-  b->kernels_per_run++;
-  const cudaError_t le = cudaGetLastError();
-  const cudaError_t ce = cudaStreamEndCapture(b->cap, &b->graph);
-  if (le != cudaSuccess || ce != cudaSuccess) {
-    set_error(TACOGB_ERR_CUDA, "batch: graph capture failed: %s",
-              cudaGetErrorString(le != cudaSuccess ? le : ce));
-    return TACOGB_ERR_CUDA;
-  }
-  TACOGB_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
-  return 0;
-}
-
-template <class P>
-int batch_spmm_vec(tacogb_batch* b, int32_t N, int32_t blocks, int vec) {
-  constexpr int esz = sizeof(typename P::BV);
-  if (vec == 2) return batch_capture_spmm<P, 2>(b, N, blocks);
-  if constexpr (esz <= 4) {
-    if (vec == 4) return batch_capture_spmm<P, 4>(b, N, blocks);
-  }
-  return batch_capture_spmm<P, 1>(b, N, blocks);
+  return batch_end_capture(b);
 }
 
 }  // namespace
@@ -512,13 +344,8 @@ int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const
     d.tma = aligned;
     d.tile = is_merge(kind) ? (int32_t)kind_tile_items(kind) : 0;
     d.snap = 0;
-    int64_t u = 0;
-    if (is_merge(kind)) {
-      const int64_t T = kind_tile_items(kind);
-      u = ((int64_t)A.rows + A.nnz + T - 1) / T;
-    } else {
-      u = ((int64_t)A.rows + vec_rows(kind) - 1) / vec_rows(kind);
-    }
+    const int64_t u = is_merge(kind) ? ((int64_t)A.rows + A.nnz + d.tile - 1) / d.tile
+                                     : ((int64_t)A.rows + vec_rows(kind) - 1) / vec_rows(kind);
     d.unit0 = (int32_t)units;
     d.units = (int32_t)u;
     d.part0 = (int32_t)parts;
@@ -543,143 +370,12 @@ int tacogb_batch_create(int32_t count, const tacogb_csr* mats, const void* const
   b->count = count;
   b->vt = vt;
   b->total_units = (int32_t)units;
-  auto fail = [&](cudaError_t e, const char* what) {
-    set_error(TACOGB_ERR_ALLOC, "batch: %s: %s", what, cudaGetErrorString(e));
-    batch_free(b);
-    return TACOGB_ERR_ALLOC;
-  };
-  cudaError_t e;
-  if ((e = cudaMalloc(&b->d_desc, sizeof(BatchDesc) * count)) != cudaSuccess) return fail(e, "descriptors");
-  if ((e = cudaMalloc(&b->d_unit_off, sizeof(int32_t) * (count + 1))) != cudaSuccess) return fail(e, "offsets");
-  if ((e = cudaMalloc(&b->d_blk_off, sizeof(int32_t) * (count + 1))) != cudaSuccess) return fail(e, "offsets");
-  if ((e = cudaMalloc(&b->d_part, sizeof(int2) * std::max<int64_t>(parts, 1))) != cudaSuccess) return fail(e, "partition");
-  if ((e = cudaMalloc(&b->d_carry_row, sizeof(int32_t) * std::max<int64_t>(units, 1))) != cudaSuccess) return fail(e, "carries");
-  if ((e = cudaMalloc(&b->d_carry_val, sizeof(double) * std::max<int64_t>(units, 1))) != cudaSuccess) return fail(e, "carries");
-  if ((e = cudaMalloc(&b->d_counter, sizeof(int))) != cudaSuccess) return fail(e, "queue");
-  if ((e = cudaMalloc(&b->d_unit_cycles, sizeof(long long) * std::max<int64_t>(units, 1))) != cudaSuccess)
-    return fail(e, "unit cycles");
-  if ((e = cudaMalloc(&b->d_mat_cycles, sizeof(long long) * count)) != cudaSuccess)
-    return fail(e, "matrix cycles");
-  cudaMemset(b->d_unit_cycles, 0, sizeof(long long) * std::max<int64_t>(units, 1));
-  cudaMemcpy(b->d_desc, desc.data(), sizeof(BatchDesc) * count, cudaMemcpyHostToDevice);
-  cudaMemcpy(b->d_unit_off, unit_off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice);
-  cudaMemcpy(b->d_blk_off, blk_off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice);
-  if ((e = cudaMemset(b->d_counter, 0, sizeof(int))) != cudaSuccess) return fail(e, "queue");
-  int rc = 0;
-  if (vt == TACOGB_F32) rc = batch_capture<PolComp32>(b, (int32_t)blocks, status);
-  else if (precision == 1) rc = batch_capture<PolNative64>(b, (int32_t)blocks, status);
-  else rc = batch_capture<PolDF64X>(b, (int32_t)blocks, status);
-  if (rc) {
-    batch_free(b);
-    return rc;
+  int rc = batch_alloc(b, desc.data(), unit_off.data(), blk_off.data(), parts, 1, false);
+  if (rc == 0) {
+    if (vt == TACOGB_F32) rc = batch_capture<PolComp32>(b, (int32_t)blocks, status);
+    else if (precision == 1) rc = batch_capture<PolNative64>(b, (int32_t)blocks, status);
+    else rc = batch_capture<PolDF64X>(b, (int32_t)blocks, status);
   }
-  *out = b;
-  return 0;
-}
-
-int tacogb_batch_spmm_create(int32_t count, const tacogb_csr* mats, int32_t N,
-                             const void* const* B, int32_t btype, void* const* C,
-                             int32_t precision, tacogb_batch** out) {
-  TACOGB_CHECK_ARG(out != nullptr, "batch: null output handle");
-  *out = nullptr;
-  TACOGB_CHECK_ARG(count > 0 && mats && B && C, "batch: empty or null batch");
-  TACOGB_CHECK_ARG(N > 0, "batch: N must be positive");
-  const int vt = mats[0].vtype;
-  const bool f64 = vt == TACOGB_F64 && btype == TACOGB_F64;
-  const bool f32 = vt == TACOGB_F32 && btype == TACOGB_F32;
-  const bool bf16 = vt == TACOGB_F32 && btype == TACOGB_BF16;
-  TACOGB_CHECK_ARG(f64 || f32 || bf16, "batch: unsupported value types (A %d, B %d)", vt, btype);
-  TACOGB_CHECK_ARG(precision == 0 || (precision == 1 && !bf16),
-                   "batch: precision %d (0 = default, 1 = native)", precision);
-  const int esz = f64 ? 8 : (f32 ? 4 : 2), osz = f64 ? 8 : 4;
-  // widest lane vector (<= 16 bytes) whose column tile divides N and that every B and C allows
-  int vec = 1;
-  for (int v : {4, 2}) {
-    if ((f64 && v == 4) || v * esz > 16 || N % (32 * v) != 0) continue;
-    bool al = true;
-    for (int m = 0; m < count && al; m++)
-      al = ((uintptr_t)B[m] % (size_t)(v * esz)) == 0 && ((uintptr_t)C[m] % (size_t)(v * osz)) == 0;
-    if (al) {
-      vec = v;
-      break;
-    }
-  }
-  std::vector<BatchDesc> desc(count);
-  std::vector<int32_t> unit_off(count + 1), blk_off(count + 1);
-  int64_t units = 0, parts = 0, blocks = 0;
-  for (int m = 0; m < count; m++) {
-    const tacogb_csr& A = mats[m];
-    TACOGB_CHECK_ARG(A.vtype == vt, "batch: matrix %d has value type %d, expected %d", m, A.vtype, vt);
-    TACOGB_CHECK_ARG(A.rows >= 0 && A.cols >= 0 && A.nnz >= 0 && A.nnz <= INT32_MAX,
-                     "batch: matrix %d has a bad size", m);
-    TACOGB_CHECK_ARG((int64_t)A.rows * N <= INT32_MAX,
-                     "batch: matrix %d: rows*N exceeds taco's int32 dense positions", m);
-    TACOGB_CHECK_ARG(A.rows == 0 || (A.pos && C[m]), "batch: matrix %d has null pos or C", m);
-    TACOGB_CHECK_ARG(A.nnz == 0 || (A.crd && A.vals && B[m]), "batch: matrix %d has null arrays", m);
-    BatchDesc& d = desc[m];
-    d.pos = A.pos;
-    d.crd = A.crd;
-    d.vals = A.vals;
-    d.x = B[m];
-    d.y = C[m];
-    d.rows = A.rows;
-    d.cols = A.cols;
-    d.nnz = (int32_t)A.nnz;
-    d.kind = kMerge7;
-    d.tile = kMmBatchTile;
-    d.snap = kMmBatchTile / 2;
-    const int64_t u = ((int64_t)A.rows + A.nnz + kMmBatchTile - 1) / kMmBatchTile;
-    d.unit0 = (int32_t)units;
-    d.units = (int32_t)u;
-    d.part0 = (int32_t)parts;
-    d.blk0 = (int32_t)blocks;
-    unit_off[m] = (int32_t)units;
-    blk_off[m] = (int32_t)blocks;
-    units += u;
-    if (u > 0) {
-      parts += u + 1;
-      blocks += ((int64_t)A.rows + 1 + kPartBlock - 1) / kPartBlock;
-    }
-    TACOGB_CHECK_ARG(units < INT32_MAX / 2 && parts < INT32_MAX / 2 && blocks < INT32_MAX / 2,
-                     "batch: too much work for one plan");
-  }
-  unit_off[count] = (int32_t)units;
-  blk_off[count] = (int32_t)blocks;
-  if (!device_status()) return last_code();
-  tacogb_batch* b = new tacogb_batch();
-  cudaGetDevice(&b->device);
-  b->count = count;
-  b->vt = vt;
-  b->total_units = (int32_t)units;
-  auto fail = [&](cudaError_t e, const char* what) {
-    set_error(TACOGB_ERR_ALLOC, "batch: %s: %s", what, cudaGetErrorString(e));
-    batch_free(b);
-    return TACOGB_ERR_ALLOC;
-  };
-  const int64_t u1 = std::max<int64_t>(units, 1);
-  cudaError_t e;
-  if ((e = cudaMalloc(&b->d_desc, sizeof(BatchDesc) * count)) != cudaSuccess) return fail(e, "descriptors");
-  if ((e = cudaMalloc(&b->d_unit_off, sizeof(int32_t) * (count + 1))) != cudaSuccess) return fail(e, "offsets");
-  if ((e = cudaMalloc(&b->d_blk_off, sizeof(int32_t) * (count + 1))) != cudaSuccess) return fail(e, "offsets");
-  if ((e = cudaMalloc(&b->d_part, sizeof(int2) * std::max<int64_t>(parts, 1))) != cudaSuccess) return fail(e, "partition");
-  if ((e = cudaMalloc(&b->d_carry_row, sizeof(int32_t) * u1)) != cudaSuccess) return fail(e, "carries");
-  if ((e = cudaMalloc(&b->d_carry_val, sizeof(double) * u1 * N)) != cudaSuccess) return fail(e, "carries");
-  if ((e = cudaMalloc(&b->d_unit_mat, sizeof(int32_t) * u1)) != cudaSuccess) return fail(e, "unit matrices");
-  if ((e = cudaMalloc(&b->d_counter, sizeof(int))) != cudaSuccess) return fail(e, "queue");
-  if ((e = cudaMalloc(&b->d_unit_cycles, sizeof(long long) * u1)) != cudaSuccess) return fail(e, "unit cycles");
-  if ((e = cudaMalloc(&b->d_mat_cycles, sizeof(long long) * count)) != cudaSuccess) return fail(e, "matrix cycles");
-  cudaMemset(b->d_unit_cycles, 0, sizeof(long long) * u1);
-  cudaMemcpy(b->d_desc, desc.data(), sizeof(BatchDesc) * count, cudaMemcpyHostToDevice);
-  cudaMemcpy(b->d_unit_off, unit_off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice);
-  cudaMemcpy(b->d_blk_off, blk_off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice);
-  if ((e = cudaMemset(b->d_counter, 0, sizeof(int))) != cudaSuccess) return fail(e, "queue");
-  const int32_t nb = (int32_t)blocks;
-  int rc;
-  if (f64) rc = precision == 1 ? batch_spmm_vec<MmNative64>(b, N, nb, vec)
-                               : batch_spmm_vec<MmDF64>(b, N, nb, vec);
-  else if (f32) rc = precision == 1 ? batch_spmm_vec<MmF32>(b, N, nb, vec)
-                                    : batch_spmm_vec<MmComp32>(b, N, nb, vec);
-  else rc = batch_spmm_vec<MmBF16>(b, N, nb, vec);
   if (rc) {
     batch_free(b);
     return rc;

@@ -241,4 +241,162 @@ __device__ __forceinline__ bool spmm_tile(const int32_t* __restrict__ pos,
   return ok;
 }
 
+// ------------------------------------------------------------------ sub-warp tile --------
+//
+// For narrow dense operands (N*sizeof(B) of 128 bytes or less, N=32 in the batched workload) one
+// lane vector per lane covers a B row with LPR = 32/SUB lanes, so the warp splits into SUB
+// sub-warps.  Rows of the tile go to sub-warps: SUB consecutive short rows at a time, one per
+// sub-warp, while a row segment of kSubLong nonzeros or more is shared by the whole warp (each
+// sub-warp takes every SUB-th group of LPR nonzeros, then the sub-warps' sums are added in a
+// fixed butterfly).  Each sub-warp issues LPR B-row loads before it multiplies, so up to 32 B
+// rows are in flight per warp whatever the row lengths.  Loop trip counts are warp-uniform (the
+// longest row of the group), so every shuffle runs on the full warp.
+
+__device__ __forceinline__ double acc_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float acc_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ DF acc_add(DF a, DF b) { return df_add(a, b); }
+__device__ __forceinline__ double acc_xor(double a, int o) {
+  return __shfl_xor_sync(0xffffffffu, a, o);
+}
+__device__ __forceinline__ float acc_xor(float a, int o) {
+  return __shfl_xor_sync(0xffffffffu, a, o);
+}
+__device__ __forceinline__ DF acc_xor(DF a, int o) {
+  return DF{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+}
+
+constexpr int kSubLong = 64;
+#ifndef TACOGB_SUB_BYTES
+#define TACOGB_SUB_BYTES 64
+#endif
+constexpr int kSubBytes = TACOGB_SUB_BYTES;  // register bytes per lane for B rows in flight
+
+// LPR nonzeros of one sub-warp: crd/val sit in the lanes [lb, lb+LPR) of mc/ma; the first cnt
+// are valid.  Issues all B-row loads before the multiplies.
+template <class P, int VEC, int LPR>
+__device__ __forceinline__ void sub_chunk(typename P::Acc (&acc)[VEC], int mc,
+                                          typename P::Prep ma, int lb, int cnt,
+                                          const typename P::BV* __restrict__ B, int32_t N,
+                                          int col0, bool active, bool& ok) {
+  using BE = typename P::BE;
+  // B-row loads in flight per lane: kSubBytes of registers
+  constexpr int UB = kSubBytes / (VEC * (int)sizeof(BE));
+  constexpr int U = LPR < UB ? LPR : (UB > 0 ? UB : 1);
+#pragma unroll 1
+  for (int u0 = 0; u0 < LPR; u0 += U) {
+    BE b[U][VEC];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int c = __shfl_sync(0xffffffffu, mc, lb + u0 + u);
+      if (active && u0 + u < cnt) load_vec<VEC>(B + (int64_t)c * N + col0, b[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const typename P::Prep a = P::shfl(ma, lb + u0 + u);
+      if (active && u0 + u < cnt) {
+#pragma unroll
+        for (int v = 0; v < VEC; v++) P::madd(acc[v], a, b[u][v], ok);
+      }
+    }
+  }
+}
+
+template <class P, int VEC>
+__device__ __forceinline__ void sub_emit(const typename P::Acc (&acc)[VEC], int r, int r1,
+                                         bool nonempty, typename P::Out* __restrict__ C,
+                                         int32_t N, int col0, int tile,
+                                         double* __restrict__ carry_val, bool& carried) {
+  if (r < r1) {
+    typename P::Out o[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) o[v] = P::out(acc[v]);
+    store_vec<VEC>(C + (int64_t)r * N + col0, o);
+  } else if (nonempty) {
+    carried = true;
+#pragma unroll
+    for (int v = 0; v < VEC; v++) carry_val[(int64_t)tile * N + col0 + v] = P::to_double(acc[v]);
+  }
+}
+
+// Columns [ct, ct + LPR*VEC) of merge tile `tile`.  Same contract as spmm_tile.
+template <class P, int VEC, int SUB>
+__device__ __forceinline__ bool spmm_tile_sub(const int32_t* __restrict__ pos,
+                                              const int32_t* __restrict__ crd,
+                                              const typename P::AV* __restrict__ vals,
+                                              const typename P::BV* __restrict__ B,
+                                              typename P::Out* __restrict__ C, int32_t n,
+                                              int32_t N, int2 c0, int2 c1, int tile, int ct,
+                                              int32_t* __restrict__ carry_row,
+                                              double* __restrict__ carry_val) {
+  using Acc = typename P::Acc;
+  using Prep = typename P::Prep;
+  constexpr int LPR = 32 / SUB;
+  const int lane = threadIdx.x & 31, sub = lane / LPR, sl = lane % LPR, lb = sub * LPR;
+  const int col0 = ct + sl * VEC;
+  const bool active = col0 < N;
+  const int r0 = c0.x, k0 = c0.y, r1 = c1.x, k1 = c1.y;
+  const int rend = min(r1, n - 1);
+  bool ok = true, carried = false;
+  int r = r0;
+  while (r <= rend) {
+    const int myr = r + sub;
+    int ps = 0, pe = 0;
+    if (myr <= rend) {
+      ps = (myr == r0) ? k0 : __ldg(pos + myr);
+      pe = (myr < r1) ? __ldg(pos + myr + 1) : k1;
+    }
+    const int len = pe - ps;
+    const unsigned lmask = __ballot_sync(0xffffffffu, sl == 0 && myr <= rend && len >= kSubLong);
+    const int first_long = lmask ? (__ffs(lmask) - 1) / LPR : SUB;
+    const int k = min(first_long, rend - r + 1);
+    Acc acc[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) acc[v] = P::zero();
+    if (k == 0) {
+      // row r shared by the whole warp: sub-warp s takes lanes [s*LPR, s*LPR+LPR) of each 32
+      const int ps0 = __shfl_sync(0xffffffffu, ps, 0), pe0 = __shfl_sync(0xffffffffu, pe, 0);
+      for (int base = ps0; base < pe0; base += 32) {
+        const int cnt = min(32, pe0 - base);
+        int mc = 0;
+        Prep ma = Prep();
+        if (lane < cnt) {
+          mc = ld_stream_i32(crd + base + lane);
+          ma = P::prep(vals[base + lane], ok);
+        }
+        sub_chunk<P, VEC, LPR>(acc, mc, ma, lb, cnt - lb, B, N, col0, active, ok);
+      }
+#pragma unroll
+      for (int o = LPR; o < 32; o <<= 1) {
+#pragma unroll
+        for (int v = 0; v < VEC; v++) acc[v] = acc_add(acc[v], acc_xor(acc[v], o));
+      }
+      if (sub == 0 && active)
+        sub_emit<P, VEC>(acc, r, r1, pe0 > ps0, C, N, col0, tile, carry_val, carried);
+      r += 1;
+    } else {
+      // rows r .. r+k-1, one per sub-warp
+      const bool mine = sub < k;
+      int trip = mine ? len : 0;
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) trip = max(trip, __shfl_xor_sync(0xffffffffu, trip, o));
+      for (int base = 0; base < trip; base += LPR) {
+        const int cnt = mine ? min(LPR, len - base) : 0;
+        int mc = 0;
+        Prep ma = Prep();
+        if (sl < cnt) {
+          mc = ld_stream_i32(crd + ps + base + sl);
+          ma = P::prep(vals[ps + base + sl], ok);
+        }
+        sub_chunk<P, VEC, LPR>(acc, mc, ma, lb, cnt, B, N, col0, active, ok);
+      }
+      if (mine && active)
+        sub_emit<P, VEC>(acc, myr, r1, len > 0, C, N, col0, tile, carry_val, carried);
+      r += k;
+    }
+  }
+  carried = __any_sync(0xffffffffu, carried);
+  if (lane == 0 && blockIdx.y == 0) carry_row[tile] = carried ? r1 : n;
+  return ok;
+}
+
 }  // namespace tacogb
