@@ -46,7 +46,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="spmv_powerlaw",
                    choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
-                            "batched_spmv", "batched_spmm"])
+                            "spgemm_random", "spgemm_poisson", "batched_spmv", "batched_spmm"])
     p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
     p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
                    help="how batched_spmv picks each matrix's work-unit kind")
@@ -398,7 +398,101 @@ class BatchSpmmOp(BatchOp):
         return ("reference" if ref else "port"), once, keep
 
 
+class SpgemmOp:
+    """Two-phase C = A A: symbolic (C pos, nnz(C) read back), column fill, numeric values.
+    One step = all three phases, with C's arrays allocated once for the known nnz(C)."""
+    pattern = "spgemm"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        s = self.spec = W.spgemm_random() if args.workload == "spgemm_random" else W.spgemm_poisson()
+        self.pos, self.crd, self.vals = W.generate(s)
+        self.rows, self.cols, self.nnz = s.rows, s.cols, len(self.crd)
+        lens = np.diff(self.pos).astype(np.int64)
+        self.products = int(lens[self.crd].sum())  # sum over A's nonzeros of B's row lengths
+        self.metric = "spgemm_f64_gbs"
+        self.workload = "%s_%d" % (args.workload, self.rows)
+        self.nnzC = None
+
+    def set_nnzC(self, nnzC):
+        n, a = self.rows, self.nnz
+        self.nnzC = nnzC
+        self.sym_bytes = 4 * (n + 1) * 2 + 4 * a + 4 * (n + 1) + 4 * a
+        self.num_bytes = 4 * (n + 1) * 2 + 12 * a + 4 * (n + 1) + 12 * a + 12 * nnzC
+        self.bytes = self.sym_bytes + self.num_bytes
+        self.flops = 2 * self.products
+
+    def device(self, torch, tg):
+        A = tg.CsrMatrix.from_numpy(self.pos, self.crd, self.vals, self.cols)
+        a = A.as_csr()
+        L = tg.lib()
+        pos = torch.empty(self.rows + 1, dtype=torch.int32, device="cuda")
+        nnz = ctypes.c_int64(0)
+        sp0 = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        tg.check(L.tacogb_spgemm_symbolic(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
+                                          ctypes.byref(nnz), sp0), "symbolic")
+        self.set_nnzC(nnz.value)
+        crd = torch.empty(max(nnz.value, 1), dtype=torch.int32, device="cuda")
+        vals = torch.empty(max(nnz.value, 1), dtype=torch.float64, device="cuda")
+        keep = (A, a, pos, crd, vals, nnz)
+
+        def step(sp):
+            tg.check(L.tacogb_spgemm_symbolic(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
+                                              ctypes.byref(nnz), sp), "symbolic")
+            tg.check(L.tacogb_spgemm_fill(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
+                                          crd.data_ptr(), sp), "fill")
+            tg.check(L.tacogb_spgemm_numeric(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
+                                             crd.data_ptr(), vals.data_ptr(), sp), "numeric")
+        return step, keep
+
+    def abi(self, torch, tg, T):
+        import ctypes.util
+        libc = ctypes.CDLL(ctypes.util.find_library("c"))
+        libc.free.argtypes = [ctypes.c_void_p]
+        hp, hc = torch.from_numpy(self.pos).pin_memory(), torch.from_numpy(self.crd).pin_memory()
+        hv = torch.from_numpy(self.vals).pin_memory()
+        At = T.csr(hp, hc, hv, [self.rows, self.cols])
+        L = tg.lib()
+        keep = (hp, hc, hv, At)
+
+        def step():
+            Ct = T.csr_result([self.rows, self.cols])
+            tg.check(L.tacogb_spgemm_evaluate(Ct.ptr, At.ptr, At.ptr), "tacogb_spgemm_evaluate")
+            for q in (Ct.index(1, 0), Ct.index(1, 1), Ct.vals_ptr):
+                libc.free(q)
+        h2d = 2 * ((self.rows + 1) * 4 + self.nnz * 12)
+        d2h = (self.rows + 1) * 4 + self.nnzC * 12
+        return step, keep, h2d, d2h, "tacogb_spgemm_evaluate(taco_tensor_t*) on pinned host arrays"
+
+    def cpu(self):
+        import ctypes.util
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        libc = ctypes.CDLL(ctypes.util.find_library("c"))
+        libc.free.argtypes = [ctypes.c_void_p]
+        At = T.csr(self.pos, self.crd, self.vals, [self.rows, self.cols])
+        if O.ref_available("spgemm"):
+            L = O.ref_lib("spgemm")
+
+            def once():
+                Ct = T.csr_result([self.rows, self.cols])
+                L.assemble(Ct.ptr, At.ptr, At.ptr)
+                L.compute(Ct.ptr, At.ptr, At.ptr)
+                nnzC = ctypes.cast(Ct.index(1, 0), ctypes.POINTER(ctypes.c_int32))[self.rows]
+                for q in (Ct.index(1, 0), Ct.index(1, 1), Ct.vals_ptr):
+                    libc.free(q)
+                return nnzC
+            self.set_nnzC(int(once()))
+            return "reference", once, (At,)
+        p, c, v = self.pos, self.crd, self.vals
+        self.set_nnzC(int(O.spgemm(p, c, None, p, c, None, self.cols)[0][-1]))
+        return "port", lambda: O.spgemm(p, c, v, p, c, v, self.cols), (At,)
+
+
 def make_op(args):
+    if args.workload.startswith("spgemm"):
+        return SpgemmOp(args)
     if args.workload == "batched_spmv":
         return BatchOp(args)
     if args.workload == "batched_spmm":
@@ -836,13 +930,16 @@ def main():
         kernels[nm] = (tot[k], cnt[k])
     dom = max(kernels, key=lambda k: kernels[k][0])
     dom_ms = kernels[dom][0] / kernels[dom][1]
+    dom_share = kernels[dom][0] / sum(v[0] for v in kernels.values())
+    if op.pattern == "spgemm":  # the bytes model covers all three phases of a step
+        dom, dom_ms = "spgemm symbolic + fill + numeric (%s largest)" % dom, ms / args.steps
     peak, peak_kind = measured_peak()
     achieved = op.bytes / (dom_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak,
                 "traffic": ncu_traffic(dom, "%s_%s" % (op.workload, args.dtype)),
                 "kernel": dom, "kernel_ms": dom_ms, "peak_source": peak_kind,
-                "kernel_share": kernels[dom][0] / sum(v[0] for v in kernels.values())}
+                "kernel_share": dom_share}
     del keep
 
     e2e = None
@@ -872,12 +969,17 @@ def main():
                "sample": "whole workload, median of %d reps" % reps, "ms_per_step": t * 1e3}
 
     if rank == 0:
-        names_v = (tg.spmv_variants() if op.pattern == "spmv" else tg.spmm_variants())
+        names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
+                   "spgemm": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,
                   "variant": "auto" if args.variant < 0 else names_v[args.variant],
                   "l2": "inputs larger than L2 (%.2f GB per step), no flush" % (op.bytes / 1e9),
                   "parallelism": "replicas" if world > 1 else "single"}
+        if op.pattern == "spgemm":
+            config.update({"nnz_c": op.nnzC, "products": op.products,
+                           "products_per_s": op.products * args.steps * world / (ms / 1e3),
+                           "symbolic_bytes": op.sym_bytes, "numeric_bytes": op.num_bytes})
         if op.pattern == "spmm":
             config["n"] = op.N
             config["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9

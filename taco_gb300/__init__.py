@@ -10,7 +10,8 @@ from . import _native
 from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBError, check,
                       lib)
 
-__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "SpmvBatch", "SpmmBatch",
+__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "spgemm", "SpmvBatch",
+           "SpmmBatch",
            "batch_variants", "lib", "check", "TacoGBError",
            "TACOGB_F64", "TACOGB_F32", "TACOGB_BF16", "VARIANT_AUTO"]
 
@@ -81,6 +82,26 @@ def spmm(A, B, C=None, variant=VARIANT_AUTO, stream=None):
     check(lib().tacogb_spmm(ctypes.byref(c), N, B.data_ptr(), _BTYPE[B.element_size()],
                             C.data_ptr(), variant, _stream_ptr(stream)), "tacogb_spmm")
     return C
+
+
+def spgemm(A, B, stream=None):
+    """C = A B for CSR A and B on the GPU (two phases, as taco's assemble then compute):
+    tacogb_spgemm_symbolic writes C's pos and returns nnz(C) (synchronising), tacogb_spgemm_fill
+    writes the sorted columns, tacogb_spgemm_numeric the values.  Returns a CsrMatrix."""
+    import torch
+    a, b = A.as_csr(), B.as_csr()
+    L, sp = lib(), _stream_ptr(stream)
+    pos = torch.empty(A.rows + 1, dtype=torch.int32, device=A.pos.device)
+    nnz = ctypes.c_int64(0)
+    check(L.tacogb_spgemm_symbolic(ctypes.byref(a), ctypes.byref(b), pos.data_ptr(),
+                                   ctypes.byref(nnz), sp), "tacogb_spgemm_symbolic")
+    crd = torch.empty(nnz.value, dtype=torch.int32, device=A.pos.device)
+    vals = torch.empty(nnz.value, dtype=A.vals.dtype, device=A.pos.device)
+    check(L.tacogb_spgemm_fill(ctypes.byref(a), ctypes.byref(b), pos.data_ptr(), crd.data_ptr(),
+                               sp), "tacogb_spgemm_fill")
+    check(L.tacogb_spgemm_numeric(ctypes.byref(a), ctypes.byref(b), pos.data_ptr(),
+                                  crd.data_ptr(), vals.data_ptr(), sp), "tacogb_spgemm_numeric")
+    return CsrMatrix(pos, crd, vals, B.cols)
 
 
 def spmm_variants():

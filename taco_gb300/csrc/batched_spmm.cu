@@ -54,8 +54,11 @@ __device__ __forceinline__ void batch_spmm_unit(const BatchDesc& d, int32_t N, i
   }
 }
 
+#ifndef TACOGB_MM_BATCH_BLOCKS
+#define TACOGB_MM_BATCH_BLOCKS 3  // resident blocks per SM the register budget is sized for
+#endif
 template <class P, int VEC, int SUB>
-__global__ void __launch_bounds__(kMmBatchBlock, 3)
+__global__ void __launch_bounds__(kMmBatchBlock, TACOGB_MM_BATCH_BLOCKS)
 batch_spmm_kernel(const BatchDesc* __restrict__ desc, const int32_t* __restrict__ unit_off,
                   int count, int32_t total, int32_t N, const int2* __restrict__ part,
                   int32_t* __restrict__ carry_row, double* __restrict__ carry_val,

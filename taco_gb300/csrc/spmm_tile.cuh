@@ -355,13 +355,20 @@ __device__ __forceinline__ bool spmm_tile_sub(const int32_t* __restrict__ pos,
     if (k == 0) {
       // row r shared by the whole warp: sub-warp s takes lanes [s*LPR, s*LPR+LPR) of each 32
       const int ps0 = __shfl_sync(0xffffffffu, ps, 0), pe0 = __shfl_sync(0xffffffffu, pe, 0);
+      // crd/vals run one chunk ahead of the B-row loads that depend on them
+      int mc_n = 0;
+      typename P::AV mv_n = typename P::AV();
+      if (ps0 + lane < pe0) {
+        mc_n = ld_stream_i32(crd + ps0 + lane);
+        mv_n = vals[ps0 + lane];
+      }
       for (int base = ps0; base < pe0; base += 32) {
         const int cnt = min(32, pe0 - base);
-        int mc = 0;
-        Prep ma = Prep();
-        if (lane < cnt) {
-          mc = ld_stream_i32(crd + base + lane);
-          ma = P::prep(vals[base + lane], ok);
+        const int mc = mc_n;
+        const Prep ma = lane < cnt ? P::prep(mv_n, ok) : Prep();
+        if (base + 32 + lane < pe0) {
+          mc_n = ld_stream_i32(crd + base + 32 + lane);
+          mv_n = vals[base + 32 + lane];
         }
         sub_chunk<P, VEC, LPR>(acc, mc, ma, lb, cnt - lb, B, N, col0, active, ok);
       }
@@ -379,13 +386,19 @@ __device__ __forceinline__ bool spmm_tile_sub(const int32_t* __restrict__ pos,
       int trip = mine ? len : 0;
 #pragma unroll
       for (int o = 16; o >= 1; o >>= 1) trip = max(trip, __shfl_xor_sync(0xffffffffu, trip, o));
+      int mc_n = 0;
+      typename P::AV mv_n = typename P::AV();
+      if (mine && sl < len) {
+        mc_n = ld_stream_i32(crd + ps + sl);
+        mv_n = vals[ps + sl];
+      }
       for (int base = 0; base < trip; base += LPR) {
         const int cnt = mine ? min(LPR, len - base) : 0;
-        int mc = 0;
-        Prep ma = Prep();
-        if (sl < cnt) {
-          mc = ld_stream_i32(crd + ps + base + sl);
-          ma = P::prep(vals[ps + base + sl], ok);
+        const int mc = mc_n;
+        const Prep ma = sl < cnt ? P::prep(mv_n, ok) : Prep();
+        if (mine && base + LPR + sl < len) {
+          mc_n = ld_stream_i32(crd + ps + base + LPR + sl);
+          mv_n = vals[ps + base + LPR + sl];
         }
         sub_chunk<P, VEC, LPR>(acc, mc, ma, lb, cnt, B, N, col0, active, ok);
       }
