@@ -120,6 +120,15 @@ int sm_count() {
   return ds->sms;
 }
 
+int gather_carveout_pct(int pct) {
+  static const int env = [] {
+    const char* e = getenv("TACOGB_SMEM_CARVEOUT");
+    const int v = e ? atoi(e) : -2;
+    return (v >= -1 && v <= 100) ? v : -2;
+  }();
+  return env != -2 ? env : pct;
+}
+
 void* scratch(size_t bytes, int slot) {
   std::lock_guard<std::mutex> lk(g_mu);
   DeviceState* ds = current_device();

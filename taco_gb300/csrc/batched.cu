@@ -271,6 +271,7 @@ int batch_capture(tacogb_batch* b, int32_t total_blocks, int* status) {
   auto kern = batch_spmv_kernel<P>;
   const size_t smem = sizeof(WmSmem<P, 7>);
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, -1));
   int per_sm = 0;
   TACOGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWmBlock, smem));
   const int grid = sm_count() * std::max(per_sm, 1);

@@ -62,6 +62,18 @@ void count_launch();
 // Number of SMs of the current device (cached per device).
 int sm_count();
 
+// Shared-memory carveout (percent of the maximum) for kernels that gather at random while
+// holding staged tiles in shared memory.  Every outstanding gather miss holds L1 capacity: on
+// GB300 random 8-byte gathers run at ~0.88 per clock per SM with a 60 KB L1 but at ~0.41 with
+// the 28 KB left by the largest carveout, which the driver picks by default whenever it lets
+// one more block fit.  Each kernel family passes the percentage measured best for it (-1 keeps
+// the driver's choice); TACOGB_SMEM_CARVEOUT, when set, overrides it for every family.
+int gather_carveout_pct(int pct);
+inline cudaError_t set_gather_carveout(const void* kern, int pct) {
+  return cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                              gather_carveout_pct(pct));
+}
+
 // Grow-only device scratch arena, one per device, used by kernels that need temporary global
 // memory (partition tables, carry-outs, bin lists, scan partials).  Grown outside any graph
 // capture; calls on one device are serialised by the caller's stream order.
@@ -72,6 +84,9 @@ void* scratch(size_t bytes, int slot);
 // check it after synchronising, tacogb_device_status() reads and clears it.
 constexpr int TACOGB_DEV_TIMEOUT = 1;
 int* device_status();
+// Word of the same zero-initialised 256-byte block holding the double-float SpMV's x-range
+// flag (set by its prep kernel, cleared by its fix-up kernel).
+constexpr int kXFlagWord = 16;
 
 // ---------------------------------------------------------------- TMA / mbarrier ----------
 

@@ -53,6 +53,33 @@ __device__ __forceinline__ bool split_df(double v, float& hi, float& lo) {
   return ok || zero;
 }
 
+// Eight-instruction split for values already known (or checked separately, df_in_range) to lie
+// in [2^-40, 2^40).  A funnel shift takes the low nine exponent bits and the top 23 mantissa
+// bits of the double in one go; subtracting 384 << 23 rebiases the exponent (e - 1023 + 127)
+// and leaves bit 31 clear; the sign is merged back with one three-input logic operation.  lo
+// is the next 23 mantissa bits, made a float exactly by the 2^-23 magic-exponent trick and
+// scaled by +-2^E, the sign-exponent of hi.  |v - (hi + lo)| < 2^-46 |v|.  Out-of-range input
+// gives meaningless hi and lo (never a fault).
+__device__ __forceinline__ void split_df_fast(double v, float& hi, float& lo) {
+  const unsigned int bh = (unsigned int)__double2hiint(v);
+  const unsigned int bl = (unsigned int)__double2loint(v);
+  const unsigned int mag = __funnelshift_l(bl, bh, 3) - (384u << 23);
+  const unsigned int hb = (mag & 0x7FFFFFFFu) | (bh & 0x80000000u);
+  hi = __uint_as_float(hb);
+  const unsigned int sc = hb & 0xFF800000u;  // +-2^E
+  const float r =
+      __fsub_rn(__uint_as_float(((bl >> 6) & 0x7FFFFFu) | (104u << 23)), 0x1p-23f);  // rem * 2^-46
+  lo = __fmul_rn(r, __uint_as_float(sc));
+}
+
+// True when 2^-40 <= |v| < 2^40, from the high word alone: doubling drops the sign and puts the
+// exponent in bits 31..21, whose unsigned offset from 983 << 21 is below 80 << 21 exactly when
+// the exponent field is in [983, 1063) (the mantissa bits below cannot carry into bit 21).
+__device__ __forceinline__ bool df_in_range(double v) {
+  const unsigned int bh = (unsigned int)__double2hiint(v);
+  return (bh * 2u - (983u << 21)) < (80u << 21);
+}
+
 // (hi + lo) * (a_hi + a_lo) for two split doubles, relative error about 2^-46.
 __device__ __forceinline__ DF df_mul(float ah, float al, float bh, float bl) {
   DF p;

@@ -38,12 +38,14 @@
 #include <climits>
 #include <cstdio>
 #include <mutex>
+#include <string>
 #include <type_traits>
 
 #include "common.cuh"
 #include "df.cuh"
 #include "kernels.h"
 #include "wmerge.cuh"
+#include "wtile.cuh"
 
 namespace tacogb {
 
@@ -69,16 +71,9 @@ __global__ void spmv_split_x(const double* __restrict__ x, DF* __restrict__ xdf,
 // (i+1, pos[i+1]), so that only rows of snap_len or more nonzeros are split between tiles;
 // snap_len < T keeps every short row within one boundary, so coordinates stay monotone.
 // Boundary 0 never moves: the first tile starts at (0, 0).
-__global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t n,
-                                        int64_t nnz, uint32_t T, int32_t tiles,
-                                        int32_t snap_len, int2* __restrict__ part) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > n) return;
-  if (i == n) {
-    part[tiles] = make_int2(n, (int)nnz);
-    return;
-  }
-  const int32_t p0 = __ldg(pos + i), p1 = __ldg(pos + i + 1);
+__device__ __forceinline__ void partition_row_body(int32_t p0, int32_t p1, uint32_t T,
+                                                   int32_t tiles, int32_t snap_len,
+                                                   int2* __restrict__ part, int64_t i) {
   const uint32_t lo = (uint32_t)p0 + (uint32_t)i;
   const uint32_t hi = (uint32_t)p1 + (uint32_t)i;
   const bool snap = (p1 - p0) < snap_len;
@@ -87,10 +82,90 @@ __global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t
                               : make_int2((int)i, (int)((uint64_t)b * T - (uint64_t)i));
 }
 
+// Rows 4g .. 4g+3 (and the end marker when row n falls in the group).  Each thread reads its
+// five pos entries at once (one 16-byte load when pos is 16-byte aligned), so the pass needs a
+// quarter of the dependent load round trips of one row per thread.
+__device__ __forceinline__ void partition_rows4(const int32_t* __restrict__ pos, int32_t n,
+                                                int64_t nnz, uint32_t T, int32_t tiles,
+                                                int32_t snap_len, int2* __restrict__ part,
+                                                int64_t g, bool vec) {
+  const int64_t i0 = 4 * g;
+  if (i0 > n) return;
+  int32_t p[5];
+  if (vec && i0 + 4 <= n) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(pos + i0));
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+    p[3] = v.w;
+    p[4] = __ldg(pos + i0 + 4);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 5; j++) p[j] = (i0 + j <= n) ? __ldg(pos + i0 + j) : 0;
+  }
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const int64_t i = i0 + j;
+    if (i > n) break;
+    if (i == n) {
+      part[tiles] = make_int2(n, (int)nnz);
+      break;
+    }
+    partition_row_body(p[j], p[j + 1], T, tiles, snap_len, part, i);
+  }
+}
+
+__global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t n,
+                                        int64_t nnz, uint32_t T, int32_t tiles,
+                                        int32_t snap_len, int2* __restrict__ part) {
+  const bool vec = ((uintptr_t)pos & 15) == 0;
+  partition_rows4(pos, n, nnz, T, tiles, snap_len, part,
+                  (int64_t)blockIdx.x * blockDim.x + threadIdx.x, vec);
+}
+
+// One pass before the double-float SpMV: thread g writes the tile boundaries inside rows
+// 4g .. 4g+3 (as merge_partition_scatter) and splits x[4g .. 4g+3] into double-float pairs,
+// setting *xflag when an entry lies outside the pairs' range (zeros split exactly).  *xflag is
+// cleared by the fix-up kernel at the end of the same product.
+__global__ void spmv_prep(const int32_t* __restrict__ pos, int32_t n, int64_t nnz, uint32_t T,
+                          int32_t tiles, int2* __restrict__ part, const double* __restrict__ x,
+                          DF* __restrict__ xdf, int32_t cols, int* __restrict__ xflag) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t c0 = 4 * g;
+  if (c0 < cols) {
+    double v[4];
+    if ((((uintptr_t)x | (uintptr_t)xdf) & 15) == 0 && c0 + 4 <= cols) {
+      const double2 a = __ldg(reinterpret_cast<const double2*>(x + c0));
+      const double2 b = __ldg(reinterpret_cast<const double2*>(x + c0 + 2));
+      v[0] = a.x;
+      v[1] = a.y;
+      v[2] = b.x;
+      v[3] = b.y;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; j++) v[j] = (c0 + j < cols) ? __ldg(x + c0 + j) : 0.0;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      DF d;
+      ok &= split_df(v[j], d.h, d.l);
+      if (c0 + j < cols) xdf[c0 + j] = d;
+    }
+    if (!ok) *xflag = 1;
+  }
+  partition_rows4(pos, n, nnz, T, tiles, 0, part, g, ((uintptr_t)pos & 15) == 0);
+}
+
+// Threads needed by the four-rows-per-thread passes over n + 1 pos entries (and cols).
+inline int64_t rows4_threads(int64_t n_plus_1, int64_t cols = 0) {
+  return (std::max(n_plus_1, cols) + 3) / 4;
+}
+
 int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_items,
                     int32_t tiles, int2* part, cudaStream_t st, int32_t snap_len) {
   TACOGB_CHECK_ARG(tile_items > 0 && tile_items < (1ll << 30), "bad merge tile size");
-  const int64_t threads = (int64_t)n + 1;
+  const int64_t threads = rows4_threads((int64_t)n + 1);
   TACOGB_LAUNCH("merge_partition_scatter", st,
                 merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
                     pos, n, nnz, (uint32_t)tile_items, tiles, snap_len, part));
@@ -101,7 +176,7 @@ int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_ite
 // FP64 x for the native fallback (same as xg for unchecked policies); xflag: non-zero when x
 // has entries outside the double-float range.
 template <class P, int IPT, bool TMA, int CH = 4>
-__global__ void __launch_bounds__(kWmBlock, 8)
+__global__ void __launch_bounds__(kWmBlock, (IPT <= 11 ? 8 : 4))
 spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                    const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
                    const typename P::Val* __restrict__ x64, const int* __restrict__ xflag,
@@ -113,11 +188,159 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
   S& s = *reinterpret_cast<S*>(smem_raw);
   const int tile = blockIdx.x;
   const int2 c0 = part[tile], c1 = part[tile + 1];
-  const double carry_d = wm_process_tile<P, IPT, TMA, CH>(
-      s, pos, crd, vals, xg, x64, xflag, y, n, nnz, c0.x, c1.x - c0.x, c0.y, c1.y - c0.y, status);
+  double carry_d;
+  if constexpr (std::is_same<P, PolGP>::value)
+    carry_d = gp_process_tile<P, IPT, TMA>(s, pos, crd, vals, xg, x64, xflag, y, n, nnz, c0.x,
+                                           c1.x - c0.x, c0.y, c1.y - c0.y, status);
+  else
+    carry_d = wm_process_tile<P, IPT, TMA, CH>(s, pos, crd, vals, xg, x64, xflag, y, n, nnz, c0.x,
+                                               c1.x - c0.x, c0.y, c1.y - c0.y, status);
   if (threadIdx.x == 0) {
     carry_row[tile] = c1.x;
     carry_val[tile] = carry_d;
+  }
+}
+
+// ------------------------------------------------------------------ wtile -----------------
+//
+// Warp-level merge tiles (wtile.cuh): CTA b runs tiles 4b .. 4b+3, one per warp, with no CTA
+// barrier; each tile's carry-out goes to the fix-up kernel.
+
+template <class P, int IPT, bool TMA, int CH>
+__global__ void __launch_bounds__(kWtWarps * 32, (IPT <= 7 ? 8 : IPT <= 11 ? 6 : 4))
+spmv_wtile_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+                  const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
+                  const typename P::Val* __restrict__ x64, const int* __restrict__ xflag,
+                  typename P::Out* __restrict__ y, const int2* __restrict__ part, int32_t n,
+                  int32_t nnz, int32_t tiles, int32_t* __restrict__ carry_row,
+                  double* __restrict__ carry_val, int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5;
+  WtSmem<P, IPT>& s = reinterpret_cast<WtSmem<P, IPT>*>(smem_raw)[warp];
+  const int t = blockIdx.x * kWtWarps + warp;
+  if (t >= tiles) return;  // whole warp: nothing below synchronises more than one warp
+  const int2 c0 = part[t], c1 = part[t + 1];
+  const double c = wt_process<P, IPT, TMA, CH>(s, pos, crd, vals, xg, x64, xflag, y, n, nnz, c0.x,
+                                               c1.x - c0.x, c0.y, c1.y - c0.y, status);
+  if ((threadIdx.x & 31) == 0) {
+    carry_row[t] = c1.x;
+    carry_val[t] = c;
+  }
+}
+
+// Persistent warp pipeline (wtile.cuh, WpSmem): warp w of the grid walks tiles
+// [tiles*w/W, tiles*(w+1)/W) with double-buffered staging and chains the open row's carry in a
+// register; one carry per warp goes to the fix-up kernel.
+template <class P, int IPT, int CH, bool STRIDED>
+__global__ void __launch_bounds__(kWtWarps * 32, 6)
+spmv_wpipe_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+                  const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
+                  const typename P::Val* __restrict__ x64, const int* __restrict__ xflag,
+                  typename P::Out* __restrict__ y, const int2* __restrict__ part, int32_t n,
+                  int32_t nnz, int32_t tiles, int32_t* __restrict__ carry_row,
+                  double* __restrict__ carry_val, int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WpSmem<P, IPT>& s = reinterpret_cast<WpSmem<P, IPT>*>(smem_raw)[warp];
+  const int64_t W = (int64_t)gridDim.x * kWtWarps, gw = (int64_t)blockIdx.x * kWtWarps + warp;
+  // contiguous runs chain carries; strided assignment (tiles gw, gw + W, ...) keeps the warps
+  // of the grid streaming one window of the matrix and writes one carry per tile
+  const int tstep = STRIDED ? (int)W : 1;
+  const int t0 = STRIDED ? (int)gw : (int)(tiles * gw / W);
+  const int t1 = STRIDED ? tiles : (int)(tiles * (gw + 1) / W);
+  auto next_t = [&](int t) { return t + tstep; };
+  if (lane == 0) {
+    mbar_init(&s.bar[0], 1);
+    mbar_init(&s.bar[1], 1);
+  }
+  __syncwarp();
+  const bool xok = (xflag == nullptr || *xflag == 0);
+  double carry_in = 0.0;
+  const int tf = min(t0, tiles);
+  int2 c0 = part[tf], c1 = part[t0 < t1 ? tf + 1 : tf];
+  int3 off_cur = make_int3(0, 0, 0), off_next = make_int3(0, 0, 0);
+  if (t0 < t1)
+    off_cur = wp_issue<P, IPT>(s.st[0], &s.bar[0], pos, crd, vals, n, nnz, c0.x, c1.x - c0.x,
+                               c0.y, c1.y - c0.y);
+  for (int t = t0, i = 0; t < t1; t = next_t(t), i++) {
+    const int buf = i & 1;
+    const int r0 = c0.x, k0 = c0.y, rn = c1.x - c0.x, kn = c1.y - c0.y;
+    int2 nc0 = c1, nc1 = c1;
+    const int tn = next_t(t);
+    if (tn < t1) {
+      nc0 = part[tn];
+      nc1 = part[tn + 1];
+      off_next = wp_issue<P, IPT>(s.st[buf ^ 1], &s.bar[buf ^ 1], pos, crd, vals, n, nnz, nc0.x,
+                                  nc1.x - nc0.x, nc0.y, nc1.y - nc0.y);
+    }
+    __syncwarp();  // every lane's tail loads of this stage are visible
+    mbar_wait_or_flag(&s.bar[buf], (uint32_t)((i >> 1) & 1), status);
+    const WpStage<P, IPT>& g = s.st[buf];
+    const int32_t* scrd = g.crd + off_cur.x;
+    const typename P::Val* sval = g.val + off_cur.y;
+    const int32_t* sre = g.re + off_cur.z;
+    int row, ks;
+    tile_search(sre, rn, kn, k0, min(lane * IPT, rn + kn), row, ks);
+    int row_e = __shfl_down_sync(0xffffffffu, row, 1), ke = __shfl_down_sync(0xffffffffu, ks, 1);
+    if (lane == 31) {
+      row_e = rn;
+      ke = kn;
+    }
+    double c;
+    bool native = !P::kChecked;
+    if constexpr (P::kChecked) {
+      typename P::Acc open, first;
+      int first_row;
+      bool ok = xok;
+      if (__all_sync(0xffffffffu, ok))
+        ok = wt_walk<P, IPT, CH>(scrd, sval, sre, xg, row, ks, row_e, ke, k0, s.y, open, first,
+                                 first_row);
+      if (__all_sync(0xffffffffu, ok)) {
+        const typename P::Acc cc = wt_join<P>(open, row_e, first, first_row, s.y);
+        __syncwarp();
+        for (int q = lane; q < rn; q += 32) {
+          double v = P::to_double(as_acc<typename P::Acc>(s.y[q]));
+          if (q == 0) v = __dadd_rn(v, carry_in);
+          y[r0 + q] = (typename P::Out)v;
+        }
+        c = P::to_double(cc);
+      } else {
+        native = true;
+      }
+    }
+    if (native) {
+      using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
+      typename Q::Acc open, first;
+      int first_row;
+      wt_walk<Q, IPT, CH>(scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64,
+                          row, ks, row_e, ke, k0, s.y, open, first, first_row);
+      const typename Q::Acc cc = wt_join<Q>(open, row_e, first, first_row, s.y);
+      __syncwarp();
+      for (int q = lane; q < rn; q += 32) {
+        double v = Q::to_double(as_acc<typename Q::Acc>(s.y[q]));
+        if (q == 0) v = __dadd_rn(v, carry_in);
+        y[r0 + q] = (typename P::Out)v;
+      }
+      c = Q::to_double(cc);
+    }
+    if constexpr (STRIDED) {
+      if (lane == 0) {
+        carry_row[t] = c1.x;
+        carry_val[t] = c;
+      }
+    } else {
+      carry_in = (rn > 0) ? c : __dadd_rn(carry_in, c);
+    }
+    __syncwarp();  // this stage and the row staging are free before they are reused
+    c0 = nc0;
+    c1 = nc1;
+    off_cur = off_next;
+  }
+  if (!STRIDED && lane == 0) {
+    // a warp without tiles reports the row at its merge position with a zero carry, so that
+    // the carries of a row stay one consecutive run for the fix-up kernel
+    carry_row[gw] = part[t1].x;
+    carry_val[gw] = carry_in;
   }
 }
 
@@ -257,24 +480,44 @@ spmv_pmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
     off_cur = off_next;
   }
   if (tid == 0) {
-    carry_row[cb] = (t0 < t1) ? part[t1].x : n;
+    carry_row[cb] = part[t1].x;  // a CTA without tiles keeps the run of carries unbroken
     carry_val[cb] = carry_in;
   }
 }
 
 // Adds the tile carry-outs to the rows that continue into later tiles.  Tiles carrying the same
 // row are consecutive; the first tile of each run sums the run in tile order.
+// xflag (optional) is the x-range flag of the product, cleared here for the next one.
+// The first tile of each run sums the run in tile order; it fetches the run eight entries at a
+// time with independent loads, so a row spanning many tiles costs few dependent round trips
+// while the order of the additions (and so the result) stays that of a serial sum.
 template <typename Out>
 __global__ void spmv_carry_fixup(const int32_t* __restrict__ carry_row,
                                  const double* __restrict__ carry_val, int32_t tiles,
-                                 Out* __restrict__ y, int32_t n) {
+                                 Out* __restrict__ y, int32_t n, int* __restrict__ xflag = nullptr) {
   const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0 && xflag != nullptr) *xflag = 0;
   if (t >= tiles) return;
   const int32_t r = carry_row[t];
   if (r >= n) return;
   if (t > 0 && carry_row[t - 1] == r) return;
   double tot = carry_val[t];
-  for (int32_t u = t + 1; u < tiles && carry_row[u] == r; u++) tot += carry_val[u];
+  for (int32_t u = t + 1; u < tiles; u += 8) {
+    int32_t rr[8];
+    double vv[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      rr[j] = (u + j < tiles) ? carry_row[u + j] : -1;
+      vv[j] = (u + j < tiles) ? carry_val[u + j] : 0.0;
+    }
+    bool more = true;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      more = more && rr[j] == r;
+      if (more) tot += vv[j];
+    }
+    if (!more) break;
+  }
   y[r] = (Out)((double)y[r] + tot);
 }
 
@@ -317,7 +560,12 @@ struct SpmvVariant {
                // 3 wmerge double-float (x split in the walk), 4 pmerge native,
                // 5 pmerge double-float (x split in the walk), 6 wmerge hybrid
                // (DFMA and double-float items interleaved), 7 family 3 with 8-deep gathers,
-               // 8 family 3 with four accumulators, 9 both
+               // 8 family 3 with four accumulators, 9 both, 10 wmerge PolDFS (x split in the
+               // partition pass, eight-instruction value split), 11 family 10, 8-deep gathers,
+               // 12 gmerge: product-staged tiles (gathers and products in nonzero order, then
+               // a walk over products in shared memory), 13 wtile (warp-level merge tiles)
+               // with PolDFS, 14 wtile native, 15 wpipe (persistent double-buffered warp
+               // tiles) with PolDFS, 16 wpipe native, 17 wpipe PolDFS with 8-deep gathers
   int param;   // IPT for wmerge, G for vector
 };
 
@@ -330,6 +578,15 @@ const SpmvVariant kSpmvVariants[] = {
     {"wmerge_hyb_ipt7", 6, 7},   {"wmerge_hyb_ipt11", 6, 11},
     {"wmerge_dfx_ipt7_c8", 7, 7}, {"wmerge_dfx4_ipt7", 8, 7}, {"wmerge_dfx_ipt5", 3, 5},
     {"wmerge_dfx_ipt9", 3, 9},   {"wmerge_dfx4_ipt11_c8", 9, 11},
+    {"wmerge_dfs_ipt7", 10, 7},  {"wmerge_dfs_ipt11", 10, 11}, {"wmerge_dfs_ipt15", 10, 15},
+    {"wmerge_dfs_ipt19", 10, 19}, {"wmerge_dfs_ipt15_c8", 11, 15},
+    {"gmerge_ipt5", 12, 5},      {"gmerge_ipt7", 12, 7},      {"gmerge_ipt9", 12, 9},
+    {"gmerge_ipt11", 12, 11},    {"gmerge_ipt15", 12, 15},
+    {"wtile_dfs_ipt7", 13, 7},   {"wtile_dfs_ipt9", 13, 9},   {"wtile_dfs_ipt11", 13, 11},
+    {"wtile_dfs_ipt15", 13, 15}, {"wtile_native_ipt7", 14, 7},
+    {"wpipe_dfs_ipt7", 15, 7},   {"wpipe_dfs_ipt9", 15, 9},   {"wpipe_native_ipt7", 16, 7},
+    {"wpipe_dfs_ipt7_c8", 17, 7}, {"wpipe_s_dfs_ipt7", 18, 7}, {"wpipe_s_native_ipt7", 19, 7},
+    {"wpipe_s_dfs_ipt9", 18, 9},
 };
 constexpr int kNumSpmvVariants = sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]);
 
@@ -343,13 +600,16 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
   if (tiles64 == 0) return 0;
   TACOGB_CHECK_ARG(tiles64 < (1ll << 31), "SpMV: too many merge tiles");
   const int32_t tiles = (int32_t)tiles64;
-  // x pre-split into double-float pairs when the policy gathers DF entries
-  constexpr bool presplit = std::is_same<typename P::XG, DF>::value;
+  // x pre-split into double-float pairs when the policy gathers DF entries; PolDFS fuses the
+  // split into the partition pass and keeps its x-range flag in the device status block.
+  constexpr bool fused = std::is_same<P, PolDFS>::value || std::is_same<P, PolGP>::value;
+  constexpr bool presplit = std::is_same<typename P::XG, DF>::value && !fused;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
   const size_t crow_bytes = al((size_t)tiles * sizeof(int32_t));
   const size_t cval_bytes = al((size_t)tiles * sizeof(double));
-  const size_t xdf_bytes = presplit ? al((size_t)A->cols * sizeof(DF)) + 256 : 0;
+  const size_t xdf_bytes =
+      presplit ? al((size_t)A->cols * sizeof(DF)) + 256 : fused ? al((size_t)A->cols * sizeof(DF)) : 0;
   unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + xdf_bytes, 0);
   if (!ws) return last_code();
   int2* part = (int2*)ws;
@@ -370,20 +630,151 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
     xg = (const typename P::XG*)xdf;
     xflag = flag;
   }
-  if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
+  int* fixup_flag = nullptr;
+  if constexpr (fused) {
+    DF* xdf = (DF*)(ws + part_bytes + crow_bytes + cval_bytes);
+    fixup_flag = status + kXFlagWord;
+    const int64_t threads = rows4_threads((int64_t)A->rows + 1, A->cols);
+    TACOGB_LAUNCH("spmv_prep", st,
+                  spmv_prep<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                      A->pos, A->rows, A->nnz, (uint32_t)tile_items, tiles, part,
+                      (const double*)x, xdf, A->cols, fixup_flag));
+    xg = (const typename P::XG*)xdf;
+    xflag = fixup_flag;
+  } else {
+    if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
+  }
   // Bulk copies need 16-byte aligned sources: true for every allocator the library meets
   // (cudaMalloc, cudaMallocManaged, torch); sliced pointers take the register-staged kernel.
   const bool tma = (((uintptr_t)A->pos | (uintptr_t)A->crd | (uintptr_t)A->vals) & 15) == 0;
   auto kern = tma ? spmv_wmerge_kernel<P, IPT, true, CH> : spmv_wmerge_kernel<P, IPT, false, CH>;
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(S)));
+  TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, 85));
   TACOGB_LAUNCH("spmv_wmerge_kernel", st,
                 kern<<<tiles, kWmBlock, sizeof(S), st>>>(
                     A->pos, A->crd, (const typename P::Val*)A->vals, xg, x, xflag, y, part,
                     A->rows, (int32_t)A->nnz, crow, cval, status));
   TACOGB_LAUNCH("spmv_carry_fixup", st,
                 spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(
-                    crow, cval, tiles, y, A->rows));
+                    crow, cval, tiles, y, A->rows, fixup_flag));
+  return 0;
+}
+
+template <class P, int IPT, int CH = 4>
+int launch_wtile(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
+                 cudaStream_t st) {
+  using S = WtSmem<P, IPT>;
+  const int64_t tile_items = S::ITEMS;
+  const int64_t total = (int64_t)A->rows + A->nnz;
+  const int64_t tiles64 = (total + tile_items - 1) / tile_items;
+  if (tiles64 == 0) return 0;
+  TACOGB_CHECK_ARG(tiles64 < (1ll << 31) - 8, "SpMV: too many merge tiles");
+  const int32_t tiles = (int32_t)tiles64;
+  constexpr bool split = std::is_same<typename P::XG, DF>::value;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
+  const size_t crow_bytes = al((size_t)tiles * sizeof(int32_t));
+  const size_t cval_bytes = al((size_t)tiles * sizeof(double));
+  const size_t xdf_bytes = split ? al((size_t)A->cols * sizeof(DF)) : 0;
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + xdf_bytes, 0);
+  if (!ws) return last_code();
+  int2* part = (int2*)ws;
+  int32_t* crow = (int32_t*)(ws + part_bytes);
+  double* cval = (double*)(ws + part_bytes + crow_bytes);
+  int* status = device_status();
+  if (!status) return last_code();
+  const typename P::XG* xg = (const typename P::XG*)x;
+  int* xflag = nullptr;
+  if constexpr (split) {
+    DF* xdf = (DF*)(ws + part_bytes + crow_bytes + cval_bytes);
+    xflag = status + kXFlagWord;
+    const int64_t threads = rows4_threads((int64_t)A->rows + 1, A->cols);
+    TACOGB_LAUNCH("spmv_prep", st,
+                  spmv_prep<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                      A->pos, A->rows, A->nnz, (uint32_t)tile_items, tiles, part,
+                      (const double*)x, xdf, A->cols, xflag));
+    xg = (const typename P::XG*)xdf;
+  } else {
+    if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
+  }
+  const bool tma = (((uintptr_t)A->pos | (uintptr_t)A->crd | (uintptr_t)A->vals) & 15) == 0;
+  auto kern = tma ? spmv_wtile_kernel<P, IPT, true, CH> : spmv_wtile_kernel<P, IPT, false, CH>;
+  const int smem = (int)(sizeof(S) * kWtWarps);
+  TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  // carveouts measured best per tile size (random-column gathers want L1 room; the banded
+  // matrices run fastest at IPT 9 with the driver's choice)
+  constexpr int carve = IPT == 7 ? 70 : IPT == 9 ? -1 : 85;
+  TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, carve));
+  const int grid = (tiles + kWtWarps - 1) / kWtWarps;
+  TACOGB_LAUNCH("spmv_wtile_kernel", st,
+                kern<<<grid, kWtWarps * 32, smem, st>>>(
+                    A->pos, A->crd, (const typename P::Val*)A->vals, xg, x, xflag, y, part,
+                    A->rows, (int32_t)A->nnz, tiles, crow, cval, status));
+  TACOGB_LAUNCH("spmv_carry_fixup", st,
+                spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(
+                    crow, cval, tiles, y, A->rows, xflag));
+  return 0;
+}
+
+template <class P, int IPT, int CH = 4, bool STRIDED = false>
+int launch_wpipe(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
+                 cudaStream_t st) {
+  using S = WpSmem<P, IPT>;
+  const int64_t tile_items = 32 * IPT;
+  const int64_t total = (int64_t)A->rows + A->nnz;
+  const int64_t tiles64 = (total + tile_items - 1) / tile_items;
+  if (tiles64 == 0) return 0;
+  TACOGB_CHECK_ARG(tiles64 < (1ll << 31) - 8, "SpMV: too many merge tiles");
+  const int32_t tiles = (int32_t)tiles64;
+  // bulk copies need 16-byte aligned sources; otherwise the non-persistent warp tiles run
+  if ((((uintptr_t)A->pos | (uintptr_t)A->crd | (uintptr_t)A->vals) & 15) != 0)
+    return launch_wtile<P, IPT, CH>(A, x, y, st);
+  auto kern = spmv_wpipe_kernel<P, IPT, CH, STRIDED>;
+  const int smem = (int)(sizeof(S) * kWtWarps);
+  TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, 85));
+  int per_sm = 0;
+  TACOGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWtWarps * 32,
+                                                                smem));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t warps64 = std::min<int64_t>(tiles64, (int64_t)sm_count() * per_sm * kWtWarps);
+  const int grid = (int)((warps64 + kWtWarps - 1) / kWtWarps);
+  const int nw = STRIDED ? tiles : grid * kWtWarps;  // carry entries
+  constexpr bool split = std::is_same<typename P::XG, DF>::value;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
+  const size_t crow_bytes = al((size_t)nw * sizeof(int32_t));
+  const size_t cval_bytes = al((size_t)nw * sizeof(double));
+  const size_t xdf_bytes = split ? al((size_t)A->cols * sizeof(DF)) : 0;
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + xdf_bytes, 0);
+  if (!ws) return last_code();
+  int2* part = (int2*)ws;
+  int32_t* crow = (int32_t*)(ws + part_bytes);
+  double* cval = (double*)(ws + part_bytes + crow_bytes);
+  int* status = device_status();
+  if (!status) return last_code();
+  const typename P::XG* xg = (const typename P::XG*)x;
+  int* xflag = nullptr;
+  if constexpr (split) {
+    DF* xdf = (DF*)(ws + part_bytes + crow_bytes + cval_bytes);
+    xflag = status + kXFlagWord;
+    const int64_t threads = rows4_threads((int64_t)A->rows + 1, A->cols);
+    TACOGB_LAUNCH("spmv_prep", st,
+                  spmv_prep<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                      A->pos, A->rows, A->nnz, (uint32_t)tile_items, tiles, part,
+                      (const double*)x, xdf, A->cols, xflag));
+    xg = (const typename P::XG*)xdf;
+  } else {
+    if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
+  }
+  TACOGB_LAUNCH("spmv_wpipe_kernel", st,
+                kern<<<grid, kWtWarps * 32, smem, st>>>(
+                    A->pos, A->crd, (const typename P::Val*)A->vals, xg, x, xflag, y, part,
+                    A->rows, (int32_t)A->nnz, tiles, crow, cval, status));
+  TACOGB_LAUNCH("spmv_carry_fixup", st,
+                spmv_carry_fixup<typename P::Out><<<(nw + 255) / 256, 256, 0, st>>>(
+                    crow, cval, nw, y, A->rows, xflag));
   return 0;
 }
 
@@ -400,6 +791,7 @@ int launch_pmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
   auto kern = spmv_pmerge_kernel<P, IPT>;
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(S)));
+  TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, -1));
   int per_sm = 0;
   TACOGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWmBlock,
                                                                 sizeof(S)));
@@ -468,6 +860,55 @@ int spmv_typed(const tacogb_csr* A, const V* x, V* y, int variant, cudaStream_t 
   if (v.family == 7) return launch_wmerge<DblX, 7, 8>(A, x, y, st);
   if (v.family == 8) return launch_wmerge<DblX4, 7>(A, x, y, st);
   if (v.family == 9) return launch_wmerge<DblX4, 11, 8>(A, x, y, st);
+  if (v.family == 10 || v.family == 11) {
+    if constexpr (sizeof(V) == 8) {
+      if (v.family == 11) return launch_wmerge<PolDFS, 15, 8>(A, x, y, st);
+      switch (v.param) {
+        case 7: return launch_wmerge<PolDFS, 7>(A, x, y, st);
+        case 11: return launch_wmerge<PolDFS, 11>(A, x, y, st);
+        case 15: return launch_wmerge<PolDFS, 15>(A, x, y, st);
+        default: return launch_wmerge<PolDFS, 19>(A, x, y, st);
+      }
+    } else {
+      return launch_wmerge<PolComp32, 7>(A, x, y, st);
+    }
+  }
+  if (v.family == 12) {
+    if constexpr (sizeof(V) == 8) {
+      switch (v.param) {
+        case 5: return launch_wmerge<PolGP, 5>(A, x, y, st);
+        case 7: return launch_wmerge<PolGP, 7>(A, x, y, st);
+        case 9: return launch_wmerge<PolGP, 9>(A, x, y, st);
+        case 11: return launch_wmerge<PolGP, 11>(A, x, y, st);
+        default: return launch_wmerge<PolGP, 15>(A, x, y, st);
+      }
+    } else {
+      return launch_wmerge<PolComp32, 7>(A, x, y, st);
+    }
+  }
+  if (v.family == 13) {
+    using Pol = typename std::conditional<sizeof(V) == 8, PolDFS, PolComp32>::type;
+    switch (v.param) {
+      case 7: return launch_wtile<Pol, 7>(A, x, y, st);
+      case 9: return launch_wtile<Pol, 9>(A, x, y, st);
+      case 11: return launch_wtile<Pol, 11>(A, x, y, st);
+      default: return launch_wtile<Pol, 15>(A, x, y, st);
+    }
+  }
+  if (v.family == 14) return launch_wtile<Native, 7>(A, x, y, st);
+  if (v.family == 15 || v.family == 17) {
+    using Pol = typename std::conditional<sizeof(V) == 8, PolDFS, PolComp32>::type;
+    if (v.family == 17) return launch_wpipe<Pol, 7, 8>(A, x, y, st);
+    if (v.param == 9) return launch_wpipe<Pol, 9>(A, x, y, st);
+    return launch_wpipe<Pol, 7>(A, x, y, st);
+  }
+  if (v.family == 16) return launch_wpipe<Native, 7>(A, x, y, st);
+  if (v.family == 18) {
+    using Pol = typename std::conditional<sizeof(V) == 8, PolDFS, PolComp32>::type;
+    if (v.param == 9) return launch_wpipe<Pol, 9, 4, true>(A, x, y, st);
+    return launch_wpipe<Pol, 7, 4, true>(A, x, y, st);
+  }
+  if (v.family == 19) return launch_wpipe<Native, 7, 4, true>(A, x, y, st);
   if (v.family == 4) return launch_pmerge<Native, 7>(A, x, y, st);
   if (v.family == 6) {
     using Hyb = typename std::conditional<sizeof(V) == 8, PolHybrid, PolComp32>::type;
@@ -497,12 +938,18 @@ const char* spmv_variant_name(int v) {
   return (v >= 0 && v < kNumSpmvVariants) ? kSpmvVariants[v].name : "";
 }
 
-// Structural rule used when neither a tuning record nor the cost model gives a choice: the
-// merge family is robust to any skew, and for FP64 values the double-float policy keeps the
-// kernel off GB300's narrow FP64 pipe (IPT 7 measured fastest on the power-law workload).
+// Structural rule used when neither a tuning record nor the cost model gives a choice: warp
+// merge tiles are robust to any skew; with no CTA-wide joins the per-tile FP64 work is small,
+// so native DFMA accumulation (taco's own arithmetic) keeps pace with the x gathers that bound
+// random-column matrices (measured fastest on the 4,194,304-row power-law workload).
 int spmv_default_variant(const tacogb_csr* A) {
   (void)A;
-  return 10;  // wmerge_dfx_ipt7: double-float for FP64 values, compensated FP32 for FP32
+  static const int v = [] {
+    for (int i = 0; i < kNumSpmvVariants; i++)
+      if (std::string(kSpmvVariants[i].name) == "wtile_native_ipt7") return i;
+    return 0;
+  }();
+  return v;  // wtile_native_ipt7: DFMA for FP64 values, compensated FP32 for FP32
 }
 
 int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStream_t st) {
@@ -600,7 +1047,7 @@ int launch_wmerge_noalloc(const tacogb_csr* A, const typename P::Val* x, typenam
   double* cval = (double*)(ws + l.part_bytes + l.crow_bytes);
   // Every entry of part, crow and cval is written before it is read, so the contents left by
   // an earlier call need no clearing.
-  const int64_t threads = (int64_t)A->rows + 1;
+  const int64_t threads = rows4_threads((int64_t)A->rows + 1);
   count_launch();
   merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
       A->pos, A->rows, A->nnz, (uint32_t)kNoAllocTileItems, tiles, 0, part);
@@ -608,6 +1055,7 @@ int launch_wmerge_noalloc(const tacogb_csr* A, const typename P::Val* x, typenam
   auto kern = spmv_wmerge_kernel<P, kNoAllocIpt, false>;
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sizeof(S)));
+  TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, -1));
   count_launch();
   kern<<<tiles, kWmBlock, sizeof(S), st>>>(A->pos, A->crd, (const typename P::Val*)A->vals,
                                           (const typename P::XG*)x, x, nullptr, y, part, A->rows,

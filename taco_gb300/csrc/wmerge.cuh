@@ -188,6 +188,47 @@ struct PolHybrid {
   };
 };
 
+// FP64 values in double-float with the fewest FP32-pipe instructions per nonzero (about 22):
+// x arrives pre-split; each value is split by split_df_fast and range-checked from its high
+// word; the walk keeps a running hi sum s and an unnormalised compensation c, so each product
+// costs one exact TwoProduct of the hi parts, two cross-term FMAs into c and one TwoSum into
+// s, and the renormalisation to a double-float pair happens once per row end.  |c| stays near
+// 2^-24 of the partial sums it collects, so the row error stays about 2^-46 of sum |a x|.
+struct PolDFS : PolDF64 {
+  struct W {
+    struct State {
+      float s, c;
+    };
+    __device__ static State init() { return State{0.f, 0.f}; }
+    template <int J>
+    __device__ static bool step(State& st, double a, DF x) {
+      float ah, al;
+      split_df_fast(a, ah, al);
+      const float ph = __fmul_rn(ah, x.h);
+      const float pe = __fmaf_rn(ah, x.h, -ph);
+      float c = __fmaf_rn(ah, x.l, st.c);
+      c = __fmaf_rn(al, x.h, c);
+      float s1, e;
+      two_sum(st.s, ph, s1, e);
+      st.c = __fadd_rn(c, __fadd_rn(pe, e));
+      st.s = s1;
+      return df_in_range(a);
+    }
+    __device__ static DF take(State& st) {
+      DF r;
+      float e;
+      two_sum(st.s, st.c, r.h, e);
+      r.l = e;
+      st.s = 0.f;
+      st.c = 0.f;
+      return r;
+    }
+  };
+};
+
+// Tag policy selecting the product-staged tile (gp_process_tile) for FP64 values.
+struct PolGP : PolDFS {};
+
 // ------------------------------------------------------------------ wmerge ----------------
 
 // 128-thread CTAs with a small shared-memory footprint, so that many tiles are in flight per
@@ -285,11 +326,26 @@ __device__ __forceinline__ void wm_stage(WmSmem<P, IPT>& s, const int32_t* __res
 }
 
 template <typename T>
-__device__ __forceinline__ T ldg_xg(const T* p) { return __ldg(p); }
+__device__ __forceinline__ T ldg_xg(const T* p);
+// Gathers of x use ld.global.cg: on GB300 random 8-byte gathers through it run at up to ~0.88
+// per clock per SM against ~0.79 for ld.global.nc (measured with a 60 KB L1).
+template <>
+__device__ __forceinline__ double ldg_xg<double>(const double* p) {
+  double v;
+  asm("ld.global.cg.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+template <>
+__device__ __forceinline__ float ldg_xg<float>(const float* p) {
+  float v;
+  asm("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
 template <>
 __device__ __forceinline__ DF ldg_xg<DF>(const DF* p) {
-  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
-  return DF{v.x, v.y};
+  DF v;
+  asm("ld.global.cg.v2.f32 {%0, %1}, [%2];" : "=f"(v.h), "=f"(v.l) : "l"(p));
+  return v;
 }
 
 // Tile-local merge coordinate of diagonal d (rows ended, nonzeros consumed).
@@ -310,6 +366,10 @@ __device__ __forceinline__ A& as_acc(double& slot) {
   return *reinterpret_cast<A*>(&slot);
 }
 
+template <class P, class S>
+__device__ __forceinline__ void wm_join(S& s, typename P::Acc accv, int key, typename P::Acc first,
+                                        int first_row, int rn, typename P::Acc& carry);
+
 // Walks this lane's IPT merge items over the staged tile with policy P, gathering x in chunks
 // of CH independent loads inside the walk (other warps' arithmetic hides their latency), joins
 // lanes and warps, and leaves every row result of the tile in s.y; the part of the row still
@@ -322,7 +382,7 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
   using Acc = typename P::Acc;
   using Val = typename P::Val;
   using XG = typename P::XG;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int items = rn + kn;
   // One merge-path search per thread: a lane's walk ends where the next lane's begins.
   int row, ks;
@@ -378,11 +438,21 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
     }
   }
   while (row < row_e) emit(row);
-  const Acc accv = Wk::take(st);
+  wm_join<P>(s, Wk::take(st), row_e, first, first_row, rn, carry);
+  return ok;
+}
 
+// Joins the lanes' open rows: `accv` is this lane's sum for row `key` (its last, still open
+// row), `first` its sum for `first_row` (the first row it ended, -1 if none), which may have
+// begun in earlier lanes.  Leaves every row result of the tile in s.y and the part of the row
+// still open at the tile end in `carry` (thread 0).
+template <class P, class S>
+__device__ __forceinline__ void wm_join(S& s, typename P::Acc accv, int key, typename P::Acc first,
+                                        int first_row, int rn, typename P::Acc& carry) {
+  using Acc = typename P::Acc;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // Segmented inclusive scan of lane carries keyed by the open row (keys are non-decreasing
   // along the lanes, so equal keys are contiguous).
-  const int key = row_e;
   Acc sc = accv;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
@@ -421,7 +491,152 @@ __device__ __forceinline__ bool wm_tile(S& s, const int32_t* scrd, const typenam
     }
   }
   __syncthreads();
-  return ok;
+}
+
+// ------------------------------------------------------------------ product-staged tile ---
+//
+// The same merge tile in two phases.  Phase 1 takes the tile's nonzeros in order, thread tid
+// owning items tid, tid + 128, ...: it reads the staged columns (consecutive, so free of bank
+// conflicts), issues all of its IPT gathers of x at once (no dependence between them, so they
+// overlap one another and the merge-path search that follows), then forms each product as a
+// double-float pair and stores it over the staged value.  Phase 2 is the merge walk, which now
+// reads products from shared memory only and sums them with TwoSum: no global load waits
+// inside the walk.  FP64 values only (a product pair fills a value's 8-byte slot).
+
+// Product of one FP64 value with a pre-split x entry as an unevaluated pair; false when the
+// value lies outside the double-float range.
+__device__ __forceinline__ bool gp_product(double a, DF x, DF& p) {
+  float ah, al;
+  split_df_fast(a, ah, al);
+  p.h = __fmul_rn(ah, x.h);
+  const float pe = __fmaf_rn(ah, x.h, -p.h);
+  p.l = __fmaf_rn(ah, x.l, __fmaf_rn(al, x.h, pe));
+  return df_in_range(a);
+}
+
+// Phase 1 (see above).  Also runs the lanes' merge-path search between the gathers and their
+// use.  Returns false (every thread) when some value of the tile is out of range.
+template <int IPT, class S>
+__device__ __forceinline__ bool gp_products(S& s, const int32_t* scrd, double* sval,
+                                            const int32_t* sre, const DF* __restrict__ x, int rn,
+                                            int kn, int k0) {
+  const int tid = threadIdx.x;
+  DF xv[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    const int i = tid + j * kWmBlock;
+    if (i < kn) {
+      const float2 v = __ldg(reinterpret_cast<const float2*>(x + scrd[i]));
+      xv[j] = DF{v.x, v.y};
+    }
+  }
+  const int items = rn + kn;
+  int row, ks;
+  tile_search(sre, rn, kn, k0, min(tid * IPT, items), row, ks);
+  s.lane_start[tid] = make_int2(row, ks);
+  if (tid == 0) {
+    int r, k;
+    tile_search(sre, rn, kn, k0, min(kWmBlock * IPT, items), r, k);
+    s.lane_start[kWmBlock] = make_int2(r, k);
+  }
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    const int i = tid + j * kWmBlock;
+    if (i < kn) {
+      DF p;
+      ok &= gp_product(sval[i], xv[j], p);
+      as_acc<DF>(sval[i]) = p;
+    }
+  }
+  return __syncthreads_and(ok);
+}
+
+// Phase 2: the lane walks its merge items over the staged products; rows are joined as in
+// wm_tile.  The open row's sum is kept as a running hi part s and an unnormalised
+// compensation c; each product costs one TwoSum.
+template <class P, int IPT, class S>
+__device__ __forceinline__ void gp_walk(S& s, const DF* sprod, const int32_t* sre, int rn, int k0,
+                                        DF& carry) {
+  const int tid = threadIdx.x;
+  int row = s.lane_start[tid].x;
+  const int ks = s.lane_start[tid].y;
+  const int row_e = s.lane_start[tid + 1].x, ke = s.lane_start[tid + 1].y;
+  const int cnt = ke - ks;
+  const int base = k0 + ks;
+  int next_end = row < row_e ? sre[row] - base : INT_MAX;  // lane-local index of the next row end
+  DF pv[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; j++)
+    if (j < cnt) pv[j] = sprod[ks + j];
+  float hs = 0.f, hc = 0.f;
+  DF first = DF{0.f, 0.f};
+  int first_row = -1;
+  auto emit = [&](int r) {
+    DF v;
+    two_sum(hs, hc, v.h, v.l);
+    hs = 0.f;
+    hc = 0.f;
+    if (first_row < 0) {
+      first_row = r;
+      first = v;
+    } else {
+      as_acc<DF>(s.y[r]) = v;
+    }
+    row = r + 1;
+    next_end = row < row_e ? sre[row] - base : INT_MAX;
+  };
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    while (next_end <= j) emit(row);
+    if (j < cnt) {
+      float s1, e;
+      two_sum(hs, pv[j].h, s1, e);
+      hc = __fadd_rn(hc, __fadd_rn(e, pv[j].l));
+      hs = s1;
+    }
+  }
+  while (row < row_e) emit(row);
+  DF acc;
+  two_sum(hs, hc, acc.h, acc.l);
+  wm_join<P>(s, acc, row_e, first, first_row, rn, carry);
+}
+
+// One product-staged tile with native FP64 redo: stage, products (+ search), walk, write y;
+// when a value or x entry is outside the double-float range the tile is staged again and
+// walked with DFMA.  Returns the FP64 carry-out (thread 0).
+template <class P, int IPT, bool TMA>
+__device__ __forceinline__ double gp_process_tile(
+    WmSmem<P, IPT>& s, const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+    const double* __restrict__ vals, const DF* __restrict__ xg, const double* __restrict__ x64,
+    const int* __restrict__ xflag, double* __restrict__ y, int32_t n, int32_t nnz, int r0, int rn,
+    int k0, int kn, int* status) {
+  static_assert(std::is_same<typename P::Val, double>::value, "FP64 values only");
+  using S = WmSmem<P, IPT>;
+  const int tid = threadIdx.x;
+  int32_t* scrd;
+  double* sval;
+  const int32_t* sre;
+  wm_stage<TMA, P, IPT>(s, pos, crd, vals, n, nnz, r0, rn, k0, kn, status, scrd, sval, sre);
+  double carry_d = 0.0;
+  if ((xflag == nullptr || *xflag == 0) &&
+      gp_products<IPT>(s, scrd, sval, sre, xg, rn, kn, k0)) {
+    DF carry = DF{0.f, 0.f};
+    gp_walk<PolDF64, IPT>(s, reinterpret_cast<const DF*>(sval), sre, rn, k0, carry);
+    for (int i = tid; i < rn; i += kWmBlock) y[r0 + i] = df_to_double(as_acc<DF>(s.y[i]));
+    carry_d = df_to_double(carry);
+  } else {
+    // products may have overwritten staged values: every thread orders its shared-memory
+    // writes before the copies that stage the tile again
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    wm_stage<TMA, P, IPT>(s, pos, crd, vals, n, nnz, r0, rn, k0, kn, status, scrd, sval, sre);
+    double carry = 0.0;
+    wm_tile<PolNative64, IPT, S>(s, scrd, sval, sre, x64, rn, kn, k0, carry);
+    for (int i = tid; i < rn; i += kWmBlock) y[r0 + i] = s.y[i];
+    carry_d = carry;
+  }
+  return carry_d;
 }
 
 // One tile of rows r0..r0+rn (ends) and nonzeros k0..k0+kn: stage, walk (checked policies first

@@ -30,6 +30,11 @@ def variants():
     return list(range(tg.lib().tacogb_spmv_variant_count()))
 
 
+def by_prefix(prefix):
+    L = tg.lib()
+    return [v for v in variants() if L.tacogb_spmv_variant_name(v).decode().startswith(prefix)]
+
+
 def run_dev(pos, crd, vals, x, variant, dtype=torch.float64):
     A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x), dtype=dtype)
     xd = torch.from_numpy(x).to("cuda", dtype)
@@ -125,28 +130,38 @@ def test_full_size_powerlaw(full_powerlaw, dtype):
     y_ref = O.spmv(pos, crd, vals, x)
     A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x), dtype=dtype)
     xd = torch.from_numpy(x).to("cuda", dtype)
-    y1 = tg.spmv(A, xd, variant=1)  # wmerge_ipt16, native accumulation
-    y2 = tg.spmv(A, xd, variant=1)
+    y1 = tg.spmv(A, xd)  # the default variant
+    y2 = tg.spmv(A, xd)
     torch.cuda.synchronize()
     assert torch.equal(y1, y2)
     tol = F64_TOL if dtype == torch.float64 else F32_TOL
     assert normwise(y1.double().cpu().numpy(), y_ref) <= tol
     z = torch.from_numpy(W.dense(24, len(x))).to("cuda", dtype)
-    lhs = tg.spmv(A, 2 * xd - z, variant=1)
-    rhs = 2 * y1 - tg.spmv(A, z, variant=1)
+    lhs = tg.spmv(A, 2 * xd - z)
+    rhs = 2 * y1 - tg.spmv(A, z)
     assert normwise(lhs.double().cpu().numpy(), rhs.double().cpu().numpy()) <= 10 * tol
 
 
-def test_full_size_powerlaw_double_float(full_powerlaw):
-    """The default FP64 variant (double-float on the FP32 pipe) at full size."""
+@pytest.mark.parametrize("name", ["wtile_dfs_ipt7", "wtile_dfs_ipt9", "wmerge_dfs_ipt7"])
+def test_full_size_powerlaw_double_float(full_powerlaw, name):
+    """Double-float variants (FP64 values on the FP32 pipe) at full size."""
     pos, crd, vals, x = full_powerlaw
     y_ref = O.spmv(pos, crd, vals, x)
     A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x))
     xd = torch.from_numpy(x).cuda()
-    y = tg.spmv(A, xd).cpu().numpy()
+    y = tg.spmv(A, xd, variant=tg.spmv_variants().index(name)).cpu().numpy()
     err = normwise(y, y_ref)
     assert err <= F64_TOL
     assert err <= 1e-13  # 46-bit significands: far inside the bar
+
+
+def test_full_size_powerlaw_default_is_native(full_powerlaw):
+    """The default FP64 variant accumulates with DFMA: error at the level of taco's own."""
+    pos, crd, vals, x = full_powerlaw
+    y_ref = O.spmv(pos, crd, vals, x)
+    A = tg.CsrMatrix.from_numpy(pos, crd, vals, len(x))
+    y = tg.spmv(A, torch.from_numpy(x).cuda()).cpu().numpy()
+    assert normwise(y, y_ref) <= 1e-14
 
 
 def test_full_size_banded():
@@ -154,8 +169,10 @@ def test_full_size_banded():
     pos, crd, vals = W.generate(s)
     x = W.dense(25, s.cols)
     y_ref = O.spmv(pos, crd, vals, x)
-    for variant in (1, 3, 6):
-        assert normwise(run_dev(pos, crd, vals, x, variant), y_ref) <= F64_TOL
+    names = tg.spmv_variants()
+    for nm in ("wmerge_ipt11", "wtile_native_ipt7", "wtile_dfs_ipt9", "wpipe_s_dfs_ipt9"):
+        assert normwise(run_dev(pos, crd, vals, x, names.index(nm)), y_ref) <= F64_TOL
+    assert normwise(run_dev(pos, crd, vals, x, -1), y_ref) <= F64_TOL
 
 
 @pytest.mark.parametrize("scale", [2.0 ** 60, 2.0 ** -60, 1e300])
@@ -168,7 +185,7 @@ def test_double_float_falls_back_outside_range(scale):
     x = W.dense(26, s.cols)
     x[:100] *= 1e-20  # some x out of range too
     y_ref = O.spmv(pos, crd, vals, x)
-    for variant in (2, 3, 10, 11, 13, 15, 16):
+    for variant in (2, 3, 10, 11, 13, 15, 16) + tuple(by_prefix("wmerge_dfs")):
         assert normwise(run_dev(pos, crd, vals, x, variant), y_ref) <= F64_TOL
 
 
