@@ -35,6 +35,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
+PROFILE_EVERY = 8  # timed steps per step whose kernels are bracketed by CUDA events
 ESZ = {"f64": 8, "f32": 4, "bf16": 2}
 
 
@@ -46,7 +47,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="spmv_powerlaw",
                    choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
-                            "spgemm_random", "spgemm_poisson", "batched_spmv", "batched_spmm"])
+                            "spgemm_random", "spgemm_poisson", "batched_spmv", "batched_spmm",
+                            "gather_probe"])
     p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
     p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
                    help="how batched_spmv picks each matrix's work-unit kind")
@@ -666,10 +668,11 @@ def main_batch(args, torch, tg, T, L, rank, world):
         raise RuntimeError("device status %d after the timed region" % status.value)
     value = op.flops / (ms / 1e3) / 1e9
 
-    # plain FP64: one tacogb_spmv (native FP64 merge path) per matrix, issued from a host loop
+    # plain FP64: one tacogb_spmv (the library's default FP64 path, DFMA accumulation) per
+    # matrix, issued from a host loop
     m64, x64, y64 = op.matrices(tg, dev, "v64")
     csrs = [A.as_csr() for A in m64]
-    native = tg.spmv_variants().index("wmerge_ipt7")
+    native = -1
 
     def per_matrix():
         for c, x, y in zip(csrs, x64, y64):
@@ -751,7 +754,7 @@ def main_batch(args, torch, tg, T, L, rank, world):
                       "kinds": kinds_used,
                       "l2": "inputs larger than L2 (%.1f GB per step), no flush" % (op.bytes / 1e9)},
            "fp64_per_matrix": {"gflops": op.flops / (ms64 / 1e3) / 1e9, "ms_per_step": ms64,
-                               "launch": "tacogb_spmv wmerge_ipt7 native FP64, one call per "
+                               "launch": "tacogb_spmv default FP64 path (wtile_native_ipt7), one call per "
                                          "matrix from a host loop", "steps": k64},
            "speedup_vs_fp64_per_matrix": ms64 / ms,
            "max_normwise_err_vs_fp64": max_err,
@@ -877,6 +880,10 @@ def main():
     from taco_gb300 import taco as T
     L = tg.lib()
 
+    if args.workload == "gather_probe":
+        if rank == 0:
+            main_gather_probe(args, torch, tg, L)
+        return
     if args.workload == "batched_spmv":
         main_batch(args, torch, tg, T, L, rank, world)
         return
@@ -900,9 +907,12 @@ def main():
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = L.tacogb_launch_count()
+    # per-kernel device times: CUDA events bracket the launches of every PROFILE_EVERY-th step
+    # of the timed region only, so that event records stay out of the headline time
     L.tacogb_profile_begin()
     e0.record(stream)
-    for _ in range(args.steps):
+    for i in range(args.steps):
+        L.tacogb_profile_enable(1 if i % PROFILE_EVERY == 0 else 0)
         step(sp)
     e1.record(stream)
     torch.cuda.synchronize()
@@ -994,6 +1004,47 @@ def main():
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def main_gather_probe(args, torch, tg, L):
+    """The random-gather ceiling behind the SpMV roofline: random 8-byte loads from a 32 MiB
+    L2-resident table of 16-byte rows (one L2 sector each, like the x gathers of a random-column
+    SpMV), eight in flight per thread, 32 warps per SM, by load form and by the shared memory
+    held per SM (which sets the L1 left).  One JSON line per configuration."""
+    rows, n = 1 << 21, 1 << 26
+    table = torch.zeros(rows * 2, dtype=torch.float64, device="cuda")  # zero: see probe.cu
+    idx = torch.randint(0, rows, (n,), dtype=torch.int32, device="cuda",
+                        generator=torch.Generator(device="cuda").manual_seed(7))
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    out = torch.empty(sms * 1024, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    clock_ghz = 2.07
+    forms = {0: "ld.global.nc", 1: "ld.global.cg", 2: "ld.global.nc.L1::no_allocate"}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for smem_kb, carve in ((0, -1), (192, -1), (64, 100)):
+        for mode in (0, 1, 2):
+            def run():
+                tg.check(L.tacogb_probe_gather(table.data_ptr(), rows, idx.data_ptr(), n,
+                                               out.data_ptr(), out.numel(), mode, smem_kb, carve,
+                                               sp), "tacogb_probe_gather")
+            for _ in range(max(3, args.warmup)):
+                run()
+            reps = max(3, min(args.steps, 20))
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                run()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            rate = n / (ms / 1e3)
+            print(json.dumps({
+                "metric": "random_gather_rate", "value": rate / (sms * clock_ghz * 1e9),
+                "unit": "gathers/clk/SM at %.2f GHz" % clock_ghz, "gathers_per_s": rate,
+                "ms_per_launch": ms, "load": forms[mode], "smem_kb_per_sm": smem_kb,
+                "carveout": carve, "config": {"workload": "gather_probe", "table_rows": rows,
+                                              "gathers": n, "sms": sms}}), flush=True)
 
 
 if __name__ == "__main__":

@@ -69,6 +69,20 @@ long long tacogb_launch_count(void);
  * in `names`), the summed milliseconds and the launch count; returns the number of kernels. */
 void tacogb_profile_begin(void);
 int tacogb_profile_end(int32_t max_kernels, char* names, double* total_ms, int32_t* launches);
+/* Between begin and end, pauses (on = 0) or resumes (on != 0) the bracketing without clearing
+ * what was recorded, so that a caller can sample some of its launches and keep the event
+ * records out of the rest. */
+void tacogb_profile_enable(int32_t on);
+
+/* Diagnostic (no counterpart in taco): random-gather throughput probe.  Launches 4 blocks of 256
+ * threads per SM on `stream`; each thread gathers entries table[2 * idx[i]] (rows of 16 bytes,
+ * idx clamped into [0, rows)) eight at a time with load form `mode` (0 ld.global.nc,
+ * 1 ld.global.cg, 2 ld.global.nc.L1::no_allocate) while every block holds
+ * smem_kb_per_sm / 4 KB of shared memory; carveout is the preferred shared-memory carveout in
+ * percent (-1: the driver's choice).  out needs 1024 * SMs entries.  The caller times it. */
+int tacogb_probe_gather(const double* table, int64_t rows, const int32_t* idx, int64_t n,
+                        double* out, int64_t out_len, int32_t mode, int32_t smem_kb_per_sm,
+                        int32_t carveout, void* stream);
 
 /* ------------------------------------------------------------------ device layer -------- */
 

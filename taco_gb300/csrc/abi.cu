@@ -365,6 +365,11 @@ void tacogb_profile_begin(void) {
   g_prof_on = true;
 }
 
+void tacogb_profile_enable(int32_t on) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof_on = on != 0;
+}
+
 int tacogb_profile_end(int32_t max_kernels, char* names, double* total_ms, int32_t* launches) {
   std::vector<ProfRec> recs;
   {

@@ -71,22 +71,51 @@ __global__ void spmv_split_x(const double* __restrict__ x, DF* __restrict__ xdf,
 // (i+1, pos[i+1]), so that only rows of snap_len or more nonzeros are split between tiles;
 // snap_len < T keeps every short row within one boundary, so coordinates stay monotone.
 // Boundary 0 never moves: the first tile starts at (0, 0).
-__device__ __forceinline__ void partition_row_body(int32_t p0, int32_t p1, uint32_t T,
+// Unsigned 32-bit division by an invariant divisor T as a multiply and shifts (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994): with
+// l = ceil(log2 T) and m = floor(2^32 (2^l - T) / T) + 1, the quotient of any 32-bit v is
+// (hi32(m v) + ((v - hi32(m v)) >> min(l, 1))) >> max(l - 1, 0).  Replaces the runtime divide,
+// which dominated the partition pass.
+struct DivU32 {
+  uint32_t T, m, s1, s2;
+};
+
+inline DivU32 make_divu32(uint32_t T) {
+  uint32_t l = 0;
+  while (l < 32 && (1ull << l) < T) l++;
+  DivU32 d;
+  d.T = T;
+  d.m = (uint32_t)(((1ull << 32) * ((1ull << l) - T)) / T + 1);
+  d.s1 = l < 1 ? l : 1;
+  d.s2 = l > 1 ? l - 1 : 0;
+  return d;
+}
+
+__device__ __forceinline__ uint32_t divu32(uint32_t v, const DivU32& d) {
+  const uint32_t t = __umulhi(d.m, v);
+  return (t + ((v - t) >> d.s1)) >> d.s2;
+}
+
+__device__ __forceinline__ void partition_row_body(int32_t p0, int32_t p1, const DivU32& dv,
                                                    int32_t tiles, int32_t snap_len,
                                                    int2* __restrict__ part, int64_t i) {
+  const uint32_t T = dv.T;
   const uint32_t lo = (uint32_t)p0 + (uint32_t)i;
   const uint32_t hi = (uint32_t)p1 + (uint32_t)i;
+  const uint32_t qlo = divu32(lo, dv);
+  const uint32_t b0 = qlo + (lo != qlo * T);   // first boundary at or after lo
+  const uint32_t b1 = divu32(hi, dv);          // last boundary at or before hi
   const bool snap = (p1 - p0) < snap_len;
-  for (uint32_t b = lo / T + (lo % T != 0); (uint64_t)b * T <= hi && (int32_t)b < tiles; b++)
-    part[b] = (snap && b > 0) ? make_int2((int)i + 1, p1)
-                              : make_int2((int)i, (int)((uint64_t)b * T - (uint64_t)i));
+  const uint32_t bend = min(b1 + 1, (uint32_t)tiles);
+  for (uint32_t b = b0; b < bend; b++)   // b * T <= hi < 2^32
+    part[b] = (snap && b > 0) ? make_int2((int)i + 1, p1) : make_int2((int)i, (int)(b * T - (uint32_t)i));
 }
 
 // Rows 4g .. 4g+3 (and the end marker when row n falls in the group).  Each thread reads its
 // five pos entries at once (one 16-byte load when pos is 16-byte aligned), so the pass needs a
 // quarter of the dependent load round trips of one row per thread.
 __device__ __forceinline__ void partition_rows4(const int32_t* __restrict__ pos, int32_t n,
-                                                int64_t nnz, uint32_t T, int32_t tiles,
+                                                int64_t nnz, const DivU32& dv, int32_t tiles,
                                                 int32_t snap_len, int2* __restrict__ part,
                                                 int64_t g, bool vec) {
   const int64_t i0 = 4 * g;
@@ -111,15 +140,15 @@ __device__ __forceinline__ void partition_rows4(const int32_t* __restrict__ pos,
       part[tiles] = make_int2(n, (int)nnz);
       break;
     }
-    partition_row_body(p[j], p[j + 1], T, tiles, snap_len, part, i);
+    partition_row_body(p[j], p[j + 1], dv, tiles, snap_len, part, i);
   }
 }
 
 __global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t n,
-                                        int64_t nnz, uint32_t T, int32_t tiles,
+                                        int64_t nnz, DivU32 dv, int32_t tiles,
                                         int32_t snap_len, int2* __restrict__ part) {
   const bool vec = ((uintptr_t)pos & 15) == 0;
-  partition_rows4(pos, n, nnz, T, tiles, snap_len, part,
+  partition_rows4(pos, n, nnz, dv, tiles, snap_len, part,
                   (int64_t)blockIdx.x * blockDim.x + threadIdx.x, vec);
 }
 
@@ -127,7 +156,7 @@ __global__ void merge_partition_scatter(const int32_t* __restrict__ pos, int32_t
 // 4g .. 4g+3 (as merge_partition_scatter) and splits x[4g .. 4g+3] into double-float pairs,
 // setting *xflag when an entry lies outside the pairs' range (zeros split exactly).  *xflag is
 // cleared by the fix-up kernel at the end of the same product.
-__global__ void spmv_prep(const int32_t* __restrict__ pos, int32_t n, int64_t nnz, uint32_t T,
+__global__ void spmv_prep(const int32_t* __restrict__ pos, int32_t n, int64_t nnz, DivU32 dv,
                           int32_t tiles, int2* __restrict__ part, const double* __restrict__ x,
                           DF* __restrict__ xdf, int32_t cols, int* __restrict__ xflag) {
   const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -154,7 +183,7 @@ __global__ void spmv_prep(const int32_t* __restrict__ pos, int32_t n, int64_t nn
     }
     if (!ok) *xflag = 1;
   }
-  partition_rows4(pos, n, nnz, T, tiles, 0, part, g, ((uintptr_t)pos & 15) == 0);
+  partition_rows4(pos, n, nnz, dv, tiles, 0, part, g, ((uintptr_t)pos & 15) == 0);
 }
 
 // Threads needed by the four-rows-per-thread passes over n + 1 pos entries (and cols).
@@ -168,7 +197,7 @@ int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_ite
   const int64_t threads = rows4_threads((int64_t)n + 1);
   TACOGB_LAUNCH("merge_partition_scatter", st,
                 merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                    pos, n, nnz, (uint32_t)tile_items, tiles, snap_len, part));
+                    pos, n, nnz, make_divu32((uint32_t)tile_items), tiles, snap_len, part));
   return 0;
 }
 
@@ -220,8 +249,11 @@ spmv_wtile_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ c
   const int t = blockIdx.x * kWtWarps + warp;
   if (t >= tiles) return;  // whole warp: nothing below synchronises more than one warp
   const int2 c0 = part[t], c1 = part[t + 1];
+  double first_val;
   const double c = wt_process<P, IPT, TMA, CH>(s, pos, crd, vals, xg, x64, xflag, y, n, nnz, c0.x,
-                                               c1.x - c0.x, c0.y, c1.y - c0.y, status);
+                                               c1.x - c0.x, c0.y, c1.y - c0.y, status, first_val);
+  // One carry per tile, added by the fix-up kernel.  (Chaining a CTA's four carries before it
+  // exits measured slower: any hand-off between warps lengthens the CTA's life.)
   if ((threadIdx.x & 31) == 0) {
     carry_row[t] = c1.x;
     carry_val[t] = c;
@@ -498,18 +530,20 @@ __global__ void spmv_carry_fixup(const int32_t* __restrict__ carry_row,
   const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t == 0 && xflag != nullptr) *xflag = 0;
   if (t >= tiles) return;
+  // every load the common case needs is issued before any of them is tested
   const int32_t r = carry_row[t];
-  if (r >= n) return;
-  if (t > 0 && carry_row[t - 1] == r) return;
+  const int32_t rp = t > 0 ? carry_row[t - 1] : -1;
   double tot = carry_val[t];
-  for (int32_t u = t + 1; u < tiles; u += 8) {
-    int32_t rr[8];
-    double vv[8];
+  int32_t rr[8];
+  double vv[8];
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      rr[j] = (u + j < tiles) ? carry_row[u + j] : -1;
-      vv[j] = (u + j < tiles) ? carry_val[u + j] : 0.0;
-    }
+  for (int j = 0; j < 8; j++) {
+    rr[j] = (t + 1 + j < tiles) ? carry_row[t + 1 + j] : -1;
+    vv[j] = (t + 1 + j < tiles) ? carry_val[t + 1 + j] : 0.0;
+  }
+  if (r >= n || rp == r) return;
+  const Out y0 = y[r];
+  for (int32_t u = t + 1;; u += 8) {
     bool more = true;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
@@ -517,8 +551,13 @@ __global__ void spmv_carry_fixup(const int32_t* __restrict__ carry_row,
       if (more) tot += vv[j];
     }
     if (!more) break;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      rr[j] = (u + 8 + j < tiles) ? carry_row[u + 8 + j] : -1;
+      vv[j] = (u + 8 + j < tiles) ? carry_val[u + 8 + j] : 0.0;
+    }
   }
-  y[r] = (Out)((double)y[r] + tot);
+  y[r] = (Out)((double)y0 + tot);
 }
 
 // ------------------------------------------------------------------ vector ----------------
@@ -637,7 +676,7 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
     const int64_t threads = rows4_threads((int64_t)A->rows + 1, A->cols);
     TACOGB_LAUNCH("spmv_prep", st,
                   spmv_prep<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                      A->pos, A->rows, A->nnz, (uint32_t)tile_items, tiles, part,
+                      A->pos, A->rows, A->nnz, make_divu32((uint32_t)tile_items), tiles, part,
                       (const double*)x, xdf, A->cols, fixup_flag));
     xg = (const typename P::XG*)xdf;
     xflag = fixup_flag;
@@ -674,6 +713,7 @@ int launch_wtile(const tacogb_csr* A, const typename P::Val* x, typename P::Out*
   constexpr bool split = std::is_same<typename P::XG, DF>::value;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
+  const int grid = (tiles + kWtWarps - 1) / kWtWarps;
   const size_t crow_bytes = al((size_t)tiles * sizeof(int32_t));
   const size_t cval_bytes = al((size_t)tiles * sizeof(double));
   const size_t xdf_bytes = split ? al((size_t)A->cols * sizeof(DF)) : 0;
@@ -692,7 +732,7 @@ int launch_wtile(const tacogb_csr* A, const typename P::Val* x, typename P::Out*
     const int64_t threads = rows4_threads((int64_t)A->rows + 1, A->cols);
     TACOGB_LAUNCH("spmv_prep", st,
                   spmv_prep<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                      A->pos, A->rows, A->nnz, (uint32_t)tile_items, tiles, part,
+                      A->pos, A->rows, A->nnz, make_divu32((uint32_t)tile_items), tiles, part,
                       (const double*)x, xdf, A->cols, xflag));
     xg = (const typename P::XG*)xdf;
   } else {
@@ -706,7 +746,6 @@ int launch_wtile(const tacogb_csr* A, const typename P::Val* x, typename P::Out*
   // matrices run fastest at IPT 9 with the driver's choice)
   constexpr int carve = IPT == 7 ? 70 : IPT == 9 ? -1 : 85;
   TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, carve));
-  const int grid = (tiles + kWtWarps - 1) / kWtWarps;
   TACOGB_LAUNCH("spmv_wtile_kernel", st,
                 kern<<<grid, kWtWarps * 32, smem, st>>>(
                     A->pos, A->crd, (const typename P::Val*)A->vals, xg, x, xflag, y, part,
@@ -762,7 +801,7 @@ int launch_wpipe(const tacogb_csr* A, const typename P::Val* x, typename P::Out*
     const int64_t threads = rows4_threads((int64_t)A->rows + 1, A->cols);
     TACOGB_LAUNCH("spmv_prep", st,
                   spmv_prep<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                      A->pos, A->rows, A->nnz, (uint32_t)tile_items, tiles, part,
+                      A->pos, A->rows, A->nnz, make_divu32((uint32_t)tile_items), tiles, part,
                       (const double*)x, xdf, A->cols, xflag));
     xg = (const typename P::XG*)xdf;
   } else {
@@ -1050,7 +1089,7 @@ int launch_wmerge_noalloc(const tacogb_csr* A, const typename P::Val* x, typenam
   const int64_t threads = rows4_threads((int64_t)A->rows + 1);
   count_launch();
   merge_partition_scatter<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-      A->pos, A->rows, A->nnz, (uint32_t)kNoAllocTileItems, tiles, 0, part);
+      A->pos, A->rows, A->nnz, make_divu32((uint32_t)kNoAllocTileItems), tiles, 0, part);
   if (int rc = launch_check("merge_partition_scatter")) return rc;
   auto kern = spmv_wmerge_kernel<P, kNoAllocIpt, false>;
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -171,14 +171,15 @@ __device__ __forceinline__ typename P::Acc wt_join(typename P::Acc open, int key
 }
 
 // One warp tile with policy P (native redo for checked policies); writes the rows ending in the
-// tile and returns the FP64 carry-out (every lane).
+// tile and returns the FP64 carry-out (every lane).  first_val (lane 0, when rn > 0) is the FP64
+// value written for the tile's first row.
 template <class P, int IPT, bool TMA, int CH>
 __device__ __forceinline__ double wt_process(
     WtSmem<P, IPT>& s, const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
     const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
     const typename P::Val* __restrict__ x64, const int* __restrict__ xflag,
     typename P::Out* __restrict__ y, int32_t n, int32_t nnz, int r0, int rn, int k0, int kn,
-    int* status) {
+    int* status, double& first_val) {
   const int lane = threadIdx.x & 31;
   const int32_t* scrd;
   const typename P::Val* sval;
@@ -205,6 +206,7 @@ __device__ __forceinline__ double wt_process(
       const typename P::Acc c = wt_join<P>(open, row_e, first, first_row, s.y);
       __syncwarp();
       for (int i = lane; i < rn; i += 32) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
+      if (lane == 0 && rn > 0) first_val = P::to_double(as_acc<typename P::Acc>(s.y[0]));
       carry = P::to_double(c);
     } else {
       native = true;
@@ -220,6 +222,7 @@ __device__ __forceinline__ double wt_process(
     __syncwarp();
     for (int i = lane; i < rn; i += 32)
       y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
+    if (lane == 0 && rn > 0) first_val = Q::to_double(as_acc<typename Q::Acc>(s.y[0]));
     carry = Q::to_double(c);
   }
   return carry;
