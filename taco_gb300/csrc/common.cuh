@@ -87,6 +87,9 @@ int* device_status();
 // Word of the same zero-initialised 256-byte block holding the double-float SpMV's x-range
 // flag (set by its prep kernel, cleared by its fix-up kernel).
 constexpr int kXFlagWord = 16;
+// Word of the same block holding the double-float SpMM's B-range flag (set by its B-split
+// kernel, cleared by its fix-up kernel).
+constexpr int kBFlagWord = 17;
 
 // ---------------------------------------------------------------- TMA / mbarrier ----------
 

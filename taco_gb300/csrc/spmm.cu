@@ -24,6 +24,7 @@
 //   F32 values, BF16 B: FFMA in FP32 (B converted by a shift), C in FP32.
 
 #include <cstdio>
+#include <cstring>
 #include <type_traits>
 
 #include "common.cuh"
@@ -33,10 +34,13 @@
 
 namespace tacogb {
 
-template <class P, int VEC>
+// B64: B as FP64 for the native redo of checked policies (the same array as B unless B was
+// pre-split); bflag (optional): non-zero when B has entries outside the double-float range.
+template <class P, int VEC, bool STREAM>
 __global__ void __launch_bounds__(kMmBlock, 3)
 spmm_merge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                   const typename P::AV* __restrict__ vals, const typename P::BV* __restrict__ B,
+                  const double* __restrict__ B64, const int* __restrict__ bflag,
                   typename P::Out* __restrict__ C, int32_t n, int32_t N,
                   const int2* __restrict__ part, int32_t tiles, int32_t* __restrict__ carry_row,
                   double* __restrict__ carry_val) {
@@ -46,21 +50,35 @@ spmm_merge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ c
   const int col0 = blockIdx.y * (32 * VEC) + lane * VEC;
   const bool active = col0 < N;
   const int2 c0 = part[tile], c1 = part[tile + 1];
-  const bool ok = spmm_tile<P, VEC>(pos, crd, vals, B, C, n, N, c0, c1, tile, col0, active,
+  bool ok = !P::kChecked || bflag == nullptr || *bflag == 0;
+  if (ok) {
+    if constexpr (STREAM)
+      ok = spmm_tile_stream<P, VEC>(pos, crd, vals, B, C, n, N, c0, c1, tile, col0, active,
                                     carry_row, carry_val);
+    else
+      ok = spmm_tile<P, VEC>(pos, crd, vals, B, C, n, N, c0, c1, tile, col0, active, carry_row,
+                             carry_val);
+  }
   if constexpr (P::kChecked) {
-    if (!__all_sync(0xffffffffu, ok))
-      spmm_tile<MmNative64, VEC>(pos, crd, vals, B, C, n, N, c0, c1, tile, col0, active,
-                                 carry_row, carry_val);
+    if (!__all_sync(0xffffffffu, ok)) {
+      if constexpr (STREAM)
+        spmm_tile_stream<MmNative64, VEC>(pos, crd, (const double*)vals, B64, (double*)C, n, N,
+                                          c0, c1, tile, col0, active, carry_row, carry_val);
+      else
+        spmm_tile<MmNative64, VEC>(pos, crd, (const double*)vals, B64, (double*)C, n, N, c0, c1,
+                                   tile, col0, active, carry_row, carry_val);
+    }
   }
 }
 
 // Adds carried partial rows, in tile order, into the row where each run of tiles ends.
+// bflag (optional) is the B-range flag of the product, cleared here for the next one.
 template <typename Out>
 __global__ void spmm_carry_fixup(const int32_t* __restrict__ carry_row,
                                  const double* __restrict__ carry_val, int32_t tiles, int32_t N,
-                                 Out* __restrict__ C, int32_t n) {
+                                 Out* __restrict__ C, int32_t n, int* __restrict__ bflag = nullptr) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx == 0 && bflag != nullptr) *bflag = 0;
   const int64_t t = idx / N;
   const int32_t col = (int32_t)(idx % N);
   if (t >= tiles) return;
@@ -73,25 +91,85 @@ __global__ void spmm_carry_fixup(const int32_t* __restrict__ carry_row,
   *c = (Out)((double)*c + tot);
 }
 
+// Splits B (count doubles, count even, both arrays 16-byte aligned) into double-float pairs,
+// two elements per thread, setting *bflag when an element lies outside the pairs' range (the
+// product then runs every tile natively).  *bflag is cleared by the fix-up kernel.
+__global__ void spmm_split_b(const double* __restrict__ B, DF* __restrict__ Bdf, int64_t count,
+                             int* __restrict__ bflag) {
+  const int64_t i = 2 * ((int64_t)blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= count) return;
+  const double2 v = __ldg(reinterpret_cast<const double2*>(B + i));
+  float4 o;
+  const bool ok = split_df(v.x, o.x, o.y) & split_df(v.y, o.z, o.w);
+  *reinterpret_cast<float4*>(Bdf + i) = o;
+  if (!ok) *bflag = 1;
+}
+
+// Sub-warp SpMM (spmm_tile_sub): warp `tile` of the merge partition, column slab blockIdx.y of
+// LPR*VEC columns.  Blocks run slab by slab (blockIdx.x fastest), so the slab of B being
+// gathered stays in L2 while A streams past once per slab.  Checked policies redo a tile with
+// DFMA on the FP64 B (B64) when a value or a B entry (*bflag) is out of range.
+template <class P, int VEC, int SUB, int LONG>
+__global__ void __launch_bounds__(kMmBlock, 3)
+spmm_sub_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+                const typename P::AV* __restrict__ vals, const typename P::BV* __restrict__ B,
+                const double* __restrict__ B64, const int* __restrict__ bflag,
+                typename P::Out* __restrict__ C, int32_t n, int32_t N,
+                const int2* __restrict__ part, int32_t tiles, int32_t* __restrict__ carry_row,
+                double* __restrict__ carry_val) {
+  constexpr int LPR = 32 / SUB;
+  const int warp = threadIdx.x >> 5;
+  const int tile = blockIdx.x * kMmWarps + warp;
+  if (tile >= tiles) return;
+  const int ct = blockIdx.y * (LPR * VEC);
+  const int2 c0 = part[tile], c1 = part[tile + 1];
+  bool ok = !P::kChecked || bflag == nullptr || *bflag == 0;
+  if (ok)
+    ok = spmm_tile_sub<P, VEC, SUB, LONG>(pos, crd, vals, B, C, n, N, c0, c1, tile, ct,
+                                          carry_row, carry_val);
+  if constexpr (P::kChecked) {
+    if (!__all_sync(0xffffffffu, ok))
+      spmm_tile_sub<MmNative64, VEC, SUB, LONG>(pos, crd, (const double*)vals, B64, (double*)C, n,
+                                                N, c0, c1, tile, ct, carry_row, carry_val);
+  }
+}
+
 // ------------------------------------------------------------------ host side -------------
 
 namespace {
 
 struct SpmmVariant {
   const char* name;
-  bool df;          // double-float (F64) / compensated (F32) accumulation
+  int df;           // 0 native, 1 double-float (F64) / compensated (F32), 2 double-float over a
+                    // pre-split B (F64; compensated for F32)
   int tile_items;   // W
+  int lpr;          // 0: warp tile (spmm_tile); else sub-warp tile with LPR lanes per B row
+  bool shared;      // sub-warp tile: every row shared by the whole warp (column slabs)
+  bool stream;      // warp tile walked as one stream of nonzeros (spmm_tile_stream)
 };
 
 const SpmmVariant kSpmmVariants[] = {
-    {"merge_w512_native", false, 512},
-    {"merge_w512_df", true, 512},
-    {"merge_w256_native", false, 256},
-    {"merge_w256_df", true, 256},
+    {"merge_w512_native", 0, 512, 0},
+    {"merge_w512_df", 1, 512, 0},
+    {"merge_w256_native", 0, 256, 0},
+    {"merge_w256_df", 1, 256, 0},
+    {"sub8_w512_native", 0, 512, 8},
+    {"sub8_w512_dfs", 2, 512, 8},
+    {"sub4_w512_native", 0, 512, 4},
+    {"sub4_w512_dfs", 2, 512, 4},
+    {"merge_w512_dfs", 2, 512, 0},
+    {"merge_w256_dfs", 2, 256, 0},
+    {"slab8_w512_native", 0, 512, 8, true},
+    {"slab8_w512_dfs", 2, 512, 8, true},
+    {"slab4_w512_native", 0, 512, 4, true},
+    {"slab4_w512_dfs", 2, 512, 4, true},
+    {"stream_w512_native", 0, 512, 0, false, true},
+    {"stream_w512_dfs", 2, 512, 0, false, true},
+    {"stream_w1024_dfs", 2, 1024, 0, false, true},
 };
 constexpr int kNumSpmmVariants = sizeof(kSpmmVariants) / sizeof(kSpmmVariants[0]);
 
-template <class P, int VEC>
+template <class P, int VEC, bool STREAM>
 int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, cudaStream_t st) {
   const int64_t total = (int64_t)A->rows + A->nnz;
   const int64_t tiles64 = (total + W - 1) / W;
@@ -100,46 +178,138 @@ int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, c
   const int32_t tiles = (int32_t)tiles64;
   const size_t part_bytes = (((size_t)tiles + 1) * sizeof(int2) + 255) & ~(size_t)255;
   const size_t crow_bytes = ((size_t)tiles * sizeof(int32_t) + 255) & ~(size_t)255;
-  const size_t cval_bytes = (size_t)tiles * (size_t)N * sizeof(double);
-  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes, 1);
+  const size_t cval_bytes = (((size_t)tiles * (size_t)N * sizeof(double)) + 255) & ~(size_t)255;
+  constexpr bool split = std::is_same<P, MmDFS>::value;
+  const size_t bdf_bytes = split ? (size_t)A->cols * (size_t)N * sizeof(DF) : 0;
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + bdf_bytes, 1);
   if (!ws) return last_code();
   int2* part = (int2*)ws;
   int32_t* crow = (int32_t*)(ws + part_bytes);
   double* cval = (double*)(ws + part_bytes + crow_bytes);
+  const typename P::BV* Bk = (const typename P::BV*)B;
+  int* bflag = nullptr;
+  if constexpr (split) {
+    // B split once into double-float pairs: every B element is then used about nnz/cols times
+    int* status = device_status();
+    if (!status) return last_code();
+    bflag = status + kBFlagWord;
+    DF* bdf = (DF*)(ws + part_bytes + crow_bytes + cval_bytes);
+    const int64_t count = (int64_t)A->cols * N;  // even: N is even whenever VEC is 2
+    if (count > 0)
+      TACOGB_LAUNCH("spmm_split_b", st,
+                    spmm_split_b<<<(unsigned)((count / 2 + 255) / 256), 256, 0, st>>>(
+                        (const double*)B, bdf, count, bflag));
+    Bk = (const typename P::BV*)bdf;
+  }
   if (int rc = merge_partition(A->pos, A->rows, A->nnz, W, tiles, part, st, W / 2)) return rc;
   constexpr int TW = 32 * VEC;
   dim3 grid((unsigned)((tiles + kMmWarps - 1) / kMmWarps), (unsigned)((N + TW - 1) / TW));
   TACOGB_CHECK_ARG(grid.y <= 65535, "SpMM: N too large");
   TACOGB_LAUNCH("spmm_merge_kernel", st,
-                (spmm_merge_kernel<P, VEC><<<grid, kMmBlock, 0, st>>>(
-                    A->pos, A->crd, (const typename P::AV*)A->vals,
-                    (const typename P::BV*)B, (typename P::Out*)C, A->rows, N, part, tiles, crow,
-                    cval)));
+                (spmm_merge_kernel<P, VEC, STREAM><<<grid, kMmBlock, 0, st>>>(
+                    A->pos, A->crd, (const typename P::AV*)A->vals, Bk, (const double*)B, bflag,
+                    (typename P::Out*)C, A->rows, N, part, tiles, crow, cval)));
   const int64_t fix_threads = (int64_t)tiles * N;
   TACOGB_LAUNCH("spmm_carry_fixup", st,
                 spmm_carry_fixup<typename P::Out><<<(unsigned)((fix_threads + 255) / 256), 256, 0,
                                                     st>>>(crow, cval, tiles, N,
-                                                          (typename P::Out*)C, A->rows));
+                                                          (typename P::Out*)C, A->rows, bflag));
   return 0;
 }
 
+// Sub-warp SpMM over column slabs.  For MmDFS, B is first split into double-float pairs in
+// scratch (one pass over B; every B element is then used about nnz/cols times without further
+// splitting).
+template <class P, int VEC, int SUB, int LONG>
+int launch_spmm_sub(const tacogb_csr* A, int32_t N, const void* B, void* C, int W,
+                    cudaStream_t st) {
+  constexpr int LPR = 32 / SUB;
+  const int64_t total = (int64_t)A->rows + A->nnz;
+  const int64_t tiles64 = (total + W - 1) / W;
+  if (tiles64 == 0 || N == 0) return 0;
+  TACOGB_CHECK_ARG(tiles64 < (1ll << 31) / kMmWarps, "SpMM: too many tiles");
+  const int32_t tiles = (int32_t)tiles64;
+  constexpr bool split = std::is_same<P, MmDFS>::value;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
+  const size_t crow_bytes = al((size_t)tiles * sizeof(int32_t));
+  const size_t cval_bytes = al((size_t)tiles * (size_t)N * sizeof(double));
+  const size_t bdf_bytes = split ? al((size_t)A->cols * (size_t)N * sizeof(DF)) : 0;
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + bdf_bytes, 1);
+  if (!ws) return last_code();
+  int2* part = (int2*)ws;
+  int32_t* crow = (int32_t*)(ws + part_bytes);
+  double* cval = (double*)(ws + part_bytes + crow_bytes);
+  const typename P::BV* Bk = (const typename P::BV*)B;
+  int* bflag = nullptr;
+  if constexpr (split) {
+    int* status = device_status();
+    if (!status) return last_code();
+    bflag = status + kBFlagWord;
+    DF* bdf = (DF*)(ws + part_bytes + crow_bytes + cval_bytes);
+    const int64_t count = (int64_t)A->cols * N;  // even: N is even for 16-byte vectors
+    if (count > 0)
+      TACOGB_LAUNCH("spmm_split_b", st,
+                    spmm_split_b<<<(unsigned)((count / 2 + 255) / 256), 256, 0, st>>>(
+                        (const double*)B, bdf, count, bflag));
+    Bk = (const typename P::BV*)bdf;
+  }
+  if (int rc = merge_partition(A->pos, A->rows, A->nnz, W, tiles, part, st, W / 2)) return rc;
+  dim3 grid((unsigned)((tiles + kMmWarps - 1) / kMmWarps),
+            (unsigned)((N + LPR * VEC - 1) / (LPR * VEC)));
+  TACOGB_CHECK_ARG(grid.y <= 65535, "SpMM: N too large");
+  TACOGB_LAUNCH("spmm_sub_kernel", st,
+                (spmm_sub_kernel<P, VEC, SUB, LONG><<<grid, kMmBlock, 0, st>>>(
+                    A->pos, A->crd, (const typename P::AV*)A->vals, Bk, (const double*)B, bflag,
+                    (typename P::Out*)C, A->rows, N, part, tiles, crow, cval)));
+  const int64_t fix_threads = (int64_t)tiles * N;
+  TACOGB_LAUNCH("spmm_carry_fixup", st,
+                spmm_carry_fixup<typename P::Out><<<(unsigned)((fix_threads + 255) / 256), 256, 0,
+                                                    st>>>(crow, cval, tiles, N,
+                                                          (typename P::Out*)C, A->rows, bflag));
+  return 0;
+}
+
+// Sub-warp variants: 16-byte lane vectors when N and B's alignment allow, else one element.
+template <class P, int LPR, int LONG>
+int spmm_dispatch_sub(const tacogb_csr* A, int32_t N, const void* B, void* C, int W,
+                      cudaStream_t st) {
+  constexpr int SUB = 32 / LPR;
+  constexpr int esz = sizeof(typename std::conditional<std::is_same<P, MmDFS>::value, double,
+                                                       typename P::BV>::type);
+  constexpr int V16 = 16 / esz;
+  const bool aligned = ((uintptr_t)B & 15) == 0 && ((uintptr_t)C & 15) == 0 && N % V16 == 0;
+  if (aligned) return launch_spmm_sub<P, V16, SUB, LONG>(A, N, B, C, W, st);
+  if constexpr (std::is_same<P, MmDFS>::value) {
+    // the split works on 16-byte pairs
+    return launch_spmm_sub<MmNative64, 1, SUB, LONG>(A, N, B, C, W, st);
+  } else {
+    return launch_spmm_sub<P, 1, SUB, LONG>(A, N, B, C, W, st);
+  }
+}
+
 // Widest lane vector (up to 16 bytes) whose column tile divides N.
-template <class P>
+template <class P, bool STREAM = false>
 int spmm_dispatch_vec(const tacogb_csr* A, int32_t N, const void* B, void* C, int W,
                       cudaStream_t st) {
+  if constexpr (std::is_same<P, MmDFS>::value) {
+    // the B split works on 16-byte pairs of elements
+    if (N % 2 != 0 || ((uintptr_t)B & 15) != 0)
+      return spmm_dispatch_vec<MmDF64, STREAM>(A, N, B, C, W, st);
+  }
   constexpr int esz = sizeof(typename P::BV);
   if constexpr (esz == 8) {
-    if (N % 64 == 0) return launch_spmm<P, 2>(A, N, B, C, W, st);
-    return launch_spmm<P, 1>(A, N, B, C, W, st);
+    if (N % 64 == 0) return launch_spmm<P, 2, STREAM>(A, N, B, C, W, st);
+    return launch_spmm<P, 1, STREAM>(A, N, B, C, W, st);
   } else if constexpr (esz == 4) {
-    if (N % 128 == 0) return launch_spmm<P, 4>(A, N, B, C, W, st);
-    if (N % 64 == 0) return launch_spmm<P, 2>(A, N, B, C, W, st);
-    return launch_spmm<P, 1>(A, N, B, C, W, st);
+    if (N % 128 == 0) return launch_spmm<P, 4, STREAM>(A, N, B, C, W, st);
+    if (N % 64 == 0) return launch_spmm<P, 2, STREAM>(A, N, B, C, W, st);
+    return launch_spmm<P, 1, STREAM>(A, N, B, C, W, st);
   } else {
-    if (N % 256 == 0) return launch_spmm<P, 8>(A, N, B, C, W, st);
-    if (N % 128 == 0) return launch_spmm<P, 4>(A, N, B, C, W, st);
-    if (N % 64 == 0) return launch_spmm<P, 2>(A, N, B, C, W, st);
-    return launch_spmm<P, 1>(A, N, B, C, W, st);
+    if (N % 256 == 0) return launch_spmm<P, 8, STREAM>(A, N, B, C, W, st);
+    if (N % 128 == 0) return launch_spmm<P, 4, STREAM>(A, N, B, C, W, st);
+    if (N % 64 == 0) return launch_spmm<P, 2, STREAM>(A, N, B, C, W, st);
+    return launch_spmm<P, 1, STREAM>(A, N, B, C, W, st);
   }
 }
 
@@ -160,17 +330,45 @@ int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void*
   TACOGB_CHECK_ARG((int64_t)A->rows * N <= INT32_MAX,
                    "SpMM: rows*N exceeds taco's int32 dense positions");
   TACOGB_CHECK_ARG(A->rows == 0 || A->pos != nullptr, "SpMM: null pos");
-  if (variant < 0) variant = 1;
+  if (variant < 0) {
+    // measured fastest on the 1,048,576-row power-law matrix: FP64 double-float over a
+    // pre-split B on the warp tile; FP32 compensated on the streaming tile; BF16 B plain FFMA
+    const char* pick = A->vtype == TACOGB_F64 ? "merge_w512_dfs"
+                       : btype == TACOGB_BF16 ? "merge_w512_native"
+                                              : "stream_w512_dfs";
+    variant = 0;
+    for (int i = 0; i < kNumSpmmVariants; i++)
+      if (strcmp(kSpmmVariants[i].name, pick) == 0) variant = i;
+  }
   TACOGB_CHECK_ARG(variant < kNumSpmmVariants, "SpMM: variant %d out of range", variant);
   const SpmmVariant& v = kSpmmVariants[variant];
-  if (A->vtype == TACOGB_F64 && btype == TACOGB_F64)
-    return v.df ? spmm_dispatch_vec<MmDF64>(A, N, B, C, v.tile_items, st)
-                : spmm_dispatch_vec<MmNative64>(A, N, B, C, v.tile_items, st);
-  if (A->vtype == TACOGB_F32 && btype == TACOGB_F32)
-    return v.df ? spmm_dispatch_vec<MmComp32>(A, N, B, C, v.tile_items, st)
-                : spmm_dispatch_vec<MmF32>(A, N, B, C, v.tile_items, st);
-  if (A->vtype == TACOGB_F32 && btype == TACOGB_BF16)
-    return spmm_dispatch_vec<MmBF16>(A, N, B, C, v.tile_items, st);
+  const int W = v.tile_items;
+  if (v.lpr > 0) {
+    auto sub = [&](auto tag) -> int {
+      using P = decltype(tag);
+      if (v.shared)
+        return v.lpr == 8 ? spmm_dispatch_sub<P, 8, 0>(A, N, B, C, W, st)
+                          : spmm_dispatch_sub<P, 4, 0>(A, N, B, C, W, st);
+      return v.lpr == 8 ? spmm_dispatch_sub<P, 8, kSubLong>(A, N, B, C, W, st)
+                        : spmm_dispatch_sub<P, 4, kSubLong>(A, N, B, C, W, st);
+    };
+    if (A->vtype == TACOGB_F64 && btype == TACOGB_F64)
+      return v.df == 2 ? sub(MmDFS{}) : v.df == 1 ? sub(MmDF64{}) : sub(MmNative64{});
+    if (A->vtype == TACOGB_F32 && btype == TACOGB_F32)
+      return v.df ? sub(MmComp32{}) : sub(MmF32{});
+    if (A->vtype == TACOGB_F32 && btype == TACOGB_BF16) return sub(MmBF16{});
+  } else {
+    auto run = [&](auto tag) -> int {
+      using P = decltype(tag);
+      return v.stream ? spmm_dispatch_vec<P, true>(A, N, B, C, W, st)
+                      : spmm_dispatch_vec<P, false>(A, N, B, C, W, st);
+    };
+    if (A->vtype == TACOGB_F64 && btype == TACOGB_F64)
+      return v.df == 2 ? run(MmDFS{}) : v.df == 1 ? run(MmDF64{}) : run(MmNative64{});
+    if (A->vtype == TACOGB_F32 && btype == TACOGB_F32)
+      return v.df ? run(MmComp32{}) : run(MmF32{});
+    if (A->vtype == TACOGB_F32 && btype == TACOGB_BF16) return run(MmBF16{});
+  }
   set_error(TACOGB_ERR_ARG, "SpMM: unsupported value types (A %d, B %d)", A->vtype, btype);
   return TACOGB_ERR_ARG;
 }

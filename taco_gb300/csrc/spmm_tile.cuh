@@ -2,6 +2,7 @@
 // kernel (batched.cu): 16-byte lane vectors, accumulation policies and the one-warp merge tile.
 #pragma once
 
+#include <climits>
 #include <cuda_bf16.h>
 #include <type_traits>
 
@@ -56,6 +57,20 @@ __device__ __forceinline__ void load_vec(const __nv_bfloat16* p, float (&o)[VEC]
   } else {
     static_assert(VEC == 1, "bf16 vectors are 1, 2, 4 or 8 wide");
     o[0] = bf16_lo((unsigned int)__ldg(reinterpret_cast<const unsigned short*>(p)));
+  }
+}
+
+// B pre-split into double-float pairs (8 bytes per element): two pairs per 16-byte load.
+template <int VEC>
+__device__ __forceinline__ void load_vec(const DF* p, DF (&o)[VEC]) {
+  if constexpr (VEC == 2) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    o[0] = DF{v.x, v.y};
+    o[1] = DF{v.z, v.w};
+  } else {
+    static_assert(VEC == 1, "double-float vectors are 1 or 2 wide");
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    o[0] = DF{v.x, v.y};
   }
 }
 
@@ -156,6 +171,64 @@ struct MmBF16 : MmF32 {
   using BV = __nv_bfloat16;
 };
 
+// Running double-float sum with deferred renormalisation: hi sum s and an unnormalised
+// compensation c (the product errors, cross terms and TwoSum errors), renormalised on output
+// and once per 32 nonzeros (so that c's own rounding stays at 2^-48 of the sum for long rows).
+struct DFAcc {
+  float s, c;
+};
+
+template <class P>
+__device__ __forceinline__ void renorm(typename P::Acc&) {}
+
+// FP64 values, B pre-split into double-float pairs: per column one exact TwoProduct of the hi
+// parts, two cross-term FMAs and one TwoSum (about 12 FP32 instructions); values are split by
+// split_df_fast and range-checked (a tile with an out-of-range value is redone natively).
+struct MmDFS {
+  using AV = double;
+  using BV = DF;
+  using BE = DF;
+  using Prep = DF;
+  using Acc = DFAcc;
+  using Out = double;
+  static constexpr bool kChecked = true;
+  __device__ static Prep prep(AV a, bool& ok) {
+    DF p;
+    split_df_fast(a, p.h, p.l);
+    ok &= df_in_range(a);
+    return p;
+  }
+  __device__ static Prep shfl(Prep a, int src) {
+    return DF{__shfl_sync(0xffffffffu, a.h, src), __shfl_sync(0xffffffffu, a.l, src)};
+  }
+  __device__ static Acc zero() { return DFAcc{0.f, 0.f}; }
+  __device__ static void madd(Acc& acc, Prep a, BE b, bool&) {
+    const float ph = __fmul_rn(a.h, b.h);
+    const float pe = __fmaf_rn(a.h, b.h, -ph);
+    float c = __fmaf_rn(a.h, b.l, acc.c);
+    c = __fmaf_rn(a.l, b.h, c);
+    float s1, e;
+    two_sum(acc.s, ph, s1, e);
+    acc.c = __fadd_rn(c, __fadd_rn(pe, e));
+    acc.s = s1;
+  }
+  __device__ static DF norm(Acc a) {
+    DF r;
+    two_sum(a.s, a.c, r.h, r.l);
+    return r;
+  }
+  __device__ static Out out(Acc a) { return df_to_double(norm(a)); }
+  __device__ static double to_double(Acc a) { return df_to_double(norm(a)); }
+};
+
+template <>
+__device__ __forceinline__ void renorm<MmDFS>(DFAcc& a) {
+  float s, e;
+  two_sum(a.s, a.c, s, e);
+  a.s = s;
+  a.c = e;
+}
+
 // ------------------------------------------------------------------ kernel ---------------
 
 constexpr int kMmBlock = 256;
@@ -221,6 +294,8 @@ __device__ __forceinline__ bool spmm_tile(const int32_t* __restrict__ pos,
           for (int v = 0; v < VEC; v++) P::madd(acc[v], a, b[v], ok);
         }
       }
+#pragma unroll
+      for (int v = 0; v < VEC; v++) renorm<P>(acc[v]);
     }
     if (r < r1) {
       if (active) {
@@ -236,6 +311,114 @@ __device__ __forceinline__ bool spmm_tile(const int32_t* __restrict__ pos,
         for (int v = 0; v < VEC; v++) carry_val[(int64_t)tile * N + col0 + v] = P::to_double(acc[v]);
       }
     }
+  }
+  if (lane == 0 && blockIdx.y == 0) carry_row[tile] = carried ? r1 : n;
+  return ok;
+}
+
+// ------------------------------------------------------------------ streaming warp tile ----
+//
+// The same merge tile walked as one stream of nonzeros instead of row by row: the warp loads
+// crd/vals 32 nonzeros at a time, one chunk ahead of the B-row loads that depend on them,
+// whatever the row boundaries; row ends come from a batch of 32 pos entries loaded at once;
+// a row is written when the stream passes its end.  A row walk waits for pos, then crd/vals,
+// then B for every row; here only the B loads are waited for.  Same contract as spmm_tile.
+template <class P, int VEC>
+__device__ __forceinline__ bool spmm_tile_stream(const int32_t* __restrict__ pos,
+                                                 const int32_t* __restrict__ crd,
+                                                 const typename P::AV* __restrict__ vals,
+                                                 const typename P::BV* __restrict__ B,
+                                                 typename P::Out* __restrict__ C, int32_t n,
+                                                 int32_t N, int2 c0, int2 c1, int tile, int col0,
+                                                 bool active, int32_t* __restrict__ carry_row,
+                                                 double* __restrict__ carry_val) {
+  using Acc = typename P::Acc;
+  using Prep = typename P::Prep;
+  using BE = typename P::BE;
+  using AV = typename P::AV;
+  constexpr int U = kMmUnroll;
+  const int lane = threadIdx.x & 31;
+  const int r0 = c0.x, k0 = c0.y, r1 = c1.x, k1 = c1.y;
+  bool ok = true;
+  // ends (pos[r + 1]) of rows rb .. rb + 31, one per lane; rows r1 and later are open
+  int rb = r0;
+  int re = (rb + lane < r1) ? __ldg(pos + rb + lane + 1) : INT_MAX;
+  int row = r0;
+  int next_end = __shfl_sync(0xffffffffu, re, 0);
+  bool open_nonempty = false;  // the current row has nonzeros in this tile
+  Acc acc[VEC];
+#pragma unroll
+  for (int v = 0; v < VEC; v++) acc[v] = P::zero();
+  auto emit = [&]() {
+    if (active) {
+      typename P::Out o[VEC];
+#pragma unroll
+      for (int v = 0; v < VEC; v++) o[v] = P::out(acc[v]);
+      store_vec<VEC>(C + (int64_t)row * N + col0, o);
+    }
+#pragma unroll
+    for (int v = 0; v < VEC; v++) acc[v] = P::zero();
+    open_nonempty = false;
+    row++;
+    if (row - rb == 32) {
+      rb = row;
+      re = (rb + lane < r1) ? __ldg(pos + rb + lane + 1) : INT_MAX;
+    }
+    next_end = __shfl_sync(0xffffffffu, re, row - rb);
+  };
+  int mc_n = 0;
+  AV mv_n = AV();
+  if (k0 + lane < k1) {
+    mc_n = __ldg(crd + k0 + lane);
+    mv_n = vals[k0 + lane];
+  }
+  for (int base = k0; base < k1; base += 32) {
+    const int cnt = min(32, k1 - base);
+    const int mc = mc_n;
+    const Prep ma = lane < cnt ? P::prep(mv_n, ok) : Prep();
+    if (base + 32 + lane < k1) {
+      mc_n = __ldg(crd + base + 32 + lane);
+      mv_n = vals[base + 32 + lane];
+    }
+    int j = 0;
+    for (; j + U <= cnt; j += U) {
+      BE b[U][VEC];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int c = __shfl_sync(0xffffffffu, mc, j + u);
+        if (active) load_vec<VEC>(B + (int64_t)c * N + col0, b[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        while (next_end <= base + j + u) emit();
+        const Prep a = P::shfl(ma, j + u);
+        if (active) {
+#pragma unroll
+          for (int v = 0; v < VEC; v++) P::madd(acc[v], a, b[u][v], ok);
+        }
+        open_nonempty = true;
+      }
+    }
+    for (; j < cnt; j++) {
+      const int c = __shfl_sync(0xffffffffu, mc, j);
+      BE b[VEC];
+      if (active) load_vec<VEC>(B + (int64_t)c * N + col0, b);
+      while (next_end <= base + j) emit();
+      const Prep a = P::shfl(ma, j);
+      if (active) {
+#pragma unroll
+        for (int v = 0; v < VEC; v++) P::madd(acc[v], a, b[v], ok);
+      }
+      open_nonempty = true;
+    }
+#pragma unroll
+    for (int v = 0; v < VEC; v++) renorm<P>(acc[v]);
+  }
+  while (row < r1) emit();  // rows that end at k1, and empty rows after the last nonzero
+  const bool carried = row < n && open_nonempty;
+  if (carried && active) {
+#pragma unroll
+    for (int v = 0; v < VEC; v++) carry_val[(int64_t)tile * N + col0 + v] = P::to_double(acc[v]);
   }
   if (lane == 0 && blockIdx.y == 0) carry_row[tile] = carried ? r1 : n;
   return ok;
@@ -263,6 +446,14 @@ __device__ __forceinline__ float acc_xor(float a, int o) {
 }
 __device__ __forceinline__ DF acc_xor(DF a, int o) {
   return DF{__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+}
+__device__ __forceinline__ DFAcc acc_add(DFAcc a, DFAcc b) {
+  float s, e;
+  two_sum(a.s, b.s, s, e);
+  return DFAcc{s, __fadd_rn(__fadd_rn(a.c, b.c), e)};
+}
+__device__ __forceinline__ DFAcc acc_xor(DFAcc a, int o) {
+  return DFAcc{__shfl_xor_sync(0xffffffffu, a.s, o), __shfl_xor_sync(0xffffffffu, a.c, o)};
 }
 
 constexpr int kSubLong = 64;
@@ -318,8 +509,11 @@ __device__ __forceinline__ void sub_emit(const typename P::Acc (&acc)[VEC], int 
   }
 }
 
-// Columns [ct, ct + LPR*VEC) of merge tile `tile`.  Same contract as spmm_tile.
-template <class P, int VEC, int SUB>
+// Columns [ct, ct + LPR*VEC) of merge tile `tile`.  Same contract as spmm_tile.  Rows of LONG
+// or more nonzeros are shared by the whole warp (sub-warp s takes every SUB-th nonzero, and a
+// butterfly joins the sub-warps at the row end); shorter rows get one sub-warp each.  LONG = 0
+// shares every row, which keeps all sub-warps busy whatever the row lengths.
+template <class P, int VEC, int SUB, int LONG = kSubLong>
 __device__ __forceinline__ bool spmm_tile_sub(const int32_t* __restrict__ pos,
                                               const int32_t* __restrict__ crd,
                                               const typename P::AV* __restrict__ vals,
@@ -346,7 +540,7 @@ __device__ __forceinline__ bool spmm_tile_sub(const int32_t* __restrict__ pos,
       pe = (myr < r1) ? __ldg(pos + myr + 1) : k1;
     }
     const int len = pe - ps;
-    const unsigned lmask = __ballot_sync(0xffffffffu, sl == 0 && myr <= rend && len >= kSubLong);
+    const unsigned lmask = __ballot_sync(0xffffffffu, sl == 0 && myr <= rend && len >= LONG);
     const int first_long = lmask ? (__ffs(lmask) - 1) / LPR : SUB;
     const int k = min(first_long, rend - r + 1);
     Acc acc[VEC];
@@ -371,6 +565,8 @@ __device__ __forceinline__ bool spmm_tile_sub(const int32_t* __restrict__ pos,
           mv_n = vals[base + 32 + lane];
         }
         sub_chunk<P, VEC, LPR>(acc, mc, ma, lb, cnt - lb, B, N, col0, active, ok);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) renorm<P>(acc[v]);
       }
 #pragma unroll
       for (int o = LPR; o < 32; o <<= 1) {
@@ -401,6 +597,8 @@ __device__ __forceinline__ bool spmm_tile_sub(const int32_t* __restrict__ pos,
           mv_n = vals[ps + base + LPR + sl];
         }
         sub_chunk<P, VEC, LPR>(acc, mc, ma, lb, cnt, B, N, col0, active, ok);
+#pragma unroll
+        for (int v = 0; v < VEC; v++) renorm<P>(acc[v]);
       }
       if (mine && active)
         sub_emit<P, VEC>(acc, myr, r1, len > 0, C, N, col0, tile, carry_val, carried);

@@ -108,7 +108,23 @@ def test_double_float_fallback(scale):
     B = W.dense(51, cols * 64).reshape(cols, 64)
     B[7, :] *= 1e20
     ref = O.spmm(pos, crd, vals, B)
-    assert normwise(run(pos, crd, vals, B, 1), ref) <= F64_TOL
+    names = tg.spmm_variants()
+    for v in [i for i, nm in enumerate(names) if nm.endswith(("_df", "_dfs"))]:
+        assert normwise(run(pos, crd, vals, B, v), ref) <= F64_TOL, names[v]
+
+
+def test_double_float_fallback_b_only():
+    """An out-of-range entry of B alone sends every tile of the pre-split product to DFMA."""
+    pos, crd, vals, cols = _mat("uniform")
+    B = W.dense(53, cols * 64).reshape(cols, 64)
+    B[11, 5] = 1e-300
+    ref = O.spmm(pos, crd, vals, B)
+    names = tg.spmm_variants()
+    for v in [i for i, nm in enumerate(names) if nm.endswith("_dfs")]:
+        assert normwise(run(pos, crd, vals, B, v), ref) <= F64_TOL, names[v]
+        # the flag is cleared: an in-range B right after is computed in double-float again
+        B2 = W.dense(54, cols * 64).reshape(cols, 64)
+        assert normwise(run(pos, crd, vals, B2, v), O.spmm(pos, crd, vals, B2)) <= F64_TOL
 
 
 def test_medium_powerlaw_n256():
