@@ -48,7 +48,7 @@ def parse():
     p.add_argument("--workload", default="spmv_powerlaw",
                    choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
                             "spgemm_random", "spgemm_poisson", "batched_spmv", "batched_spmm",
-                            "gather_probe"])
+                            "gather_probe", "pack_powerlaw"])
     p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
     p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
                    help="how batched_spmv picks each matrix's work-unit kind")
@@ -492,9 +492,81 @@ class SpgemmOp:
         return "port", lambda: O.spgemm(p, c, v, p, c, v, self.cols), (At,)
 
 
+class PackOp:
+    """COO -> CSR pack (taco's TensorBase::pack): the coordinates of the 4,194,304-row power-law
+    matrix (1.0e8 entries) in a fixed random order, with their FP64 values, packed into CSR.
+    value = algorithmic GB/s: 16 bytes read per coordinate record + 12 written per CSR entry +
+    4 per pos entry.  The CPU baseline is the oracle's restatement of taco's pack (one qsort of
+    the records, then the merge), single-threaded like taco's, on a 1/16 sample."""
+    pattern = "pack"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        s = self.spec = W.spmv_powerlaw()
+        pos, crd, vals = W.generate(s)
+        self.rows, self.cols, self.nnz = s.rows, s.cols, len(crd)
+        rng = np.random.default_rng(77)
+        perm = rng.permutation(self.nnz)
+        self.ri = np.repeat(np.arange(s.rows, dtype=np.int32), np.diff(pos))[perm]
+        self.ci = crd[perm]
+        self.v = vals[perm]
+        self.bytes = 16 * self.nnz + 12 * self.nnz + 4 * (self.rows + 1)
+        self.flops = 0
+        self.metric = "pack_f64_gbs"
+        self.workload = "pack_powerlaw_%d" % self.rows
+        k = self.nnz // 16
+        self.cpu_sample = (self.ri[:k], self.ci[:k], self.v[:k])
+        self.cpu_bytes = 28 * k + 4 * (self.rows + 1)
+        self.cpu_sample_desc = "first 1/16 of the records (%d), packed by the oracle's qsort" % k
+
+    def device(self, torch, tg):
+        L = tg.lib()
+        ri = torch.from_numpy(self.ri).cuda()
+        ci = torch.from_numpy(self.ci).cuda()
+        v = torch.from_numpy(self.v).cuda()
+        pos = torch.empty(self.rows + 1, dtype=torch.int32, device="cuda")
+        crd = torch.empty(self.nnz, dtype=torch.int32, device="cuda")
+        out = torch.empty(self.nnz, dtype=torch.float64, device="cuda")
+        nnz = ctypes.c_int64(0)
+        keep = (ri, ci, v, pos, crd, out, nnz)
+
+        def step(sp):
+            tg.check(L.tacogb_pack_csr(self.rows, self.cols, self.nnz, ri.data_ptr(), ci.data_ptr(),
+                                       v.data_ptr(), 0, pos.data_ptr(), crd.data_ptr(),
+                                       out.data_ptr(), ctypes.byref(nnz), sp), "tacogb_pack_csr")
+        return step, keep
+
+    def abi(self, torch, tg, T):
+        import ctypes.util
+        libc = ctypes.CDLL(ctypes.util.find_library("c"))
+        libc.free.argtypes = [ctypes.c_void_p]
+        dt = np.dtype([("r", "<i4"), ("c", "<i4"), ("v", "<f8")])
+        rec = np.empty(self.nnz, dtype=dt)
+        rec["r"], rec["c"], rec["v"] = self.ri, self.ci, self.v
+        buf = torch.from_numpy(rec.view(np.uint8)).pin_memory()
+        L = tg.lib()
+        keep = (buf,)
+
+        def step():
+            Tt = T.csr_result([self.rows, self.cols])
+            tg.check(L.tacogb_pack_taco(Tt.ptr, buf.data_ptr(), self.nnz), "tacogb_pack_taco")
+            for q in (Tt.index(1, 0), Tt.index(1, 1), Tt.vals_ptr):
+                libc.free(q)
+        return (step, keep, 16 * self.nnz, 12 * self.nnz + 4 * (self.rows + 1),
+                "tacogb_pack_taco(taco_tensor_t*) on taco's coordinate-buffer layout, pinned host")
+
+    def cpu(self):
+        from oracle import oracle as O
+        ri, ci, v = self.cpu_sample
+        return "port", lambda: O.pack_csr(self.rows, self.cols, ri, ci, v), None
+
+
 def make_op(args):
     if args.workload.startswith("spgemm"):
         return SpgemmOp(args)
+    if args.workload == "pack_powerlaw":
+        return PackOp(args)
     if args.workload == "batched_spmv":
         return BatchOp(args)
     if args.workload == "batched_spmm":
@@ -597,11 +669,14 @@ def run_reference(args):
             break
     dt = time.perf_counter() - t0
     unit = getattr(op, "unit", "GB/s")
-    work = op.cpu_units if op.pattern == "batch" else op.bytes
-    sample = (op.cpu_sample if op.pattern == "batch" else "whole workload") + \
+    work = (op.cpu_units if op.pattern == "batch"
+            else getattr(op, "cpu_bytes", op.bytes))
+    sample = (op.cpu_sample if op.pattern == "batch"
+              else getattr(op, "cpu_sample_desc", "whole workload")) + \
         " per step, %d steps" % steps
     v = work * steps / dt / 1e9
     code = ("taco generated C, -O3 -ffast-math -std=c99 -fopenmp" if kind == "reference"
+            else "C restatement of taco's pack: qsort + merge, one thread" if op.pattern == "pack"
             else "C restatement of taco's loop, -O2 -fopenmp")
     out = {"metric": op.metric, "value": v, "unit": unit, "impl": "reference",
            "n_gpus": world, "steps": steps, "warmup": args.warmup,
@@ -950,6 +1025,8 @@ def main():
                 "traffic": ncu_traffic(dom, "%s_%s" % (op.workload, args.dtype)),
                 "kernel": dom, "kernel_ms": dom_ms, "peak_source": peak_kind,
                 "kernel_share": dom_share}
+    if op.pattern == "spmv" and rank == 0:
+        roofline["gather"] = gather_roofline(torch, L, op.nnz, dom_ms)
     del keep
 
     e2e = None
@@ -975,12 +1052,16 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         kind, cores, t, reps = time_cpu(op)
-        cpu = {"value": op.bytes / t / 1e9, "unit": "GB/s", "cores": cores, "kind": kind,
-               "sample": "whole workload, median of %d reps" % reps, "ms_per_step": t * 1e3}
+        cpu_bytes = getattr(op, "cpu_bytes", op.bytes)
+        cpu = {"value": cpu_bytes / t / 1e9, "unit": "GB/s",
+               "cores": 1 if op.pattern == "pack" else cores, "kind": kind,
+               "sample": "%s, median of %d reps" % (getattr(op, "cpu_sample_desc",
+                                                            "whole workload"), reps),
+               "ms_per_step": t * 1e3}
 
     if rank == 0:
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
-                   "spgemm": lambda: ["default"]}[op.pattern]()
+                   "spgemm": lambda: ["default"], "pack": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,
                   "variant": "auto" if args.variant < 0 else names_v[args.variant],
@@ -1004,6 +1085,44 @@ def main():
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def gather_ceiling(torch, L, reps=5):
+    """Random 8-byte gathers per second of tacogb_probe_gather (ld.global.cg, 32 warps per SM,
+    shared memory as the SpMV kernels hold it): the ceiling of an x-gathering SpMV."""
+    rows, n = 1 << 21, 1 << 25
+    table = torch.zeros(rows * 2, dtype=torch.float64, device="cuda")
+    idx = torch.randint(0, rows, (n,), dtype=torch.int32, device="cuda",
+                        generator=torch.Generator(device="cuda").manual_seed(7))
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    out = torch.empty(sms * 1024, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    def run():
+        rc = L.tacogb_probe_gather(table.data_ptr(), rows, idx.data_ptr(), n, out.data_ptr(),
+                                   out.numel(), 1, 160, 70, sp)
+        if rc:
+            raise RuntimeError(L.tacogb_last_error().decode())
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return n * reps / (e0.elapsed_time(e1) / 1e3), sms
+
+
+def gather_roofline(torch, L, nnz, kernel_ms):
+    """The SpMV kernel's x gathers (one per nonzero) per second against the gather ceiling
+    measured now on this GPU (run after the timed region)."""
+    ceiling, sms = gather_ceiling(torch, L)
+    achieved = nnz / (kernel_ms / 1e3)
+    return {"achieved": achieved, "peak": ceiling, "unit": "gathers/s", "frac": achieved / ceiling,
+            "floor_ms": nnz / ceiling * 1e3,
+            "probe": "tacogb_probe_gather: random 8-byte ld.global.cg from a 32 MiB L2-resident "
+                     "table, 160 KB shared memory held per SM (carveout 70 %), as the kernel"}
 
 
 def main_gather_probe(args, torch, tg, L):

@@ -74,6 +74,26 @@ int tacogb_profile_end(int32_t max_kernels, char* names, double* total_ms, int32
  * records out of the rest. */
 void tacogb_profile_enable(int32_t on);
 
+/* COO -> CSR pack on the GPU.  Replaces the host sort and generated pack of TensorBase::pack
+ * (src/tensor.cpp:295-463, qsort at :420-422) for a rows x cols CSR ({Dense,Sparse}) tensor:
+ * n coordinates (coord_rows[i], coord_cols[i]) with values vals[i] (vtype TACOGB_F64 or
+ * TACOGB_F32), in any order and with duplicates, become pos (rows + 1 entries), crd and
+ * out_vals (capacity n each) with columns ascending per row and duplicates summed in input
+ * order; explicit zeros are kept, as taco keeps them.  Device (or managed) arrays, work on
+ * `stream`; *nnz is read back (the call synchronises).  A coordinate outside the matrix
+ * returns TACOGB_ERR_ARG. */
+int tacogb_pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_rows,
+                    const int32_t* coord_cols, const void* vals, int32_t vtype, int32_t* pos,
+                    int32_t* crd, void* out_vals, int64_t* nnz, void* stream);
+
+/* The same on taco's own data: `buffer` holds n records laid out as taco's coordinate buffer
+ * (int32 row, int32 column, then the value: 16 bytes per FP64 record, 12 per FP32), host or
+ * device memory; T is the 2-D CSR result tensor (dimensions, csize set).  Allocates pos, crd
+ * and vals (malloc, or cudaMallocManaged when the buffer is device-accessible, the allocators
+ * taco frees them with, src/storage/array.cpp:22-33) and stores them in T->indices[1] and
+ * T->vals as unpackTensorData does (src/tensor.cpp:263-292). */
+int tacogb_pack_taco(taco_tensor_t* T, const void* buffer, int64_t n);
+
 /* Diagnostic (no counterpart in taco): random-gather throughput probe.  Launches 4 blocks of 256
  * threads per SM on `stream`; each thread gathers entries table[2 * idx[i]] (rows of 16 bytes,
  * idx clamped into [0, rows)) eight at a time with load form `mode` (0 ld.global.nc,

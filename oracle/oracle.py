@@ -57,6 +57,8 @@ def lib():
         L.oracle_spgemm_assemble.argtypes = [I32, I32, P, P, P, P, P, ctypes.POINTER(P)]
         L.oracle_spgemm_compute.argtypes = [I32, I32, P, P, P, P, P, P, P, P, P]
         L.oracle_free.argtypes = [P]
+        L.oracle_pack_csr.restype = I64
+        L.oracle_pack_csr.argtypes = [I32, I32, I64, P, P, P, P, P, P]
         L.oracle_num_threads.restype = I32
         L.oracle_set_num_threads.argtypes = [I32]
         _lib = L
@@ -98,6 +100,22 @@ def spgemm(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, K):
         lib().oracle_spgemm_compute(rows, K, _p(Apos), _p(Acrd), _p(Avals), _p(Bpos), _p(Bcrd),
                                     _p(Bvals), _p(Cpos), _p(Ccrd), _p(Cvals))
     return Cpos, Ccrd, (Cvals if vals_given else None)
+
+
+def pack_csr(rows, cols, ri, ci, v):
+    """(pos, crd, vals) of the COO coordinates (ri, ci) with values v packed into CSR the way
+    taco's pack does: sorted, duplicates summed (in input order)."""
+    ri = np.ascontiguousarray(ri, dtype=np.int32)
+    ci = np.ascontiguousarray(ci, dtype=np.int32)
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    n = len(ri)
+    pos = np.empty(rows + 1, dtype=np.int32)
+    crd = np.empty(max(n, 1), dtype=np.int32)
+    out = np.empty(max(n, 1), dtype=np.float64)
+    m = lib().oracle_pack_csr(rows, cols, n, _p(ri), _p(ci), _p(v), _p(pos), _p(crd), _p(out))
+    if m < 0:
+        raise ValueError("coordinate outside the matrix")
+    return pos, crd[:m].copy(), out[:m].copy()
 
 
 def set_threads(n):

@@ -27,6 +27,13 @@
  * (test/tests-scheduling-eval.cpp:68-94, src/lower/lowerer_impl_imperative.cpp:2616-2781); its
  * output is identical to the serial form.
  *
+ *   pack   COO coordinates -> CSR, as TensorBase::pack does for a {Dense,Sparse} tensor
+ *          (src/tensor.cpp:295-463): sort the coordinates lexicographically (taco: qsort with
+ *          lexicographicalCmp, :253-261 and :420-422), then merge runs of equal coordinates
+ *          into one entry whose value is their sum (the generated pack over the COO buffer,
+ *          :935-1020; duplicates sum, tests-tensor.cpp:68-79).  taco's qsort is not stable;
+ *          this restatement breaks ties by input position, so duplicates sum in input order.
+ *
  * Compiled with -O2 -fopenmp -ffp-contract=off: products and sums are rounded separately, in
  * the written order.
  */
@@ -148,6 +155,55 @@ void oracle_spgemm_compute(int32_t rows, int32_t K, const int32_t* Apos, const i
     free(set);
     free(w);
   }
+}
+
+/* pack: (row, col, input position) records sorted lexicographically */
+typedef struct {
+  int32_t r, c;
+  int64_t k;
+} PackRec;
+
+static int cmp_pack(const void* a, const void* b) {
+  const PackRec* x = (const PackRec*)a;
+  const PackRec* y = (const PackRec*)b;
+  if (x->r != y->r) return x->r < y->r ? -1 : 1;
+  if (x->c != y->c) return x->c < y->c ? -1 : 1;
+  return x->k < y->k ? -1 : (x->k > y->k);
+}
+
+/* COO -> CSR with duplicates summed in input order; pos has rows + 1 entries, crd and out have
+ * room for n.  Returns nnz, or -1 when a coordinate is outside the matrix. */
+int64_t oracle_pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* ri,
+                        const int32_t* ci, const double* v, int32_t* pos, int32_t* crd,
+                        double* out) {
+  PackRec* rec = (PackRec*)malloc((size_t)(n > 0 ? n : 1) * sizeof(PackRec));
+  for (int64_t i = 0; i < n; i++) {
+    if (ri[i] < 0 || ri[i] >= rows || ci[i] < 0 || ci[i] >= cols) {
+      free(rec);
+      return -1;
+    }
+    rec[i].r = ri[i];
+    rec[i].c = ci[i];
+    rec[i].k = i;
+  }
+  qsort(rec, (size_t)n, sizeof(PackRec), cmp_pack);
+  int64_t m = 0;
+  int32_t row = 0;
+  pos[0] = 0;
+  for (int64_t i = 0; i < n;) {
+    const int32_t r = rec[i].r, c = rec[i].c;
+    double sum = v[rec[i].k];
+    int64_t j = i + 1;
+    for (; j < n && rec[j].r == r && rec[j].c == c; j++) sum = sum + v[rec[j].k];
+    while (row < r) pos[++row] = (int32_t)m;
+    crd[m] = c;
+    out[m] = sum;
+    m++;
+    i = j;
+  }
+  while (row < rows) pos[++row] = (int32_t)m;
+  free(rec);
+  return m;
 }
 
 void oracle_free(void* p) { free(p); }

@@ -10,7 +10,8 @@ from . import _native
 from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBError, check,
                       lib)
 
-__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "spgemm", "SpmvBatch",
+__all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "spgemm", "pack_csr",
+           "SpmvBatch",
            "SpmmBatch",
            "batch_variants", "lib", "check", "TacoGBError",
            "TACOGB_F64", "TACOGB_F32", "TACOGB_BF16", "VARIANT_AUTO"]
@@ -102,6 +103,24 @@ def spgemm(A, B, stream=None):
     check(L.tacogb_spgemm_numeric(ctypes.byref(a), ctypes.byref(b), pos.data_ptr(),
                                   crd.data_ptr(), vals.data_ptr(), sp), "tacogb_spgemm_numeric")
     return CsrMatrix(pos, crd, vals, B.cols)
+
+
+def pack_csr(rows, cols, coord_rows, coord_cols, vals, stream=None):
+    """COO -> CSR on the GPU through tacogb_pack_csr: int32 coordinate tensors and float64 or
+    float32 values on the GPU, any order, duplicates summed.  Returns a CsrMatrix."""
+    import torch
+    n = coord_rows.numel()
+    dev = coord_rows.device
+    pos = torch.empty(rows + 1, dtype=torch.int32, device=dev)
+    crd = torch.empty(max(n, 1), dtype=torch.int32, device=dev)
+    out = torch.empty(max(n, 1), dtype=vals.dtype, device=dev)
+    nnz = ctypes.c_int64(0)
+    check(lib().tacogb_pack_csr(rows, cols, n, coord_rows.data_ptr(), coord_cols.data_ptr(),
+                                vals.data_ptr(), _VTYPE[vals.element_size()], pos.data_ptr(),
+                                crd.data_ptr(), out.data_ptr(), ctypes.byref(nnz),
+                                _stream_ptr(stream)), "tacogb_pack_csr")
+    k = nnz.value
+    return CsrMatrix(pos, crd[:k].clone(), out[:k].clone(), cols)
 
 
 def spmm_variants():

@@ -84,7 +84,7 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 5;  // spmv, spmm, spgemm x2, tuner
+constexpr int kScratchSlots = 6;  // spmv, spmm, spgemm x2, tuner, pack
 
 struct DeviceState {
   int sms = 0;
@@ -682,6 +682,56 @@ int _shim_tacogb_spgemm_compute(void** a) {
 }
 int _shim_tacogb_spgemm_evaluate(void** a) {
   return tacogb_spgemm_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]);
+}
+
+// ------------------------------------------------------------------ pack ------------------
+//
+// Replaces TensorBase::pack (src/tensor.cpp:295-463) for a 2-D CSR tensor: taco's coordinate
+// buffer (any order, duplicates) becomes pos/crd/vals allocated with the allocator taco frees
+// them with, stored in the tensor as unpackTensorData (src/tensor.cpp:263-292) does.
+
+int tacogb_pack_taco(taco_tensor_t* T, const void* buffer, int64_t n) {
+  TACOGB_CHECK_ARG(T != nullptr, "pack: null tensor");
+  TACOGB_CHECK_ARG(T->order == 2 && T->dimensions && T->mode_types && T->indices,
+                   "pack: expected a 2-D tensor");
+  TACOGB_CHECK_ARG(T->mode_types[0] == taco_mode_dense && T->mode_types[1] == taco_mode_sparse,
+                   "pack: expected the CSR format {Dense, Sparse}");
+  TACOGB_CHECK_ARG(T->mode_ordering == nullptr ||
+                       (T->mode_ordering[0] == 0 && T->mode_ordering[1] == 1),
+                   "pack: expected mode ordering (0, 1)");
+  const int vt = value_type_of_csize(T->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "pack: csize %d bits", T->csize);
+  TACOGB_CHECK_ARG(n >= 0 && (n == 0 || buffer != nullptr), "pack: bad coordinate buffer");
+  const int32_t rows = T->dimensions[0], cols = T->dimensions[1];
+  const size_t vb = value_bytes(vt);
+  cudaStream_t st = lib_stream();
+  const bool managed = n > 0 && device_accessible(buffer);
+  Operand in;
+  if (int rc = stage_in(in, buffer, (size_t)n * (8 + vb), 10, st)) return rc;
+  int32_t* dr = (int32_t*)stage_buffer(11, (size_t)n * 4);
+  int32_t* dc = (int32_t*)stage_buffer(12, (size_t)n * 4);
+  void* dv = stage_buffer(13, (size_t)n * vb);
+  int32_t* dpos = (int32_t*)stage_buffer(14, ((size_t)rows + 1) * 4);
+  int32_t* dcrd = (int32_t*)stage_buffer(15, (size_t)n * 4);
+  void* dvals = stage_buffer(16, (size_t)n * vb);
+  if (!dr || !dc || !dv || !dpos || !dcrd || !dvals) return TACOGB_ERR_ALLOC;
+  if (int rc = pack_split_records(in.dev, n, vt, dr, dc, dv, st)) return rc;
+  int64_t nnz = 0;
+  if (int rc = pack_csr(rows, cols, n, dr, dc, dv, vt, dpos, dcrd, dvals, &nnz, st)) return rc;
+  int32_t* pos = (int32_t*)alloc_result(((size_t)rows + 1) * 4, managed);
+  int32_t* crd = (int32_t*)alloc_result((size_t)nnz * 4, managed);
+  void* vals = alloc_result((size_t)nnz * vb, managed);
+  if (!pos || !crd || !vals) return TACOGB_ERR_ALLOC;
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, dpos, ((size_t)rows + 1) * 4, cudaMemcpyDefault, st));
+  if (nnz) {
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(crd, dcrd, (size_t)nnz * 4, cudaMemcpyDefault, st));
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(vals, dvals, (size_t)nnz * vb, cudaMemcpyDefault, st));
+  }
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  T->indices[1][0] = (uint8_t*)pos;
+  T->indices[1][1] = (uint8_t*)crd;
+  T->vals = (uint8_t*)vals;
+  return 0;
 }
 
 }  // extern "C"

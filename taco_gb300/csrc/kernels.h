@@ -31,4 +31,12 @@ int spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos, i
 int spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
                    const int32_t* Ccrd, void* Cvals, cudaStream_t st);
 
+// COO -> CSR pack (pack.cu): device arrays in and out; *nnz read back (synchronises).
+int pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_rows,
+             const int32_t* coord_cols, const void* vals, int32_t vtype, int32_t* pos,
+             int32_t* crd, void* out_vals, int64_t* nnz, cudaStream_t st);
+// taco's coordinate-buffer records (int32 row, int32 column, value) -> separate arrays.
+int pack_split_records(const void* buf, int64_t n, int32_t vtype, int32_t* r, int32_t* c,
+                       void* v, cudaStream_t st);
+
 }  // namespace tacogb

@@ -94,6 +94,53 @@ def spgemm_cases():
          Cpos=cp, Ccrd=cc, Cvals=cv, K=np.array([s.cols]))
 
 
+def taco_pack_cli(rows, cols, ri, ci, v, workdir):
+    """CSR (pos, crd, vals) that taco itself makes of the coordinates: the taco CLI reads them
+    from a .tns file (Tensor::insert for every line, then TensorBase::pack: sort, sum
+    duplicates), evaluates B(i,j) = A(i,j) with A and B in CSR, and writes B.  .tns coordinates
+    are 1-based and the CLI infers each dimension from the largest coordinate, so the caller
+    puts an entry at (rows-1, cols-1)."""
+    import subprocess
+    src = os.path.join(workdir, "pack_in.tns")
+    dst = os.path.join(workdir, "pack_out.tns")
+    with open(src, "w") as f:
+        for a, b, x in zip(ri, ci, v):
+            f.write("%d %d %r\n" % (a + 1, b + 1, float(x)))
+    cli = os.path.join(ROOT, "oracle", "_ref", "bin", "taco")
+    subprocess.run([cli, "B(i,j) = A(i,j)", "-f=A:ds", "-f=B:ds", "-i=A:" + src, "-o=B:" + dst,
+                    "-time=1"], check=True, cwd=workdir, stdout=subprocess.DEVNULL)
+    entries = [line.split() for line in open(dst) if line.strip()]
+    r = np.array([int(e[0]) - 1 for e in entries], np.int64)
+    c = np.array([int(e[1]) - 1 for e in entries], np.int32)
+    x = np.array([float(e[2]) for e in entries])
+    order = np.lexsort((c, r))
+    r, c, x = r[order], c[order], x[order]
+    pos = np.searchsorted(r, np.arange(rows + 1), side="left").astype(np.int32)
+    return pos, c, x
+
+
+def pack_cases():
+    """COO with duplicates (integer values, so every summation order gives the same sums and
+    the CLI's printed values are exact), a pair that cancels to an explicit zero, empty rows,
+    and the last row/column present."""
+    import tempfile
+    rng = np.random.default_rng(21)
+    rows, cols, n = 700, 500, 30000
+    ri = rng.integers(0, rows, n)
+    ci = rng.integers(0, cols, n)
+    ri[ri % 7 == 3] = 0                     # rows 3, 10, ... stay empty
+    dup = rng.choice(n, 4000, replace=False)  # repeat some coordinates
+    ri = np.concatenate([ri, ri[dup], [5, 5, rows - 1]])
+    ci = np.concatenate([ci, ci[dup], [7, 7, cols - 1]])
+    v = np.concatenate([rng.integers(-50, 51, n + len(dup)), [13, -13, 2]]).astype(np.float64)
+    perm = rng.permutation(len(ri))
+    ri, ci, v = ri[perm].astype(np.int32), ci[perm].astype(np.int32), v[perm]
+    with tempfile.TemporaryDirectory() as d:
+        pos, crd, vals = taco_pack_cli(rows, cols, ri, ci, v, d)
+    save("pack_taco_cli", rows=np.int32(rows), cols=np.int32(cols), ri=ri, ci=ci, v=v, pos=pos,
+         crd=crd, vals=vals)
+
+
 if __name__ == "__main__":
     B.build()
     O.build()
@@ -103,3 +150,4 @@ if __name__ == "__main__":
     spmm_cases()
     assert O.ref_available("spgemm")
     spgemm_cases()
+    pack_cases()

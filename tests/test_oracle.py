@@ -78,3 +78,24 @@ def test_oracle_matches_golden_spmv(case):
     g = _golden(case + ".npz")
     y = O.spmv(g["pos"], g["crd"], g["vals"], g["x"])
     assert normwise(y, g["y"]) <= 1e-14
+
+
+def test_pack_kat():
+    """taco's test tensor/duplicates (test/tests-tensor.cpp:68-79): duplicates sum."""
+    pos, crd, v = O.pack_csr(5, 5, [1, 2, 1], [2, 2, 2], [42.0, 10.0, 1.0])
+    assert list(pos) == [0, 0, 1, 2, 2, 2] and list(crd) == [2, 2] and list(v) == [43.0, 10.0]
+
+
+def test_pack_oracle_matches_taco():
+    """The pack restatement against a fixture taco itself packed (tests/golden/make_golden.py
+    runs the taco CLI on a .tns file with duplicates, a cancelling pair and empty rows)."""
+    g = np.load(os.path.join(GOLDEN, "pack_taco_cli.npz"))
+    pos, crd, v = O.pack_csr(int(g["rows"]), int(g["cols"]), g["ri"], g["ci"], g["v"])
+    assert np.array_equal(pos, g["pos"]) and np.array_equal(crd, g["crd"])
+    assert np.array_equal(v, g["vals"])
+    assert (g["vals"] == 0.0).any()  # the cancelling pair stays an explicit zero, as in taco
+
+
+def test_pack_oracle_rejects_out_of_range():
+    with pytest.raises(ValueError):
+        O.pack_csr(3, 3, [0, 3], [0, 0], [1.0, 2.0])
