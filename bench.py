@@ -1164,6 +1164,24 @@ def main_gather_probe(args, torch, tg, L):
                 "ms_per_launch": ms, "load": forms[mode], "smem_kb_per_sm": smem_kb,
                 "carveout": carve, "config": {"workload": "gather_probe", "table_rows": rows,
                                               "gathers": n, "sms": sms}}), flush=True)
+    # host -> device link: the bound of the end-to-end (taco ABI, host operands) numbers
+    del table, idx
+    hbuf = torch.empty(1 << 30, dtype=torch.uint8).pin_memory()
+    dbuf = torch.empty(1 << 30, dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        dbuf.copy_(hbuf, non_blocking=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(5):
+        dbuf.copy_(hbuf, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 5
+    print(json.dumps({"metric": "h2d_copy_gbs", "value": (1 << 30) / (ms / 1e3) / 1e9,
+                      "unit": "GB/s", "ms_per_copy": ms,
+                      "config": {"workload": "gather_probe", "bytes": 1 << 30,
+                                 "how": "pinned host -> device copy (cudaMemcpyAsync), 1 GiB"}}),
+          flush=True)
 
 
 if __name__ == "__main__":

@@ -94,6 +94,17 @@ int tacogb_pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_
  * T->vals as unpackTensorData does (src/tensor.cpp:263-292). */
 int tacogb_pack_taco(taco_tensor_t* T, const void* buffer, int64_t n);
 
+/* Reads a 2-D Matrix Market (.mtx: coordinate or array, real, general or symmetric) or FROSTT
+ * (.tns: "i j value" lines) file into COO records, as taco's readMTX / readTNS insert them
+ * (src/storage/file_io_mtx.cpp:38-215, src/storage/file_io_tns.cpp:37-85): 0-based
+ * coordinates, symmetric off-diagonal entries followed by their mirror, values by strtod; the
+ * format is taken from the first line ("%%MatrixMarket" or not).  Lines are parsed by all host
+ * threads.  *coord_rows, *coord_cols and *vals are malloc'ed (free with tacogb_free_host); pass
+ * them to tacogb_pack_csr (after copying them to the GPU) for CSR. */
+int tacogb_read_coo(const char* path, int32_t* rows, int32_t* cols, int64_t* n,
+                    int32_t** coord_rows, int32_t** coord_cols, double** vals);
+void tacogb_free_host(void* p);
+
 /* Diagnostic (no counterpart in taco): random-gather throughput probe.  Launches 4 blocks of 256
  * threads per SM on `stream`; each thread gathers entries table[2 * idx[i]] (rows of 16 bytes,
  * idx clamped into [0, rows)) eight at a time with load form `mode` (0 ld.global.nc,

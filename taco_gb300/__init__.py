@@ -11,6 +11,7 @@ from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBE
                       lib)
 
 __all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "spgemm", "pack_csr",
+           "read_coo", "read_csr",
            "SpmvBatch",
            "SpmmBatch",
            "batch_variants", "lib", "check", "TacoGBError",
@@ -121,6 +122,37 @@ def pack_csr(rows, cols, coord_rows, coord_cols, vals, stream=None):
                                 _stream_ptr(stream)), "tacogb_pack_csr")
     k = nnz.value
     return CsrMatrix(pos, crd[:k].clone(), out[:k].clone(), cols)
+
+
+def read_coo(path):
+    """(rows, cols, coord_rows, coord_cols, vals) numpy arrays of a .mtx or .tns file, as taco's
+    readers insert them (tacogb_read_coo)."""
+    import numpy as np
+    L = lib()
+    rows, cols, n = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+    pr, pc, pv = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    check(L.tacogb_read_coo(str(path).encode(), ctypes.byref(rows), ctypes.byref(cols),
+                            ctypes.byref(n), ctypes.byref(pr), ctypes.byref(pc), ctypes.byref(pv)),
+          "tacogb_read_coo")
+    k = n.value
+    try:
+        as_np = lambda p, ct: np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ct)),  # noqa
+                                                     (max(k, 1),))[:k].copy()
+        out = (rows.value, cols.value, as_np(pr, ctypes.c_int32), as_np(pc, ctypes.c_int32),
+               as_np(pv, ctypes.c_double))
+    finally:
+        for p in (pr, pc, pv):
+            L.tacogb_free_host(p)
+    return out
+
+
+def read_csr(path, device="cuda"):
+    """A .mtx or .tns file as a CsrMatrix on the GPU: parsed on the host (all threads), packed
+    on the GPU (tacogb_pack_csr), duplicates summed in file order."""
+    import torch
+    rows, cols, ri, ci, v = read_coo(path)
+    t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
+    return pack_csr(rows, cols, t(ri), t(ci), t(v))
 
 
 def spmm_variants():

@@ -141,6 +141,66 @@ def pack_cases():
          crd=crd, vals=vals)
 
 
+def reader_cases():
+    """Small .mtx / .tns files (general with comments and duplicates, symmetric, array, tns)
+    and, for each, the CSR that taco makes of it: the CLI reads the file with its own reader
+    (readMTX / readTNS, then pack) and writes B(i,j) = A(i,j).  Values are multiples of 1/4 so
+    that the CLI's printed output is exact."""
+    import subprocess
+    import tempfile
+    rng = np.random.default_rng(31)
+    q = lambda k: rng.integers(-400, 401, k) / 4.0  # noqa: E731
+    files = {}
+    # general coordinate, comments, duplicates, corner entries present
+    rows, cols, k = 60, 45, 700
+    r, c = rng.integers(1, rows + 1, k), rng.integers(1, cols + 1, k)
+    r[:2], c[:2] = [rows, 1], [cols, 1]
+    r[2:12], c[2:12] = r[12:22], c[12:22]  # repeats
+    lines = ["%%MatrixMarket matrix coordinate real general", "% a comment", "%another",
+             "%d %d %d" % (rows, cols, k)]
+    lines += ["%d %d %r" % (a, b, float(v)) for a, b, v in zip(r, c, q(k))]
+    files["read_general.mtx"] = "\n".join(lines) + "\n"
+    # symmetric coordinate (lower triangle with diagonal)
+    n, k = 50, 300
+    a, b = rng.integers(1, n + 1, k), rng.integers(1, n + 1, k)
+    lo, hi = np.maximum(a, b), np.minimum(a, b)
+    lo[0], hi[0] = n, n
+    lines = ["%%MatrixMarket matrix coordinate real symmetric", "%d %d %d" % (n, n, k)]
+    lines += ["%d %d %r" % (x, y, float(v)) for x, y, v in zip(lo, hi, q(k))]
+    files["read_symmetric.mtx"] = "\n".join(lines) + "\n"
+    # array (column-major, every entry, zeros included)
+    rows, cols = 9, 7
+    vals = q(rows * cols)
+    vals[rng.choice(rows * cols, 20, replace=False)] = 0.0
+    lines = ["%%MatrixMarket matrix array real general", "%d %d" % (rows, cols)]
+    lines += ["%r" % float(v) for v in vals]
+    files["read_array.mtx"] = "\n".join(lines) + "\n"
+    # tns
+    rows, cols, k = 80, 33, 500
+    r, c = rng.integers(1, rows + 1, k), rng.integers(1, cols + 1, k)
+    r[0], c[0] = rows, cols
+    files["read_plain.tns"] = "".join("%d %d %r\n" % (a, b, float(v))
+                                      for a, b, v in zip(r, c, q(k)))
+    cli = os.path.join(ROOT, "oracle", "_ref", "bin", "taco")
+    for name, text in files.items():
+        path = os.path.join(OUT, name)
+        with open(path, "w") as f:
+            f.write(text)
+        with tempfile.TemporaryDirectory() as d:
+            dst = os.path.join(d, "out.tns")
+            subprocess.run([cli, "B(i,j) = A(i,j)", "-f=A:ds", "-f=B:ds", "-i=A:" + path,
+                            "-o=B:" + dst, "-time=1"], check=True, cwd=d, stdout=subprocess.DEVNULL)
+            ent = [line.split() for line in open(dst) if line.strip()]
+        rr = np.array([int(e[0]) - 1 for e in ent], np.int64)
+        cc = np.array([int(e[1]) - 1 for e in ent], np.int32)
+        vv = np.array([float(e[2]) for e in ent])
+        o = np.lexsort((cc, rr))
+        rr, cc, vv = rr[o], cc[o], vv[o]
+        nrows = int(rr.max()) + 1
+        pos = np.searchsorted(rr, np.arange(nrows + 1), side="left").astype(np.int32)
+        save(name.replace(".", "_"), pos=pos, crd=cc, vals=vv)
+
+
 if __name__ == "__main__":
     B.build()
     O.build()
@@ -151,3 +211,4 @@ if __name__ == "__main__":
     assert O.ref_available("spgemm")
     spgemm_cases()
     pack_cases()
+    reader_cases()

@@ -120,3 +120,16 @@ def test_taco_buffer_entry(where):
     crd = np.ctypeslib.as_array(ctypes.cast(Tt.index(1, 1), P(ctypes.c_int32)), (nnz,))
     val = np.ctypeslib.as_array(ctypes.cast(Tt.vals_ptr, P(ctypes.c_double)), (nnz,))
     assert_same((pos.copy(), crd.copy(), val.copy()), ref)
+
+
+@pytest.mark.parametrize("name", ["read_general.mtx", "read_symmetric.mtx", "read_array.mtx",
+                                  "read_plain.tns"])
+def test_read_csr_matches_taco(name):
+    """File -> host parse -> GPU pack equals what taco's reader and pack make of the file."""
+    A = tg.read_csr(os.path.join(GOLDEN, name))
+    g = np.load(os.path.join(GOLDEN, name.replace(".", "_") + ".npz"))
+    pos = A.pos.cpu().numpy()
+    nr = len(g["pos"]) - 1
+    assert np.array_equal(pos[:nr + 1], g["pos"]) and (pos[nr:] == pos[nr]).all()
+    assert np.array_equal(A.crd.cpu().numpy(), g["crd"])
+    assert np.array_equal(A.vals.cpu().numpy(), g["vals"])
