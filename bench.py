@@ -57,6 +57,8 @@ def parse():
                    help="dense columns of B for SpMM (default 64; 32 for batched_spmm)")
     p.add_argument("--variant", type=int, default=-1)
     p.add_argument("--e2e-steps", type=int, default=30)
+    p.add_argument("--pack-n", type=int, default=0,
+                   help="pack_powerlaw: pack only the first N shuffled records (0 = all)")
     p.add_argument("--no-cpu", action="store_true")
     a = p.parse_args()
     if a.n is None:
@@ -508,13 +510,17 @@ class PackOp:
         self.rows, self.cols, self.nnz = s.rows, s.cols, len(crd)
         rng = np.random.default_rng(77)
         perm = rng.permutation(self.nnz)
+        if args.pack_n > 0:  # a smaller case of the same records (profiling captures)
+            perm = perm[:args.pack_n]
         self.ri = np.repeat(np.arange(s.rows, dtype=np.int32), np.diff(pos))[perm]
         self.ci = crd[perm]
         self.v = vals[perm]
+        self.nnz = len(perm)
         self.bytes = 16 * self.nnz + 12 * self.nnz + 4 * (self.rows + 1)
         self.flops = 0
         self.metric = "pack_f64_gbs"
-        self.workload = "pack_powerlaw_%d" % self.rows
+        self.workload = "pack_powerlaw_%d" % self.rows + (
+            "_n%d" % self.nnz if args.pack_n > 0 else "")
         k = self.nnz // 16
         self.cpu_sample = (self.ri[:k], self.ci[:k], self.v[:k])
         self.cpu_bytes = 28 * k + 4 * (self.rows + 1)
