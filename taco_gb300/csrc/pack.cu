@@ -23,8 +23,8 @@ namespace tacogb {
 namespace {
 
 constexpr int kPkThreads = 256;
-constexpr int kPkRounds = 16;                       // items per thread per tile
-constexpr int kPkTile = kPkThreads * kPkRounds;     // 4096 items per block
+constexpr int kPkRounds = 8;                        // items per thread per tile
+constexpr int kPkTile = kPkThreads * kPkRounds;     // 2048 items per block
 constexpr int kPkWarps = kPkThreads / 32;
 constexpr int kRadix = 256;
 
@@ -47,37 +47,60 @@ pk_hist(const uint32_t* __restrict__ keys, int64_t n, int shift, int32_t* __rest
   hist[(int64_t)tid * nblocks + blockIdx.x] = h[tid];
 }
 
-// Stable scatter of one tile by the digit at `shift` of `keys`: item j*256 + t of the tile goes
-// to offs[d][block] + (number of earlier items of the tile with digit d).  The rank inside a
-// round of 256 items comes from __match_any_sync within each warp and per-warp digit counts;
-// run[d] carries the counts of earlier rounds.  `pass` (with its own idx_in == nullptr on the
-// first pass, meaning identity) and `other` travel with the keys.
+// Stable scatter of one tile by the digit at `shift` of `keys`: the tile's records are ranked
+// (record j*256 + t of the tile follows every earlier record of the same digit), reordered by
+// digit in shared memory, then written out so that each digit's records of the tile form one
+// contiguous run at offs[d][block] (coalesced writes instead of one 4-byte store per record
+// into a different place).  The rank inside a round of 256 records comes from
+// __match_any_sync within each warp and per-warp digit counts; run[d] carries earlier rounds.
+// idx_in == nullptr means identity indices (the first pass).
 __global__ void __launch_bounds__(kPkThreads)
 pk_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ other,
            const int32_t* __restrict__ idx_in, uint32_t* __restrict__ keys_out,
            uint32_t* __restrict__ other_out, int32_t* __restrict__ idx_out, int64_t n, int shift,
            const int32_t* __restrict__ offs, int32_t nblocks) {
+  __shared__ uint32_t s_key[kPkTile], s_oth[kPkTile];
+  __shared__ int32_t s_idx[kPkTile];
+  __shared__ int32_t loc[kRadix + 1];  // tile-local start of every digit
   __shared__ int32_t run[kRadix];
   __shared__ int32_t wcnt[kPkWarps][kRadix];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  run[tid] = offs[(int64_t)tid * nblocks + blockIdx.x];
+  const int64_t base = (int64_t)blockIdx.x * kPkTile;
+  const int cnt = (int)(n - base < kPkTile ? n - base : kPkTile);
+  uint32_t k[kPkRounds], o[kPkRounds];
+  int32_t x[kPkRounds];
+  run[tid] = 0;
 #pragma unroll
   for (int w = 0; w < kPkWarps; w++) wcnt[w][tid] = 0;
   __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * kPkTile;
-  const unsigned lt = (1u << lane) - 1;
+#pragma unroll
   for (int j = 0; j < kPkRounds; j++) {
-    const int64_t i = base + j * kPkThreads + tid;
-    const bool valid = i < n;
-    uint32_t k = 0, o = 0;
-    int32_t x = 0;
-    int d = kRadix;  // sentinel digit for items past the end
-    if (valid) {
-      k = keys[i];
-      o = other[i];
-      x = idx_in ? idx_in[i] : (int32_t)i;
-      d = (int)((k >> shift) & (kRadix - 1));
+    const int i = j * kPkThreads + tid;
+    if (i < cnt) {
+      k[j] = keys[base + i];
+      o[j] = other[base + i];
+      x[j] = idx_in ? idx_in[base + i] : (int32_t)(base + i);
+      atomicAdd(&run[(k[j] >> shift) & (kRadix - 1)], 1);
     }
+  }
+  __syncthreads();
+  if (tid == 0) {  // exclusive scan of the tile's 256 digit counts
+    int acc = 0;
+    for (int d = 0; d < kRadix; d++) {
+      loc[d] = acc;
+      acc += run[d];
+    }
+    loc[kRadix] = acc;
+  }
+  __syncthreads();
+  run[tid] = loc[tid];
+  __syncthreads();
+  const unsigned lt = (1u << lane) - 1;
+#pragma unroll
+  for (int j = 0; j < kPkRounds; j++) {
+    const int i = j * kPkThreads + tid;
+    const bool valid = i < cnt;
+    const int d = valid ? (int)((k[j] >> shift) & (kRadix - 1)) : kRadix;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const int intra = __popc(peers & lt);
     if (valid && intra == 0) wcnt[warp][d] = __popc(peers);
@@ -85,10 +108,10 @@ pk_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ other
     if (valid) {
       int pre = 0;
       for (int w = 0; w < warp; w++) pre += wcnt[w][d];
-      const int64_t dst = (int64_t)run[d] + pre + intra;
-      keys_out[dst] = k;
-      other_out[dst] = o;
-      idx_out[dst] = x;
+      const int p = run[d] + pre + intra;
+      s_key[p] = k[j];
+      s_oth[p] = o[j];
+      s_idx[p] = x[j];
     }
     __syncthreads();
     int add = 0;
@@ -99,6 +122,14 @@ pk_scatter(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ other
     }
     run[tid] += add;
     __syncthreads();
+  }
+  for (int p = tid; p < cnt; p += kPkThreads) {
+    const uint32_t kk = s_key[p];
+    const int d = (int)((kk >> shift) & (kRadix - 1));
+    const int64_t dst = (int64_t)offs[(int64_t)d * nblocks + blockIdx.x] + (p - loc[d]);
+    keys_out[dst] = kk;
+    other_out[dst] = s_oth[p];
+    idx_out[dst] = s_idx[p];
   }
 }
 
