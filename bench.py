@@ -39,7 +39,7 @@ PROFILE_EVERY = 8  # timed steps per step whose kernels are bracketed by CUDA ev
 ESZ = {"f64": 8, "f32": 4, "bf16": 2}
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=2000)
@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--pack-n", type=int, default=0,
                    help="pack_powerlaw: pack only the first N shuffled records (0 = all)")
     p.add_argument("--no-cpu", action="store_true")
-    a = p.parse_args()
+    a = p.parse_args(argv)
     if a.n is None:
         a.n = 32 if a.workload == "batched_spmm" else 64
     if a.workload.startswith("spmv") and a.dtype == "bf16":
@@ -71,6 +71,23 @@ def parse():
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
             int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def max_over_ranks(torch, value, world):
+    """The largest of every rank's value (a job's time is its slowest replica's); the value
+    itself on one rank.  Works on the job's process group, NCCL on GPUs or gloo on CPUs."""
+    if world <= 1:
+        return value
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_step, steps, world, seconds):
+    """Whole-job throughput of `world` replicas that each process units_per_step per step."""
+    return units_per_step * steps * world / seconds
 
 
 def measured_peak():
@@ -1008,12 +1025,8 @@ def main():
     L.tacogb_device_status(ctypes.byref(status))
     if status.value:
         raise RuntimeError("device status %d after the timed region" % status.value)
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = op.bytes * args.steps * world / (ms / 1e3) / 1e9
+    ms = max_over_ranks(torch, e0.elapsed_time(e1), world)
+    value = whole_job_rate(op.bytes, args.steps, world, ms / 1e3) / 1e9
 
     kernels = {}
     for k in range(nk):
@@ -1045,12 +1058,9 @@ def main():
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             astep()
-        e2e_s = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([e2e_s], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": op.bytes * args.e2e_steps * world / e2e_s / 1e9, "unit": "GB/s",
+        e2e_s = max_over_ranks(torch, time.perf_counter() - t0, world)
+        e2e = {"value": whole_job_rate(op.bytes, args.e2e_steps, world, e2e_s) / 1e9,
+               "unit": "GB/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "steps": args.e2e_steps, "ms_per_step": e2e_s / args.e2e_steps * 1e3, "api": api}
         del akeep
