@@ -48,7 +48,7 @@ def parse(argv=None):
     p.add_argument("--workload", default="spmv_powerlaw",
                    choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
                             "spgemm_random", "spgemm_poisson", "batched_spmv", "batched_spmm",
-                            "gather_probe", "pack_powerlaw"])
+                            "gather_probe", "pack_powerlaw", "sddmm_powerlaw"])
     p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
     p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
                    help="how batched_spmv picks each matrix's work-unit kind")
@@ -585,7 +585,94 @@ class PackOp:
         return "port", lambda: O.pack_csr(self.rows, self.cols, ri, ci, v), None
 
 
+class SddmmOp:
+    """SDDMM A(i,k) = B(i,k) * C(i,j) * D(j,k) kept at B's nonzeros: B the 1,048,576-row
+    power-law matrix (3.4e7 nonzeros), J = 128 (taco's sddmmGPU width), C and D U(-1,1).
+    value = GFLOP/s on 2 J flops per nonzero; the roofline is on the compulsory bytes (B's crd
+    and values, pos, C and D once, the result once).  The CPU baseline is the oracle's
+    restatement of taco's loop in its sampled form (taco's generated dense-result code would
+    need an I x K result of 8.8 TB here) on the first 1/16 of the rows, all host cores."""
+    pattern = "sddmm"
+    unit = "GFLOP/s"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        s = self.spec = W.sddmm_powerlaw()
+        self.pos, self.crd, self.vals = W.generate(s)
+        self.rows, self.cols, self.nnz = s.rows, s.cols, len(self.crd)
+        J = self.J = W.SDDMM_J
+        self.C = W.dense(61, s.rows * J).reshape(s.rows, J)
+        self.D = W.dense(62, J * s.cols).reshape(J, s.cols)
+        e = self.esz = 8 if args.dtype == "f64" else 4
+        self.bytes = (self.nnz * (4 + 2 * e) + 4 * (self.rows + 1) + e * self.rows * J
+                      + e * J * self.cols)
+        self.gather_bytes = (self.nnz * (4 + 2 * e) + 4 * (self.rows + 1) + e * self.rows * J
+                             + e * self.nnz * J)
+        self.flops = self.work = 2 * J * self.nnz
+        self.metric = "sddmm_%s_j%d_gflops" % (args.dtype, J)
+        self.workload = "%s_%d_j%d" % (args.workload, self.rows, J)
+        R = self.cpu_rows = self.rows // 16
+        self.cpu_work = 2 * J * int(self.pos[R])
+        self.cpu_sample_desc = ("first %d rows (%d nonzeros), oracle's sampled restatement of "
+                                "taco's loop" % (R, int(self.pos[R])))
+
+    def _dtype(self, torch):
+        return torch.float64 if self.args.dtype == "f64" else torch.float32
+
+    def device(self, torch, tg):
+        dt = self._dtype(torch)
+        B = tg.CsrMatrix.from_numpy(self.pos, self.crd, self.vals, self.cols, dtype=dt)
+        Cd = torch.from_numpy(self.C).to("cuda", dt)
+        Dd = torch.from_numpy(self.D).to("cuda", dt)
+        out = torch.empty(self.nnz, dtype=dt, device="cuda")
+        b = B.as_csr()
+        L, v = tg.lib(), self.args.variant
+        keep = (B, Cd, Dd, out, b)
+
+        def step(sp):
+            rc = L.tacogb_sddmm(ctypes.byref(b), self.J, Cd.data_ptr(), Dd.data_ptr(),
+                                out.data_ptr(), v, sp)
+            if rc:
+                raise RuntimeError(L.tacogb_last_error().decode())
+        return step, keep
+
+    def abi(self, torch, tg, T):
+        dt = self._dtype(torch)
+        hp, hc = torch.from_numpy(self.pos).pin_memory(), torch.from_numpy(self.crd).pin_memory()
+        hv = torch.from_numpy(self.vals).to(dt).pin_memory()
+        hC = torch.from_numpy(self.C).to(dt).pin_memory()
+        hD = torch.from_numpy(self.D).to(dt).pin_memory()
+        ho = torch.empty(self.nnz, dtype=dt).pin_memory()
+        Bt = T.csr(hp, hc, hv, [self.rows, self.cols])
+        At = T.csr(hp, hc, ho, [self.rows, self.cols])  # result with B's pattern
+        Ct, Dt = T.dense(hC, [self.rows, self.J]), T.dense(hD, [self.J, self.cols])
+        L = tg.lib()
+        keep = (hp, hc, hv, hC, hD, ho, Bt, At, Ct, Dt)
+
+        def step():
+            tg.check(L.tacogb_sddmm_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr),
+                     "tacogb_sddmm_compute")
+        e = self.esz
+        h2d = ((self.rows + 1) * 4 + self.nnz * (4 + e) + e * self.rows * self.J
+               + e * self.J * self.cols)
+        return (step, keep, h2d, self.nnz * e,
+                "tacogb_sddmm_compute(taco_tensor_t*) on pinned host arrays, CSR result")
+
+    def cpu(self):
+        from oracle import oracle as O
+        lib = O.lib()
+        R = self.cpu_rows
+        out = np.empty(int(self.pos[R]))
+        p, c, v, C, D = self.pos, self.crd, self.vals, self.C, self.D
+        return "port", lambda: lib.oracle_sddmm_sampled_f64(
+            R, self.cols, self.J, p.ctypes.data, c.ctypes.data, v.ctypes.data, C.ctypes.data,
+            D.ctypes.data, out.ctypes.data), out
+
+
 def make_op(args):
+    if args.workload == "sddmm_powerlaw":
+        return SddmmOp(args)
     if args.workload.startswith("spgemm"):
         return SpgemmOp(args)
     if args.workload == "pack_powerlaw":
@@ -693,7 +780,7 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     unit = getattr(op, "unit", "GB/s")
     work = (op.cpu_units if op.pattern == "batch"
-            else getattr(op, "cpu_bytes", op.bytes))
+            else getattr(op, "cpu_work", getattr(op, "cpu_bytes", op.bytes)))
     sample = (op.cpu_sample if op.pattern == "batch"
               else getattr(op, "cpu_sample_desc", "whole workload")) + \
         " per step, %d steps" % steps
@@ -711,7 +798,8 @@ def run_reference(args):
                             "sample": sample},
            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if op.pattern != "batch":
-        out["gflops"] = op.flops * steps / dt / 1e9
+        out["gflops"] = getattr(op, "cpu_work" if op.pattern == "sddmm" else "flops",
+                                op.flops) * steps / dt / 1e9
     print(json.dumps(out), flush=True)
     del keep
 
@@ -1026,7 +1114,9 @@ def main():
     if status.value:
         raise RuntimeError("device status %d after the timed region" % status.value)
     ms = max_over_ranks(torch, e0.elapsed_time(e1), world)
-    value = whole_job_rate(op.bytes, args.steps, world, ms / 1e3) / 1e9
+    unit = getattr(op, "unit", "GB/s")
+    work = getattr(op, "work", op.bytes)  # units of the metric per step (bytes or flops)
+    value = whole_job_rate(work, args.steps, world, ms / 1e3) / 1e9
 
     kernels = {}
     for k in range(nk):
@@ -1059,8 +1149,8 @@ def main():
         for _ in range(args.e2e_steps):
             astep()
         e2e_s = max_over_ranks(torch, time.perf_counter() - t0, world)
-        e2e = {"value": whole_job_rate(op.bytes, args.e2e_steps, world, e2e_s) / 1e9,
-               "unit": "GB/s",
+        e2e = {"value": whole_job_rate(work, args.e2e_steps, world, e2e_s) / 1e9,
+               "unit": unit,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "steps": args.e2e_steps, "ms_per_step": e2e_s / args.e2e_steps * 1e3, "api": api}
         del akeep
@@ -1068,8 +1158,8 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         kind, cores, t, reps = time_cpu(op)
-        cpu_bytes = getattr(op, "cpu_bytes", op.bytes)
-        cpu = {"value": cpu_bytes / t / 1e9, "unit": "GB/s",
+        cpu_work = getattr(op, "cpu_work", getattr(op, "cpu_bytes", work))
+        cpu = {"value": cpu_work / t / 1e9, "unit": unit,
                "cores": 1 if op.pattern == "pack" else cores, "kind": kind,
                "sample": "%s, median of %d reps" % (getattr(op, "cpu_sample_desc",
                                                             "whole workload"), reps),
@@ -1077,7 +1167,8 @@ def main():
 
     if rank == 0:
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
-                   "spgemm": lambda: ["default"], "pack": lambda: ["default"]}[op.pattern]()
+                   "sddmm": tg.sddmm_variants, "spgemm": lambda: ["default"],
+                   "pack": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,
                   "variant": "auto" if args.variant < 0 else names_v[args.variant],
@@ -1090,11 +1181,15 @@ def main():
         if op.pattern == "spmm":
             config["n"] = op.N
             config["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9
-        out = {"metric": op.metric, "value": value, "unit": "GB/s",
+        if op.pattern == "sddmm":
+            config["j"] = op.J
+            config["compulsory_gbs"] = op.bytes * args.steps * world / (ms / 1e3) / 1e9
+            config["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9
+        out = {"metric": op.metric, "value": value, "unit": unit,
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": args.dtype, "data": "synthetic", "config": config,
-               "pct_of_peak": value / peak, "gflops": op.flops * args.steps * world / (ms / 1e3) / 1e9,
+               "pct_of_peak": value / peak if unit == "GB/s" else None, "gflops": op.flops * args.steps * world / (ms / 1e3) / 1e9,
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clocks,
                "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kernels.items()}}

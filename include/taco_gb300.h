@@ -259,6 +259,21 @@ int tacogb_spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* 
 int tacogb_spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
                           const int32_t* Ccrd, void* Cvals, void* stream);
 
+/* SDDMM, A(i,k) = B(i,k) * C(i,j) * D(j,k): B CSR (rows I, cols K), C dense row-major I x J,
+ * D dense row-major J x K, all of B's value type (FP64 or FP32).  tacogb_sddmm writes the result
+ * at B's nonzeros, out[p] = B.vals[p] * sum_j C(i,j) D(j,k) for nonzero p = (i,k);
+ * tacogb_sddmm_dense writes taco's test form, a dense I x K result of row stride lda, zero
+ * outside B's pattern.  FP64 within 1e-12 normwise of taco's serial loop (double-float or
+ * DFMA, variant 1 or 0); FP32 natively.  Replaces the generated compute of that statement
+ * (test/tests-scheduling-eval.cpp:783-840 CPU, 1360-1417 with the GPU schedule at :270-286).
+ * Uses a K x J scratch copy of D (transposed) per call. */
+int tacogb_sddmm(const tacogb_csr* B, int32_t J, const void* C, const void* D, void* out,
+                 int32_t variant, void* stream);
+int tacogb_sddmm_dense(const tacogb_csr* B, int32_t J, const void* C, const void* D, void* A,
+                       int64_t lda, int32_t variant, void* stream);
+int tacogb_sddmm_variant_count(void);
+const char* tacogb_sddmm_variant_name(int32_t variant);
+
 /* ------------------------------------------------------------------ taco kernel ABI ----- */
 
 /* y(i) = A(i,j) * x(j).  Replaces the generated assemble/compute/evaluate of that statement
@@ -292,6 +307,16 @@ int tacogb_spgemm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B)
 int _shim_tacogb_spgemm_assemble(void** args);
 int _shim_tacogb_spgemm_compute(void** args);
 int _shim_tacogb_spgemm_evaluate(void** args);
+
+/* A(i,k) = B(i,k) * C(i,j) * D(j,k), B CSR, C and D {Dense,Dense} row-major; A either
+ * {Dense,Dense} (taco's test form: assemble allocates I*K values, compute zero-fills and writes
+ * B's pattern) or CSR with B's pattern (assemble copies B's pos and crd, allocates vals). */
+int tacogb_sddmm_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D);
+int tacogb_sddmm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D);
+int tacogb_sddmm_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D);
+int _shim_tacogb_sddmm_assemble(void** args);
+int _shim_tacogb_sddmm_compute(void** args);
+int _shim_tacogb_sddmm_evaluate(void** args);
 
 #ifdef __cplusplus
 }

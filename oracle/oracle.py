@@ -57,6 +57,8 @@ def lib():
         L.oracle_spgemm_assemble.argtypes = [I32, I32, P, P, P, P, P, ctypes.POINTER(P)]
         L.oracle_spgemm_compute.argtypes = [I32, I32, P, P, P, P, P, P, P, P, P]
         L.oracle_free.argtypes = [P]
+        L.oracle_sddmm_f64.argtypes = [I32, I32, I32, P, P, P, P, P, P]
+        L.oracle_sddmm_sampled_f64.argtypes = [I32, I32, I32, P, P, P, P, P, P]
         L.oracle_pack_csr.restype = I64
         L.oracle_pack_csr.argtypes = [I32, I32, I64, P, P, P, P, P, P]
         L.oracle_num_threads.restype = I32
@@ -118,6 +120,28 @@ def pack_csr(rows, cols, ri, ci, v):
     return pos, crd[:m].copy(), out[:m].copy()
 
 
+def sddmm(pos, crd, vals, C, D):
+    """Dense I x K result of A(i,k) = B(i,k) * C(i,j) * D(j,k), B = (pos, crd, vals)."""
+    pos, crd, vals = (np.ascontiguousarray(pos, np.int32), np.ascontiguousarray(crd, np.int32),
+                      np.ascontiguousarray(vals, np.float64))
+    C, D = np.ascontiguousarray(C, np.float64), np.ascontiguousarray(D, np.float64)
+    I, J, K = C.shape[0], C.shape[1], D.shape[1]
+    A = np.empty((I, K))
+    lib().oracle_sddmm_f64(I, K, J, _p(pos), _p(crd), _p(vals), _p(C), _p(D), _p(A))
+    return A
+
+
+def sddmm_sampled(pos, crd, vals, C, D):
+    """The same sums kept at B's nonzeros (one value per nonzero)."""
+    pos, crd, vals = (np.ascontiguousarray(pos, np.int32), np.ascontiguousarray(crd, np.int32),
+                      np.ascontiguousarray(vals, np.float64))
+    C, D = np.ascontiguousarray(C, np.float64), np.ascontiguousarray(D, np.float64)
+    I, J, K = C.shape[0], C.shape[1], D.shape[1]
+    out = np.empty(len(crd))
+    lib().oracle_sddmm_sampled_f64(I, K, J, _p(pos), _p(crd), _p(vals), _p(C), _p(D), _p(out))
+    return out
+
+
 def set_threads(n):
     lib().oracle_set_num_threads(n)
 
@@ -136,13 +160,14 @@ _ref = {}
 
 
 def ref_lib(pattern):
-    """taco's generated C for pattern (spmv, spmm, spgemm) as compiled by Makefile.ref; exports
+    """taco's generated C for pattern (spmv, spmm, spgemm, sddmm) as compiled by Makefile.ref; exports
     taco's own assemble/compute/evaluate(taco_tensor_t*...)."""
     if pattern not in _ref:
         path = os.path.join(REF_DIR, "libtacoref_%s.so" % pattern)
         L = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
+        nargs = 4 if pattern == "sddmm" else 3
         for fn in ("assemble", "compute", "evaluate"):
-            getattr(L, fn).argtypes = [P, P, P]
+            getattr(L, fn).argtypes = [P] * nargs
             getattr(L, fn).restype = ctypes.c_int
         _ref[pattern] = L
     return _ref[pattern]

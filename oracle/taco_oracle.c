@@ -34,6 +34,11 @@
  *          :935-1020; duplicates sum, tests-tensor.cpp:68-79).  taco's qsort is not stable;
  *          this restatement breaks ties by input position, so duplicates sum in input order.
  *
+ *   SDDMM  A(i,k) = B(i,k) * C(i,j) * D(j,k), B {Dense,Sparse}, A, C, D dense row-major
+ *          generated `compute` (taco's CLI, -f=A:dd -f=B:ds -f=C:dd -f=D:dd): zero A, then for
+ *          i, for j, for p in row i: A[i*K+k] += (B[p]*C[i*J+j]) * D[j*K+k] (the statement of
+ *          test/tests-scheduling-eval.cpp:783-840 and 1360-1417).
+ *
  * Compiled with -O2 -fopenmp -ffp-contract=off: products and sums are rounded separately, in
  * the written order.
  */
@@ -207,3 +212,43 @@ int64_t oracle_pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* ri
 }
 
 void oracle_free(void* p) { free(p); }
+
+/* A(i,k) = B(i,k) * C(i,j) * D(j,k): B CSR (I x K), C I x J and D J x K dense row-major.
+ * taco's tests use a dense I x K result (test/tests-scheduling-eval.cpp:783-840, 1360-1417);
+ * its default lowering of that statement zero-fills A, then for each row i, for each j, runs
+ * over row i's nonzeros k adding the term (B*C)*D into A(i,k), so each result sums its J terms
+ * in j order.  oracle_sddmm_f64 restates that loop; oracle_sddmm_sampled_f64 is the same loop
+ * with the result kept at B's nonzeros (out[p] for nonzero p) instead of a dense I x K array,
+ * for sizes where the dense result cannot be held. */
+void oracle_sddmm_f64(int32_t I, int32_t K, int32_t J, const int32_t* pos, const int32_t* crd,
+                      const double* bv, const double* C, const double* D, double* A) {
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < (int64_t)I * K; q++) A[q] = 0.0;
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < I; i++) {
+    double* a = A + (int64_t)i * K;
+    for (int32_t j = 0; j < J; j++) {
+      const double c = C[(int64_t)i * J + j];
+      const double* d = D + (int64_t)j * K;
+      for (int32_t p = pos[i]; p < pos[i + 1]; p++) {
+        const int32_t k = crd[p];
+        a[k] = a[k] + (bv[p] * c) * d[k];
+      }
+    }
+  }
+}
+
+void oracle_sddmm_sampled_f64(int32_t I, int32_t K, int32_t J, const int32_t* pos,
+                              const int32_t* crd, const double* bv, const double* C,
+                              const double* D, double* out) {
+  (void)K;
+#pragma omp parallel for schedule(static)
+  for (int32_t i = 0; i < I; i++) {
+    for (int32_t p = pos[i]; p < pos[i + 1]; p++) out[p] = 0.0;
+    for (int32_t j = 0; j < J; j++) {
+      const double c = C[(int64_t)i * J + j];
+      const double* d = D + (int64_t)j * K;
+      for (int32_t p = pos[i]; p < pos[i + 1]; p++) out[p] = out[p] + (bv[p] * c) * d[crd[p]];
+    }
+  }
+}

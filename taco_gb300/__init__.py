@@ -11,6 +11,7 @@ from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBE
                       lib)
 
 __all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "spgemm", "pack_csr",
+           "sddmm", "sddmm_variants",
            "read_coo", "read_csr",
            "SpmvBatch",
            "SpmmBatch",
@@ -84,6 +85,33 @@ def spmm(A, B, C=None, variant=VARIANT_AUTO, stream=None):
     check(lib().tacogb_spmm(ctypes.byref(c), N, B.data_ptr(), _BTYPE[B.element_size()],
                             C.data_ptr(), variant, _stream_ptr(stream)), "tacogb_spmm")
     return C
+
+
+def sddmm(B, C, D, out=None, dense=False, variant=VARIANT_AUTO, stream=None):
+    """A(i,k) = B(i,k) * C(i,j) * D(j,k) on the GPU: B a CsrMatrix, C (B.rows x J) and D
+    (J x B.cols) row-major torch tensors of B's value type.  Returns the values at B's nonzeros
+    (tacogb_sddmm) or, with dense=True, taco's dense B.rows x B.cols result, zero outside B's
+    pattern (tacogb_sddmm_dense)."""
+    import torch
+    J = C.shape[1]
+    b = B.as_csr()
+    if dense:
+        if out is None:
+            out = torch.empty(B.rows, B.cols, dtype=B.vals.dtype, device=C.device)
+        check(lib().tacogb_sddmm_dense(ctypes.byref(b), J, C.data_ptr(), D.data_ptr(),
+                                       out.data_ptr(), B.cols, variant, _stream_ptr(stream)),
+              "tacogb_sddmm_dense")
+        return out
+    if out is None:
+        out = torch.empty(B.nnz, dtype=B.vals.dtype, device=C.device)
+    check(lib().tacogb_sddmm(ctypes.byref(b), J, C.data_ptr(), D.data_ptr(), out.data_ptr(),
+                             variant, _stream_ptr(stream)), "tacogb_sddmm")
+    return out
+
+
+def sddmm_variants():
+    L = lib()
+    return [L.tacogb_sddmm_variant_name(i).decode() for i in range(L.tacogb_sddmm_variant_count())]
 
 
 def spgemm(A, B, stream=None):

@@ -100,6 +100,16 @@ SIGNATURES = {
     "tacogb_batch_autotune": (I32, [I32, ctypes.POINTER(Csr), P, P, I32, I32, P, P, P]),
     "tacogb_batch_select": (I32, [I32, ctypes.POINTER(Csr), P, P, P, P]),
     "tacogb_spmm": (I32, [ctypes.POINTER(Csr), I32, P, I32, P, I32, P]),
+    "tacogb_sddmm": (I32, [ctypes.POINTER(Csr), I32, P, P, P, I32, P]),
+    "tacogb_sddmm_dense": (I32, [ctypes.POINTER(Csr), I32, P, P, P, I64, I32, P]),
+    "tacogb_sddmm_variant_count": (I32, []),
+    "tacogb_sddmm_variant_name": (ctypes.c_char_p, [I32]),
+    "tacogb_sddmm_assemble": (I32, [P, P, P, P]),
+    "tacogb_sddmm_compute": (I32, [P, P, P, P]),
+    "tacogb_sddmm_evaluate": (I32, [P, P, P, P]),
+    "_shim_tacogb_sddmm_assemble": (I32, [P]),
+    "_shim_tacogb_sddmm_compute": (I32, [P]),
+    "_shim_tacogb_sddmm_evaluate": (I32, [P]),
     "tacogb_spmm_variant_count": (I32, []),
     "tacogb_spmm_variant_name": (ctypes.c_char_p, [I32]),
     "tacogb_spmm_assemble": (I32, [P, P, P]),

@@ -21,7 +21,7 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "lib", "obj")
 
 CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu", "spgemm.cu", "batched.cu", "batched_spmm.cu",
-              "tuner.cu", "probe.cu", "pack.cu", "fileio.cpp"]
+              "tuner.cu", "probe.cu", "pack.cu", "sddmm.cu", "fileio.cpp"]
 PATTERNS = ["spmv", "spmm", "spgemm"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 NVCC_FLAGS = [

@@ -84,7 +84,7 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 6;  // spmv, spmm, spgemm x2, tuner, pack
+constexpr int kScratchSlots = 7;  // spmv, spmm, spgemm x2, tuner, pack, sddmm
 
 struct DeviceState {
   int sms = 0;
@@ -732,6 +732,140 @@ int tacogb_pack_taco(taco_tensor_t* T, const void* buffer, int64_t n) {
   T->indices[1][1] = (uint8_t*)crd;
   T->vals = (uint8_t*)vals;
   return 0;
+}
+
+// ------------------------------------------------------------------ SDDMM -----------------
+//
+// A(i,k) = B(i,k) * C(i,j) * D(j,k) (test/tests-scheduling-eval.cpp:783-840 and 1360-1417).
+// A is either taco's test form, {Dense,Dense} I x K (zero outside B's pattern), or CSR with
+// B's pattern (assemble copies B's pos and crd).
+
+int tacogb_sddmm(const tacogb_csr* B, int32_t J, const void* C, const void* D, void* out,
+                 int32_t variant, void* stream) {
+  return sddmm_run(B, J, C, D, out, 0, variant, (cudaStream_t)stream);
+}
+int tacogb_sddmm_dense(const tacogb_csr* B, int32_t J, const void* C, const void* D, void* A,
+                       int64_t lda, int32_t variant, void* stream) {
+  TACOGB_CHECK_ARG(lda > 0 || (B != nullptr && (int64_t)B->rows * B->cols == 0),
+                   "sddmm: dense result needs a positive row stride");
+  return sddmm_run(B, J, C, D, A, lda > 0 ? lda : 1, variant, (cudaStream_t)stream);
+}
+int tacogb_sddmm_variant_count(void) { return sddmm_variant_count(); }
+const char* tacogb_sddmm_variant_name(int32_t v) { return sddmm_variant_name(v); }
+
+namespace {
+bool is_csr_result(const taco_tensor_t* A) {
+  return A != nullptr && A->order == 2 && A->mode_types != nullptr &&
+         A->mode_types[1] == taco_mode_sparse;
+}
+
+int check_sddmm(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D) {
+  if (is_csr_result(A)) {
+    if (int rc = check_csr(A, "sddmm result A")) return rc;
+  } else if (int rc = check_dense_matrix(A, "sddmm result A")) {
+    return rc;
+  }
+  if (int rc = check_csr(B, "sddmm operand B")) return rc;
+  if (int rc = check_dense_matrix(C, "sddmm operand C")) return rc;
+  if (int rc = check_dense_matrix(D, "sddmm operand D")) return rc;
+  const int32_t I = B->dimensions[0], K = B->dimensions[1];
+  TACOGB_CHECK_ARG(A->dimensions[0] == I && A->dimensions[1] == K,
+                   "sddmm: A is %dx%d, B is %dx%d", A->dimensions[0], A->dimensions[1], I, K);
+  TACOGB_CHECK_ARG(C->dimensions[0] == I, "sddmm: C has %d rows, B has %d", C->dimensions[0], I);
+  TACOGB_CHECK_ARG(D->dimensions[1] == K, "sddmm: D has %d columns, B has %d", D->dimensions[1],
+                   K);
+  TACOGB_CHECK_ARG(C->dimensions[1] == D->dimensions[0], "sddmm: C has %d columns, D has %d rows",
+                   C->dimensions[1], D->dimensions[0]);
+  const int vt = value_type_of_csize(B->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "sddmm: unsupported csize %d", B->csize);
+  TACOGB_CHECK_ARG(A->csize == B->csize && C->csize == B->csize && D->csize == B->csize,
+                   "sddmm: operand component sizes differ (%d, %d, %d, %d)", A->csize, B->csize,
+                   C->csize, D->csize);
+  return 0;
+}
+}  // namespace
+
+int tacogb_sddmm_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D) {
+  if (int rc = check_sddmm(A, B, C, D)) return rc;
+  const int vt = value_type_of_csize(B->csize);
+  const int32_t I = B->dimensions[0], K = B->dimensions[1];
+  const bool managed = device_accessible(B->vals) && B->vals != nullptr;
+  if (!is_csr_result(A)) {
+    void* p = alloc_result((size_t)I * (size_t)K * value_bytes(vt), managed);
+    if (!p) return TACOGB_ERR_ALLOC;
+    A->vals = (uint8_t*)p;
+    return 0;
+  }
+  const int32_t* bpos = (const int32_t*)B->indices[1][0];
+  TACOGB_CHECK_ARG(bpos != nullptr, "sddmm: null pos");
+  int32_t nnz = 0;
+  if (int rc = read_i32(bpos + I, &nnz)) return rc;
+  int32_t* pos = (int32_t*)alloc_result(((size_t)I + 1) * 4, managed);
+  int32_t* crd = (int32_t*)alloc_result((size_t)nnz * 4, managed);
+  void* vals = alloc_result((size_t)nnz * value_bytes(vt), managed);
+  if (!pos || !crd || !vals) return TACOGB_ERR_ALLOC;
+  cudaStream_t st = lib_stream();
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, bpos, ((size_t)I + 1) * 4, cudaMemcpyDefault, st));
+  if (nnz)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(crd, B->indices[1][1], (size_t)nnz * 4, cudaMemcpyDefault, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  A->indices[1][0] = (uint8_t*)pos;
+  A->indices[1][1] = (uint8_t*)crd;
+  A->vals = (uint8_t*)vals;
+  return 0;
+}
+
+int tacogb_sddmm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D) {
+  if (int rc = check_sddmm(A, B, C, D)) return rc;
+  TACOGB_CHECK_ARG(A->vals != nullptr, "sddmm: result values not assembled");
+  const int vt = value_type_of_csize(B->csize);
+  const size_t vb = value_bytes(vt);
+  const int32_t I = B->dimensions[0], K = B->dimensions[1], J = C->dimensions[1];
+  const int32_t* pos = (const int32_t*)B->indices[1][0];
+  TACOGB_CHECK_ARG(pos != nullptr, "sddmm: null pos");
+  int32_t nnz = 0;
+  if (int rc = read_i32(pos + I, &nnz)) return rc;
+  const bool dense = !is_csr_result(A);
+  cudaStream_t st = lib_stream();
+  Operand opos, ocrd, ovals, oc, od;
+  if (int rc = stage_in(opos, pos, ((size_t)I + 1) * 4, 20, st)) return rc;
+  if (int rc = stage_in(ocrd, B->indices[1][1], (size_t)nnz * 4, 21, st)) return rc;
+  if (int rc = stage_in(ovals, B->vals, (size_t)nnz * vb, 22, st)) return rc;
+  if (int rc = stage_in(oc, C->vals, (size_t)I * J * vb, 23, st)) return rc;
+  if (int rc = stage_in(od, D->vals, (size_t)J * K * vb, 24, st)) return rc;
+  const size_t obytes = dense ? (size_t)I * (size_t)K * vb : (size_t)nnz * vb;
+  void* odev = A->vals;
+  const bool staged = !device_accessible(A->vals);
+  if (staged) {
+    odev = stage_buffer(25, obytes);
+    if (!odev) return TACOGB_ERR_ALLOC;
+  }
+  tacogb_csr b{I, K, nnz, (const int32_t*)opos.dev, (const int32_t*)ocrd.dev, ovals.dev, vt};
+  if (int rc = sddmm_run(&b, J, oc.dev, od.dev, odev, dense ? (K > 0 ? K : 1) : 0,
+                         TACOGB_VARIANT_AUTO, st))
+    return rc;
+  if (staged && obytes)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(A->vals, odev, obytes, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return consume_device_status();
+}
+
+int tacogb_sddmm_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D) {
+  if (int rc = tacogb_sddmm_assemble(A, B, C, D)) return rc;
+  return tacogb_sddmm_compute(A, B, C, D);
+}
+
+int _shim_tacogb_sddmm_assemble(void** a) {
+  return tacogb_sddmm_assemble((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2],
+                               (taco_tensor_t*)a[3]);
+}
+int _shim_tacogb_sddmm_compute(void** a) {
+  return tacogb_sddmm_compute((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2],
+                              (taco_tensor_t*)a[3]);
+}
+int _shim_tacogb_sddmm_evaluate(void** a) {
+  return tacogb_sddmm_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2],
+                               (taco_tensor_t*)a[3]);
 }
 
 }  // extern "C"

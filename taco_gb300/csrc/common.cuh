@@ -90,6 +90,9 @@ constexpr int kXFlagWord = 16;
 // Word of the same block holding the double-float SpMM's B-range flag (set by its B-split
 // kernel, cleared by its fix-up kernel).
 constexpr int kBFlagWord = 17;
+// Word of the same block holding the double-float SDDMM's D-range flag (cleared before, set by
+// its transpose kernel).
+constexpr int kDFlagWord = 18;
 
 // ---------------------------------------------------------------- TMA / mbarrier ----------
 

@@ -31,6 +31,13 @@ int spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos, i
 int spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
                    const int32_t* Ccrd, void* Cvals, cudaStream_t st);
 
+// SDDMM (sddmm.cu): values of B .* (C * D) at B's nonzeros (out_ld == 0) or into a dense
+// rows x cols result of row stride out_ld (zero-filled first).
+int sddmm_variant_count();
+const char* sddmm_variant_name(int v);
+int sddmm_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, void* out,
+              int64_t out_ld, int variant, cudaStream_t st);
+
 // COO -> CSR pack (pack.cu): device arrays in and out; *nnz read back (synchronises).
 int pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_rows,
              const int32_t* coord_cols, const void* vals, int32_t vtype, int32_t* pos,

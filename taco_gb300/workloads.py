@@ -47,6 +47,14 @@ def spmm_powerlaw(rows=1048576, seed=SEED_BASE + 3):
     return spec(rows, kind=POWERLAW, mean=32.0, len_max=min(10000, rows), seed=seed)
 
 
+# SDDMM: the SpMM power-law matrix as the sampling pattern, J = 128 (taco's sddmmGPU width)
+SDDMM_J = 128
+
+
+def sddmm_powerlaw(rows=1048576, seed=SEED_BASE + 3):
+    return spmm_powerlaw(rows, seed)
+
+
 def spgemm_random(rows=262144, seed=SEED_BASE + 4):
     return spec(rows, kind=UNIFORM, len_lo=8, len_hi=8, seed=seed)
 

@@ -94,6 +94,24 @@ def spgemm_cases():
          Cpos=cp, Ccrd=cc, Cvals=cv, K=np.array([s.cols]))
 
 
+def sddmm_cases():
+    # taco's sddmmGPU inputs (test/tests-scheduling-eval.cpp:1360-1417): I 102, K 103, J 128
+    (pos, crd, vals), C, D = H.taco_sddmm_inputs(1021 // 10, 128, 1039 // 10, 0.3, 535366)
+    save("sddmm_taco_gpu", pos=pos, crd=crd, vals=vals, C=C, D=D,
+         A=H.ref_sddmm(pos, crd, vals, C, D))
+    # taco's sddmmCPU inputs (:783-840): I 102, J 103, K 105
+    (pos, crd, vals), C, D = H.taco_sddmm_inputs(1021 // 10, 1039 // 10, 1057 // 10, 0.3, 268238)
+    save("sddmm_taco_cpu", pos=pos, crd=crd, vals=vals, C=C, D=D,
+         A=H.ref_sddmm(pos, crd, vals, C, D))
+    # power-law rows, real values, J 96 (three quarters of a 128-wide slab); C and D are
+    # W.dense(17, 512 * 96) and W.dense(18, 96 * 512), regenerated by the tests
+    s = W.spec(512, kind=W.POWERLAW, mean=32.0, len_max=512, seed=W.SEED_BASE + 104)
+    pos, crd, vals = W.generate(s)
+    C = W.dense(17, s.rows * 96).reshape(s.rows, 96)
+    D = W.dense(18, 96 * s.cols).reshape(96, s.cols)
+    save("sddmm_powerlaw_j96", pos=pos, crd=crd, vals=vals, A=H.ref_sddmm(pos, crd, vals, C, D))
+
+
 def taco_pack_cli(rows, cols, ri, ci, v, workdir):
     """CSR (pos, crd, vals) that taco itself makes of the coordinates: the taco CLI reads them
     from a .tns file (Tensor::insert for every line, then TensorBase::pack: sort, sum
@@ -210,5 +228,7 @@ if __name__ == "__main__":
     spmm_cases()
     assert O.ref_available("spgemm")
     spgemm_cases()
+    assert O.ref_available("sddmm")
+    sddmm_cases()
     pack_cases()
     reader_cases()

@@ -47,6 +47,31 @@ def taco_rand_csr(rows, cols, sparsity, seed=75883, dense_b_cols=None, b_sparse=
     return A, B
 
 
+def taco_sddmm_inputs(I, J, K, sparsity, seed):
+    """The inputs of taco's sddmm tests (test/tests-scheduling-eval.cpp:783-840 and
+    1360-1417): srand(seed); C (I x J) dense, then B (I x K) with an entry where
+    rand_float < SPARSITY, then D (J x K) dense, every value (double)(int)(rand_float*3/SPARSITY).
+    Returns (pos, crd, vals), C, D."""
+    _libc.srand(seed)
+    sp = np.float32(sparsity)
+
+    def draw():
+        r = np.float32(_libc.rand()) / np.float32(RAND_MAX)
+        return r, float(int(np.float32(np.float32(r * np.float32(3)) / sp)))
+
+    C = np.array([[draw()[1] for _ in range(J)] for _ in range(I)])
+    pos, crd, vals = [0], [], []
+    for i in range(I):
+        for k in range(K):
+            r, v = draw()
+            if r < sp:
+                crd.append(k)
+                vals.append(v)
+        pos.append(len(crd))
+    D = np.array([[draw()[1] for _ in range(K)] for _ in range(J)])
+    return (np.array(pos, np.int32), np.array(crd, np.int32), np.array(vals)), C, D
+
+
 def normwise(approx, exact):
     """||approx - exact||_2 / ||exact||_2 (0 when both are zero)."""
     a = np.asarray(approx, dtype=np.float64).ravel()
@@ -81,6 +106,19 @@ def ref_spmm(pos, crd, vals, B, threads=1):
     At, Bt, Ct = T.csr(pos, crd, vals, [rows, cols]), T.dense(B, [cols, N]), T.dense(C, [rows, N])
     assert L.compute(Ct.ptr, At.ptr, Bt.ptr) == 0
     return C
+
+
+def ref_sddmm(pos, crd, vals, C, D, threads=1):
+    """taco's generated SDDMM compute (dense I x K result) on host arrays."""
+    L = O.ref_lib("sddmm")
+    O.ref_set_threads(threads)
+    C, D = np.ascontiguousarray(C, np.float64), np.ascontiguousarray(D, np.float64)
+    I, J, K = C.shape[0], C.shape[1], D.shape[1]
+    A = np.empty((I, K))
+    At, Bt = T.dense(A, [I, K]), T.csr(pos, crd, vals, [I, K])
+    Ct, Dt = T.dense(C, [I, J]), T.dense(D, [J, K])
+    assert L.compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr) == 0
+    return A
 
 
 def ref_spgemm(A, B, threads=1):
