@@ -22,7 +22,8 @@ OBJDIR = os.path.join(HERE, "lib", "obj")
 
 CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu", "spgemm.cu", "batched.cu", "batched_spmm.cu",
               "tuner.cu", "probe.cu", "pack.cu", "sddmm.cu", "fileio.cpp"]
-PATTERNS = ["spmv", "spmm", "spgemm"]
+PATTERNS = ["spmv", "spmm", "spgemm", "sddmm"]
+NARGS = {"sddmm": 4}  # tensors per call (result and operands); 3 otherwise
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
@@ -80,7 +81,8 @@ def build(verbose=False, extra_flags=()):
             out = os.path.join(LIBDIR, "libtacogb_%s.so" % p)
             if _stale(out, [mod_src, lib, os.path.join(INC, "taco_gb300.h")]):
                 mods.append(ex.submit(_run, ["gcc", "-O2", "-fPIC", "-shared", "-I" + INC,
-                                             "-DTACOGB_PATTERN=%s" % p, mod_src, "-o", out,
+                                             "-DTACOGB_PATTERN=%s" % p,
+                                             "-DTACOGB_NARGS=%d" % NARGS.get(p, 3), mod_src, "-o", out,
                                              "-L" + LIBDIR, "-ltacogb", "-Wl,-rpath,$ORIGIN"]))
         for f in mods:
             f.result()

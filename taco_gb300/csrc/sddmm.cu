@@ -13,6 +13,9 @@
 // nine shuffles leaves every lane with one whole dot; four groups fill the warp's 32 results,
 // multiplied by B's values and written with one coalesced store.
 //
+// The group loop is kept rolled: unrolled over a batch's four groups the body overflowed the
+// instruction cache (ncu: "no instruction" the second stall reason; 6.32 -> 5.69 ms rolled).
+//
 // FP64 runs natively (DFMA) or in double-float on the FP32 pipe (Dt split into hi/lo float
 // pairs by the transpose, C split when its row is loaded): GB300's FP64 pipe retires about
 // 1.6 DFMA per clock per SM, so the 2J flops per nonzero are pipe-bound natively.  Values
@@ -363,7 +366,7 @@ __global__ void __launch_bounds__(kSdBlock, 2) sddmm_kernel(const SdArgs<P> a) {
     const int r = sd_batch_rows(a.pos, a.rows, lo, pl, lane);
     lo = __shfl_sync(kFull, r, 31);
     V res = V(0);
-#pragma unroll
+#pragma unroll 1  // one group's code: the fully unrolled batch overflows the instruction cache
     for (int g = 0; g < 4; g++) {
       if (base + 8 * g >= pend) break;
       Acc part[8];
@@ -436,7 +439,9 @@ namespace {
 // copies of the next two groups are in flight while a group is computed, so a warp keeps up to
 // 24 KB of gathers outstanding without holding them in registers.  Per group the eight rows'
 // C slices are settled first (a reload when the row changes), then the 8 x JL products run
-// without branches.
+// without branches.  Measured slower than the register form at J = 128 in FP64 (8.08 against
+// 5.69 ms on the 1,048,576-row power-law B): 1 KB rows leave room for only eight warps per SM,
+// too few to cover the double-float arithmetic; it stays a selectable variant.
 constexpr int kStWarps = 4;
 constexpr int kStStages = 3;
 
@@ -579,7 +584,7 @@ namespace {
 struct SddmmVariant {
   const char* name;
   int df;   // FP64: 0 native DFMA, 1 double-float (FP32 values always run natively)
-  int tma;  // 1: TMA-staged Dt rows for J <= 128 (wider J falls back to the register form)
+  int tma;  // 1: TMA-staged Dt rows for J <= 128 (wider J runs the register form)
 };
 constexpr SddmmVariant kSddmmVariants[] = {
     {"warp_native", 0, 0}, {"warp_dfs", 1, 0}, {"tma_native", 0, 1}, {"tma_dfs", 1, 1}};
@@ -621,7 +626,7 @@ int sd_launch_tma(const SdArgs<P>& a, cudaStream_t st) {
 }
 
 template <class P>
-int sd_dispatch(const SdArgs<P>& a, int JL, int CH, bool tma, cudaStream_t st) {
+int sd_dispatch(const SdArgs<P>& a, int JL, int CH, int tma, cudaStream_t st) {
   if (tma && CH == 1) {
     if (JL == 4) return sd_launch_tma<P, 4>(a, st);
     if (JL == 2) return sd_launch_tma<P, 2>(a, st);
@@ -639,7 +644,7 @@ int sd_dispatch(const SdArgs<P>& a, int JL, int CH, bool tma, cudaStream_t st) {
 // multiplies by B's values and writes the result.
 template <class P>
 int sd_run(const tacogb_csr* B, int32_t J, const void* Cv, const void* Dv, void* outv,
-           int64_t out_ld, bool tma, cudaStream_t st) {
+           int64_t out_ld, int tma, cudaStream_t st) {
   using V = typename P::V;
   using DT = typename P::DT;
   const V* C = (const V*)Cv;
@@ -729,7 +734,9 @@ int sddmm_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, void
                    "SDDMM: null result");
   TACOGB_CHECK_ARG(B->vtype == TACOGB_F64 || B->vtype == TACOGB_F32,
                    "SDDMM: unsupported value type %d", B->vtype);
-  if (variant < 0) variant = 3;  // TMA-staged rows; FP64 in double-float on the FP32 pipe
+  // register form, FP64 in double-float on the FP32 pipe: measured fastest (1,048,576-row
+  // power-law B, J = 128: 5.69 ms against 8.08 TMA-staged and 10.2 native DFMA)
+  if (variant < 0) variant = 1;
   TACOGB_CHECK_ARG(variant < kNumSddmmVariants, "SDDMM: variant %d out of range", variant);
   const SddmmVariant& v = kSddmmVariants[variant];
   if (B->vtype == TACOGB_F32) return sd_run<Sd32>(B, J, C, D, out, out_ld, v.tma, st);

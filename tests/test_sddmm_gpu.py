@@ -226,3 +226,20 @@ def test_rejects_mismatched_shapes():
     Dt = T.dense(np.ascontiguousarray(D), [D.shape[0], K])
     At = T.dense_result([I, K])
     assert tg.lib().tacogb_sddmm_evaluate(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr) != 0
+
+
+def test_dropin_module_shim_compute():
+    """taco's sddmmGPU inputs through libtacogb_sddmm.so's _shim_compute (taco's packed-argument
+    entry: result, then B, C, D), into a dense result holding stale values."""
+    pos, crd, vals, C, D, A = fixture("sddmm_taco_gpu")
+    I, K = A.shape
+    J = C.shape[1]
+    L = ctypes.CDLL(os.path.join(os.path.dirname(tg.__file__), "lib", "libtacogb_sddmm.so"))
+    out = np.full((I, K), 7.0)
+    At = T.dense(out, [I, K])
+    Bt = T.csr(pos.astype(np.int32), crd.astype(np.int32), vals, [I, K])
+    Ct, Dt = T.dense(np.ascontiguousarray(C), [I, J]), T.dense(np.ascontiguousarray(D), [J, K])
+    args = (ctypes.c_void_p * 4)(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr)
+    L._shim_compute.argtypes = [ctypes.c_void_p]
+    assert L._shim_compute(args) == 0
+    assert np.array_equal(out, A)
