@@ -48,7 +48,7 @@ def parse(argv=None):
     p.add_argument("--workload", default="spmv_powerlaw",
                    choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
                             "spgemm_random", "spgemm_poisson", "batched_spmv", "batched_spmm",
-                            "gather_probe", "pack_powerlaw", "sddmm_powerlaw"])
+                            "gather_probe", "pack_powerlaw", "sddmm_powerlaw", "mttkrp_nell2"])
     p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
     p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
                    help="how batched_spmv picks each matrix's work-unit kind")
@@ -675,7 +675,95 @@ class SddmmOp:
             D.ctypes.data, out.ctypes.data), out
 
 
+class MttkrpOp:
+    """MTTKRP A(i,j) = B(i,k,l) * C(k,j) * D(l,j), B {Sparse,Sparse,Sparse} with nell-2's shape
+    (12,092 x 9,184 x 28,818) and 7.7e7 synthetic nonzeros (power-law fibers), rank J = 32,
+    FP64.  value = GFLOP/s on taco's 3 J flops per nonzero.  The roofline is on the fiber
+    SpMM's compulsory bytes (B's level-2 arrays, D once, T written), its dominant kernel.  The
+    CPU baseline is taco's own generated code for the statement on all host cores (the whole
+    tensor; A is only 12,092 x 32)."""
+    pattern = "mttkrp"
+    unit = "GFLOP/s"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        self.B = W.tensor3_powerlaw()
+        dims, crd0, pos1, crd1, pos2, crd2, vals = self.B
+        J = self.J = W.MTTKRP_J
+        self.C = W.dense(71, dims[1] * J).reshape(dims[1], J)
+        self.D = W.dense(72, dims[2] * J).reshape(dims[2], J)
+        self.rows, self.cols, self.nnz = dims[0], dims[2], len(crd2)
+        self.nfib = len(crd1)
+        e = 8 if args.dtype == "f64" else 4
+        self.roofline_bytes = (self.nnz * (4 + e) + 4 * (self.nfib + 1) + e * dims[2] * J
+                               + e * self.nfib * J)
+        self.bytes = (self.roofline_bytes + 4 * (dims[0] + 1) + 4 * self.nfib
+                      + e * self.nfib * J + e * dims[1] * J + e * dims[0] * J)
+        self.flops = self.work = 3 * J * self.nnz
+        self.metric = "mttkrp_%s_r%d_gflops" % (args.dtype, J)
+        self.workload = "mttkrp_nell2_%d_%d_%d_r%d" % (dims[0], dims[1], dims[2], J)
+
+    def _dtype(self, torch):
+        return torch.float64 if self.args.dtype == "f64" else torch.float32
+
+    def device(self, torch, tg):
+        dt = self._dtype(torch)
+        Bd = tg.CsfTensor.from_numpy(*self.B, dtype=dt)
+        Cd = torch.from_numpy(self.C).to("cuda", dt)
+        Dd = torch.from_numpy(self.D).to("cuda", dt)
+        A = torch.empty(self.rows, self.J, dtype=dt, device="cuda")
+        b = Bd.as_csf3()
+        L = tg.lib()
+        keep = (Bd, Cd, Dd, A, b)
+
+        def step(sp):
+            rc = L.tacogb_mttkrp(ctypes.byref(b), self.J, Cd.data_ptr(), Dd.data_ptr(),
+                                 A.data_ptr(), sp)
+            if rc:
+                raise RuntimeError(L.tacogb_last_error().decode())
+        return step, keep
+
+    def abi(self, torch, tg, T):
+        dt = self._dtype(torch)
+        dims, crd0, pos1, crd1, pos2, crd2, vals = self.B
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()  # noqa: E731
+        hb = [pin(a) for a in (crd0, pos1, crd1, pos2, crd2)]
+        hv = torch.from_numpy(vals).to(dt).pin_memory()
+        hC, hD = torch.from_numpy(self.C).to(dt).pin_memory(), torch.from_numpy(self.D).to(dt).pin_memory()
+        hA = torch.empty(self.rows, self.J, dtype=dt).pin_memory()
+        Bt = T.csf3(dims, *hb, hv)
+        Ct, Dt = T.dense(hC, list(self.C.shape)), T.dense(hD, list(self.D.shape))
+        At = T.dense(hA, [self.rows, self.J])
+        L = tg.lib()
+        keep = (hb, hv, hC, hD, hA, Bt, Ct, Dt, At)
+
+        def step():
+            tg.check(L.tacogb_mttkrp_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr),
+                     "tacogb_mttkrp_compute")
+        e = 8 if self.args.dtype == "f64" else 4
+        h2d = (4 * (len(crd0) + len(pos1) + len(crd1) + len(pos2) + len(crd2)) + e * self.nnz
+               + e * (self.C.size + self.D.size))
+        return (step, keep, h2d, e * self.rows * self.J,
+                "tacogb_mttkrp_compute(taco_tensor_t*) on pinned host arrays")
+
+    def cpu(self):
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        A = np.empty((self.rows, self.J))
+        if O.ref_available("mttkrp"):
+            L = O.ref_lib("mttkrp")
+            Bt = T.csf3(*self.B)
+            Ct, Dt = T.dense(self.C, list(self.C.shape)), T.dense(self.D, list(self.D.shape))
+            At = T.dense(A, [self.rows, self.J])
+            return ("reference", lambda: L.compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr),
+                    (Bt, Ct, Dt, At, A))
+        return "port", lambda: O.mttkrp(self.B, self.C, self.D), A
+
+
 def make_op(args):
+    if args.workload == "mttkrp_nell2":
+        return MttkrpOp(args)
     if args.workload == "sddmm_powerlaw":
         return SddmmOp(args)
     if args.workload.startswith("spgemm"):
@@ -1173,6 +1261,7 @@ def main():
     if rank == 0:
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
                    "sddmm": tg.sddmm_variants, "spgemm": lambda: ["default"],
+                   "mttkrp": lambda: ["default"],
                    "pack": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,

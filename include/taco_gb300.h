@@ -274,6 +274,41 @@ int tacogb_sddmm_dense(const tacogb_csr* B, int32_t J, const void* C, const void
 int tacogb_sddmm_variant_count(void);
 const char* tacogb_sddmm_variant_name(int32_t variant);
 
+/* An order-3 tensor in taco's {Sparse,Sparse,Sparse} or {Dense,Sparse,Sparse} storage (CSF),
+ * device pointers, int32 positions (taco's TensorStorage, src/storage/storage.cpp:127-177).
+ * Level 0: n0 entries with coordinates crd0 (NULL for a dense level: n0 == dims[0], entry e is
+ * i = e); level 1: pos1 (n0 + 1), crd1 (nfib = pos1[n0]), one entry per (i, j) fiber;
+ * level 2: pos2 (nfib + 1), crd2 and vals (nnz = pos2[nfib]). */
+typedef struct tacogb_csf3 {
+  int32_t dims[3];
+  int32_t n0;
+  int32_t nfib;
+  int64_t nnz;
+  const int32_t* crd0;
+  const int32_t* pos1;
+  const int32_t* crd1;
+  const int32_t* pos2;
+  const int32_t* crd2;
+  const void* vals;
+  int32_t vtype; /* TACOGB_F64 or TACOGB_F32; the dense operands and results share it */
+} tacogb_csf3;
+
+/* A(i,j) = B(i,j,k) * c(k) (taco: test/tests-scheduling-eval.cpp:993-1043, 1474-1524).
+ * tacogb_ttv writes one value per fiber (out[f] for fiber f = (i,j)); tacogb_ttv_dense taco's
+ * dense dims[0] x dims[1] result, zero where B has no fiber.  SpMV over the fibers. */
+int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, void* stream);
+int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, void* stream);
+/* A(i,j,l) = B(i,j,k) * C(k,l), C dims[2] x L row-major (taco: :1094-1146, 1420-1472).
+ * tacogb_ttm writes one row of L values per fiber (nfib x L); tacogb_ttm_dense the dense
+ * dims[0] x dims[1] x L result.  SpMM over the fibers. */
+int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, void* stream);
+int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, void* stream);
+/* A(i,j) = B(i,k,l) * C(k,j) * D(l,j), C dims[1] x J, D dims[2] x J, A dims[0] x J, all
+ * row-major (taco: :1148-1206, 1526-1580).  SpMM of the fibers with D, then per i the sum of
+ * C(k,:) times the fiber rows.  FP64 within 1e-12 normwise of taco's loop. */
+int tacogb_mttkrp(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
+                  void* stream);
+
 /* ------------------------------------------------------------------ taco kernel ABI ----- */
 
 /* y(i) = A(i,j) * x(j).  Replaces the generated assemble/compute/evaluate of that statement
@@ -317,6 +352,31 @@ int tacogb_sddmm_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, 
 int _shim_tacogb_sddmm_assemble(void** args);
 int _shim_tacogb_sddmm_compute(void** args);
 int _shim_tacogb_sddmm_evaluate(void** args);
+
+/* Order-3 statements with B {Sparse,Sparse,Sparse} or {Dense,Sparse,Sparse} and dense
+ * row-major operands and results (taco's test forms): A(i,j) = B(i,j,k) * c(k);
+ * A(i,j,l) = B(i,j,k) * C(k,l); A(i,j) = B(i,k,l) * C(k,j) * D(l,j).  assemble allocates A's
+ * values, compute fills them, evaluate does both. */
+int tacogb_ttv_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c);
+int tacogb_ttv_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c);
+int tacogb_ttv_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c);
+int _shim_tacogb_ttv_assemble(void** args);
+int _shim_tacogb_ttv_compute(void** args);
+int _shim_tacogb_ttv_evaluate(void** args);
+int tacogb_ttm_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C);
+int tacogb_ttm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C);
+int tacogb_ttm_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C);
+int _shim_tacogb_ttm_assemble(void** args);
+int _shim_tacogb_ttm_compute(void** args);
+int _shim_tacogb_ttm_evaluate(void** args);
+int tacogb_mttkrp_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C,
+                           taco_tensor_t* D);
+int tacogb_mttkrp_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D);
+int tacogb_mttkrp_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C,
+                           taco_tensor_t* D);
+int _shim_tacogb_mttkrp_assemble(void** args);
+int _shim_tacogb_mttkrp_compute(void** args);
+int _shim_tacogb_mttkrp_evaluate(void** args);
 
 #ifdef __cplusplus
 }

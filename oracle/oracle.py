@@ -59,6 +59,9 @@ def lib():
         L.oracle_free.argtypes = [P]
         L.oracle_sddmm_f64.argtypes = [I32, I32, I32, P, P, P, P, P, P]
         L.oracle_sddmm_sampled_f64.argtypes = [I32, I32, I32, P, P, P, P, P, P]
+        L.oracle_ttv_f64.argtypes = [I32, I32, I32] + [P] * 8
+        L.oracle_ttm_f64.argtypes = [I32, I32, I32, I32] + [P] * 8
+        L.oracle_mttkrp_f64.argtypes = [I32, I32, I32] + [P] * 9
         L.oracle_pack_csr.restype = I64
         L.oracle_pack_csr.argtypes = [I32, I32, I64, P, P, P, P, P, P]
         L.oracle_num_threads.restype = I32
@@ -142,6 +145,46 @@ def sddmm_sampled(pos, crd, vals, C, D):
     return out
 
 
+def _csf(B):
+    """(dims, crd0, pos1, crd1, pos2, crd2, vals) as contiguous arrays."""
+    dims, crd0, pos1, crd1, pos2, crd2, vals = B
+    ints = [np.ascontiguousarray(a, np.int32) for a in (crd0, pos1, crd1, pos2, crd2)]
+    return [int(d) for d in dims], ints, np.ascontiguousarray(vals, np.float64)
+
+
+def ttv(B, c):
+    """Dense I x J result of A(i,j) = B(i,j,k) * c(k); B = (dims, crd0, pos1, crd1, pos2,
+    crd2, vals), a {Sparse,Sparse,Sparse} tensor."""
+    dims, (crd0, pos1, crd1, pos2, crd2), vals = _csf(B)
+    c = np.ascontiguousarray(c, np.float64)
+    A = np.empty((dims[0], dims[1]))
+    lib().oracle_ttv_f64(dims[0], dims[1], len(crd0), _p(crd0), _p(pos1), _p(crd1), _p(pos2),
+                         _p(crd2), _p(vals), _p(c), _p(A))
+    return A
+
+
+def ttm(B, C):
+    """Dense I x J x L result of A(i,j,l) = B(i,j,k) * C(k,l)."""
+    dims, (crd0, pos1, crd1, pos2, crd2), vals = _csf(B)
+    C = np.ascontiguousarray(C, np.float64)
+    L = C.shape[1]
+    A = np.empty((dims[0], dims[1], L))
+    lib().oracle_ttm_f64(dims[0], dims[1], L, len(crd0), _p(crd0), _p(pos1), _p(crd1), _p(pos2),
+                         _p(crd2), _p(vals), _p(C), _p(A))
+    return A
+
+
+def mttkrp(B, C, D):
+    """Dense I x J result of A(i,j) = B(i,k,l) * C(k,j) * D(l,j)."""
+    dims, (crd0, pos1, crd1, pos2, crd2), vals = _csf(B)
+    C, D = np.ascontiguousarray(C, np.float64), np.ascontiguousarray(D, np.float64)
+    J = C.shape[1]
+    A = np.empty((dims[0], J))
+    lib().oracle_mttkrp_f64(dims[0], J, len(crd0), _p(crd0), _p(pos1), _p(crd1), _p(pos2),
+                            _p(crd2), _p(vals), _p(C), _p(D), _p(A))
+    return A
+
+
 def set_threads(n):
     lib().oracle_set_num_threads(n)
 
@@ -160,12 +203,12 @@ _ref = {}
 
 
 def ref_lib(pattern):
-    """taco's generated C for pattern (spmv, spmm, spgemm, sddmm) as compiled by Makefile.ref; exports
+    """taco's generated C for pattern (spmv, spmm, spgemm, sddmm, ttv, ttm, mttkrp) as compiled by Makefile.ref; exports
     taco's own assemble/compute/evaluate(taco_tensor_t*...)."""
     if pattern not in _ref:
         path = os.path.join(REF_DIR, "libtacoref_%s.so" % pattern)
         L = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
-        nargs = 4 if pattern == "sddmm" else 3
+        nargs = 4 if pattern in ("sddmm", "mttkrp") else 3
         for fn in ("assemble", "compute", "evaluate"):
             getattr(L, fn).argtypes = [P] * nargs
             getattr(L, fn).restype = ctypes.c_int

@@ -39,6 +39,12 @@
  *          i, for j, for p in row i: A[i*K+k] += (B[p]*C[i*J+j]) * D[j*K+k] (the statement of
  *          test/tests-scheduling-eval.cpp:783-840 and 1360-1417).
  *
+ *   TTV    A(i,j) = B(i,j,k) * c(k);  TTM  A(i,j,l) = B(i,j,k) * C(k,l);
+ *   MTTKRP A(i,j) = B(i,k,l) * C(k,j) * D(l,j);  B {Sparse,Sparse,Sparse}, the rest dense
+ *          generated `compute` of each (taco's CLI, -f=B:sss): zero A, then walk B's three
+ *          levels; TTV sums a fiber into a scalar and stores it; TTM adds B*C(k,:) into
+ *          A(i,j,:); MTTKRP adds (B*C(k,j))*D(l,j) over j for every nonzero.
+ *
  * Compiled with -O2 -fopenmp -ffp-contract=off: products and sums are rounded separately, in
  * the written order.
  */
@@ -249,6 +255,72 @@ void oracle_sddmm_sampled_f64(int32_t I, int32_t K, int32_t J, const int32_t* po
       const double c = C[(int64_t)i * J + j];
       const double* d = D + (int64_t)j * K;
       for (int32_t p = pos[i]; p < pos[i + 1]; p++) out[p] = out[p] + (bv[p] * c) * d[crd[p]];
+    }
+  }
+}
+
+/* Order-3 kernels over B in taco's {Sparse,Sparse,Sparse} format (CSF): level 0 holds the n0
+ * distinct i (crd0; taco's pos0 is {0, n0}); level 1 pos1 (n0 + 1) and crd1 (one entry per
+ * (i, j) fiber); level 2 pos2 (fibers + 1), crd2 and vals per nonzero.  Results are dense
+ * row-major, as in taco's tests (test/tests-scheduling-eval.cpp:993-1043 ttvCPU, 1094-1146
+ * ttmCPU, 1148-1206 mttkrpCPU; GPU forms :1420-1580).  Each function restates the loop taco's
+ * default lowering emits for the statement (taco's CLI, -f=B:sss, dense A, C, D, c). */
+
+/* A(i,j) = B(i,j,k) * c(k): per fiber a running sum over k, stored (not added) into A(i,j). */
+void oracle_ttv_f64(int32_t I, int32_t J, int32_t n0, const int32_t* crd0, const int32_t* pos1,
+                    const int32_t* crd1, const int32_t* pos2, const int32_t* crd2,
+                    const double* bv, const double* c, double* A) {
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < (int64_t)I * J; q++) A[q] = 0.0;
+#pragma omp parallel for schedule(static)
+  for (int32_t e = 0; e < n0; e++) {
+    const int32_t i = crd0[e];
+    for (int32_t f = pos1[e]; f < pos1[e + 1]; f++) {
+      double t = 0.0;
+      for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) t += bv[p] * c[crd2[p]];
+      A[(int64_t)i * J + crd1[f]] = t;
+    }
+  }
+}
+
+/* A(i,j,l) = B(i,j,k) * C(k,l): for each nonzero, the row C(k,:) scaled by B added into A(i,j,:). */
+void oracle_ttm_f64(int32_t I, int32_t J, int32_t L, int32_t n0, const int32_t* crd0,
+                    const int32_t* pos1, const int32_t* crd1, const int32_t* pos2,
+                    const int32_t* crd2, const double* bv, const double* C, double* A) {
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < (int64_t)I * J * L; q++) A[q] = 0.0;
+#pragma omp parallel for schedule(static)
+  for (int32_t e = 0; e < n0; e++) {
+    const int32_t i = crd0[e];
+    for (int32_t f = pos1[e]; f < pos1[e + 1]; f++) {
+      double* a = A + ((int64_t)i * J + crd1[f]) * L;
+      for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) {
+        const double b = bv[p];
+        const double* cr = C + (int64_t)crd2[p] * L;
+        for (int32_t l = 0; l < L; l++) a[l] = a[l] + b * cr[l];
+      }
+    }
+  }
+}
+
+/* A(i,j) = B(i,k,l) * C(k,j) * D(l,j): for each nonzero (i,k,l), for each j,
+ * A(i,j) += (B * C(k,j)) * D(l,j). */
+void oracle_mttkrp_f64(int32_t I, int32_t J, int32_t n0, const int32_t* crd0,
+                       const int32_t* pos1, const int32_t* crd1, const int32_t* pos2,
+                       const int32_t* crd2, const double* bv, const double* C, const double* D,
+                       double* A) {
+#pragma omp parallel for schedule(static)
+  for (int64_t q = 0; q < (int64_t)I * J; q++) A[q] = 0.0;
+#pragma omp parallel for schedule(static)
+  for (int32_t e = 0; e < n0; e++) {
+    double* a = A + (int64_t)crd0[e] * J;
+    for (int32_t f = pos1[e]; f < pos1[e + 1]; f++) {
+      const double* cr = C + (int64_t)crd1[f] * J;
+      for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) {
+        const double b = bv[p];
+        const double* dr = D + (int64_t)crd2[p] * J;
+        for (int32_t j = 0; j < J; j++) a[j] = a[j] + (b * cr[j]) * dr[j];
+      }
     }
   }
 }

@@ -11,7 +11,7 @@ from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBE
                       lib)
 
 __all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "spgemm", "pack_csr",
-           "sddmm", "sddmm_variants",
+           "sddmm", "sddmm_variants", "CsfTensor", "ttv", "ttm", "mttkrp",
            "read_coo", "read_csr",
            "SpmvBatch",
            "SpmmBatch",
@@ -57,6 +57,79 @@ class CsrMatrix:
         c.pos, c.crd, c.vals = self.pos.data_ptr(), self.crd.data_ptr(), self.vals.data_ptr()
         c.vtype = self.vtype
         return c
+
+
+class CsfTensor:
+    """An order-3 tensor in taco's {Sparse,Sparse,Sparse} storage on the GPU ({Dense,Sparse,Sparse}
+    when crd0 is None): int32 torch tensors crd0 (level-0 i), pos1/crd1 (one (i,j) fiber per
+    level-1 entry), pos2/crd2 and float64 or float32 vals."""
+
+    def __init__(self, dims, crd0, pos1, crd1, pos2, crd2, vals):
+        self.dims = tuple(int(d) for d in dims)
+        self.crd0, self.pos1, self.crd1 = crd0, pos1, crd1
+        self.pos2, self.crd2, self.vals = pos2, crd2, vals
+        self.n0 = self.dims[0] if crd0 is None else crd0.numel()
+        self.nfib = crd1.numel()
+        self.nnz = crd2.numel()
+        self.vtype = _VTYPE[vals.element_size()]
+
+    @classmethod
+    def from_numpy(cls, dims, crd0, pos1, crd1, pos2, crd2, vals, device="cuda", dtype=None,
+                   dense0=False):
+        import torch
+        t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
+        v = torch.from_numpy(vals)
+        if dtype is not None:
+            v = v.to(dtype)
+        return cls(dims, None if dense0 else t(crd0), t(pos1), t(crd1), t(pos2), t(crd2),
+                   v.to(device))
+
+    def as_csf3(self):
+        c = _native.Csf3()
+        for m in range(3):
+            c.dims[m] = self.dims[m]
+        c.n0, c.nfib, c.nnz = self.n0, self.nfib, self.nnz
+        c.crd0 = None if self.crd0 is None else self.crd0.data_ptr()
+        c.pos1, c.crd1 = self.pos1.data_ptr(), self.crd1.data_ptr()
+        c.pos2, c.crd2, c.vals = self.pos2.data_ptr(), self.crd2.data_ptr(), self.vals.data_ptr()
+        c.vtype = self.vtype
+        return c
+
+
+def ttv(B, c, dense=False, stream=None):
+    """A(i,j) = B(i,j,k) * c(k): one value per (i,j) fiber of B (tacogb_ttv) or, with dense=True,
+    taco's dense dims[0] x dims[1] result (tacogb_ttv_dense)."""
+    import torch
+    b = B.as_csf3()
+    shape = (B.dims[0], B.dims[1]) if dense else (B.nfib,)
+    out = torch.empty(shape, dtype=B.vals.dtype, device=B.vals.device)
+    fn = lib().tacogb_ttv_dense if dense else lib().tacogb_ttv
+    check(fn(ctypes.byref(b), c.data_ptr(), out.data_ptr(), _stream_ptr(stream)), "tacogb_ttv")
+    return out
+
+
+def ttm(B, C, dense=False, stream=None):
+    """A(i,j,l) = B(i,j,k) * C(k,l): one row of L values per (i,j) fiber (tacogb_ttm) or taco's
+    dense dims[0] x dims[1] x L result (tacogb_ttm_dense)."""
+    import torch
+    L = C.shape[1]
+    b = B.as_csf3()
+    shape = (B.dims[0], B.dims[1], L) if dense else (B.nfib, L)
+    out = torch.empty(shape, dtype=B.vals.dtype, device=B.vals.device)
+    fn = lib().tacogb_ttm_dense if dense else lib().tacogb_ttm
+    check(fn(ctypes.byref(b), L, C.data_ptr(), out.data_ptr(), _stream_ptr(stream)), "tacogb_ttm")
+    return out
+
+
+def mttkrp(B, C, D, stream=None):
+    """A(i,j) = B(i,k,l) * C(k,j) * D(l,j): dense dims[0] x J result (tacogb_mttkrp)."""
+    import torch
+    J = C.shape[1]
+    b = B.as_csf3()
+    out = torch.empty(B.dims[0], J, dtype=B.vals.dtype, device=B.vals.device)
+    check(lib().tacogb_mttkrp(ctypes.byref(b), J, C.data_ptr(), D.data_ptr(), out.data_ptr(),
+                              _stream_ptr(stream)), "tacogb_mttkrp")
+    return out
 
 
 def spmv(A, x, y=None, variant=VARIANT_AUTO, stream=None):

@@ -29,6 +29,23 @@ class TacoTensor(ctypes.Structure):
     ]
 
 
+class Csf3(ctypes.Structure):
+    """tacogb_csf3: an order-3 {Sparse|Dense,Sparse,Sparse} tensor in device memory."""
+    _fields_ = [
+        ("dims", ctypes.c_int32 * 3),
+        ("n0", ctypes.c_int32),
+        ("nfib", ctypes.c_int32),
+        ("nnz", ctypes.c_int64),
+        ("crd0", ctypes.c_void_p),
+        ("pos1", ctypes.c_void_p),
+        ("crd1", ctypes.c_void_p),
+        ("pos2", ctypes.c_void_p),
+        ("crd2", ctypes.c_void_p),
+        ("vals", ctypes.c_void_p),
+        ("vtype", ctypes.c_int32),
+    ]
+
+
 class Csr(ctypes.Structure):
     """tacogb_csr: a CSR matrix in device memory."""
     _fields_ = [
@@ -110,6 +127,29 @@ SIGNATURES = {
     "_shim_tacogb_sddmm_assemble": (I32, [P]),
     "_shim_tacogb_sddmm_compute": (I32, [P]),
     "_shim_tacogb_sddmm_evaluate": (I32, [P]),
+    "tacogb_ttv": (I32, [ctypes.POINTER(Csf3), P, P, P]),
+    "tacogb_ttv_dense": (I32, [ctypes.POINTER(Csf3), P, P, P]),
+    "tacogb_ttm": (I32, [ctypes.POINTER(Csf3), I32, P, P, P]),
+    "tacogb_ttm_dense": (I32, [ctypes.POINTER(Csf3), I32, P, P, P]),
+    "tacogb_mttkrp": (I32, [ctypes.POINTER(Csf3), I32, P, P, P, P]),
+    "tacogb_ttv_assemble": (I32, [P, P, P]),
+    "tacogb_ttv_compute": (I32, [P, P, P]),
+    "tacogb_ttv_evaluate": (I32, [P, P, P]),
+    "tacogb_ttm_assemble": (I32, [P, P, P]),
+    "tacogb_ttm_compute": (I32, [P, P, P]),
+    "tacogb_ttm_evaluate": (I32, [P, P, P]),
+    "tacogb_mttkrp_assemble": (I32, [P, P, P, P]),
+    "tacogb_mttkrp_compute": (I32, [P, P, P, P]),
+    "tacogb_mttkrp_evaluate": (I32, [P, P, P, P]),
+    "_shim_tacogb_ttv_assemble": (I32, [P]),
+    "_shim_tacogb_ttv_compute": (I32, [P]),
+    "_shim_tacogb_ttv_evaluate": (I32, [P]),
+    "_shim_tacogb_ttm_assemble": (I32, [P]),
+    "_shim_tacogb_ttm_compute": (I32, [P]),
+    "_shim_tacogb_ttm_evaluate": (I32, [P]),
+    "_shim_tacogb_mttkrp_assemble": (I32, [P]),
+    "_shim_tacogb_mttkrp_compute": (I32, [P]),
+    "_shim_tacogb_mttkrp_evaluate": (I32, [P]),
     "tacogb_spmm_variant_count": (I32, []),
     "tacogb_spmm_variant_name": (ctypes.c_char_p, [I32]),
     "tacogb_spmm_assemble": (I32, [P, P, P]),

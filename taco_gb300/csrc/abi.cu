@@ -84,7 +84,7 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 7;  // spmv, spmm, spgemm x2, tuner, pack, sddmm
+constexpr int kScratchSlots = 8;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3
 
 struct DeviceState {
   int sms = 0;
@@ -867,5 +867,273 @@ int _shim_tacogb_sddmm_evaluate(void** a) {
   return tacogb_sddmm_evaluate((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2],
                                (taco_tensor_t*)a[3]);
 }
+
+// ------------------------------------------------------------------ order-3 ---------------
+//
+// TTV, TTM and MTTKRP over B {Sparse,Sparse,Sparse} or {Dense,Sparse,Sparse}
+// (test/tests-scheduling-eval.cpp:993-1206, 1420-1580), dense results.
+
+int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, void* stream) {
+  return ttv_run(B, c, out, false, (cudaStream_t)stream);
+}
+int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, void* stream) {
+  return ttv_run(B, c, A, true, (cudaStream_t)stream);
+}
+int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, void* stream) {
+  return ttm_run(B, L, C, out, false, (cudaStream_t)stream);
+}
+int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, void* stream) {
+  return ttm_run(B, L, C, A, true, (cudaStream_t)stream);
+}
+int tacogb_mttkrp(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
+                  void* stream) {
+  return mttkrp_run(B, J, C, D, A, (cudaStream_t)stream);
+}
+
+extern "C++" {  // the helpers below include a template
+namespace {
+
+int check_dense_order(const taco_tensor_t* t, int order, const char* name) {
+  TACOGB_CHECK_ARG(t != nullptr, "%s: null tensor", name);
+  TACOGB_CHECK_ARG(t->order == order, "%s: expected order %d, got %d", name, order, t->order);
+  TACOGB_CHECK_ARG(t->dimensions != nullptr, "%s: null dimensions", name);
+  for (int m = 0; m < order; m++) {
+    TACOGB_CHECK_ARG(t->mode_types == nullptr || t->mode_types[m] == taco_mode_dense,
+                     "%s: expected every mode dense", name);
+    TACOGB_CHECK_ARG(t->mode_ordering == nullptr || t->mode_ordering[m] == m,
+                     "%s: expected row-major mode ordering", name);
+  }
+  return 0;
+}
+
+// B's arrays as a tacogb_csf3 on the device (host arrays staged in slots base .. base+6).
+int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3& out) {
+  TACOGB_CHECK_ARG(T != nullptr && T->order == 3 && T->dimensions && T->mode_types && T->indices,
+                   "order-3 operand B: expected an order-3 tensor");
+  const bool dense0 = T->mode_types[0] == taco_mode_dense;
+  TACOGB_CHECK_ARG((dense0 || T->mode_types[0] == taco_mode_sparse) &&
+                       T->mode_types[1] == taco_mode_sparse && T->mode_types[2] == taco_mode_sparse,
+                   "operand B: expected {Sparse,Sparse,Sparse} or {Dense,Sparse,Sparse}");
+  for (int m = 0; m < 3; m++)
+    TACOGB_CHECK_ARG(T->mode_ordering == nullptr || T->mode_ordering[m] == m,
+                     "operand B: expected mode ordering (0, 1, 2)");
+  TACOGB_CHECK_ARG(T->indices[1] && T->indices[2] && (dense0 || T->indices[0]),
+                   "operand B: missing indices");
+  const int vt = value_type_of_csize(T->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "operand B: unsupported csize %d",
+                   T->csize);
+  tacogb_csf3 b{};
+  for (int m = 0; m < 3; m++) b.dims[m] = T->dimensions[m];
+  b.vtype = vt;
+  const int32_t* crd0 = nullptr;
+  if (dense0) {
+    b.n0 = b.dims[0];
+  } else {
+    const int32_t* pos0 = (const int32_t*)T->indices[0][0];
+    TACOGB_CHECK_ARG(pos0 != nullptr, "operand B: null level-0 pos");
+    int32_t p0 = 0;
+    if (int rc = read_i32(pos0, &p0)) return rc;
+    if (int rc = read_i32(pos0 + 1, &b.n0)) return rc;
+    TACOGB_CHECK_ARG(p0 == 0 && b.n0 >= 0, "operand B: level-0 pos must be {0, n}");
+    crd0 = (const int32_t*)T->indices[0][1];
+  }
+  const int32_t* pos1 = (const int32_t*)T->indices[1][0];
+  const int32_t* crd1 = (const int32_t*)T->indices[1][1];
+  const int32_t* pos2 = (const int32_t*)T->indices[2][0];
+  const int32_t* crd2 = (const int32_t*)T->indices[2][1];
+  TACOGB_CHECK_ARG(pos1 != nullptr && pos2 != nullptr, "operand B: null pos");
+  if (int rc = read_i32(pos1 + b.n0, &b.nfib)) return rc;
+  int32_t nnz = 0;
+  if (int rc = read_i32(pos2 + b.nfib, &nnz)) return rc;
+  b.nnz = nnz;
+  Operand o0, op1, oc1, op2, oc2, ov;
+  if (crd0) {
+    if (int rc = stage_in(o0, crd0, (size_t)b.n0 * 4, base, st)) return rc;
+    b.crd0 = (const int32_t*)o0.dev;
+  }
+  if (int rc = stage_in(op1, pos1, ((size_t)b.n0 + 1) * 4, base + 1, st)) return rc;
+  if (int rc = stage_in(oc1, crd1, (size_t)b.nfib * 4, base + 2, st)) return rc;
+  if (int rc = stage_in(op2, pos2, ((size_t)b.nfib + 1) * 4, base + 3, st)) return rc;
+  if (int rc = stage_in(oc2, crd2, (size_t)b.nnz * 4, base + 4, st)) return rc;
+  if (int rc = stage_in(ov, T->vals, (size_t)b.nnz * value_bytes(vt), base + 5, st)) return rc;
+  b.pos1 = (const int32_t*)op1.dev;
+  b.crd1 = (const int32_t*)oc1.dev;
+  b.pos2 = (const int32_t*)op2.dev;
+  b.crd2 = (const int32_t*)oc2.dev;
+  b.vals = ov.dev;
+  out = b;
+  return 0;
+}
+
+// The shared body of the three compute entry points: B and the dense operands staged, the
+// result written in place (device-accessible) or through a staging buffer.
+template <class Run>
+int t3_compute(taco_tensor_t* A, taco_tensor_t* B, size_t abytes, int nops,
+               taco_tensor_t* const* ops, const size_t* op_bytes, Run run) {
+  TACOGB_CHECK_ARG(A->vals != nullptr || abytes == 0, "result values not assembled");
+  cudaStream_t st = lib_stream();
+  tacogb_csf3 b;
+  if (int rc = csf3_operand(B, 30, st, b)) return rc;
+  const void* dev[2] = {nullptr, nullptr};
+  Operand o[2];
+  for (int q = 0; q < nops; q++) {
+    if (int rc = stage_in(o[q], ops[q]->vals, op_bytes[q], 37 + q, st)) return rc;
+    dev[q] = o[q].dev;
+  }
+  void* adev = A->vals;
+  const bool staged = !device_accessible(A->vals);
+  if (staged) {
+    adev = stage_buffer(39, abytes);
+    if (!adev) return TACOGB_ERR_ALLOC;
+  }
+  if (int rc = run(b, dev, adev, st)) return rc;
+  if (staged && abytes)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(A->vals, adev, abytes, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return consume_device_status();
+}
+
+int t3_assemble(taco_tensor_t* A, taco_tensor_t* B, size_t elems) {
+  const int vt = value_type_of_csize(A->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "result: unsupported csize %d", A->csize);
+  const bool managed = B->vals != nullptr && device_accessible(B->vals);
+  void* p = alloc_result(elems * value_bytes(vt), managed);
+  if (!p) return TACOGB_ERR_ALLOC;
+  A->vals = (uint8_t*)p;
+  return 0;
+}
+
+int check_same_csize(const taco_tensor_t* A, const taco_tensor_t* B, const taco_tensor_t* C,
+                     const taco_tensor_t* D) {
+  TACOGB_CHECK_ARG(A->csize == B->csize && C->csize == B->csize && (!D || D->csize == B->csize),
+                   "operand component sizes differ");
+  return 0;
+}
+
+int check_ttv(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c) {
+  if (int rc = check_dense_order(A, 2, "ttv result A")) return rc;
+  if (int rc = check_dense_order(c, 1, "ttv operand c")) return rc;
+  TACOGB_CHECK_ARG(B != nullptr && B->order == 3 && B->dimensions, "ttv: B must be order 3");
+  TACOGB_CHECK_ARG(A->dimensions[0] == B->dimensions[0] && A->dimensions[1] == B->dimensions[1],
+                   "ttv: A is %dx%d, B is %dx%dx%d", A->dimensions[0], A->dimensions[1],
+                   B->dimensions[0], B->dimensions[1], B->dimensions[2]);
+  TACOGB_CHECK_ARG(c->dimensions[0] == B->dimensions[2], "ttv: c has %d entries, B's k is %d",
+                   c->dimensions[0], B->dimensions[2]);
+  return check_same_csize(A, B, c, nullptr);
+}
+
+int check_ttm(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C) {
+  if (int rc = check_dense_order(A, 3, "ttm result A")) return rc;
+  if (int rc = check_dense_order(C, 2, "ttm operand C")) return rc;
+  TACOGB_CHECK_ARG(B != nullptr && B->order == 3 && B->dimensions, "ttm: B must be order 3");
+  TACOGB_CHECK_ARG(A->dimensions[0] == B->dimensions[0] && A->dimensions[1] == B->dimensions[1] &&
+                       A->dimensions[2] == C->dimensions[1],
+                   "ttm: A's shape does not match B and C");
+  TACOGB_CHECK_ARG(C->dimensions[0] == B->dimensions[2], "ttm: C has %d rows, B's k is %d",
+                   C->dimensions[0], B->dimensions[2]);
+  return check_same_csize(A, B, C, nullptr);
+}
+
+int check_mttkrp(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D) {
+  if (int rc = check_dense_order(A, 2, "mttkrp result A")) return rc;
+  if (int rc = check_dense_order(C, 2, "mttkrp operand C")) return rc;
+  if (int rc = check_dense_order(D, 2, "mttkrp operand D")) return rc;
+  TACOGB_CHECK_ARG(B != nullptr && B->order == 3 && B->dimensions, "mttkrp: B must be order 3");
+  const int32_t J = A->dimensions[1];
+  TACOGB_CHECK_ARG(A->dimensions[0] == B->dimensions[0], "mttkrp: A has %d rows, B's i is %d",
+                   A->dimensions[0], B->dimensions[0]);
+  TACOGB_CHECK_ARG(C->dimensions[0] == B->dimensions[1] && C->dimensions[1] == J,
+                   "mttkrp: C must be %d x %d", B->dimensions[1], J);
+  TACOGB_CHECK_ARG(D->dimensions[0] == B->dimensions[2] && D->dimensions[1] == J,
+                   "mttkrp: D must be %d x %d", B->dimensions[2], J);
+  return check_same_csize(A, B, C, D);
+}
+
+size_t vbytes_of(const taco_tensor_t* t) { return value_bytes(value_type_of_csize(t->csize)); }
+
+}  // namespace
+}  // extern "C++"
+
+int tacogb_ttv_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c) {
+  if (int rc = check_ttv(A, B, c)) return rc;
+  return t3_assemble(A, B, (size_t)A->dimensions[0] * A->dimensions[1]);
+}
+int tacogb_ttv_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c) {
+  if (int rc = check_ttv(A, B, c)) return rc;
+  const size_t vb = vbytes_of(B);
+  taco_tensor_t* ops[1] = {c};
+  const size_t ob[1] = {(size_t)c->dimensions[0] * vb};
+  return t3_compute(A, B, (size_t)A->dimensions[0] * A->dimensions[1] * vb, 1, ops, ob,
+                    [](const tacogb_csf3& b, const void* const* d, void* a, cudaStream_t st) {
+                      return ttv_run(&b, d[0], a, true, st);
+                    });
+}
+int tacogb_ttv_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c) {
+  if (int rc = tacogb_ttv_assemble(A, B, c)) return rc;
+  return tacogb_ttv_compute(A, B, c);
+}
+
+int tacogb_ttm_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C) {
+  if (int rc = check_ttm(A, B, C)) return rc;
+  return t3_assemble(A, B, (size_t)A->dimensions[0] * A->dimensions[1] * A->dimensions[2]);
+}
+int tacogb_ttm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C) {
+  if (int rc = check_ttm(A, B, C)) return rc;
+  const size_t vb = vbytes_of(B);
+  const int32_t L = C->dimensions[1];
+  taco_tensor_t* ops[1] = {C};
+  const size_t ob[1] = {(size_t)C->dimensions[0] * L * vb};
+  return t3_compute(A, B, (size_t)A->dimensions[0] * A->dimensions[1] * L * vb, 1, ops, ob,
+                    [L](const tacogb_csf3& b, const void* const* d, void* a, cudaStream_t st) {
+                      return ttm_run(&b, L, d[0], a, true, st);
+                    });
+}
+int tacogb_ttm_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C) {
+  if (int rc = tacogb_ttm_assemble(A, B, C)) return rc;
+  return tacogb_ttm_compute(A, B, C);
+}
+
+int tacogb_mttkrp_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C,
+                           taco_tensor_t* D) {
+  if (int rc = check_mttkrp(A, B, C, D)) return rc;
+  return t3_assemble(A, B, (size_t)A->dimensions[0] * A->dimensions[1]);
+}
+int tacogb_mttkrp_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D) {
+  if (int rc = check_mttkrp(A, B, C, D)) return rc;
+  const size_t vb = vbytes_of(B);
+  const int32_t J = A->dimensions[1];
+  taco_tensor_t* ops[2] = {C, D};
+  const size_t ob[2] = {(size_t)C->dimensions[0] * J * vb, (size_t)D->dimensions[0] * J * vb};
+  return t3_compute(A, B, (size_t)A->dimensions[0] * J * vb, 2, ops, ob,
+                    [J](const tacogb_csf3& b, const void* const* d, void* a, cudaStream_t st) {
+                      return mttkrp_run(&b, J, d[0], d[1], a, st);
+                    });
+}
+int tacogb_mttkrp_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C,
+                           taco_tensor_t* D) {
+  if (int rc = tacogb_mttkrp_assemble(A, B, C, D)) return rc;
+  return tacogb_mttkrp_compute(A, B, C, D);
+}
+
+#define TACOGB_SHIM3(name)                                                                \
+  int _shim_tacogb_##name(void** a) {                                                     \
+    return tacogb_##name((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2]); \
+  }
+#define TACOGB_SHIM4(name)                                                                \
+  int _shim_tacogb_##name(void** a) {                                                     \
+    return tacogb_##name((taco_tensor_t*)a[0], (taco_tensor_t*)a[1], (taco_tensor_t*)a[2], \
+                         (taco_tensor_t*)a[3]);                                           \
+  }
+TACOGB_SHIM3(ttv_assemble)
+TACOGB_SHIM3(ttv_compute)
+TACOGB_SHIM3(ttv_evaluate)
+TACOGB_SHIM3(ttm_assemble)
+TACOGB_SHIM3(ttm_compute)
+TACOGB_SHIM3(ttm_evaluate)
+TACOGB_SHIM4(mttkrp_assemble)
+TACOGB_SHIM4(mttkrp_compute)
+TACOGB_SHIM4(mttkrp_evaluate)
+#undef TACOGB_SHIM3
+#undef TACOGB_SHIM4
 
 }  // extern "C"

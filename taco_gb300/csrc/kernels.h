@@ -38,6 +38,13 @@ const char* sddmm_variant_name(int v);
 int sddmm_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, void* out,
               int64_t out_ld, int variant, cudaStream_t st);
 
+// Order-3 kernels (tensor3.cu); dense selects taco's dense result form.
+int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStream_t st);
+int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense,
+            cudaStream_t st);
+int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
+               cudaStream_t st);
+
 // COO -> CSR pack (pack.cu): device arrays in and out; *nnz read back (synchronises).
 int pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_rows,
              const int32_t* coord_cols, const void* vals, int32_t vtype, int32_t* pos,

@@ -8,9 +8,9 @@
 #include "taco_gb300.h"
 
 #ifndef TACOGB_PATTERN
-#error "define TACOGB_PATTERN (spmv, spmm, spgemm or sddmm)"
+#error "define TACOGB_PATTERN (spmv, spmm, spgemm, sddmm, ttv, ttm or mttkrp)"
 #endif
-/* tensors per call: 3 (result and two operands), 4 for sddmm (A, B, C, D) */
+/* tensors per call: 3 (result and two operands), 4 for sddmm and mttkrp (A, B, C, D) */
 #ifndef TACOGB_NARGS
 #define TACOGB_NARGS 3
 #endif

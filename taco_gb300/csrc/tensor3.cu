@@ -1,0 +1,227 @@
+// Order-3 kernels over a CSF tensor B ({Sparse,Sparse,Sparse} or {Dense,Sparse,Sparse}):
+//   TTV     A(i,j)   = B(i,j,k) * c(k)
+//   TTM     A(i,j,l) = B(i,j,k) * C(k,l)
+//   MTTKRP  A(i,j)   = B(i,k,l) * C(k,j) * D(l,j)
+// taco's statements and schedules: test/tests-scheduling-eval.cpp:993-1206 (CPU), 1420-1580
+// (GPU, scheduleTTVGPU / scheduleTTMGPU / scheduleMTTKRPGPU at :288-343).
+//
+// B's last level is a CSR matrix whose rows are B's fibers: pos2 over nfib fibers, crd2 the
+// last coordinate.  So TTV is SpMV and TTM is SpMM over that fiber matrix (the library's
+// merge-tile kernels, load-balanced over nonzeros however long the fibers are), each giving
+// one value or one dense row per (i,j) fiber; dense results (taco's test form) are zero-filled
+// and the fiber results scattered to (i, j).  MTTKRP factors the sum over l inside the sum over
+// k: T(f,:) = sum_l B(i,k,l) D(l,:) per level-1 fiber f = (i,k) (SpMM over the fiber matrix),
+// then A(i,:) = sum_f C(k_f,:) * T(f,:) over the fibers of i (t3_mttkrp_combine): 2J flops per
+// nonzero plus 2J per fiber, where taco's loop spends 3J per nonzero.
+#include <cstdint>
+#include <cstring>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace tacogb {
+
+namespace {
+
+// dest[f] = i_f * dims1 + j_f for every fiber f: its level-0 entry e by a binary search over
+// pos1 (the last e with pos1[e] <= f), i = crd0[e] (or e itself for a dense level 0).
+__global__ void t3_fiber_dest(const int32_t* __restrict__ pos1, const int32_t* __restrict__ crd0,
+                              const int32_t* __restrict__ crd1, int32_t n0, int32_t nfib,
+                              int32_t dims1, int64_t* __restrict__ dest) {
+  const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nfib) return;
+  int lo = 0, hi = n0 - 1;  // pos1[0] = 0 <= f < pos1[n0]
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(pos1 + mid) <= f)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int64_t i = crd0 ? __ldg(crd0 + lo) : lo;
+  dest[f] = i * dims1 + __ldg(crd1 + f);
+}
+
+template <class V>
+__global__ void t3_scatter_vals(const int64_t* __restrict__ dest, const V* __restrict__ y,
+                                int32_t nfib, V* __restrict__ A) {
+  const int32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f < nfib) A[dest[f]] = y[f];
+}
+
+// A[dest[f] * L + l] = Y[f * L + l]: one thread per element, rows copied whole by consecutive
+// threads.
+template <class V>
+__global__ void t3_scatter_rows(const int64_t* __restrict__ dest, const V* __restrict__ Y,
+                                int32_t nfib, int32_t L, V* __restrict__ A) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)nfib * L) return;
+  const int64_t f = idx / L;
+  const int32_t l = (int32_t)(idx - f * L);
+  A[dest[f] * L + l] = Y[idx];
+}
+
+// A(i,:) = sum over the fibers f of level-0 entry e (i = crd0[e] or e) of C(crd1[f],:) * T(f,:):
+// one warp per entry, lanes over j, fibers in order.
+template <class V>
+__global__ void t3_mttkrp_combine(const int32_t* __restrict__ pos1,
+                                  const int32_t* __restrict__ crd0,
+                                  const int32_t* __restrict__ crd1, int32_t n0, int32_t J,
+                                  const V* __restrict__ C, const V* __restrict__ T,
+                                  V* __restrict__ A) {
+  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (e >= n0) return;
+  const int32_t f0 = __ldg(pos1 + e), f1 = __ldg(pos1 + e + 1);
+  const int64_t i = crd0 ? __ldg(crd0 + e) : e;
+  for (int32_t j0 = 0; j0 < J; j0 += 32) {
+    const int32_t j = j0 + lane;
+    V acc = V(0);
+    if (j < J) {
+      for (int32_t f = f0; f < f1; f++) {
+        const int32_t k = __ldg(crd1 + f);
+        acc = fma(__ldg(C + (int64_t)k * J + j), __ldg(T + (int64_t)f * J + j), acc);
+      }
+      A[i * J + j] = acc;
+    }
+  }
+}
+
+int check_csf3(const tacogb_csf3* B, const char* what) {
+  TACOGB_CHECK_ARG(B != nullptr, "%s: null tensor", what);
+  TACOGB_CHECK_ARG(B->dims[0] >= 0 && B->dims[1] >= 0 && B->dims[2] >= 0 && B->n0 >= 0 &&
+                       B->nfib >= 0 && B->nnz >= 0,
+                   "%s: negative size", what);
+  TACOGB_CHECK_ARG(B->nnz <= INT32_MAX, "%s: nnz exceeds int32 positions", what);
+  TACOGB_CHECK_ARG(B->crd0 != nullptr || B->n0 == B->dims[0] || B->n0 == 0,
+                   "%s: a dense first level has dims[0] entries", what);
+  TACOGB_CHECK_ARG(B->n0 == 0 || (B->pos1 != nullptr), "%s: null pos1", what);
+  TACOGB_CHECK_ARG(B->nfib == 0 || (B->crd1 != nullptr && B->pos2 != nullptr),
+                   "%s: null level-1 crd or level-2 pos", what);
+  TACOGB_CHECK_ARG(B->nnz == 0 || (B->crd2 != nullptr && B->vals != nullptr),
+                   "%s: null level-2 crd or values", what);
+  TACOGB_CHECK_ARG(B->vtype == TACOGB_F64 || B->vtype == TACOGB_F32,
+                   "%s: unsupported value type %d", what, B->vtype);
+  return 0;
+}
+
+size_t vsize(int vt) { return vt == TACOGB_F64 ? 8 : 4; }
+
+// The fiber matrix: rows are B's (i,j) fibers, columns B's last coordinate.
+tacogb_csr fiber_csr(const tacogb_csf3* B) {
+  return tacogb_csr{B->nfib, B->dims[2], B->nnz, B->pos2, B->crd2, B->vals, B->vtype};
+}
+
+// dest of every fiber, written at ws (nfib int64 values).
+int fiber_dest(const tacogb_csf3* B, unsigned char* ws, cudaStream_t st, int64_t*& dest) {
+  dest = reinterpret_cast<int64_t*>(ws);
+  if (B->nfib == 0) return 0;
+  TACOGB_LAUNCH("t3_fiber_dest", st,
+                (t3_fiber_dest<<<(unsigned)((B->nfib + 255) / 256), 256, 0, st>>>(
+                    B->pos1, B->crd0, B->crd1, B->n0, B->nfib, B->dims[1], dest)));
+  return 0;
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStream_t st) {
+  if (int rc = check_csf3(B, "TTV")) return rc;
+  const size_t vb = vsize(B->vtype);
+  TACOGB_CHECK_ARG(B->nnz == 0 || c != nullptr, "TTV: null c");
+  if (dense) {
+    const size_t abytes = (size_t)B->dims[0] * (size_t)B->dims[1] * vb;
+    TACOGB_CHECK_ARG(abytes == 0 || out != nullptr, "TTV: null result");
+    if (abytes) TACOGB_CUDA_TRY(cudaMemsetAsync(out, 0, abytes, st));
+    if (B->nfib == 0) return 0;
+    unsigned char* ws = (unsigned char*)scratch(
+        align256((size_t)B->nfib * 8) + align256((size_t)B->nfib * vb), 7);
+    if (!ws) return last_code();
+    int64_t* dest;
+    if (int rc = fiber_dest(B, ws, st, dest)) return rc;
+    void* y = ws + align256((size_t)B->nfib * 8);
+    const tacogb_csr f = fiber_csr(B);
+    if (int rc = spmv_run(&f, c, y, TACOGB_VARIANT_AUTO, st)) return rc;
+    if (B->vtype == TACOGB_F64)
+      TACOGB_LAUNCH("t3_scatter_vals", st,
+                    (t3_scatter_vals<double><<<(unsigned)((B->nfib + 255) / 256), 256, 0, st>>>(
+                        dest, (const double*)y, B->nfib, (double*)out)));
+    else
+      TACOGB_LAUNCH("t3_scatter_vals", st,
+                    (t3_scatter_vals<float><<<(unsigned)((B->nfib + 255) / 256), 256, 0, st>>>(
+                        dest, (const float*)y, B->nfib, (float*)out)));
+    return 0;
+  }
+  TACOGB_CHECK_ARG(B->nfib == 0 || out != nullptr, "TTV: null result");
+  if (B->nfib == 0) return 0;
+  const tacogb_csr f = fiber_csr(B);
+  return spmv_run(&f, c, out, TACOGB_VARIANT_AUTO, st);
+}
+
+int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense,
+            cudaStream_t st) {
+  if (int rc = check_csf3(B, "TTM")) return rc;
+  TACOGB_CHECK_ARG(L >= 0, "TTM: negative L");
+  TACOGB_CHECK_ARG(B->nnz == 0 || L == 0 || C != nullptr, "TTM: null C");
+  const size_t vb = vsize(B->vtype);
+  if (!dense) {
+    TACOGB_CHECK_ARG((int64_t)B->nfib * L == 0 || out != nullptr, "TTM: null result");
+    if ((int64_t)B->nfib * L == 0) return 0;
+    const tacogb_csr f = fiber_csr(B);
+    return spmm_run(&f, L, C, B->vtype, out, TACOGB_VARIANT_AUTO, st);
+  }
+  const size_t abytes = (size_t)B->dims[0] * (size_t)B->dims[1] * (size_t)L * vb;
+  TACOGB_CHECK_ARG(abytes == 0 || out != nullptr, "TTM: null result");
+  if (abytes) TACOGB_CUDA_TRY(cudaMemsetAsync(out, 0, abytes, st));
+  if ((int64_t)B->nfib * L == 0) return 0;
+  unsigned char* ws = (unsigned char*)scratch(
+      align256((size_t)B->nfib * 8) + align256((size_t)B->nfib * L * vb), 7);
+  if (!ws) return last_code();
+  int64_t* dest;
+  if (int rc = fiber_dest(B, ws, st, dest)) return rc;
+  void* Y = ws + align256((size_t)B->nfib * 8);
+  const tacogb_csr f = fiber_csr(B);
+  if (int rc = spmm_run(&f, L, C, B->vtype, Y, TACOGB_VARIANT_AUTO, st)) return rc;
+  const int64_t n = (int64_t)B->nfib * L;
+  if (B->vtype == TACOGB_F64)
+    TACOGB_LAUNCH("t3_scatter_rows", st,
+                  (t3_scatter_rows<double><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                      dest, (const double*)Y, B->nfib, L, (double*)out)));
+  else
+    TACOGB_LAUNCH("t3_scatter_rows", st,
+                  (t3_scatter_rows<float><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
+                      dest, (const float*)Y, B->nfib, L, (float*)out)));
+  return 0;
+}
+
+int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
+               cudaStream_t st) {
+  if (int rc = check_csf3(B, "MTTKRP")) return rc;
+  TACOGB_CHECK_ARG(J >= 0, "MTTKRP: negative J");
+  const size_t vb = vsize(B->vtype);
+  const size_t abytes = (size_t)B->dims[0] * (size_t)J * vb;
+  TACOGB_CHECK_ARG(abytes == 0 || A != nullptr, "MTTKRP: null result");
+  TACOGB_CHECK_ARG(B->nnz == 0 || J == 0 || (C != nullptr && D != nullptr),
+                   "MTTKRP: null C or D");
+  if (abytes) TACOGB_CUDA_TRY(cudaMemsetAsync(A, 0, abytes, st));
+  if ((int64_t)B->nfib * J == 0 || B->n0 == 0) return 0;
+  void* T = scratch(align256((size_t)B->nfib * J * vb), 7);
+  if (!T) return last_code();
+  const tacogb_csr f = fiber_csr(B);
+  if (int rc = spmm_run(&f, J, D, B->vtype, T, TACOGB_VARIANT_AUTO, st)) return rc;
+  const int64_t threads = (int64_t)B->n0 * 32;
+  if (B->vtype == TACOGB_F64)
+    TACOGB_LAUNCH("t3_mttkrp_combine", st,
+                  (t3_mttkrp_combine<double><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                      B->pos1, B->crd0, B->crd1, B->n0, J, (const double*)C, (const double*)T,
+                      (double*)A)));
+  else
+    TACOGB_LAUNCH("t3_mttkrp_combine", st,
+                  (t3_mttkrp_combine<float><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                      B->pos1, B->crd0, B->crd1, B->n0, J, (const float*)C, (const float*)T,
+                      (float*)A)));
+  return 0;
+}
+
+}  // namespace tacogb

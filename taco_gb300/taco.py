@@ -98,3 +98,17 @@ def csr_result(dims, csize=64):
     t = TacoTensor(dims, [MODE_DENSE, MODE_SPARSE], vals=None, csize=csize,
                    index_arrays={1: (None, None)})
     return t
+
+
+def csf3(dims, crd0, pos1, crd1, pos2, crd2, vals, dense0=False):
+    """An order-3 {Sparse,Sparse,Sparse} tensor ({Dense,Sparse,Sparse} with dense0, crd0 then
+    unused): level 0 pos {0, len(crd0)} and crd0, level 1 pos1/crd1, level 2 pos2/crd2."""
+    n0 = (crd0.shape[0] if hasattr(crd0, "shape") else len(crd0))
+    pos0 = np.array([0, n0], np.int32)
+    types = [MODE_DENSE if dense0 else MODE_SPARSE, MODE_SPARSE, MODE_SPARSE]
+    idx = {1: (pos1, crd1), 2: (pos2, crd2)}
+    if not dense0:
+        idx[0] = (pos0, crd0)
+    t = TacoTensor(list(dims), types, vals=vals, index_arrays=idx)
+    t._keep.append(pos0)
+    return t

@@ -55,6 +55,23 @@ def sddmm_powerlaw(rows=1048576, seed=SEED_BASE + 3):
     return spmm_powerlaw(rows, seed)
 
 
+# Order-3 tensors for TTV / TTM / MTTKRP: nell-2's shape in FROSTT (12,092 x 9,184 x 28,818,
+# 7.7e7 nonzeros) with synthetic structure: every i present, a power-law number of (i,k) fibers
+# per i (mean 200) and of l per fiber (mean 32), values U(-1,1).
+TENSOR3_DIMS = (12092, 9184, 28818)
+MTTKRP_J = 32
+
+
+def tensor3_powerlaw(dims=TENSOR3_DIMS, fib_mean=200.0, leaf_mean=32.0, seed=SEED_BASE + 5):
+    """(dims, crd0, pos1, crd1, pos2, crd2, vals): a {Sparse,Sparse,Sparse} tensor."""
+    s1 = spec(dims[0], cols=dims[1], kind=POWERLAW, mean=fib_mean, len_max=dims[1], seed=seed)
+    pos1, crd1, _ = generate(s1)
+    s2 = spec(len(crd1), cols=dims[2], kind=POWERLAW, mean=leaf_mean,
+              len_max=min(dims[2], 4096), seed=seed + 1)
+    pos2, crd2, vals = generate(s2)
+    return (tuple(dims), np.arange(dims[0], dtype=np.int32), pos1, crd1, pos2, crd2, vals)
+
+
 def spgemm_random(rows=262144, seed=SEED_BASE + 4):
     return spec(rows, kind=UNIFORM, len_lo=8, len_hi=8, seed=seed)
 

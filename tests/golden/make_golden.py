@@ -112,6 +112,32 @@ def sddmm_cases():
     save("sddmm_powerlaw_j96", pos=pos, crd=crd, vals=vals, A=H.ref_sddmm(pos, crd, vals, C, D))
 
 
+def _save_csf3(name, B, A, **dense):
+    dims, crd0, pos1, crd1, pos2, crd2, vals = B
+    save(name, dims=np.array(dims), crd0=crd0, pos1=pos1, crd1=crd1, pos2=pos2, crd2=crd2,
+         vals=vals, A=A, **dense)
+
+
+def tensor3_cases():
+    """taco's order-3 test inputs (test/tests-scheduling-eval.cpp), B {Sparse,Sparse,Sparse}
+    (taco's mttkrpCPU has a dense first level; its values are the same)."""
+    for name, dims, sp, seed in (("ttv_taco_gpu", (102, 103, 105), 0.3, 35325),
+                                 ("ttv_taco_cpu", (102, 103, 105), 0.3, 9536)):
+        co, v, (c,) = H.taco_tensor3_inputs(dims, sp, seed, [(dims[2],)])
+        B = H.csf3(dims, co, v)
+        _save_csf3(name, B, H.ref_tensor3("ttv", B, c), c=c)
+    for name, dims, L, seed in (("ttm_taco_gpu", (25, 25, 30), 128, 34644),
+                                ("ttm_taco_cpu", (25, 25, 26), 30, 935)):
+        co, v, (C,) = H.taco_tensor3_inputs(dims, 0.1, seed, [(dims[2], L)])
+        B = H.csf3(dims, co, v)
+        _save_csf3(name, B, H.ref_tensor3("ttm", B, C), C=C)
+    for name, dims, J, seed in (("mttkrp_taco_gpu", (25, 25, 30), 32, 5464164),
+                                ("mttkrp_taco_cpu", (51, 52, 61), 51, 549694)):
+        co, v, (C, D) = H.taco_tensor3_inputs(dims, 0.1, seed, [(dims[1], J), (dims[2], J)])
+        B = H.csf3(dims, co, v)
+        _save_csf3(name, B, H.ref_tensor3("mttkrp", B, C, D), C=C, D=D)
+
+
 def taco_pack_cli(rows, cols, ri, ci, v, workdir):
     """CSR (pos, crd, vals) that taco itself makes of the coordinates: the taco CLI reads them
     from a .tns file (Tensor::insert for every line, then TensorBase::pack: sort, sum
@@ -230,5 +256,7 @@ if __name__ == "__main__":
     spgemm_cases()
     assert O.ref_available("sddmm")
     sddmm_cases()
+    assert O.ref_available("ttv") and O.ref_available("ttm") and O.ref_available("mttkrp")
+    tensor3_cases()
     pack_cases()
     reader_cases()

@@ -72,6 +72,82 @@ def taco_sddmm_inputs(I, J, K, sparsity, seed):
     return (np.array(pos, np.int32), np.array(crd, np.int32), np.array(vals)), C, D
 
 
+def taco_tensor3_inputs(dims, sparsity, seed, dense_shapes):
+    """The inputs of taco's order-3 tests (test/tests-scheduling-eval.cpp:993-1206, 1420-1580):
+    srand(seed); B's coordinates in lexicographic order with an entry where
+    rand_float < SPARSITY, value (double)(int)(rand_float*3/SPARSITY); then each dense operand
+    in row-major order, value (double)(int)(rand_float*3).  Returns (coords n x 3, vals,
+    [dense arrays])."""
+    _libc.srand(seed)
+    sp = np.float32(sparsity)
+
+    def draw():
+        return np.float32(_libc.rand()) / np.float32(RAND_MAX)
+
+    coords, vals = [], []
+    I, J, K = dims
+    for i in range(I):
+        for j in range(J):
+            for k in range(K):
+                r = draw()
+                if r < sp:
+                    coords.append((i, j, k))
+                    vals.append(float(int(np.float32(np.float32(r * np.float32(3)) / sp))))
+    mats = []
+    for shape in dense_shapes:
+        n = int(np.prod(shape))
+        mats.append(np.array([float(int(np.float32(draw() * np.float32(3)))) for _ in range(n)])
+                    .reshape(shape))
+    return np.array(coords, np.int32).reshape(-1, 3), np.array(vals), mats
+
+
+def csf3(dims, coords, vals, dense0=False):
+    """taco's {Sparse,Sparse,Sparse} (or {Dense,Sparse,Sparse}) storage of lexicographically
+    sorted, distinct coordinates: (dims, crd0, pos1, crd1, pos2, crd2, vals); with dense0 the
+    first level lists every i (crd0 = 0..I-1)."""
+    coords = np.asarray(coords, np.int64).reshape(-1, 3)
+    n = len(coords)
+    new_f = np.ones(n, bool)
+    new_f[1:] = np.any(coords[1:, :2] != coords[:-1, :2], axis=1)
+    fib = np.flatnonzero(new_f)
+    pos2 = np.append(fib, n).astype(np.int32)
+    crd2 = coords[:, 2].astype(np.int32)
+    fi, fj = coords[fib, 0], coords[fib, 1]
+    if dense0:
+        crd0 = np.arange(dims[0], dtype=np.int32)
+    else:
+        crd0 = np.unique(fi).astype(np.int32)
+    pos1 = np.searchsorted(fi, crd0, side="left").astype(np.int32)
+    pos1 = np.append(pos1, len(fib)).astype(np.int32)
+    return (tuple(int(d) for d in dims), crd0, pos1, fj.astype(np.int32), pos2, crd2,
+            np.asarray(vals, np.float64))
+
+
+def taco_csf3_tensor(B, dense0=False):
+    """A taco_tensor_t over a csf3 tuple (taco_gb300.taco.csf3)."""
+    return T.csf3(*B, dense0=dense0)
+
+
+def ref_tensor3(pattern, B, *dense):
+    """taco's generated compute for ttv / ttm / mttkrp ({Sparse,Sparse,Sparse} B, dense
+    operands and result) on host arrays."""
+    L = O.ref_lib(pattern)
+    O.ref_set_threads(1)
+    dims = B[0]
+    Bt = taco_csf3_tensor(B)
+    ops = [np.ascontiguousarray(d, np.float64) for d in dense]
+    if pattern == "ttv":
+        A = np.empty((dims[0], dims[1]))
+    elif pattern == "ttm":
+        A = np.empty((dims[0], dims[1], ops[0].shape[1]))
+    else:
+        A = np.empty((dims[0], ops[0].shape[1]))
+    At = T.dense(A, list(A.shape))
+    ts = [T.dense(o, list(o.shape)) for o in ops]
+    assert L.compute(At.ptr, Bt.ptr, *[t.ptr for t in ts]) == 0
+    return A
+
+
 def normwise(approx, exact):
     """||approx - exact||_2 / ||exact||_2 (0 when both are zero)."""
     a = np.asarray(approx, dtype=np.float64).ravel()

@@ -37,7 +37,7 @@ def test_libtacogb_gen_exports_header():
     assert all(hasattr(L, n) for n in names)
 
 
-@pytest.mark.parametrize("pattern", ["spmv", "spmm", "spgemm", "sddmm"])
+@pytest.mark.parametrize("pattern", ["spmv", "spmm", "spgemm", "sddmm", "ttv", "ttm", "mttkrp"])
 def test_dropin_modules_export_taco_names(pattern):
     L = ctypes.CDLL(os.path.join(N.LIBDIR, "libtacogb_%s.so" % pattern))
     for n in ("assemble", "compute", "evaluate", "_shim_assemble", "_shim_compute",

@@ -125,3 +125,33 @@ def test_sddmm_inputs_follow_taco_draws():
     (pos, crd, vals), C, D = taco_sddmm_inputs(1021 // 10, 128, 1039 // 10, 0.3, 535366)
     for a, b in ((pos, "pos"), (crd, "crd"), (vals, "vals"), (C, "C"), (D, "D")):
         assert np.array_equal(a, g[b])
+
+
+def _csf3_fixture(name):
+    g = _golden(name + ".npz")
+    B = (tuple(int(d) for d in g["dims"]), g["crd0"], g["pos1"], g["crd1"], g["pos2"], g["crd2"],
+         g["vals"])
+    return g, B
+
+
+@pytest.mark.parametrize("case", ["ttv_taco_gpu", "ttv_taco_cpu", "ttm_taco_gpu", "ttm_taco_cpu",
+                                  "mttkrp_taco_gpu", "mttkrp_taco_cpu"])
+def test_oracle_matches_golden_tensor3(case):
+    """The order-3 restatements against taco's own generated code on taco's test inputs."""
+    g, B = _csf3_fixture(case)
+    if case.startswith("ttv"):
+        A = O.ttv(B, g["c"])
+    elif case.startswith("ttm"):
+        A = O.ttm(B, g["C"])
+    else:
+        A = O.mttkrp(B, g["C"], g["D"])
+    assert np.array_equal(A, g["A"])
+
+
+def test_tensor3_inputs_follow_taco_draws():
+    from tests.helpers import csf3, taco_tensor3_inputs
+    g, B = _csf3_fixture("mttkrp_taco_gpu")
+    co, v, (C, D) = taco_tensor3_inputs((25, 25, 30), 0.1, 5464164, [(25, 32), (30, 32)])
+    for a, b in zip(csf3((25, 25, 30), co, v)[1:], B[1:]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(C, g["C"]) and np.array_equal(D, g["D"])
