@@ -60,7 +60,8 @@ def parse(argv=None):
     p.add_argument("--pack-n", type=int, default=0,
                    help="pack_powerlaw: pack only the first N shuffled records (0 = all)")
     p.add_argument("--rows", type=int, default=0,
-                   help="sddmm_powerlaw: rows (and columns) of B (0 = 1,048,576)")
+                   help="sddmm_powerlaw: rows (and columns) of B (0 = 1,048,576); mttkrp_nell2: "
+                        "B's first dimension (0 = 12,092)")
     p.add_argument("--no-cpu", action="store_true")
     a = p.parse_args(argv)
     if a.n is None:
@@ -688,7 +689,8 @@ class MttkrpOp:
     def __init__(self, args):
         from taco_gb300 import workloads as W
         self.args = args
-        self.B = W.tensor3_powerlaw()
+        dims = W.TENSOR3_DIMS if args.rows <= 0 else (args.rows,) + W.TENSOR3_DIMS[1:]
+        self.B = W.tensor3_powerlaw(dims=dims)
         dims, crd0, pos1, crd1, pos2, crd2, vals = self.B
         J = self.J = W.MTTKRP_J
         self.C = W.dense(71, dims[1] * J).reshape(dims[1], J)
@@ -717,9 +719,11 @@ class MttkrpOp:
         L = tg.lib()
         keep = (Bd, Cd, Dd, A, b)
 
+        v = self.args.variant
+
         def step(sp):
             rc = L.tacogb_mttkrp(ctypes.byref(b), self.J, Cd.data_ptr(), Dd.data_ptr(),
-                                 A.data_ptr(), sp)
+                                 A.data_ptr(), v, sp)
             if rc:
                 raise RuntimeError(L.tacogb_last_error().decode())
         return step, keep
@@ -1261,7 +1265,7 @@ def main():
     if rank == 0:
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
                    "sddmm": tg.sddmm_variants, "spgemm": lambda: ["default"],
-                   "mttkrp": lambda: ["default"],
+                   "mttkrp": tg.spmm_variants,
                    "pack": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,

@@ -300,14 +300,19 @@ int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, void* stream);
 int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, void* stream);
 /* A(i,j,l) = B(i,j,k) * C(k,l), C dims[2] x L row-major (taco: :1094-1146, 1420-1472).
  * tacogb_ttm writes one row of L values per fiber (nfib x L); tacogb_ttm_dense the dense
- * dims[0] x dims[1] x L result.  SpMM over the fibers. */
-int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, void* stream);
-int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, void* stream);
+ * dims[0] x dims[1] x L result.  SpMM over the fibers (variant: a tacogb_spmm variant,
+ * TACOGB_VARIANT_AUTO for the library's choice). */
+int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, int32_t variant,
+               void* stream);
+int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, int32_t variant,
+                     void* stream);
 /* A(i,j) = B(i,k,l) * C(k,j) * D(l,j), C dims[1] x J, D dims[2] x J, A dims[0] x J, all
- * row-major (taco: :1148-1206, 1526-1580).  SpMM of the fibers with D, then per i the sum of
- * C(k,:) times the fiber rows.  FP64 within 1e-12 normwise of taco's loop. */
+ * row-major (taco: :1148-1206, 1526-1580).  SpMM of the fibers with D (variant as for
+ * tacogb_ttm), then per i the sum of C(k,:) times the fiber rows, added into A atomically per
+ * run of fibers (the order of those adds is not fixed).  FP64 within 1e-12 normwise of taco's
+ * loop. */
 int tacogb_mttkrp(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
-                  void* stream);
+                  int32_t variant, void* stream);
 
 /* ------------------------------------------------------------------ taco kernel ABI ----- */
 

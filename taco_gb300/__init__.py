@@ -108,7 +108,7 @@ def ttv(B, c, dense=False, stream=None):
     return out
 
 
-def ttm(B, C, dense=False, stream=None):
+def ttm(B, C, dense=False, variant=VARIANT_AUTO, stream=None):
     """A(i,j,l) = B(i,j,k) * C(k,l): one row of L values per (i,j) fiber (tacogb_ttm) or taco's
     dense dims[0] x dims[1] x L result (tacogb_ttm_dense)."""
     import torch
@@ -117,18 +117,19 @@ def ttm(B, C, dense=False, stream=None):
     shape = (B.dims[0], B.dims[1], L) if dense else (B.nfib, L)
     out = torch.empty(shape, dtype=B.vals.dtype, device=B.vals.device)
     fn = lib().tacogb_ttm_dense if dense else lib().tacogb_ttm
-    check(fn(ctypes.byref(b), L, C.data_ptr(), out.data_ptr(), _stream_ptr(stream)), "tacogb_ttm")
+    check(fn(ctypes.byref(b), L, C.data_ptr(), out.data_ptr(), variant, _stream_ptr(stream)),
+          "tacogb_ttm")
     return out
 
 
-def mttkrp(B, C, D, stream=None):
+def mttkrp(B, C, D, variant=VARIANT_AUTO, stream=None):
     """A(i,j) = B(i,k,l) * C(k,j) * D(l,j): dense dims[0] x J result (tacogb_mttkrp)."""
     import torch
     J = C.shape[1]
     b = B.as_csf3()
     out = torch.empty(B.dims[0], J, dtype=B.vals.dtype, device=B.vals.device)
     check(lib().tacogb_mttkrp(ctypes.byref(b), J, C.data_ptr(), D.data_ptr(), out.data_ptr(),
-                              _stream_ptr(stream)), "tacogb_mttkrp")
+                              variant, _stream_ptr(stream)), "tacogb_mttkrp")
     return out
 
 

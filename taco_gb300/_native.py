@@ -129,9 +129,9 @@ SIGNATURES = {
     "_shim_tacogb_sddmm_evaluate": (I32, [P]),
     "tacogb_ttv": (I32, [ctypes.POINTER(Csf3), P, P, P]),
     "tacogb_ttv_dense": (I32, [ctypes.POINTER(Csf3), P, P, P]),
-    "tacogb_ttm": (I32, [ctypes.POINTER(Csf3), I32, P, P, P]),
-    "tacogb_ttm_dense": (I32, [ctypes.POINTER(Csf3), I32, P, P, P]),
-    "tacogb_mttkrp": (I32, [ctypes.POINTER(Csf3), I32, P, P, P, P]),
+    "tacogb_ttm": (I32, [ctypes.POINTER(Csf3), I32, P, P, I32, P]),
+    "tacogb_ttm_dense": (I32, [ctypes.POINTER(Csf3), I32, P, P, I32, P]),
+    "tacogb_mttkrp": (I32, [ctypes.POINTER(Csf3), I32, P, P, P, I32, P]),
     "tacogb_ttv_assemble": (I32, [P, P, P]),
     "tacogb_ttv_compute": (I32, [P, P, P]),
     "tacogb_ttv_evaluate": (I32, [P, P, P]),

@@ -879,15 +879,17 @@ int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, void* stream) {
 int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, void* stream) {
   return ttv_run(B, c, A, true, (cudaStream_t)stream);
 }
-int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, void* stream) {
-  return ttm_run(B, L, C, out, false, (cudaStream_t)stream);
+int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, int32_t variant,
+               void* stream) {
+  return ttm_run(B, L, C, out, false, variant, (cudaStream_t)stream);
 }
-int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, void* stream) {
-  return ttm_run(B, L, C, A, true, (cudaStream_t)stream);
+int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, int32_t variant,
+                     void* stream) {
+  return ttm_run(B, L, C, A, true, variant, (cudaStream_t)stream);
 }
 int tacogb_mttkrp(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
-                  void* stream) {
-  return mttkrp_run(B, J, C, D, A, (cudaStream_t)stream);
+                  int32_t variant, void* stream) {
+  return mttkrp_run(B, J, C, D, A, variant, (cudaStream_t)stream);
 }
 
 extern "C++" {  // the helpers below include a template
@@ -1085,7 +1087,7 @@ int tacogb_ttm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C) {
   const size_t ob[1] = {(size_t)C->dimensions[0] * L * vb};
   return t3_compute(A, B, (size_t)A->dimensions[0] * A->dimensions[1] * L * vb, 1, ops, ob,
                     [L](const tacogb_csf3& b, const void* const* d, void* a, cudaStream_t st) {
-                      return ttm_run(&b, L, d[0], a, true, st);
+                      return ttm_run(&b, L, d[0], a, true, TACOGB_VARIANT_AUTO, st);
                     });
 }
 int tacogb_ttm_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C) {
@@ -1106,7 +1108,7 @@ int tacogb_mttkrp_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, 
   const size_t ob[2] = {(size_t)C->dimensions[0] * J * vb, (size_t)D->dimensions[0] * J * vb};
   return t3_compute(A, B, (size_t)A->dimensions[0] * J * vb, 2, ops, ob,
                     [J](const tacogb_csf3& b, const void* const* d, void* a, cudaStream_t st) {
-                      return mttkrp_run(&b, J, d[0], d[1], a, st);
+                      return mttkrp_run(&b, J, d[0], d[1], a, TACOGB_VARIANT_AUTO, st);
                     });
 }
 int tacogb_mttkrp_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C,

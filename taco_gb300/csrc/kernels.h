@@ -20,6 +20,7 @@ int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_ite
 // SpMM (spmm.cu)
 int spmm_variant_count();
 const char* spmm_variant_name(int v);
+int spmm_variant_index(const char* name);  // -1 when no variant has that name
 int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,
              cudaStream_t st);
 
@@ -40,10 +41,10 @@ int sddmm_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, void
 
 // Order-3 kernels (tensor3.cu); dense selects taco's dense result form.
 int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStream_t st);
-int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense,
+int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense, int variant,
             cudaStream_t st);
 int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
-               cudaStream_t st);
+               int variant, cudaStream_t st);
 
 // COO -> CSR pack (pack.cu): device arrays in and out; *nnz read back (synchronises).
 int pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_rows,

@@ -320,6 +320,12 @@ const char* spmm_variant_name(int v) {
   return (v >= 0 && v < kNumSpmmVariants) ? kSpmmVariants[v].name : "";
 }
 
+int spmm_variant_index(const char* name) {
+  for (int i = 0; i < kNumSpmmVariants; i++)
+    if (strcmp(kSpmmVariants[i].name, name) == 0) return i;
+  return -1;
+}
+
 int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,
              cudaStream_t st) {
   TACOGB_CHECK_ARG(A != nullptr, "SpMM: null matrix");

@@ -12,7 +12,8 @@
 // and the fiber results scattered to (i, j).  MTTKRP factors the sum over l inside the sum over
 // k: T(f,:) = sum_l B(i,k,l) D(l,:) per level-1 fiber f = (i,k) (SpMM over the fiber matrix),
 // then A(i,:) = sum_f C(k_f,:) * T(f,:) over the fibers of i (t3_mttkrp_combine): 2J flops per
-// nonzero plus 2J per fiber, where taco's loop spends 3J per nonzero.
+// nonzero plus 2J per fiber, where taco's loop spends 3J per nonzero.  TTM and MTTKRP take the
+// SpMM variant of the fiber product (-1: the library's choice).
 #include <cstdint>
 #include <cstring>
 
@@ -61,29 +62,63 @@ __global__ void t3_scatter_rows(const int64_t* __restrict__ dest, const V* __res
   A[dest[f] * L + l] = Y[idx];
 }
 
-// A(i,:) = sum over the fibers f of level-0 entry e (i = crd0[e] or e) of C(crd1[f],:) * T(f,:):
-// one warp per entry, lanes over j, fibers in order.
+constexpr int kCombFibers = 64;  // fibers per warp in t3_mttkrp_combine
+
+// A(i,:) += C(crd1[f],:) * T(f,:) for the fibers f of one chunk of 64: one warp per chunk, lanes
+// over j, the C and T rows of eight fibers loaded together; each run of fibers of one i is
+// summed in registers and added to A(i,:) with one atomic add per lane (A zero-filled first).
+// Chunks balance the work however many fibers an i has; an i whose fibers straddle chunks
+// receives several adds, in no fixed order (taco's GPU schedule for this statement also uses
+// atomics, OutputRaceStrategy::Atomics at test/tests-scheduling-eval.cpp:342).
 template <class V>
 __global__ void t3_mttkrp_combine(const int32_t* __restrict__ pos1,
                                   const int32_t* __restrict__ crd0,
-                                  const int32_t* __restrict__ crd1, int32_t n0, int32_t J,
-                                  const V* __restrict__ C, const V* __restrict__ T,
+                                  const int32_t* __restrict__ crd1, int32_t n0, int32_t nfib,
+                                  int32_t J, const V* __restrict__ C, const V* __restrict__ T,
                                   V* __restrict__ A) {
-  const int64_t e = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (e >= n0) return;
-  const int32_t f0 = __ldg(pos1 + e), f1 = __ldg(pos1 + e + 1);
-  const int64_t i = crd0 ? __ldg(crd0 + e) : e;
+  const int64_t f0 = w * kCombFibers;
+  if (f0 >= nfib) return;
+  const int32_t f1 = (int32_t)min(f0 + kCombFibers, (int64_t)nfib);
+  int e0 = 0, hi = n0 - 1;  // the level-0 entry of f0: last e with pos1[e] <= f0
+  while (e0 < hi) {
+    const int mid = (e0 + hi + 1) >> 1;
+    if (__ldg(pos1 + mid) <= f0)
+      e0 = mid;
+    else
+      hi = mid - 1;
+  }
   for (int32_t j0 = 0; j0 < J; j0 += 32) {
     const int32_t j = j0 + lane;
+    const bool on = j < J;
+    int e = e0;
+    int32_t nx = __ldg(pos1 + e + 1);
     V acc = V(0);
-    if (j < J) {
-      for (int32_t f = f0; f < f1; f++) {
-        const int32_t k = __ldg(crd1 + f);
-        acc = fma(__ldg(C + (int64_t)k * J + j), __ldg(T + (int64_t)f * J + j), acc);
+    for (int32_t fb = (int32_t)f0; fb < f1; fb += 8) {
+      const int kq = (lane < 8 && fb + lane < f1) ? __ldg(crd1 + fb + lane) : 0;
+      V cv[8], tv[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int k = __shfl_sync(0xffffffffu, kq, q);
+        const bool ld = on && fb + q < f1;
+        cv[q] = ld ? __ldg(C + (int64_t)k * J + j) : V(0);
+        tv[q] = ld ? __ldg(T + (int64_t)(fb + q) * J + j) : V(0);
       }
-      A[i * J + j] = acc;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int32_t f = fb + q;
+        if (f >= f1) break;
+        while (f >= nx) {  // the fibers of entry e end here (warp-uniform)
+          if (on) atomicAdd(A + (crd0 ? (int64_t)__ldg(crd0 + e) : (int64_t)e) * J + j, acc);
+          acc = V(0);
+          e++;
+          nx = __ldg(pos1 + e + 1);
+        }
+        acc = fma(cv[q], tv[q], acc);
+      }
     }
+    if (on) atomicAdd(A + (crd0 ? (int64_t)__ldg(crd0 + e) : (int64_t)e) * J + j, acc);
   }
 }
 
@@ -159,7 +194,7 @@ int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStre
   return spmv_run(&f, c, out, TACOGB_VARIANT_AUTO, st);
 }
 
-int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense,
+int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense, int variant,
             cudaStream_t st) {
   if (int rc = check_csf3(B, "TTM")) return rc;
   TACOGB_CHECK_ARG(L >= 0, "TTM: negative L");
@@ -169,7 +204,7 @@ int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dens
     TACOGB_CHECK_ARG((int64_t)B->nfib * L == 0 || out != nullptr, "TTM: null result");
     if ((int64_t)B->nfib * L == 0) return 0;
     const tacogb_csr f = fiber_csr(B);
-    return spmm_run(&f, L, C, B->vtype, out, TACOGB_VARIANT_AUTO, st);
+    return spmm_run(&f, L, C, B->vtype, out, variant, st);
   }
   const size_t abytes = (size_t)B->dims[0] * (size_t)B->dims[1] * (size_t)L * vb;
   TACOGB_CHECK_ARG(abytes == 0 || out != nullptr, "TTM: null result");
@@ -182,7 +217,7 @@ int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dens
   if (int rc = fiber_dest(B, ws, st, dest)) return rc;
   void* Y = ws + align256((size_t)B->nfib * 8);
   const tacogb_csr f = fiber_csr(B);
-  if (int rc = spmm_run(&f, L, C, B->vtype, Y, TACOGB_VARIANT_AUTO, st)) return rc;
+  if (int rc = spmm_run(&f, L, C, B->vtype, Y, variant, st)) return rc;
   const int64_t n = (int64_t)B->nfib * L;
   if (B->vtype == TACOGB_F64)
     TACOGB_LAUNCH("t3_scatter_rows", st,
@@ -196,7 +231,7 @@ int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dens
 }
 
 int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
-               cudaStream_t st) {
+               int variant, cudaStream_t st) {
   if (int rc = check_csf3(B, "MTTKRP")) return rc;
   TACOGB_CHECK_ARG(J >= 0, "MTTKRP: negative J");
   const size_t vb = vsize(B->vtype);
@@ -209,18 +244,22 @@ int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, vo
   void* T = scratch(align256((size_t)B->nfib * J * vb), 7);
   if (!T) return last_code();
   const tacogb_csr f = fiber_csr(B);
-  if (int rc = spmm_run(&f, J, D, B->vtype, T, TACOGB_VARIANT_AUTO, st)) return rc;
-  const int64_t threads = (int64_t)B->n0 * 32;
+  // D (dims[2] x J) is small next to B and stays in L2: the streaming tile, which walks
+  // nonzeros across fiber boundaries, measured fastest for the fiber product (nell-2's shape,
+  // J = 32: 4.02 ms against 4.42 for the library's SpMM default)
+  if (variant < 0) variant = spmm_variant_index("stream_w512_dfs");
+  if (int rc = spmm_run(&f, J, D, B->vtype, T, variant, st)) return rc;
+  const int64_t threads = (((int64_t)B->nfib + kCombFibers - 1) / kCombFibers) * 32;
   if (B->vtype == TACOGB_F64)
     TACOGB_LAUNCH("t3_mttkrp_combine", st,
                   (t3_mttkrp_combine<double><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                      B->pos1, B->crd0, B->crd1, B->n0, J, (const double*)C, (const double*)T,
-                      (double*)A)));
+                      B->pos1, B->crd0, B->crd1, B->n0, B->nfib, J, (const double*)C,
+                      (const double*)T, (double*)A)));
   else
     TACOGB_LAUNCH("t3_mttkrp_combine", st,
                   (t3_mttkrp_combine<float><<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-                      B->pos1, B->crd0, B->crd1, B->n0, J, (const float*)C, (const float*)T,
-                      (float*)A)));
+                      B->pos1, B->crd0, B->crd1, B->n0, B->nfib, J, (const float*)C,
+                      (const float*)T, (float*)A)));
   return 0;
 }
 
