@@ -314,10 +314,45 @@ int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, in
 int tacogb_mttkrp(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
                   int32_t variant, void* stream);
 
+/* Operand formats on the SpMV / SpMM path (taco's tests: test/tests-expr_storage.cpp:873-937,
+ * tests-scheduling-eval.cpp:1309-1358 and :655-662).  A DCSR matrix ({Sparse,Sparse}) stores n0
+ * nonempty rows: crd0 their row numbers, pos (n0 + 1) and crd/vals their entries. */
+typedef struct tacogb_dcsr {
+  int32_t rows;
+  int32_t cols;
+  int32_t n0;
+  int64_t nnz;
+  const int32_t* crd0;
+  const int32_t* pos;
+  const int32_t* crd;
+  const void* vals;
+  int32_t vtype;
+} tacogb_dcsr;
+/* y = A x for DCSR A: dense_y != 0 writes all rows of y (zero where A stores no row); otherwise
+ * y holds n0 values, the sparse result whose coordinates are crd0. */
+int tacogb_spmv_dcsr(const tacogb_dcsr* A, const void* x, void* y, int32_t dense_y, void* stream);
+/* C = A B for DCSR A, dense row-major B (cols x N) and C (rows x N; rows A does not store are
+ * zero). */
+int tacogb_spmm_dcsr(const tacogb_dcsr* A, int32_t N, const void* B, void* C, void* stream);
+/* y = A x for CSC A given as a tacogb_csr whose pos has cols + 1 column starts and whose crd
+ * holds row numbers (rows, cols are A's).  Transposes to CSR on the GPU per call. */
+int tacogb_spmv_csc(const tacogb_csr* A, const void* x, void* y, void* stream);
+/* CSC (colpos, rowidx, vals) -> CSR (pos rows + 1, crd, out_vals), rows sorted by column;
+ * synchronises the stream.  TACOGB_ERR_ARG when a coordinate repeats. */
+int tacogb_csc_to_csr(int32_t rows, int32_t cols, int64_t nnz, const int32_t* colpos,
+                      const int32_t* rowidx, const void* vals, int32_t vtype, int32_t* pos,
+                      int32_t* crd, void* out_vals, void* stream);
+/* A sparse vector (k entries idx/vals) as a dense one of n entries. */
+int tacogb_densify(int32_t n, int64_t k, const int32_t* idx, const void* vals, int32_t vtype,
+                   void* out, void* stream);
+
 /* ------------------------------------------------------------------ taco kernel ABI ----- */
 
 /* y(i) = A(i,j) * x(j).  Replaces the generated assemble/compute/evaluate of that statement
- * (taco "y(i) = A(i,j) * x(j)" -f=A:ds; generated text at the lowering cited above). */
+ * (taco "y(i) = A(i,j) * x(j)" -f=A:ds; generated text at the lowering cited above).  Also the
+ * format combinations of taco's spmv tests (test/tests-expr_storage.cpp:873-937): A CSC
+ * ({Dense,Sparse} ordered {1,0}) or DCSR ({Sparse,Sparse}), x {Sparse}, and y {Sparse} with a
+ * DCSR A (assemble gives y A's stored rows as its coordinates). */
 int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x);
 int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x);
 int tacogb_spmv_evaluate(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x);

@@ -209,7 +209,8 @@ def ref_lib(pattern):
         path = os.path.join(REF_DIR, "libtacoref_%s.so" % pattern)
         L = ctypes.CDLL(path, mode=ctypes.RTLD_LOCAL)
         nargs = 4 if pattern in ("sddmm", "mttkrp") else 3
-        for fn in ("assemble", "compute", "evaluate"):
+        fns = ("assemble", "compute", "evaluate")
+        for fn in fns:
             getattr(L, fn).argtypes = [P] * nargs
             getattr(L, fn).restype = ctypes.c_int
         _ref[pattern] = L

@@ -46,6 +46,21 @@ class Csf3(ctypes.Structure):
     ]
 
 
+class Dcsr(ctypes.Structure):
+    """tacogb_dcsr: a {Sparse,Sparse} matrix in device memory."""
+    _fields_ = [
+        ("rows", ctypes.c_int32),
+        ("cols", ctypes.c_int32),
+        ("n0", ctypes.c_int32),
+        ("nnz", ctypes.c_int64),
+        ("crd0", ctypes.c_void_p),
+        ("pos", ctypes.c_void_p),
+        ("crd", ctypes.c_void_p),
+        ("vals", ctypes.c_void_p),
+        ("vtype", ctypes.c_int32),
+    ]
+
+
 class Csr(ctypes.Structure):
     """tacogb_csr: a CSR matrix in device memory."""
     _fields_ = [
@@ -127,6 +142,11 @@ SIGNATURES = {
     "_shim_tacogb_sddmm_assemble": (I32, [P]),
     "_shim_tacogb_sddmm_compute": (I32, [P]),
     "_shim_tacogb_sddmm_evaluate": (I32, [P]),
+    "tacogb_spmv_dcsr": (I32, [ctypes.POINTER(Dcsr), P, P, I32, P]),
+    "tacogb_spmm_dcsr": (I32, [ctypes.POINTER(Dcsr), I32, P, P, P]),
+    "tacogb_spmv_csc": (I32, [ctypes.POINTER(Csr), P, P, P]),
+    "tacogb_csc_to_csr": (I32, [I32, I32, I64, P, P, P, I32, P, P, P, P]),
+    "tacogb_densify": (I32, [I32, I64, P, P, I32, P, P]),
     "tacogb_ttv": (I32, [ctypes.POINTER(Csf3), P, P, P]),
     "tacogb_ttv_dense": (I32, [ctypes.POINTER(Csf3), P, P, P]),
     "tacogb_ttm": (I32, [ctypes.POINTER(Csf3), I32, P, P, I32, P]),

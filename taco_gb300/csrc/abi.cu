@@ -84,7 +84,7 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 8;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3
+constexpr int kScratchSlots = 11;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3, formats x3
 
 struct DeviceState {
   int sms = 0;
@@ -431,7 +431,194 @@ int tacogb_spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_
 
 // ---------------------------------------------------------------- SpMV taco ABI -----------
 
+// ------------------------------------------------------- SpMV operand formats (taco ABI) ---
+//
+// Besides CSR A with dense x and y, tacogb_spmv_assemble/compute take the format combinations of
+// taco's spmv tests (test/tests-expr_storage.cpp:873-937): A CSC ({Dense,Sparse}, mode ordering
+// {1,0}) or DCSR ({Sparse,Sparse}); x {Sparse}; y {Sparse} when A is DCSR (y's coordinates are
+// A's stored rows, taco's generated assemble for that statement).
+
+namespace {
+
+enum { kFmtOther = 0, kFmtCSR, kFmtCSC, kFmtDCSR };
+
+int mat_format(const taco_tensor_t* A) {
+  if (!A || A->order != 2 || !A->mode_types || !A->dimensions || !A->indices) return kFmtOther;
+  const bool o01 = !A->mode_ordering || (A->mode_ordering[0] == 0 && A->mode_ordering[1] == 1);
+  const bool o10 = A->mode_ordering && A->mode_ordering[0] == 1 && A->mode_ordering[1] == 0;
+  const int m0 = A->mode_types[0], m1 = A->mode_types[1];
+  if (m0 == taco_mode_dense && m1 == taco_mode_sparse) return o01 ? kFmtCSR : o10 ? kFmtCSC : kFmtOther;
+  if (m0 == taco_mode_sparse && m1 == taco_mode_sparse && o01) return kFmtDCSR;
+  return kFmtOther;
+}
+
+bool is_sparse_vector(const taco_tensor_t* t) {
+  return t && t->order == 1 && t->mode_types && t->mode_types[0] == taco_mode_sparse;
+}
+
+bool plain_spmv(const taco_tensor_t* y, const taco_tensor_t* A, const taco_tensor_t* x) {
+  return mat_format(A) == kFmtCSR && !is_sparse_vector(x) && !is_sparse_vector(y);
+}
+
+int check_any_vector(const taco_tensor_t* t, const char* name) {
+  TACOGB_CHECK_ARG(t != nullptr && t->order == 1 && t->dimensions != nullptr,
+                   "%s: expected an order-1 tensor", name);
+  if (is_sparse_vector(t))
+    TACOGB_CHECK_ARG(t->indices && t->indices[0], "%s: missing sparse indices", name);
+  return 0;
+}
+
+// The checks shared by the format path's assemble and compute; *fmt receives A's format.
+int check_spmv_formats(const taco_tensor_t* y, const taco_tensor_t* A, const taco_tensor_t* x,
+                       int* fmt) {
+  *fmt = mat_format(A);
+  TACOGB_CHECK_ARG(*fmt != kFmtOther,
+                   "spmv: A must be CSR, CSC ({Dense,Sparse} ordered {1,0}) or DCSR");
+  if (int rc = check_any_vector(y, "spmv result y")) return rc;
+  if (int rc = check_any_vector(x, "spmv operand x")) return rc;
+  TACOGB_CHECK_ARG(!is_sparse_vector(y) || *fmt == kFmtDCSR,
+                   "spmv: a {Sparse} result needs a DCSR A (its stored rows are y's pattern)");
+  const int vt = value_type_of_csize(A->csize);
+  TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spmv: unsupported csize %d", A->csize);
+  TACOGB_CHECK_ARG(x->csize == A->csize && y->csize == A->csize,
+                   "spmv: operand component sizes differ");
+  TACOGB_CHECK_ARG(y->dimensions[0] == A->dimensions[0] && x->dimensions[0] == A->dimensions[1],
+                   "spmv: shapes differ (y %d, A %dx%d, x %d)", y->dimensions[0],
+                   A->dimensions[0], A->dimensions[1], x->dimensions[0]);
+  return 0;
+}
+
+// A DCSR operand's level-0 row list and level-1 arrays on the device (slots base .. base+4).
+int dcsr_operand(const taco_tensor_t* A, int base, cudaStream_t st, tacogb_dcsr& out) {
+  const int32_t* pos0 = (const int32_t*)A->indices[0][0];
+  TACOGB_CHECK_ARG(pos0 != nullptr && A->indices[1], "DCSR: missing indices");
+  tacogb_dcsr d{};
+  d.rows = A->dimensions[0];
+  d.cols = A->dimensions[1];
+  d.vtype = value_type_of_csize(A->csize);
+  if (int rc = read_i32(pos0 + 1, &d.n0)) return rc;
+  const int32_t* pos1 = (const int32_t*)A->indices[1][0];
+  TACOGB_CHECK_ARG(pos1 != nullptr, "DCSR: null pos");
+  int32_t nnz = 0;
+  if (int rc = read_i32(pos1 + d.n0, &nnz)) return rc;
+  d.nnz = nnz;
+  Operand o0, op, oc, ov;
+  if (int rc = stage_in(o0, A->indices[0][1], (size_t)d.n0 * 4, base, st)) return rc;
+  if (int rc = stage_in(op, pos1, ((size_t)d.n0 + 1) * 4, base + 1, st)) return rc;
+  if (int rc = stage_in(oc, A->indices[1][1], (size_t)nnz * 4, base + 2, st)) return rc;
+  if (int rc = stage_in(ov, A->vals, (size_t)nnz * value_bytes(d.vtype), base + 3, st)) return rc;
+  d.crd0 = (const int32_t*)o0.dev;
+  d.pos = (const int32_t*)op.dev;
+  d.crd = (const int32_t*)oc.dev;
+  d.vals = ov.dev;
+  out = d;
+  return 0;
+}
+
+// x as a dense device vector: a {Dense} x staged as is, a {Sparse} x scattered into zeros.
+int dense_x(const taco_tensor_t* x, int vt, int base, cudaStream_t st, const void** out) {
+  const int32_t n = x->dimensions[0];
+  const size_t vb = value_bytes(vt);
+  if (!is_sparse_vector(x)) {
+    Operand o;
+    if (int rc = stage_in(o, x->vals, (size_t)n * vb, base, st)) return rc;
+    *out = o.dev;
+    return 0;
+  }
+  const int32_t* pos = (const int32_t*)x->indices[0][0];
+  TACOGB_CHECK_ARG(pos != nullptr, "spmv: null pos of the sparse x");
+  int32_t k = 0;
+  if (int rc = read_i32(pos + 1, &k)) return rc;
+  Operand oi, ov;
+  if (int rc = stage_in(oi, x->indices[0][1], (size_t)k * 4, base, st)) return rc;
+  if (int rc = stage_in(ov, x->vals, (size_t)k * vb, base + 1, st)) return rc;
+  void* d = stage_buffer(base + 2, (size_t)n * vb);
+  if (!d) return TACOGB_ERR_ALLOC;
+  if (int rc = densify_run(n, k, (const int32_t*)oi.dev, ov.dev, vt, d, st)) return rc;
+  *out = d;
+  return 0;
+}
+
+int spmv_fmt_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
+  int fmt;
+  if (int rc = check_spmv_formats(y, A, x, &fmt)) return rc;
+  const int vt = value_type_of_csize(A->csize);
+  const bool managed = A->vals != nullptr && device_accessible(A->vals);
+  if (!is_sparse_vector(y)) {
+    void* p = alloc_result((size_t)y->dimensions[0] * value_bytes(vt), managed);
+    if (!p) return TACOGB_ERR_ALLOC;
+    y->vals = (uint8_t*)p;
+    return 0;
+  }
+  int32_t n0 = 0;  // y's pattern: A's stored rows
+  if (int rc = read_i32((const int32_t*)A->indices[0][0] + 1, &n0)) return rc;
+  int32_t* pos = (int32_t*)alloc_result(2 * sizeof(int32_t), managed);
+  int32_t* crd = (int32_t*)alloc_result((size_t)n0 * 4, managed);
+  void* vals = alloc_result((size_t)n0 * value_bytes(vt), managed);
+  if (!pos || !crd || !vals) return TACOGB_ERR_ALLOC;
+  const int32_t head[2] = {0, n0};
+  cudaStream_t st = lib_stream();
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, head, sizeof(head), cudaMemcpyDefault, st));
+  if (n0)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(crd, A->indices[0][1], (size_t)n0 * 4, cudaMemcpyDefault, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  y->indices[0][0] = (uint8_t*)pos;
+  y->indices[0][1] = (uint8_t*)crd;
+  y->vals = (uint8_t*)vals;
+  return 0;
+}
+
+int spmv_fmt_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
+  int fmt;
+  if (int rc = check_spmv_formats(y, A, x, &fmt)) return rc;
+  TACOGB_CHECK_ARG(y->vals != nullptr, "spmv: result values not assembled");
+  const int vt = value_type_of_csize(A->csize);
+  const size_t vb = value_bytes(vt);
+  const int32_t rows = A->dimensions[0], cols = A->dimensions[1];
+  cudaStream_t st = lib_stream();
+  const void* xd = nullptr;
+  if (int rc = dense_x(x, vt, 45, st, &xd)) return rc;
+  const bool sparse_y = is_sparse_vector(y);
+  size_t ybytes = (size_t)rows * vb;
+  tacogb_dcsr d{};
+  if (fmt == kFmtDCSR) {
+    if (int rc = dcsr_operand(A, 40, st, d)) return rc;
+    if (sparse_y) ybytes = (size_t)d.n0 * vb;
+  }
+  void* yd = y->vals;
+  const bool staged = !device_accessible(y->vals);
+  if (staged) {
+    yd = stage_buffer(48, ybytes);
+    if (!yd) return TACOGB_ERR_ALLOC;
+  }
+  if (fmt == kFmtDCSR) {
+    if (int rc = spmv_dcsr_run(&d, xd, yd, !sparse_y, st)) return rc;
+  } else {
+    // CSR, or CSC: level 1 runs over columns (cols + 1 pos entries, crd = rows)
+    const int32_t outer = fmt == kFmtCSC ? cols : rows;
+    const int32_t* pos = (const int32_t*)A->indices[1][0];
+    TACOGB_CHECK_ARG(pos != nullptr, "spmv: null pos");
+    int32_t nnz = 0;
+    if (int rc = read_i32(pos + outer, &nnz)) return rc;
+    Operand op, oc, ov;
+    if (int rc = stage_in(op, pos, ((size_t)outer + 1) * 4, 40, st)) return rc;
+    if (int rc = stage_in(oc, A->indices[1][1], (size_t)nnz * 4, 41, st)) return rc;
+    if (int rc = stage_in(ov, A->vals, (size_t)nnz * vb, 42, st)) return rc;
+    tacogb_csr c{rows, cols, nnz, (const int32_t*)op.dev, (const int32_t*)oc.dev, ov.dev, vt};
+    if (int rc = fmt == kFmtCSC ? spmv_csc_run(&c, xd, yd, st)
+                                : spmv_run(&c, xd, yd, TACOGB_VARIANT_AUTO, st))
+      return rc;
+  }
+  if (staged && ybytes)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(y->vals, yd, ybytes, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return consume_device_status();
+}
+
+}  // namespace
+
 int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
+  if (!plain_spmv(y, A, x)) return spmv_fmt_assemble(y, A, x);
   if (int rc = check_dense_vector(y, "spmv result y")) return rc;
   if (int rc = check_csr(A, "spmv operand A")) return rc;
   const int vt = value_type_of_csize(y->csize);
@@ -444,6 +631,7 @@ int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
 }
 
 int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
+  if (!plain_spmv(y, A, x)) return spmv_fmt_compute(y, A, x);
   if (int rc = check_dense_vector(y, "spmv result y")) return rc;
   if (int rc = check_csr(A, "spmv operand A")) return rc;
   if (int rc = check_dense_vector(x, "spmv operand x")) return rc;
@@ -504,7 +692,8 @@ int _shim_tacogb_spmv_evaluate(void** a) {
 
 int tacogb_spmm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   if (int rc = check_dense_matrix(C, "spmm result C")) return rc;
-  if (int rc = check_csr(A, "spmm operand A")) return rc;
+  if (mat_format(A) != kFmtDCSR)
+    if (int rc = check_csr(A, "spmm operand A")) return rc;
   const int vt = value_type_of_csize(C->csize);
   TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spmm: unsupported result csize %d",
                    C->csize);
@@ -516,7 +705,41 @@ int tacogb_spmm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   return 0;
 }
 
+// C = A B with A DCSR ({Sparse,Sparse}; taco's spmmDCSRGPU, test/tests-scheduling-eval.cpp
+// :1309-1358), B and C dense row-major, FP64 or FP32.
+static int spmm_dcsr_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (int rc = check_dense_matrix(C, "spmm result C")) return rc;
+  if (int rc = check_dense_matrix(B, "spmm operand B")) return rc;
+  const int vt = value_type_of_csize(A->csize);
+  TACOGB_CHECK_ARG((vt == TACOGB_F64 || vt == TACOGB_F32) && B->csize == A->csize &&
+                       C->csize == A->csize,
+                   "spmm: DCSR A needs FP64 or FP32 operands of one type");
+  const int32_t rows = A->dimensions[0], cols = A->dimensions[1], N = B->dimensions[1];
+  TACOGB_CHECK_ARG(B->dimensions[0] == cols && C->dimensions[0] == rows && C->dimensions[1] == N,
+                   "spmm: shapes differ");
+  TACOGB_CHECK_ARG(C->vals != nullptr, "spmm: result values not assembled");
+  cudaStream_t st = lib_stream();
+  tacogb_dcsr d;
+  if (int rc = dcsr_operand(A, 40, st, d)) return rc;
+  const size_t vb = value_bytes(vt);
+  Operand ob;
+  if (int rc = stage_in(ob, B->vals, (size_t)cols * N * vb, 44, st)) return rc;
+  const size_t cbytes = (size_t)rows * N * vb;
+  void* cdev = C->vals;
+  const bool staged = !device_accessible(C->vals);
+  if (staged) {
+    cdev = stage_buffer(48, cbytes);
+    if (!cdev) return TACOGB_ERR_ALLOC;
+  }
+  if (int rc = spmm_dcsr_run(&d, N, ob.dev, cdev, st)) return rc;
+  if (staged && cbytes)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(C->vals, cdev, cbytes, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return consume_device_status();
+}
+
 int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
+  if (mat_format(A) == kFmtDCSR) return spmm_dcsr_compute(C, A, B);
   if (int rc = check_dense_matrix(C, "spmm result C")) return rc;
   if (int rc = check_csr(A, "spmm operand A")) return rc;
   if (int rc = check_dense_matrix(B, "spmm operand B")) return rc;
@@ -1137,5 +1360,27 @@ TACOGB_SHIM4(mttkrp_compute)
 TACOGB_SHIM4(mttkrp_evaluate)
 #undef TACOGB_SHIM3
 #undef TACOGB_SHIM4
+
+// ------------------------------------------------------------------ formats ---------------
+
+int tacogb_spmv_dcsr(const tacogb_dcsr* A, const void* x, void* y, int32_t dense_y, void* stream) {
+  return spmv_dcsr_run(A, x, y, dense_y != 0, (cudaStream_t)stream);
+}
+int tacogb_spmm_dcsr(const tacogb_dcsr* A, int32_t N, const void* B, void* C, void* stream) {
+  return spmm_dcsr_run(A, N, B, C, (cudaStream_t)stream);
+}
+int tacogb_spmv_csc(const tacogb_csr* A, const void* x, void* y, void* stream) {
+  return spmv_csc_run(A, x, y, (cudaStream_t)stream);
+}
+int tacogb_csc_to_csr(int32_t rows, int32_t cols, int64_t nnz, const int32_t* colpos,
+                      const int32_t* rowidx, const void* vals, int32_t vtype, int32_t* pos,
+                      int32_t* crd, void* out_vals, void* stream) {
+  return csc_to_csr_run(rows, cols, nnz, colpos, rowidx, vals, vtype, pos, crd, out_vals,
+                        (cudaStream_t)stream);
+}
+int tacogb_densify(int32_t n, int64_t k, const int32_t* idx, const void* vals, int32_t vtype,
+                   void* out, void* stream) {
+  return densify_run(n, k, idx, vals, vtype, out, (cudaStream_t)stream);
+}
 
 }  // extern "C"

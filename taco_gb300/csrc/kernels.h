@@ -46,6 +46,17 @@ int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dens
 int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
                int variant, cudaStream_t st);
 
+// Operand formats (formats.cu): DCSR SpMV (dense result, or the values of the sparse result
+// whose pattern is the stored rows) and SpMM, CSC SpMV by a GPU transpose, sparse -> dense x.
+int spmv_dcsr_run(const tacogb_dcsr* A, const void* x, void* y, bool dense, cudaStream_t st);
+int spmm_dcsr_run(const tacogb_dcsr* A, int32_t N, const void* B, void* C, cudaStream_t st);
+int spmv_csc_run(const tacogb_csr* Acsc, const void* x, void* y, cudaStream_t st);
+int csc_to_csr_run(int32_t rows, int32_t cols, int64_t nnz, const int32_t* colpos,
+                   const int32_t* rowidx, const void* vals, int32_t vtype, int32_t* pos,
+                   int32_t* crd, void* out_vals, cudaStream_t st);
+int densify_run(int32_t n, int64_t k, const int32_t* idx, const void* vals, int32_t vtype,
+                void* out, cudaStream_t st);
+
 // COO -> CSR pack (pack.cu): device arrays in and out; *nnz read back (synchronises).
 int pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_rows,
              const int32_t* coord_cols, const void* vals, int32_t vtype, int32_t* pos,

@@ -148,6 +148,86 @@ def ref_tensor3(pattern, B, *dense):
     return A
 
 
+def to_dcsr(pos, crd):
+    """(crd0, pos1) of the {Sparse,Sparse} form of a CSR matrix: its nonempty rows."""
+    lens = np.diff(pos)
+    crd0 = np.flatnonzero(lens > 0).astype(np.int32)
+    pos1 = np.concatenate([[0], np.cumsum(lens[crd0])]).astype(np.int32)
+    return crd0, pos1
+
+
+def to_csc(pos, crd, vals, cols):
+    """(colpos, rowidx, vals) of a CSR matrix's CSC form, rows ascending in each column."""
+    rows = np.repeat(np.arange(len(pos) - 1, dtype=np.int32), np.diff(pos))
+    o = np.lexsort((rows, crd))
+    colpos = np.searchsorted(crd[o], np.arange(cols + 1), side="left").astype(np.int32)
+    return colpos, rows[o].astype(np.int32), np.asarray(vals)[o]
+
+
+def taco_dcsr_tensor(crd0, pos1, crd, vals, dims):
+    pos0 = np.array([0, len(crd0)], np.int32)
+    t = T.TacoTensor(list(dims), [T.MODE_SPARSE, T.MODE_SPARSE], vals=vals,
+                     index_arrays={0: (pos0, crd0), 1: (pos1, crd)})
+    t._keep.append(pos0)
+    return t
+
+
+def taco_csc_tensor(colpos, rowidx, vals, dims):
+    return T.TacoTensor(list(dims), [T.MODE_DENSE, T.MODE_SPARSE], vals=vals,
+                        index_arrays={1: (colpos, rowidx)}, mode_ordering=[1, 0])
+
+
+def taco_sparse_vector(idx, vals, n):
+    pos = np.array([0, len(idx)], np.int32)
+    t = T.TacoTensor([n], [T.MODE_SPARSE], vals=vals, index_arrays={0: (pos, idx)})
+    t._keep.append(pos)
+    return t
+
+
+def taco_sparse_vector_result(n, csize=64):
+    return T.TacoTensor([n], [T.MODE_SPARSE], vals=None, csize=csize,
+                        index_arrays={0: (None, None)})
+
+
+def ref_spmv_formats(kind, pos, crd, vals, cols, x, x_sparse=None):
+    """taco's generated SpMV for A DCSR ("dcsr"), CSC ("csc") or DCSR with {Sparse} x and y
+    ("dcsr_sv": x_sparse = (idx, vals); returns (crd, vals) of y)."""
+    import ctypes
+    rows = len(pos) - 1
+    L = O.ref_lib("spmv_" + kind)
+    O.ref_set_threads(1)
+    if kind == "csc":
+        At = taco_csc_tensor(*to_csc(pos, crd, vals, cols), [rows, cols])
+    else:
+        crd0, pos1 = to_dcsr(pos, crd)
+        At = taco_dcsr_tensor(crd0, pos1, crd, vals, [rows, cols])
+    if kind != "dcsr_sv":
+        y = np.empty(rows)
+        Yt, Xt = T.dense(y, [rows]), T.dense(x, [cols])
+        assert L.compute(Yt.ptr, At.ptr, Xt.ptr) == 0
+        return y
+    Xt = taco_sparse_vector(x_sparse[0], x_sparse[1], cols)
+    Yt = taco_sparse_vector_result(rows)
+    assert L.assemble(Yt.ptr, At.ptr, Xt.ptr) == 0
+    assert L.compute(Yt.ptr, At.ptr, Xt.ptr) == 0
+    n = np.ctypeslib.as_array(ctypes.cast(Yt.index(0, 0), ctypes.POINTER(ctypes.c_int32)), (2,))[1]
+    yc = np.ctypeslib.as_array(ctypes.cast(Yt.index(0, 1), ctypes.POINTER(ctypes.c_int32)), (n,))
+    yv = np.ctypeslib.as_array(ctypes.cast(Yt.vals_ptr, ctypes.POINTER(ctypes.c_double)), (n,))
+    return yc.copy(), yv.copy()
+
+
+def ref_spmm_dcsr(pos, crd, vals, B):
+    L = O.ref_lib("spmm_dcsr")
+    O.ref_set_threads(1)
+    rows, cols, N = len(pos) - 1, B.shape[0], B.shape[1]
+    crd0, pos1 = to_dcsr(pos, crd)
+    At = taco_dcsr_tensor(crd0, pos1, crd, vals, [rows, cols])
+    C = np.empty((rows, N))
+    Ct, Bt = T.dense(C, [rows, N]), T.dense(np.ascontiguousarray(B), [cols, N])
+    assert L.compute(Ct.ptr, At.ptr, Bt.ptr) == 0
+    return C
+
+
 def normwise(approx, exact):
     """||approx - exact||_2 / ||exact||_2 (0 when both are zero)."""
     a = np.asarray(approx, dtype=np.float64).ravel()
