@@ -138,6 +138,23 @@ def tensor3_cases():
         _save_csf3(name, B, H.ref_tensor3("mttkrp", B, C, D), C=C, D=D)
 
 
+def format_cases():
+    """SpMV with A DCSR or CSC, with A DCSR and {Sparse} x and y, and taco's spmmDCSRGPU
+    (test/tests-scheduling-eval.cpp:1309-1358, srand 25643), through taco's generated code."""
+    (pos, crd, vals, _), _ = H.taco_rand_csr(1021 // 10, 1039 // 10, 0.3)
+    cols = 1039 // 10
+    x = W.dense(21, cols)
+    xi = np.arange(0, cols, 3, dtype=np.int32)
+    ys_crd, ys_vals = H.ref_spmv_formats("dcsr_sv", pos, crd, vals, cols, None, (xi, x[xi]))
+    save("spmv_formats_taco", pos=pos, crd=crd, vals=vals, x=x, xi=xi,
+         y_dcsr=H.ref_spmv_formats("dcsr", pos, crd, vals, cols, x),
+         y_csc=H.ref_spmv_formats("csc", pos, crd, vals, cols, x), ys_crd=ys_crd, ys_vals=ys_vals)
+    (pos, crd, vals, _), (_, _, _, Bd) = H.taco_rand_csr(1021 // 10, 1039 // 10, 0.3, seed=25643,
+                                                          dense_b_cols=128)
+    save("spmm_dcsr_taco_gpu", pos=pos, crd=crd, vals=vals, B=Bd,
+         C=H.ref_spmm_dcsr(pos, crd, vals, Bd))
+
+
 def taco_pack_cli(rows, cols, ri, ci, v, workdir):
     """CSR (pos, crd, vals) that taco itself makes of the coordinates: the taco CLI reads them
     from a .tns file (Tensor::insert for every line, then TensorBase::pack: sort, sum
@@ -258,5 +275,7 @@ if __name__ == "__main__":
     sddmm_cases()
     assert O.ref_available("ttv") and O.ref_available("ttm") and O.ref_available("mttkrp")
     tensor3_cases()
+    assert O.ref_available("spmv_dcsr") and O.ref_available("spmm_dcsr")
+    format_cases()
     pack_cases()
     reader_cases()
