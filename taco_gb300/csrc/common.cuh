@@ -93,6 +93,8 @@ constexpr int kBFlagWord = 17;
 // Word of the same block holding the double-float SDDMM's D-range flag (cleared before, set by
 // its transpose kernel).
 constexpr int kDFlagWord = 18;
+// Word of the same block holding the fused MTTKRP's D-range flag (cleared before its split).
+constexpr int kMFlagWord = 19;
 
 // ---------------------------------------------------------------- TMA / mbarrier ----------
 
@@ -211,5 +213,53 @@ struct CompF32 {
   }
   __device__ __forceinline__ float result() const { return __fadd_rn(hi, lo); }
 };
+
+// ---------------------------------------------------------------- warp row search ----------
+
+// Row of nonzero p: the last r in [0, rows) with pos[r] <= p (pos[rows] > p).  32-ary search,
+// one ballot per level: about log32(rows) dependent loads.
+__device__ __forceinline__ int warp_find_row(const int32_t* __restrict__ pos, int32_t rows,
+                                             int32_t p, int lane) {
+  int lo = 0;
+  int len = rows;
+  while (len > 1) {
+    const int step = (len + 31) >> 5;
+    const int64_t off = (int64_t)lane * step;
+    const bool ok = off < len && __ldg(pos + lo + off) <= p;
+    const unsigned b = __ballot_sync(0xffffffffu, ok);  // a prefix of lanes; lane 0 always set
+    const int L = 31 - __clz(b);
+    const int nlo = lo + L * step;
+    len = min(step, lo + len - nlo);
+    lo = nlo;
+  }
+  return lo;
+}
+
+// Each lane's row for its nonzero p, given lo with pos[lo] <= every lane's p: lane m reads the
+// row start pos[lo + 1 + m], each lane counts the starts <= its p by a five-step search over
+// the lanes' sorted values, and lanes past 32 rows (runs of empty rows) go round again.
+__device__ __forceinline__ int warp_batch_rows(const int32_t* __restrict__ pos, int32_t rows,
+                                               int lo, int32_t p, int lane) {
+  int r = lo;
+  bool done = false;
+  for (;;) {
+    const int q = lo + 1 + lane;
+    const int s = q <= rows ? __ldg(pos + q) : INT32_MAX;
+    int c = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const int v = __shfl_sync(0xffffffffu, s, c + step - 1);
+      if (v <= p) c += step;
+    }
+    if (__shfl_sync(0xffffffffu, s, 31) <= p) c = 32;
+    if (!done && c < 32) {
+      r = lo + c;
+      done = true;
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+    lo += 32;
+  }
+  return r;
+}
 
 }  // namespace tacogb

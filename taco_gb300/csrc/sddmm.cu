@@ -206,52 +206,6 @@ __device__ __forceinline__ void ld_shared_slice(const T* p, T (&r)[N]) {
   }
 }
 
-// Row of nonzero p: the last r in [0, rows) with pos[r] <= p (pos[rows] > p).  32-ary search,
-// one ballot per level: about log32(rows) dependent loads.
-__device__ __forceinline__ int sd_find_row(const int32_t* __restrict__ pos, int32_t rows,
-                                           int32_t p, int lane) {
-  int lo = 0;
-  int len = rows;
-  while (len > 1) {
-    const int step = (len + 31) >> 5;
-    const int64_t off = (int64_t)lane * step;
-    const bool ok = off < len && __ldg(pos + lo + off) <= p;
-    const unsigned b = __ballot_sync(kFull, ok);  // a prefix of lanes; lane 0 always set
-    const int L = 31 - __clz(b);
-    const int nlo = lo + L * step;
-    len = min(step, lo + len - nlo);
-    lo = nlo;
-  }
-  return lo;
-}
-
-// Each lane's row for its nonzero p, given lo with pos[lo] <= every lane's p: lane m reads the
-// row start pos[lo + 1 + m], each lane counts the starts <= its p by a five-step search over
-// the lanes' sorted values, and lanes past 32 rows (runs of empty rows) go round again.
-__device__ __forceinline__ int sd_batch_rows(const int32_t* __restrict__ pos, int32_t rows,
-                                             int lo, int32_t p, int lane) {
-  int r = lo;
-  bool done = false;
-  for (;;) {
-    const int q = lo + 1 + lane;
-    const int s = q <= rows ? __ldg(pos + q) : INT32_MAX;
-    int c = 0;
-#pragma unroll
-    for (int step = 16; step >= 1; step >>= 1) {
-      const int v = __shfl_sync(kFull, s, c + step - 1);
-      if (v <= p) c += step;
-    }
-    if (__shfl_sync(kFull, s, 31) <= p) c = 32;
-    if (!done && c < 32) {
-      r = lo + c;
-      done = true;
-    }
-    if (__all_sync(kFull, done)) break;
-    lo += 32;
-  }
-  return r;
-}
-
 // Reduce-scatter of eight per-lane partials: lane l ends with the warp-wide sum of partial
 // (l >> 2) & 7.  Halving exchanges over lane bits 4, 3, 2 (4 + 2 + 1 shuffles), then a
 // butterfly over bits 1, 0.
@@ -344,7 +298,7 @@ __global__ void __launch_bounds__(kSdBlock, 2) sddmm_kernel(const SdArgs<P> a) {
   const int64_t pend = min(p0 + (int64_t)kSdWarpNnz, a.nnz);
   bool dok = true;
   if constexpr (P::kChecked) dok = *a.dflag == 0;
-  int lo = sd_find_row(a.pos, a.rows, (int32_t)p0, lane);
+  int lo = warp_find_row(a.pos, a.rows, (int32_t)p0, lane);
   int crow = -1;  // row whose C slice creg holds (CH == 1)
   CR creg[JL];
   bool cok = true;
@@ -363,7 +317,7 @@ __global__ void __launch_bounds__(kSdBlock, 2) sddmm_kernel(const SdArgs<P> a) {
   for (int64_t base = p0; base < pend; base += 32) {
     const int32_t pl = (int32_t)min(base + lane, a.nnz - 1);
     const int kreg = __ldg(a.crd + pl);
-    const int r = sd_batch_rows(a.pos, a.rows, lo, pl, lane);
+    const int r = warp_batch_rows(a.pos, a.rows, lo, pl, lane);
     lo = __shfl_sync(kFull, r, 31);
     V res = V(0);
 #pragma unroll 1  // one group's code: the fully unrolled batch overflows the instruction cache
@@ -488,7 +442,7 @@ __global__ void __launch_bounds__(kStWarps * 32) sddmm_tma_kernel(const SdArgs<P
 
   bool dok = true;
   if constexpr (P::kChecked) dok = *a.dflag == 0;
-  int lo = sd_find_row(a.pos, a.rows, (int32_t)p0, lane);
+  int lo = warp_find_row(a.pos, a.rows, (int32_t)p0, lane);
   int crow = -1;
   CR creg[JL];
   bool cok = true;
@@ -500,7 +454,7 @@ __global__ void __launch_bounds__(kStWarps * 32) sddmm_tma_kernel(const SdArgs<P
     if (g == 0) {  // a new batch of 32 nonzeros: columns and rows, one per lane
       const int32_t pl = (int32_t)min(base + lane, a.nnz - 1);
       kreg = __ldg(a.crd + pl);
-      r = sd_batch_rows(a.pos, a.rows, lo, pl, lane);
+      r = warp_batch_rows(a.pos, a.rows, lo, pl, lane);
       lo = __shfl_sync(kFull, r, 31);
       res = V(0);
     }

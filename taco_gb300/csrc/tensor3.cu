@@ -13,11 +13,13 @@
 // k: T(f,:) = sum_l B(i,k,l) D(l,:) per level-1 fiber f = (i,k) (SpMM over the fiber matrix),
 // then A(i,:) = sum_f C(k_f,:) * T(f,:) over the fibers of i (t3_mttkrp_combine): 2J flops per
 // nonzero plus 2J per fiber, where taco's loop spends 3J per nonzero.  TTM and MTTKRP take the
-// SpMM variant of the fiber product (-1: the library's choice).
+// SpMM variant of the fiber product; for FP64 MTTKRP variant -1 selects the fused kernel
+// (t3_mttkrp_fused), which never writes the fiber rows.
 #include <cstdint>
 #include <cstring>
 
 #include "common.cuh"
+#include "df.cuh"
 #include "kernels.h"
 
 namespace tacogb {
@@ -119,6 +121,121 @@ __global__ void t3_mttkrp_combine(const int32_t* __restrict__ pos1,
       }
     }
     if (on) atomicAdd(A + (crd0 ? (int64_t)__ldg(crd0 + e) : (int64_t)e) * J + j, acc);
+  }
+}
+
+constexpr int kFuWarps = 8;
+constexpr int kFuNnz = 256;  // nonzeros per warp in t3_mttkrp_fused
+
+// Ds[l * J + j] = D(l, j) as double-float pairs; *flag set when an entry is outside the pairs'
+// range (the fused kernel then takes those batches natively).
+__global__ void t3_split_d(const double* __restrict__ D, DF* __restrict__ Ds, int64_t n,
+                           int* __restrict__ flag) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  DF r;
+  if (!split_df(D[i], r.h, r.l)) *flag = 1;
+  Ds[i] = r;
+}
+
+// Fused MTTKRP over 256 consecutive nonzeros per warp (balanced however long the fibers are):
+// lanes over j (32 columns per pass), per nonzero the product B * D(l, j) accumulated in
+// double-float on the FP32 pipe (12 instructions per term; a batch with a value outside the
+// pairs' range runs in native FP64 into a second accumulator), at each fiber end the fiber's sum
+// times C(k, j) added to the row sum of i in FP64, and at each change of i (and at the end of
+// the chunk) that row sum added into A(i, j) atomically.  Replaces the fiber SpMM, its scratch
+// T (nfib x J) and the combine; each nonzero costs a broadcast of its value and column, one
+// 8-byte load of D per lane from L2 and the product.
+__global__ void __launch_bounds__(kFuWarps * 32) t3_mttkrp_fused(
+    const int32_t* __restrict__ pos1, const int32_t* __restrict__ crd0,
+    const int32_t* __restrict__ crd1, const int32_t* __restrict__ pos2,
+    const int32_t* __restrict__ crd2, const double* __restrict__ vals, int32_t n0, int32_t nfib,
+    int64_t nnz, int32_t J, const double* __restrict__ C, const double* __restrict__ D,
+    const DF* __restrict__ Ds, const int* __restrict__ dflag, double* __restrict__ A) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t p0 = ((int64_t)blockIdx.x * kFuWarps + (threadIdx.x >> 5)) * kFuNnz;
+  if (p0 >= nnz) return;
+  const int64_t pend = min(p0 + (int64_t)kFuNnz, nnz);
+  const bool dok = *dflag == 0;
+  const int f_first = warp_find_row(pos2, nfib, (int32_t)p0, lane);
+  const int e_first = warp_find_row(pos1, n0, f_first, lane);
+  for (int32_t j0 = 0; j0 < J; j0 += 32) {
+    const int32_t j = j0 + lane;
+    const bool on = j < J;
+    int lo = f_first;        // fiber search base for the next batch
+    int cf = f_first;        // current fiber
+    int e = e_first;         // its level-0 entry
+    int32_t e_end = __ldg(pos1 + e + 1);
+    double ck = on ? __ldg(C + (int64_t)__ldg(crd1 + cf) * J + j) : 0.0;
+    float s = 0.f, c = 0.f;  // the fiber's double-float sum (hi, unnormalised compensation)
+    double nat = 0.0;        // the fiber's natively summed part
+    double rowsum = 0.0;     // sum over i's fibers so far of C(k, j) * fiber sum
+    for (int64_t base = p0; base < pend; base += 32) {
+      const int32_t pl = (int32_t)min(base + lane, pend - 1);
+      const int32_t lreg = __ldg(crd2 + pl);
+      const double vreg = __ldg(vals + pl);
+      const int freg = warp_batch_rows(pos2, nfib, lo, pl, lane);
+      lo = __shfl_sync(full, freg, 31);
+      DF vs;
+      const bool ok = __all_sync(full, split_df(vreg, vs.h, vs.l)) && dok;
+      const int cnt = (int)min((int64_t)32, pend - base);
+      for (int n0b = 0; n0b < cnt; n0b += 8) {
+        DF d[8];
+        double dn[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int l = __shfl_sync(full, lreg, n0b + q);
+          if (ok) {
+            d[q] = on ? Ds[(int64_t)l * J + j] : DF{0.f, 0.f};
+          } else {
+            dn[q] = on ? __ldg(D + (int64_t)l * J + j) : 0.0;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const int n = n0b + q;
+          if (n >= cnt) break;
+          const int f = __shfl_sync(full, freg, n);
+          if (f != cf) {  // fiber cf ends (warp-uniform)
+            DF t;
+            two_sum(s, c, t.h, t.l);
+            rowsum = __fma_rn(ck, __dadd_rn(df_to_double(t), nat), rowsum);
+            s = c = 0.f;
+            nat = 0.0;
+            while (f >= e_end) {  // entry e ends too
+              if (on) atomicAdd(A + (crd0 ? (int64_t)__ldg(crd0 + e) : (int64_t)e) * J + j, rowsum);
+              rowsum = 0.0;
+              e++;
+              e_end = __ldg(pos1 + e + 1);
+            }
+            cf = f;
+            ck = on ? __ldg(C + (int64_t)__ldg(crd1 + cf) * J + j) : 0.0;
+          }
+          if (ok) {
+            const float vh = __shfl_sync(full, vs.h, n), vl = __shfl_sync(full, vs.l, n);
+            const float ph = __fmul_rn(vh, d[q].h);
+            const float pe = __fmaf_rn(vh, d[q].h, -ph);
+            float cc = __fmaf_rn(vh, d[q].l, c);
+            cc = __fmaf_rn(vl, d[q].h, cc);
+            float s1, er;
+            two_sum(s, ph, s1, er);
+            c = __fadd_rn(cc, __fadd_rn(pe, er));
+            s = s1;
+          } else {
+            nat = __fma_rn(__shfl_sync(full, vreg, n), dn[q], nat);
+          }
+        }
+        float s2, e2;  // renormalise once per eight terms
+        two_sum(s, c, s2, e2);
+        s = s2;
+        c = e2;
+      }
+    }
+    DF t;
+    two_sum(s, c, t.h, t.l);
+    rowsum = __fma_rn(ck, __dadd_rn(df_to_double(t), nat), rowsum);
+    if (on) atomicAdd(A + (crd0 ? (int64_t)__ldg(crd0 + e) : (int64_t)e) * J + j, rowsum);
   }
 }
 
@@ -240,7 +357,28 @@ int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, vo
   TACOGB_CHECK_ARG(B->nnz == 0 || J == 0 || (C != nullptr && D != nullptr),
                    "MTTKRP: null C or D");
   if (abytes) TACOGB_CUDA_TRY(cudaMemsetAsync(A, 0, abytes, st));
-  if ((int64_t)B->nfib * J == 0 || B->n0 == 0) return 0;
+  if ((int64_t)B->nfib * J == 0 || B->n0 == 0 || B->nnz == 0) return 0;
+  if (B->vtype == TACOGB_F64 && variant < 0) {  // fused: no fiber rows in memory
+    const int64_t nd = (int64_t)B->dims[2] * J;
+    DF* Ds = (DF*)scratch(align256((size_t)nd * sizeof(DF)), 7);
+    if (!Ds) return last_code();
+    int* status = device_status();
+    if (!status) return last_code();
+    int* flag = status + kMFlagWord;
+    TACOGB_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    if (nd)
+      TACOGB_LAUNCH("t3_split_d", st,
+                    (t3_split_d<<<(unsigned)((nd + 255) / 256), 256, 0, st>>>((const double*)D, Ds,
+                                                                             nd, flag)));
+    const int64_t warps = (B->nnz + kFuNnz - 1) / kFuNnz;
+    TACOGB_LAUNCH("t3_mttkrp_fused", st,
+                  (t3_mttkrp_fused<<<(unsigned)((warps + kFuWarps - 1) / kFuWarps), kFuWarps * 32,
+                                     0, st>>>(B->pos1, B->crd0, B->crd1, B->pos2, B->crd2,
+                                              (const double*)B->vals, B->n0, B->nfib, B->nnz, J,
+                                              (const double*)C, (const double*)D, Ds, flag,
+                                              (double*)A)));
+    return 0;
+  }
   void* T = scratch(align256((size_t)B->nfib * J * vb), 7);
   if (!T) return last_code();
   const tacogb_csr f = fiber_csr(B);

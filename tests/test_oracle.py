@@ -155,3 +155,30 @@ def test_tensor3_inputs_follow_taco_draws():
     for a, b in zip(csf3((25, 25, 30), co, v)[1:], B[1:]):
         assert np.array_equal(a, b)
     assert np.array_equal(C, g["C"]) and np.array_equal(D, g["D"])
+
+
+def test_format_fixtures_match_oracle():
+    """taco's generated code for DCSR / CSC / sparse-vector SpMV and DCSR SpMM sums in the same
+    order as the CSR restatement: the fixtures equal the oracle's results."""
+    g = _golden("spmv_formats_taco.npz")
+    pos, crd, vals, x = g["pos"], g["crd"], g["vals"], g["x"]
+    y = O.spmv(pos, crd, vals, x)
+    assert normwise(g["y_dcsr"], y) <= 1e-15 and normwise(g["y_csc"], y) <= 1e-15
+    xs = np.zeros_like(x)
+    xs[g["xi"]] = x[g["xi"]]
+    ys = O.spmv(pos, crd, vals, xs)
+    assert np.array_equal(g["ys_crd"], np.flatnonzero(np.diff(pos) > 0))
+    assert normwise(g["ys_vals"], ys[g["ys_crd"]]) <= 1e-15
+    g = _golden("spmm_dcsr_taco_gpu.npz")
+    assert np.array_equal(O.spmm(g["pos"], g["crd"], g["vals"], g["B"]), g["C"])
+
+
+@pytest.mark.skipif(not O.ref_available("spmv_dcsr_sv"), reason="taco generated code not built here")
+def test_taco_generated_sparse_result_kat():
+    """taco's own code for a{Sparse} = B{Sparse,Sparse} * c{Sparse} reproduces the KAT
+    (test/tests-expr_storage.cpp:922-934): coordinates {0,2}, values {0,18}."""
+    from tests.helpers import ref_spmv_formats
+    kp, kc, kv = np.array([0, 1, 1, 3], np.int32), np.array([1, 0, 2], np.int32), np.array([2., 3., 4.])
+    crd, vals = ref_spmv_formats("dcsr_sv", kp, kc, kv, 3, None,
+                                 (np.array([0, 2], np.int32), np.array([2., 3.])))
+    assert list(crd) == [0, 2] and list(vals) == [0, 18]

@@ -110,14 +110,48 @@ def test_ttm_random(L):
     assert normwise(tg.ttm(Bd, cu(C)).cpu().numpy(), ref[fi, fj]) <= F64_TOL
 
 
+# -1: the fused FP64 kernel; a named SpMM variant: the fiber SpMM and the combine
+MTTKRP_PATHS = [-1, "stream_w512_dfs", "merge_w512_native"]
+
+
+def path_variant(p):
+    return p if isinstance(p, int) else tg.spmm_variants().index(p)
+
+
+@pytest.mark.parametrize("path", MTTKRP_PATHS)
 @pytest.mark.parametrize("J", [1, 7, 16, 32, 33, 64, 100])
-def test_mttkrp_random(J):
+def test_mttkrp_random(J, path):
     B = small(seed=40 + J)
     dims = B[0]
     C = W.dense(J + 1, dims[1] * J).reshape(dims[1], J)
     D = W.dense(J + 2, dims[2] * J).reshape(dims[2], J)
-    got = tg.mttkrp(dev_tensor(B), cu(C), cu(D)).cpu().numpy()
+    got = tg.mttkrp(dev_tensor(B), cu(C), cu(D), variant=path_variant(path)).cpu().numpy()
     assert normwise(got, O.mttkrp(B, C, D)) <= F64_TOL
+
+
+@pytest.mark.parametrize("path", MTTKRP_PATHS)
+@pytest.mark.parametrize("case", ["mttkrp_taco_gpu", "mttkrp_taco_cpu"])
+def test_mttkrp_fixtures_every_path(case, path):
+    g, B = fixture(case)
+    A = tg.mttkrp(dev_tensor(B), cu(g["C"]), cu(g["D"]), variant=path_variant(path)).cpu().numpy()
+    assert np.array_equal(A, g["A"])
+
+
+def test_mttkrp_fused_range_fallback():
+    """B values or D entries outside the double-float range: those batches run natively."""
+    B = small(seed=123)
+    dims, crd0, pos1, crd1, pos2, crd2, vals = B
+    vals = vals.copy()
+    vals[::97] *= 1e45
+    B2 = (dims, crd0, pos1, crd1, pos2, crd2, vals)
+    C = W.dense(5, dims[1] * 32).reshape(dims[1], 32)
+    D = W.dense(6, dims[2] * 32).reshape(dims[2], 32)
+    got = tg.mttkrp(dev_tensor(B2), cu(C), cu(D)).cpu().numpy()
+    assert normwise(got, O.mttkrp(B2, C, D)) <= F64_TOL
+    D2 = D.copy()
+    D2[3, 4] = 1e-50
+    got = tg.mttkrp(dev_tensor(B), cu(C), cu(D2)).cpu().numpy()
+    assert normwise(got, O.mttkrp(B, C, D2)) <= F64_TOL
 
 
 def test_sparse_first_level_with_missing_i():
