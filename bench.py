@@ -702,7 +702,7 @@ class MttkrpOp:
                                + e * self.nfib * J)
         self.bytes = (self.roofline_bytes + 4 * (dims[0] + 1) + 4 * self.nfib
                       + e * self.nfib * J + e * dims[1] * J + e * dims[0] * J)
-        self.flops = self.work = 3 * J * self.nnz
+        self.flops = self.work = self.cpu_work = 3 * J * self.nnz
         self.metric = "mttkrp_%s_r%d_gflops" % (args.dtype, J)
         self.workload = "mttkrp_nell2_%d_%d_%d_r%d" % (dims[0], dims[1], dims[2], J)
 
