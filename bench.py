@@ -1269,7 +1269,8 @@ def main():
                    "pack": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,
-                  "variant": "auto" if args.variant < 0 else names_v[args.variant],
+                  "variant": ("auto" if args.variant == -1 else
+                              "fused" if args.variant == -2 else names_v[args.variant]),
                   "l2": "inputs larger than L2 (%.2f GB per step), no flush" % (op.bytes / 1e9),
                   "parallelism": "replicas" if world > 1 else "single"}
         if op.pattern == "spgemm":

@@ -307,9 +307,9 @@ int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, int32_
 int tacogb_ttm_dense(const tacogb_csf3* B, int32_t L, const void* C, void* A, int32_t variant,
                      void* stream);
 /* A(i,j) = B(i,k,l) * C(k,j) * D(l,j), C dims[1] x J, D dims[2] x J, A dims[0] x J, all
- * row-major (taco: :1148-1206, 1526-1580).  FP64 with TACOGB_VARIANT_AUTO: one fused kernel
- * over nonzero chunks; otherwise SpMM of the fibers with D (variant as for tacogb_ttm), then per
- * i the sum of C(k,:) times the fiber rows.  Either way partial row sums are added into A
+ * row-major (taco: :1148-1206, 1526-1580).  SpMM of the fibers with D (variant as for
+ * tacogb_ttm), then per i the sum of C(k,:) times the fiber rows; variant -2 (FP64 only) runs one
+ * fused kernel over nonzero chunks instead.  Either way partial row sums are added into A
  * atomically (the order of those adds is not fixed).  FP64 within 1e-12 normwise of taco's
  * loop. */
 int tacogb_mttkrp(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,

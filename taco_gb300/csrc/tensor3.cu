@@ -13,8 +13,9 @@
 // k: T(f,:) = sum_l B(i,k,l) D(l,:) per level-1 fiber f = (i,k) (SpMM over the fiber matrix),
 // then A(i,:) = sum_f C(k_f,:) * T(f,:) over the fibers of i (t3_mttkrp_combine): 2J flops per
 // nonzero plus 2J per fiber, where taco's loop spends 3J per nonzero.  TTM and MTTKRP take the
-// SpMM variant of the fiber product; for FP64 MTTKRP variant -1 selects the fused kernel
-// (t3_mttkrp_fused), which never writes the fiber rows.
+// SpMM variant of the fiber product; for FP64 MTTKRP variant -2 selects the fused kernel
+// (t3_mttkrp_fused), which never writes the fiber rows but measured slower (5.41 against 4.28 ms
+// on the nell-2-shaped tensor, J = 32: 60 warp-instructions per nonzero against the SpMM's 45).
 #include <cstdint>
 #include <cstring>
 
@@ -124,6 +125,7 @@ __global__ void t3_mttkrp_combine(const int32_t* __restrict__ pos1,
   }
 }
 
+constexpr int kMttkrpFused = -2;  // the variant number of the fused FP64 kernel
 constexpr int kFuWarps = 8;
 constexpr int kFuNnz = 256;  // nonzeros per warp in t3_mttkrp_fused
 
@@ -168,15 +170,28 @@ __global__ void __launch_bounds__(kFuWarps * 32) t3_mttkrp_fused(
     int e = e_first;         // its level-0 entry
     int32_t e_end = __ldg(pos1 + e + 1);
     double ck = on ? __ldg(C + (int64_t)__ldg(crd1 + cf) * J + j) : 0.0;
-    float s = 0.f, c = 0.f;  // the fiber's double-float sum (hi, unnormalised compensation)
-    double nat = 0.0;        // the fiber's natively summed part
-    double rowsum = 0.0;     // sum over i's fibers so far of C(k, j) * fiber sum
+    // the fiber's double-float sum in two interleaved (hi, unnormalised compensation) pairs, so
+    // that consecutive terms do not wait on each other; nat: its natively summed part
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+    double nat = 0.0;
+    double rowsum = 0.0;  // sum over i's fibers so far of C(k, j) * fiber sum
+    auto fiber_sum = [&]() {
+      float s, e;
+      two_sum(s0, s1, s, e);
+      const float c = __fadd_rn(__fadd_rn(c0, c1), e);
+      DF t;
+      two_sum(s, c, t.h, t.l);
+      return __dadd_rn(df_to_double(t), nat);
+    };
     for (int64_t base = p0; base < pend; base += 32) {
       const int32_t pl = (int32_t)min(base + lane, pend - 1);
       const int32_t lreg = __ldg(crd2 + pl);
       const double vreg = __ldg(vals + pl);
       const int freg = warp_batch_rows(pos2, nfib, lo, pl, lane);
       lo = __shfl_sync(full, freg, 31);
+      const int fprev = __shfl_up_sync(full, freg, 1);
+      const unsigned fchg =  // nonzeros that open a new fiber
+          __ballot_sync(full, base + lane < pend && freg != (lane == 0 ? cf : fprev));
       DF vs;
       const bool ok = __all_sync(full, split_df(vreg, vs.h, vs.l)) && dok;
       const int cnt = (int)min((int64_t)32, pend - base);
@@ -196,13 +211,11 @@ __global__ void __launch_bounds__(kFuWarps * 32) t3_mttkrp_fused(
         for (int q = 0; q < 8; q++) {
           const int n = n0b + q;
           if (n >= cnt) break;
-          const int f = __shfl_sync(full, freg, n);
-          if (f != cf) {  // fiber cf ends (warp-uniform)
-            DF t;
-            two_sum(s, c, t.h, t.l);
-            rowsum = __fma_rn(ck, __dadd_rn(df_to_double(t), nat), rowsum);
-            s = c = 0.f;
+          if ((fchg >> n) & 1u) {  // fiber cf ends here (warp-uniform)
+            rowsum = __fma_rn(ck, fiber_sum(), rowsum);
+            s0 = c0 = s1 = c1 = 0.f;
             nat = 0.0;
+            const int f = __shfl_sync(full, freg, n);
             while (f >= e_end) {  // entry e ends too
               if (on) atomicAdd(A + (crd0 ? (int64_t)__ldg(crd0 + e) : (int64_t)e) * J + j, rowsum);
               rowsum = 0.0;
@@ -214,27 +227,30 @@ __global__ void __launch_bounds__(kFuWarps * 32) t3_mttkrp_fused(
           }
           if (ok) {
             const float vh = __shfl_sync(full, vs.h, n), vl = __shfl_sync(full, vs.l, n);
+            float& s = (q & 1) ? s1 : s0;
+            float& c = (q & 1) ? c1 : c0;
             const float ph = __fmul_rn(vh, d[q].h);
             const float pe = __fmaf_rn(vh, d[q].h, -ph);
             float cc = __fmaf_rn(vh, d[q].l, c);
             cc = __fmaf_rn(vl, d[q].h, cc);
-            float s1, er;
-            two_sum(s, ph, s1, er);
+            float sn, er;
+            two_sum(s, ph, sn, er);
             c = __fadd_rn(cc, __fadd_rn(pe, er));
-            s = s1;
+            s = sn;
           } else {
             nat = __fma_rn(__shfl_sync(full, vreg, n), dn[q], nat);
           }
         }
-        float s2, e2;  // renormalise once per eight terms
-        two_sum(s, c, s2, e2);
-        s = s2;
-        c = e2;
+        float t0, t1;  // renormalise once per eight terms
+        two_sum(s0, c0, t0, t1);
+        s0 = t0;
+        c0 = t1;
+        two_sum(s1, c1, t0, t1);
+        s1 = t0;
+        c1 = t1;
       }
     }
-    DF t;
-    two_sum(s, c, t.h, t.l);
-    rowsum = __fma_rn(ck, __dadd_rn(df_to_double(t), nat), rowsum);
+    rowsum = __fma_rn(ck, fiber_sum(), rowsum);
     if (on) atomicAdd(A + (crd0 ? (int64_t)__ldg(crd0 + e) : (int64_t)e) * J + j, rowsum);
   }
 }
@@ -358,7 +374,7 @@ int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, vo
                    "MTTKRP: null C or D");
   if (abytes) TACOGB_CUDA_TRY(cudaMemsetAsync(A, 0, abytes, st));
   if ((int64_t)B->nfib * J == 0 || B->n0 == 0 || B->nnz == 0) return 0;
-  if (B->vtype == TACOGB_F64 && variant < 0) {  // fused: no fiber rows in memory
+  if (B->vtype == TACOGB_F64 && variant == kMttkrpFused) {  // fused: no fiber rows in memory
     const int64_t nd = (int64_t)B->dims[2] * J;
     DF* Ds = (DF*)scratch(align256((size_t)nd * sizeof(DF)), 7);
     if (!Ds) return last_code();

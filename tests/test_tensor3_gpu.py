@@ -110,8 +110,9 @@ def test_ttm_random(L):
     assert normwise(tg.ttm(Bd, cu(C)).cpu().numpy(), ref[fi, fj]) <= F64_TOL
 
 
-# -1: the fused FP64 kernel; a named SpMM variant: the fiber SpMM and the combine
-MTTKRP_PATHS = [-1, "stream_w512_dfs", "merge_w512_native"]
+# -1: the library's choice (fiber SpMM and combine); -2: the fused FP64 kernel; a named SpMM
+# variant: the fiber SpMM with that variant, then the combine
+MTTKRP_PATHS = [-1, -2, "merge_w512_native"]
 
 
 def path_variant(p):
@@ -146,12 +147,13 @@ def test_mttkrp_fused_range_fallback():
     B2 = (dims, crd0, pos1, crd1, pos2, crd2, vals)
     C = W.dense(5, dims[1] * 32).reshape(dims[1], 32)
     D = W.dense(6, dims[2] * 32).reshape(dims[2], 32)
-    got = tg.mttkrp(dev_tensor(B2), cu(C), cu(D)).cpu().numpy()
-    assert normwise(got, O.mttkrp(B2, C, D)) <= F64_TOL
     D2 = D.copy()
     D2[3, 4] = 1e-50
-    got = tg.mttkrp(dev_tensor(B), cu(C), cu(D2)).cpu().numpy()
-    assert normwise(got, O.mttkrp(B, C, D2)) <= F64_TOL
+    for v in (-1, -2):
+        got = tg.mttkrp(dev_tensor(B2), cu(C), cu(D), variant=v).cpu().numpy()
+        assert normwise(got, O.mttkrp(B2, C, D)) <= F64_TOL
+        got = tg.mttkrp(dev_tensor(B), cu(C), cu(D2), variant=v).cpu().numpy()
+        assert normwise(got, O.mttkrp(B, C, D2)) <= F64_TOL
 
 
 def test_sparse_first_level_with_missing_i():
