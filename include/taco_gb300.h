@@ -371,7 +371,9 @@ int _shim_tacogb_spmm_assemble(void** args);
 int _shim_tacogb_spmm_compute(void** args);
 int _shim_tacogb_spmm_evaluate(void** args);
 
-/* C(i,k) = A(i,j) * B(j,k), all CSR.  assemble allocates and fills C's pos and crd and
+/* C(i,k) = A(i,j) * B(j,k), C CSR; A and B CSR, DCSR ({Sparse,Sparse}), CSC ({Dense,Sparse}
+ * ordered {1,0}) or DCSC ({Sparse,Sparse} ordered {1,0}), converted to CSR on the GPU (taco's
+ * spgemm format test, test/tests-scheduling-eval.cpp:655-662).  assemble allocates and fills C's pos and crd and
  * allocates its vals (taco's generated assemble, which leaves vals for compute); compute fills
  * vals over the assembled pattern; evaluate does both.  Result arrays come from malloc for
  * host operands and cudaMallocManaged for GPU operands (taco's allocator choice,

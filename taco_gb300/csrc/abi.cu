@@ -440,7 +440,7 @@ int tacogb_spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_
 
 namespace {
 
-enum { kFmtOther = 0, kFmtCSR, kFmtCSC, kFmtDCSR };
+enum { kFmtOther = 0, kFmtCSR, kFmtCSC, kFmtDCSR, kFmtDCSC };
 
 int mat_format(const taco_tensor_t* A) {
   if (!A || A->order != 2 || !A->mode_types || !A->dimensions || !A->indices) return kFmtOther;
@@ -448,7 +448,7 @@ int mat_format(const taco_tensor_t* A) {
   const bool o10 = A->mode_ordering && A->mode_ordering[0] == 1 && A->mode_ordering[1] == 0;
   const int m0 = A->mode_types[0], m1 = A->mode_types[1];
   if (m0 == taco_mode_dense && m1 == taco_mode_sparse) return o01 ? kFmtCSR : o10 ? kFmtCSC : kFmtOther;
-  if (m0 == taco_mode_sparse && m1 == taco_mode_sparse && o01) return kFmtDCSR;
+  if (m0 == taco_mode_sparse && m1 == taco_mode_sparse) return o01 ? kFmtDCSR : o10 ? kFmtDCSC : kFmtOther;
   return kFmtOther;
 }
 
@@ -472,7 +472,7 @@ int check_any_vector(const taco_tensor_t* t, const char* name) {
 int check_spmv_formats(const taco_tensor_t* y, const taco_tensor_t* A, const taco_tensor_t* x,
                        int* fmt) {
   *fmt = mat_format(A);
-  TACOGB_CHECK_ARG(*fmt != kFmtOther,
+  TACOGB_CHECK_ARG(*fmt != kFmtOther && *fmt != kFmtDCSC,
                    "spmv: A must be CSR, CSC ({Dense,Sparse} ordered {1,0}) or DCSR");
   if (int rc = check_any_vector(y, "spmv result y")) return rc;
   if (int rc = check_any_vector(x, "spmv operand x")) return rc;
@@ -802,9 +802,57 @@ int _shim_tacogb_spmm_evaluate(void** a) {
 
 namespace {
 
-// Device views of a CSR taco_tensor_t; host arrays are staged into slots base..base+2.
+// A matrix operand of SpGEMM as device CSR arrays: CSR as it is; DCSR with its pointer array
+// expanded to every row; CSC transposed on the GPU; DCSC expanded to CSC, then transposed
+// (taco's spgemm format test, test/tests-scheduling-eval.cpp:655-662).  Host arrays are staged
+// into slots base .. base+9.
 int csr_operand(const taco_tensor_t* T, int base, bool with_vals, cudaStream_t st,
                 tacogb_csr& out) {
+  const int fmt = mat_format(T);
+  if (fmt != kFmtCSR) {
+    const int32_t rows = T->dimensions[0], cols = T->dimensions[1];
+    const int vt = value_type_of_csize(T->csize);
+    TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spgemm: unsupported csize %d",
+                     T->csize);
+    const bool doubly = fmt == kFmtDCSR || fmt == kFmtDCSC;
+    const int32_t outer = (fmt == kFmtCSC || fmt == kFmtDCSC) ? cols : rows;
+    const int32_t* p1 = (const int32_t*)T->indices[1][0];
+    TACOGB_CHECK_ARG(p1 != nullptr, "spgemm: null pos");
+    int32_t n0 = outer;
+    if (doubly) {
+      TACOGB_CHECK_ARG(T->indices[0] && T->indices[0][0], "spgemm: null level-0 pos");
+      if (int rc = read_i32((const int32_t*)T->indices[0][0] + 1, &n0)) return rc;
+    }
+    int32_t nnz = 0;
+    if (int rc = read_i32(p1 + n0, &nnz)) return rc;
+    const size_t vb = value_bytes(vt);
+    Operand op, oc, ov;
+    if (int rc = stage_in(op, p1, ((size_t)n0 + 1) * 4, base, st)) return rc;
+    if (int rc = stage_in(oc, T->indices[1][1], (size_t)nnz * 4, base + 1, st)) return rc;
+    if (int rc = stage_in(ov, T->vals, (size_t)nnz * vb, base + 2, st)) return rc;
+    const int32_t* pos = (const int32_t*)op.dev;
+    if (doubly) {  // every row (column) gets its range
+      Operand o0;
+      if (int rc = stage_in(o0, T->indices[0][1], (size_t)n0 * 4, base + 3, st)) return rc;
+      int32_t* full = (int32_t*)stage_buffer(base + 4, ((size_t)outer + 1) * 4);
+      if (!full) return TACOGB_ERR_ALLOC;
+      if (int rc = expand_pos_run((const int32_t*)o0.dev, pos, n0, outer, full, st)) return rc;
+      pos = full;
+    }
+    if (fmt == kFmtDCSR) {
+      out = tacogb_csr{rows, cols, nnz, pos, (const int32_t*)oc.dev, ov.dev, vt};
+      return 0;
+    }
+    int32_t* cpos = (int32_t*)stage_buffer(base + 5, ((size_t)rows + 1) * 4);
+    int32_t* ccrd = (int32_t*)stage_buffer(base + 6, (size_t)nnz * 4);
+    void* cval = stage_buffer(base + 7, (size_t)nnz * vb);
+    if (!cpos || !ccrd || !cval) return TACOGB_ERR_ALLOC;
+    if (int rc = csc_to_csr_run(rows, cols, nnz, pos, (const int32_t*)oc.dev, ov.dev, vt, cpos,
+                                ccrd, cval, st))
+      return rc;
+    out = tacogb_csr{rows, cols, nnz, cpos, ccrd, cval, vt};
+    return 0;
+  }
   const int32_t rows = T->dimensions[0], cols = T->dimensions[1];
   const int32_t* pos = (const int32_t*)T->indices[1][0];
   const int32_t* crd = (const int32_t*)T->indices[1][1];
@@ -826,8 +874,8 @@ int csr_operand(const taco_tensor_t* T, int base, bool with_vals, cudaStream_t s
 
 int check_spgemm(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   if (int rc = check_csr(C, "spgemm result C")) return rc;
-  if (int rc = check_csr(A, "spgemm operand A")) return rc;
-  if (int rc = check_csr(B, "spgemm operand B")) return rc;
+  TACOGB_CHECK_ARG(mat_format(A) != kFmtOther && mat_format(B) != kFmtOther,
+                   "spgemm: operands must be CSR, DCSR, CSC or DCSC");
   TACOGB_CHECK_ARG(A->dimensions[1] == B->dimensions[0], "spgemm: A has %d columns, B has %d rows",
                    A->dimensions[1], B->dimensions[0]);
   TACOGB_CHECK_ARG(C->dimensions[0] == A->dimensions[0] && C->dimensions[1] == B->dimensions[1],
@@ -845,8 +893,8 @@ int tacogb_spgemm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B)
   if (int rc = check_spgemm(C, A, B)) return rc;
   cudaStream_t st = lib_stream();
   tacogb_csr a, b;
-  if (int rc = csr_operand(A, 0, false, st, a)) return rc;
-  if (int rc = csr_operand(B, 3, false, st, b)) return rc;
+  if (int rc = csr_operand(A, 60, false, st, a)) return rc;
+  if (int rc = csr_operand(B, 70, false, st, b)) return rc;
   const int32_t rows = a.rows;
   const bool managed = device_accessible(A->indices[1][0]);
   int32_t* dpos = (int32_t*)stage_buffer(6, ((size_t)rows + 1) * 4);
@@ -875,8 +923,8 @@ int tacogb_spgemm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) 
                    "spgemm: result not assembled");
   cudaStream_t st = lib_stream();
   tacogb_csr a, b, c;
-  if (int rc = csr_operand(A, 0, true, st, a)) return rc;
-  if (int rc = csr_operand(B, 3, true, st, b)) return rc;
+  if (int rc = csr_operand(A, 60, true, st, a)) return rc;
+  if (int rc = csr_operand(B, 70, true, st, b)) return rc;
   if (int rc = csr_operand(C, 6, false, st, c)) return rc;
   const size_t vbytes = (size_t)c.nnz * value_bytes(a.vtype);
   void* dvals = C->vals;

@@ -10,7 +10,9 @@
 // scattered into a zero-filled dense result, or kept as the values of the sparse result (its
 // pattern is crd0).  A CSC matrix is transposed to CSR on the GPU by the COO pack (stable radix
 // sort of (row, column) keys; columns come out ascending in each row).  A sparse vector is
-// scattered into a zero-filled dense one: the products it drops are exact zeros.
+// scattered into a zero-filled dense one: the products it drops are exact zeros.  For SpGEMM a
+// DCSR (or DCSC) operand's pointer array is expanded to every row (or column) and a CSC one
+// transposed, so that the CSR x CSR kernels take every combination of taco's spgemm test.
 #include <cstdint>
 
 #include "common.cuh"
@@ -52,6 +54,24 @@ __global__ void fmt_expand_cols(const int32_t* __restrict__ colpos, int32_t cols
       hi = mid - 1;
   }
   colidx[p] = lo;
+}
+
+// Full pointer array of a doubly compressed level: pos[i] = pos1[e] with e the number of stored
+// outer coordinates crd0 below i (binary search), for i in [0, outer]; rows (or columns) that
+// are not stored get empty ranges.
+__global__ void fmt_expand_pos(const int32_t* __restrict__ crd0, const int32_t* __restrict__ pos1,
+                               int32_t n0, int32_t outer, int32_t* __restrict__ pos) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > outer) return;
+  int lo = 0, hi = n0;  // first e with crd0[e] >= i
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(crd0 + mid) < i)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  pos[i] = __ldg(pos1 + lo);
 }
 
 unsigned blocks_for(int64_t n) { return (unsigned)((n + 255) / 256); }
@@ -163,6 +183,17 @@ int csc_to_csr_run(int32_t rows, int32_t cols, int64_t nnz, const int32_t* colpo
     return rc;
   TACOGB_CHECK_ARG(out_nnz == nnz, "CSC: repeated coordinates (%lld of %lld distinct)",
                    (long long)out_nnz, (long long)nnz);
+  return 0;
+}
+
+int expand_pos_run(const int32_t* crd0, const int32_t* pos1, int32_t n0, int32_t outer,
+                   int32_t* pos, cudaStream_t st) {
+  TACOGB_CHECK_ARG(n0 >= 0 && outer >= 0 && n0 <= outer, "expand: bad sizes");
+  TACOGB_CHECK_ARG(pos != nullptr && pos1 != nullptr && (n0 == 0 || crd0 != nullptr),
+                   "expand: null array");
+  TACOGB_LAUNCH("fmt_expand_pos", st,
+                (fmt_expand_pos<<<blocks_for((int64_t)outer + 1), 256, 0, st>>>(crd0, pos1, n0,
+                                                                                outer, pos)));
   return 0;
 }
 

@@ -56,6 +56,9 @@ int csc_to_csr_run(int32_t rows, int32_t cols, int64_t nnz, const int32_t* colpo
                    int32_t* crd, void* out_vals, cudaStream_t st);
 int densify_run(int32_t n, int64_t k, const int32_t* idx, const void* vals, int32_t vtype,
                 void* out, cudaStream_t st);
+// pos[0..outer] of a doubly compressed level with n0 stored outer coordinates crd0.
+int expand_pos_run(const int32_t* crd0, const int32_t* pos1, int32_t n0, int32_t outer,
+                   int32_t* pos, cudaStream_t st);
 
 // COO -> CSR pack (pack.cu): device arrays in and out; *nnz read back (synchronises).
 int pack_csr(int32_t rows, int32_t cols, int64_t n, const int32_t* coord_rows,

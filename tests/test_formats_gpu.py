@@ -209,3 +209,55 @@ def test_sparse_x_random():
     xd[xi] = xv
     y = spmv_abi(T.csr(pos, crd, vals, [s.rows, s.cols]), taco_sparse_vector(xi, xv, s.cols), s.rows)
     assert normwise(y, O.spmv(pos, crd, vals, xd)) <= TOL
+
+
+def _spgemm_operand(fmt, pos, crd, vals, dims):
+    if fmt == "csr":
+        return T.csr(pos, crd, vals, dims)
+    if fmt == "dcsr":
+        crd0, pos1 = to_dcsr(pos, crd)
+        return taco_dcsr_tensor(crd0, pos1, crd, vals, dims)
+    colpos, rowidx, cv = to_csc(pos, crd, vals, dims[1])
+    if fmt == "csc":
+        return taco_csc_tensor(colpos, rowidx, cv, dims)
+    c0, p1 = to_dcsr(colpos, rowidx)  # DCSC: the stored columns and their ranges
+    p0 = np.array([0, len(c0)], np.int32)
+    t = T.TacoTensor(list(dims), [T.MODE_SPARSE, T.MODE_SPARSE], vals=cv,
+                     index_arrays={0: (p0, c0), 1: (p1, rowidx)}, mode_ordering=[1, 0])
+    t._keep.append(p0)
+    return t
+
+
+def _spgemm_abi(At, Bt, rows, cols):
+    Ct = T.csr_result([rows, cols])
+    assert lib().tacogb_spgemm_evaluate(Ct.ptr, At.ptr, Bt.ptr) == 0, lib().tacogb_last_error()
+    torch.cuda.synchronize()
+    pos = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 0), PI), (rows + 1,)).copy()
+    crd = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 1), PI), (int(pos[-1]),)).copy()
+    val = np.ctypeslib.as_array(ctypes.cast(Ct.vals_ptr, PD), (int(pos[-1]),)).copy()
+    return pos, crd, val
+
+
+@pytest.mark.parametrize("afmt,bfmt", [("csr", "csr"), ("dcsr", "csr"), ("dcsr", "dcsr"),
+                                       ("csr", "csc"), ("dcsr", "dcsc")])
+def test_spgemm_formats_taco_inputs(afmt, bfmt):
+    """taco's spgemm format combinations (test/tests-scheduling-eval.cpp:655-662) on its spgemm
+    inputs: the CSR result bit-exact against the fixture taco's generated code made."""
+    g = np.load(os.path.join(GOLDEN, "spgemm_taco_rand.npz"))
+    n = int(g["K"][0])
+    At = _spgemm_operand(afmt, g["Apos"], g["Acrd"], g["Avals"], [len(g["Apos"]) - 1, n])
+    Bt = _spgemm_operand(bfmt, g["Bpos"], g["Bcrd"], g["Bvals"], [n, n])
+    pos, crd, val = _spgemm_abi(At, Bt, len(g["Apos"]) - 1, n)
+    assert np.array_equal(pos, g["Cpos"]) and np.array_equal(crd, g["Ccrd"])
+    assert np.array_equal(val, g["Cvals"])
+
+
+@pytest.mark.parametrize("afmt,bfmt", [("dcsr", "dcsc"), ("csr", "csc")])
+def test_spgemm_formats_empty_rows_and_columns(afmt, bfmt):
+    pa, ca, va = sparse_rows_matrix(3000, 2000, 5, frac=0.3)
+    pb, cb, vb = sparse_rows_matrix(2000, 2500, 6, frac=0.3)
+    ref = O.spgemm(pa, ca, va, pb, cb, vb, 2500)
+    pos, crd, val = _spgemm_abi(_spgemm_operand(afmt, pa, ca, va, [3000, 2000]),
+                                _spgemm_operand(bfmt, pb, cb, vb, [2000, 2500]), 3000, 2500)
+    assert np.array_equal(pos, ref[0]) and np.array_equal(crd, ref[1])
+    assert np.array_equal(val, ref[2])
