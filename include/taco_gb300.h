@@ -103,6 +103,11 @@ int tacogb_pack_taco(taco_tensor_t* T, const void* buffer, int64_t n);
  * them to tacogb_pack_csr (after copying them to the GPU) for CSR. */
 int tacogb_read_coo(const char* path, int32_t* rows, int32_t* cols, int64_t* n,
                     int32_t** coord_rows, int32_t** coord_cols, double** vals);
+/* A Rutherford-Boeing file as taco's readRB loads it (src/storage/file_io_rb.cpp:319-350): real
+ * unsymmetric assembled (RUA) only, as CSC — colptr (cols + 1), rowidx and vals (nnz), 0-based,
+ * in host memory released with tacogb_free_host.  tacogb_csc_to_csr turns it into CSR. */
+int tacogb_read_rb(const char* path, int32_t* rows, int32_t* cols, int64_t* nnz,
+                   int32_t** colptr, int32_t** rowidx, double** vals);
 void tacogb_free_host(void* p);
 
 /* Diagnostic (no counterpart in taco): random-gather throughput probe.  Launches 4 blocks of 256

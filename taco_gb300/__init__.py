@@ -12,7 +12,7 @@ from ._native import (TACOGB_F64, TACOGB_F32, TACOGB_BF16, VARIANT_AUTO, TacoGBE
 
 __all__ = ["CsrMatrix", "spmv", "spmv_variants", "spmm", "spmm_variants", "spgemm", "pack_csr",
            "sddmm", "sddmm_variants", "CsfTensor", "ttv", "ttm", "mttkrp",
-           "read_coo", "read_csr",
+           "read_coo", "read_csr", "read_csc",
            "SpmvBatch",
            "SpmmBatch",
            "batch_variants", "lib", "check", "TacoGBError",
@@ -248,12 +248,46 @@ def read_coo(path):
     return out
 
 
+def read_csc(path):
+    """(rows, cols, colptr, rowidx, vals) numpy arrays of a Rutherford-Boeing (.rb, RUA) file, as
+    taco's readRB loads it into CSC (tacogb_read_rb)."""
+    import numpy as np
+    L = lib()
+    rows, cols, n = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+    pp, pr, pv = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    check(L.tacogb_read_rb(str(path).encode(), ctypes.byref(rows), ctypes.byref(cols),
+                           ctypes.byref(n), ctypes.byref(pp), ctypes.byref(pr), ctypes.byref(pv)),
+          "tacogb_read_rb")
+    k = n.value
+    try:
+        as_np = lambda p, ct, m: np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ct)),  # noqa
+                                                        (max(m, 1),))[:m].copy()
+        out = (rows.value, cols.value, as_np(pp, ctypes.c_int32, cols.value + 1),
+               as_np(pr, ctypes.c_int32, k), as_np(pv, ctypes.c_double, k))
+    finally:
+        for p in (pp, pr, pv):
+            L.tacogb_free_host(p)
+    return out
+
+
 def read_csr(path, device="cuda"):
-    """A .mtx or .tns file as a CsrMatrix on the GPU: parsed on the host (all threads), packed
-    on the GPU (tacogb_pack_csr), duplicates summed in file order."""
+    """A .mtx, .tns or .rb file as a CsrMatrix on the GPU: parsed on the host (all threads for
+    .mtx/.tns), then packed (tacogb_pack_csr, duplicates summed in file order) or, for a
+    Rutherford-Boeing file's CSC, transposed (tacogb_csc_to_csr) on the GPU."""
     import torch
-    rows, cols, ri, ci, v = read_coo(path)
     t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
+    if str(path).lower().endswith(".rb"):
+        rows, cols, colptr, rowidx, v = read_csc(path)
+        nnz = len(rowidx)
+        pos = torch.empty(rows + 1, dtype=torch.int32, device=device)
+        crd = torch.empty(nnz, dtype=torch.int32, device=device)
+        vals = torch.empty(nnz, dtype=torch.float64, device=device)
+        cp, ri, vv = t(colptr), t(rowidx), t(v)
+        check(lib().tacogb_csc_to_csr(rows, cols, nnz, cp.data_ptr(), ri.data_ptr(), vv.data_ptr(),
+                                      TACOGB_F64, pos.data_ptr(), crd.data_ptr(), vals.data_ptr(),
+                                      None), "tacogb_csc_to_csr")
+        return CsrMatrix(pos, crd, vals, cols)
+    rows, cols, ri, ci, v = read_coo(path)
     return pack_csr(rows, cols, t(ri), t(ci), t(v))
 
 

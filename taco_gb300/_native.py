@@ -104,6 +104,9 @@ SIGNATURES = {
     "tacogb_probe_gather": (I32, [P, I64, P, I64, P, I64, I32, I32, I32, P]),
     "tacogb_pack_csr": (I32, [I32, I32, I64, P, P, P, I32, P, P, P, P, P]),
     "tacogb_pack_taco": (I32, [P, P, I64]),
+    "tacogb_read_rb": (I32, [ctypes.c_char_p, ctypes.POINTER(I32), ctypes.POINTER(I32),
+                             ctypes.POINTER(I64), ctypes.POINTER(P), ctypes.POINTER(P),
+                             ctypes.POINTER(P)]),
     "tacogb_read_coo": (I32, [ctypes.c_char_p, P, P, P, P, P, P]),
     "tacogb_free_host": (None, [P]),
     "tacogb_spmv": (I32, [ctypes.POINTER(Csr), P, P, I32, P]),

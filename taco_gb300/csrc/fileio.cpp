@@ -276,7 +276,101 @@ T* to_malloc(const std::vector<T>& v) {
   return p;
 }
 
+// Rutherford-Boeing, as taco's readRB loads it (src/storage/file_io_rb.cpp:22-88, 142-228,
+// 246-283, 319-350): real unsymmetric assembled matrices only (type RUA, any case), loaded as CSC.
+// Line 2 gives the line counts of the sections (pointers, row indices, values); a fifth header
+// line follows when right-hand sides are present; within each section every whitespace-separated
+// token of the section's lines is read in order (1-based pointers and indices become 0-based).
+int read_rb(const std::vector<const char*>& lines, int32_t* rows, int32_t* cols,
+            std::vector<int32_t>& colptr, std::vector<int32_t>& rowidx, std::vector<double>& vals) {
+  if (lines.size() < 4) return fail("read: %s", "a Rutherford-Boeing file needs four header lines");
+  long cnt[5] = {0, 0, 0, 0, 0};
+  const char* p = lines[1];
+  const char* e = line_end(p);
+  for (int k = 0; k < 5; k++) {
+    const char* t = next_token(p, e);
+    if (!t) return fail("read: %s", "the second header line needs five line counts");
+    char* end;
+    cnt[k] = strtol(t, &end, 10);
+    p = end;
+  }
+  p = lines[2];
+  e = line_end(p);
+  const char* t = next_token(p, e);
+  if (!t || e - t < 3 || (t[0] != 'R' && t[0] != 'r') || (t[1] != 'U' && t[1] != 'u') ||
+      (t[2] != 'A' && t[2] != 'a'))
+    return fail("read: %s", "only real unsymmetric assembled (RUA) Rutherford-Boeing matrices");
+  p = t + 3;
+  long dims[3];
+  for (int k = 0; k < 3; k++) {
+    t = next_token(p, e);
+    if (!t) return fail("read: %s", "the third header line needs rows, columns and entries");
+    char* end;
+    dims[k] = strtol(t, &end, 10);
+    p = end;
+  }
+  if (dims[0] < 0 || dims[1] < 0 || dims[2] < 0 || dims[0] > INT32_MAX || dims[1] > INT32_MAX ||
+      dims[2] > INT32_MAX)
+    return fail("read: %s", "sizes out of range");
+  size_t l = cnt[4] > 0 ? 5 : 4;  // the right-hand side header line, when present, is skipped
+  auto section = [&](long nlines, auto&& take) -> bool {
+    for (long k = 0; k < nlines; k++, l++) {
+      if (l >= lines.size()) return false;
+      const char* q = lines[l];
+      const char* qe = line_end(q);
+      while (const char* tok = next_token(q, qe)) {
+        char* end;
+        take(tok, &end);
+        if (end == tok) return false;
+        q = end;
+      }
+    }
+    return true;
+  };
+  colptr.clear();
+  rowidx.clear();
+  vals.clear();
+  if (!section(cnt[1], [&](const char* tok, char** end) {
+        colptr.push_back((int32_t)strtol(tok, end, 10) - 1);
+      }) ||
+      !section(cnt[2], [&](const char* tok, char** end) {
+        rowidx.push_back((int32_t)strtol(tok, end, 10) - 1);
+      }) ||
+      !section(cnt[3], [&](const char* tok, char** end) { vals.push_back(strtod(tok, end)); }))
+    return fail("read: %s", "a Rutherford-Boeing section is shorter than its header says");
+  if ((long)colptr.size() != dims[1] + 1 || (long)rowidx.size() != dims[2] ||
+      (long)vals.size() != dims[2] || colptr.front() != 0 || colptr.back() != dims[2])
+    return fail("read: %s", "Rutherford-Boeing sections do not match the header's sizes");
+  *rows = (int32_t)dims[0];
+  *cols = (int32_t)dims[1];
+  return 0;
+}
+
 }  // namespace
+
+extern "C" int tacogb_read_rb(const char* path, int32_t* rows, int32_t* cols, int64_t* nnz,
+                              int32_t** colptr, int32_t** rowidx, double** vals) {
+  if (!path || !rows || !cols || !nnz || !colptr || !rowidx || !vals)
+    return fail("read: %s", "null argument");
+  std::string buf;
+  if (int rc = read_file(path, buf)) return rc;
+  Lines L;
+  split_lines(buf.data(), buf.data() + buf.size() - 1, L);
+  std::vector<int32_t> cp, ri;
+  std::vector<double> v;
+  if (int rc = read_rb(L.start, rows, cols, cp, ri, v)) return rc;
+  *colptr = to_malloc(cp);
+  *rowidx = to_malloc(ri);
+  *vals = to_malloc(v);
+  if (!*colptr || !*rowidx || !*vals) {
+    free(*colptr);
+    free(*rowidx);
+    free(*vals);
+    return fail("read: %s", "out of host memory");
+  }
+  *nnz = (int64_t)ri.size();
+  return 0;
+}
 
 extern "C" int tacogb_read_coo(const char* path, int32_t* rows, int32_t* cols, int64_t* n,
                                int32_t** coord_rows, int32_t** coord_cols, double** vals) {

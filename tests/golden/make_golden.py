@@ -262,6 +262,72 @@ def reader_cases():
         save(name.replace(".", "_"), pos=pos, crd=cc, vals=vv)
 
 
+def _write_rb(path, rows, cols, colptr, rowidx, vals, rhs_line=None):
+    """A Rutherford-Boeing file (RUA) in this script's own layout: 10 integers or 4 values per
+    line; with rhs_line, right-hand sides are announced (a fifth header line, no data)."""
+    chunk = lambda xs, k: [xs[i:i + k] for i in range(0, len(xs), k)]  # noqa: E731
+    pl = [" ".join("%d" % (x + 1) for x in c) for c in chunk(list(colptr), 10)]
+    il = [" ".join("%d" % (x + 1) for x in c) for c in chunk(list(rowidx), 10)]
+    vl = [" ".join("%r" % float(x) for x in c) for c in chunk(list(vals), 4)]
+    hdr = ["%-72s%-8s" % ("a test matrix written by make_golden", "GOLDEN"),
+           "%14d%14d%14d%14d%14d" % (len(pl) + len(il) + len(vl), len(pl), len(il), len(vl),
+                                     1 if rhs_line else 0),
+           "RUA%11s%14d%14d%14d%14d" % ("", rows, cols, len(rowidx), 0),
+           "%-16s%-16s%-20s%-20s" % ("(10I8)", "(10I8)", "(4E24.16)", "(4E24.16)" if rhs_line else "")]
+    if rhs_line:
+        hdr.append(rhs_line)
+    with open(path, "w") as f:
+        f.write("\n".join(hdr + pl + il + vl) + "\n")
+
+
+def rb_cases(reference_root="/root/reference"):
+    """Rutherford-Boeing: taco's own test matrix rua_32 (test/data/rua_32.rb and its .mtx twin).
+    taco's CLI crashes on .rb input and output here, so the CSR expected of the .rb file is the
+    one taco's CLI makes of rua_32.mtx; this script writes the matrix again in its own RB layout
+    (read_rua32.rb) and checks that libtacogb's reader gives the same CSC for taco's file and for
+    this one.  read_rhs.rb (a random matrix, right-hand sides announced) checks the fifth header
+    line."""
+    import subprocess
+    import tempfile
+    import taco_gb300 as tg
+    cli = os.path.join(ROOT, "oracle", "_ref", "bin", "taco")
+    src_mtx = os.path.join(reference_root, "test", "data", "rua_32.mtx")
+    src_rb = os.path.join(reference_root, "test", "data", "rua_32.rb")
+    with tempfile.TemporaryDirectory() as d:
+        dst = os.path.join(d, "out.tns")
+        subprocess.run([cli, "B(i,j) = A(i,j)", "-f=A:ds", "-f=B:ds", "-i=A:" + src_mtx,
+                        "-o=B:" + dst, "-time=1"], check=True, cwd=d, stdout=subprocess.DEVNULL)
+        ent = [line.split() for line in open(dst) if line.strip()]
+    rr = np.array([int(e[0]) - 1 for e in ent], np.int64)
+    cc = np.array([int(e[1]) - 1 for e in ent], np.int32)
+    vv = np.array([float(e[2]) for e in ent])
+    o = np.lexsort((cc, rr))
+    rr, cc, vv = rr[o], cc[o], vv[o]
+    rows, cols, colptr, rowidx, cvals = tg.read_csc(src_rb)
+    pos = np.searchsorted(rr, np.arange(rows + 1), side="left").astype(np.int32)
+    save("read_rua32_rb", pos=pos, crd=cc, vals=vv, colptr=colptr, rowidx=rowidx, cvals=cvals,
+         dims=np.array([rows, cols]))
+    out = os.path.join(OUT, "read_rua32.rb")
+    _write_rb(out, rows, cols, colptr, rowidx, cvals)
+    again = tg.read_csc(out)
+    assert again[:2] == (rows, cols)
+    for a, b in zip(again[2:], (colptr, rowidx, cvals)):
+        assert np.array_equal(a, b)
+    # CSR of the CSC read equals taco's CSR of the .mtx twin
+    cr = np.repeat(np.arange(cols, dtype=np.int32), np.diff(colptr))
+    o = np.lexsort((cr, rowidx))
+    assert np.array_equal(rowidx[o], rr) and np.array_equal(cr[o], cc) and np.array_equal(cvals[o], vv)
+    rng = np.random.default_rng(41)
+    r, c = 23, 17
+    dense = np.where(rng.random((r, c)) < 0.3, rng.integers(-40, 41, (r, c)) / 4.0, 0.0)
+    cp = np.concatenate([[0], np.cumsum((dense != 0).sum(axis=0))]).astype(np.int32)
+    ri = np.concatenate([np.flatnonzero(dense[:, j]) for j in range(c)]).astype(np.int32)
+    cv = np.concatenate([dense[np.flatnonzero(dense[:, j]), j] for j in range(c)])
+    _write_rb(os.path.join(OUT, "read_rhs.rb"), r, c, cp, ri, cv,
+              rhs_line="F%13s%14d%14d" % ("", 1, 0))
+    save("read_rhs_rb", colptr=cp, rowidx=ri, cvals=cv, dims=np.array([r, c]))
+
+
 if __name__ == "__main__":
     B.build()
     O.build()
@@ -279,3 +345,4 @@ if __name__ == "__main__":
     format_cases()
     pack_cases()
     reader_cases()
+    rb_cases()

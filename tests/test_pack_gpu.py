@@ -123,7 +123,7 @@ def test_taco_buffer_entry(where):
 
 
 @pytest.mark.parametrize("name", ["read_general.mtx", "read_symmetric.mtx", "read_array.mtx",
-                                  "read_plain.tns"])
+                                  "read_plain.tns", "read_rua32.rb"])
 def test_read_csr_matches_taco(name):
     """File -> host parse -> GPU pack equals what taco's reader and pack make of the file."""
     A = tg.read_csr(os.path.join(GOLDEN, name))
