@@ -48,7 +48,8 @@ def parse(argv=None):
     p.add_argument("--workload", default="spmv_powerlaw",
                    choices=["spmv_powerlaw", "spmv_banded", "spmv_small", "spmm_powerlaw",
                             "spgemm_random", "spgemm_poisson", "batched_spmv", "batched_spmm",
-                            "gather_probe", "pack_powerlaw", "sddmm_powerlaw", "mttkrp_nell2"])
+                            "gather_probe", "pack_powerlaw", "sddmm_powerlaw", "mttkrp_nell2", "ttv_nell2",
+                            "ttm_nell2"])
     p.add_argument("--batch-count", type=int, default=4096, help="matrices of batched_spmv")
     p.add_argument("--select", default="default", choices=["default", "exhaustive", "learned"],
                    help="how batched_spmv picks each matrix's work-unit kind")
@@ -765,7 +766,70 @@ class MttkrpOp:
         return "port", lambda: O.mttkrp(self.B, self.C, self.D), A
 
 
+class Tensor3Op:
+    """TTV (A(i,j) = B(i,j,k) c(k)) or TTM (A(i,j,l) = B(i,j,k) C(k,l), L = 128 as in taco's
+    ttmGPU) over the MTTKRP tensor (nell-2's shape, 7.7e7 synthetic nonzeros), FP64, results per
+    (i,j) fiber.  value = GFLOP/s on 2 flops per nonzero (TTV) or 2 L (TTM); the roofline is on
+    the compulsory bytes (B's level-2 arrays, c or C once, the fiber results written).  CPU
+    baseline: TTV by taco's generated code (dense 12,092 x 9,184 result), TTM by the oracle's
+    loop with per-fiber results (the dense result would be 113 GB)."""
+    unit = "GFLOP/s"
+
+    def __init__(self, args):
+        from taco_gb300 import workloads as W
+        self.args = args
+        self.pattern = args.workload.split("_")[0]
+        self.B = W.tensor3_powerlaw()
+        dims, crd0, pos1, crd1, pos2, crd2, vals = self.B
+        self.rows, self.cols, self.nnz, self.nfib = dims[0], dims[2], len(crd2), len(crd1)
+        self.L = 128 if self.pattern == "ttm" else 1
+        self.C = W.dense(81, dims[2] * self.L).reshape(dims[2], self.L)
+        self.bytes = self.roofline_bytes = (12 * self.nnz + 4 * (self.nfib + 1) + 8 * dims[2] * self.L
+                                            + 8 * self.nfib * self.L)
+        self.flops = self.work = self.cpu_work = 2 * self.L * self.nnz
+        self.metric = "%s_f64_gflops" % self.pattern + ("_l%d" % self.L if self.L > 1 else "")
+        self.workload = "%s_nell2_%d_%d_%d" % (self.pattern, *dims)
+
+    def device(self, torch, tg):
+        Bd = tg.CsfTensor.from_numpy(*self.B)
+        b = Bd.as_csf3()
+        Cd = torch.from_numpy(np.ascontiguousarray(self.C if self.L > 1 else self.C[:, 0])).cuda()
+        out = torch.empty(self.nfib * self.L, dtype=torch.float64, device="cuda")
+        L = tg.lib()
+        keep = (Bd, b, Cd, out)
+        if self.pattern == "ttv":
+            def step(sp):
+                tg.check(L.tacogb_ttv(ctypes.byref(b), Cd.data_ptr(), out.data_ptr(), sp), "ttv")
+        else:
+            def step(sp):
+                tg.check(L.tacogb_ttm(ctypes.byref(b), self.L, Cd.data_ptr(), out.data_ptr(),
+                                      self.args.variant, sp), "ttm")
+        return step, keep
+
+    def abi(self, torch, tg, T):
+        return None
+
+    def cpu(self):
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        dims, crd0, pos1, crd1, pos2, crd2, vals = self.B
+        if self.pattern == "ttv" and O.ref_available("ttv"):
+            L = O.ref_lib("ttv")
+            A = np.empty((dims[0], dims[1]))
+            c = np.ascontiguousarray(self.C[:, 0])
+            Bt, Ct, At = T.csf3(*self.B), T.dense(c, [dims[2]]), T.dense(A, [dims[0], dims[1]])
+            return "reference", lambda: L.compute(At.ptr, Bt.ptr, Ct.ptr), (Bt, Ct, At, A, c)
+        out = np.empty(self.nfib * self.L)
+        lib = O.lib()
+        C = np.ascontiguousarray(self.C)
+        return "port", lambda: lib.oracle_ttm_fibers_f64(
+            self.L, self.nfib, pos2.ctypes.data, crd2.ctypes.data, vals.ctypes.data,
+            C.ctypes.data, out.ctypes.data), (out, C)
+
+
 def make_op(args):
+    if args.workload in ("ttv_nell2", "ttm_nell2"):
+        return Tensor3Op(args)
     if args.workload == "mttkrp_nell2":
         return MttkrpOp(args)
     if args.workload == "sddmm_powerlaw":
@@ -1236,8 +1300,9 @@ def main():
     del keep
 
     e2e = None
-    if args.e2e_steps > 0:
-        astep, akeep, h2d, d2h, api = op.abi(torch, tg, T)
+    abi = op.abi(torch, tg, T) if args.e2e_steps > 0 else None
+    if abi is not None:
+        astep, akeep, h2d, d2h, api = abi
         for _ in range(2):
             astep()
         if world > 1:
@@ -1265,7 +1330,8 @@ def main():
     if rank == 0:
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
                    "sddmm": tg.sddmm_variants, "spgemm": lambda: ["default"],
-                   "mttkrp": tg.spmm_variants,
+                   "mttkrp": tg.spmm_variants, "ttm": tg.spmm_variants,
+                   "ttv": lambda: ["default"],
                    "pack": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,

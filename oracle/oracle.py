@@ -62,6 +62,7 @@ def lib():
         L.oracle_ttv_f64.argtypes = [I32, I32, I32] + [P] * 8
         L.oracle_ttm_f64.argtypes = [I32, I32, I32, I32] + [P] * 8
         L.oracle_mttkrp_f64.argtypes = [I32, I32, I32] + [P] * 9
+        L.oracle_ttm_fibers_f64.argtypes = [I32, I32] + [P] * 5
         L.oracle_pack_csr.restype = I64
         L.oracle_pack_csr.argtypes = [I32, I32, I64, P, P, P, P, P, P]
         L.oracle_num_threads.restype = I32

@@ -324,3 +324,19 @@ void oracle_mttkrp_f64(int32_t I, int32_t J, int32_t n0, const int32_t* crd0,
     }
   }
 }
+
+/* TTM with the result kept per (i,j) fiber (out[f * L + l]), the loop of oracle_ttm_f64 without
+ * the dense I x J x L array, for sizes where that array cannot be held. */
+void oracle_ttm_fibers_f64(int32_t L, int32_t nfib, const int32_t* pos2, const int32_t* crd2,
+                           const double* bv, const double* C, double* out) {
+#pragma omp parallel for schedule(static)
+  for (int32_t f = 0; f < nfib; f++) {
+    double* o = out + (int64_t)f * L;
+    for (int32_t l = 0; l < L; l++) o[l] = 0.0;
+    for (int32_t p = pos2[f]; p < pos2[f + 1]; p++) {
+      const double b = bv[p];
+      const double* cr = C + (int64_t)crd2[p] * L;
+      for (int32_t l = 0; l < L; l++) o[l] = o[l] + b * cr[l];
+    }
+  }
+}
