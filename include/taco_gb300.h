@@ -223,7 +223,7 @@ int tacogb_mlp_grad(const float* params, const float* norm, const float* X, cons
 int tacogb_mlp_train(float* params, const float* norm, const float* X, const float* Y,
                      const float* M, int32_t n, int32_t steps, int32_t step0, float lr,
                      float* adam_state, float* losses, void* stream);
-/* Exhaustive autotuner, the model's judge and fallback: plans the batch once per kind (every
+/* Exhaustive autotuner, the model's reference labels and fallback: plans the batch once per kind (every
  * matrix with that kind), runs it reps times after one warm-up, keeps each matrix's minimum
  * cycles (tacogb_batch_matrix_cycles) and writes the cheapest kind per matrix to the host array
  * kinds; cycles (host, count x TACOGB_MLP_KINDS, may be NULL) receives the table.  x and y are

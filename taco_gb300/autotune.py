@@ -3,7 +3,8 @@ model trained on that database with the library's own GPU kernels.
 
     features(mats)                 sparsity features (tacogb_batch_features, on the GPU)
     exhaustive(mats, xs, ys)       per-matrix cycles of every work-unit kind and the argmin
-                                   (tacogb_batch_autotune: the judge and the fallback)
+                                   (tacogb_batch_autotune: the labels the model is scored
+                                   against, and the fallback)
     CostModel                      10 -> 32 -> 32 -> 6 ReLU network; fit() runs
                                    tacogb_mlp_train (forward, backward and Adam kernels),
                                    predict() tacogb_mlp_predict
