@@ -17,7 +17,8 @@
 // Work decomposition: per row, the product count P_i = sum of B-row lengths over A's row.  Rows
 // are binned by P_i; each bin runs expand-sort-compress (ESC) on (column, sequence) keys:
 //   bin 1  P <= 32     one warp per row, keys in registers, warp bitonic sort by shuffles
-//   bin 2  P <= 256    one warp per row, bitonic sort in the warp's shared-memory slice
+//   bin 2  P <= 256    one warp per row, bitonic sort in registers (P <= 128: two or four keys
+//                      per lane, shuffles) or in the warp's shared-memory slice
 //   bin 3  P <= 4096   one CTA per row, bitonic sort in shared memory
 //   bin 4  P >  4096   one CTA per row over a dense per-CTA accumulator in global scratch
 //                      (column bitmap for the pattern, stamp + value arrays for the numbers)
@@ -246,6 +247,93 @@ spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
 
 // ---- bin 2: P <= 256, one warp per row, shared memory -------------------------------------
 
+// Bitonic sort of a warp's 32*R keys (and payloads) held in registers, element r*32 + lane in
+// key[r]: strides of 32 and more swap registers within a lane, shorter ones exchange by shuffle.
+// Ascending; no shared memory, so the sort does not occupy the shared-memory pipe.
+template <int R, typename V>
+__device__ __forceinline__ void reg_bitonic(uint64_t (&key)[R], V (&val)[R]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const int jr = j >> 5;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          if (r & jr) continue;
+          const int e = r * 32 + lane;
+          const bool up = (e & k) == 0;
+          const uint64_t a = key[r], b = key[r | jr];
+          if ((a > b) == up) {
+            key[r] = b;
+            key[r | jr] = a;
+            const V t = val[r];
+            val[r] = val[r | jr];
+            val[r | jr] = t;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const int e = r * 32 + lane;
+          const uint64_t ok = __shfl_xor_sync(0xffffffffu, key[r], j);
+          const V ov = __shfl_xor_sync(0xffffffffu, val[r], j);
+          const bool up = (e & k) == 0;
+          const bool lower = (lane & j) == 0;
+          const bool take = lower == up ? ok < key[r] : ok > key[r];
+          if (take) {
+            key[r] = ok;
+            val[r] = ov;
+          }
+        }
+      }
+    }
+  }
+}
+
+// Rows of at most 32*R products: each lane computes products lane, lane + 32, ... by walking
+// A's row (as bin 1 does), sorts them in registers, then leaves them in the warp's shared slice
+// for the run detection and emission of esc_emit_warp.
+template <int R, int MODE, typename V>
+__device__ __forceinline__ void bin2_row_regs(const int32_t* __restrict__ Apos,
+                                              const int32_t* __restrict__ Acrd,
+                                              const V* __restrict__ Avals,
+                                              const int32_t* __restrict__ Bpos,
+                                              const int32_t* __restrict__ Bcrd,
+                                              const V* __restrict__ Bvals, int row, uint64_t* skey,
+                                              V* sval) {
+  const int lane = threadIdx.x & 31;
+  uint64_t key[R];
+  V val[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    key[r] = ~0ull;
+    val[r] = V();
+  }
+  int seq0 = 0;
+  for (int32_t q = __ldg(Apos + row); q < __ldg(Apos + row + 1); q++) {
+    const int32_t j = __ldg(Acrd + q);
+    const int32_t b0 = __ldg(Bpos + j), len = __ldg(Bpos + j + 1) - b0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int u = r * 32 + lane - seq0;
+      if (u >= 0 && u < len) {
+        key[r] = esc_key(__ldg(Bcrd + b0 + u), r * 32 + lane);
+        if (MODE == 2) val[r] = mul_rn(Avals[q], Bvals[b0 + u]);
+      }
+    }
+    seq0 += len;
+  }
+  reg_bitonic<R>(key, val);
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    skey[r * 32 + lane] = key[r];
+    if (MODE == 2) sval[r * 32 + lane] = val[r];
+  }
+  __syncwarp();
+}
+
 template <int MODE, typename V>
 __global__ void __launch_bounds__(256)
 spgemm_bin2(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
@@ -266,10 +354,16 @@ spgemm_bin2(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
     const int P = (int)prod[row];
     int cap = 32;
     while (cap < P) cap <<= 1;
-    esc_expand<MODE == 2>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, lane, 32);
-    for (int e = P + lane; e < cap; e += 32) key[e] = ~0ull;
-    __syncwarp();
-    smem_bitonic(key, val, cap, lane, 32, [] __device__() { __syncwarp(); });
+    if (cap <= 64) {
+      bin2_row_regs<2, MODE>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
+    } else if (cap <= 128) {
+      bin2_row_regs<4, MODE>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
+    } else {
+      esc_expand<MODE == 2>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, lane, 32);
+      for (int e = P + lane; e < cap; e += 32) key[e] = ~0ull;
+      __syncwarp();
+      smem_bitonic(key, val, cap, lane, 32, [] __device__() { __syncwarp(); });
+    }
     esc_emit_warp<MODE>(key, val, P, row, Cpos, cnt, Ccrd, Cvals);
     __syncwarp();
   }
