@@ -249,8 +249,9 @@ spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
 
 // Bitonic sort of a warp's 32*R keys (and payloads) held in registers, element r*32 + lane in
 // key[r]: strides of 32 and more swap registers within a lane, shorter ones exchange by shuffle.
-// Ascending; no shared memory, so the sort does not occupy the shared-memory pipe.
-template <int R, typename V>
+// Ascending; no shared memory, so the sort does not occupy the shared-memory pipe.  Without
+// VALS (the symbolic and fill phases) the payloads are left alone.
+template <int R, bool VALS, typename V>
 __device__ __forceinline__ void reg_bitonic(uint64_t (&key)[R], V (&val)[R]) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -268,9 +269,11 @@ __device__ __forceinline__ void reg_bitonic(uint64_t (&key)[R], V (&val)[R]) {
           if ((a > b) == up) {
             key[r] = b;
             key[r | jr] = a;
-            const V t = val[r];
-            val[r] = val[r | jr];
-            val[r | jr] = t;
+            if (VALS) {
+              const V t = val[r];
+              val[r] = val[r | jr];
+              val[r | jr] = t;
+            }
           }
         }
       } else {
@@ -278,13 +281,14 @@ __device__ __forceinline__ void reg_bitonic(uint64_t (&key)[R], V (&val)[R]) {
         for (int r = 0; r < R; r++) {
           const int e = r * 32 + lane;
           const uint64_t ok = __shfl_xor_sync(0xffffffffu, key[r], j);
-          const V ov = __shfl_xor_sync(0xffffffffu, val[r], j);
+          V ov = V();
+          if (VALS) ov = __shfl_xor_sync(0xffffffffu, val[r], j);
           const bool up = (e & k) == 0;
           const bool lower = (lane & j) == 0;
           const bool take = lower == up ? ok < key[r] : ok > key[r];
           if (take) {
             key[r] = ok;
-            val[r] = ov;
+            if (VALS) val[r] = ov;
           }
         }
       }
@@ -325,7 +329,7 @@ __device__ __forceinline__ void bin2_row_regs(const int32_t* __restrict__ Apos,
     }
     seq0 += len;
   }
-  reg_bitonic<R>(key, val);
+  reg_bitonic<R, MODE == 2>(key, val);
 #pragma unroll
   for (int r = 0; r < R; r++) {
     skey[r * 32 + lane] = key[r];
