@@ -799,7 +799,8 @@ class Tensor3Op:
         keep = (Bd, b, Cd, out)
         if self.pattern == "ttv":
             def step(sp):
-                tg.check(L.tacogb_ttv(ctypes.byref(b), Cd.data_ptr(), out.data_ptr(), sp), "ttv")
+                tg.check(L.tacogb_ttv(ctypes.byref(b), Cd.data_ptr(), out.data_ptr(),
+                                      self.args.variant, sp), "ttv")
         else:
             def step(sp):
                 tg.check(L.tacogb_ttm(ctypes.byref(b), self.L, Cd.data_ptr(), out.data_ptr(),
@@ -1331,7 +1332,7 @@ def main():
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
                    "sddmm": tg.sddmm_variants, "spgemm": lambda: ["default"],
                    "mttkrp": tg.spmm_variants, "ttm": tg.spmm_variants,
-                   "ttv": lambda: ["default"],
+                   "ttv": tg.spmv_variants,
                    "pack": lambda: ["default"]}[op.pattern]()
         config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
                   "bytes_per_step": op.bytes,

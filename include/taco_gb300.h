@@ -300,9 +300,11 @@ typedef struct tacogb_csf3 {
 
 /* A(i,j) = B(i,j,k) * c(k) (taco: test/tests-scheduling-eval.cpp:993-1043, 1474-1524).
  * tacogb_ttv writes one value per fiber (out[f] for fiber f = (i,j)); tacogb_ttv_dense taco's
- * dense dims[0] x dims[1] result, zero where B has no fiber.  SpMV over the fibers. */
-int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, void* stream);
-int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, void* stream);
+ * dense dims[0] x dims[1] result, zero where B has no fiber.  SpMV over the fibers (variant: a
+ * tacogb_spmv variant, TACOGB_VARIANT_AUTO for the library's choice). */
+int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, int32_t variant, void* stream);
+int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, int32_t variant,
+                     void* stream);
 /* A(i,j,l) = B(i,j,k) * C(k,l), C dims[2] x L row-major (taco: :1094-1146, 1420-1472).
  * tacogb_ttm writes one row of L values per fiber (nfib x L); tacogb_ttm_dense the dense
  * dims[0] x dims[1] x L result.  SpMM over the fibers (variant: a tacogb_spmm variant,

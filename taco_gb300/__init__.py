@@ -96,7 +96,7 @@ class CsfTensor:
         return c
 
 
-def ttv(B, c, dense=False, stream=None):
+def ttv(B, c, dense=False, variant=VARIANT_AUTO, stream=None):
     """A(i,j) = B(i,j,k) * c(k): one value per (i,j) fiber of B (tacogb_ttv) or, with dense=True,
     taco's dense dims[0] x dims[1] result (tacogb_ttv_dense)."""
     import torch
@@ -104,7 +104,8 @@ def ttv(B, c, dense=False, stream=None):
     shape = (B.dims[0], B.dims[1]) if dense else (B.nfib,)
     out = torch.empty(shape, dtype=B.vals.dtype, device=B.vals.device)
     fn = lib().tacogb_ttv_dense if dense else lib().tacogb_ttv
-    check(fn(ctypes.byref(b), c.data_ptr(), out.data_ptr(), _stream_ptr(stream)), "tacogb_ttv")
+    check(fn(ctypes.byref(b), c.data_ptr(), out.data_ptr(), variant, _stream_ptr(stream)),
+          "tacogb_ttv")
     return out
 
 

@@ -150,8 +150,8 @@ SIGNATURES = {
     "tacogb_spmv_csc": (I32, [ctypes.POINTER(Csr), P, P, P]),
     "tacogb_csc_to_csr": (I32, [I32, I32, I64, P, P, P, I32, P, P, P, P]),
     "tacogb_densify": (I32, [I32, I64, P, P, I32, P, P]),
-    "tacogb_ttv": (I32, [ctypes.POINTER(Csf3), P, P, P]),
-    "tacogb_ttv_dense": (I32, [ctypes.POINTER(Csf3), P, P, P]),
+    "tacogb_ttv": (I32, [ctypes.POINTER(Csf3), P, P, I32, P]),
+    "tacogb_ttv_dense": (I32, [ctypes.POINTER(Csf3), P, P, I32, P]),
     "tacogb_ttm": (I32, [ctypes.POINTER(Csf3), I32, P, P, I32, P]),
     "tacogb_ttm_dense": (I32, [ctypes.POINTER(Csf3), I32, P, P, I32, P]),
     "tacogb_mttkrp": (I32, [ctypes.POINTER(Csf3), I32, P, P, P, I32, P]),

@@ -1144,11 +1144,12 @@ int _shim_tacogb_sddmm_evaluate(void** a) {
 // TTV, TTM and MTTKRP over B {Sparse,Sparse,Sparse} or {Dense,Sparse,Sparse}
 // (test/tests-scheduling-eval.cpp:993-1206, 1420-1580), dense results.
 
-int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, void* stream) {
-  return ttv_run(B, c, out, false, (cudaStream_t)stream);
+int tacogb_ttv(const tacogb_csf3* B, const void* c, void* out, int32_t variant, void* stream) {
+  return ttv_run(B, c, out, false, variant, (cudaStream_t)stream);
 }
-int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, void* stream) {
-  return ttv_run(B, c, A, true, (cudaStream_t)stream);
+int tacogb_ttv_dense(const tacogb_csf3* B, const void* c, void* A, int32_t variant,
+                     void* stream) {
+  return ttv_run(B, c, A, true, variant, (cudaStream_t)stream);
 }
 int tacogb_ttm(const tacogb_csf3* B, int32_t L, const void* C, void* out, int32_t variant,
                void* stream) {
@@ -1338,7 +1339,7 @@ int tacogb_ttv_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c) {
   const size_t ob[1] = {(size_t)c->dimensions[0] * vb};
   return t3_compute(A, B, (size_t)A->dimensions[0] * A->dimensions[1] * vb, 1, ops, ob,
                     [](const tacogb_csf3& b, const void* const* d, void* a, cudaStream_t st) {
-                      return ttv_run(&b, d[0], a, true, st);
+                      return ttv_run(&b, d[0], a, true, TACOGB_VARIANT_AUTO, st);
                     });
 }
 int tacogb_ttv_evaluate(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* c) {

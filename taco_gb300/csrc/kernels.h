@@ -40,7 +40,8 @@ int sddmm_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, void
               int64_t out_ld, int variant, cudaStream_t st);
 
 // Order-3 kernels (tensor3.cu); dense selects taco's dense result form.
-int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStream_t st);
+int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, int variant,
+            cudaStream_t st);
 int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense, int variant,
             cudaStream_t st);
 int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,

@@ -294,7 +294,8 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace
 
-int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStream_t st) {
+int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, int variant,
+            cudaStream_t st) {
   if (int rc = check_csf3(B, "TTV")) return rc;
   const size_t vb = vsize(B->vtype);
   TACOGB_CHECK_ARG(B->nnz == 0 || c != nullptr, "TTV: null c");
@@ -310,7 +311,7 @@ int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStre
     if (int rc = fiber_dest(B, ws, st, dest)) return rc;
     void* y = ws + align256((size_t)B->nfib * 8);
     const tacogb_csr f = fiber_csr(B);
-    if (int rc = spmv_run(&f, c, y, TACOGB_VARIANT_AUTO, st)) return rc;
+    if (int rc = spmv_run(&f, c, y, variant, st)) return rc;
     if (B->vtype == TACOGB_F64)
       TACOGB_LAUNCH("t3_scatter_vals", st,
                     (t3_scatter_vals<double><<<(unsigned)((B->nfib + 255) / 256), 256, 0, st>>>(
@@ -324,7 +325,7 @@ int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, cudaStre
   TACOGB_CHECK_ARG(B->nfib == 0 || out != nullptr, "TTV: null result");
   if (B->nfib == 0) return 0;
   const tacogb_csr f = fiber_csr(B);
-  return spmv_run(&f, c, out, TACOGB_VARIANT_AUTO, st);
+  return spmv_run(&f, c, out, variant, st);
 }
 
 int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense, int variant,

@@ -88,15 +88,21 @@ def small(dims=(300, 200, 400), fib=20.0, leaf=8.0, seed=5):
     return W.tensor3_powerlaw(dims=dims, fib_mean=fib, leaf_mean=leaf, seed=seed)
 
 
+def spmv_variant_names():
+    return tg.spmv_variants()
+
+
 @pytest.mark.parametrize("seed", [1, 2])
 def test_ttv_random(seed):
+    """The library's SpMV choice and every SpMV variant on the fiber matrix."""
     B = small(seed=seed)
     c = W.dense(seed + 10, B[0][2])
     ref = O.ttv(B, c)
     Bd = dev_tensor(B)
-    assert normwise(tg.ttv(Bd, cu(c), dense=True).cpu().numpy(), ref) <= F64_TOL
     fi, fj = fiber_coords(B)
-    assert normwise(tg.ttv(Bd, cu(c)).cpu().numpy(), ref[fi, fj]) <= F64_TOL
+    for v in [-1] + list(range(len(spmv_variant_names()))):
+        assert normwise(tg.ttv(Bd, cu(c), dense=True, variant=v).cpu().numpy(), ref) <= F64_TOL, v
+        assert normwise(tg.ttv(Bd, cu(c), variant=v).cpu().numpy(), ref[fi, fj]) <= F64_TOL, v
 
 
 @pytest.mark.parametrize("L", [1, 7, 32, 64, 100, 128])
