@@ -917,14 +917,51 @@ def time_cpu(op, budget_s=8.0, reps=None):
     return kind, ncores, float(np.median(times)), len(times)
 
 
+def workload_config(op, world):
+    """The workload as both arms print it: the same dict from the same op, so that a line of
+    this implementation and a line of taco's generated code name one configuration.  Results
+    and implementation choices (variant, threads, derived rates) go outside it."""
+    if op.pattern == "batch":
+        c = {"workload": op.workload, "matrices": op.count, "rows": op.rows}
+        if getattr(op, "N", None):
+            c["n"] = op.N
+    else:
+        c = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
+             "bytes_per_step": op.bytes,
+             "l2": "inputs larger than L2 (%.2f GB per step), no flush" % (op.bytes / 1e9)}
+        if op.pattern == "spgemm":
+            c.update({"nnz_c": op.nnzC, "products": op.products})
+        for key, attr in (("n", "N"), ("j", "J")):
+            if getattr(op, attr, None) is not None and op.pattern in ("spmm", "sddmm", "mttkrp",
+                                                                       "ttm"):
+                c[key] = getattr(op, attr)
+    c["parallelism"] = "replicas" if world > 1 else "single"
+    return c
+
+
+def mapped_libraries():
+    """Shared objects of this repository mapped into the process (from /proc/self/maps)."""
+    out = set()
+    try:
+        for line in open("/proc/self/maps"):
+            path = line.split()[-1] if len(line.split()) >= 6 else ""
+            if path.startswith(ROOT) and ".so" in path:
+                out.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
 def run_reference(args):
     rank, _, world = dist_env()
     if rank != 0:
         return
     from oracle import oracle as O
-    from taco_gb300 import build as Bd
-    Bd.build()
+    from taco_gb300 import _native as N
     O.build()
+    # the inputs come from the oracle's own build of the generators: this arm maps no library
+    # of taco_gb300
+    N.set_generator_library(O.generator_library())
     op = make_op(args)
     ncores = os.cpu_count() or 1
     O.ref_set_threads(ncores)
@@ -954,14 +991,19 @@ def run_reference(args):
            "n_gpus": world, "steps": steps, "warmup": args.warmup,
            "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": op.workload, "rows": op.rows, "nnz": op.nnz,
-                      "work_per_step": work, "code": code, "threads": ncores},
+           "config": workload_config(op, world),
            "cpu_baseline": {"value": v, "unit": unit, "cores": ncores, "kind": kind,
-                            "sample": sample},
+                            "sample": sample, "code": code, "work_per_step": work},
            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if op.pattern != "batch":
         out["gflops"] = getattr(op, "cpu_work" if op.pattern == "sddmm" else "flops",
                                 op.flops) * steps / dt / 1e9
+    libs = mapped_libraries()
+    product = [l for l in libs if l.startswith("taco_gb300")]
+    if product:
+        raise RuntimeError("the reference arm mapped this repository's product libraries: %s"
+                           % product)
+    out["native_libs"] = libs
     print(json.dumps(out), flush=True)
     del keep
 
@@ -1097,8 +1139,8 @@ def main_batch(args, torch, tg, T, L, rank, world):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32c" if vkey == "v32" else "f64", "data": "synthetic",
-           "config": {"workload": op.workload, "matrices": op.count, "rows": op.rows,
-                      "nnz": op.nnz, "bytes_per_step": op.bytes, "selection": how,
+           "config": workload_config(op, world),
+           "detail": {"nnz": op.nnz, "bytes_per_step": op.bytes, "selection": how,
                       "kinds": kinds_used,
                       "l2": "inputs larger than L2 (%.1f GB per step), no flush" % (op.bytes / 1e9)},
            "fp64_per_matrix": {"gflops": op.flops / (ms64 / 1e3) / 1e9, "ms_per_step": ms64,
@@ -1191,8 +1233,8 @@ def main_batch_spmm(args, torch, tg, L, rank):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": {"f64": "f64", "f32": "f32c", "bf16": "bf16b_f32"}[args.dtype],
            "data": "synthetic",
-           "config": {"workload": op.workload, "matrices": op.count, "rows": op.rows,
-                      "nnz": op.nnz, "n": op.N, "bytes_per_step": op.bytes,
+           "config": workload_config(op, 1),
+           "detail": {"nnz": op.nnz, "bytes_per_step": op.bytes,
                       "l2": "inputs larger than L2 (%.1f GB per step), no flush" % (op.bytes / 1e9)},
            "fp64_per_matrix": {"gflops": op.flops / (ms64 / 1e3) / 1e9, "ms_per_step": ms64,
                                "launch": "tacogb_spmm merge_w512_native FP64, one call per "
@@ -1334,27 +1376,23 @@ def main():
                    "mttkrp": tg.spmm_variants, "ttm": tg.spmm_variants,
                    "ttv": tg.spmv_variants,
                    "pack": lambda: ["default"]}[op.pattern]()
-        config = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
-                  "bytes_per_step": op.bytes,
-                  "variant": ("auto" if args.variant == -1 else
-                              "fused" if args.variant == -2 else names_v[args.variant]),
-                  "l2": "inputs larger than L2 (%.2f GB per step), no flush" % (op.bytes / 1e9),
-                  "parallelism": "replicas" if world > 1 else "single"}
+        config = workload_config(op, world)
+        variant = ("auto" if args.variant == -1 else "fused" if args.variant == -2
+                   else names_v[args.variant])
+        derived = {}
         if op.pattern == "spgemm":
-            config.update({"nnz_c": op.nnzC, "products": op.products,
-                           "products_per_s": op.products * args.steps * world / (ms / 1e3),
-                           "symbolic_bytes": op.sym_bytes, "numeric_bytes": op.num_bytes})
+            derived.update({"products_per_s": op.products * args.steps * world / (ms / 1e3),
+                            "symbolic_bytes": op.sym_bytes, "numeric_bytes": op.num_bytes})
         if op.pattern == "spmm":
-            config["n"] = op.N
-            config["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9
+            derived["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9
         if op.pattern == "sddmm":
-            config["j"] = op.J
-            config["compulsory_gbs"] = op.bytes * args.steps * world / (ms / 1e3) / 1e9
-            config["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9
+            derived["compulsory_gbs"] = op.bytes * args.steps * world / (ms / 1e3) / 1e9
+            derived["gather_model_gbs"] = op.gather_bytes * args.steps * world / (ms / 1e3) / 1e9
         out = {"metric": op.metric, "value": value, "unit": unit,
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": args.dtype, "data": "synthetic", "config": config,
+               "variant": variant, "derived": derived,
                "pct_of_peak": value / peak if unit == "GB/s" else None, "gflops": op.flops * args.steps * world / (ms / 1e3) / 1e9,
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clocks,
@@ -1367,6 +1405,8 @@ def main():
 def gather_ceiling(torch, L, reps=5):
     """Random 8-byte gathers per second of tacogb_probe_gather (ld.global.cg, 32 warps per SM,
     shared memory as the SpMV kernels hold it): the ceiling of an x-gathering SpMV."""
+    from taco_gb300 import _native as N
+    PR = N.probe()
     rows, n = 1 << 21, 1 << 25
     table = torch.zeros(rows * 2, dtype=torch.float64, device="cuda")
     idx = torch.randint(0, rows, (n,), dtype=torch.int32, device="cuda",
@@ -1376,7 +1416,7 @@ def gather_ceiling(torch, L, reps=5):
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     def run():
-        rc = L.tacogb_probe_gather(table.data_ptr(), rows, idx.data_ptr(), n, out.data_ptr(),
+        rc = PR.tacogb_probe_gather(table.data_ptr(), rows, idx.data_ptr(), n, out.data_ptr(),
                                    out.numel(), 1, 160, 70, sp)
         if rc:
             raise RuntimeError(L.tacogb_last_error().decode())
@@ -1407,6 +1447,8 @@ def main_gather_probe(args, torch, tg, L):
     L2-resident table of 16-byte rows (one L2 sector each, like the x gathers of a random-column
     SpMV), eight in flight per thread, 32 warps per SM, by load form and by the shared memory
     held per SM (which sets the L1 left).  One JSON line per configuration."""
+    from taco_gb300 import _native as N
+    PR = N.probe()
     rows, n = 1 << 21, 1 << 26
     table = torch.zeros(rows * 2, dtype=torch.float64, device="cuda")  # zero: see probe.cu
     idx = torch.randint(0, rows, (n,), dtype=torch.int32, device="cuda",
@@ -1421,7 +1463,7 @@ def main_gather_probe(args, torch, tg, L):
     for smem_kb, carve in ((0, -1), (192, -1), (64, 100)):
         for mode in (0, 1, 2):
             def run():
-                tg.check(L.tacogb_probe_gather(table.data_ptr(), rows, idx.data_ptr(), n,
+                tg.check(PR.tacogb_probe_gather(table.data_ptr(), rows, idx.data_ptr(), n,
                                                out.data_ptr(), out.numel(), mode, smem_kb, carve,
                                                sp), "tacogb_probe_gather")
             for _ in range(max(3, args.warmup)):

@@ -110,16 +110,6 @@ int tacogb_read_rb(const char* path, int32_t* rows, int32_t* cols, int64_t* nnz,
                    int32_t** colptr, int32_t** rowidx, double** vals);
 void tacogb_free_host(void* p);
 
-/* Diagnostic (no counterpart in taco): random-gather throughput probe.  Launches 4 blocks of 256
- * threads per SM on `stream`; each thread gathers entries table[2 * idx[i]] (rows of 16 bytes,
- * idx clamped into [0, rows)) eight at a time with load form `mode` (0 ld.global.nc,
- * 1 ld.global.cg, 2 ld.global.nc.L1::no_allocate) while every block holds
- * smem_kb_per_sm / 4 KB of shared memory; carveout is the preferred shared-memory carveout in
- * percent (-1: the driver's choice).  out needs 1024 * SMs entries.  The caller times it. */
-int tacogb_probe_gather(const double* table, int64_t rows, const int32_t* idx, int64_t n,
-                        double* out, int64_t out_len, int32_t mode, int32_t smem_kb_per_sm,
-                        int32_t carveout, void* stream);
-
 /* ------------------------------------------------------------------ device layer -------- */
 
 /* A CSR matrix in device (or managed) memory: {Dense,Sparse} with int32 pos/crd. */
@@ -153,7 +143,9 @@ const char* tacogb_spmv_variant_name(int32_t variant);
  * which bounds the problem to about 2.9e8 rows + nonzeros; larger problems are rejected with
  * TACOGB_ERR_ARG and a message (use tacogb_spmv).  The first call on each device looks the
  * array's address up (cudaGetSymbolAddress) and caches it, so make that first call before any
- * stream capture.  All calls share the one array: calls that overlap on the GPU (different
+ * stream capture.  The cached address belongs to the device's primary context: after a
+ * cudaDeviceReset in this process it is stale, so do not call this function again after a
+ * reset.  All calls share the one array: calls that overlap on the GPU (different
  * streams, or graphs replayed concurrently) race and must be serialised by the caller. */
 int tacogb_spmv_noalloc(const tacogb_csr* A, const void* x, void* y, void* stream);
 

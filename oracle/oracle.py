@@ -27,18 +27,32 @@ def _run(cmd, cwd=None):
         raise RuntimeError("oracle build failed: %s\n%s" % (" ".join(cmd), r.stdout))
 
 
-def build(reference_root="/root/reference"):
+def build(reference_root=None):
     """Compiles the C restatement; compiles taco's generated C when it is available, first
-    regenerating it from the reference tree when that tree exists."""
+    regenerating it from taco's source tree when one is named (reference_root, else the
+    TACO_REFERENCE environment variable) and exists."""
+    reference_root = reference_root or os.environ.get("TACO_REFERENCE") or ""
     src = os.path.join(HERE, "taco_oracle.c")
     out = os.path.join(HERE, "liboracle.so")
     if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
         _run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", out])
     root = os.path.dirname(HERE)
-    if os.path.isdir(os.path.join(reference_root, "src")):
+    # the workload generators (taco_gb300/csrc/gen.c) built again on the oracle side, for
+    # processes that time taco's code and must not map the product's libraries
+    gsrc = os.path.join(root, "taco_gb300", "csrc", "gen.c")
+    gout = generator_library()
+    if not os.path.exists(gout) or os.path.getmtime(gout) < os.path.getmtime(gsrc):
+        _run(["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+              "-I" + os.path.join(root, "include"), gsrc, "-o", gout, "-lm"])
+    if reference_root and os.path.isdir(os.path.join(reference_root, "src")):
         _run(["make", "-s", "-f", "oracle/Makefile.ref", "-j8", "REF=" + reference_root], cwd=root)
     elif os.path.isdir(GEN_DIR):
         _run(["make", "-s", "-f", "oracle/Makefile.ref", "lib", "REF=/nonexistent"], cwd=root)
+
+
+def generator_library():
+    """Path of the oracle-side build of the workload generators."""
+    return os.path.join(HERE, "liboracle_gen.so")
 
 
 _lib = None

@@ -101,7 +101,6 @@ SIGNATURES = {
     "tacogb_profile_begin": (None, []),
     "tacogb_profile_end": (I32, [I32, P, P, P]),
     "tacogb_profile_enable": (None, [I32]),
-    "tacogb_probe_gather": (I32, [P, I64, P, I64, P, I64, I32, I32, I32, P]),
     "tacogb_pack_csr": (I32, [I32, I32, I64, P, P, P, I32, P, P, P, P, P]),
     "tacogb_pack_taco": (I32, [P, P, I64]),
     "tacogb_read_rb": (I32, [ctypes.c_char_p, ctypes.POINTER(I32), ctypes.POINTER(I32),
@@ -221,10 +220,37 @@ def lib():
     return _lib
 
 
+# include/taco_gb300_probe.h (libtacogb_probe.so, loaded by the benchmark only)
+PROBE_SIGNATURES = {
+    "tacogb_probe_gather": (I32, [P, I64, P, I64, P, I64, I32, I32, I32, P]),
+}
+_probe = None
+
+
+def probe():
+    """The random-gather probe library (a measurement the benchmark uses; not libtacogb)."""
+    global _probe
+    if _probe is None:
+        lib()
+        _probe = ctypes.CDLL(os.path.join(LIBDIR, "libtacogb_probe.so"))
+        _bind(_probe, PROBE_SIGNATURES)
+    return _probe
+
+
+_gen_path = None
+
+
+def set_generator_library(path):
+    """Loads the generators from another build of the same source (the oracle builds its own
+    copy, so that a process timing taco's code maps no library of this package)."""
+    global _gen, _gen_path
+    _gen, _gen_path = None, path
+
+
 def gen():
     global _gen
     if _gen is None:
-        path = os.path.join(LIBDIR, "libtacogb_gen.so")
+        path = _gen_path or os.path.join(LIBDIR, "libtacogb_gen.so")
         if not os.path.exists(path):
             raise RuntimeError("libtacogb_gen.so is not built (run taco_gb300.build.build())")
         _gen = ctypes.CDLL(path)

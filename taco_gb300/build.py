@@ -4,6 +4,8 @@
   libtacogb_<p>.so      per-pattern modules exporting taco's unprefixed kernel names
                         (assemble / compute / evaluate / _shim_*) for p in spmv, spmm, spgemm
   libtacogb_gen.so      deterministic synthetic-matrix generators (include/taco_gb300_gen.h)
+  libtacogb_probe.so    the random-gather probe bench.py measures the SpMV ceiling with
+                        (include/taco_gb300_probe.h); not part of libtacogb
 
 Every .cu file compiles in parallel with one -gencode (compute_103a / sm_103a); objects are
 reused when their source and the shared headers are older than the object.
@@ -21,7 +23,7 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "lib", "obj")
 
 CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu", "spgemm.cu", "batched.cu", "batched_spmm.cu",
-              "tuner.cu", "probe.cu", "pack.cu", "sddmm.cu", "tensor3.cu", "formats.cu",
+              "tuner.cu", "pack.cu", "sddmm.cu", "tensor3.cu", "formats.cu",
               "fileio.cpp"]
 PATTERNS = ["spmv", "spmm", "spgemm", "sddmm", "ttv", "ttm", "mttkrp"]
 NARGS = {"sddmm": 4, "mttkrp": 4}  # tensors per call (result and operands); 3 otherwise
@@ -65,7 +67,8 @@ def build(verbose=False, extra_flags=()):
     os.makedirs(OBJDIR, exist_ok=True)
     extra = list(extra_flags)
     with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile_cu(s, extra), CU_SOURCES))
+        objs = list(ex.map(lambda s: _compile_cu(s, extra), CU_SOURCES + ["probe.cu"]))
+        probe_obj = objs.pop()
         gen_src = os.path.join(CSRC, "gen.c")
         gen_lib = os.path.join(LIBDIR, "libtacogb_gen.so")
         fut_gen = None
@@ -76,6 +79,10 @@ def build(verbose=False, extra_flags=()):
         if _stale(lib, objs):
             _run([NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a"] + objs
                  + ["-o", lib])
+        probe_lib = os.path.join(LIBDIR, "libtacogb_probe.so")
+        if _stale(probe_lib, [probe_obj, lib]):
+            _run([NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", probe_obj,
+                  "-o", probe_lib, "-L" + LIBDIR, "-ltacogb", "-Xlinker", "-rpath,$ORIGIN"])
         mods = []
         mod_src = os.path.join(CSRC, "module.c")
         for p in PATTERNS:

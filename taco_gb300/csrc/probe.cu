@@ -3,11 +3,14 @@
 // (one L2 sector per gather, as an x gather of a random-column SpMV), with a chosen load form
 // and a chosen amount of shared memory held per SM (which sets how much L1 remains).  The
 // caller times the launch; bench.py --workload gather_probe reports gathers per clock per SM.
+// Built into its own library (libtacogb_probe.so, include/taco_gb300_probe.h), which only the
+// benchmark loads: it is a measurement, not part of libtacogb.
 
 #include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
+#include "taco_gb300_probe.h"
 
 namespace tacogb {
 

@@ -2,9 +2,9 @@
 
 The generated code comes from taco's CLI built from the reference sources by
 oracle/Makefile.ref (taco "y(i) = A(i,j) * x(j)" -f=A:ds -write-source=..., etc.) and is
-compiled with taco's JIT flags.  Run from the repository root where the reference tree exists:
+compiled with taco's JIT flags.  Run from the repository root, naming taco's source tree:
 
-    python tests/golden/make_golden.py
+    TACO_REFERENCE=<taco source tree> python tests/golden/make_golden.py
 
 Each fixture stores its inputs and taco's outputs, so the tests that read it need neither the
 reference nor the generator.
@@ -280,7 +280,7 @@ def _write_rb(path, rows, cols, colptr, rowidx, vals, rhs_line=None):
         f.write("\n".join(hdr + pl + il + vl) + "\n")
 
 
-def rb_cases(reference_root="/root/reference"):
+def rb_cases(reference_root):
     """Rutherford-Boeing: taco's own test matrix rua_32 (test/data/rua_32.rb and its .mtx twin).
     taco's CLI crashes on .rb input and output here, so the CSR expected of the .rb file is the
     one taco's CLI makes of rua_32.mtx; this script writes the matrix again in its own RB layout
@@ -329,8 +329,11 @@ def rb_cases(reference_root="/root/reference"):
 
 
 if __name__ == "__main__":
+    ref_root = os.environ.get("TACO_REFERENCE")
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src")):
+        sys.exit("set TACO_REFERENCE to taco's source tree")
     B.build()
-    O.build()
+    O.build(ref_root)
     assert O.ref_available("spmv"), "taco's generated code is not built (oracle/Makefile.ref)"
     spmv_cases()
     assert O.ref_available("spmm")
@@ -345,4 +348,4 @@ if __name__ == "__main__":
     format_cases()
     pack_cases()
     reader_cases()
-    rb_cases()
+    rb_cases(ref_root)

@@ -297,3 +297,24 @@ def ref_spgemm(A, B, threads=1):
     vals = np.ctypeslib.as_array(ctypes.cast(Ct.vals_ptr, ctypes.POINTER(ctypes.c_double)),
                                  (max(nnz, 1),))[:nnz].copy()
     return pos, crd, vals
+
+
+def sample_rows(pos, count, seed=0, longest=64):
+    """Sorted distinct row indices for a sampled check of a large result: the `longest` longest
+    rows (they span many merge tiles, so their carries cross tile and CTA boundaries), the first
+    and last rows, and random rows up to `count`."""
+    rows = len(pos) - 1
+    lens = np.diff(pos)
+    rng = np.random.default_rng(seed)
+    pick = [np.argsort(lens, kind="stable")[-longest:], [0, rows - 1],
+            rng.choice(rows, min(count, rows), replace=False)]
+    return np.unique(np.concatenate(pick).astype(np.int64))
+
+
+def sub_rows(pos, crd, vals, idx):
+    """(pos, crd, vals) of the CSR matrix made of rows idx of (pos, crd, vals), in that order."""
+    lens = (pos[idx + 1] - pos[idx]).astype(np.int64)
+    spos = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    take = np.concatenate([np.arange(pos[i], pos[i + 1], dtype=np.int64) for i in idx]) \
+        if len(idx) else np.zeros(0, np.int64)
+    return spos, crd[take], vals[take]

@@ -31,6 +31,14 @@ def test_libtacogb_exports_header():
     assert set(names) <= set(N.SIGNATURES), "bindings miss %s" % (set(names) - set(N.SIGNATURES))
 
 
+def test_probe_library_exports_header():
+    names = declared("taco_gb300_probe.h")
+    assert names == ["tacogb_probe_gather"]
+    assert set(names) == set(N.PROBE_SIGNATURES)
+    assert hasattr(N.probe(), names[0])
+    assert not hasattr(ctypes.CDLL(os.path.join(N.LIBDIR, "libtacogb.so")), names[0])
+
+
 def test_libtacogb_gen_exports_header():
     names = declared("taco_gb300_gen.h")
     L = ctypes.CDLL(os.path.join(N.LIBDIR, "libtacogb_gen.so"))
@@ -43,6 +51,25 @@ def test_dropin_modules_export_taco_names(pattern):
     for n in ("assemble", "compute", "evaluate", "_shim_assemble", "_shim_compute",
               "_shim_evaluate"):
         assert hasattr(L, n)
+
+
+def test_oracle_generator_build_is_identical():
+    """The oracle's own build of the generators (used by the benchmark's taco arm, which maps
+    no product library) gives the same matrices bit for bit."""
+    from oracle import oracle as O
+    O.build()
+    specs = [W.spmv_powerlaw(rows=40000), W.spmv_banded(rows=30000), W.spmv_small(),
+             W.batch_spec(5), W.spgemm_poisson(64)]
+    ours = [W.generate(s) for s in specs] + [W.dense(23, 1000)]
+    try:
+        N.set_generator_library(O.generator_library())
+        theirs = [W.generate(s) for s in specs] + [W.dense(23, 1000)]
+        assert N.gen()._name == O.generator_library()
+    finally:
+        N.set_generator_library(None)
+    for a, b in zip(ours, theirs):
+        for x, y in zip(a if isinstance(a, tuple) else (a,), b if isinstance(b, tuple) else (b,)):
+            assert np.array_equal(x, y)
 
 
 def test_version_and_error_without_gpu():

@@ -104,6 +104,49 @@ def test_all_bins_float32():
     assert normwise(cv, ref[2]) <= 1e-6
 
 
+def _sort_path_matrix():
+    """Rows whose product counts sit on and around every sort-path boundary of bins 1 and 2
+    (32/33 products: bin 1 to bin 2; 64/65: two to four keys per lane in registers; 128/129:
+    registers to the warp's shared-memory slice; 256/257: bin 2 to bin 3), plus random counts
+    in between.  B's rows draw their columns from [0, 150), so most output columns collect
+    several products and the runs that are summed cross the lanes' register boundaries."""
+    rng = np.random.default_rng(29)
+    K, copies = 150, 5
+    blens = np.repeat(np.arange(1, 65), copies)  # B row copies*(L-1)+c has L entries
+    bpos = np.concatenate([[0], np.cumsum(blens)]).astype(np.int32)
+    bcrd = np.concatenate([np.sort(rng.choice(K, l, replace=False)) for l in blens]).astype(np.int32)
+    bvals = rng.uniform(-1, 1, len(bcrd))
+    targets = [32, 33, 63, 64, 65, 96, 100, 127, 128, 129, 200, 255, 256, 257, 300]
+    targets = targets * 3 + list(rng.integers(1, 320, 200))
+    arows = []
+    for P in targets:
+        rows, left = [], int(P)
+        cs = list(rng.permutation(copies))
+        while left > 64:
+            rows.append(copies * 63 + cs.pop())
+            left -= 64
+        rows.append(copies * (left - 1) + int(rng.integers(copies)))
+        arows.append(np.unique(np.array(rows, dtype=np.int64)))
+    apos = np.concatenate([[0], np.cumsum([len(r) for r in arows])]).astype(np.int32)
+    acrd = np.concatenate(arows).astype(np.int32)
+    avals = rng.uniform(-1, 1, len(acrd))
+    return (apos, acrd, avals, len(blens)), (bpos, bcrd, bvals, K)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_sort_path_boundaries(dtype):
+    A, B = _sort_path_matrix()
+    prods = [int(np.sum(np.diff(B[0])[A[1][A[0][i]:A[0][i + 1]]])) for i in range(len(A[0]) - 1)]
+    assert {32, 33, 64, 65, 128, 129, 256, 257} <= set(prods)
+    ref = O.spgemm(A[0], A[1], A[2], B[0], B[1], B[2], B[3])
+    cp, cc, cv = gpu_spgemm(A, B, dtype)
+    assert np.array_equal(cp, ref[0]) and np.array_equal(cc, ref[1])
+    if dtype == torch.float64:
+        assert np.array_equal(cv, ref[2])
+    else:
+        assert normwise(cv, ref[2]) <= 1e-6
+
+
 @pytest.mark.parametrize("which", ["random", "poisson"])
 def test_full_size(which):
     """262,144^2 with 8 uniform nonzeros per row, and the 512x512 Poisson stencil squared."""
