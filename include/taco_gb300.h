@@ -62,6 +62,26 @@ const char* tacogb_version(void);
  * TACOGB_ERR_TIMEOUT; stream-ordered callers of the device layer check it when they sync. */
 int tacogb_device_status(int32_t* status);
 
+/* Index validation.  taco's pack produces valid compressed levels by construction
+ * (src/tensor.cpp:295-463) and its generated kernels trust them; this library's taco-ABI entry
+ * points instead check every compressed level they are handed before any kernel gathers through
+ * it: pos[0] == 0, pos non-decreasing with pos[outer] == nnz, 0 <= crd < the level's dimension,
+ * and crd strictly increasing within each segment (taco's sorted, distinct coordinates).  A
+ * violation returns TACOGB_ERR_ARG naming the first offending segment or position.
+ * Host-resident levels are checked by host threads while the call's copies to the GPU run;
+ * device-resident levels by one kernel reading pos and crd once.  The device layer (tacogb_spmv
+ * and the other functions on tacogb_csr) trusts its arguments; tacogb_csr_validate checks a
+ * device CSR explicitly.  tacogb_set_validation(0) turns the taco-ABI checks off (and returns the
+ * previous setting); they are on by default. */
+int tacogb_set_validation(int32_t on);
+/* Checks one compressed level held in host memory (outer segments over a dimension of size
+ * inner, nnz = pos[outer]); 0 or TACOGB_ERR_ARG.  Uses host threads only; needs no GPU. */
+int tacogb_validate_level_host(int64_t outer, int32_t inner, const int32_t* pos,
+                               const int32_t* crd, int64_t nnz);
+/* Checks a device-resident CSR matrix on the GPU (A->nnz must equal pos[rows]); synchronises
+ * stream. */
+int tacogb_csr_validate(const struct tacogb_csr* A, void* stream);
+
 /* Number of kernels this library has launched in this process. */
 long long tacogb_launch_count(void);
 /* Per-kernel device timing: between begin and end every launch is bracketed by CUDA events on

@@ -101,6 +101,9 @@ SIGNATURES = {
     "tacogb_profile_begin": (None, []),
     "tacogb_profile_end": (I32, [I32, P, P, P]),
     "tacogb_profile_enable": (None, [I32]),
+    "tacogb_set_validation": (I32, [I32]),
+    "tacogb_validate_level_host": (I32, [I64, I32, P, P, I64]),
+    "tacogb_csr_validate": (I32, [P, P]),
     "tacogb_pack_csr": (I32, [I32, I32, I64, P, P, P, I32, P, P, P, P, P]),
     "tacogb_pack_taco": (I32, [P, P, I64]),
     "tacogb_read_rb": (I32, [ctypes.c_char_p, ctypes.POINTER(I32), ctypes.POINTER(I32),
@@ -223,6 +226,7 @@ def lib():
 # include/taco_gb300_probe.h (libtacogb_probe.so, loaded by the benchmark only)
 PROBE_SIGNATURES = {
     "tacogb_probe_gather": (I32, [P, I64, P, I64, P, I64, I32, I32, I32, P]),
+    "tacogb_probe_wait_timeout": (I32, [P, P, I32, P]),
 }
 _probe = None
 

@@ -23,7 +23,7 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "lib", "obj")
 
 CU_SOURCES = ["abi.cu", "spmv.cu", "spmm.cu", "spgemm.cu", "batched.cu", "batched_spmm.cu",
-              "tuner.cu", "pack.cu", "sddmm.cu", "tensor3.cu", "formats.cu",
+              "tuner.cu", "pack.cu", "sddmm.cu", "tensor3.cu", "formats.cu", "validate.cu",
               "fileio.cpp"]
 PATTERNS = ["spmv", "spmm", "spgemm", "sddmm", "ttv", "ttm", "mttkrp"]
 NARGS = {"sddmm": 4, "mttkrp": 4}  # tensors per call (result and operands); 3 otherwise

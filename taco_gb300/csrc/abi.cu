@@ -15,6 +15,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "validate.h"
 
 namespace tacogb {
 
@@ -84,7 +85,8 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 11;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3, formats x3
+constexpr int kScratchSlots = 12;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3, formats x3,
+                                   // index validation
 
 struct DeviceState {
   int sms = 0;
@@ -246,6 +248,23 @@ int stage_in(Operand& o, const void* p, size_t bytes, int slot, cudaStream_t st)
   o.staged = true;
   if (bytes) TACOGB_CUDA_TRY(cudaMemcpyAsync(o.dev, p, bytes, cudaMemcpyHostToDevice, st));
   return 0;
+}
+
+// Stages one compressed level (pos: outer + 1 entries, crd: nnz entries, and optionally the
+// values: vbytes) into slots slot, slot + 1, slot + 2 while the level is checked (validate.h):
+// host-resident arrays by host threads during the copies, device-resident ones by a kernel.
+// A failed check is reported before any error of the staging.
+int stage_checked_level(const char* what, int64_t outer, int32_t inner, int64_t nnz,
+                        const void* pos, const void* crd, const void* vals, size_t vbytes,
+                        int slot, cudaStream_t st, Operand& op, Operand& oc, Operand* ov) {
+  LevelCheck chk;
+  chk.begin(what, outer, inner, (const int32_t*)pos, (const int32_t*)crd, nnz,
+            !device_accessible(pos) && !device_accessible(crd));
+  int src = stage_in(op, pos, ((size_t)outer + 1) * 4, slot, st);
+  if (!src) src = stage_in(oc, crd, (size_t)nnz * 4, slot + 1, st);
+  if (!src && ov) src = stage_in(*ov, vals, vbytes, slot + 2, st);
+  if (int rc = chk.finish(st, src == 0 ? op.dev : nullptr, oc.dev)) return rc;
+  return src;
 }
 
 int value_type_of_csize(int32_t csize) {
@@ -502,11 +521,14 @@ int dcsr_operand(const taco_tensor_t* A, int base, cudaStream_t st, tacogb_dcsr&
   int32_t nnz = 0;
   if (int rc = read_i32(pos1 + d.n0, &nnz)) return rc;
   d.nnz = nnz;
-  Operand o0, op, oc, ov;
-  if (int rc = stage_in(o0, A->indices[0][1], (size_t)d.n0 * 4, base, st)) return rc;
-  if (int rc = stage_in(op, pos1, ((size_t)d.n0 + 1) * 4, base + 1, st)) return rc;
-  if (int rc = stage_in(oc, A->indices[1][1], (size_t)nnz * 4, base + 2, st)) return rc;
-  if (int rc = stage_in(ov, A->vals, (size_t)nnz * value_bytes(d.vtype), base + 3, st)) return rc;
+  Operand o0p, o0, op, oc, ov;
+  if (int rc = stage_checked_level("DCSR level 0", 1, d.rows, d.n0, pos0, A->indices[0][1],
+                                   nullptr, 0, 83, st, o0p, o0, nullptr))
+    return rc;
+  if (int rc = stage_checked_level("DCSR level 1", d.n0, d.cols, nnz, pos1, A->indices[1][1],
+                                   A->vals, (size_t)nnz * value_bytes(d.vtype), base + 1, st, op,
+                                   oc, &ov))
+    return rc;
   d.crd0 = (const int32_t*)o0.dev;
   d.pos = (const int32_t*)op.dev;
   d.crd = (const int32_t*)oc.dev;
@@ -529,9 +551,10 @@ int dense_x(const taco_tensor_t* x, int vt, int base, cudaStream_t st, const voi
   TACOGB_CHECK_ARG(pos != nullptr, "spmv: null pos of the sparse x");
   int32_t k = 0;
   if (int rc = read_i32(pos + 1, &k)) return rc;
-  Operand oi, ov;
-  if (int rc = stage_in(oi, x->indices[0][1], (size_t)k * 4, base, st)) return rc;
-  if (int rc = stage_in(ov, x->vals, (size_t)k * vb, base + 1, st)) return rc;
+  Operand op, oi, ov;
+  if (int rc = stage_checked_level("spmv operand x", 1, n, k, pos, x->indices[0][1], x->vals,
+                                   (size_t)k * vb, 80, st, op, oi, &ov))
+    return rc;
   void* d = stage_buffer(base + 2, (size_t)n * vb);
   if (!d) return TACOGB_ERR_ALLOC;
   if (int rc = densify_run(n, k, (const int32_t*)oi.dev, ov.dev, vt, d, st)) return rc;
@@ -601,9 +624,10 @@ int spmv_fmt_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
     int32_t nnz = 0;
     if (int rc = read_i32(pos + outer, &nnz)) return rc;
     Operand op, oc, ov;
-    if (int rc = stage_in(op, pos, ((size_t)outer + 1) * 4, 40, st)) return rc;
-    if (int rc = stage_in(oc, A->indices[1][1], (size_t)nnz * 4, 41, st)) return rc;
-    if (int rc = stage_in(ov, A->vals, (size_t)nnz * vb, 42, st)) return rc;
+    if (int rc = stage_checked_level("spmv operand A", outer, fmt == kFmtCSC ? rows : cols, nnz,
+                                     pos, A->indices[1][1], A->vals, (size_t)nnz * vb, 40, st,
+                                     op, oc, &ov))
+      return rc;
     tacogb_csr c{rows, cols, nnz, (const int32_t*)op.dev, (const int32_t*)oc.dev, ov.dev, vt};
     if (int rc = fmt == kFmtCSC ? spmv_csc_run(&c, xd, yd, st)
                                 : spmv_run(&c, xd, yd, TACOGB_VARIANT_AUTO, st))
@@ -655,9 +679,9 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
 
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ox;
-  if (int rc = stage_in(opos, pos, ((size_t)rows + 1) * 4, 0, st)) return rc;
-  if (int rc = stage_in(ocrd, crd, (size_t)nnz * 4, 1, st)) return rc;
-  if (int rc = stage_in(ovals, A->vals, (size_t)nnz * vb, 2, st)) return rc;
+  if (int rc = stage_checked_level("spmv operand A", rows, cols, nnz, pos, crd, A->vals,
+                                   (size_t)nnz * vb, 0, st, opos, ocrd, &ovals))
+    return rc;
   if (int rc = stage_in(ox, x->vals, (size_t)cols * vb, 3, st)) return rc;
   void* ydev = y->vals;
   const bool y_staged = !device_accessible(y->vals);
@@ -764,9 +788,9 @@ int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   if (int rc = read_i32(pos + rows, &nnz)) return rc;
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ob;
-  if (int rc = stage_in(opos, pos, ((size_t)rows + 1) * 4, 0, st)) return rc;
-  if (int rc = stage_in(ocrd, crd, (size_t)nnz * 4, 1, st)) return rc;
-  if (int rc = stage_in(ovals, A->vals, (size_t)nnz * value_bytes(at), 2, st)) return rc;
+  if (int rc = stage_checked_level("spmm operand A", rows, cols, nnz, pos, crd, A->vals,
+                                   (size_t)nnz * value_bytes(at), 0, st, opos, ocrd, &ovals))
+    return rc;
   if (int rc = stage_in(ob, B->vals, (size_t)cols * N * value_bytes(bt), 3, st)) return rc;
   const size_t cbytes = (size_t)rows * N * value_bytes(ct);
   void* cdev = C->vals;
@@ -806,8 +830,8 @@ namespace {
 // expanded to every row; CSC transposed on the GPU; DCSC expanded to CSC, then transposed
 // (taco's spgemm format test, test/tests-scheduling-eval.cpp:655-662).  Host arrays are staged
 // into slots base .. base+9.
-int csr_operand(const taco_tensor_t* T, int base, bool with_vals, cudaStream_t st,
-                tacogb_csr& out) {
+int csr_operand(const char* what, const taco_tensor_t* T, int base, bool with_vals,
+                cudaStream_t st, tacogb_csr& out) {
   const int fmt = mat_format(T);
   if (fmt != kFmtCSR) {
     const int32_t rows = T->dimensions[0], cols = T->dimensions[1];
@@ -827,13 +851,16 @@ int csr_operand(const taco_tensor_t* T, int base, bool with_vals, cudaStream_t s
     if (int rc = read_i32(p1 + n0, &nnz)) return rc;
     const size_t vb = value_bytes(vt);
     Operand op, oc, ov;
-    if (int rc = stage_in(op, p1, ((size_t)n0 + 1) * 4, base, st)) return rc;
-    if (int rc = stage_in(oc, T->indices[1][1], (size_t)nnz * 4, base + 1, st)) return rc;
-    if (int rc = stage_in(ov, T->vals, (size_t)nnz * vb, base + 2, st)) return rc;
+    const int32_t inner = (fmt == kFmtCSC || fmt == kFmtDCSC) ? rows : cols;
+    if (int rc = stage_checked_level(what, n0, inner, nnz, p1, T->indices[1][1], T->vals,
+                                     (size_t)nnz * vb, base, st, op, oc, &ov))
+      return rc;
     const int32_t* pos = (const int32_t*)op.dev;
     if (doubly) {  // every row (column) gets its range
-      Operand o0;
-      if (int rc = stage_in(o0, T->indices[0][1], (size_t)n0 * 4, base + 3, st)) return rc;
+      Operand o0p, o0;
+      if (int rc = stage_checked_level(what, 1, outer, n0, T->indices[0][0], T->indices[0][1],
+                                       nullptr, 0, base + 20, st, o0p, o0, nullptr))
+        return rc;
       int32_t* full = (int32_t*)stage_buffer(base + 4, ((size_t)outer + 1) * 4);
       if (!full) return TACOGB_ERR_ALLOC;
       if (int rc = expand_pos_run((const int32_t*)o0.dev, pos, n0, outer, full, st)) return rc;
@@ -862,11 +889,10 @@ int csr_operand(const taco_tensor_t* T, int base, bool with_vals, cudaStream_t s
   const int vt = value_type_of_csize(T->csize);
   TACOGB_CHECK_ARG(vt == TACOGB_F64 || vt == TACOGB_F32, "spgemm: unsupported csize %d", T->csize);
   Operand op, oc, ov;
-  if (int rc = stage_in(op, pos, ((size_t)rows + 1) * 4, base, st)) return rc;
-  if (int rc = stage_in(oc, crd, (size_t)nnz * 4, base + 1, st)) return rc;
-  if (with_vals) {
-    if (int rc = stage_in(ov, T->vals, (size_t)nnz * value_bytes(vt), base + 2, st)) return rc;
-  }
+  if (int rc = stage_checked_level(what, rows, cols, nnz, pos, crd, T->vals,
+                                   (size_t)nnz * value_bytes(vt), base, st, op, oc,
+                                   with_vals ? &ov : nullptr))
+    return rc;
   out = tacogb_csr{rows, cols, nnz, (const int32_t*)op.dev, (const int32_t*)oc.dev,
                    with_vals ? ov.dev : nullptr, vt};
   return 0;
@@ -893,8 +919,8 @@ int tacogb_spgemm_assemble(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B)
   if (int rc = check_spgemm(C, A, B)) return rc;
   cudaStream_t st = lib_stream();
   tacogb_csr a, b;
-  if (int rc = csr_operand(A, 60, false, st, a)) return rc;
-  if (int rc = csr_operand(B, 70, false, st, b)) return rc;
+  if (int rc = csr_operand("spgemm operand A", A, 60, false, st, a)) return rc;
+  if (int rc = csr_operand("spgemm operand B", B, 70, false, st, b)) return rc;
   const int32_t rows = a.rows;
   const bool managed = device_accessible(A->indices[1][0]);
   int32_t* dpos = (int32_t*)stage_buffer(6, ((size_t)rows + 1) * 4);
@@ -923,9 +949,9 @@ int tacogb_spgemm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) 
                    "spgemm: result not assembled");
   cudaStream_t st = lib_stream();
   tacogb_csr a, b, c;
-  if (int rc = csr_operand(A, 60, true, st, a)) return rc;
-  if (int rc = csr_operand(B, 70, true, st, b)) return rc;
-  if (int rc = csr_operand(C, 6, false, st, c)) return rc;
+  if (int rc = csr_operand("spgemm operand A", A, 60, true, st, a)) return rc;
+  if (int rc = csr_operand("spgemm operand B", B, 70, true, st, b)) return rc;
+  if (int rc = csr_operand("spgemm result C", C, 6, false, st, c)) return rc;
   const size_t vbytes = (size_t)c.nnz * value_bytes(a.vtype);
   void* dvals = C->vals;
   const bool staged = !device_accessible(C->vals);
@@ -1099,9 +1125,9 @@ int tacogb_sddmm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, t
   const bool dense = !is_csr_result(A);
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, oc, od;
-  if (int rc = stage_in(opos, pos, ((size_t)I + 1) * 4, 20, st)) return rc;
-  if (int rc = stage_in(ocrd, B->indices[1][1], (size_t)nnz * 4, 21, st)) return rc;
-  if (int rc = stage_in(ovals, B->vals, (size_t)nnz * vb, 22, st)) return rc;
+  if (int rc = stage_checked_level("sddmm operand B", I, K, nnz, pos, B->indices[1][1], B->vals,
+                                   (size_t)nnz * vb, 20, st, opos, ocrd, &ovals))
+    return rc;
   if (int rc = stage_in(oc, C->vals, (size_t)I * J * vb, 23, st)) return rc;
   if (int rc = stage_in(od, D->vals, (size_t)J * K * vb, 24, st)) return rc;
   const size_t obytes = dense ? (size_t)I * (size_t)K * vb : (size_t)nnz * vb;
@@ -1180,7 +1206,8 @@ int check_dense_order(const taco_tensor_t* t, int order, const char* name) {
   return 0;
 }
 
-// B's arrays as a tacogb_csf3 on the device (host arrays staged in slots base .. base+6).
+// B's arrays as a tacogb_csf3 on the device (host arrays staged in slots base + 1 .. base + 5
+// and base + 60 .. base + 62), each level checked on the way (stage_checked_level).
 int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3& out) {
   TACOGB_CHECK_ARG(T != nullptr && T->order == 3 && T->dimensions && T->mode_types && T->indices,
                    "order-3 operand B: expected an order-3 tensor");
@@ -1220,16 +1247,21 @@ int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3&
   int32_t nnz = 0;
   if (int rc = read_i32(pos2 + b.nfib, &nnz)) return rc;
   b.nnz = nnz;
-  Operand o0, op1, oc1, op2, oc2, ov;
+  Operand o0p, o0, op1, oc1, op2, oc2, ov;
   if (crd0) {
-    if (int rc = stage_in(o0, crd0, (size_t)b.n0 * 4, base, st)) return rc;
+    if (int rc = stage_checked_level("order-3 operand B level 0", 1, b.dims[0], b.n0,
+                                     T->indices[0][0], crd0, nullptr, 0, base + 60, st, o0p, o0,
+                                     nullptr))
+      return rc;
     b.crd0 = (const int32_t*)o0.dev;
   }
-  if (int rc = stage_in(op1, pos1, ((size_t)b.n0 + 1) * 4, base + 1, st)) return rc;
-  if (int rc = stage_in(oc1, crd1, (size_t)b.nfib * 4, base + 2, st)) return rc;
-  if (int rc = stage_in(op2, pos2, ((size_t)b.nfib + 1) * 4, base + 3, st)) return rc;
-  if (int rc = stage_in(oc2, crd2, (size_t)b.nnz * 4, base + 4, st)) return rc;
-  if (int rc = stage_in(ov, T->vals, (size_t)b.nnz * value_bytes(vt), base + 5, st)) return rc;
+  if (int rc = stage_checked_level("order-3 operand B level 1", b.n0, b.dims[1], b.nfib, pos1,
+                                   crd1, nullptr, 0, base + 1, st, op1, oc1, nullptr))
+    return rc;
+  if (int rc = stage_checked_level("order-3 operand B level 2", b.nfib, b.dims[2], b.nnz, pos2,
+                                   crd2, T->vals, (size_t)b.nnz * value_bytes(vt), base + 3, st,
+                                   op2, oc2, &ov))
+    return rc;
   b.pos1 = (const int32_t*)op1.dev;
   b.crd1 = (const int32_t*)oc1.dev;
   b.pos2 = (const int32_t*)op2.dev;

@@ -143,11 +143,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
   return ok != 0;
 }
 
-// Waits for phase `phase` of `bar` at most ~max_iters polls (with back-off); false on timeout.
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Longest a bounded wait polls before it gives up (the library's copies land in microseconds).
+constexpr uint64_t kWaitLimitNs = 200ull * 1000 * 1000;
+
+// Waits for phase `phase` of `bar`; false once about limit_ns of wall time (read from the
+// global timer every 16 polls, the first reading taken only after 16 failed polls) or
+// 2^22 polls have passed, whichever comes first.  try_wait may suspend the thread for a
+// system-dependent time per poll; the time check bounds the total whatever that time is.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase,
-                                                  uint32_t max_iters = (1u << 20)) {
-  for (uint32_t it = 0; it < max_iters; it++) {
+                                                  uint64_t limit_ns = kWaitLimitNs) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 0; it < (1u << 22); it++) {
     if (mbar_try_wait(bar, phase)) return true;
+    if ((it & 15) == 15) {
+      const uint64_t now = globaltimer_ns();
+      if (t0 == 0)
+        t0 = now;
+      else if (now - t0 > limit_ns)
+        return false;
+    }
     if (it > 64) __nanosleep(64);
   }
   return false;

@@ -56,9 +56,55 @@ probe_gather_kernel(const double* __restrict__ table, int32_t rows, const int32_
   out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// ---- bounded-wait self-test --------------------------------------------------------------
+//
+// Every TMA-staged kernel of the library waits for its copies with mbar_wait_or_flag: a bounded
+// poll that, when it gives up, sets the timeout bit of the device status word, waits once more
+// (again bounded) so that no copy still writes shared memory when the CTA exits, and returns.
+// This kernel makes that wait run out without any fault: one CTA announces extra bytes more
+// than its one bulk copy brings, so the mbarrier phase can never complete.  It then copies what
+// landed in shared memory to out, with the wait's verdict in the last int4, so the caller can
+// check that the copy itself completed.
+constexpr int kWaitBytes = 4096;
+
+__global__ void __launch_bounds__(32)
+probe_wait_timeout_kernel(const int4* __restrict__ src, int4* __restrict__ out,
+                          int* __restrict__ status, uint32_t extra) {
+  __shared__ __align__(128) int4 buf[kWaitBytes / 16];
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    mbar_arrive_expect_tx(&bar, kWaitBytes + extra);
+    tma_load_bulk(buf, src, kWaitBytes, &bar);
+  }
+  __syncwarp();
+  const bool ok = mbar_wait_or_flag(&bar, 0, status);
+  __syncwarp();
+  for (int i = threadIdx.x; i < kWaitBytes / 16; i += 32) out[i] = buf[i];
+  if (threadIdx.x == 0) out[kWaitBytes / 16] = make_int4(ok ? 1 : 0, 0, 0, 0);
+}
+
 }  // namespace
 
 }  // namespace tacogb
+
+extern "C" int tacogb_probe_wait_timeout(const void* src, void* out, int32_t extra_bytes,
+                                         void* stream) {
+  using namespace tacogb;
+  TACOGB_CHECK_ARG(src != nullptr && out != nullptr, "wait probe: null pointer");
+  TACOGB_CHECK_ARG(((uintptr_t)src & 15) == 0 && ((uintptr_t)out & 15) == 0,
+                   "wait probe: src and out must be 16-byte aligned");
+  TACOGB_CHECK_ARG(extra_bytes >= 0 && extra_bytes <= 4096 && extra_bytes % 16 == 0,
+                   "wait probe: extra_bytes %d is not a multiple of 16 in [0, 4096]", extra_bytes);
+  int* status = device_status();
+  if (!status) return last_code();
+  const cudaStream_t st = (cudaStream_t)stream;
+  TACOGB_LAUNCH("probe_wait_timeout_kernel", st,
+                probe_wait_timeout_kernel<<<1, 32, 0, st>>>((const int4*)src, (int4*)out, status,
+                                                            (uint32_t)extra_bytes));
+  return 0;
+}
 
 extern "C" int tacogb_probe_gather(const double* table, int64_t rows, const int32_t* idx,
                                    int64_t n, double* out, int64_t out_len, int32_t mode,

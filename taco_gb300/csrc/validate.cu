@@ -1,0 +1,306 @@
+// Validation of compressed index levels (pos, crd) at the taco-ABI boundary.
+//
+// taco's pack builds pos and crd that are valid by construction (src/tensor.cpp:295-463: sort,
+// then the generated pack appends sorted, distinct coordinates), and its generated kernels trust
+// them.  A caller of this C ABI hands over arrays that nothing has checked, and a corrupt crd
+// here becomes an out-of-bounds gather on the GPU.  So before any kernel that gathers through a
+// level runs, the level is checked for
+//   pos[0] == 0,  pos non-decreasing,  pos[outer] == nnz (when nnz is known separately),
+//   0 <= crd[p] < inner,  crd strictly increasing within each segment [pos[i], pos[i+1]),
+// and a violation returns TACOGB_ERR_ARG with the first offending index.
+//
+// Host-resident levels (taco without CUDA, pinned buffers) are checked by host threads that run
+// while the call's copies to the GPU proceed, so the check costs no time on the copy-bound
+// path.  Device-resident levels (managed or device memory) are checked by one streaming kernel
+// that reads pos and crd once, in bounds: crd is read at [0, nnz) only, pos at [0, outer].
+// Sortedness on the GPU: a descent (crd[p] <= crd[p-1]) is legal only where p starts a
+// non-empty segment, so the kernel counts all descents and the descents at segment starts; the
+// two counts agree exactly when every segment is sorted.
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "common.cuh"
+#include "validate.h"
+
+namespace tacogb {
+
+namespace {
+
+std::atomic<int> g_validate{1};
+
+enum : unsigned {
+  kBadPos0 = 1,      // pos[0] != 0
+  kBadPosOrder = 2,  // pos decreases
+  kBadCrdRange = 4,  // crd outside [0, inner)
+  kBadCrdOrder = 8,  // crd not strictly increasing within a segment
+  kBadPosEnd = 16,   // pos[outer] != nnz, or pos outside [0, nnz]
+};
+
+void describe(unsigned bits, int64_t at_pos, int64_t at_crd, const char* what, char* msg,
+              size_t cap) {
+  if (bits & kBadPos0)
+    snprintf(msg, cap, "%s: pos[0] is not 0", what);
+  else if (bits & kBadPosOrder)
+    snprintf(msg, cap, "%s: pos decreases at segment %lld", what, (long long)at_pos);
+  else if (bits & kBadPosEnd)
+    snprintf(msg, cap, "%s: pos leaves [0, nnz] at segment %lld", what, (long long)at_pos);
+  else if (bits & kBadCrdRange)
+    snprintf(msg, cap, "%s: crd out of range at position %lld", what, (long long)at_crd);
+  else if (at_crd >= 0)
+    snprintf(msg, cap, "%s: crd not strictly increasing within a segment at position %lld",
+             what, (long long)at_crd);
+  else
+    snprintf(msg, cap, "%s: crd not strictly increasing within a segment", what);
+}
+
+// Host check of segments [s0, s1): first offending segment / position per kind.
+struct HostPart {
+  unsigned bits = 0;
+  int64_t at_pos = INT64_MAX, at_crd = INT64_MAX;
+};
+
+void host_check_range(int64_t s0, int64_t s1, int32_t inner, const int32_t* pos,
+                      const int32_t* crd, int64_t nnz, HostPart& r) {
+  for (int64_t i = s0; i < s1; i++) {
+    const int64_t a = pos[i], b = pos[i + 1];
+    if (b < a) {
+      r.bits |= kBadPosOrder;
+      r.at_pos = std::min(r.at_pos, i);
+      continue;
+    }
+    if (a < 0 || b > nnz) {
+      r.bits |= kBadPosEnd;
+      r.at_pos = std::min(r.at_pos, i);
+      continue;
+    }
+    if (!crd) continue;
+    int32_t prev = -1;
+    for (int64_t p = a; p < b; p++) {
+      const int32_t c = crd[p];
+      if (c < 0 || c >= inner) {
+        r.bits |= kBadCrdRange;
+        r.at_crd = std::min(r.at_crd, p);
+        break;
+      }
+      if (c <= prev) {
+        r.bits |= kBadCrdOrder;
+        r.at_crd = std::min(r.at_crd, p);
+        break;
+      }
+      prev = c;
+    }
+  }
+}
+
+int host_threads(int64_t work) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  if (work < (1 << 20)) return 1;
+  return (int)std::min<unsigned>(hw, 32);
+}
+
+// The whole host check; threads take chunks of segments from a shared counter.
+int host_check(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
+               const int32_t* crd, int64_t nnz, char* msg, size_t cap) {
+  if (pos[0] != 0) {
+    describe(kBadPos0, 0, 0, what, msg, cap);
+    return TACOGB_ERR_ARG;
+  }
+  if ((int64_t)pos[outer] != nnz) {
+    describe(kBadPosEnd, outer, 0, what, msg, cap);
+    return TACOGB_ERR_ARG;
+  }
+  const int nt = host_threads(outer + nnz);
+  const int64_t chunks = std::max<int64_t>(1, std::min<int64_t>(outer, (int64_t)nt * 16));
+  const int64_t per = (outer + chunks - 1) / std::max<int64_t>(chunks, 1);
+  std::vector<HostPart> parts(nt);
+  std::atomic<int64_t> next{0};
+  auto worker = [&](int t) {
+    for (;;) {
+      const int64_t k = next.fetch_add(1);
+      if (k >= chunks) break;
+      const int64_t s0 = k * per, s1 = std::min(outer, s0 + per);
+      if (s0 < s1) host_check_range(s0, s1, inner, pos, crd, nnz, parts[t]);
+    }
+  };
+  if (nt == 1) {
+    worker(0);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) th.emplace_back(worker, t);
+    for (auto& x : th) x.join();
+  }
+  HostPart all;
+  for (auto& p : parts) {
+    all.bits |= p.bits;
+    all.at_pos = std::min(all.at_pos, p.at_pos);
+    all.at_crd = std::min(all.at_crd, p.at_crd);
+  }
+  if (all.bits) {
+    describe(all.bits, all.at_pos, all.at_crd, what, msg, cap);
+    return TACOGB_ERR_ARG;
+  }
+  return 0;
+}
+
+// Device check.  out: [0] bits, [1] first bad segment, [2] first bad position, [3] descents,
+// [4] descents at the starts of non-empty segments (all zero / ~0 before the launch).
+__global__ void level_check_kernel(int64_t outer, int32_t inner, const int32_t* __restrict__ pos,
+                                   const int32_t* __restrict__ crd, int64_t nnz,
+                                   unsigned long long* __restrict__ out) {
+  unsigned bits = 0;
+  unsigned long long bad_seg = ~0ull, bad_p = ~0ull, desc = 0, desc_start = 0;
+  const int64_t n = std::max(outer, nnz);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    if (k < outer) {
+      const int64_t a = __ldg(pos + k), b = __ldg(pos + k + 1);
+      if (b < a) {
+        bits |= kBadPosOrder;
+        bad_seg = min(bad_seg, (unsigned long long)k);
+      } else if (a < 0 || b > nnz) {
+        bits |= kBadPosEnd;
+        bad_seg = min(bad_seg, (unsigned long long)k);
+      } else if (crd && a < b && a > 0) {
+        desc_start += __ldg(crd + a) <= __ldg(crd + a - 1);
+      }
+    }
+    if (k < nnz && crd) {
+      const int32_t c = __ldg(crd + k);
+      if (c < 0 || c >= inner) {
+        bits |= kBadCrdRange;
+        bad_p = min(bad_p, (unsigned long long)k);
+      }
+      if (k > 0) desc += c <= __ldg(crd + k - 1);
+    }
+  }
+  // one atomic per warp and counter
+  const unsigned lane = threadIdx.x & 31;
+  bits = __reduce_or_sync(0xffffffffu, bits);
+  for (int o = 16; o; o >>= 1) {
+    bad_seg = min(bad_seg, __shfl_xor_sync(0xffffffffu, bad_seg, o));
+    bad_p = min(bad_p, __shfl_xor_sync(0xffffffffu, bad_p, o));
+    desc += __shfl_xor_sync(0xffffffffu, desc, o);
+    desc_start += __shfl_xor_sync(0xffffffffu, desc_start, o);
+  }
+  if (lane == 0) {
+    if (bits) atomicOr(out, (unsigned long long)bits);
+    if (bad_seg != ~0ull) atomicMin(out + 1, bad_seg);
+    if (bad_p != ~0ull) atomicMin(out + 2, bad_p);
+    if (desc) atomicAdd(out + 3, desc);
+    if (desc_start) atomicAdd(out + 4, desc_start);
+  }
+}
+
+}  // namespace
+
+bool validation_on() { return g_validate.load(std::memory_order_relaxed) != 0; }
+
+int validate_level_device(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
+                          const int32_t* crd, int64_t nnz, cudaStream_t st) {
+  if (outer <= 0 && nnz <= 0) return 0;
+  TACOGB_CHECK_ARG(pos != nullptr, "%s: null pos", what);
+  // five counters in the library's scratch arena (slot reserved for the checks)
+  unsigned long long* out = (unsigned long long*)scratch(5 * sizeof(unsigned long long), 11);
+  if (!out) return last_code();
+  const unsigned long long init[5] = {0, ~0ull, ~0ull, 0, 0};
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(out, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  int32_t first = 0;
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(&first, pos, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  const int64_t n = std::max(outer, nnz);
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
+  TACOGB_LAUNCH("level_check_kernel", st,
+                level_check_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
+                    outer, inner, pos, crd, nnz, out));
+  unsigned long long h[5];
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  unsigned bits = (unsigned)h[0];
+  if (first != 0) bits |= kBadPos0;
+  if (!(bits & (kBadPosOrder | kBadPosEnd)) && h[3] != h[4]) bits |= kBadCrdOrder;
+  if (bits) {
+    // the kernel locates range errors; an order error is known from the two counts only
+    char msg[256];
+    describe(bits, (int64_t)h[1], (bits & kBadCrdRange) ? (int64_t)h[2] : -1, what, msg,
+             sizeof(msg));
+    set_error(TACOGB_ERR_ARG, "%s", msg);
+    return TACOGB_ERR_ARG;
+  }
+  return 0;
+}
+
+void LevelCheck::begin(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
+                       const int32_t* crd, int64_t nnz, bool host_resident) {
+  what_ = what;
+  outer_ = outer;
+  inner_ = inner;
+  pos_ = pos;
+  crd_ = crd;
+  nnz_ = nnz;
+  active_ = validation_on() && (outer > 0 || nnz > 0);
+  host_ = host_resident;
+  rc_ = 0;
+  msg_[0] = 0;
+  if (active_ && host_) {
+    if (!pos) {
+      rc_ = TACOGB_ERR_ARG;
+      snprintf(msg_, sizeof(msg_), "%s: null pos", what);
+      host_ = false;
+      return;
+    }
+    worker_ = std::thread([this] {
+      rc_ = host_check(what_, outer_, inner_, pos_, crd_, nnz_, msg_, sizeof(msg_));
+    });
+  }
+}
+
+int LevelCheck::finish(cudaStream_t st, const void* dpos, const void* dcrd) {
+  if (worker_.joinable()) worker_.join();
+  if (!active_) return 0;
+  active_ = false;
+  if (rc_) {
+    set_error(rc_, "%s", msg_);
+    return rc_;
+  }
+  if (host_ || !dpos) return 0;
+  return validate_level_device(what_, outer_, inner_, (const int32_t*)dpos,
+                               (const int32_t*)dcrd, nnz_, st);
+}
+
+LevelCheck::~LevelCheck() {
+  if (worker_.joinable()) worker_.join();
+}
+
+}  // namespace tacogb
+
+using namespace tacogb;
+
+extern "C" {
+
+int tacogb_set_validation(int32_t on) {
+  return g_validate.exchange(on ? 1 : 0);
+}
+
+int tacogb_validate_level_host(int64_t outer, int32_t inner, const int32_t* pos,
+                               const int32_t* crd, int64_t nnz) {
+  TACOGB_CHECK_ARG(outer >= 0 && inner >= 0 && nnz >= 0, "validate: negative size");
+  if (outer == 0 && nnz == 0) return 0;
+  TACOGB_CHECK_ARG(pos != nullptr && (nnz == 0 || crd != nullptr), "validate: null pos or crd");
+  char msg[256];
+  const int rc = host_check("level", outer, inner, pos, crd, nnz, msg, sizeof(msg));
+  if (rc) set_error(rc, "%s", msg);
+  return rc;
+}
+
+int tacogb_csr_validate(const tacogb_csr* A, void* stream) {
+  TACOGB_CHECK_ARG(A != nullptr, "validate: null matrix");
+  TACOGB_CHECK_ARG(A->rows >= 0 && A->cols >= 0 && A->nnz >= 0, "validate: negative size");
+  return validate_level_device("CSR matrix", A->rows, A->cols, A->pos, A->crd, A->nnz,
+                               (cudaStream_t)stream);
+}
+
+}  // extern "C"
