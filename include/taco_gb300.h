@@ -152,6 +152,11 @@ typedef struct tacogb_csr {
 int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, void* stream);
 int tacogb_spmv_variant_count(void);
 const char* tacogb_spmv_variant_name(int32_t variant);
+/* The variant TACOGB_VARIANT_AUTO runs for A: warp tiles sized for scattered columns, or for
+ * local columns when most gaps between consecutive stored columns (4096 samples) are under 64.
+ * The choice is cached per matrix (pos and crd pointers, rows, nonzeros); the first call for a
+ * matrix runs one small kernel on stream and synchronises it, unless the stream is capturing. */
+int tacogb_spmv_auto_variant(const tacogb_csr* A, void* stream);
 
 /* y = A x like tacogb_spmv (merge-path kernel, default accumulation per value type), for
  * callers that cannot allocate GPU memory during the call: code running under another

@@ -114,6 +114,7 @@ SIGNATURES = {
     "tacogb_spmv": (I32, [ctypes.POINTER(Csr), P, P, I32, P]),
     "tacogb_spmv_variant_count": (I32, []),
     "tacogb_spmv_variant_name": (ctypes.c_char_p, [I32]),
+    "tacogb_spmv_auto_variant": (I32, [P, P]),
     "tacogb_spmv_noalloc": (I32, [ctypes.POINTER(Csr), P, P, P]),
     "tacogb_spmv_assemble": (I32, [P, P, P]),
     "tacogb_spmv_compute": (I32, [P, P, P]),

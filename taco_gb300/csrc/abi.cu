@@ -426,6 +426,10 @@ int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, vo
   return spmv_run(A, x, y, variant, (cudaStream_t)stream);
 }
 int tacogb_spmv_variant_count(void) { return spmv_variant_count(); }
+int tacogb_spmv_auto_variant(const tacogb_csr* A, void* stream) {
+  TACOGB_CHECK_ARG(A != nullptr && A->nnz >= 0, "SpMV: bad matrix");
+  return spmv_auto_variant(A, (cudaStream_t)stream);
+}
 const char* tacogb_spmv_variant_name(int32_t v) { return spmv_variant_name(v); }
 
 int tacogb_spmm(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C,

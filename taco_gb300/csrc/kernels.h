@@ -10,6 +10,8 @@ namespace tacogb {
 int spmv_variant_count();
 const char* spmv_variant_name(int v);
 int spmv_default_variant(const tacogb_csr* A);
+// The variant TACOGB_VARIANT_AUTO runs for A (a cached per-matrix choice; may sync st once).
+int spmv_auto_variant(const tacogb_csr* A, cudaStream_t st);
 int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStream_t st);
 
 // Merge-path tile boundaries (spmv.cu): part[0..tiles] = (rows ended, nonzeros consumed) at

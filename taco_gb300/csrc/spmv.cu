@@ -46,6 +46,7 @@
 #include "kernels.h"
 #include "wmerge.cuh"
 #include "wtile.cuh"
+#include "wspec.cuh"
 
 namespace tacogb {
 
@@ -235,8 +236,11 @@ spmv_wmerge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ 
 // Warp-level merge tiles (wtile.cuh): CTA b runs tiles 4b .. 4b+3, one per warp, with no CTA
 // barrier; each tile's carry-out goes to the fix-up kernel.
 
-template <class P, int IPT, bool TMA, int CH>
-__global__ void __launch_bounds__(kWtWarps * 32, (IPT <= 7 ? 8 : IPT <= 11 ? 6 : 4))
+// DIRECT tiles store their rows straight to y (WdSmem, no staging area for row results);
+// MINB is the CTAs per SM the register allocation must allow (0: by tile size).
+template <class P, int IPT, bool TMA, int CH, bool DIRECT = false, int MINB = 0>
+__global__ void __launch_bounds__(kWtWarps * 32,
+                                  (MINB ? MINB : IPT <= 7 ? 8 : IPT <= 11 ? 6 : 4))
 spmv_wtile_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                   const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
                   const typename P::Val* __restrict__ x64, const int* __restrict__ xflag,
@@ -245,7 +249,8 @@ spmv_wtile_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ c
                   double* __restrict__ carry_val, int* status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5;
-  WtSmem<P, IPT>& s = reinterpret_cast<WtSmem<P, IPT>*>(smem_raw)[warp];
+  using S = typename std::conditional<DIRECT, WdSmem<P, IPT>, WtSmem<P, IPT>>::type;
+  S& s = reinterpret_cast<S*>(smem_raw)[warp];
   const int t = blockIdx.x * kWtWarps + warp;
   if (t >= tiles) return;  // whole warp: nothing below synchronises more than one warp
   const int2 c0 = part[t], c1 = part[t + 1];
@@ -325,10 +330,10 @@ spmv_wpipe_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ c
       int first_row;
       bool ok = xok;
       if (__all_sync(0xffffffffu, ok))
-        ok = wt_walk<P, IPT, CH>(scrd, sval, sre, xg, row, ks, row_e, ke, k0, s.y, open, first,
-                                 first_row);
+        ok = wt_walk<P, IPT, CH>(scrd, sval, sre, xg, row, ks, row_e, ke, k0, SinkSmem{s.y},
+                                 open, first, first_row);
       if (__all_sync(0xffffffffu, ok)) {
-        const typename P::Acc cc = wt_join<P>(open, row_e, first, first_row, s.y);
+        const typename P::Acc cc = wt_join<P>(open, row_e, first, first_row, SinkSmem{s.y});
         __syncwarp();
         for (int q = lane; q < rn; q += 32) {
           double v = P::to_double(as_acc<typename P::Acc>(s.y[q]));
@@ -345,8 +350,8 @@ spmv_wpipe_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ c
       typename Q::Acc open, first;
       int first_row;
       wt_walk<Q, IPT, CH>(scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64,
-                          row, ks, row_e, ke, k0, s.y, open, first, first_row);
-      const typename Q::Acc cc = wt_join<Q>(open, row_e, first, first_row, s.y);
+                          row, ks, row_e, ke, k0, SinkSmem{s.y}, open, first, first_row);
+      const typename Q::Acc cc = wt_join<Q>(open, row_e, first, first_row, SinkSmem{s.y});
       __syncwarp();
       for (int q = lane; q < rn; q += 32) {
         double v = Q::to_double(as_acc<typename Q::Acc>(s.y[q]));
@@ -626,6 +631,21 @@ const SpmvVariant kSpmvVariants[] = {
     {"wpipe_dfs_ipt7", 15, 7},   {"wpipe_dfs_ipt9", 15, 9},   {"wpipe_native_ipt7", 16, 7},
     {"wpipe_dfs_ipt7_c8", 17, 7}, {"wpipe_s_dfs_ipt7", 18, 7}, {"wpipe_s_native_ipt7", 19, 7},
     {"wpipe_s_dfs_ipt9", 18, 9},
+    // warp tiles storing rows straight to y: param = IPT + 100 * min CTAs per SM (+ 10000 for
+    // 8-deep gathers); family 20 native, 21 PolDFS, 22 hybrid
+    {"wtile_d_native_ipt7", 20, 807},    {"wtile_d_native_ipt7_b10", 20, 1007},
+    {"wtile_d_native_ipt7_b12", 20, 1207}, {"wtile_d_native_ipt9", 20, 809},
+    {"wtile_d_native_ipt11", 20, 611},   {"wtile_d_native_ipt7_c8", 20, 10807},
+    {"wtile_d_dfs_ipt7", 21, 807},       {"wtile_d_dfs_ipt9", 21, 809},
+    {"wtile_d_dfs_ipt11", 21, 611},      {"wtile_d_hyb_ipt7", 22, 807},
+    {"wtile_d_hyb_ipt11", 22, 611},      {"wtile_d_native_ipt9_b10", 20, 1009},
+    {"wtile_d_native_ipt11_b8", 20, 811}, {"wtile_d_native_ipt15_b6", 20, 615},
+    // warp-specialised persistent tiles: param = IPT + 100 * consumers + 10000 * stages;
+    // family 23 native, 24 PolDFS
+    {"wspec_native_ipt7_c12s20", 23, 201207}, {"wspec_native_ipt7_c24s40", 23, 402407},
+    {"wspec_native_ipt9_c12s16", 23, 161209}, {"wspec_native_ipt11_c8s12", 23, 120811},
+    {"wspec_native_ipt7_c8s12", 23, 120807}, {"wspec_dfs_ipt9_c12s16", 24, 161209},
+    {"wspec_dfs_ipt7_c12s20", 24, 201207},
 };
 constexpr int kNumSpmvVariants = sizeof(kSpmvVariants) / sizeof(kSpmvVariants[0]);
 
@@ -700,10 +720,10 @@ int launch_wmerge(const tacogb_csr* A, const typename P::Val* x, typename P::Out
   return 0;
 }
 
-template <class P, int IPT, int CH = 4>
+template <class P, int IPT, int CH = 4, bool DIRECT = false, int MINB = 0>
 int launch_wtile(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
                  cudaStream_t st) {
-  using S = WtSmem<P, IPT>;
+  using S = typename std::conditional<DIRECT, WdSmem<P, IPT>, WtSmem<P, IPT>>::type;
   const int64_t tile_items = S::ITEMS;
   const int64_t total = (int64_t)A->rows + A->nnz;
   const int64_t tiles64 = (total + tile_items - 1) / tile_items;
@@ -739,15 +759,82 @@ int launch_wtile(const tacogb_csr* A, const typename P::Val* x, typename P::Out*
     if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
   }
   const bool tma = (((uintptr_t)A->pos | (uintptr_t)A->crd | (uintptr_t)A->vals) & 15) == 0;
-  auto kern = tma ? spmv_wtile_kernel<P, IPT, true, CH> : spmv_wtile_kernel<P, IPT, false, CH>;
+  auto kern = tma ? spmv_wtile_kernel<P, IPT, true, CH, DIRECT, MINB>
+                  : spmv_wtile_kernel<P, IPT, false, CH, DIRECT, MINB>;
   const int smem = (int)(sizeof(S) * kWtWarps);
   TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   // carveouts measured best per tile size (random-column gathers want L1 room; the banded
   // matrices run fastest at IPT 9 with the driver's choice)
-  constexpr int carve = IPT == 7 ? 70 : IPT == 9 ? -1 : 85;
+  // direct tiles: the smallest carveout of 160 KB or 196 KB that holds MINB CTAs
+  constexpr int carve = DIRECT ? ((int)sizeof(S) * kWtWarps * MINB > 160 * 1024 ? 86 : 70)
+                        : IPT == 7 ? 70 : IPT == 9 ? -1 : 85;
   TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, carve));
   TACOGB_LAUNCH("spmv_wtile_kernel", st,
                 kern<<<grid, kWtWarps * 32, smem, st>>>(
+                    A->pos, A->crd, (const typename P::Val*)A->vals, xg, x, xflag, y, part,
+                    A->rows, (int32_t)A->nnz, tiles, crow, cval, status));
+  TACOGB_LAUNCH("spmv_carry_fixup", st,
+                spmv_carry_fixup<typename P::Out><<<(tiles + 255) / 256, 256, 0, st>>>(
+                    crow, cval, tiles, y, A->rows, xflag));
+  return 0;
+}
+
+// Warp-specialised persistent tiles (wspec.cuh): C consumer warps and one producer warp per
+// CTA over a ring of S stages, as many CTAs as fit on the GPU at once.
+template <class P, int IPT, int C, int S, int CH = 4>
+int launch_wspec(const tacogb_csr* A, const typename P::Val* x, typename P::Out* y,
+                 cudaStream_t st) {
+  static_assert(S <= 32 * (C + 1), "one thread initialises each stage's barriers");
+  using SM = WsSmem<P, IPT, S>;
+  const int64_t tile_items = 32 * IPT;
+  const int64_t total = (int64_t)A->rows + A->nnz;
+  const int64_t tiles64 = (total + tile_items - 1) / tile_items;
+  if (tiles64 == 0) return 0;
+  TACOGB_CHECK_ARG(tiles64 < (1ll << 31) - 8, "SpMV: too many merge tiles");
+  const int32_t tiles = (int32_t)tiles64;
+  // bulk copies need 16-byte aligned sources; otherwise the warp tiles' plain-load form runs
+  if ((((uintptr_t)A->pos | (uintptr_t)A->crd | (uintptr_t)A->vals) & 15) != 0)
+    return launch_wtile<P, IPT, CH, true, 8>(A, x, y, st);
+  auto kern = spmv_wspec_kernel<P, IPT, C, S, CH>;
+  const int smem = (int)sizeof(SM);
+  TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  // 160 KB of shared memory (96 KB of L1 for the gathers) unless two CTAs fit only in 196 KB
+  const bool two_in_196 = 2 * smem > 160 * 1024 && 2 * smem <= 196 * 1024;
+  TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, two_in_196 ? 86 : 70));
+  int per_sm = 0;
+  TACOGB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (C + 1) * 32,
+                                                                smem));
+  if (per_sm < 1) per_sm = 1;
+  const int grid = (int)std::min<int64_t>(tiles64, (int64_t)sm_count() * per_sm);
+  constexpr bool split = std::is_same<typename P::XG, DF>::value;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t part_bytes = al(((size_t)tiles + 1) * sizeof(int2));
+  const size_t crow_bytes = al((size_t)tiles * sizeof(int32_t));
+  const size_t cval_bytes = al((size_t)tiles * sizeof(double));
+  const size_t xdf_bytes = split ? al((size_t)A->cols * sizeof(DF)) : 0;
+  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + xdf_bytes, 0);
+  if (!ws) return last_code();
+  int2* part = (int2*)ws;
+  int32_t* crow = (int32_t*)(ws + part_bytes);
+  double* cval = (double*)(ws + part_bytes + crow_bytes);
+  int* status = device_status();
+  if (!status) return last_code();
+  const typename P::XG* xg = (const typename P::XG*)x;
+  int* xflag = nullptr;
+  if constexpr (split) {
+    DF* xdf = (DF*)(ws + part_bytes + crow_bytes + cval_bytes);
+    xflag = status + kXFlagWord;
+    const int64_t threads = rows4_threads((int64_t)A->rows + 1, A->cols);
+    TACOGB_LAUNCH("spmv_prep", st,
+                  spmv_prep<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+                      A->pos, A->rows, A->nnz, make_divu32((uint32_t)tile_items), tiles, part,
+                      (const double*)x, xdf, A->cols, xflag));
+    xg = (const typename P::XG*)xdf;
+  } else {
+    if (int rc = merge_partition(A->pos, A->rows, A->nnz, tile_items, tiles, part, st)) return rc;
+  }
+  TACOGB_LAUNCH("spmv_wspec_kernel", st,
+                kern<<<grid, (C + 1) * 32, smem, st>>>(
                     A->pos, A->crd, (const typename P::Val*)A->vals, xg, x, xflag, y, part,
                     A->rows, (int32_t)A->nnz, tiles, crow, cval, status));
   TACOGB_LAUNCH("spmv_carry_fixup", st,
@@ -935,6 +1022,46 @@ int spmv_typed(const tacogb_csr* A, const V* x, V* y, int variant, cudaStream_t 
     }
   }
   if (v.family == 14) return launch_wtile<Native, 7>(A, x, y, st);
+  if (v.family == 20) {
+    switch (v.param) {
+      case 807: return launch_wtile<Native, 7, 4, true, 8>(A, x, y, st);
+      case 1007: return launch_wtile<Native, 7, 4, true, 10>(A, x, y, st);
+      case 1207: return launch_wtile<Native, 7, 4, true, 12>(A, x, y, st);
+      case 809: return launch_wtile<Native, 9, 4, true, 8>(A, x, y, st);
+      case 611: return launch_wtile<Native, 11, 4, true, 6>(A, x, y, st);
+      case 1009: return launch_wtile<Native, 9, 4, true, 10>(A, x, y, st);
+      case 811: return launch_wtile<Native, 11, 4, true, 8>(A, x, y, st);
+      case 615: return launch_wtile<Native, 15, 4, true, 6>(A, x, y, st);
+      default: return launch_wtile<Native, 7, 8, true, 8>(A, x, y, st);
+    }
+  }
+  if (v.family == 23) {
+    switch (v.param) {
+      case 201207: return launch_wspec<Native, 7, 12, 20>(A, x, y, st);
+      case 402407: return launch_wspec<Native, 7, 24, 40>(A, x, y, st);
+      case 161209: return launch_wspec<Native, 9, 12, 16>(A, x, y, st);
+      case 120811: return launch_wspec<Native, 11, 8, 12>(A, x, y, st);
+      default: return launch_wspec<Native, 7, 8, 12>(A, x, y, st);
+    }
+  }
+  if (v.family == 24) {
+    using Pol = typename std::conditional<sizeof(V) == 8, PolDFS, PolComp32>::type;
+    if (v.param == 161209) return launch_wspec<Pol, 9, 12, 16>(A, x, y, st);
+    return launch_wspec<Pol, 7, 12, 20>(A, x, y, st);
+  }
+  if (v.family == 21) {
+    using Pol = typename std::conditional<sizeof(V) == 8, PolDFS, PolComp32>::type;
+    switch (v.param) {
+      case 807: return launch_wtile<Pol, 7, 4, true, 8>(A, x, y, st);
+      case 809: return launch_wtile<Pol, 9, 4, true, 8>(A, x, y, st);
+      default: return launch_wtile<Pol, 11, 4, true, 6>(A, x, y, st);
+    }
+  }
+  if (v.family == 22) {
+    using Hyb = typename std::conditional<sizeof(V) == 8, PolHybrid, PolComp32>::type;
+    if (v.param == 807) return launch_wtile<Hyb, 7, 4, true, 8>(A, x, y, st);
+    return launch_wtile<Hyb, 11, 4, true, 6>(A, x, y, st);
+  }
   if (v.family == 15 || v.family == 17) {
     using Pol = typename std::conditional<sizeof(V) == 8, PolDFS, PolComp32>::type;
     if (v.family == 17) return launch_wpipe<Pol, 7, 8>(A, x, y, st);
@@ -977,18 +1104,99 @@ const char* spmv_variant_name(int v) {
   return (v >= 0 && v < kNumSpmvVariants) ? kSpmvVariants[v].name : "";
 }
 
-// Structural rule used when neither a tuning record nor the cost model gives a choice: warp
-// merge tiles are robust to any skew; with no CTA-wide joins the per-tile FP64 work is small,
-// so native DFMA accumulation (taco's own arithmetic) keeps pace with the x gathers that bound
-// random-column matrices (measured fastest on the 4,194,304-row power-law workload).
+// ---- the library's choice of variant (TACOGB_VARIANT_AUTO) ----
+//
+// Measured on GB300 (FP64 and compensated FP32): warp tiles that store their rows straight to y
+// are fastest on every workload, but the best tile shape depends on where the x gathers go.
+// Scattered columns (the power-law matrix) need the L1 for the gathers: 11 items per lane with
+// 160 KB of shared memory (96 KB of L1) — 0.433 ms per 1.0e8 nonzeros in FP64.  Local columns
+// (the banded matrix) gather from few lines: 9 items per lane with ten CTAs per SM in 196 KB of
+// shared memory — 0.413 ms per 1.34e8 nonzeros, where the scattered choice takes 0.494 ms and
+// the local choice on the power-law matrix 0.664 ms.  A matrix is local when most gaps between
+// consecutive stored columns are short: one small kernel counts, over 4096 evenly spaced
+// nonzeros, how many have |crd[p+1] - crd[p]| < 64 (one or a few x lines).  The decision is
+// cached per matrix (pos and crd pointers, rows, nonzeros), so an iterated SpMV pays for the
+// count once; a call made while its stream is being captured uses the scattered choice without
+// counting.
+
+namespace {
+
+constexpr int kLocalSamples = 4096;
+constexpr int kLocalGap = 64;
+
+__global__ void spmv_locality_kernel(const int32_t* __restrict__ crd, int64_t nnz,
+                                     int32_t* __restrict__ out) {
+  __shared__ int warp_count[8];
+  int c = 0;
+  for (int i = threadIdx.x; i < kLocalSamples; i += blockDim.x) {
+    const int64_t p = (nnz - 1) * (int64_t)i / kLocalSamples;  // p + 1 < nnz
+    c += abs(__ldg(crd + p + 1) - __ldg(crd + p)) < kLocalGap;
+  }
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0) warp_count[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += warp_count[w];
+    *out = t;
+  }
+}
+
+struct AutoEntry {
+  const void* pos;
+  const void* crd;
+  int32_t rows;
+  int64_t nnz;
+  int variant;
+};
+std::mutex g_auto_mu;
+AutoEntry g_auto[32];
+int g_auto_next = 0;
+
+int variant_index(const char* name) {
+  for (int i = 0; i < kNumSpmvVariants; i++)
+    if (std::string(kSpmvVariants[i].name) == name) return i;
+  return 0;
+}
+
+}  // namespace
+
 int spmv_default_variant(const tacogb_csr* A) {
   (void)A;
-  static const int v = [] {
-    for (int i = 0; i < kNumSpmvVariants; i++)
-      if (std::string(kSpmvVariants[i].name) == "wtile_native_ipt7") return i;
-    return 0;
-  }();
-  return v;  // wtile_native_ipt7: DFMA for FP64 values, compensated FP32 for FP32
+  static const int v = variant_index("wtile_d_native_ipt11");
+  return v;  // the scattered-column choice: DFMA for FP64 values, compensated FP32 for FP32
+}
+
+// The variant TACOGB_VARIANT_AUTO runs for A on stream st (see above).
+int spmv_auto_variant(const tacogb_csr* A, cudaStream_t st) {
+  static const int scattered = variant_index("wtile_d_native_ipt11");
+  static const int local = variant_index("wtile_d_native_ipt9_b10");
+  if (A->nnz < 2 * kLocalSamples) return scattered;
+  {
+    std::lock_guard<std::mutex> lk(g_auto_mu);
+    for (const AutoEntry& e : g_auto)
+      if (e.pos == A->pos && e.crd == A->crd && e.rows == A->rows && e.nnz == A->nnz)
+        return e.variant;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return scattered;
+  }
+  int32_t* dcount = (int32_t*)scratch(256, 11);
+  if (!dcount) return scattered;
+  count_launch();
+  spmv_locality_kernel<<<1, 256, 0, st>>>(A->crd, A->nnz, dcount);
+  int32_t h = 0;
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(&h, dcount, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return scattered;
+  const int v = 2 * h > kLocalSamples ? local : scattered;
+  std::lock_guard<std::mutex> lk(g_auto_mu);
+  g_auto[g_auto_next] = AutoEntry{A->pos, A->crd, A->rows, A->nnz, v};
+  g_auto_next = (g_auto_next + 1) % 32;
+  return v;
 }
 
 int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStream_t st) {
@@ -1000,7 +1208,7 @@ int spmv_run(const tacogb_csr* A, const void* x, void* y, int variant, cudaStrea
   TACOGB_CHECK_ARG(A->rows == 0 || A->pos != nullptr, "SpMV: null pos");
   TACOGB_CHECK_ARG(A->nnz == 0 || (A->crd != nullptr && A->vals != nullptr),
                    "SpMV: null crd/vals");
-  if (variant < 0) variant = spmv_default_variant(A);
+  if (variant < 0) variant = spmv_auto_variant(A, st);
   TACOGB_CHECK_ARG(variant < kNumSpmvVariants, "SpMV: variant %d out of range", variant);
   if (A->vtype == TACOGB_F64)
     return spmv_typed<double>(A, (const double*)x, (double*)y, variant, st);

@@ -28,18 +28,49 @@ struct alignas(16) WtSmem {
   uint64_t bar;
 };
 
+// The same staging area without the row-result array, for tiles whose rows go straight to y
+// (3.7 KB per warp at IPT 7 instead of 5.5 KB, so more warps fit on an SM).
+template <class P, int IPT>
+struct alignas(16) WdSmem {
+  using Val = typename P::Val;
+  static constexpr int ITEMS = 32 * IPT;
+  static constexpr int VPAD = 16 / sizeof(Val);
+  alignas(16) int32_t crd[ITEMS + 8];
+  alignas(16) Val val[ITEMS + 2 * VPAD];
+  alignas(16) int32_t re[ITEMS + 8];
+  uint64_t bar;
+};
+
+// Where a warp tile puts the sums of the rows that end in it: staged in shared memory (written
+// to y by one coalesced pass after the join) or stored straight to y (y + the tile's first row).
+struct SinkSmem {
+  double* ys;
+  template <class P>
+  __device__ __forceinline__ void put(int r, typename P::Acc v) const {
+    as_acc<typename P::Acc>(ys[r]) = v;
+  }
+};
+template <class Out>
+struct SinkDirect {
+  Out* yg;
+  template <class P>
+  __device__ __forceinline__ void put(int r, typename P::Acc v) const {
+    yg[r] = (Out)P::out(v);
+  }
+};
+
 // Stages one warp tile: lane 0 issues bulk copies over the 16-byte-aligned spans of crd, vals
 // and pos; every lane loads its share of the sub-16-byte tails; every lane then waits (bounded)
 // on the warp's mbarrier.  Without TMA (unaligned bases) the lanes load everything.
-template <bool TMA, class P, int IPT>
-__device__ __forceinline__ void wt_stage(WtSmem<P, IPT>& s, const int32_t* __restrict__ pos,
+template <bool TMA, class P, int IPT, class S>
+__device__ __forceinline__ void wt_stage(S& s, const int32_t* __restrict__ pos,
                                          const int32_t* __restrict__ crd,
                                          const typename P::Val* __restrict__ vals, int32_t n,
                                          int32_t nnz, int r0, int rn, int k0, int kn, int* status,
                                          const int32_t*& scrd, const typename P::Val*& sval,
                                          const int32_t*& sre) {
   using Val = typename P::Val;
-  constexpr int VP = WtSmem<P, IPT>::VPAD;
+  constexpr int VP = S::VPAD;
   const int lane = threadIdx.x & 31;
   const int k1 = k0 + kn;
   const int q0 = r0 + 1, q1 = r0 + 1 + rn;  // pos indices of the row ends
@@ -77,17 +108,17 @@ __device__ __forceinline__ void wt_stage(WtSmem<P, IPT>& s, const int32_t* __res
 }
 
 // Walks this lane's merge items [(row, ks), (row_e, ke)) over the staged tile with policy P,
-// gathering x in chunks of CH independent loads.  Rows that end inside the lane's range are
-// stored in ys, except the first one (which may have begun in an earlier lane): its sum is
+// gathering x in chunks of CH independent loads.  Rows that end inside the lane's range go to
+// the sink, except the first one (which may have begun in an earlier lane): its sum is
 // returned in `first` (first_row = its tile-local index, -1 if none).  Returns the sum of the
 // open row at the lane's end in `open`, and false when a checked policy met an out-of-range
 // value.
-template <class P, int IPT, int CH>
+template <class P, int IPT, int CH, class Sink>
 __device__ __forceinline__ bool wt_walk(const int32_t* scrd, const typename P::Val* sval,
                                         const int32_t* sre, const typename P::XG* __restrict__ x,
-                                        int row, int ks, int row_e, int ke, int k0, double* ys,
-                                        typename P::Acc& open, typename P::Acc& first,
-                                        int& first_row) {
+                                        int row, int ks, int row_e, int ke, int k0,
+                                        const Sink& sink, typename P::Acc& open,
+                                        typename P::Acc& first, int& first_row) {
   using Acc = typename P::Acc;
   using Val = typename P::Val;
   using XG = typename P::XG;
@@ -105,7 +136,7 @@ __device__ __forceinline__ bool wt_walk(const int32_t* scrd, const typename P::V
       first_row = r;
       first = v;
     } else {
-      as_acc<Acc>(ys[r]) = v;
+      sink.template put<P>(r, v);
     }
     row = r + 1;
     next_end = row < row_e ? sre[row] - base : INT_MAX;
@@ -141,25 +172,30 @@ __device__ __forceinline__ bool wt_walk(const int32_t* scrd, const typename P::V
 // by the open row (non-decreasing along the lanes), then each lane adds the preceding lanes'
 // part to its first ended row.  Returns (every lane) the sum of the row still open at the
 // tile's end, which is lane 31's key.
-template <class P>
+template <class P, class Sink>
 __device__ __forceinline__ typename P::Acc wt_join(typename P::Acc open, int key,
                                                    typename P::Acc first, int first_row,
-                                                   double* ys) {
+                                                   const Sink& sink) {
   using Acc = typename P::Acc;
   const int lane = threadIdx.x & 31;
   Acc sc = open;
+  // A step whose distance no run of equal keys spans is skipped, and so are the longer ones
+  // (keys never decrease along the lanes): on GB300 an FP64 add costs the FP64 pipe the same
+  // with one lane active as with 32, and short rows need one or two steps, not five.
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
-    const Acc o = P::shfl_up(sc, d);
     const int ko = __shfl_up_sync(0xffffffffu, key, d);
-    if (lane >= d && ko == key) sc = P::add(o, sc);
+    const bool need = lane >= d && ko == key;
+    if (!__any_sync(0xffffffffu, need)) break;
+    const Acc o = P::shfl_up(sc, d);
+    if (need) sc = P::add(o, sc);
   }
   const Acc prev = P::shfl_up(sc, 1);
   const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
   if (first_row >= 0) {
     Acc tot = first;
     if (lane > 0 && kprev == first_row) tot = P::add(prev, first);
-    as_acc<Acc>(ys[first_row]) = tot;
+    sink.template put<P>(first_row, tot);
   }
   Acc out;
   if constexpr (sizeof(Acc) == 8 && std::is_same<Acc, double>::value) {
@@ -173,9 +209,9 @@ __device__ __forceinline__ typename P::Acc wt_join(typename P::Acc open, int key
 // One warp tile with policy P (native redo for checked policies); writes the rows ending in the
 // tile and returns the FP64 carry-out (every lane).  first_val (lane 0, when rn > 0) is the FP64
 // value written for the tile's first row.
-template <class P, int IPT, bool TMA, int CH>
+template <class P, int IPT, bool TMA, int CH, class S>
 __device__ __forceinline__ double wt_process(
-    WtSmem<P, IPT>& s, const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+    S& s, const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
     const typename P::Val* __restrict__ vals, const typename P::XG* __restrict__ xg,
     const typename P::Val* __restrict__ x64, const int* __restrict__ xflag,
     typename P::Out* __restrict__ y, int32_t n, int32_t nnz, int r0, int rn, int k0, int kn,
@@ -184,6 +220,8 @@ __device__ __forceinline__ double wt_process(
   const int32_t* scrd;
   const typename P::Val* sval;
   const int32_t* sre;
+  // direct tiles (no y staging area) store their rows straight to y
+  constexpr bool kDirect = std::is_same<S, WdSmem<P, IPT>>::value;
   wt_stage<TMA, P, IPT>(s, pos, crd, vals, n, nnz, r0, rn, k0, kn, status, scrd, sval, sre);
   // lane starts on the merge path; lane 31 ends at the tile end (rn, kn)
   int row, ks;
@@ -199,31 +237,53 @@ __device__ __forceinline__ double wt_process(
     typename P::Acc open, first;
     int first_row;
     bool ok = (xflag == nullptr || *xflag == 0);
-    if (__all_sync(0xffffffffu, ok))
-      ok = wt_walk<P, IPT, CH>(scrd, sval, sre, xg, row, ks, row_e, ke, k0, s.y, open, first,
-                               first_row);
-    if (__all_sync(0xffffffffu, ok)) {
-      const typename P::Acc c = wt_join<P>(open, row_e, first, first_row, s.y);
-      __syncwarp();
-      for (int i = lane; i < rn; i += 32) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
-      if (lane == 0 && rn > 0) first_val = P::to_double(as_acc<typename P::Acc>(s.y[0]));
-      carry = P::to_double(c);
+    if constexpr (kDirect) {
+      const SinkDirect<typename P::Out> sink{y + r0};
+      if (__all_sync(0xffffffffu, ok))
+        ok = wt_walk<P, IPT, CH>(scrd, sval, sre, xg, row, ks, row_e, ke, k0, sink, open, first,
+                                 first_row);
+      if (__all_sync(0xffffffffu, ok)) {
+        carry = P::to_double(wt_join<P>(open, row_e, first, first_row, sink));
+      } else {
+        native = true;
+      }
     } else {
-      native = true;
+      const SinkSmem sink{s.y};
+      if (__all_sync(0xffffffffu, ok))
+        ok = wt_walk<P, IPT, CH>(scrd, sval, sre, xg, row, ks, row_e, ke, k0, sink, open, first,
+                                 first_row);
+      if (__all_sync(0xffffffffu, ok)) {
+        const typename P::Acc c = wt_join<P>(open, row_e, first, first_row, sink);
+        __syncwarp();
+        for (int i = lane; i < rn; i += 32) y[r0 + i] = P::out(as_acc<typename P::Acc>(s.y[i]));
+        if (lane == 0 && rn > 0) first_val = P::to_double(as_acc<typename P::Acc>(s.y[0]));
+        carry = P::to_double(c);
+      } else {
+        native = true;
+      }
     }
   }
   if (native) {
     using Q = typename std::conditional<P::kChecked, PolNative64, P>::type;
     typename Q::Acc open, first;
     int first_row;
-    wt_walk<Q, IPT, CH>(scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64, row,
-                        ks, row_e, ke, k0, s.y, open, first, first_row);
-    const typename Q::Acc c = wt_join<Q>(open, row_e, first, first_row, s.y);
-    __syncwarp();
-    for (int i = lane; i < rn; i += 32)
-      y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
-    if (lane == 0 && rn > 0) first_val = Q::to_double(as_acc<typename Q::Acc>(s.y[0]));
-    carry = Q::to_double(c);
+    if constexpr (kDirect) {
+      // rows a checked first pass stored are stored again here
+      const SinkDirect<typename P::Out> sink{y + r0};
+      wt_walk<Q, IPT, CH>(scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64,
+                          row, ks, row_e, ke, k0, sink, open, first, first_row);
+      carry = Q::to_double(wt_join<Q>(open, row_e, first, first_row, sink));
+    } else {
+      const SinkSmem sink{s.y};
+      wt_walk<Q, IPT, CH>(scrd, (const typename Q::Val*)sval, sre, (const typename Q::XG*)x64,
+                          row, ks, row_e, ke, k0, sink, open, first, first_row);
+      const typename Q::Acc c = wt_join<Q>(open, row_e, first, first_row, sink);
+      __syncwarp();
+      for (int i = lane; i < rn; i += 32)
+        y[r0 + i] = (typename P::Out)Q::out(as_acc<typename Q::Acc>(s.y[i]));
+      if (lane == 0 && rn > 0) first_val = Q::to_double(as_acc<typename Q::Acc>(s.y[0]));
+      carry = Q::to_double(c);
+    }
   }
   return carry;
 }

@@ -253,3 +253,28 @@ def test_abi_csc_operand_and_mismatch():
     Y4, A3 = T.dense(np.zeros(4), [4]), T.csr(*D33A, [3, 3])
     rc = _abi("tacogb_spmv_compute", Y4, A3, X)
     assert rc != 0 and b"rows" in tg.lib().tacogb_last_error()
+
+
+@pytest.mark.parametrize("which", ["powerlaw", "banded", "small_rows"])
+def test_auto_variant_choice(which):
+    """TACOGB_VARIANT_AUTO picks the local-column tiles for banded columns and the
+    scattered-column tiles otherwise, caches the choice per matrix, and computes exactly what
+    the chosen variant computes."""
+    s = {"powerlaw": lambda: W.spmv_powerlaw(rows=300000),
+         "banded": lambda: W.spmv_banded(rows=300000),
+         "small_rows": lambda: W.spec(5000, kind=W.UNIFORM, len_lo=0, len_hi=3, seed=5)}[which]()
+    pos, crd, vals = W.generate(s)
+    x = W.dense(24, s.cols)
+    A = tg.CsrMatrix.from_numpy(pos, crd, vals, s.cols)
+    c = A.as_csr()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    v = tg.lib().tacogb_spmv_auto_variant(ctypes.byref(c), sp)
+    assert v == tg.lib().tacogb_spmv_auto_variant(ctypes.byref(c), sp)  # cached
+    name = tg.spmv_variants()[v]
+    expect = "wtile_d_native_ipt9_b10" if which == "banded" else "wtile_d_native_ipt11"
+    assert name == expect
+    xd = torch.from_numpy(x).cuda()
+    y_auto = tg.spmv(A, xd).cpu().numpy()
+    y_v = tg.spmv(A, xd, variant=v).cpu().numpy()
+    assert np.array_equal(y_auto, y_v)
+    assert normwise(y_auto, O.spmv(pos, crd, vals, x)) <= F64_TOL
