@@ -64,6 +64,8 @@ def parse(argv=None):
                    help="sddmm_powerlaw: rows (and columns) of B (0 = 1,048,576); mttkrp_nell2: "
                         "B's first dimension (0 = 12,092)")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="skip the secondary workloads the default run reports beside the headline")
     a = p.parse_args(argv)
     if a.n is None:
         a.n = 32 if a.workload == "batched_spmm" else 64
@@ -490,6 +492,35 @@ class SpgemmOp:
         d2h = (self.rows + 1) * 4 + self.nnzC * 12
         return step, keep, h2d, d2h, "tacogb_spgemm_evaluate(taco_tensor_t*) on pinned host arrays"
 
+    def _taco_step(self, pattern):
+        """One assemble + compute of taco's generated code for `pattern` (a callable that
+        returns nnz(C) and frees C's arrays)."""
+        import ctypes.util
+        from oracle import oracle as O
+        from taco_gb300 import taco as T
+        libc = ctypes.CDLL(ctypes.util.find_library("c"))
+        libc.free.argtypes = [ctypes.c_void_p]
+        At = T.csr(self.pos, self.crd, self.vals, [self.rows, self.cols])
+        L = O.ref_lib(pattern)
+
+        def once():
+            Ct = T.csr_result([self.rows, self.cols])
+            L.assemble(Ct.ptr, At.ptr, At.ptr)
+            L.compute(Ct.ptr, At.ptr, At.ptr)
+            nnzC = ctypes.cast(Ct.index(1, 0), ctypes.POINTER(ctypes.c_int32))[self.rows]
+            for q in (Ct.index(1, 0), Ct.index(1, 1), Ct.vals_ptr):
+                libc.free(q)
+            return nnzC
+        return once, At
+
+    def cpu_serial(self):
+        """taco's default (serial) generated SpGEMM, timed beside the scheduled one."""
+        from oracle import oracle as O
+        if not O.ref_available("spgemm"):
+            return None
+        once, At = self._taco_step("spgemm")
+        return once, At
+
     def cpu(self):
         import ctypes.util
         from oracle import oracle as O
@@ -497,6 +528,13 @@ class SpgemmOp:
         libc = ctypes.CDLL(ctypes.util.find_library("c"))
         libc.free.argtypes = [ctypes.c_void_p]
         At = T.csr(self.pos, self.crd, self.vals, [self.rows, self.cols])
+        if O.ref_available("spgemm_sched"):
+            # taco's parallel two-pass schedule (scheduleSpGEMMCPU) on all host cores
+            once, At = self._taco_step("spgemm_sched")
+            self.set_nnzC(int(once()))
+            self.cpu_sample_desc = ("whole workload, taco's scheduleSpGEMMCPU (parallel two-pass "
+                                    "assembly, dense workspace) on all threads")
+            return "reference", once, (At,)
         if O.ref_available("spgemm"):
             L = O.ref_lib("spgemm")
 
@@ -1144,8 +1182,10 @@ def main_batch(args, torch, tg, T, L, rank, world):
                       "kinds": kinds_used,
                       "l2": "inputs larger than L2 (%.1f GB per step), no flush" % (op.bytes / 1e9)},
            "fp64_per_matrix": {"gflops": op.flops / (ms64 / 1e3) / 1e9, "ms_per_step": ms64,
-                               "launch": "tacogb_spmv default FP64 path (wtile_native_ipt7), one call per "
-                                         "matrix from a host loop", "steps": k64},
+                               "launch": "tacogb_spmv with TACOGB_VARIANT_AUTO (the library's own "
+                                         "choice per matrix, DFMA accumulation), one call per "
+                                         "matrix from a host loop, after 3 untimed passes",
+                               "steps": k64},
            "speedup_vs_fp64_per_matrix": ms64 / ms,
            "max_normwise_err_vs_fp64": max_err,
            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
@@ -1253,6 +1293,56 @@ def main_batch_spmm(args, torch, tg, L, rank):
 
 # ----------------------------------------------------------------------------- main
 
+# The workloads the default run measures beside the headline, each in its own process (the
+# same bench.py, so the same code paths and timing rules), summarised into the headline line.
+SECONDARY = [
+    ("spmv_small_f64 (L2-resident: 13.9 MB fits the 129 MB L2)",
+     ["--workload", "spmv_small", "--steps", "500", "--warmup", "20", "--e2e-steps", "10"]),
+    ("spmv_banded_f64", ["--workload", "spmv_banded", "--steps", "50", "--warmup", "5",
+                         "--e2e-steps", "5"]),
+    ("spmv_powerlaw_f32c", ["--workload", "spmv_powerlaw", "--dtype", "f32", "--steps", "50",
+                            "--warmup", "5", "--e2e-steps", "5"]),
+    ("spmm_powerlaw_n64_f64", ["--workload", "spmm_powerlaw", "--n", "64", "--steps", "20",
+                               "--warmup", "3", "--e2e-steps", "3"]),
+    ("spgemm_random_f64", ["--workload", "spgemm_random", "--steps", "20", "--warmup", "3",
+                           "--e2e-steps", "3"]),
+    ("batched_spmv_4096_f32c_learned", ["--workload", "batched_spmv", "--dtype", "f32",
+                                        "--select", "learned", "--steps", "5", "--warmup", "3"]),
+]
+
+
+def run_secondary():
+    keys = ("metric", "value", "unit", "ms_per_step", "dtype", "gpu_launches", "clocks",
+            "speedup_vs_fp64_per_matrix", "max_normwise_err_vs_fp64", "derived", "variant")
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT")}
+    out = []
+    for name, argv in SECONDARY:
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--no-secondary"]
+                               + argv, cwd=ROOT, env=env, stdout=subprocess.PIPE,
+                               stderr=subprocess.PIPE, text=True, timeout=400)
+            line = [l for l in r.stdout.splitlines() if l.startswith("{")]
+            if r.returncode != 0 or not line:
+                out.append({"workload": name, "error": (r.stderr or r.stdout)[-300:]})
+                continue
+            d = json.loads(line[-1])
+        except subprocess.TimeoutExpired:
+            out.append({"workload": name, "error": "timed out"})
+            continue
+        e = {"workload": name, "config": d.get("config")}
+        e.update({k: d[k] for k in keys if k in d})
+        rf = d.get("roofline") or {}
+        e["roofline"] = {k: rf.get(k) for k in ("bound", "achieved", "peak", "unit", "frac",
+                                                 "traffic", "kernel", "kernel_ms")}
+        e["cpu_baseline"] = d.get("cpu_baseline")
+        e["e2e"] = d.get("e2e")
+        e["wall_s"] = time.perf_counter() - t0
+        out.append(e)
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1359,6 +1449,7 @@ def main():
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "steps": args.e2e_steps, "ms_per_step": e2e_s / args.e2e_steps * 1e3, "api": api}
         del akeep
+        e2e["link"] = host_link(torch, h2d, d2h)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -1369,6 +1460,19 @@ def main():
                "sample": "%s, median of %d reps" % (getattr(op, "cpu_sample_desc",
                                                             "whole workload"), reps),
                "ms_per_step": t * 1e3}
+        serial = op.cpu_serial() if hasattr(op, "cpu_serial") else None
+        if serial is not None:
+            once, keep_s = serial
+            once()
+            ts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                once()
+                ts.append(time.perf_counter() - t0)
+            cpu["serial"] = {"value": cpu_work / float(np.median(ts)) / 1e9, "unit": unit,
+                             "cores": 1, "ms_per_step": float(np.median(ts)) * 1e3,
+                             "code": "taco's default generated SpGEMM (serial)"}
+            del keep_s
 
     if rank == 0:
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
@@ -1397,9 +1501,36 @@ def main():
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clocks,
                "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kernels.items()}}
+        if args.workload == "spmv_powerlaw" and args.dtype == "f64" and world == 1 and \
+                not args.no_secondary:
+            torch.cuda.empty_cache()
+            out["secondary"] = run_secondary()
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def host_link(torch, h2d, d2h, reps=5):
+    """What the host link alone allows for a step's copies: one pinned host -> device copy of
+    h2d bytes and one device -> host copy of d2h bytes, timed back to back (the bound of the
+    e2e number, which moves the same bytes)."""
+    if h2d <= 0:
+        return None
+    hb = torch.empty(h2d, dtype=torch.uint8).pin_memory()
+    db = torch.empty(h2d, dtype=torch.uint8, device="cuda")
+    hy = torch.empty(max(d2h, 1), dtype=torch.uint8).pin_memory()
+    dy = torch.empty(max(d2h, 1), dtype=torch.uint8, device="cuda")
+    db.copy_(hb, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        db.copy_(hb, non_blocking=True)
+        if d2h > 0:
+            hy.copy_(dy, non_blocking=True)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    return {"ms_per_step": ms, "h2d_gbs": h2d / (ms / 1e3) / 1e9,
+            "how": "pinned copies of the step's bytes alone (cudaMemcpyAsync via torch)"}
 
 
 def gather_ceiling(torch, L, reps=5):

@@ -68,8 +68,10 @@ int tacogb_device_status(int32_t* status);
  * it: pos[0] == 0, pos non-decreasing with pos[outer] == nnz, 0 <= crd < the level's dimension,
  * and crd strictly increasing within each segment (taco's sorted, distinct coordinates).  A
  * violation returns TACOGB_ERR_ARG naming the first offending segment or position.
- * Host-resident levels are checked by host threads while the call's copies to the GPU run;
- * device-resident levels by one kernel reading pos and crd once.  The device layer (tacogb_spmv
+ * The check is one kernel reading pos and crd once, on the arrays the kernels will read (the
+ * caller's device arrays or the staged copies of host arrays), before any gathering kernel; a
+ * call that cannot reach a GPU checks host-resident levels on the host, so invalid input is
+ * still reported as TACOGB_ERR_ARG.  The device layer (tacogb_spmv
  * and the other functions on tacogb_csr) trusts its arguments; tacogb_csr_validate checks a
  * device CSR explicitly.  tacogb_set_validation(0) turns the taco-ABI checks off (and returns the
  * previous setting); they are on by default. */
@@ -152,10 +154,11 @@ typedef struct tacogb_csr {
 int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, void* stream);
 int tacogb_spmv_variant_count(void);
 const char* tacogb_spmv_variant_name(int32_t variant);
-/* The variant TACOGB_VARIANT_AUTO runs for A: warp tiles sized for scattered columns, or for
- * local columns when most gaps between consecutive stored columns (4096 samples) are under 64.
- * The choice is cached per matrix (pos and crd pointers, rows, nonzeros); the first call for a
- * matrix runs one small kernel on stream and synchronises it, unless the stream is capturing. */
+/* The variant TACOGB_VARIANT_AUTO runs for A: warp tiles sized for scattered columns, or, for a
+ * matrix of at least 2^20 nonzeros, for local columns when most gaps between consecutive stored
+ * columns (4096 samples) are under 64.  The choice is cached per matrix (pos and crd pointers,
+ * rows, nonzeros); the first call for such a matrix runs one small kernel on stream and
+ * synchronises it, unless the stream is capturing. */
 int tacogb_spmv_auto_variant(const tacogb_csr* A, void* stream);
 
 /* y = A x like tacogb_spmv (merge-path kernel, default accumulation per value type), for

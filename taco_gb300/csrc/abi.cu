@@ -251,20 +251,34 @@ int stage_in(Operand& o, const void* p, size_t bytes, int slot, cudaStream_t st)
 }
 
 // Stages one compressed level (pos: outer + 1 entries, crd: nnz entries, and optionally the
-// values: vbytes) into slots slot, slot + 1, slot + 2 while the level is checked (validate.h):
-// host-resident arrays by host threads during the copies, device-resident ones by a kernel.
-// A failed check is reported before any error of the staging.
-int stage_checked_level(const char* what, int64_t outer, int32_t inner, int64_t nnz,
-                        const void* pos, const void* crd, const void* vals, size_t vbytes,
-                        int slot, cudaStream_t st, Operand& op, Operand& oc, Operand* ov) {
-  LevelCheck chk;
+// values: vbytes) into slots slot, slot + 1, slot + 2 and checks it (validate.h) on the arrays
+// the kernels will read.  A failed check is reported before any error of the staging.
+// The same without the check yet: chk records the level, and the caller runs
+// chk.finish(st, op.dev, oc.dev) once it has issued its other copies, so that the check's
+// synchronisation waits for all of them together.  When the staging fails, chk diagnoses
+// host-resident input first.
+int stage_level(const char* what, int64_t outer, int32_t inner, int64_t nnz, const void* pos,
+                const void* crd, const void* vals, size_t vbytes, int slot, cudaStream_t st,
+                Operand& op, Operand& oc, Operand* ov, LevelCheck& chk) {
   chk.begin(what, outer, inner, (const int32_t*)pos, (const int32_t*)crd, nnz,
             !device_accessible(pos) && !device_accessible(crd));
   int src = stage_in(op, pos, ((size_t)outer + 1) * 4, slot, st);
   if (!src) src = stage_in(oc, crd, (size_t)nnz * 4, slot + 1, st);
   if (!src && ov) src = stage_in(*ov, vals, vbytes, slot + 2, st);
-  if (int rc = chk.finish(st, src == 0 ? op.dev : nullptr, oc.dev)) return rc;
+  if (src) {
+    if (int rc = chk.finish(st, nullptr, nullptr)) return rc;
+  }
   return src;
+}
+
+int stage_checked_level(const char* what, int64_t outer, int32_t inner, int64_t nnz,
+                        const void* pos, const void* crd, const void* vals, size_t vbytes,
+                        int slot, cudaStream_t st, Operand& op, Operand& oc, Operand* ov) {
+  LevelCheck chk;
+  if (int rc = stage_level(what, outer, inner, nnz, pos, crd, vals, vbytes, slot, st, op, oc, ov,
+                           chk))
+    return rc;
+  return chk.finish(st, op.dev, oc.dev);
 }
 
 int value_type_of_csize(int32_t csize) {
@@ -683,10 +697,12 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
 
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ox;
-  if (int rc = stage_checked_level("spmv operand A", rows, cols, nnz, pos, crd, A->vals,
-                                   (size_t)nnz * vb, 0, st, opos, ocrd, &ovals))
+  LevelCheck chk;
+  if (int rc = stage_level("spmv operand A", rows, cols, nnz, pos, crd, A->vals, (size_t)nnz * vb,
+                           0, st, opos, ocrd, &ovals, chk))
     return rc;
   if (int rc = stage_in(ox, x->vals, (size_t)cols * vb, 3, st)) return rc;
+  if (int rc = chk.finish(st, opos.dev, ocrd.dev)) return rc;
   void* ydev = y->vals;
   const bool y_staged = !device_accessible(y->vals);
   if (y_staged) {
@@ -792,10 +808,12 @@ int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   if (int rc = read_i32(pos + rows, &nnz)) return rc;
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ob;
-  if (int rc = stage_checked_level("spmm operand A", rows, cols, nnz, pos, crd, A->vals,
-                                   (size_t)nnz * value_bytes(at), 0, st, opos, ocrd, &ovals))
+  LevelCheck chk;
+  if (int rc = stage_level("spmm operand A", rows, cols, nnz, pos, crd, A->vals,
+                           (size_t)nnz * value_bytes(at), 0, st, opos, ocrd, &ovals, chk))
     return rc;
   if (int rc = stage_in(ob, B->vals, (size_t)cols * N * value_bytes(bt), 3, st)) return rc;
+  if (int rc = chk.finish(st, opos.dev, ocrd.dev)) return rc;
   const size_t cbytes = (size_t)rows * N * value_bytes(ct);
   void* cdev = C->vals;
   const bool c_staged = !device_accessible(C->vals);
@@ -1129,11 +1147,13 @@ int tacogb_sddmm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, t
   const bool dense = !is_csr_result(A);
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, oc, od;
-  if (int rc = stage_checked_level("sddmm operand B", I, K, nnz, pos, B->indices[1][1], B->vals,
-                                   (size_t)nnz * vb, 20, st, opos, ocrd, &ovals))
+  LevelCheck chk;
+  if (int rc = stage_level("sddmm operand B", I, K, nnz, pos, B->indices[1][1], B->vals,
+                           (size_t)nnz * vb, 20, st, opos, ocrd, &ovals, chk))
     return rc;
   if (int rc = stage_in(oc, C->vals, (size_t)I * J * vb, 23, st)) return rc;
   if (int rc = stage_in(od, D->vals, (size_t)J * K * vb, 24, st)) return rc;
+  if (int rc = chk.finish(st, opos.dev, ocrd.dev)) return rc;
   const size_t obytes = dense ? (size_t)I * (size_t)K * vb : (size_t)nnz * vb;
   void* odev = A->vals;
   const bool staged = !device_accessible(A->vals);

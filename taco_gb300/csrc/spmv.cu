@@ -40,6 +40,7 @@
 #include <mutex>
 #include <string>
 #include <type_traits>
+#include <unordered_map>
 
 #include "common.cuh"
 #include "df.cuh"
@@ -1116,8 +1117,8 @@ const char* spmv_variant_name(int v) {
 // consecutive stored columns are short: one small kernel counts, over 4096 evenly spaced
 // nonzeros, how many have |crd[p+1] - crd[p]| < 64 (one or a few x lines).  The decision is
 // cached per matrix (pos and crd pointers, rows, nonzeros), so an iterated SpMV pays for the
-// count once; a call made while its stream is being captured uses the scattered choice without
-// counting.
+// count once; a call made while its stream is being captured, and any matrix of fewer than
+// 2^20 nonzeros, uses the scattered choice without counting.
 
 namespace {
 
@@ -1142,16 +1143,18 @@ __global__ void spmv_locality_kernel(const int32_t* __restrict__ crd, int64_t nn
   }
 }
 
+// Matrices this small run the scattered choice without a count: the count and its
+// synchronisation would cost more than the choice can save.
+constexpr int64_t kLocalMinNnz = (int64_t)1 << 20;
+
 struct AutoEntry {
   const void* pos;
-  const void* crd;
   int32_t rows;
   int64_t nnz;
   int variant;
 };
 std::mutex g_auto_mu;
-AutoEntry g_auto[32];
-int g_auto_next = 0;
+std::unordered_map<const void*, AutoEntry> g_auto;  // keyed by crd
 
 int variant_index(const char* name) {
   for (int i = 0; i < kNumSpmvVariants; i++)
@@ -1171,12 +1174,13 @@ int spmv_default_variant(const tacogb_csr* A) {
 int spmv_auto_variant(const tacogb_csr* A, cudaStream_t st) {
   static const int scattered = variant_index("wtile_d_native_ipt11");
   static const int local = variant_index("wtile_d_native_ipt9_b10");
-  if (A->nnz < 2 * kLocalSamples) return scattered;
+  if (A->nnz < kLocalMinNnz) return scattered;
   {
     std::lock_guard<std::mutex> lk(g_auto_mu);
-    for (const AutoEntry& e : g_auto)
-      if (e.pos == A->pos && e.crd == A->crd && e.rows == A->rows && e.nnz == A->nnz)
-        return e.variant;
+    const auto it = g_auto.find(A->crd);
+    if (it != g_auto.end() && it->second.pos == A->pos && it->second.rows == A->rows &&
+        it->second.nnz == A->nnz)
+      return it->second.variant;
   }
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
@@ -1194,8 +1198,8 @@ int spmv_auto_variant(const tacogb_csr* A, cudaStream_t st) {
     return scattered;
   const int v = 2 * h > kLocalSamples ? local : scattered;
   std::lock_guard<std::mutex> lk(g_auto_mu);
-  g_auto[g_auto_next] = AutoEntry{A->pos, A->crd, A->rows, A->nnz, v};
-  g_auto_next = (g_auto_next + 1) % 32;
+  if (g_auto.size() >= 65536) g_auto.clear();  // bounded: a long-running caller starts over
+  g_auto[A->crd] = AutoEntry{A->pos, A->rows, A->nnz, v};
   return v;
 }
 

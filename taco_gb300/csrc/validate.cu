@@ -9,10 +9,13 @@
 //   0 <= crd[p] < inner,  crd strictly increasing within each segment [pos[i], pos[i+1]),
 // and a violation returns TACOGB_ERR_ARG with the first offending index.
 //
-// Host-resident levels (taco without CUDA, pinned buffers) are checked by host threads that run
-// while the call's copies to the GPU proceed, so the check costs no time on the copy-bound
-// path.  Device-resident levels (managed or device memory) are checked by one streaming kernel
-// that reads pos and crd once, in bounds: crd is read at [0, nnz) only, pos at [0, outer].
+// The check runs on the GPU, on the arrays the kernels will read (the caller's device or managed
+// arrays, or the staged copies of host arrays): one streaming kernel that reads pos and crd
+// once, in bounds (crd at [0, nnz) only, pos at [0, outer]), then one synchronisation to read
+// the verdict before any gathering kernel is launched.  When a call cannot reach a GPU at all,
+// host-resident levels are checked on the host instead, so that invalid input is still reported
+// as TACOGB_ERR_ARG rather than as the missing device; tacogb_validate_level_host exposes that
+// host check (multi-threaded for large levels).
 // Sortedness on the GPU: a descent (crd[p] <= crd[p-1]) is legal only where p starts a
 // non-empty segment, so the kernel counts all descents and the descents at segment starts; the
 // two counts agree exactly when every segment is sorted.
@@ -243,36 +246,19 @@ void LevelCheck::begin(const char* what, int64_t outer, int32_t inner, const int
   nnz_ = nnz;
   active_ = validation_on() && (outer > 0 || nnz > 0);
   host_ = host_resident;
-  rc_ = 0;
-  msg_[0] = 0;
-  if (active_ && host_) {
-    if (!pos) {
-      rc_ = TACOGB_ERR_ARG;
-      snprintf(msg_, sizeof(msg_), "%s: null pos", what);
-      host_ = false;
-      return;
-    }
-    worker_ = std::thread([this] {
-      rc_ = host_check(what_, outer_, inner_, pos_, crd_, nnz_, msg_, sizeof(msg_));
-    });
-  }
 }
 
 int LevelCheck::finish(cudaStream_t st, const void* dpos, const void* dcrd) {
-  if (worker_.joinable()) worker_.join();
   if (!active_) return 0;
   active_ = false;
-  if (rc_) {
-    set_error(rc_, "%s", msg_);
-    return rc_;
-  }
-  if (host_ || !dpos) return 0;
-  return validate_level_device(what_, outer_, inner_, (const int32_t*)dpos,
-                               (const int32_t*)dcrd, nnz_, st);
-}
-
-LevelCheck::~LevelCheck() {
-  if (worker_.joinable()) worker_.join();
+  if (dpos)
+    return validate_level_device(what_, outer_, inner_, (const int32_t*)dpos,
+                                 (const int32_t*)dcrd, nnz_, st);
+  if (!host_ || !pos_) return 0;  // nothing reached the GPU: the staging error is reported
+  char msg[256];
+  const int rc = host_check(what_, outer_, inner_, pos_, crd_, nnz_, msg, sizeof(msg));
+  if (rc) set_error(rc, "%s", msg);
+  return rc;
 }
 
 }  // namespace tacogb

@@ -2,7 +2,6 @@
 #pragma once
 
 #include <cstdint>
-#include <thread>
 
 #include <cuda_runtime.h>
 
@@ -17,17 +16,16 @@ bool validation_on();
 int validate_level_device(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
                           const int32_t* crd, int64_t nnz, cudaStream_t st);
 
-// One level's check around a call's staging: begin() starts host threads on host-resident
-// arrays (so the check overlaps the copies to the GPU); finish() joins them, or, when the level
-// is not host-resident, runs validate_level_device on its device copies dpos/dcrd.  finish()
-// reports a failed check before anything else, so call it before returning any error of the
-// staging in between (dpos null skips the device check after a failed staging).
+// One level's check around a call's staging: begin() records the level as the caller passed it;
+// finish() checks the device copies dpos/dcrd the kernels will read (validate_level_device), or,
+// when the staging failed (dpos null) and the level is host-resident, checks it on the host so
+// that invalid input is reported before the staging error.  Call finish() before returning any
+// error of the staging in between.
 class LevelCheck {
  public:
   void begin(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
              const int32_t* crd, int64_t nnz, bool host_resident);
   int finish(cudaStream_t st, const void* dpos, const void* dcrd);
-  ~LevelCheck();
 
  private:
   const char* what_ = "";
@@ -36,9 +34,6 @@ class LevelCheck {
   const int32_t* pos_ = nullptr;
   const int32_t* crd_ = nullptr;
   bool active_ = false, host_ = false;
-  int rc_ = 0;
-  char msg_[256] = "";
-  std::thread worker_;
 };
 
 }  // namespace tacogb

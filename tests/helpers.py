@@ -277,11 +277,12 @@ def ref_sddmm(pos, crd, vals, C, D, threads=1):
     return A
 
 
-def ref_spgemm(A, B, threads=1):
+def ref_spgemm(A, B, threads=1, pattern="spgemm"):
     """taco's generated SpGEMM (assemble then compute) on host CSR arrays; A, B = (pos, crd,
-    vals, cols).  Returns (pos, crd, vals) of C copied out of the arrays taco allocated."""
+    vals, cols).  Returns (pos, crd, vals) of C copied out of the arrays taco allocated.
+    pattern "spgemm_sched" runs taco's parallel two-pass schedule (scheduleSpGEMMCPU)."""
     import ctypes
-    L = O.ref_lib("spgemm")
+    L = O.ref_lib(pattern)
     O.ref_set_threads(threads)
     (ap, ac, av, acols), (bp, bc, bv, bcols) = A, B
     rows = len(ap) - 1

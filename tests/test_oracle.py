@@ -8,6 +8,7 @@ import pytest
 
 from oracle import oracle as O
 from taco_gb300 import workloads as W
+from tests import helpers as H
 from tests.helpers import normwise, ref_spmv, taco_rand_csr
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
@@ -182,3 +183,18 @@ def test_taco_generated_sparse_result_kat():
     crd, vals = ref_spmv_formats("dcsr_sv", kp, kc, kv, 3, None,
                                  (np.array([0, 2], np.int32), np.array([2., 3.])))
     assert list(crd) == [0, 2] and list(vals) == [0, 18]
+
+
+@pytest.mark.skipif(not O.ref_available("spgemm_sched"), reason="taco generated code not built here")
+@pytest.mark.parametrize("case", ["spgemm_taco_rand", "spgemm_random_512", "spgemm_poisson_32"])
+def test_scheduled_spgemm_matches_serial(case):
+    """taco's parallel two-pass SpGEMM (scheduleSpGEMMCPU, test/tests-scheduling-eval.cpp:68-94,
+    emitted by taco's CLI with the same scheduling directives) against the golden fixtures made
+    by taco's serial default code, on 4 threads: pos, crd and values bit for bit."""
+    g = np.load(os.path.join(GOLDEN, case + ".npz"))
+    K = int(g["K"][0])
+    A = (g["Apos"], g["Acrd"], g["Avals"], len(g["Bpos"]) - 1)
+    B = (g["Bpos"], g["Bcrd"], g["Bvals"], K)
+    cp, cc, cv = H.ref_spgemm(A, B, threads=4, pattern="spgemm_sched")
+    assert np.array_equal(cp, g["Cpos"]) and np.array_equal(cc, g["Ccrd"])
+    assert np.array_equal(cv, g["Cvals"])
