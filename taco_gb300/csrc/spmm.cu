@@ -23,6 +23,7 @@
 //   F32 values/B  native: FFMA.  df: TwoProduct/TwoSum-compensated FP32.
 //   F32 values, BF16 B: FFMA in FP32 (B converted by a shift), C in FP32.
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
@@ -71,7 +72,36 @@ spmm_merge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ c
   }
 }
 
-// Adds carried partial rows, in tile order, into the row where each run of tiles ends.
+// The TMA-staged warp tile (spmm_tile_tma): one ring of S B-row slots per warp in dynamic
+// shared memory.  Checked policies redo a tile natively (register-staged stream tile) when a
+// value or B entry is out of range.
+template <class P, int VEC, int S>
+__global__ void __launch_bounds__(kMmBlock, 3)
+spmm_tma_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
+                const typename P::AV* __restrict__ vals, const typename P::BV* __restrict__ B,
+                const double* __restrict__ B64, const int* __restrict__ bflag,
+                typename P::Out* __restrict__ C, int32_t n, int32_t N,
+                const int2* __restrict__ part, int32_t tiles, int32_t* __restrict__ carry_row,
+                double* __restrict__ carry_val, int* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.x * kMmWarps + warp;
+  if (tile >= tiles) return;
+  MmRing<P, VEC, S>& ring = reinterpret_cast<MmRing<P, VEC, S>*>(smem_raw)[warp];
+  const int colt = blockIdx.y * (32 * VEC);
+  const int2 c0 = part[tile], c1 = part[tile + 1];
+  bool ok = !P::kChecked || bflag == nullptr || *bflag == 0;
+  if (ok)
+    ok = spmm_tile_tma<P, VEC, S>(ring, pos, crd, vals, B, C, n, N, c0, c1, tile, colt, status,
+                                  carry_row, carry_val);
+  if constexpr (P::kChecked) {
+    if (!__all_sync(0xffffffffu, ok))
+      spmm_tile_stream<MmNative64, VEC>(pos, crd, (const double*)vals, B64, (double*)C, n, N, c0,
+                                        c1, tile, colt + lane * VEC, true, carry_row, carry_val);
+  }
+}
+
+// Adds carried partial rows, in tile order, into the row where each run of tiles ends.// Adds carried partial rows, in tile order, into the row where each run of tiles ends.
 // bflag (optional) is the B-range flag of the product, cleared here for the next one.
 template <typename Out>
 __global__ void spmm_carry_fixup(const int32_t* __restrict__ carry_row,
@@ -146,6 +176,7 @@ struct SpmmVariant {
   int lpr;          // 0: warp tile (spmm_tile); else sub-warp tile with LPR lanes per B row
   bool shared;      // sub-warp tile: every row shared by the whole warp (column slabs)
   bool stream;      // warp tile walked as one stream of nonzeros (spmm_tile_stream)
+  int tma;          // > 0: streaming tile with B rows staged by bulk copies, this many in flight
 };
 
 const SpmmVariant kSpmmVariants[] = {
@@ -166,10 +197,14 @@ const SpmmVariant kSpmmVariants[] = {
     {"stream_w512_native", 0, 512, 0, false, true},
     {"stream_w512_dfs", 2, 512, 0, false, true},
     {"stream_w1024_dfs", 2, 1024, 0, false, true},
+    {"tma12_w512_dfs", 2, 512, 0, false, true, 12},
+    {"tma16_w512_dfs", 2, 512, 0, false, true, 16},
+    {"tma12_w512_native", 0, 512, 0, false, true, 12},
+    {"tma12_w512_df", 1, 512, 0, false, true, 12},
 };
 constexpr int kNumSpmmVariants = sizeof(kSpmmVariants) / sizeof(kSpmmVariants[0]);
 
-template <class P, int VEC, bool STREAM>
+template <class P, int VEC, bool STREAM, int TMA = 0>
 int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, cudaStream_t st) {
   const int64_t total = (int64_t)A->rows + A->nnz;
   const int64_t tiles64 = (total + W - 1) / W;
@@ -205,10 +240,25 @@ int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, c
   constexpr int TW = 32 * VEC;
   dim3 grid((unsigned)((tiles + kMmWarps - 1) / kMmWarps), (unsigned)((N + TW - 1) / TW));
   TACOGB_CHECK_ARG(grid.y <= 65535, "SpMM: N too large");
-  TACOGB_LAUNCH("spmm_merge_kernel", st,
-                (spmm_merge_kernel<P, VEC, STREAM><<<grid, kMmBlock, 0, st>>>(
-                    A->pos, A->crd, (const typename P::AV*)A->vals, Bk, (const double*)B, bflag,
-                    (typename P::Out*)C, A->rows, N, part, tiles, crow, cval)));
+  if constexpr (TMA > 0) {
+    int* status = device_status();
+    if (!status) return last_code();
+    auto kern = spmm_tma_kernel<P, VEC, TMA>;
+    const int smem = (int)(sizeof(MmRing<P, VEC, TMA>) * kMmWarps);
+    TACOGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    // room for the three CTAs per SM the registers allow
+    const int pct = std::min(100, (3 * smem * 100 + 228 * 1024 - 1) / (228 * 1024));
+    TACOGB_CUDA_TRY(set_gather_carveout((const void*)kern, pct));
+    TACOGB_LAUNCH("spmm_tma_kernel", st,
+                  (kern<<<grid, kMmBlock, smem, st>>>(
+                      A->pos, A->crd, (const typename P::AV*)A->vals, Bk, (const double*)B, bflag,
+                      (typename P::Out*)C, A->rows, N, part, tiles, crow, cval, status)));
+  } else {
+    TACOGB_LAUNCH("spmm_merge_kernel", st,
+                  (spmm_merge_kernel<P, VEC, STREAM><<<grid, kMmBlock, 0, st>>>(
+                      A->pos, A->crd, (const typename P::AV*)A->vals, Bk, (const double*)B,
+                      bflag, (typename P::Out*)C, A->rows, N, part, tiles, crow, cval)));
+  }
   const int64_t fix_threads = (int64_t)tiles * N;
   TACOGB_LAUNCH("spmm_carry_fixup", st,
                 spmm_carry_fixup<typename P::Out><<<(unsigned)((fix_threads + 255) / 256), 256, 0,
@@ -288,14 +338,37 @@ int spmm_dispatch_sub(const tacogb_csr* A, int32_t N, const void* B, void* C, in
   }
 }
 
+// TMA-staged tiles for ring depth S: the widest lane vector whose column tile divides N, with
+// B's row segments 16-byte aligned; otherwise the register-staged streaming tile.
+template <class P, int S>
+int spmm_dispatch_tma(const tacogb_csr* A, int32_t N, const void* B, void* C, int W,
+                      cudaStream_t st) {
+  constexpr int esz = sizeof(typename P::BV);
+  const bool al16 = ((uintptr_t)B & 15) == 0 && ((int64_t)N * esz) % 16 == 0;
+  if constexpr (esz == 8) {
+    if (al16 && N % 64 == 0) return launch_spmm<P, 2, true, S>(A, N, B, C, W, st);
+  } else if constexpr (esz == 4) {
+    if (al16 && N % 128 == 0) return launch_spmm<P, 4, true, S>(A, N, B, C, W, st);
+  } else {
+    if (al16 && N % 256 == 0) return launch_spmm<P, 8, true, S>(A, N, B, C, W, st);
+  }
+  return -1;  // not applicable: the caller runs the streaming tile
+}
+
 // Widest lane vector (up to 16 bytes) whose column tile divides N.
-template <class P, bool STREAM = false>
+template <class P, bool STREAM = false, int TMA = 0>
 int spmm_dispatch_vec(const tacogb_csr* A, int32_t N, const void* B, void* C, int W,
                       cudaStream_t st) {
   if constexpr (std::is_same<P, MmDFS>::value) {
     // the B split works on 16-byte pairs of elements
     if (N % 2 != 0 || ((uintptr_t)B & 15) != 0)
       return spmm_dispatch_vec<MmDF64, STREAM>(A, N, B, C, W, st);
+  }
+  if constexpr (TMA > 0) {
+    // the split B (MmDFS) lives in the library's scratch, 256-byte aligned, so the test on the
+    // caller's B (16-byte aligned, N even) above covers it too
+    const int rc = spmm_dispatch_tma<P, TMA>(A, N, B, C, W, st);
+    if (rc >= 0) return rc;
   }
   constexpr int esz = sizeof(typename P::BV);
   if constexpr (esz == 8) {
@@ -366,6 +439,8 @@ int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void*
   } else {
     auto run = [&](auto tag) -> int {
       using P = decltype(tag);
+      if (v.tma == 12) return spmm_dispatch_vec<P, true, 12>(A, N, B, C, W, st);
+      if (v.tma == 16) return spmm_dispatch_vec<P, true, 16>(A, N, B, C, W, st);
       return v.stream ? spmm_dispatch_vec<P, true>(A, N, B, C, W, st)
                       : spmm_dispatch_vec<P, false>(A, N, B, C, W, st);
     };

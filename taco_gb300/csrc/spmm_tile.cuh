@@ -424,6 +424,197 @@ __device__ __forceinline__ bool spmm_tile_stream(const int32_t* __restrict__ pos
   return ok;
 }
 
+// ------------------------------------------------------------------ TMA-staged warp tile ---
+//
+// The streaming warp tile with its B rows staged by bulk copies (cp.async.bulk) instead of
+// register loads.  Each warp keeps a ring of S slots in shared memory, one slot per nonzero
+// holding the warp's TW = 32 * VEC columns of that nonzero's B row, each completing on its own
+// mbarrier.  Lane 0 keeps the copies of the next S nonzeros in flight (re-arming U slots at a
+// time after the lanes have read them), so S B rows per warp are in flight without holding any
+// registers, where the register-staged tile holds kMmUnroll.  Waits are bounded
+// (mbar_wait_or_flag); a wait that gives up records the timeout in the status word and the walk
+// goes on, so every copy issued is waited for again before the warp exits.  Needs every lane
+// active (N a multiple of TW) and B's row segments 16-byte aligned.
+
+template <class P, int VEC, int S>
+struct alignas(16) MmRing {
+  alignas(16) typename P::BV row[S][32 * VEC];
+  uint64_t bar[S];
+};
+
+template <int VEC>
+__device__ __forceinline__ void smem_vec(const double* p, double (&o)[VEC]) {
+  if constexpr (VEC == 2) {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+  } else {
+    o[0] = p[0];
+  }
+}
+template <int VEC>
+__device__ __forceinline__ void smem_vec(const float* p, float (&o)[VEC]) {
+  if constexpr (VEC == 4) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  } else if constexpr (VEC == 2) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    o[0] = v.x; o[1] = v.y;
+  } else {
+    o[0] = p[0];
+  }
+}
+template <int VEC>
+__device__ __forceinline__ void smem_vec(const __nv_bfloat16* p, float (&o)[VEC]) {
+  if constexpr (VEC == 8) {
+    const uint4 v = *reinterpret_cast<const uint4*>(p);
+    o[0] = bf16_lo(v.x); o[1] = bf16_hi(v.x); o[2] = bf16_lo(v.y); o[3] = bf16_hi(v.y);
+    o[4] = bf16_lo(v.z); o[5] = bf16_hi(v.z); o[6] = bf16_lo(v.w); o[7] = bf16_hi(v.w);
+  } else if constexpr (VEC == 4) {
+    const uint2 v = *reinterpret_cast<const uint2*>(p);
+    o[0] = bf16_lo(v.x); o[1] = bf16_hi(v.x); o[2] = bf16_lo(v.y); o[3] = bf16_hi(v.y);
+  } else if constexpr (VEC == 2) {
+    const unsigned int v = *reinterpret_cast<const unsigned int*>(p);
+    o[0] = bf16_lo(v); o[1] = bf16_hi(v);
+  } else {
+    o[0] = bf16_lo((unsigned int)*reinterpret_cast<const unsigned short*>(p));
+  }
+}
+template <int VEC>
+__device__ __forceinline__ void smem_vec(const DF* p, DF (&o)[VEC]) {
+  if constexpr (VEC == 2) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = DF{v.x, v.y};
+    o[1] = DF{v.z, v.w};
+  } else {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    o[0] = DF{v.x, v.y};
+  }
+}
+
+template <class P, int VEC, int S>
+__device__ __forceinline__ bool spmm_tile_tma(MmRing<P, VEC, S>& ring,
+                                              const int32_t* __restrict__ pos,
+                                              const int32_t* __restrict__ crd,
+                                              const typename P::AV* __restrict__ vals,
+                                              const typename P::BV* __restrict__ B,
+                                              typename P::Out* __restrict__ C, int32_t n,
+                                              int32_t N, int2 c0, int2 c1, int tile, int colt,
+                                              int* status, int32_t* __restrict__ carry_row,
+                                              double* __restrict__ carry_val) {
+  using Acc = typename P::Acc;
+  using Prep = typename P::Prep;
+  using BE = typename P::BE;
+  using AV = typename P::AV;
+  using BV = typename P::BV;
+  constexpr int U = kMmUnroll;
+  constexpr uint32_t kRowBytes = 32 * VEC * sizeof(BV);
+  static_assert(S >= U && S <= 32, "ring depth");
+  static_assert(kRowBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+  const int lane = threadIdx.x & 31;
+  const int col0 = colt + lane * VEC;
+  const int r0 = c0.x, k0 = c0.y, r1 = c1.x, k1 = c1.y;
+  bool ok = true;
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < S; q++) mbar_init(&ring.bar[q], 1);
+  }
+  __syncwarp();
+  auto issue = [&](int g, int c) {  // lane 0: nonzero g's B row segment into its slot
+    const int q = (g - k0) % S;
+    mbar_arrive_expect_tx(&ring.bar[q], kRowBytes);
+    tma_load_bulk(ring.row[q], B + (int64_t)c * N + colt, kRowBytes, &ring.bar[q]);
+  };
+  int rb = r0;
+  int re = (rb + lane < r1) ? __ldg(pos + rb + lane + 1) : INT_MAX;
+  int row = r0;
+  int next_end = __shfl_sync(0xffffffffu, re, 0);
+  bool open_nonempty = false;
+  Acc acc[VEC];
+#pragma unroll
+  for (int v = 0; v < VEC; v++) acc[v] = P::zero();
+  auto emit = [&]() {
+    typename P::Out o[VEC];
+#pragma unroll
+    for (int v = 0; v < VEC; v++) o[v] = P::out(acc[v]);
+    store_vec<VEC>(C + (int64_t)row * N + col0, o);
+#pragma unroll
+    for (int v = 0; v < VEC; v++) acc[v] = P::zero();
+    open_nonempty = false;
+    row++;
+    if (row - rb == 32) {
+      rb = row;
+      re = (rb + lane < r1) ? __ldg(pos + rb + lane + 1) : INT_MAX;
+    }
+    next_end = __shfl_sync(0xffffffffu, re, row - rb);
+  };
+  // crd/vals of the chunk being walked (mc, mv) and of the next one (mc_n, mv_n)
+  int mc_n = 0;
+  AV mv_n = AV();
+  if (k0 + lane < k1) {
+    mc_n = __ldg(crd + k0 + lane);
+    mv_n = vals[k0 + lane];
+  }
+  // prologue: the first S nonzeros' rows (their columns are all in the first chunk)
+  {
+    const int m = min(S, k1 - k0);
+    for (int u = 0; u < m; u++) {
+      const int c = __shfl_sync(0xffffffffu, mc_n, u);
+      if (lane == 0) issue(k0 + u, c);
+    }
+  }
+  for (int base = k0; base < k1; base += 32) {
+    const int cnt = min(32, k1 - base);
+    const int mc = mc_n;
+    const Prep ma = lane < cnt ? P::prep(mv_n, ok) : Prep();
+    if (base + 32 + lane < k1) {
+      mc_n = __ldg(crd + base + 32 + lane);
+      mv_n = vals[base + 32 + lane];
+    }
+    for (int j = 0; j < cnt; j += U) {
+      const int m = min(U, cnt - j);
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (u < m) {
+          const int g = base + j + u;
+          const int q = g - k0;
+          if (!mbar_wait_or_flag(&ring.bar[q % S], (uint32_t)((q / S) & 1), status)) ok = false;
+          BE b[VEC];
+          smem_vec<VEC>(&ring.row[q % S][lane * VEC], b);
+          while (next_end <= g) emit();
+          const Prep a = P::shfl(ma, j + u);
+#pragma unroll
+          for (int v = 0; v < VEC; v++) P::madd(acc[v], a, b[v], ok);
+          open_nonempty = true;
+        }
+      }
+      // re-arm the slots just read with the rows S nonzeros ahead (columns from this chunk or
+      // the next; S <= 32 keeps them within the two chunks held)
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int jj = j + u + S;
+        const int ca = __shfl_sync(0xffffffffu, mc, jj & 31);
+        const int cb = __shfl_sync(0xffffffffu, mc_n, jj & 31);
+        if (lane == 0 && u < m && base + jj < k1) {
+          if (u == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          issue(base + jj, jj < 32 ? ca : cb);
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < VEC; v++) renorm<P>(acc[v]);
+  }
+  while (row < r1) emit();
+  const bool carried = row < n && open_nonempty;
+  if (carried) {
+#pragma unroll
+    for (int v = 0; v < VEC; v++) carry_val[(int64_t)tile * N + col0 + v] = P::to_double(acc[v]);
+  }
+  if (lane == 0 && blockIdx.y == 0) carry_row[tile] = carried ? r1 : n;
+  return ok;
+}
+
 // ------------------------------------------------------------------ sub-warp tile --------
 //
 // For narrow dense operands (N*sizeof(B) of 128 bytes or less, N=32 in the batched workload) one
