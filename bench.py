@@ -426,8 +426,10 @@ class BatchSpmmOp(BatchOp):
 
 
 class SpgemmOp:
-    """Two-phase C = A A: symbolic (C pos, nnz(C) read back), column fill, numeric values.
-    One step = all three phases, with C's arrays allocated once for the known nnz(C)."""
+    """C = A A with every structural product kept, columns sorted per row.  One step = the
+    one-pass product (pos and nnz(C) read back, then columns and values moved into C's arrays,
+    allocated once for the known nnz(C)); --variant 1 runs the three phases (symbolic, column
+    fill, numeric) instead."""
     pattern = "spgemm"
 
     def __init__(self, args):
@@ -464,14 +466,21 @@ class SpgemmOp:
         vals = torch.empty(max(nnz.value, 1), dtype=torch.float64, device="cuda")
         keep = (A, a, pos, crd, vals, nnz)
 
-        def step(sp):
+        def phases(sp):
             tg.check(L.tacogb_spgemm_symbolic(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
                                               ctypes.byref(nnz), sp), "symbolic")
             tg.check(L.tacogb_spgemm_fill(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
                                           crd.data_ptr(), sp), "fill")
             tg.check(L.tacogb_spgemm_numeric(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
                                              crd.data_ptr(), vals.data_ptr(), sp), "numeric")
-        return step, keep
+
+        def onepass(sp):
+            tg.check(L.tacogb_spgemm_onepass(ctypes.byref(a), ctypes.byref(a), pos.data_ptr(),
+                                             ctypes.byref(nnz), sp), "onepass")
+            tg.check(L.tacogb_spgemm_onepass_finish(pos.data_ptr(), crd.data_ptr(),
+                                                    vals.data_ptr(), sp), "onepass_finish")
+        # --variant 1: the three phases (symbolic, fill, numeric); default: one pass
+        return (phases if self.args.variant == 1 else onepass), keep
 
     def abi(self, torch, tg, T):
         import ctypes.util
@@ -1476,7 +1485,7 @@ def main():
 
     if rank == 0:
         names_v = {"spmv": tg.spmv_variants, "spmm": tg.spmm_variants,
-                   "sddmm": tg.sddmm_variants, "spgemm": lambda: ["default"],
+                   "sddmm": tg.sddmm_variants, "spgemm": lambda: ["one pass", "phases"],
                    "mttkrp": tg.spmm_variants, "ttm": tg.spmm_variants,
                    "ttv": tg.spmv_variants,
                    "pack": lambda: ["default"]}[op.pattern]()

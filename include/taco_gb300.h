@@ -283,6 +283,16 @@ int tacogb_spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* 
                        int32_t* Ccrd, void* stream);
 int tacogb_spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
                           const int32_t* Ccrd, void* Cvals, void* stream);
+/* The same product in one pass, as taco's assemble-while-compute (one sort per row where the
+ * three phases sort three times): tacogb_spgemm_onepass writes Cpos and returns nnz(C)
+ * (synchronises the stream), leaving C's columns and values in library scratch; the caller
+ * allocates Ccrd and Cvals for nnz(C) and tacogb_spgemm_onepass_finish moves them there (same
+ * device, same stream, before the next one-pass product on that device).  Same results as the
+ * three phases, bit for bit.  Products beyond int32 are refused (TACOGB_ERR_ARG): use the
+ * phases. */
+int tacogb_spgemm_onepass(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos,
+                          int64_t* nnzC, void* stream);
+int tacogb_spgemm_onepass_finish(const int32_t* Cpos, int32_t* Ccrd, void* Cvals, void* stream);
 
 /* SDDMM, A(i,k) = B(i,k) * C(i,j) * D(j,k): B CSR (rows I, cols K), C dense row-major I x J,
  * D dense row-major J x K, all of B's value type (FP64 or FP32).  tacogb_sddmm writes the result

@@ -188,6 +188,9 @@ SIGNATURES = {
                                       ctypes.POINTER(I64), P]),
     "tacogb_spgemm_fill": (I32, [ctypes.POINTER(Csr), ctypes.POINTER(Csr), P, P, P]),
     "tacogb_spgemm_numeric": (I32, [ctypes.POINTER(Csr), ctypes.POINTER(Csr), P, P, P, P]),
+    "tacogb_spgemm_onepass": (I32, [ctypes.POINTER(Csr), ctypes.POINTER(Csr), P,
+                                    ctypes.POINTER(I64), P]),
+    "tacogb_spgemm_onepass_finish": (I32, [P, P, P, P]),
     "tacogb_spgemm_assemble": (I32, [P, P, P]),
     "tacogb_spgemm_compute": (I32, [P, P, P]),
     "tacogb_spgemm_evaluate": (I32, [P, P, P]),

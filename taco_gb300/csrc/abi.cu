@@ -85,8 +85,8 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 12;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3, formats x3,
-                                   // index validation
+constexpr int kScratchSlots = 14;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3, formats x3,
+                                   // index validation, one-pass SpGEMM x2
 
 struct DeviceState {
   int sms = 0;
@@ -464,6 +464,13 @@ int tacogb_spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* 
 int tacogb_spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
                           const int32_t* Ccrd, void* Cvals, void* stream) {
   return spgemm_numeric(A, B, Cpos, Ccrd, Cvals, (cudaStream_t)stream);
+}
+int tacogb_spgemm_onepass(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos,
+                          int64_t* nnzC, void* stream) {
+  return spgemm_onepass(A, B, Cpos, nnzC, (cudaStream_t)stream);
+}
+int tacogb_spgemm_onepass_finish(const int32_t* Cpos, int32_t* Ccrd, void* Cvals, void* stream) {
+  return spgemm_onepass_finish(Cpos, Ccrd, Cvals, (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------- SpMV taco ABI -----------
@@ -988,9 +995,38 @@ int tacogb_spgemm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) 
   return consume_device_status();
 }
 
+// evaluate = assemble and compute in one pass (spgemm_onepass): one sort per row.
 int tacogb_spgemm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
-  if (int rc = tacogb_spgemm_assemble(C, A, B)) return rc;
-  return tacogb_spgemm_compute(C, A, B);
+  if (int rc = check_spgemm(C, A, B)) return rc;
+  cudaStream_t st = lib_stream();
+  tacogb_csr a, b;
+  if (int rc = csr_operand("spgemm operand A", A, 60, true, st, a)) return rc;
+  if (int rc = csr_operand("spgemm operand B", B, 70, true, st, b)) return rc;
+  const int32_t rows = a.rows;
+  const bool managed = device_accessible(A->indices[1][0]);
+  int32_t* dpos = (int32_t*)stage_buffer(6, ((size_t)rows + 1) * 4);
+  if (!dpos) return TACOGB_ERR_ALLOC;
+  int64_t nnz = 0;
+  if (int rc = spgemm_onepass(&a, &b, dpos, &nnz, st)) return rc;
+  const size_t vb = value_bytes(a.vtype);
+  int32_t* pos = (int32_t*)alloc_result(((size_t)rows + 1) * 4, managed);
+  int32_t* crd = (int32_t*)alloc_result((size_t)nnz * 4, managed);
+  void* vals = alloc_result((size_t)nnz * vb, managed);
+  if (!pos || !crd || !vals) return TACOGB_ERR_ALLOC;
+  int32_t* dcrd = managed ? crd : (int32_t*)stage_buffer(7, (size_t)nnz * 4);
+  void* dvals = managed ? vals : stage_buffer(9, (size_t)nnz * vb);
+  if (!dcrd || !dvals) return TACOGB_ERR_ALLOC;
+  if (int rc = spgemm_onepass_finish(dpos, dcrd, dvals, st)) return rc;
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, dpos, ((size_t)rows + 1) * 4, cudaMemcpyDefault, st));
+  if (!managed && nnz) {
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(crd, dcrd, (size_t)nnz * 4, cudaMemcpyDeviceToHost, st));
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(vals, dvals, (size_t)nnz * vb, cudaMemcpyDeviceToHost, st));
+  }
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  C->indices[1][0] = (uint8_t*)pos;
+  C->indices[1][1] = (uint8_t*)crd;
+  C->vals = (uint8_t*)vals;
+  return consume_device_status();
 }
 
 int _shim_tacogb_spgemm_assemble(void** a) {

@@ -31,6 +31,11 @@ int spgemm_symbolic(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int
                     cudaStream_t st);
 int spgemm_fill(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos, int32_t* Ccrd,
                 cudaStream_t st);
+// One pass (assemble while computing): pos of C and nnz(C) (synchronises); the columns and
+// values wait in scratch until spgemm_onepass_finish moves them into C's arrays.
+int spgemm_onepass(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int64_t* nnzC,
+                   cudaStream_t st);
+int spgemm_onepass_finish(const int32_t* Cpos, int32_t* Ccrd, void* Cvals, cudaStream_t st);
 int spgemm_numeric(const tacogb_csr* A, const tacogb_csr* B, const int32_t* Cpos,
                    const int32_t* Ccrd, void* Cvals, cudaStream_t st);
 

@@ -23,9 +23,15 @@
 //   bin 4  P >  4096   one CTA per row over a dense per-CTA accumulator in global scratch
 //                      (column bitmap for the pattern, stamp + value arrays for the numbers)
 // Phases: symbolic count -> device exclusive scan -> (caller allocates) -> crd fill; numeric.
+// One-pass form (taco's assemble-while-compute, used by evaluate): the rows' products go to
+// slots sized by P_i (an exclusive scan of the product counts); one ESC pass sorts keys and
+// values together and writes each row's sorted columns, summed values and count into its slot;
+// a scan of the counts gives pos and a compaction moves the slots into C.  One sort per row
+// where the three-phase form sorts three times.
 // Bin lists are built with per-bin atomic counters; the order of rows inside a list does not
 // affect any result.
 
+#include <algorithm>
 #include <cstdio>
 
 #include "common.cuh"
@@ -130,6 +136,13 @@ __device__ __forceinline__ uint64_t esc_key(int32_t col, int32_t seq) {
 }
 __device__ __forceinline__ int32_t key_col(uint64_t k) { return (int32_t)(k >> 32); }
 
+// What a pass computes and writes: MODE 0 counts (cnt), 1 writes columns at Cpos, 2 writes
+// values at Cpos, 3 (one pass) writes columns and values at the row's product slot (Cpos holds
+// the slot offsets) and counts.
+template <int MODE> constexpr bool mode_vals() { return MODE == 2 || MODE == 3; }
+template <int MODE> constexpr bool mode_crd() { return MODE == 1 || MODE == 3; }
+template <int MODE> constexpr bool mode_count() { return MODE == 0 || MODE == 3; }
+
 // MODE 0: count unique columns -> cnt[row]; 1: write sorted columns at Cpos[row];
 // 2: write values (sum of products in sequence order) at Cpos[row].
 template <int MODE, typename V>
@@ -146,9 +159,8 @@ __device__ __forceinline__ void esc_emit_warp(const uint64_t* key, const V* val,
     const unsigned m = __ballot_sync(0xffffffffu, head);
     if (MODE != 0 && head) {
       const int rank = base + __popc(m & ((1u << lane) - 1));
-      if (MODE == 1) {
-        Ccrd[out0 + rank] = key_col(key[e]);
-      } else {
+      if (mode_crd<MODE>()) Ccrd[out0 + rank] = key_col(key[e]);
+      if (mode_vals<MODE>()) {
         V s = val[e];
         for (int f = e + 1; f < P && key_col(key[f]) == key_col(key[e]); f++) s = add_rn(s, val[f]);
         Cvals[out0 + rank] = s;
@@ -156,7 +168,7 @@ __device__ __forceinline__ void esc_emit_warp(const uint64_t* key, const V* val,
     }
     base += __popc(m);
   }
-  if (MODE == 0 && lane == 0) cnt[row] = base;
+  if (mode_count<MODE>() && lane == 0) cnt[row] = base;
 }
 
 // Expands row `row`'s products into (key, value) slots [0, P) of a buffer, strided over
@@ -209,7 +221,7 @@ spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
       const int u = lane - seq0;
       if (u >= 0 && u < len) {
         key = esc_key(__ldg(Bcrd + b0 + u), lane);
-        if (MODE == 2) val = mul_rn(Avals[q], Bvals[b0 + u]);
+        if (mode_vals<MODE>()) val = mul_rn(Avals[q], Bvals[b0 + u]);
       }
       seq0 += len;
     }
@@ -219,12 +231,11 @@ spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
     const bool valid = lane < P;
     const bool head = valid && (lane == 0 || key_col(prevk) != key_col(key));
     const unsigned m = __ballot_sync(0xffffffffu, head);
-    if (MODE == 0) {
-      if (lane == 0) cnt[row] = __popc(m);
-    } else {
+    if (mode_count<MODE>() && lane == 0) cnt[row] = __popc(m);
+    if (MODE != 0) {
       // run sums in sequence order: lane-serial accumulation along each run
       V s = val;
-      if (MODE == 2) {
+      if (mode_vals<MODE>()) {
         // walk forward within the run from each head
         for (int d = 1; d < 32; d++) {
           const uint64_t kd = __shfl_down_sync(0xffffffffu, key, d);
@@ -238,8 +249,8 @@ spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
       if (head) {
         const int rank = __popc(m & ((1u << lane) - 1));
         const int o = Cpos[row] + rank;
-        if (MODE == 1) Ccrd[o] = key_col(key);
-        else Cvals[o] = s;
+        if (mode_crd<MODE>()) Ccrd[o] = key_col(key);
+        if (mode_vals<MODE>()) Cvals[o] = s;
       }
     }
   }
@@ -324,16 +335,16 @@ __device__ __forceinline__ void bin2_row_regs(const int32_t* __restrict__ Apos,
       const int u = r * 32 + lane - seq0;
       if (u >= 0 && u < len) {
         key[r] = esc_key(__ldg(Bcrd + b0 + u), r * 32 + lane);
-        if (MODE == 2) val[r] = mul_rn(Avals[q], Bvals[b0 + u]);
+        if (mode_vals<MODE>()) val[r] = mul_rn(Avals[q], Bvals[b0 + u]);
       }
     }
     seq0 += len;
   }
-  reg_bitonic<R, MODE == 2>(key, val);
+  reg_bitonic<R, mode_vals<MODE>()>(key, val);
 #pragma unroll
   for (int r = 0; r < R; r++) {
     skey[r * 32 + lane] = key[r];
-    if (MODE == 2) sval[r * 32 + lane] = val[r];
+    if (mode_vals<MODE>()) sval[r * 32 + lane] = val[r];
   }
   __syncwarp();
 }
@@ -363,7 +374,8 @@ spgemm_bin2(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
     } else if (cap <= 128) {
       bin2_row_regs<4, MODE>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
     } else {
-      esc_expand<MODE == 2>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, lane, 32);
+      esc_expand<mode_vals<MODE>()>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, lane,
+                                    32);
       for (int e = P + lane; e < cap; e += 32) key[e] = ~0ull;
       __syncwarp();
       smem_bitonic(key, val, cap, lane, 32, [] __device__() { __syncwarp(); });
@@ -394,7 +406,8 @@ spgemm_bin3(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
     const int P = (int)prod[row];
     int cap = 32;
     while (cap < P) cap <<= 1;
-    esc_expand<MODE == 2>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, tid, 256);
+    esc_expand<mode_vals<MODE>()>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, tid,
+                                  256);
     for (int e = P + tid; e < cap; e += 256) key[e] = ~0ull;
     __syncthreads();
     smem_bitonic(key, val, cap, tid, 256, [] __device__() { __syncthreads(); });
@@ -416,15 +429,13 @@ spgemm_bin3(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
     int wbase = 0;
     for (int x = 0; x < warp; x++) wbase += s_wcount[x];
     int rank = wbase + incl - local;
-    if (MODE == 0) {
-      if (tid == 255) cnt[row] = wbase + incl;
-    } else {
+    if (mode_count<MODE>() && tid == 255) cnt[row] = wbase + incl;
+    if (MODE != 0) {
       const int o0 = Cpos[row];
       for (int e = e0; e < e0 + ELEMS && e < P; e++) {
         if (e == 0 || key_col(key[e]) != key_col(key[e - 1])) {
-          if (MODE == 1) {
-            Ccrd[o0 + rank] = key_col(key[e]);
-          } else {
+          if (mode_crd<MODE>()) Ccrd[o0 + rank] = key_col(key[e]);
+          if (mode_vals<MODE>()) {
             V s = val[e];
             for (int f = e + 1; f < P && key_col(key[f]) == key_col(key[e]); f++) s = add_rn(s, val[f]);
             Cvals[o0 + rank] = s;
@@ -468,10 +479,10 @@ spgemm_bin4(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
       const int32_t j = __ldg(Acrd + q);
       const int32_t b0 = __ldg(Bpos + j), b1 = __ldg(Bpos + j + 1);
       V a = V();
-      if (MODE == 2) a = Avals[q];
+      if (mode_vals<MODE>()) a = Avals[q];
       for (int32_t u = b0 + tid; u < b1; u += 256) {
         const int32_t k = __ldg(Bcrd + u);
-        if (MODE == 2) {
+        if (mode_vals<MODE>()) {
           const V pr = mul_rn(a, Bvals[u]);
           if (stamp[k] != row) {
             stamp[k] = row;
@@ -479,9 +490,8 @@ spgemm_bin4(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
           } else {
             acc[k] = add_rn(acc[k], pr);
           }
-        } else {
-          atomicOr(bitmap + (k >> 5), 1u << (k & 31));
         }
+        if (MODE != 2) atomicOr(bitmap + (k >> 5), 1u << (k & 31));
       }
       __syncthreads();  // B rows of later A nonzeros may hit the same columns
     }
@@ -511,13 +521,16 @@ spgemm_bin4(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
         if (x < warp) wbase += s_wcount[x];
         total += s_wcount[x];
       }
-      if (MODE == 1 && bits) {
+      if (mode_crd<MODE>() && bits) {
         int r = s_base + wbase + incl - pc;
         const int o0 = Cpos[row];
         uint32_t bb = bits;
         while (bb) {
           const int bit = __ffs(bb) - 1;
-          Ccrd[o0 + r++] = (wi << 5) + bit;
+          const int col = (wi << 5) + bit;
+          Ccrd[o0 + r] = col;
+          if (mode_vals<MODE>()) Cvals[o0 + r] = acc[col];
+          r++;
           bb &= bb - 1;
         }
       }
@@ -526,7 +539,7 @@ spgemm_bin4(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
       if (tid == 0) s_base += total;
       __syncthreads();
     }
-    if (MODE == 0 && tid == 0) cnt[row] = s_base;
+    if (mode_count<MODE>() && tid == 0) cnt[row] = s_base;
     __syncthreads();
   }
 }
@@ -673,23 +686,82 @@ int run_bins(const tacogb_csr* A, const tacogb_csr* B, const Plan& pl, const int
     const size_t words = (size_t)((K + 31) / 32);
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t bm_bytes = al(sizeof(uint32_t) * words * slots);
-    const size_t st_bytes = MODE == 2 ? al(sizeof(int32_t) * K * slots) : 0;
-    const size_t acc_bytes = MODE == 2 ? al(sizeof(V) * K * slots) : 0;
+    const size_t st_bytes = mode_vals<MODE>() ? al(sizeof(int32_t) * K * slots) : 0;
+    const size_t acc_bytes = mode_vals<MODE>() ? al(sizeof(V) * K * slots) : 0;
     unsigned char* ws = (unsigned char*)scratch(bm_bytes + st_bytes + acc_bytes, 3);
     if (!ws) return last_code();
     uint32_t* bitmap = (uint32_t*)ws;
     int32_t* stamp = (int32_t*)(ws + bm_bytes);
     V* acc = (V*)(ws + bm_bytes + st_bytes);
     TACOGB_CUDA_TRY(cudaMemsetAsync(bitmap, 0, bm_bytes, st));
-    if (MODE == 2) TACOGB_CUDA_TRY(cudaMemsetAsync(stamp, 0xFF, st_bytes, st));
+    if (mode_vals<MODE>()) TACOGB_CUDA_TRY(cudaMemsetAsync(stamp, 0xFF, st_bytes, st));
     TACOGB_LAUNCH("spgemm_bin4", st,
                   (spgemm_bin4<MODE, V><<<slots, 256, 0, st>>>(
                       A->pos, A->crd, Av, B->pos, B->crd, Bv, rows_of(4), pl.bin_cnt + 4,
-                      (int32_t)K, bitmap, MODE == 2 ? stamp : nullptr, MODE == 2 ? acc : nullptr,
+                      (int32_t)K, bitmap, mode_vals<MODE>() ? stamp : nullptr,
+                      mode_vals<MODE>() ? acc : nullptr,
                       Cpos, pl.cnt, Ccrd, Cvals)));
   }
   return 0;
 }
+
+// Product counts (int64) as int32 for the scan of the one-pass slot offsets (values beyond
+// int32 are clamped; the scan then flags the overflow).
+__global__ void spgemm_prod32(const int64_t* __restrict__ prod, int32_t n, int32_t* __restrict__ p32) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p32[i] = (int32_t)min(prod[i], (int64_t)INT32_MAX);
+}
+
+// Moves row i's slot [off[i], off[i] + cnt[i]) to [Cpos[i], Cpos[i+1]) of C; one warp per row.
+template <typename V>
+__global__ void spgemm_compact(const int32_t* __restrict__ off, const int32_t* __restrict__ Cpos,
+                               int32_t n, const int32_t* __restrict__ scrd,
+                               const V* __restrict__ svals, int32_t* __restrict__ Ccrd,
+                               V* __restrict__ Cvals) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n;
+       row += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int32_t s0 = __ldg(off + row), d0 = __ldg(Cpos + row);
+    const int32_t len = __ldg(Cpos + row + 1) - d0;
+    for (int32_t e = lane; e < len; e += 32) {
+      Ccrd[d0 + e] = scrd[s0 + e];
+      Cvals[d0 + e] = svals[s0 + e];
+    }
+  }
+}
+
+// Exclusive scan of cnt[0..n) into pos[0..n] (pos[n] = total); *total and the overflow flag
+// are read back (synchronises).
+int scan_counts(const int32_t* cnt, int64_t n, int64_t* sums, int32_t* flag, int32_t* pos,
+                int64_t* total, bool* overflow, cudaStream_t st) {
+  const int64_t nblocks = (n + kScanChunk - 1) / kScanChunk;
+  TACOGB_LAUNCH("spgemm_scan_sums", st,
+                scan_block_sums<<<(unsigned)nblocks, 256, 0, st>>>(cnt, (int32_t)n, sums));
+  TACOGB_LAUNCH("spgemm_scan_top", st,
+                scan_sums_exclusive<<<1, 32, 0, st>>>(sums, (int32_t)nblocks, flag));
+  TACOGB_LAUNCH("spgemm_scan_pos", st,
+                scan_write_pos<<<(unsigned)nblocks, 256, 0, st>>>(cnt, (int32_t)n, sums, pos));
+  int32_t f = 0;
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(total, sums + nblocks, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                  st));
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(&f, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  *overflow = f != 0;
+  return 0;
+}
+
+// State of the last one-pass product on this device, between spgemm_onepass and
+// spgemm_onepass_finish (library scratch slots 12: offsets, 13: slots; the counts live in the
+// plan's scratch, slot 2).
+struct OnePassState {
+  int32_t* off = nullptr;   // slot offsets, n + 1
+  int32_t* cnt = nullptr;   // unique columns per row, n + 1
+  int32_t* scrd = nullptr;  // slot columns, total products
+  void* svals = nullptr;    // slot values, total products
+  int64_t n = -1;
+  int vtype = 0;
+};
+OnePassState g_onepass[64];
 
 int check_pair(const tacogb_csr* A, const tacogb_csr* B) {
   TACOGB_CHECK_ARG(A != nullptr && B != nullptr, "SpGEMM: null matrix");
@@ -738,6 +810,90 @@ int spgemm_symbolic(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int
     return TACOGB_ERR_OVERFLOW;
   }
   *nnzC = total;
+  return 0;
+}
+
+int spgemm_onepass(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int64_t* nnzC,
+                   cudaStream_t st) {
+  if (int rc = check_pair(A, B)) return rc;
+  TACOGB_CHECK_ARG(Cpos != nullptr && nnzC != nullptr, "SpGEMM: null output");
+  TACOGB_CHECK_ARG(A->vtype == B->vtype && (A->vtype == TACOGB_F64 || A->vtype == TACOGB_F32),
+                   "SpGEMM: A and B need the same value type (F64 or F32)");
+  TACOGB_CHECK_ARG(A->nnz == 0 || A->vals != nullptr, "SpGEMM: null A values");
+  TACOGB_CHECK_ARG(B->nnz == 0 || B->vals != nullptr, "SpGEMM: null B values");
+  int dev = 0;
+  TACOGB_CUDA_TRY(cudaGetDevice(&dev));
+  TACOGB_CHECK_ARG(dev >= 0 && dev < 64, "SpGEMM: device %d out of range", dev);
+  OnePassState& os = g_onepass[dev];
+  const int64_t n = A->rows;
+  os.n = n;
+  os.vtype = A->vtype;
+  if (n == 0) {
+    TACOGB_CUDA_TRY(cudaMemsetAsync(Cpos, 0, sizeof(int32_t), st));
+    TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+    *nnzC = 0;
+    return 0;
+  }
+  Plan pl;
+  if (int rc = make_plan(A, B, pl, st)) return rc;
+  // slot offsets: exclusive scan of the product counts
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t vb = A->vtype == TACOGB_F64 ? 8 : 4;
+  const size_t head = 2 * al(sizeof(int32_t) * (n + 1));
+  unsigned char* ws = (unsigned char*)scratch(head, 12);
+  if (!ws) return last_code();
+  int32_t* p32 = (int32_t*)ws;
+  int32_t* off = (int32_t*)(ws + al(sizeof(int32_t) * (n + 1)));
+  TACOGB_LAUNCH("spgemm_prod32", st,
+                spgemm_prod32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pl.prod, (int32_t)n,
+                                                                            p32));
+  int64_t products = 0;
+  bool overflow = false;
+  if (int rc = scan_counts(p32, n, pl.sums, pl.flag, off, &products, &overflow, st)) return rc;
+  TACOGB_CHECK_ARG(!overflow, "SpGEMM: %lld products exceed the one-pass slots' int32 offsets; "
+                   "use the symbolic/fill/numeric phases", (long long)products);
+  // the slots, in a scratch slot of their own (growing it leaves the offsets alone)
+  unsigned char* sl = (unsigned char*)scratch(al(4 * (size_t)products) + al(vb * (size_t)products),
+                                              13);
+  if (!sl) return last_code();
+  os.off = off;
+  os.cnt = pl.cnt;
+  os.scrd = (int32_t*)sl;
+  os.svals = sl + al(4 * (size_t)products);
+  if (A->vtype == TACOGB_F64) {
+    if (int rc = run_bins<3, double>(A, B, pl, os.off, os.scrd, (double*)os.svals, st)) return rc;
+  } else {
+    if (int rc = run_bins<3, float>(A, B, pl, os.off, os.scrd, (float*)os.svals, st)) return rc;
+  }
+  int64_t total = 0;
+  if (int rc = scan_counts(pl.cnt, n, pl.sums, pl.flag, Cpos, &total, &overflow, st)) return rc;
+  if (overflow) {
+    set_error(TACOGB_ERR_OVERFLOW, "SpGEMM: nnz(C) = %lld exceeds int32 positions",
+              (long long)total);
+    return TACOGB_ERR_OVERFLOW;
+  }
+  *nnzC = total;
+  return 0;
+}
+
+int spgemm_onepass_finish(const int32_t* Cpos, int32_t* Ccrd, void* Cvals, cudaStream_t st) {
+  int dev = 0;
+  TACOGB_CUDA_TRY(cudaGetDevice(&dev));
+  TACOGB_CHECK_ARG(dev >= 0 && dev < 64 && g_onepass[dev].n >= 0,
+                   "SpGEMM: no one-pass product to finish on this device");
+  const OnePassState& os = g_onepass[dev];
+  if (os.n == 0) return 0;
+  const unsigned blocks = (unsigned)std::min<int64_t>((os.n + 7) / 8, (int64_t)sm_count() * 16);
+  if (os.vtype == TACOGB_F64)
+    TACOGB_LAUNCH("spgemm_compact", st,
+                  spgemm_compact<double><<<blocks, 256, 0, st>>>(
+                      os.off, Cpos, (int32_t)os.n, os.scrd, (const double*)os.svals, Ccrd,
+                      (double*)Cvals));
+  else
+    TACOGB_LAUNCH("spgemm_compact", st,
+                  spgemm_compact<float><<<blocks, 256, 0, st>>>(
+                      os.off, Cpos, (int32_t)os.n, os.scrd, (const float*)os.svals, Ccrd,
+                      (float*)Cvals));
   return 0;
 }
 

@@ -28,6 +28,35 @@ def _csr(pos, crd, vals, cols, dtype=torch.float64):
 
 
 def gpu_spgemm(A, B, dtype=torch.float64):
+    """(pos, crd, vals) of A*B through tacogb_spgemm_symbolic/fill/numeric, after checking that
+    the one-pass form (tacogb_spgemm_onepass/_finish) gives the same arrays bit for bit."""
+    phases = gpu_spgemm_phases(A, B, dtype)
+    one = gpu_spgemm_onepass(A, B, dtype)
+    for x, y in zip(phases, one):
+        assert np.array_equal(x, y)
+    return phases
+
+
+def gpu_spgemm_onepass(A, B, dtype=torch.float64):
+    (ap, ac, av, acols), (bp, bc, bv, bcols) = A, B
+    Ad, Bd = _csr(ap, ac, av, acols, dtype), _csr(bp, bc, bv, bcols, dtype)
+    a, b = Ad.as_csr(), Bd.as_csr()
+    L = tg.lib()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    Cpos = torch.full((len(ap),), -1, dtype=torch.int32, device="cuda")
+    nnz = ctypes.c_int64(0)
+    tg.check(L.tacogb_spgemm_onepass(ctypes.byref(a), ctypes.byref(b), Cpos.data_ptr(),
+                                     ctypes.byref(nnz), sp), "onepass")
+    Ccrd = torch.full((max(nnz.value, 1),), -1, dtype=torch.int32, device="cuda")
+    Cvals = torch.full((max(nnz.value, 1),), float("nan"), dtype=dtype, device="cuda")
+    tg.check(L.tacogb_spgemm_onepass_finish(Cpos.data_ptr(), Ccrd.data_ptr(), Cvals.data_ptr(),
+                                            sp), "onepass_finish")
+    torch.cuda.synchronize()
+    n = nnz.value
+    return (Cpos.cpu().numpy(), Ccrd[:n].cpu().numpy(), Cvals[:n].double().cpu().numpy())
+
+
+def gpu_spgemm_phases(A, B, dtype=torch.float64):
     """(pos, crd, vals) of A*B through tacogb_spgemm_symbolic/fill/numeric."""
     (ap, ac, av, acols), (bp, bc, bv, bcols) = A, B
     Ad, Bd = _csr(ap, ac, av, acols, dtype), _csr(bp, bc, bv, bcols, dtype)
