@@ -73,16 +73,13 @@ int tacogb_device_status(int32_t* status);
  * call that cannot reach a GPU checks host-resident levels on the host, so invalid input is
  * still reported as TACOGB_ERR_ARG.  The device layer (tacogb_spmv
  * and the other functions on tacogb_csr) trusts its arguments; tacogb_csr_validate checks a
- * device CSR explicitly.  tacogb_set_validation(0) turns the taco-ABI checks off (and returns the
- * previous setting); they are on by default. */
+ * device CSR explicitly (declared with the device layer below).  tacogb_set_validation(0) turns
+ * the taco-ABI checks off (and returns the previous setting); they are on by default. */
 int tacogb_set_validation(int32_t on);
 /* Checks one compressed level held in host memory (outer segments over a dimension of size
  * inner, nnz = pos[outer]); 0 or TACOGB_ERR_ARG.  Uses host threads only; needs no GPU. */
 int tacogb_validate_level_host(int64_t outer, int32_t inner, const int32_t* pos,
                                const int32_t* crd, int64_t nnz);
-/* Checks a device-resident CSR matrix on the GPU (A->nnz must equal pos[rows]); synchronises
- * stream. */
-int tacogb_csr_validate(const struct tacogb_csr* A, void* stream);
 
 /* Number of kernels this library has launched in this process. */
 long long tacogb_launch_count(void);
@@ -143,6 +140,10 @@ typedef struct tacogb_csr {
   const void* vals;    /* nnz values of type vtype */
   int32_t vtype;       /* TACOGB_F64 or TACOGB_F32 */
 } tacogb_csr;
+
+/* Checks a device-resident CSR matrix on the GPU, as the taco-ABI entry points check their
+ * operands (A->nnz must equal pos[rows]); synchronises stream. */
+int tacogb_csr_validate(const tacogb_csr* A, void* stream);
 
 /* SpMV kernel variants.  TACOGB_VARIANT_AUTO lets the library choose (tuning database, cost
  * model, then a structural rule). */

@@ -328,6 +328,42 @@ def rb_cases(reference_root):
     save("read_rhs_rb", colptr=cp, rowidx=ri, cvals=cv, dims=np.array([r, c]))
 
 
+def dropin_cases(reference_root):
+    """taco's own API into the library: tests/cpp/taco_dropin.cpp builds taco::Tensor<double>
+    statements for SpMV, SpMM and SpGEMM with taco's library (compiled from the taco sources by
+    oracle/Makefile.ref), gives each the forwarding source of INTEGRATION.md through
+    TensorBase::compileSource, and runs assemble() and compute().  Without a GPU here the
+    forwarding source is linked against the recorder (tests/cpp/tacogb_recorder.c), which keeps
+    every argument pack taco passes and completes the call with taco's generated code; the
+    driver checks the result equals taco's own.  The fixtures hold the packs of the assemble
+    and compute calls and taco's result; tests/test_taco_dropin_gpu.py replays them into the
+    drop-in modules on a GPU."""
+    import subprocess
+    import tempfile
+    ref_dir = os.path.join(ROOT, "oracle", "_ref")
+    subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", "-j8", "REF=" + reference_root,
+                    "dropin"], cwd=ROOT, check=True)
+    with tempfile.TemporaryDirectory() as d:
+        env = dict(os.environ, TACOGB_RECORD_DIR=d, TACOGB_REF_DIR=ref_dir,
+                   TACO_CFLAGS="-O3 -std=c99 -I%s -Wl,--no-as-needed -L%s -ltacogb_recorder "
+                               "-Wl,-rpath,%s" % (os.path.join(ROOT, "include"), ref_dir, ref_dir))
+        subprocess.run([os.path.join(ref_dir, "bin", "taco_dropin"), d], env=env, check=True)
+        for p in ("spmv", "spmm", "spgemm"):
+            arrays = {}
+            (a_call,) = H.read_abi_record(os.path.join(d, p + "_assemble.bin"))
+            (c_call,) = H.read_abi_record(os.path.join(d, p + "_compute.bin"))
+            for k, t in enumerate(a_call):
+                arrays.update(H.record_to_arrays("a%d" % k, t))
+            for k, t in enumerate(c_call):
+                arrays.update(H.record_to_arrays("c%d" % k, t))
+            levels, vals = H.read_result_dump(os.path.join(d, p + "_expected.bin"))
+            for m, lv in enumerate(levels):
+                if lv is not None:
+                    arrays["e_pos%d" % m], arrays["e_crd%d" % m] = lv
+            arrays["e_vals"] = vals
+            save("taco_dropin_" + p, **arrays)
+
+
 if __name__ == "__main__":
     ref_root = os.environ.get("TACO_REFERENCE")
     if not ref_root or not os.path.isdir(os.path.join(ref_root, "src")):
@@ -349,3 +385,4 @@ if __name__ == "__main__":
     pack_cases()
     reader_cases()
     rb_cases(ref_root)
+    dropin_cases(ref_root)

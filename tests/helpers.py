@@ -319,3 +319,112 @@ def sub_rows(pos, crd, vals, idx):
     take = np.concatenate([np.arange(pos[i], pos[i + 1], dtype=np.int64) for i in idx]) \
         if len(idx) else np.zeros(0, np.int64)
     return spos, crd[take], vals[take]
+
+
+def read_abi_record(path):
+    """The calls recorded by tests/cpp/tacogb_recorder.c: a list of calls, each a list of
+    tensors {order, csize, dims, ordering, types, levels, vals}; levels[m] is None for a dense
+    mode or an unassembled level, else (pos, crd); vals is None when absent."""
+    raw = open(path, "rb").read()
+    off = 0
+
+    def i64():
+        nonlocal off
+        v = int(np.frombuffer(raw, np.int64, 1, off)[0])
+        off += 8
+        return v
+
+    def arr(dtype, count):
+        nonlocal off
+        a = np.frombuffer(raw, dtype, count, off).copy()
+        off += a.nbytes
+        return a
+
+    calls = []
+    while off < len(raw):
+        tensors = []
+        for _ in range(i64()):
+            order, csize = i64(), i64()
+            dims = [i64() for _ in range(order)]
+            ordering = [i64() for _ in range(order)]
+            types = [i64() for _ in range(order)]
+            levels = []
+            for m in range(order):
+                if types[m] == 0:
+                    levels.append(None)
+                    continue
+                np_ = i64()
+                if np_ < 0:
+                    levels.append(None)
+                    continue
+                pos = arr(np.int32, np_)
+                crd = arr(np.int32, i64())
+                levels.append((pos, crd))
+            nv = i64()
+            vals = arr(np.float64 if csize == 64 else np.float32, nv) if nv >= 0 else None
+            tensors.append({"order": order, "csize": csize, "dims": dims, "ordering": ordering,
+                            "types": types, "levels": levels, "vals": vals})
+        calls.append(tensors)
+    return calls
+
+
+def read_result_dump(path):
+    """(levels, vals) of a result written by taco_dropin's dump_result: levels[m] None for a
+    dense mode, else (pos, crd)."""
+    raw = open(path, "rb").read()
+    off = 0
+    order = int(np.frombuffer(raw, np.int32, 1, off)[0])
+    off += 4
+    levels = []
+    for _ in range(order):
+        kind = int(np.frombuffer(raw, np.int32, 1, off)[0])
+        off += 4
+        if not kind:
+            levels.append(None)
+            continue
+        n = int(np.frombuffer(raw, np.int64, 1, off)[0])
+        off += 8
+        pos = np.frombuffer(raw, np.int32, n, off).copy()
+        off += 4 * n
+        n = int(np.frombuffer(raw, np.int64, 1, off)[0])
+        off += 8
+        crd = np.frombuffer(raw, np.int32, n, off).copy()
+        off += 4 * n
+        levels.append((pos, crd))
+    n = int(np.frombuffer(raw, np.int64, 1, off)[0])
+    off += 8
+    vals = np.frombuffer(raw, np.float64, n, off).copy()
+    return levels, vals
+
+
+def record_to_arrays(prefix, tensor):
+    """Flattens one recorded tensor into npz-ready arrays under `prefix`."""
+    out = {prefix + "_hdr": np.array([tensor["order"], tensor["csize"]] + tensor["dims"]
+                                     + tensor["ordering"] + tensor["types"], np.int64)}
+    for m, lv in enumerate(tensor["levels"]):
+        if lv is not None:
+            out["%s_pos%d" % (prefix, m)], out["%s_crd%d" % (prefix, m)] = lv
+    if tensor["vals"] is not None:
+        out[prefix + "_vals"] = tensor["vals"]
+    return out
+
+
+def arrays_to_taco(g, prefix, with_arrays=True):
+    """A taco_tensor_t (taco_gb300.taco.TacoTensor) rebuilt from record_to_arrays's arrays: the
+    same order, csize, dimensions, mode ordering, mode types, index arrays and values."""
+    h = [int(v) for v in g[prefix + "_hdr"]]
+    order, csize = h[0], h[1]
+    dims, ordering, types = h[2:2 + order], h[2 + order:2 + 2 * order], h[2 + 2 * order:]
+    idx = {}
+    for m in range(order):
+        if types[m] == 1:
+            key = "%s_pos%d" % (prefix, m)
+            if with_arrays and key in g:
+                idx[m] = (np.ascontiguousarray(g[key]), np.ascontiguousarray(g["%s_crd%d" % (prefix, m)]))
+            else:
+                idx[m] = (None, None)
+    vals = None
+    if with_arrays and prefix + "_vals" in g:
+        vals = np.ascontiguousarray(g[prefix + "_vals"])
+    return T.TacoTensor(dims, types, vals=vals, index_arrays=idx, csize=csize,
+                        mode_ordering=ordering)
