@@ -96,6 +96,9 @@ struct DeviceState {
   std::vector<void*> stage;
   std::vector<size_t> stage_cap;
   cudaStream_t stream = nullptr;
+  // the pipelined SpMV's copy streams (host -> device, device -> host) and chunk events
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t ev[2 * 16 + 1] = {};
   int* status = nullptr;  // device status word (see device_status())
 };
 
@@ -214,6 +217,23 @@ cudaStream_t lib_stream() {
   if (!ds) return nullptr;
   if (!ds->stream) cudaStreamCreateWithFlags(&ds->stream, cudaStreamNonBlocking);
   return ds->stream;
+}
+
+// The pipelined SpMV's two copy streams and its events (created once per device).
+bool pipeline_streams(cudaStream_t* h2d, cudaStream_t* d2h, cudaEvent_t** ev) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState* ds = current_device();
+  if (!ds) return false;
+  if (!ds->h2d && cudaStreamCreateWithFlags(&ds->h2d, cudaStreamNonBlocking) != cudaSuccess)
+    return false;
+  if (!ds->d2h && cudaStreamCreateWithFlags(&ds->d2h, cudaStreamNonBlocking) != cudaSuccess)
+    return false;
+  for (cudaEvent_t& e : ds->ev)
+    if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
+  *h2d = ds->h2d;
+  *d2h = ds->d2h;
+  *ev = ds->ev;
+  return true;
 }
 
 // True when the GPU can dereference p directly (device or managed memory).
@@ -349,6 +369,20 @@ int check_dense_matrix(const taco_tensor_t* t, const char* name) {
                    "%s: expected row-major mode ordering {0,1}", name);
   TACOGB_CHECK_ARG(t->dimensions != nullptr, "%s: null dimensions", name);
   return 0;
+}
+
+// Rows j*rows_chunk.. of a chunked SpMV: pos of every chunk rebased to start at zero, each chunk
+// at its own 4-entry-aligned offset (so the warp tiles' bulk copies stay 16-byte aligned).
+__global__ void spmv_rebase_pos(const int32_t* __restrict__ pos, const int64_t* __restrict__ meta,
+                                int chunks, int32_t* __restrict__ out) {
+  // meta: per chunk (first row, rows, output offset)
+  const int j = blockIdx.y;
+  if (j >= chunks) return;
+  const int64_t r0 = meta[3 * j], nr = meta[3 * j + 1], o = meta[3 * j + 2];
+  const int32_t base = __ldg(pos + r0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= nr;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[o + i] = __ldg(pos + r0 + i) - base;
 }
 
 int check_csr(const taco_tensor_t* t, const char* name) {
@@ -679,6 +713,116 @@ int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   return 0;
 }
 
+// SpMV over host operands as a pipeline: the rows are cut into chunks of about equal nonzeros;
+// one stream copies x, pos and then every chunk's crd and values to the GPU, the library stream
+// checks and multiplies each chunk as soon as its copy has landed, and a third stream returns
+// each chunk's rows of y.  The copies of later chunks overlap the checks, products and returns
+// of earlier ones, so the call takes about as long as the copies alone (the host link bounds
+// it).  Results are those of the unchunked product up to summation order within the merge tiles.
+namespace {
+constexpr int kPipeChunks = 8;
+constexpr int64_t kPipeMinNnz = (int64_t)1 << 23;  // below this, copy then compute
+
+int spmv_compute_pipelined(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x, int vt,
+                           int32_t rows, int32_t cols, int32_t nnz) {
+  const int32_t* pos = (const int32_t*)A->indices[1][0];
+  const int32_t* crd = (const int32_t*)A->indices[1][1];
+  const size_t vb = value_bytes(vt);
+  cudaStream_t st = lib_stream(), h2d, d2h;
+  cudaEvent_t* ev;
+  if (!st || !pipeline_streams(&h2d, &d2h, &ev)) {
+    set_error(TACOGB_ERR_CUDA, "spmv: no GPU streams");
+    return TACOGB_ERR_CUDA;
+  }
+  // chunk boundaries on the host pos: first row whose start reaches j * nnz / K
+  const int K = (int)std::min<int64_t>(kPipeChunks, std::max<int64_t>(1, nnz / (kPipeMinNnz / 2)));
+  TACOGB_CHECK_ARG(pos[0] == 0, "spmv operand A: pos[0] is not 0");
+  int32_t rb[kPipeChunks + 1];
+  rb[0] = 0;
+  for (int j = 1; j < K; j++) {
+    const int64_t target = (int64_t)nnz * j / K;
+    int32_t lo = rb[j - 1], hi = rows;
+    while (lo < hi) {
+      const int32_t mid = lo + (hi - lo) / 2;
+      if ((int64_t)pos[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    rb[j] = lo;
+  }
+  rb[K] = rows;
+  int64_t meta[3 * kPipeChunks], coff[kPipeChunks + 1], voff[kPipeChunks + 1];
+  int64_t poff = 0, c = 0, v = 0;
+  for (int j = 0; j < K; j++) {
+    const int64_t k0 = pos[rb[j]], k1 = pos[rb[j + 1]];
+    TACOGB_CHECK_ARG(k1 >= k0, "spmv operand A: pos decreases before segment %d", rb[j + 1]);
+    meta[3 * j] = rb[j];
+    meta[3 * j + 1] = rb[j + 1] - rb[j];
+    meta[3 * j + 2] = poff;
+    poff += ((rb[j + 1] - rb[j] + 1) + 3) & ~(int64_t)3;
+    coff[j] = c;
+    voff[j] = v;
+    c += ((k1 - k0) + 3) & ~(int64_t)3;  // every chunk's crd and values start 16-byte aligned
+    v += ((k1 - k0) + 3) & ~(int64_t)3;
+  }
+  int32_t* dpos = (int32_t*)stage_buffer(5, ((size_t)rows + 1) * 4);
+  int32_t* dposc = (int32_t*)stage_buffer(0, (size_t)poff * 4 + 64);
+  int32_t* dcrd = (int32_t*)stage_buffer(1, (size_t)c * 4 + 64);
+  unsigned char* dval = (unsigned char*)stage_buffer(2, (size_t)v * vb + 64);
+  void* dx = stage_buffer(3, (size_t)cols * vb + 64);
+  unsigned char* dy = (unsigned char*)stage_buffer(4, (size_t)rows * vb + 64);
+  int64_t* dmeta = (int64_t*)stage_buffer(8, sizeof(meta));
+  if (!dpos || !dposc || !dcrd || !dval || !dx || !dy || !dmeta) return TACOGB_ERR_ALLOC;
+  // every copy is issued up front on the host -> device stream
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(dmeta, meta, sizeof(int64_t) * 3 * K, cudaMemcpyHostToDevice, h2d));
+  if (cols) TACOGB_CUDA_TRY(cudaMemcpyAsync(dx, x->vals, (size_t)cols * vb, cudaMemcpyHostToDevice, h2d));
+  TACOGB_CUDA_TRY(cudaMemcpyAsync(dpos, pos, ((size_t)rows + 1) * 4, cudaMemcpyHostToDevice, h2d));
+  TACOGB_CUDA_TRY(cudaEventRecord(ev[2 * kPipeChunks], h2d));
+  for (int j = 0; j < K; j++) {
+    const int64_t k0 = pos[rb[j]], n = pos[rb[j + 1]] - k0;
+    if (n) {
+      TACOGB_CUDA_TRY(cudaMemcpyAsync(dcrd + coff[j], crd + k0, (size_t)n * 4,
+                                      cudaMemcpyHostToDevice, h2d));
+      TACOGB_CUDA_TRY(cudaMemcpyAsync(dval + voff[j] * vb, (const unsigned char*)A->vals + k0 * vb,
+                                      (size_t)n * vb, cudaMemcpyHostToDevice, h2d));
+    }
+    TACOGB_CUDA_TRY(cudaEventRecord(ev[j], h2d));
+  }
+  // chunks' pos rebased once x and pos are in
+  int rc = 0;
+  TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[2 * kPipeChunks], 0));
+  count_launch();
+  spmv_rebase_pos<<<dim3(64, K), 256, 0, st>>>(dpos, dmeta, K, dposc);
+  rc = launch_check("spmv_rebase_pos");
+  for (int j = 0; j < K && rc == 0; j++) {
+    const int32_t nr = (int32_t)meta[3 * j + 1];
+    const int32_t n = pos[rb[j + 1]] - pos[rb[j]];
+    TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[j], 0));
+    tacogb_csr cj{nr, cols, n, dposc + meta[3 * j + 2], dcrd + coff[j], dval + voff[j] * vb, vt};
+    if (validation_on()) {
+      rc = validate_level_device("spmv operand A", nr, cols, cj.pos, cj.crd, n, st);
+      if (rc) break;
+    }
+    rc = spmv_run(&cj, dx, dy + (size_t)rb[j] * vb, TACOGB_VARIANT_AUTO, st);
+    if (rc) break;
+    TACOGB_CUDA_TRY(cudaEventRecord(ev[kPipeChunks + j], st));
+    TACOGB_CUDA_TRY(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0));
+    if (nr)
+      TACOGB_CUDA_TRY(cudaMemcpyAsync((unsigned char*)y->vals + (size_t)rb[j] * vb,
+                                      dy + (size_t)rb[j] * vb, (size_t)nr * vb,
+                                      cudaMemcpyDeviceToHost, d2h));
+  }
+  // nothing may still be copying when the call returns, whatever happened
+  const cudaError_t e1 = cudaStreamSynchronize(h2d), e2 = cudaStreamSynchronize(st),
+                    e3 = cudaStreamSynchronize(d2h);
+  if (rc) return rc;
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+    set_error(TACOGB_ERR_CUDA, "spmv: %s", cudaGetErrorString(e1 != cudaSuccess ? e1
+                                                               : e2 != cudaSuccess ? e2 : e3));
+    return TACOGB_ERR_CUDA;
+  }
+  return consume_device_status();
+}
+}  // namespace
+
 int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   if (!plain_spmv(y, A, x)) return spmv_fmt_compute(y, A, x);
   if (int rc = check_dense_vector(y, "spmv result y")) return rc;
@@ -701,6 +845,11 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   if (int rc = read_i32(pos + rows, &nnz)) return rc;
   TACOGB_CHECK_ARG(nnz >= 0, "spmv: negative nnz");
   const size_t vb = value_bytes(vt);
+  // large host operands: copies, checks, products and returns overlapped chunk by chunk
+  if (nnz >= kPipeMinNnz && !device_accessible(pos) && !device_accessible(crd) &&
+      !device_accessible(A->vals) && !device_accessible(x->vals) &&
+      !device_accessible(y->vals) && crd != nullptr && A->vals != nullptr && x->vals != nullptr)
+    return spmv_compute_pipelined(y, A, x, vt, rows, cols, nnz);
 
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ox;

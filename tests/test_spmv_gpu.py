@@ -278,3 +278,38 @@ def test_auto_variant_choice(which):
     y_v = tg.spmv(A, xd, variant=v).cpu().numpy()
     assert np.array_equal(y_auto, y_v)
     assert normwise(y_auto, O.spmv(pos, crd, vals, x)) <= F64_TOL
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_abi_pipelined_host_operands(dtype):
+    """Host operands of 2^23 nonzeros or more go through the pipelined path (chunked copies,
+    checks, products and returns overlapped): the oracle's result, on two calls in a row."""
+    s = W.spmv_powerlaw(rows=600000)
+    pos, crd, vals = W.generate(s)
+    assert len(crd) >= 1 << 23
+    x = W.dense(25, s.cols)
+    ref = O.spmv(pos, crd, vals, x)
+    v = vals.astype(dtype)
+    xx = x.astype(dtype)
+    for _ in range(2):
+        y = np.full(s.rows, np.nan, dtype=dtype)
+        At, Xt, Yt = T.csr(pos, crd, v, [s.rows, s.cols]), T.dense(xx, [s.cols]), T.dense(y, [s.rows])
+        assert tg.lib().tacogb_spmv_compute(Yt.ptr, At.ptr, Xt.ptr) == 0, tg.lib().tacogb_last_error()
+        assert normwise(y, ref) <= (F64_TOL if dtype == np.float64 else F32_TOL)
+
+
+def test_abi_pipelined_rejects_a_corrupt_late_chunk():
+    s = W.spmv_powerlaw(rows=600000)
+    pos, crd, vals = W.generate(s)
+    crd = crd.copy()
+    crd[len(crd) - 1000] = s.cols + 5  # in the last chunk
+    x = W.dense(26, s.cols)
+    y = np.zeros(s.rows)
+    At, Xt, Yt = T.csr(pos, crd, vals, [s.rows, s.cols]), T.dense(x, [s.cols]), T.dense(y, [s.rows])
+    assert tg.lib().tacogb_spmv_compute(Yt.ptr, At.ptr, Xt.ptr) == 1
+    assert b"out of range" in tg.lib().tacogb_last_error()
+    # the library is usable right after
+    y2 = np.zeros(s.rows)
+    At2, Yt2 = T.csr(pos, W.generate(s)[1], vals, [s.rows, s.cols]), T.dense(y2, [s.rows])
+    assert tg.lib().tacogb_spmv_compute(Yt2.ptr, At2.ptr, Xt.ptr) == 0
+    assert normwise(y2, O.spmv(pos, W.generate(s)[1], vals, x)) <= F64_TOL
