@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
 #include <vector>
 
@@ -100,6 +101,7 @@ struct DeviceState {
   cudaStream_t h2d = nullptr, d2h = nullptr;
   cudaEvent_t ev[2 * 16 + 1] = {};
   int* status = nullptr;  // device status word (see device_status())
+  unsigned long long* mailbox = nullptr;  // mapped pinned host words (see host_mailbox())
 };
 
 std::mutex g_mu;
@@ -170,6 +172,31 @@ int* device_status() {
     cudaMemset(ds->status, 0, 256);
   }
   return ds->status;
+}
+
+unsigned long long* host_mailbox() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  DeviceState* ds = current_device();
+  if (!ds) return nullptr;
+  if (!ds->mailbox) {
+    void* p = nullptr;
+    cudaError_t e = cudaHostAlloc(&p, kMailboxWords * sizeof(unsigned long long), cudaHostAllocMapped);
+    if (e != cudaSuccess) {
+      set_error(TACOGB_ERR_ALLOC, "mailbox: cudaHostAlloc failed: %s", cudaGetErrorString(e));
+      return nullptr;
+    }
+    void* d = nullptr;
+    e = cudaHostGetDevicePointer(&d, p, 0);
+    if (e != cudaSuccess || d != p) {
+      // unified addressing gives one address for both sides; without it there is no mailbox
+      cudaFreeHost(p);
+      set_error(TACOGB_ERR_CUDA, "mailbox: mapped host memory has no common address");
+      return nullptr;
+    }
+    std::memset(p, 0, kMailboxWords * sizeof(unsigned long long));
+    ds->mailbox = (unsigned long long*)p;
+  }
+  return ds->mailbox;
 }
 
 namespace {
@@ -713,30 +740,53 @@ int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   return 0;
 }
 
-// SpMV over host operands as a pipeline: the rows are cut into chunks of about equal nonzeros;
-// one stream copies x, pos and then every chunk's crd and values to the GPU, the library stream
+// A CSR product over host operands as a pipeline (SpMV: dense operand x, result y; SpMM: B and
+// C, N values per row): the rows are cut into chunks of about equal nonzeros; one stream copies
+// the dense operand, pos and then every chunk's crd and values to the GPU, the library stream
 // checks and multiplies each chunk as soon as its copy has landed, and a third stream returns
-// each chunk's rows of y.  The copies of later chunks overlap the checks, products and returns
-// of earlier ones, so the call takes about as long as the copies alone (the host link bounds
-// it).  Results are those of the unchunked product up to summation order within the merge tiles.
+// each chunk's rows of the result.  The copies of later chunks overlap the checks, products and
+// returns of earlier ones, so the call takes little more than its copies (the host link bounds
+// it).  The checks never wait for the host: a chunk that fails is rewritten on the device into
+// a harmless level before its product runs, and the verdicts are read after the last chunk, so
+// an invalid operand returns TACOGB_ERR_ARG (first failing chunk, positions in the whole
+// operand) with the result's contents unspecified.  Results are those of the unchunked product
+// up to summation order within merge tiles.
 namespace {
 constexpr int kPipeChunks = 8;
 constexpr int64_t kPipeMinNnz = (int64_t)1 << 23;  // below this, copy then compute
 
-int spmv_compute_pipelined(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x, int vt,
-                           int32_t rows, int32_t cols, int32_t nnz) {
+using ChunkRun = int (*)(const tacogb_csr* A, const void* dense, void* result, int32_t N,
+                         int32_t btype, cudaStream_t st);
+
+int run_spmv_chunk(const tacogb_csr* A, const void* x, void* y, int32_t, int32_t,
+                   cudaStream_t st) {
+  return spmv_run(A, x, y, TACOGB_VARIANT_AUTO, st);
+}
+
+// FP64 chunks use the double-float tile that splits B on the fly (no per-call split of B, whose
+// range flag would be shared by the chunks); the other types use the library's default.
+int run_spmm_chunk(const tacogb_csr* A, const void* B, void* C, int32_t N, int32_t btype,
+                   cudaStream_t st) {
+  static const int df = spmm_variant_index("merge_w512_df");
+  return spmm_run(A, N, B, btype, C, A->vtype == TACOGB_F64 ? df : TACOGB_VARIANT_AUTO, st);
+}
+
+int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int32_t rows,
+                          int32_t cols, int32_t nnz, const void* dense, size_t dense_bytes,
+                          int32_t N, int32_t btype, void* result, size_t res_row_bytes,
+                          ChunkRun run) {
   const int32_t* pos = (const int32_t*)A->indices[1][0];
   const int32_t* crd = (const int32_t*)A->indices[1][1];
   const size_t vb = value_bytes(vt);
   cudaStream_t st = lib_stream(), h2d, d2h;
   cudaEvent_t* ev;
   if (!st || !pipeline_streams(&h2d, &d2h, &ev)) {
-    set_error(TACOGB_ERR_CUDA, "spmv: no GPU streams");
+    set_error(TACOGB_ERR_CUDA, "%s: no GPU streams", what);
     return TACOGB_ERR_CUDA;
   }
   // chunk boundaries on the host pos: first row whose start reaches j * nnz / K
   const int K = (int)std::min<int64_t>(kPipeChunks, std::max<int64_t>(1, nnz / (kPipeMinNnz / 2)));
-  TACOGB_CHECK_ARG(pos[0] == 0, "spmv operand A: pos[0] is not 0");
+  TACOGB_CHECK_ARG(pos[0] == 0, "%s: pos[0] is not 0", what);
   int32_t rb[kPipeChunks + 1];
   rb[0] = 0;
   for (int j = 1; j < K; j++) {
@@ -749,11 +799,20 @@ int spmv_compute_pipelined(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x,
     rb[j] = lo;
   }
   rb[K] = rows;
+  // each chunk is checked on the device into its own counters (no synchronisation per chunk)
+  static_assert(kPipeChunks <= kMaxPublishedChecks, "one published check per chunk");
+  const bool check = validation_on();
+  TACOGB_CHECK_ARG(cols > 0 || nnz == 0, "%s: %d nonzeros in a matrix of 0 columns", what, nnz);
+  unsigned long long* cnt = nullptr;
+  if (check) {
+    cnt = (unsigned long long*)scratch(5 * sizeof(unsigned long long) * kPipeChunks, 11);
+    if (!cnt) return last_code();
+  }
   int64_t meta[3 * kPipeChunks], coff[kPipeChunks + 1], voff[kPipeChunks + 1];
   int64_t poff = 0, c = 0, v = 0;
   for (int j = 0; j < K; j++) {
     const int64_t k0 = pos[rb[j]], k1 = pos[rb[j + 1]];
-    TACOGB_CHECK_ARG(k1 >= k0, "spmv operand A: pos decreases before segment %d", rb[j + 1]);
+    TACOGB_CHECK_ARG(k1 >= k0, "%s: pos decreases before segment %d", what, rb[j + 1]);
     meta[3 * j] = rb[j];
     meta[3 * j + 1] = rb[j + 1] - rb[j];
     meta[3 * j + 2] = poff;
@@ -767,13 +826,14 @@ int spmv_compute_pipelined(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x,
   int32_t* dposc = (int32_t*)stage_buffer(0, (size_t)poff * 4 + 64);
   int32_t* dcrd = (int32_t*)stage_buffer(1, (size_t)c * 4 + 64);
   unsigned char* dval = (unsigned char*)stage_buffer(2, (size_t)v * vb + 64);
-  void* dx = stage_buffer(3, (size_t)cols * vb + 64);
-  unsigned char* dy = (unsigned char*)stage_buffer(4, (size_t)rows * vb + 64);
+  void* ddense = stage_buffer(3, dense_bytes + 64);
+  unsigned char* dres = (unsigned char*)stage_buffer(4, (size_t)rows * res_row_bytes + 64);
   int64_t* dmeta = (int64_t*)stage_buffer(8, sizeof(meta));
-  if (!dpos || !dposc || !dcrd || !dval || !dx || !dy || !dmeta) return TACOGB_ERR_ALLOC;
+  if (!dpos || !dposc || !dcrd || !dval || !ddense || !dres || !dmeta) return TACOGB_ERR_ALLOC;
   // every copy is issued up front on the host -> device stream
   TACOGB_CUDA_TRY(cudaMemcpyAsync(dmeta, meta, sizeof(int64_t) * 3 * K, cudaMemcpyHostToDevice, h2d));
-  if (cols) TACOGB_CUDA_TRY(cudaMemcpyAsync(dx, x->vals, (size_t)cols * vb, cudaMemcpyHostToDevice, h2d));
+  if (dense_bytes)
+    TACOGB_CUDA_TRY(cudaMemcpyAsync(ddense, dense, dense_bytes, cudaMemcpyHostToDevice, h2d));
   TACOGB_CUDA_TRY(cudaMemcpyAsync(dpos, pos, ((size_t)rows + 1) * 4, cudaMemcpyHostToDevice, h2d));
   TACOGB_CUDA_TRY(cudaEventRecord(ev[2 * kPipeChunks], h2d));
   for (int j = 0; j < K; j++) {
@@ -786,7 +846,7 @@ int spmv_compute_pipelined(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x,
     }
     TACOGB_CUDA_TRY(cudaEventRecord(ev[j], h2d));
   }
-  // chunks' pos rebased once x and pos are in
+  // chunks' pos rebased once the dense operand and pos are in
   int rc = 0;
   TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[2 * kPipeChunks], 0));
   count_launch();
@@ -796,30 +856,48 @@ int spmv_compute_pipelined(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x,
     const int32_t nr = (int32_t)meta[3 * j + 1];
     const int32_t n = pos[rb[j + 1]] - pos[rb[j]];
     TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[j], 0));
-    tacogb_csr cj{nr, cols, n, dposc + meta[3 * j + 2], dcrd + coff[j], dval + voff[j] * vb, vt};
-    if (validation_on()) {
-      rc = validate_level_device("spmv operand A", nr, cols, cj.pos, cj.crd, n, st);
+    int32_t* cpos = dposc + meta[3 * j + 2];
+    int32_t* ccrd = dcrd + coff[j];
+    tacogb_csr cj{nr, cols, n, cpos, ccrd, dval + voff[j] * vb, vt};
+    if (check) {
+      // a chunk that fails its check is made harmless before its product runs; the verdicts
+      // are read once every chunk is done
+      rc = level_check_enqueue(nr, cols, cpos, ccrd, n, cnt + 5 * j, st);
+      if (rc == 0) rc = level_gate_enqueue(nr, cpos, ccrd, n, cnt + 5 * j, st);
       if (rc) break;
     }
-    rc = spmv_run(&cj, dx, dy + (size_t)rb[j] * vb, TACOGB_VARIANT_AUTO, st);
+    rc = run(&cj, ddense, dres + (size_t)rb[j] * res_row_bytes, N, btype, st);
     if (rc) break;
     TACOGB_CUDA_TRY(cudaEventRecord(ev[kPipeChunks + j], st));
     TACOGB_CUDA_TRY(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0));
     if (nr)
-      TACOGB_CUDA_TRY(cudaMemcpyAsync((unsigned char*)y->vals + (size_t)rb[j] * vb,
-                                      dy + (size_t)rb[j] * vb, (size_t)nr * vb,
-                                      cudaMemcpyDeviceToHost, d2h));
+      TACOGB_CUDA_TRY(cudaMemcpyAsync((unsigned char*)result + (size_t)rb[j] * res_row_bytes,
+                                      dres + (size_t)rb[j] * res_row_bytes,
+                                      (size_t)nr * res_row_bytes, cudaMemcpyDeviceToHost, d2h));
   }
+  if (check && rc == 0) rc = level_checks_publish(cnt, K, st);
   // nothing may still be copying when the call returns, whatever happened
   const cudaError_t e1 = cudaStreamSynchronize(h2d), e2 = cudaStreamSynchronize(st),
                     e3 = cudaStreamSynchronize(d2h);
   if (rc) return rc;
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
-    set_error(TACOGB_ERR_CUDA, "spmv: %s", cudaGetErrorString(e1 != cudaSuccess ? e1
-                                                               : e2 != cudaSuccess ? e2 : e3));
+    set_error(TACOGB_ERR_CUDA, "%s: %s", what,
+              cudaGetErrorString(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3));
     return TACOGB_ERR_CUDA;
   }
+  // the first chunk that failed, with its segment and position in the whole operand
+  if (check)
+    for (int j = 0; j < K; j++)
+      if (int v = level_verdict(what, j, rb[j], pos[rb[j]])) return v;
   return consume_device_status();
+}
+
+// Large host operands, every array host-resident: the pipelined path.
+bool pipeline_applies(int32_t nnz, std::initializer_list<const void*> arrays) {
+  if (nnz < kPipeMinNnz) return false;
+  for (const void* p : arrays)
+    if (p == nullptr || device_accessible(p)) return false;
+  return true;
 }
 }  // namespace
 
@@ -846,10 +924,9 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   TACOGB_CHECK_ARG(nnz >= 0, "spmv: negative nnz");
   const size_t vb = value_bytes(vt);
   // large host operands: copies, checks, products and returns overlapped chunk by chunk
-  if (nnz >= kPipeMinNnz && !device_accessible(pos) && !device_accessible(crd) &&
-      !device_accessible(A->vals) && !device_accessible(x->vals) &&
-      !device_accessible(y->vals) && crd != nullptr && A->vals != nullptr && x->vals != nullptr)
-    return spmv_compute_pipelined(y, A, x, vt, rows, cols, nnz);
+  if (pipeline_applies(nnz, {pos, crd, A->vals, x->vals, y->vals}))
+    return csr_product_pipelined("spmv operand A", A, vt, rows, cols, nnz, x->vals,
+                                 (size_t)cols * vb, 1, vt, y->vals, vb, run_spmv_chunk);
 
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ox;
@@ -962,6 +1039,11 @@ int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   TACOGB_CHECK_ARG(pos != nullptr, "spmm: null pos");
   int32_t nnz = 0;
   if (int rc = read_i32(pos + rows, &nnz)) return rc;
+  // large host operands: copies, checks, products and returns overlapped chunk by chunk
+  if (pipeline_applies(nnz, {pos, crd, A->vals, B->vals, C->vals}))
+    return csr_product_pipelined("spmm operand A", A, at, rows, cols, nnz, B->vals,
+                                 (size_t)cols * N * value_bytes(bt), N, bt, C->vals,
+                                 (size_t)N * value_bytes(ct), run_spmm_chunk);
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ob;
   LevelCheck chk;

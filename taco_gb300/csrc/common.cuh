@@ -84,6 +84,14 @@ void* scratch(size_t bytes, int slot);
 // check it after synchronising, tacogb_device_status() reads and clears it.
 constexpr int TACOGB_DEV_TIMEOUT = 1;
 int* device_status();
+// Per-device mailbox of kMailboxWords 64-bit words in mapped pinned host memory (the device
+// address; the same address reads on the host under unified addressing).  Kernels publish
+// small results there with plain stores, so the host reads them after a stream synchronisation
+// without a device -> host copy queued behind large copies on the copy engines.
+// Words 0..59: published index checks (validate.cu); the last word: the SpMV locality count.
+constexpr int kMailboxWords = 64;
+constexpr int kMailboxLocality = kMailboxWords - 1;
+unsigned long long* host_mailbox();
 // Word of the same zero-initialised 256-byte block holding the double-float SpMV's x-range
 // flag (set by its prep kernel, cleared by its fix-up kernel).
 constexpr int kXFlagWord = 16;

@@ -1126,7 +1126,7 @@ constexpr int kLocalSamples = 4096;
 constexpr int kLocalGap = 64;
 
 __global__ void spmv_locality_kernel(const int32_t* __restrict__ crd, int64_t nnz,
-                                     int32_t* __restrict__ out) {
+                                     volatile unsigned long long* out) {
   __shared__ int warp_count[8];
   int c = 0;
   for (int i = threadIdx.x; i < kLocalSamples; i += blockDim.x) {
@@ -1139,7 +1139,8 @@ __global__ void spmv_locality_kernel(const int32_t* __restrict__ crd, int64_t nn
   if (threadIdx.x == 0) {
     int t = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += warp_count[w];
-    *out = t;
+    *out = (unsigned long long)t;  // mapped host memory
+    __threadfence_system();
   }
 }
 
@@ -1187,15 +1188,16 @@ int spmv_auto_variant(const tacogb_csr* A, cudaStream_t st) {
     cudaGetLastError();
     return scattered;
   }
-  int32_t* dcount = (int32_t*)scratch(256, 11);
-  if (!dcount) return scattered;
+  // the count goes straight to the host mailbox: no copy that could queue behind large copies
+  // on the copy engines (the pipelined products run this on chunks while copies are in flight)
+  unsigned long long* box = host_mailbox();
+  if (!box) return scattered;
+  volatile unsigned long long* word = box + kMailboxLocality;
   count_launch();
-  spmv_locality_kernel<<<1, 256, 0, st>>>(A->crd, A->nnz, dcount);
-  int32_t h = 0;
-  if (cudaGetLastError() != cudaSuccess ||
-      cudaMemcpyAsync(&h, dcount, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess)
+  spmv_locality_kernel<<<1, 256, 0, st>>>(A->crd, A->nnz, word);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
     return scattered;
+  const int64_t h = (int64_t)*word;
   const int v = 2 * h > kLocalSamples ? local : scattered;
   std::lock_guard<std::mutex> lk(g_auto_mu);
   if (g_auto.size() >= 65536) g_auto.clear();  // bounded: a long-running caller starts over

@@ -12,7 +12,10 @@
 // The check runs on the GPU, on the arrays the kernels will read (the caller's device or managed
 // arrays, or the staged copies of host arrays): one streaming kernel that reads pos and crd
 // once, in bounds (crd at [0, nnz) only, pos at [0, outer]), then one synchronisation to read
-// the verdict before any gathering kernel is launched.  When a call cannot reach a GPU at all,
+// the verdict before any gathering kernel is launched.  The counters are set and read by
+// kernels (the verdict is published into mapped host memory), so a check issues no copies: in
+// the pipelined products it runs between large copies in flight on the copy engines and does
+// not queue behind them.  When a call cannot reach a GPU at all,
 // host-resident levels are checked on the host instead, so that invalid input is still reported
 // as TACOGB_ERR_ARG rather than as the missing device; tacogb_validate_level_host exposes that
 // host check (multi-threaded for large levels).
@@ -150,8 +153,33 @@ int host_check(const char* what, int64_t outer, int32_t inner, const int32_t* po
   return 0;
 }
 
-// Device check.  out: [0] bits, [1] first bad segment, [2] first bad position, [3] descents,
-// [4] descents at the starts of non-empty segments (all zero / ~0 before the launch).
+// Counters of one check: [0] bits, [1] first bad segment, [2] first bad position, [3] descents,
+// [4] descents at the starts of non-empty segments.
+__global__ void level_check_init(unsigned long long* __restrict__ out) {
+  if (threadIdx.x < 5) out[threadIdx.x] = (threadIdx.x == 1 || threadIdx.x == 2) ? ~0ull : 0ull;
+}
+
+// `count` sets of counters into the host mailbox (plain stores to mapped host memory).
+__global__ void level_check_publish(const unsigned long long* __restrict__ out, int count,
+                                    volatile unsigned long long* box) {
+  for (int i = threadIdx.x; i < 5 * count; i += blockDim.x) box[i] = out[i];
+  __threadfence_system();
+}
+
+// A level whose counters show a violation becomes pos = 0, ..., 0, nnz and crd = 0.
+__global__ void level_gate_kernel(int64_t outer, int32_t* __restrict__ pos,
+                                  int32_t* __restrict__ crd, int64_t nnz,
+                                  const unsigned long long* __restrict__ out) {
+  if (out[0] == 0 && out[3] == out[4]) return;
+  const int64_t n = std::max(outer + 1, nnz);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    if (k <= outer) pos[k] = k == outer ? (int32_t)nnz : 0;
+    if (k < nnz && crd) crd[k] = 0;
+  }
+}
+
+// Device check into the counters (set by level_check_init before the launch).
 __global__ void level_check_kernel(int64_t outer, int32_t inner, const int32_t* __restrict__ pos,
                                    const int32_t* __restrict__ crd, int64_t nnz,
                                    unsigned long long* __restrict__ out) {
@@ -160,6 +188,7 @@ __global__ void level_check_kernel(int64_t outer, int32_t inner, const int32_t* 
   const int64_t n = std::max(outer, nnz);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+    if (k == 0 && __ldg(pos) != 0) bits |= kBadPos0;
     if (k < outer) {
       const int64_t a = __ldg(pos + k), b = __ldg(pos + k + 1);
       if (b < a) {
@@ -203,6 +232,58 @@ __global__ void level_check_kernel(int64_t outer, int32_t inner, const int32_t* 
 
 bool validation_on() { return g_validate.load(std::memory_order_relaxed) != 0; }
 
+int level_check_enqueue(int64_t outer, int32_t inner, const int32_t* pos, const int32_t* crd,
+                        int64_t nnz, unsigned long long* out, cudaStream_t st) {
+  TACOGB_LAUNCH("level_check_init", st, level_check_init<<<1, 32, 0, st>>>(out));
+  if (outer <= 0 && nnz <= 0) return 0;
+  const int64_t n = std::max<int64_t>(std::max(outer, nnz), 1);  // thread 0 reads pos[0]
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
+  TACOGB_LAUNCH("level_check_kernel", st,
+                level_check_kernel<<<(unsigned)blocks, 256, 0, st>>>(outer, inner, pos, crd,
+                                                                      nnz, out));
+  return 0;
+}
+
+int level_gate_enqueue(int64_t outer, int32_t* pos, int32_t* crd, int64_t nnz,
+                       const unsigned long long* out, cudaStream_t st) {
+  if (outer <= 0 && nnz <= 0) return 0;
+  const int64_t n = std::max(outer + 1, nnz);
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 4);
+  TACOGB_LAUNCH("level_gate_kernel", st,
+                level_gate_kernel<<<(unsigned)blocks, 256, 0, st>>>(outer, pos, crd, nnz, out));
+  return 0;
+}
+
+static_assert(5 * kMaxPublishedChecks <= kMailboxLocality, "published checks fit the mailbox");
+
+int level_checks_publish(const unsigned long long* out, int count, cudaStream_t st) {
+  TACOGB_CHECK_ARG(count >= 1 && count <= kMaxPublishedChecks, "validate: %d checks to publish",
+                   count);
+  volatile unsigned long long* box = host_mailbox();
+  if (!box) return last_code();
+  TACOGB_LAUNCH("level_check_publish", st,
+                level_check_publish<<<1, 64, 0, st>>>(out, count, (unsigned long long*)box));
+  return 0;
+}
+
+int level_verdict(const char* what, int index, int64_t seg_base, int64_t pos_base) {
+  volatile unsigned long long* box = host_mailbox();
+  if (!box) return last_code();
+  unsigned long long h[5];
+  for (int i = 0; i < 5; i++) h[i] = box[5 * index + i];
+  unsigned bits = (unsigned)h[0];
+  if (!(bits & (kBadPosOrder | kBadPosEnd)) && h[3] != h[4]) bits |= kBadCrdOrder;
+  if (bits) {
+    // the kernel locates range errors; an order error is known from the two counts only
+    char msg[256];
+    describe(bits, seg_base + (int64_t)h[1],
+             (bits & kBadCrdRange) ? pos_base + (int64_t)h[2] : -1, what, msg, sizeof(msg));
+    set_error(TACOGB_ERR_ARG, "%s", msg);
+    return TACOGB_ERR_ARG;
+  }
+  return 0;
+}
+
 int validate_level_device(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
                           const int32_t* crd, int64_t nnz, cudaStream_t st) {
   if (outer <= 0 && nnz <= 0) return 0;
@@ -210,30 +291,10 @@ int validate_level_device(const char* what, int64_t outer, int32_t inner, const 
   // five counters in the library's scratch arena (slot reserved for the checks)
   unsigned long long* out = (unsigned long long*)scratch(5 * sizeof(unsigned long long), 11);
   if (!out) return last_code();
-  const unsigned long long init[5] = {0, ~0ull, ~0ull, 0, 0};
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(out, init, sizeof(init), cudaMemcpyHostToDevice, st));
-  int32_t first = 0;
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(&first, pos, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  const int64_t n = std::max(outer, nnz);
-  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
-  TACOGB_LAUNCH("level_check_kernel", st,
-                level_check_kernel<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, st>>>(
-                    outer, inner, pos, crd, nnz, out));
-  unsigned long long h[5];
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, st));
+  if (int rc = level_check_enqueue(outer, inner, pos, crd, nnz, out, st)) return rc;
+  if (int rc = level_checks_publish(out, 1, st)) return rc;
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
-  unsigned bits = (unsigned)h[0];
-  if (first != 0) bits |= kBadPos0;
-  if (!(bits & (kBadPosOrder | kBadPosEnd)) && h[3] != h[4]) bits |= kBadCrdOrder;
-  if (bits) {
-    // the kernel locates range errors; an order error is known from the two counts only
-    char msg[256];
-    describe(bits, (int64_t)h[1], (bits & kBadCrdRange) ? (int64_t)h[2] : -1, what, msg,
-             sizeof(msg));
-    set_error(TACOGB_ERR_ARG, "%s", msg);
-    return TACOGB_ERR_ARG;
-  }
-  return 0;
+  return level_verdict(what, 0, 0, 0);
 }
 
 void LevelCheck::begin(const char* what, int64_t outer, int32_t inner, const int32_t* pos,

@@ -16,6 +16,23 @@ bool validation_on();
 int validate_level_device(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
                           const int32_t* crd, int64_t nnz, cudaStream_t st);
 
+// The same check without synchronising, for levels checked while copies are in flight (the
+// pipelined products): level_check_enqueue checks a level (device arrays) into five counters at
+// `out` (device memory); level_gate_enqueue then makes the level harmless when its counters
+// show a violation (pos becomes 0, ..., 0, nnz and crd all 0, which every kernel reads in
+// bounds; inner >= 1 is required), so that a kernel launched after it on st never gathers
+// through a bad index; level_checks_publish copies `count` counter sets into the host mailbox
+// (at most kMaxPublishedChecks), and level_verdict reads one published set after the stream
+// has been synchronised: 0, or TACOGB_ERR_ARG with a message whose segment and position are
+// offset by seg_base and pos_base (the level's place in the whole operand).
+constexpr int kMaxPublishedChecks = 12;
+int level_check_enqueue(int64_t outer, int32_t inner, const int32_t* pos, const int32_t* crd,
+                        int64_t nnz, unsigned long long* out, cudaStream_t st);
+int level_gate_enqueue(int64_t outer, int32_t* pos, int32_t* crd, int64_t nnz,
+                       const unsigned long long* out, cudaStream_t st);
+int level_checks_publish(const unsigned long long* out, int count, cudaStream_t st);
+int level_verdict(const char* what, int index, int64_t seg_base, int64_t pos_base);
+
 // One level's check around a call's staging: begin() records the level as the caller passed it;
 // finish() checks the device copies dpos/dcrd the kernels will read (validate_level_device), or,
 // when the staging failed (dpos null) and the level is host-resident, checks it on the host so

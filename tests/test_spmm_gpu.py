@@ -178,3 +178,57 @@ def test_abi_rejects_mismatch():
     Ct = T.dense(np.zeros((1, 4)), [1, 4])
     assert tg.lib().tacogb_spmm_compute(Ct.ptr, At.ptr, Bt.ptr) == 1
     assert b"B has 3 rows" in tg.lib().tacogb_last_error()
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_abi_pipelined_host_operands(dtype):
+    """Host operands of 2^23 nonzeros or more go through the pipelined path (B first, then A's
+    chunks copied, checked and multiplied as each lands, C returned chunk by chunk)."""
+    s = W.spmm_powerlaw(rows=300000)
+    pos, crd, vals = W.generate(s)
+    assert len(crd) >= 1 << 23
+    N = 16
+    B = W.dense(61, s.cols * N).reshape(s.cols, N)
+    idx = np.unique(np.concatenate([np.argsort(np.diff(pos))[-32:],
+                                    np.random.default_rng(2).choice(s.rows, 3000, False)]))
+    from tests.helpers import sub_rows
+    ref = O.spmm(*sub_rows(pos, crd, vals, idx), B)
+    v, Bt_ = vals.astype(dtype), np.ascontiguousarray(B.astype(dtype))
+    for _ in range(2):
+        C = np.full((s.rows, N), np.nan, dtype=dtype)
+        Ct, At, Bt = T.dense(C, [s.rows, N]), T.csr(pos, crd, v, [s.rows, s.cols]), T.dense(Bt_, [s.cols, N])
+        assert tg.lib().tacogb_spmm_compute(Ct.ptr, At.ptr, Bt.ptr) == 0, tg.lib().tacogb_last_error()
+        assert not np.isnan(C).any()
+        assert normwise(C[idx], ref) <= (F64_TOL if dtype == np.float64 else TOL["f32"])
+
+
+@pytest.mark.parametrize("kind", ["crd_high", "pos_order"])
+def test_abi_pipelined_rejects_a_corrupt_chunk(kind):
+    """A corrupt chunk of the pipelined path: TACOGB_ERR_ARG naming the segment or position in
+    the whole operand, and the next call with valid operands computes the oracle's result."""
+    s = W.spmm_powerlaw(rows=300000)
+    pos, crd, vals = W.generate(s)
+    N = 8
+    B = np.ascontiguousarray(W.dense(62, s.cols * N).reshape(s.cols, N))
+    bad_pos, bad_crd = pos.copy(), crd.copy()
+    if kind == "crd_high":
+        where = len(crd) - 1000  # in the last chunk
+        bad_crd[where] = s.cols + 3
+        expect = b"out of range at position %d" % where
+    else:
+        # a middle row of a middle chunk whose segment and the next are non-empty
+        i = int(np.searchsorted(pos, len(crd) // 2)) + 7
+        while not (pos[i - 1] < pos[i] < pos[i + 1]):
+            i += 1
+        bad_pos[i] = pos[i + 1] + 1
+        expect = b"pos decreases at segment %d" % i
+    C = np.zeros((s.rows, N))
+    Ct, At, Bt = T.dense(C, [s.rows, N]), T.csr(bad_pos, bad_crd, vals, [s.rows, s.cols]), T.dense(B, [s.cols, N])
+    assert tg.lib().tacogb_spmm_compute(Ct.ptr, At.ptr, Bt.ptr) == 1
+    assert expect in tg.lib().tacogb_last_error(), tg.lib().tacogb_last_error()
+    C2 = np.full((s.rows, N), np.nan)
+    Ct2, At2 = T.dense(C2, [s.rows, N]), T.csr(pos, crd, vals, [s.rows, s.cols])
+    assert tg.lib().tacogb_spmm_compute(Ct2.ptr, At2.ptr, Bt.ptr) == 0, tg.lib().tacogb_last_error()
+    idx = np.random.default_rng(3).choice(s.rows, 2000, False)
+    from tests.helpers import sub_rows
+    assert normwise(C2[idx], O.spmm(*sub_rows(pos, crd, vals, idx), B)) <= F64_TOL
