@@ -755,26 +755,55 @@ namespace {
 constexpr int kPipeChunks = 8;
 constexpr int64_t kPipeMinNnz = (int64_t)1 << 23;  // below this, copy then compute
 
-using ChunkRun = int (*)(const tacogb_csr* A, const void* dense, void* result, int32_t N,
-                         int32_t btype, cudaStream_t st);
+// One kind of product of the pipeline.  reserve() takes any buffers it needs before the copies
+// are issued (an allocation later could wait on them); prepare() runs on the library stream
+// once the dense operand has landed; run() multiplies one chunk.
+struct ChunkProduct {
+  virtual ~ChunkProduct() = default;
+  virtual int reserve(int32_t /*cols*/, int32_t /*N*/, int32_t /*btype*/, int /*vt*/) { return 0; }
+  virtual int prepare(const void* /*dense*/, int32_t /*cols*/, int32_t /*N*/, cudaStream_t) {
+    return 0;
+  }
+  virtual int run(const tacogb_csr* A, const void* dense, void* result, int32_t N, int32_t btype,
+                  cudaStream_t st) = 0;
+};
 
-int run_spmv_chunk(const tacogb_csr* A, const void* x, void* y, int32_t, int32_t,
-                   cudaStream_t st) {
-  return spmv_run(A, x, y, TACOGB_VARIANT_AUTO, st);
-}
+struct SpmvChunks final : ChunkProduct {
+  int run(const tacogb_csr* A, const void* x, void* y, int32_t, int32_t, cudaStream_t st) override {
+    return spmv_run(A, x, y, TACOGB_VARIANT_AUTO, st);
+  }
+};
 
-// FP64 chunks use the double-float tile that splits B on the fly (no per-call split of B, whose
-// range flag would be shared by the chunks); the other types use the library's default.
-int run_spmm_chunk(const tacogb_csr* A, const void* B, void* C, int32_t N, int32_t btype,
-                   cudaStream_t st) {
-  static const int df = spmm_variant_index("merge_w512_df");
-  return spmm_run(A, N, B, btype, C, A->vtype == TACOGB_F64 ? df : TACOGB_VARIANT_AUTO, st);
-}
+// FP64: B split into double-float pairs once, when it lands, and every chunk multiplied over
+// the split (the library's default FP64 tile, without a split per chunk); FP64 with odd N:
+// the double-float tile that splits B on the fly; FP32 and BF16 B: the library's default.
+struct SpmmChunks final : ChunkProduct {
+  void* bdf = nullptr;
+  int* flag = nullptr;
+  int reserve(int32_t cols, int32_t N, int32_t btype, int vt) override {
+    // the split takes pairs of B's elements: N even (the staged B is 256-byte aligned)
+    if (vt != TACOGB_F64 || btype != TACOGB_F64 || N <= 0 || N % 2 != 0) return 0;
+    int* status = device_status();
+    if (!status) return last_code();
+    flag = status + kPFlagWord;
+    bdf = stage_buffer(60, (size_t)cols * N * sizeof(double) + 64);
+    return bdf ? 0 : TACOGB_ERR_ALLOC;
+  }
+  int prepare(const void* B, int32_t cols, int32_t N, cudaStream_t st) override {
+    return bdf ? spmm_split_once((const double*)B, cols, N, bdf, flag, st) : 0;
+  }
+  int run(const tacogb_csr* A, const void* B, void* C, int32_t N, int32_t btype,
+          cudaStream_t st) override {
+    if (bdf) return spmm_run_presplit(A, N, (const double*)B, bdf, flag, (double*)C, st);
+    static const int df = spmm_variant_index("merge_w512_df");
+    return spmm_run(A, N, B, btype, C, A->vtype == TACOGB_F64 ? df : TACOGB_VARIANT_AUTO, st);
+  }
+};
 
 int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int32_t rows,
                           int32_t cols, int32_t nnz, const void* dense, size_t dense_bytes,
                           int32_t N, int32_t btype, void* result, size_t res_row_bytes,
-                          ChunkRun run) {
+                          ChunkProduct& prod) {
   const int32_t* pos = (const int32_t*)A->indices[1][0];
   const int32_t* crd = (const int32_t*)A->indices[1][1];
   const size_t vb = value_bytes(vt);
@@ -830,6 +859,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   unsigned char* dres = (unsigned char*)stage_buffer(4, (size_t)rows * res_row_bytes + 64);
   int64_t* dmeta = (int64_t*)stage_buffer(8, sizeof(meta));
   if (!dpos || !dposc || !dcrd || !dval || !ddense || !dres || !dmeta) return TACOGB_ERR_ALLOC;
+  if (int rc = prod.reserve(cols, N, btype, vt)) return rc;
   // every copy is issued up front on the host -> device stream
   TACOGB_CUDA_TRY(cudaMemcpyAsync(dmeta, meta, sizeof(int64_t) * 3 * K, cudaMemcpyHostToDevice, h2d));
   if (dense_bytes)
@@ -852,6 +882,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   count_launch();
   spmv_rebase_pos<<<dim3(64, K), 256, 0, st>>>(dpos, dmeta, K, dposc);
   rc = launch_check("spmv_rebase_pos");
+  if (rc == 0) rc = prod.prepare(ddense, cols, N, st);
   for (int j = 0; j < K && rc == 0; j++) {
     const int32_t nr = (int32_t)meta[3 * j + 1];
     const int32_t n = pos[rb[j + 1]] - pos[rb[j]];
@@ -866,7 +897,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
       if (rc == 0) rc = level_gate_enqueue(nr, cpos, ccrd, n, cnt + 5 * j, st);
       if (rc) break;
     }
-    rc = run(&cj, ddense, dres + (size_t)rb[j] * res_row_bytes, N, btype, st);
+    rc = prod.run(&cj, ddense, dres + (size_t)rb[j] * res_row_bytes, N, btype, st);
     if (rc) break;
     TACOGB_CUDA_TRY(cudaEventRecord(ev[kPipeChunks + j], st));
     TACOGB_CUDA_TRY(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0));
@@ -924,9 +955,11 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   TACOGB_CHECK_ARG(nnz >= 0, "spmv: negative nnz");
   const size_t vb = value_bytes(vt);
   // large host operands: copies, checks, products and returns overlapped chunk by chunk
-  if (pipeline_applies(nnz, {pos, crd, A->vals, x->vals, y->vals}))
+  if (pipeline_applies(nnz, {pos, crd, A->vals, x->vals, y->vals})) {
+    SpmvChunks spmv_chunks;
     return csr_product_pipelined("spmv operand A", A, vt, rows, cols, nnz, x->vals,
-                                 (size_t)cols * vb, 1, vt, y->vals, vb, run_spmv_chunk);
+                                 (size_t)cols * vb, 1, vt, y->vals, vb, spmv_chunks);
+  }
 
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ox;
@@ -1040,10 +1073,12 @@ int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   int32_t nnz = 0;
   if (int rc = read_i32(pos + rows, &nnz)) return rc;
   // large host operands: copies, checks, products and returns overlapped chunk by chunk
-  if (pipeline_applies(nnz, {pos, crd, A->vals, B->vals, C->vals}))
+  if (pipeline_applies(nnz, {pos, crd, A->vals, B->vals, C->vals})) {
+    SpmmChunks spmm_chunks;
     return csr_product_pipelined("spmm operand A", A, at, rows, cols, nnz, B->vals,
                                  (size_t)cols * N * value_bytes(bt), N, bt, C->vals,
-                                 (size_t)N * value_bytes(ct), run_spmm_chunk);
+                                 (size_t)N * value_bytes(ct), spmm_chunks);
+  }
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, ob;
   LevelCheck chk;

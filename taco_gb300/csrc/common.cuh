@@ -103,6 +103,9 @@ constexpr int kBFlagWord = 17;
 constexpr int kDFlagWord = 18;
 // Word of the same block holding the fused MTTKRP's D-range flag (cleared before its split).
 constexpr int kMFlagWord = 19;
+// Word of the same block holding the pipelined SpMM's B-range flag (cleared before its one
+// split of B, read by every chunk's product).
+constexpr int kPFlagWord = 20;
 
 // ---------------------------------------------------------------- TMA / mbarrier ----------
 

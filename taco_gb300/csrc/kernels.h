@@ -23,6 +23,16 @@ int merge_partition(const int32_t* pos, int32_t n, int64_t nnz, int64_t tile_ite
 int spmm_variant_count();
 const char* spmm_variant_name(int v);
 int spmm_variant_index(const char* name);  // -1 when no variant has that name
+// One split of an FP64 B (cols x N, N even, B and bdf 16-byte aligned; bdf holds cols*N
+// double-float pairs) for several products over it, and the product of one CSR A over that
+// split (the merge_w512_dfs tile; an entry of B outside the double-float range, recorded in
+// *flag by the split, sends every tile to native FP64 over B).  Used by the pipelined taco-ABI
+// SpMM, whose chunks share one B.
+bool spmm_presplit_applies(const void* B, int32_t N);
+int spmm_split_once(const double* B, int32_t cols, int32_t N, void* bdf, int* flag,
+                    cudaStream_t st);
+int spmm_run_presplit(const tacogb_csr* A, int32_t N, const double* B, const void* bdf, int* flag,
+                      double* C, cudaStream_t st);
 int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,
              cudaStream_t st);
 

@@ -101,7 +101,7 @@ spmm_tma_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd
   }
 }
 
-// Adds carried partial rows, in tile order, into the row where each run of tiles ends.// Adds carried partial rows, in tile order, into the row where each run of tiles ends.
+// Adds carried partial rows, in tile order, into the row where each run of tiles ends.
 // bflag (optional) is the B-range flag of the product, cleared here for the next one.
 template <typename Out>
 __global__ void spmm_carry_fixup(const int32_t* __restrict__ carry_row,
@@ -204,8 +204,11 @@ const SpmmVariant kSpmmVariants[] = {
 };
 constexpr int kNumSpmmVariants = sizeof(kSpmmVariants) / sizeof(kSpmmVariants[0]);
 
+// presplit/pflag (MmDFS only): B already split into double-float pairs, with its range flag,
+// by spmm_split_once for several products; the fix-up then leaves the flag alone.
 template <class P, int VEC, bool STREAM, int TMA = 0>
-int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, cudaStream_t st) {
+int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, cudaStream_t st,
+                const void* presplit = nullptr, int* pflag = nullptr) {
   const int64_t total = (int64_t)A->rows + A->nnz;
   const int64_t tiles64 = (total + W - 1) / W;
   if (tiles64 == 0 || N == 0) return 0;
@@ -215,7 +218,8 @@ int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, c
   const size_t crow_bytes = ((size_t)tiles * sizeof(int32_t) + 255) & ~(size_t)255;
   const size_t cval_bytes = (((size_t)tiles * (size_t)N * sizeof(double)) + 255) & ~(size_t)255;
   constexpr bool split = std::is_same<P, MmDFS>::value;
-  const size_t bdf_bytes = split ? (size_t)A->cols * (size_t)N * sizeof(DF) : 0;
+  const size_t bdf_bytes =
+      split && presplit == nullptr ? (size_t)A->cols * (size_t)N * sizeof(DF) : 0;
   unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + bdf_bytes, 1);
   if (!ws) return last_code();
   int2* part = (int2*)ws;
@@ -223,7 +227,11 @@ int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, c
   double* cval = (double*)(ws + part_bytes + crow_bytes);
   const typename P::BV* Bk = (const typename P::BV*)B;
   int* bflag = nullptr;
-  if constexpr (split) {
+  int* clear_flag = nullptr;  // the flag the fix-up clears (this call's own split only)
+  if (split && presplit != nullptr) {
+    Bk = (const typename P::BV*)presplit;
+    bflag = pflag;
+  } else if constexpr (split) {
     // B split once into double-float pairs: every B element is then used about nnz/cols times
     int* status = device_status();
     if (!status) return last_code();
@@ -235,6 +243,7 @@ int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, c
                     spmm_split_b<<<(unsigned)((count / 2 + 255) / 256), 256, 0, st>>>(
                         (const double*)B, bdf, count, bflag));
     Bk = (const typename P::BV*)bdf;
+    clear_flag = bflag;
   }
   if (int rc = merge_partition(A->pos, A->rows, A->nnz, W, tiles, part, st, W / 2)) return rc;
   constexpr int TW = 32 * VEC;
@@ -263,9 +272,12 @@ int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, c
   TACOGB_LAUNCH("spmm_carry_fixup", st,
                 spmm_carry_fixup<typename P::Out><<<(unsigned)((fix_threads + 255) / 256), 256, 0,
                                                     st>>>(crow, cval, tiles, N,
-                                                          (typename P::Out*)C, A->rows, bflag));
+                                                          (typename P::Out*)C, A->rows,
+                                                          clear_flag));
   return 0;
 }
+
+__global__ void spmm_flag_clear(int* flag) { *flag = 0; }
 
 // Sub-warp SpMM over column slabs.  For MmDFS, B is first split into double-float pairs in
 // scratch (one pass over B; every B element is then used about nnz/cols times without further
@@ -397,6 +409,35 @@ int spmm_variant_index(const char* name) {
   for (int i = 0; i < kNumSpmmVariants; i++)
     if (strcmp(kSpmmVariants[i].name, name) == 0) return i;
   return -1;
+}
+
+bool spmm_presplit_applies(const void* B, int32_t N) {
+  return N > 0 && N % 2 == 0 && ((uintptr_t)B & 15) == 0;
+}
+
+int spmm_split_once(const double* B, int32_t cols, int32_t N, void* bdf, int* flag,
+                    cudaStream_t st) {
+  TACOGB_CHECK_ARG(spmm_presplit_applies(B, N) && ((uintptr_t)bdf & 15) == 0,
+                   "SpMM: B split needs even N and 16-byte aligned arrays");
+  TACOGB_LAUNCH("spmm_flag_clear", st, spmm_flag_clear<<<1, 1, 0, st>>>(flag));
+  const int64_t count = (int64_t)cols * N;
+  if (count > 0)
+    TACOGB_LAUNCH("spmm_split_b", st,
+                  spmm_split_b<<<(unsigned)((count / 2 + 255) / 256), 256, 0, st>>>(
+                      B, (DF*)bdf, count, flag));
+  return 0;
+}
+
+int spmm_run_presplit(const tacogb_csr* A, int32_t N, const double* B, const void* bdf, int* flag,
+                      double* C, cudaStream_t st) {
+  TACOGB_CHECK_ARG(A != nullptr && A->vtype == TACOGB_F64, "SpMM: pre-split B needs FP64 A");
+  TACOGB_CHECK_ARG(A->rows >= 0 && A->cols >= 0 && A->nnz >= 0 && N >= 0, "SpMM: negative size");
+  TACOGB_CHECK_ARG((int64_t)A->rows * N <= INT32_MAX,
+                   "SpMM: rows*N exceeds taco's int32 dense positions");
+  TACOGB_CHECK_ARG(spmm_presplit_applies(B, N), "SpMM: B split needs even N, 16-byte aligned B");
+  static const int W = kSpmmVariants[spmm_variant_index("merge_w512_dfs")].tile_items;
+  if (N % 64 == 0) return launch_spmm<MmDFS, 2, false>(A, N, B, C, W, st, bdf, flag);
+  return launch_spmm<MmDFS, 1, false>(A, N, B, C, W, st, bdf, flag);
 }
 
 int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,

@@ -180,26 +180,61 @@ def test_abi_rejects_mismatch():
     assert b"B has 3 rows" in tg.lib().tacogb_last_error()
 
 
-@pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_abi_pipelined_host_operands(dtype):
+_PIPE = {}
+
+
+def _pipe_matrix():
+    if not _PIPE:
+        s = W.spmm_powerlaw(rows=300000)
+        _PIPE["m"] = (s,) + tuple(W.generate(s))
+    return _PIPE["m"]
+
+
+def _pipe_call(pos, crd, vals, B, s, dtype):
+    N = B.shape[1]
+    C = np.full((s.rows, N), np.nan, dtype=dtype)
+    Bt_ = np.ascontiguousarray(B.astype(dtype))
+    Ct, At, Bt = (T.dense(C, [s.rows, N]), T.csr(pos, crd, vals.astype(dtype), [s.rows, s.cols]),
+                  T.dense(Bt_, [s.cols, N]))
+    assert tg.lib().tacogb_spmm_compute(Ct.ptr, At.ptr, Bt.ptr) == 0, tg.lib().tacogb_last_error()
+    assert not np.isnan(C).any()
+    return C
+
+
+@pytest.mark.parametrize("dtype,N", [(np.float64, 16), (np.float32, 16), (np.float64, 64),
+                                     (np.float64, 7)])
+def test_abi_pipelined_host_operands(dtype, N):
     """Host operands of 2^23 nonzeros or more go through the pipelined path (B first, then A's
-    chunks copied, checked and multiplied as each lands, C returned chunk by chunk)."""
-    s = W.spmm_powerlaw(rows=300000)
-    pos, crd, vals = W.generate(s)
+    chunks copied, checked and multiplied as each lands, C returned chunk by chunk).  FP64 with
+    even N multiplies every chunk over one split of B (N=64: the two-wide tile), odd N the
+    tile that splits on the fly."""
+    from tests.helpers import sub_rows
+    s, pos, crd, vals = _pipe_matrix()
     assert len(crd) >= 1 << 23
-    N = 16
     B = W.dense(61, s.cols * N).reshape(s.cols, N)
     idx = np.unique(np.concatenate([np.argsort(np.diff(pos))[-32:],
                                     np.random.default_rng(2).choice(s.rows, 3000, False)]))
-    from tests.helpers import sub_rows
     ref = O.spmm(*sub_rows(pos, crd, vals, idx), B)
-    v, Bt_ = vals.astype(dtype), np.ascontiguousarray(B.astype(dtype))
     for _ in range(2):
-        C = np.full((s.rows, N), np.nan, dtype=dtype)
-        Ct, At, Bt = T.dense(C, [s.rows, N]), T.csr(pos, crd, v, [s.rows, s.cols]), T.dense(Bt_, [s.cols, N])
-        assert tg.lib().tacogb_spmm_compute(Ct.ptr, At.ptr, Bt.ptr) == 0, tg.lib().tacogb_last_error()
-        assert not np.isnan(C).any()
+        C = _pipe_call(pos, crd, vals, B, s, dtype)
         assert normwise(C[idx], ref) <= (F64_TOL if dtype == np.float64 else TOL["f32"])
+
+
+def test_abi_pipelined_b_outside_double_float_range():
+    """An entry of B outside the double-float range sends every chunk's tiles to native FP64
+    over B; the next call, with B in range, is split and multiplied in double-float again."""
+    from tests.helpers import sub_rows
+    s, pos, crd, vals = _pipe_matrix()
+    N = 16
+    idx = np.random.default_rng(4).choice(s.rows, 3000, False)
+    B = W.dense(63, s.cols * N).reshape(s.cols, N)
+    B[s.cols // 2, 3] = 1e-300
+    B[17, :] *= 1e30
+    C = _pipe_call(pos, crd, vals, B, s, np.float64)
+    assert normwise(C[idx], O.spmm(*sub_rows(pos, crd, vals, idx), B)) <= F64_TOL
+    B2 = W.dense(64, s.cols * N).reshape(s.cols, N)
+    C2 = _pipe_call(pos, crd, vals, B2, s, np.float64)
+    assert normwise(C2[idx], O.spmm(*sub_rows(pos, crd, vals, idx), B2)) <= F64_TOL
 
 
 @pytest.mark.parametrize("kind", ["crd_high", "pos_order"])
