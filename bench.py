@@ -36,6 +36,7 @@ sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
 PROFILE_EVERY = 8  # timed steps per step whose kernels are bracketed by CUDA events
+L2_BYTES = 129e6  # GB300's L2
 ESZ = {"f64": 8, "f32": 4, "bf16": 2}
 
 
@@ -66,6 +67,9 @@ def parse(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-secondary", action="store_true",
                    help="skip the secondary workloads the default run reports beside the headline")
+    p.add_argument("--graph", action="store_true",
+                   help="capture the K timed steps in one CUDA graph and time its replay (for "
+                        "launch-bound workloads; per-kernel times come from an untimed pass)")
     a = p.parse_args(argv)
     if a.n is None:
         a.n = 32 if a.workload == "batched_spmm" else 64
@@ -975,7 +979,10 @@ def workload_config(op, world):
     else:
         c = {"workload": op.workload, "rows": op.rows, "cols": op.cols, "nnz": op.nnz,
              "bytes_per_step": op.bytes,
-             "l2": "inputs larger than L2 (%.2f GB per step), no flush" % (op.bytes / 1e9)}
+             "l2": ("inputs larger than L2 (%.2f GB per step), no flush" % (op.bytes / 1e9)
+                    if op.bytes > L2_BYTES else
+                    "L2-resident (%.1f MB per step fits the 129 MB L2), no flush"
+                    % (op.bytes / 1e6))}
         if op.pattern == "spgemm":
             c.update({"nnz_c": op.nnzC, "products": op.products})
         for key, attr in (("n", "N"), ("j", "J")):
@@ -1305,8 +1312,9 @@ def main_batch_spmm(args, torch, tg, L, rank):
 # The workloads the default run measures beside the headline, each in its own process (the
 # same bench.py, so the same code paths and timing rules), summarised into the headline line.
 SECONDARY = [
-    ("spmv_small_f64 (L2-resident: 13.9 MB fits the 129 MB L2)",
-     ["--workload", "spmv_small", "--steps", "500", "--warmup", "20", "--e2e-steps", "10"]),
+    ("spmv_small_f64 (L2-resident: 13.9 MB fits the 129 MB L2; steps replayed as a CUDA graph)",
+     ["--workload", "spmv_small", "--steps", "500", "--warmup", "20", "--e2e-steps", "10",
+      "--graph"]),
     ("spmv_banded_f64", ["--workload", "spmv_banded", "--steps", "50", "--warmup", "5",
                          "--e2e-steps", "5"]),
     ("spmv_powerlaw_f32c", ["--workload", "spmv_powerlaw", "--dtype", "f32", "--steps", "50",
@@ -1322,7 +1330,8 @@ SECONDARY = [
 
 def run_secondary():
     keys = ("metric", "value", "unit", "ms_per_step", "dtype", "gpu_launches", "clocks",
-            "speedup_vs_fp64_per_matrix", "max_normwise_err_vs_fp64", "derived", "variant")
+            "speedup_vs_fp64_per_matrix", "max_normwise_err_vs_fp64", "derived", "variant",
+            "timing")
     env = {k: v for k, v in os.environ.items()
            if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "MASTER_ADDR", "MASTER_PORT")}
     out = []
@@ -1395,20 +1404,48 @@ def main():
         torch.distributed.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    launches0 = L.tacogb_launch_count()
-    # per-kernel device times: CUDA events bracket the launches of every PROFILE_EVERY-th step
-    # of the timed region only, so that event records stay out of the headline time
-    L.tacogb_profile_begin()
-    e0.record(stream)
-    for i in range(args.steps):
-        L.tacogb_profile_enable(1 if i % PROFILE_EVERY == 0 else 0)
-        step(sp)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    launches = L.tacogb_launch_count() - launches0
     names = ctypes.create_string_buffer(64 * 16)
     tot, cnt = (ctypes.c_double * 16)(), (ctypes.c_int32 * 16)()
-    nk = L.tacogb_profile_end(16, names, tot, cnt)
+    if args.graph:
+        # the per-kernel pass, untimed: every PROFILE_EVERY-th step bracketed by events
+        L.tacogb_profile_begin()
+        for i in range(args.steps):
+            L.tacogb_profile_enable(1 if i % PROFILE_EVERY == 0 else 0)
+            step(sp)
+        torch.cuda.synchronize()
+        nk = L.tacogb_profile_end(16, names, tot, cnt)
+        # the K steps captured once (the library's launches are counted at capture) and replayed
+        cs = torch.cuda.Stream()
+        csp = ctypes.c_void_p(cs.cuda_stream)
+        cs.wait_stream(stream)
+        with torch.cuda.stream(cs):
+            step(csp)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        launches0 = L.tacogb_launch_count()
+        with torch.cuda.graph(graph, stream=cs):
+            for _ in range(args.steps):
+                step(csp)
+        launches = L.tacogb_launch_count() - launches0
+        graph.replay()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    else:
+        launches0 = L.tacogb_launch_count()
+        # per-kernel device times: CUDA events bracket the launches of every PROFILE_EVERY-th
+        # step of the timed region only, so that event records stay out of the headline time
+        L.tacogb_profile_begin()
+        e0.record(stream)
+        for i in range(args.steps):
+            L.tacogb_profile_enable(1 if i % PROFILE_EVERY == 0 else 0)
+            step(sp)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches = L.tacogb_launch_count() - launches0
+        nk = L.tacogb_profile_end(16, names, tot, cnt)
     if world > 1:
         torch.distributed.barrier()
     clocks = sampler.stop() if sampler else None
@@ -1428,6 +1465,10 @@ def main():
     dom = max(kernels, key=lambda k: kernels[k][0])
     dom_ms = kernels[dom][0] / kernels[dom][1]
     dom_share = kernels[dom][0] / sum(v[0] for v in kernels.values())
+    if args.graph:
+        # events around single launches overstate microsecond kernels; the replayed step bounds
+        # the kernel from above (exact when the step is that one launch)
+        dom_ms = min(dom_ms, ms / args.steps)
     if op.pattern == "spgemm":  # the bytes model covers all three phases of a step
         dom, dom_ms = "spgemm symbolic + fill + numeric (%s largest)" % dom, ms / args.steps
     peak, peak_kind = measured_peak()
@@ -1509,6 +1550,9 @@ def main():
                "pct_of_peak": value / peak if unit == "GB/s" else None, "gflops": op.flops * args.steps * world / (ms / 1e3) / 1e9,
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": clocks,
+               "timing": ("one CUDA-graph replay of the %d steps (captured after warm-up)"
+                          % args.steps if args.graph else "the %d steps launched from the host"
+                          % args.steps),
                "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kernels.items()}}
         if args.workload == "spmv_powerlaw" and args.dtype == "f64" and world == 1 and \
                 not args.no_secondary:

@@ -160,10 +160,11 @@ int tacogb_spmv(const tacogb_csr* A, const void* x, void* y, int32_t variant, vo
 int tacogb_spmv_variant_count(void);
 const char* tacogb_spmv_variant_name(int32_t variant);
 /* The variant TACOGB_VARIANT_AUTO runs for A: warp tiles sized for scattered columns, or, for a
- * matrix of at least 2^20 nonzeros, for local columns when most gaps between consecutive stored
- * columns (4096 samples) are under 64.  The choice is cached per matrix (pos and crd pointers,
- * rows, nonzeros); the first call for such a matrix runs one small kernel on stream and
- * synchronises it, unless the stream is capturing. */
+ * matrix of at least 2^21 nonzeros, for local columns when most gaps between consecutive stored
+ * columns (4096 samples) are under 64; a matrix of fewer nonzeros whose rows all hold at most 32
+ * runs vector_g4 (one launch, four lanes per row).  The choice is cached per matrix (pos and crd
+ * pointers, rows, nonzeros); the first call for a matrix with rows and nonzeros runs one small
+ * kernel on stream and synchronises it, unless the stream is capturing. */
 int tacogb_spmv_auto_variant(const tacogb_csr* A, void* stream);
 
 /* y = A x like tacogb_spmv (merge-path kernel, default accumulation per value type), for

@@ -254,7 +254,7 @@ int level_gate_enqueue(int64_t outer, int32_t* pos, int32_t* crd, int64_t nnz,
   return 0;
 }
 
-static_assert(5 * kMaxPublishedChecks <= kMailboxLocality, "published checks fit the mailbox");
+static_assert(5 * kMaxPublishedChecks <= kMailboxRowLen, "published checks fit the mailbox");
 
 int level_checks_publish(const unsigned long long* out, int count, cudaStream_t st) {
   TACOGB_CHECK_ARG(count >= 1 && count <= kMaxPublishedChecks, "validate: %d checks to publish",

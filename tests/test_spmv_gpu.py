@@ -255,15 +255,22 @@ def test_abi_csc_operand_and_mismatch():
     assert rc != 0 and b"rows" in tg.lib().tacogb_last_error()
 
 
-@pytest.mark.parametrize("which", ["powerlaw", "banded", "small_rows"])
+@pytest.mark.parametrize("which", ["powerlaw", "banded", "small_rows", "small_bench",
+                                   "small_long_row"])
 def test_auto_variant_choice(which):
     """TACOGB_VARIANT_AUTO picks the local-column tiles for banded columns and the
-    scattered-column tiles otherwise, caches the choice per matrix, and computes exactly what
+    scattered-column tiles otherwise; below 2^21 nonzeros, the one-launch vector kernel when no
+    row holds more than 32 nonzeros.  It caches the choice per matrix and computes exactly what
     the chosen variant computes."""
     s = {"powerlaw": lambda: W.spmv_powerlaw(rows=300000),
          "banded": lambda: W.spmv_banded(rows=300000),
-         "small_rows": lambda: W.spec(5000, kind=W.UNIFORM, len_lo=0, len_hi=3, seed=5)}[which]()
+         "small_rows": lambda: W.spec(5000, kind=W.UNIFORM, len_lo=0, len_hi=3, seed=5),
+         "small_bench": W.spmv_small,
+         "small_long_row": lambda: W.spec(20000, kind=W.POWERLAW, mean=8.0, len_max=2000,
+                                          seed=6)}[which]()
     pos, crd, vals = W.generate(s)
+    if which == "small_long_row":
+        assert np.diff(pos).max() > 32
     x = W.dense(24, s.cols)
     A = tg.CsrMatrix.from_numpy(pos, crd, vals, s.cols)
     c = A.as_csr()
@@ -271,7 +278,8 @@ def test_auto_variant_choice(which):
     v = tg.lib().tacogb_spmv_auto_variant(ctypes.byref(c), sp)
     assert v == tg.lib().tacogb_spmv_auto_variant(ctypes.byref(c), sp)  # cached
     name = tg.spmv_variants()[v]
-    expect = "wtile_d_native_ipt9_b10" if which == "banded" else "wtile_d_native_ipt11"
+    expect = {"banded": "wtile_d_native_ipt9_b10", "small_rows": "vector_g4",
+              "small_bench": "vector_g4"}.get(which, "wtile_d_native_ipt11")
     assert name == expect
     xd = torch.from_numpy(x).cuda()
     y_auto = tg.spmv(A, xd).cpu().numpy()
