@@ -99,6 +99,73 @@ __device__ __forceinline__ void warp_bitonic(uint64_t& key, V& val) {
   }
 }
 
+// warp_bitonic / reg_bitonic on narrow keys without payloads.
+__device__ __forceinline__ void warp_bitonic32(uint32_t& key) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, j);
+      const bool up = (lane & k) == 0;
+      const bool lower = (lane & j) == 0;
+      if (lower == up ? ok < key : ok > key) key = ok;
+    }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void reg_bitonic32(uint32_t (&key)[R]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= 32) {
+        const int jr = j >> 5;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          if (r & jr) continue;
+          const bool up = ((r * 32 + lane) & k) == 0;
+          const uint32_t a = key[r], b = key[r | jr];
+          if ((a > b) == up) {
+            key[r] = b;
+            key[r | jr] = a;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          const uint32_t ok = __shfl_xor_sync(0xffffffffu, key[r], j);
+          const bool up = ((r * 32 + lane) & k) == 0;
+          const bool lower = (lane & j) == 0;
+          if (lower == up ? ok < key[r] : ok > key[r]) key[r] = ok;
+        }
+      }
+    }
+  }
+}
+
+// The values of sorted narrow keys: slot (r, lane) takes the value of product key[r] & 0xFF
+// from the registers val[] of the lane that computed it.
+template <int R, typename V>
+__device__ __forceinline__ void gather_sorted_vals(const uint32_t (&key)[R], V (&val)[R]) {
+  V out[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const int e = (int)(key[r] & 0xFFu);
+    V g = V();
+#pragma unroll
+    for (int rr = 0; rr < R; rr++) {
+      const V t = __shfl_sync(0xffffffffu, val[rr], e & 31);
+      if ((e >> 5) == rr) g = t;
+    }
+    out[r] = g;
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) val[r] = out[r];
+}
+
 // Bitonic sort of cap (power of two) keys/payloads in shared memory by `nthreads` threads
 // starting at thread index `t0`; `sync` synchronises those threads.
 template <typename V, typename Sync>
@@ -135,6 +202,20 @@ __device__ __forceinline__ uint64_t esc_key(int32_t col, int32_t seq) {
   return ((uint64_t)(uint32_t)col << 32) | (uint32_t)seq;
 }
 __device__ __forceinline__ int32_t key_col(uint64_t k) { return (int32_t)(k >> 32); }
+
+// Narrow keys for the register sorts when B has fewer than 2^24 columns: column << 8 | the
+// product's sequence number (< 256 in bins 1 and 2), with 0xFFFFFFFF for empty slots (above
+// every key, since columns stay below 2^24 - 1).  Only the keys move through the sorting
+// network; each value is fetched once afterwards from the lane and register that computed it
+// (sequence number e lives in lane e % 32, register e / 32).  The order is that of the wide
+// keys (column, then sequence), so the sums are the same bit for bit.
+constexpr int64_t kNarrowKeyCols = (1 << 24) - 1;
+__device__ __forceinline__ uint32_t narrow_key(uint64_t k) {
+  return k == ~0ull ? 0xFFFFFFFFu : ((uint32_t)key_col(k) << 8) | ((uint32_t)k & 0xFFu);
+}
+__device__ __forceinline__ uint64_t wide_key(uint32_t k) {
+  return k == 0xFFFFFFFFu ? ~0ull : esc_key((int32_t)(k >> 8), (int32_t)(k & 0xFFu));
+}
 
 // What a pass computes and writes: MODE 0 counts (cnt), 1 writes columns at Cpos, 2 writes
 // values at Cpos, 3 (one pass) writes columns and values at the row's product slot (Cpos holds
@@ -196,9 +277,69 @@ __device__ __forceinline__ void esc_expand(const int32_t* __restrict__ Apos,
   }
 }
 
+// Expands row `row`'s products into a warp's registers: product e = r * 32 + lane, in sequence
+// order (A's entries in order, each B row in order), gets key esc_key(column, e) and, with
+// VALS, the value A(row, j) * B(j, column); slots past the row's P products are left alone.
+// The lanes load up to 32 of A's entries and their B row bounds at once, and a scan of the B
+// row lengths places every product (the source entry of slot e is the number of entries whose
+// inclusive end is at most e, found by a five-step shuffle search), so a row costs four rounds
+// of dependent loads instead of three per A entry.  P <= 32 * R.  Returns P.
+template <int R, bool VALS, typename V>
+__device__ __forceinline__ int warp_expand_regs(const int32_t* __restrict__ Apos,
+                                                const int32_t* __restrict__ Acrd,
+                                                const V* __restrict__ Avals,
+                                                const int32_t* __restrict__ Bpos,
+                                                const int32_t* __restrict__ Bcrd,
+                                                const V* __restrict__ Bvals, int row,
+                                                uint64_t (&key)[R], V (&val)[R]) {
+  const int lane = threadIdx.x & 31;
+  const int32_t a0 = __ldg(Apos + row), na = __ldg(Apos + row + 1) - a0;
+  int seq0 = 0;
+  for (int c = 0; c < na; c += 32) {
+    int32_t b0 = 0, len = 0;
+    V av = V();
+    if (c + lane < na) {
+      const int32_t j = __ldg(Acrd + a0 + c + lane);
+      if (VALS) av = Avals[a0 + c + lane];
+      b0 = __ldg(Bpos + j);
+      len = __ldg(Bpos + j + 1) - b0;
+    }
+    int inc = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    const int exc = inc - len;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int e = r * 32 + lane - seq0;  // this chunk's product index of slot (r, lane)
+      const int ec = min(max(e, 0), max(total - 1, 0));
+      int src = 0;
+#pragma unroll
+      for (int step = 16; step >= 1; step >>= 1) {
+        const int t = __shfl_sync(0xffffffffu, inc, src + step - 1);
+        if (t <= ec) src += step;
+      }
+      const int sb = __shfl_sync(0xffffffffu, b0, src);
+      const int sx = __shfl_sync(0xffffffffu, exc, src);
+      V sa = V();
+      if (VALS) sa = __shfl_sync(0xffffffffu, av, src);
+      if (e >= 0 && e < total) {
+        const int u = e - sx;
+        key[r] = esc_key(__ldg(Bcrd + sb + u), r * 32 + lane);
+        if (VALS) val[r] = mul_rn(sa, Bvals[sb + u]);
+      }
+    }
+    seq0 += total;
+  }
+  return seq0;
+}
+
 // ---- bin 1: P <= 32, one warp per row, registers -----------------------------------------
 
-template <int MODE, typename V>
+template <int MODE, typename V, bool K32>
 __global__ void __launch_bounds__(256)
 spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
             const V* __restrict__ Avals, const int32_t* __restrict__ Bpos,
@@ -211,22 +352,22 @@ spgemm_bin1(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
   for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nr;
        w += (gridDim.x * blockDim.x) >> 5) {
     const int row = rows[w];
-    // lane l takes product l: find its A nonzero by walking the row (<= 32 products)
-    uint64_t key = ~0ull;
-    V val = V();
-    int seq0 = 0;
-    for (int32_t q = __ldg(Apos + row); q < __ldg(Apos + row + 1); q++) {
-      const int32_t j = __ldg(Acrd + q);
-      const int32_t b0 = __ldg(Bpos + j), len = __ldg(Bpos + j + 1) - b0;
-      const int u = lane - seq0;
-      if (u >= 0 && u < len) {
-        key = esc_key(__ldg(Bcrd + b0 + u), lane);
-        if (mode_vals<MODE>()) val = mul_rn(Avals[q], Bvals[b0 + u]);
-      }
-      seq0 += len;
+    // lane l takes product l (<= 32 products)
+    uint64_t k1[1] = {~0ull};
+    V v1[1] = {V()};
+    const int P = warp_expand_regs<1, mode_vals<MODE>()>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals,
+                                                         row, k1, v1);
+    uint64_t key = k1[0];
+    V val = v1[0];
+    if constexpr (K32) {
+      uint32_t k32[1] = {narrow_key(key)};
+      warp_bitonic32(k32[0]);
+      if (mode_vals<MODE>()) gather_sorted_vals<1>(k32, v1);
+      key = wide_key(k32[0]);
+      val = v1[0];
+    } else {
+      warp_bitonic(key, val);
     }
-    warp_bitonic(key, val);
-    const int P = seq0;
     const uint64_t prevk = __shfl_up_sync(0xffffffffu, key, 1);
     const bool valid = lane < P;
     const bool head = valid && (lane == 0 || key_col(prevk) != key_col(key));
@@ -307,10 +448,10 @@ __device__ __forceinline__ void reg_bitonic(uint64_t (&key)[R], V (&val)[R]) {
   }
 }
 
-// Rows of at most 32*R products: each lane computes products lane, lane + 32, ... by walking
-// A's row (as bin 1 does), sorts them in registers, then leaves them in the warp's shared slice
-// for the run detection and emission of esc_emit_warp.
-template <int R, int MODE, typename V>
+// Rows of at most 32*R products: each lane computes products lane, lane + 32, ...
+// (warp_expand_regs), sorts them in registers, then leaves them in the warp's shared slice for
+// the run detection and emission of esc_emit_warp.
+template <int R, int MODE, bool K32, typename V>
 __device__ __forceinline__ void bin2_row_regs(const int32_t* __restrict__ Apos,
                                               const int32_t* __restrict__ Acrd,
                                               const V* __restrict__ Avals,
@@ -326,21 +467,18 @@ __device__ __forceinline__ void bin2_row_regs(const int32_t* __restrict__ Apos,
     key[r] = ~0ull;
     val[r] = V();
   }
-  int seq0 = 0;
-  for (int32_t q = __ldg(Apos + row); q < __ldg(Apos + row + 1); q++) {
-    const int32_t j = __ldg(Acrd + q);
-    const int32_t b0 = __ldg(Bpos + j), len = __ldg(Bpos + j + 1) - b0;
+  warp_expand_regs<R, mode_vals<MODE>()>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
+  if constexpr (K32) {
+    uint32_t k32[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-      const int u = r * 32 + lane - seq0;
-      if (u >= 0 && u < len) {
-        key[r] = esc_key(__ldg(Bcrd + b0 + u), r * 32 + lane);
-        if (mode_vals<MODE>()) val[r] = mul_rn(Avals[q], Bvals[b0 + u]);
-      }
-    }
-    seq0 += len;
+    for (int r = 0; r < R; r++) k32[r] = narrow_key(key[r]);
+    reg_bitonic32<R>(k32);
+    if (mode_vals<MODE>()) gather_sorted_vals<R>(k32, val);
+#pragma unroll
+    for (int r = 0; r < R; r++) key[r] = wide_key(k32[r]);
+  } else {
+    reg_bitonic<R, mode_vals<MODE>()>(key, val);
   }
-  reg_bitonic<R, mode_vals<MODE>()>(key, val);
 #pragma unroll
   for (int r = 0; r < R; r++) {
     skey[r * 32 + lane] = key[r];
@@ -349,7 +487,7 @@ __device__ __forceinline__ void bin2_row_regs(const int32_t* __restrict__ Apos,
   __syncwarp();
 }
 
-template <int MODE, typename V>
+template <int MODE, typename V, bool K32>
 __global__ void __launch_bounds__(256)
 spgemm_bin2(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
             const V* __restrict__ Avals, const int32_t* __restrict__ Bpos,
@@ -370,9 +508,9 @@ spgemm_bin2(const int32_t* __restrict__ Apos, const int32_t* __restrict__ Acrd,
     int cap = 32;
     while (cap < P) cap <<= 1;
     if (cap <= 64) {
-      bin2_row_regs<2, MODE>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
+      bin2_row_regs<2, MODE, K32>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
     } else if (cap <= 128) {
-      bin2_row_regs<4, MODE>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
+      bin2_row_regs<4, MODE, K32>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val);
     } else {
       esc_expand<mode_vals<MODE>()>(Apos, Acrd, Avals, Bpos, Bcrd, Bvals, row, key, val, lane,
                                     32);
@@ -660,16 +798,21 @@ int run_bins(const tacogb_csr* A, const tacogb_csr* B, const Plan& pl, const int
   const int sms = sm_count();
   auto rows_of = [&](int b) { return pl.bin_rows + (int64_t)b * n; };
   auto grid = [](int64_t items, int64_t cap) { return (unsigned)(items < cap ? items : cap); };
-  if (pl.h_cnt[1] > 0)
+  const bool k32 = B->cols <= kNarrowKeyCols;
+  if (pl.h_cnt[1] > 0) {
+    auto kern = k32 ? spgemm_bin1<MODE, V, true> : spgemm_bin1<MODE, V, false>;
     TACOGB_LAUNCH("spgemm_bin1", st,
-                  (spgemm_bin1<MODE, V><<<grid((pl.h_cnt[1] + 7) / 8, sms * 8), 256, 0, st>>>(
+                  (kern<<<grid((pl.h_cnt[1] + 7) / 8, sms * 8), 256, 0, st>>>(
                       A->pos, A->crd, Av, B->pos, B->crd, Bv, rows_of(1), pl.bin_cnt + 1, Cpos,
                       pl.cnt, Ccrd, Cvals)));
-  if (pl.h_cnt[2] > 0)
+  }
+  if (pl.h_cnt[2] > 0) {
+    auto kern = k32 ? spgemm_bin2<MODE, V, true> : spgemm_bin2<MODE, V, false>;
     TACOGB_LAUNCH("spgemm_bin2", st,
-                  (spgemm_bin2<MODE, V><<<grid((pl.h_cnt[2] + 7) / 8, sms * 4), 256, 0, st>>>(
+                  (kern<<<grid((pl.h_cnt[2] + 7) / 8, sms * 5), 256, 0, st>>>(
                       A->pos, A->crd, Av, B->pos, B->crd, Bv, rows_of(2), pl.bin_cnt + 2, pl.prod,
                       Cpos, pl.cnt, Ccrd, Cvals)));
+  }
   if (pl.h_cnt[3] > 0) {
     const size_t smem3 = (size_t)kBin3 * (sizeof(uint64_t) + sizeof(V));
     TACOGB_CUDA_TRY(cudaFuncSetAttribute(spgemm_bin3<MODE, V>,

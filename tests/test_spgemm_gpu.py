@@ -162,6 +162,66 @@ def _sort_path_matrix():
     return (apos, acrd, avals, len(blens)), (bpos, bcrd, bvals, K)
 
 
+def _long_a_rows_matrix():
+    """Rows of A with 33 to 100 entries whose B rows are mostly empty, so that the product
+    counts (1 to 128) fall in bins 1 and 2 while the expansion takes A's entries in several
+    chunks of 32 lanes; B rows of 0, 1 and 3 entries over 40 columns."""
+    rng = np.random.default_rng(31)
+    nb, K = 400, 40
+    blens = rng.choice([0, 0, 0, 1, 3], nb)
+    bpos = np.concatenate([[0], np.cumsum(blens)]).astype(np.int32)
+    bcrd = np.concatenate([np.sort(rng.choice(K, l, replace=False)) for l in blens]).astype(np.int32)
+    bvals = rng.uniform(-1, 1, len(bcrd))
+    arows = [np.sort(rng.choice(nb, int(rng.integers(33, 101)), replace=False)) for _ in range(300)]
+    apos = np.concatenate([[0], np.cumsum([len(r) for r in arows])]).astype(np.int32)
+    acrd = np.concatenate(arows).astype(np.int32)
+    avals = rng.uniform(-1, 1, len(acrd))
+    return (apos, acrd, avals, nb), (bpos, bcrd, bvals, K)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_long_a_rows_few_products(dtype):
+    A, B = _long_a_rows_matrix()
+    prods = [int(np.sum(np.diff(B[0])[A[1][A[0][i]:A[0][i + 1]]])) for i in range(len(A[0]) - 1)]
+    assert max(prods) <= 128 and min(np.diff(A[0])) > 32
+    ref = O.spgemm(A[0], A[1], A[2], B[0], B[1], B[2], B[3])
+    cp, cc, cv = gpu_spgemm(A, B, dtype)
+    assert np.array_equal(cp, ref[0]) and np.array_equal(cc, ref[1])
+    if dtype == torch.float64:
+        assert np.array_equal(cv, ref[2])
+    else:
+        assert normwise(cv, ref[2]) <= 1e-6
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_wide_column_keys(dtype):
+    """B with 2^24 + 7 columns: bins 1 and 2 sort (column, sequence) keys of 64 bits instead
+    of the narrow 32-bit keys; columns on both sides of 2^24 and repeated across B's rows."""
+    rng = np.random.default_rng(37)
+    K, nb = (1 << 24) + 7, 200
+    colset = np.concatenate([np.arange(K - 40, K), np.arange((1 << 24) - 40, 1 << 24),
+                             rng.choice(1 << 24, 40, replace=False)])
+    colset = np.unique(colset)
+    blens = rng.integers(0, 9, nb)
+    bpos = np.concatenate([[0], np.cumsum(blens)]).astype(np.int32)
+    bcrd = np.concatenate([np.sort(rng.choice(colset, l, replace=False)) for l in blens]).astype(np.int32)
+    bvals = rng.uniform(-1, 1, len(bcrd))
+    arows = [np.sort(rng.choice(nb, int(rng.integers(1, 25)), replace=False)) for _ in range(400)]
+    apos = np.concatenate([[0], np.cumsum([len(r) for r in arows])]).astype(np.int32)
+    acrd = np.concatenate(arows).astype(np.int32)
+    avals = rng.uniform(-1, 1, len(acrd))
+    A, B = (apos, acrd, avals, nb), (bpos, bcrd, bvals, K)
+    prods = [int(np.sum(blens[acrd[apos[i]:apos[i + 1]]])) for i in range(len(apos) - 1)]
+    assert min(prods) <= 32 < max(prods) <= 128 and bcrd.max() >= 1 << 24
+    ref = O.spgemm(A[0], A[1], A[2], B[0], B[1], B[2], B[3])
+    cp, cc, cv = gpu_spgemm(A, B, dtype)
+    assert np.array_equal(cp, ref[0]) and np.array_equal(cc, ref[1])
+    if dtype == torch.float64:
+        assert np.array_equal(cv, ref[2])
+    else:
+        assert normwise(cv, ref[2]) <= 1e-6
+
+
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_sort_path_boundaries(dtype):
     A, B = _sort_path_matrix()
