@@ -88,13 +88,11 @@ __device__ __forceinline__ void warp_bitonic(uint64_t& key, V& val) {
     for (int j = k >> 1; j > 0; j >>= 1) {
       const uint64_t ok = __shfl_xor_sync(0xffffffffu, key, j);
       const V ov = __shfl_xor_sync(0xffffffffu, val, j);
-      const bool up = (lane & k) == 0;
-      const bool lower = (lane & j) == 0;
-      const bool take = lower == up ? ok < key : ok > key;
-      if (take) {
-        key = ok;
-        val = ov;
-      }
+      // keys are distinct but for the empty slots', whose payloads are all zero
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      const bool take = (ok < key) == keep_min;
+      key = take ? ok : key;
+      val = take ? ov : val;
     }
   }
 }
@@ -107,9 +105,9 @@ __device__ __forceinline__ void warp_bitonic32(uint32_t& key) {
 #pragma unroll
     for (int j = k >> 1; j > 0; j >>= 1) {
       const uint32_t ok = __shfl_xor_sync(0xffffffffu, key, j);
-      const bool up = (lane & k) == 0;
-      const bool lower = (lane & j) == 0;
-      if (lower == up ? ok < key : ok > key) key = ok;
+      // the lower lane of an ascending pair (or the upper of a descending one) keeps the min
+      const bool keep_min = ((lane & j) == 0) == ((lane & k) == 0);
+      key = keep_min ? min(ok, key) : max(ok, key);
     }
   }
 }
@@ -126,20 +124,17 @@ __device__ __forceinline__ void reg_bitonic32(uint32_t (&key)[R]) {
 #pragma unroll
         for (int r = 0; r < R; r++) {
           if (r & jr) continue;
-          const bool up = ((r * 32 + lane) & k) == 0;
-          const uint32_t a = key[r], b = key[r | jr];
-          if ((a > b) == up) {
-            key[r] = b;
-            key[r | jr] = a;
-          }
+          const bool up = ((r * 32) & k) == 0;  // k >= 64 here: the lane's bits do not matter
+          const uint32_t lo = min(key[r], key[r | jr]), hi = max(key[r], key[r | jr]);
+          key[r] = up ? lo : hi;
+          key[r | jr] = up ? hi : lo;
         }
       } else {
 #pragma unroll
         for (int r = 0; r < R; r++) {
           const uint32_t ok = __shfl_xor_sync(0xffffffffu, key[r], j);
-          const bool up = ((r * 32 + lane) & k) == 0;
-          const bool lower = (lane & j) == 0;
-          if (lower == up ? ok < key[r] : ok > key[r]) key[r] = ok;
+          const bool keep_min = ((lane & j) == 0) == (((r * 32 + lane) & k) == 0);
+          key[r] = keep_min ? min(ok, key[r]) : max(ok, key[r]);
         }
       }
     }
@@ -415,33 +410,27 @@ __device__ __forceinline__ void reg_bitonic(uint64_t (&key)[R], V (&val)[R]) {
 #pragma unroll
         for (int r = 0; r < R; r++) {
           if (r & jr) continue;
-          const int e = r * 32 + lane;
-          const bool up = (e & k) == 0;
+          const bool up = ((r * 32) & k) == 0;  // k >= 64 here: the lane's bits do not matter
           const uint64_t a = key[r], b = key[r | jr];
-          if ((a > b) == up) {
-            key[r] = b;
-            key[r | jr] = a;
-            if (VALS) {
-              const V t = val[r];
-              val[r] = val[r | jr];
-              val[r | jr] = t;
-            }
+          const bool sw = (a > b) == up;
+          key[r] = sw ? b : a;
+          key[r | jr] = sw ? a : b;
+          if (VALS) {
+            const V va = val[r], vb = val[r | jr];
+            val[r] = sw ? vb : va;
+            val[r | jr] = sw ? va : vb;
           }
         }
       } else {
 #pragma unroll
         for (int r = 0; r < R; r++) {
-          const int e = r * 32 + lane;
           const uint64_t ok = __shfl_xor_sync(0xffffffffu, key[r], j);
           V ov = V();
           if (VALS) ov = __shfl_xor_sync(0xffffffffu, val[r], j);
-          const bool up = (e & k) == 0;
-          const bool lower = (lane & j) == 0;
-          const bool take = lower == up ? ok < key[r] : ok > key[r];
-          if (take) {
-            key[r] = ok;
-            if (VALS) val[r] = ov;
-          }
+          const bool keep_min = ((lane & j) == 0) == (((r * 32 + lane) & k) == 0);
+          const bool take = (ok < key[r]) == keep_min;
+          key[r] = take ? ok : key[r];
+          if (VALS) val[r] = take ? ov : val[r];
         }
       }
     }
