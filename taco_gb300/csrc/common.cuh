@@ -88,9 +88,10 @@ int* device_status();
 // address; the same address reads on the host under unified addressing).  Kernels publish
 // small results there with plain stores, so the host reads them after a stream synchronisation
 // without a device -> host copy queued behind large copies on the copy engines.
-// Words 0..59: published index checks (validate.cu); the last two: the SpMV longest-row and
-// locality counts.
-constexpr int kMailboxWords = 64;
+// Words 0..59: published index checks (validate.cu); 64..71: SpGEMM's bin sizes and totals;
+// the last two: the SpMV longest-row and locality counts.
+constexpr int kMailboxWords = 80;
+constexpr int kMailboxSpgemm = 64;
 constexpr int kMailboxLocality = kMailboxWords - 1;
 constexpr int kMailboxRowLen = kMailboxWords - 2;
 unsigned long long* host_mailbox();

@@ -691,17 +691,39 @@ __global__ void scan_block_sums(const int32_t* __restrict__ cnt, int32_t n,
   if (threadIdx.x == 0) sums[blockIdx.x] = s[0];
 }
 
+// Exclusive scan of the block sums by one warp, 32 at a time; sums[nblocks] = the total.
 __global__ void scan_sums_exclusive(int64_t* __restrict__ sums, int32_t nblocks,
                                     int32_t* __restrict__ total_overflow) {
-  if (threadIdx.x != 0) return;
-  int64_t acc = 0;
-  for (int b = 0; b < nblocks; b++) {
-    const int64_t v = sums[b];
-    sums[b] = acc;
-    acc += v;
+  const int lane = threadIdx.x & 31;
+  int64_t carry = 0;
+  for (int32_t b0 = 0; b0 < nblocks; b0 += 32) {
+    const int32_t b = b0 + lane;
+    const int64_t v = b < nblocks ? sums[b] : 0;
+    int64_t inc = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int64_t t = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += t;
+    }
+    if (b < nblocks) sums[b] = carry + inc - v;
+    carry += __shfl_sync(0xffffffffu, inc, 31);
   }
-  sums[nblocks] = acc;
-  *total_overflow = acc > INT32_MAX ? 1 : 0;
+  if (lane == 0) {
+    sums[nblocks] = carry;
+    *total_overflow = carry > INT32_MAX ? 1 : 0;
+  }
+}
+
+// Small results into the host mailbox from kMailboxSpgemm on: nb bin sizes, then a total and
+// an overflow flag (plain stores to mapped host memory).
+__global__ void spgemm_publish(const int32_t* __restrict__ bin_cnt, int nb,
+                               const int64_t* __restrict__ total, const int32_t* __restrict__ flag,
+                               volatile unsigned long long* box) {
+  const int t = threadIdx.x;
+  if (t < nb) box[t] = (unsigned long long)(uint32_t)bin_cnt[t];
+  if (t == nb && total) box[t] = (unsigned long long)*total;
+  if (t == nb + 1 && flag) box[t] = (unsigned long long)(uint32_t)*flag;
+  __threadfence_system();
 }
 
 __global__ void scan_write_pos(const int32_t* __restrict__ cnt, int32_t n,
@@ -747,8 +769,30 @@ struct Plan {
   int32_t h_cnt[kBins];
 };
 
-// Bins the rows of A*B and reads the bin sizes back (one small synchronising copy).
-int make_plan(const tacogb_csr* A, const tacogb_csr* B, Plan& pl, cudaStream_t st) {
+// The mailbox words SpGEMM publishes into, or null (the error is set).
+volatile unsigned long long* spgemm_box() {
+  unsigned long long* box = host_mailbox();
+  return box ? box + kMailboxSpgemm : nullptr;
+}
+
+// Publishes (nb bin sizes, total, flag) into the mailbox, waits for st, and reads them back.
+int publish_and_wait(const int32_t* bin_cnt, int nb, const int64_t* total, const int32_t* flag,
+                     int32_t* h_cnt, int64_t* h_total, bool* h_overflow, cudaStream_t st) {
+  volatile unsigned long long* box = spgemm_box();
+  if (!box) return last_code();
+  TACOGB_LAUNCH("spgemm_publish", st,
+                spgemm_publish<<<1, 32, 0, st>>>(bin_cnt, nb, total, flag,
+                                                 (unsigned long long*)box));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int b = 0; b < nb; b++) h_cnt[b] = (int32_t)box[b];
+  if (h_total) *h_total = (int64_t)box[nb];
+  if (h_overflow) *h_overflow = box[nb + 1] != 0;
+  return 0;
+}
+
+// Bins the rows of A*B; with `wait`, reads the bin sizes back (one synchronisation).
+int make_plan(const tacogb_csr* A, const tacogb_csr* B, Plan& pl, cudaStream_t st,
+              bool wait = true) {
   const int64_t n = A->rows;
   const int64_t nblocks = (n + kScanChunk - 1) / kScanChunk;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -773,9 +817,8 @@ int make_plan(const tacogb_csr* A, const tacogb_csr* B, Plan& pl, cudaStream_t s
     TACOGB_LAUNCH("spgemm_bin_rows", st,
                   spgemm_bin_rows<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
                       A->pos, A->crd, B->pos, (int32_t)n, pl.prod, pl.bin_cnt, pl.bin_rows));
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(pl.h_cnt, pl.bin_cnt, sizeof(pl.h_cnt), cudaMemcpyDeviceToHost, st));
-  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
-  return 0;
+  if (!wait) return 0;
+  return publish_and_wait(pl.bin_cnt, kBins, nullptr, nullptr, pl.h_cnt, nullptr, nullptr, st);
 }
 
 template <int MODE, typename V>
@@ -864,22 +907,27 @@ __global__ void spgemm_compact(const int32_t* __restrict__ off, const int32_t* _
 
 // Exclusive scan of cnt[0..n) into pos[0..n] (pos[n] = total); *total and the overflow flag
 // are read back (synchronises).
-int scan_counts(const int32_t* cnt, int64_t n, int64_t* sums, int32_t* flag, int32_t* pos,
-                int64_t* total, bool* overflow, cudaStream_t st) {
+// Exclusive scan of cnt[0, n) into pos[0, n] (pos[n] = the total) on st, without waiting; the
+// total is left at sums[nblocks] and its int32 overflow flag at *flag.
+int scan_counts_launch(const int32_t* cnt, int64_t n, int64_t* sums, int32_t* flag, int32_t* pos,
+                       cudaStream_t st, int64_t* nblocks_out) {
   const int64_t nblocks = (n + kScanChunk - 1) / kScanChunk;
+  *nblocks_out = nblocks;
   TACOGB_LAUNCH("spgemm_scan_sums", st,
                 scan_block_sums<<<(unsigned)nblocks, 256, 0, st>>>(cnt, (int32_t)n, sums));
   TACOGB_LAUNCH("spgemm_scan_top", st,
                 scan_sums_exclusive<<<1, 32, 0, st>>>(sums, (int32_t)nblocks, flag));
   TACOGB_LAUNCH("spgemm_scan_pos", st,
                 scan_write_pos<<<(unsigned)nblocks, 256, 0, st>>>(cnt, (int32_t)n, sums, pos));
-  int32_t f = 0;
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(total, sums + nblocks, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                  st));
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(&f, flag, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
-  *overflow = f != 0;
   return 0;
+}
+
+// The same, then waits and reads the total and the overflow flag.
+int scan_counts(const int32_t* cnt, int64_t n, int64_t* sums, int32_t* flag, int32_t* pos,
+                int64_t* total, bool* overflow, cudaStream_t st) {
+  int64_t nblocks = 0;
+  if (int rc = scan_counts_launch(cnt, n, sums, flag, pos, st, &nblocks)) return rc;
+  return publish_and_wait(nullptr, 0, sums + nblocks, flag, nullptr, total, overflow, st);
 }
 
 // State of the last one-pass product on this device, between spgemm_onepass and
@@ -967,8 +1015,8 @@ int spgemm_onepass(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int6
     return 0;
   }
   Plan pl;
-  if (int rc = make_plan(A, B, pl, st)) return rc;
-  // slot offsets: exclusive scan of the product counts
+  if (int rc = make_plan(A, B, pl, st, false)) return rc;
+  // slot offsets: exclusive scan of the product counts, read back with the bin sizes (one wait)
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t vb = A->vtype == TACOGB_F64 ? 8 : 4;
   const size_t head = 2 * al(sizeof(int32_t) * (n + 1));
@@ -979,9 +1027,12 @@ int spgemm_onepass(const tacogb_csr* A, const tacogb_csr* B, int32_t* Cpos, int6
   TACOGB_LAUNCH("spgemm_prod32", st,
                 spgemm_prod32<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pl.prod, (int32_t)n,
                                                                             p32));
-  int64_t products = 0;
+  int64_t products = 0, nblocks = 0;
   bool overflow = false;
-  if (int rc = scan_counts(p32, n, pl.sums, pl.flag, off, &products, &overflow, st)) return rc;
+  if (int rc = scan_counts_launch(p32, n, pl.sums, pl.flag, off, st, &nblocks)) return rc;
+  if (int rc = publish_and_wait(pl.bin_cnt, kBins, pl.sums + nblocks, pl.flag, pl.h_cnt,
+                                &products, &overflow, st))
+    return rc;
   TACOGB_CHECK_ARG(!overflow, "SpGEMM: %lld products exceed the one-pass slots' int32 offsets; "
                    "use the symbolic/fill/numeric phases", (long long)products);
   // the slots, in a scratch slot of their own (growing it leaves the offsets alone)
