@@ -1470,7 +1470,9 @@ def main():
         # the kernel from above (exact when the step is that one launch)
         dom_ms = min(dom_ms, ms / args.steps)
     if op.pattern == "spgemm":  # the bytes model covers all three phases of a step
-        dom, dom_ms = "spgemm symbolic + fill + numeric (%s largest)" % dom, ms / args.steps
+        what = ("symbolic + fill + numeric" if args.variant == 1 else
+                "one pass: binning, sort into product slots, scans, compaction")
+        dom, dom_ms = "spgemm %s (%s largest)" % (what, dom), ms / args.steps
     peak, peak_kind = measured_peak()
     achieved = getattr(op, "roofline_bytes", op.bytes) / (dom_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
