@@ -10,9 +10,13 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <initializer_list>
 #include <mutex>
+#include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -359,6 +363,75 @@ int read_i32(const int32_t* p, int32_t* out) {
 // Allocation for a result array, with the allocator taco releases it with
 // (src/storage/array.cpp:22-33): cudaMallocManaged when the operands are GPU memory (taco's
 // CUDA build), malloc otherwise.
+// Device -> host copies into fresh host allocations (the malloc'd results taco frees).  A copy
+// into pages the OS has not mapped yet pays a fault and the page's zeroing per page inside the
+// copy: 200 MB took 8.5-12.7 ms that way on the GB300 machine's host, against 1.4 ms into mapped
+// pageable or pinned memory, while eight threads map 134 MB in about 1.2 ms.  So for large
+// results, host threads map the pages chunk by chunk (one write per page, inside the buffer
+// only) and each chunk's copy is issued on st as soon as its pages are mapped: the mapping of
+// later chunks overlaps the copies of earlier ones.  Small results are copied directly (the
+// threads would cost more than the faults).
+struct HostCopy {
+  void* dst;
+  const void* src;
+  size_t bytes;
+};
+
+int copy_to_fresh_host(std::initializer_list<HostCopy> copies, cudaStream_t st) {
+  constexpr size_t kPipelineBytes = (size_t)64 << 20, kChunk = (size_t)16 << 20;
+  size_t total = 0;
+  bool pinned = false;  // page-locked destinations are mapped already
+  for (const HostCopy& c : copies) {
+    total += c.bytes;
+    cudaPointerAttributes at;
+    if (c.bytes && cudaPointerGetAttributes(&at, c.dst) == cudaSuccess)
+      pinned = pinned || at.type == cudaMemoryTypeHost;
+    else
+      cudaGetLastError();
+  }
+  if (total < kPipelineBytes || pinned) {
+    for (const HostCopy& c : copies)
+      if (c.bytes)
+        TACOGB_CUDA_TRY(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, st));
+    return 0;
+  }
+  // the chunks of every copy, in order
+  std::vector<HostCopy> chunks;
+  for (const HostCopy& c : copies)
+    for (size_t o = 0; o < c.bytes; o += kChunk)
+      chunks.push_back({(unsigned char*)c.dst + o, (const unsigned char*)c.src + o,
+                        std::min(kChunk, c.bytes - o)});
+  const long pg = sysconf(_SC_PAGESIZE);
+  const size_t page = pg > 0 ? (size_t)pg : 4096;
+  const int nt = (int)std::min(8u, std::max(1u, std::thread::hardware_concurrency()));
+  std::vector<std::atomic<int>> done(chunks.size());
+  for (auto& d : done) d.store(0, std::memory_order_relaxed);
+  auto worker = [&](int t) {
+    for (size_t k = 0; k < chunks.size(); k++) {
+      const HostCopy& c = chunks[k];
+      const size_t a = c.bytes * t / nt, b = c.bytes * (t + 1) / nt;
+      volatile unsigned char* p = (volatile unsigned char*)c.dst;
+      for (size_t o = a; o < b; o = (o / page + 1) * page) p[o] = 0;
+      done[k].fetch_add(1, std::memory_order_release);
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; t++) th.emplace_back(worker, t);
+  cudaError_t err = cudaSuccess;
+  for (size_t k = 0; k < chunks.size(); k++) {
+    while (done[k].load(std::memory_order_acquire) < nt) std::this_thread::yield();
+    if (err == cudaSuccess)
+      err = cudaMemcpyAsync(chunks[k].dst, chunks[k].src, chunks[k].bytes, cudaMemcpyDeviceToHost,
+                            st);
+  }
+  for (auto& x : th) x.join();
+  if (err != cudaSuccess) {
+    set_error(TACOGB_ERR_CUDA, "copy to host: %s", cudaGetErrorString(err));
+    return TACOGB_ERR_CUDA;
+  }
+  return 0;
+}
+
 void* alloc_result(size_t bytes, bool managed) {
   if (bytes == 0) bytes = 1;
   if (managed) {
@@ -366,6 +439,15 @@ void* alloc_result(size_t bytes, bool managed) {
     if (cudaMallocManaged(&p, bytes) != cudaSuccess) {
       set_error(TACOGB_ERR_ALLOC, "cudaMallocManaged(%zu) failed", bytes);
       return nullptr;
+    }
+    // the kernels write it first: populate it on this GPU in bulk rather than page by page
+    // under the kernels' stores (0.2 GB of SpGEMM results: 6.2 ms of faults otherwise)
+    int dev = 0;
+    if (bytes >= ((size_t)1 << 20) && cudaGetDevice(&dev) == cudaSuccess) {
+      cudaMemLocation loc{};
+      loc.type = cudaMemLocationTypeDevice;
+      loc.id = dev;
+      if (cudaMemPrefetchAsync(p, bytes, loc, 0, lib_stream()) != cudaSuccess) cudaGetLastError();
     }
     return p;
   }
@@ -1256,7 +1338,7 @@ int tacogb_spgemm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) 
   }
   if (int rc = spgemm_numeric(&a, &b, c.pos, c.crd, dvals, st)) return rc;
   if (staged && vbytes)
-    TACOGB_CUDA_TRY(cudaMemcpyAsync(C->vals, dvals, vbytes, cudaMemcpyDeviceToHost, st));
+    if (int rc = copy_to_fresh_host({{C->vals, dvals, vbytes}}, st)) return rc;
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
   return consume_device_status();
 }
@@ -1284,10 +1366,10 @@ int tacogb_spgemm_evaluate(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B)
   if (!dcrd || !dvals) return TACOGB_ERR_ALLOC;
   if (int rc = spgemm_onepass_finish(dpos, dcrd, dvals, st)) return rc;
   TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, dpos, ((size_t)rows + 1) * 4, cudaMemcpyDefault, st));
-  if (!managed && nnz) {
-    TACOGB_CUDA_TRY(cudaMemcpyAsync(crd, dcrd, (size_t)nnz * 4, cudaMemcpyDeviceToHost, st));
-    TACOGB_CUDA_TRY(cudaMemcpyAsync(vals, dvals, (size_t)nnz * vb, cudaMemcpyDeviceToHost, st));
-  }
+  if (!managed && nnz)
+    if (int rc = copy_to_fresh_host({{crd, dcrd, (size_t)nnz * 4}, {vals, dvals, (size_t)nnz * vb}},
+                                    st))
+      return rc;
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
   C->indices[1][0] = (uint8_t*)pos;
   C->indices[1][1] = (uint8_t*)crd;
@@ -1344,9 +1426,13 @@ int tacogb_pack_taco(taco_tensor_t* T, const void* buffer, int64_t n) {
   void* vals = alloc_result((size_t)nnz * vb, managed);
   if (!pos || !crd || !vals) return TACOGB_ERR_ALLOC;
   TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, dpos, ((size_t)rows + 1) * 4, cudaMemcpyDefault, st));
-  if (nnz) {
+  if (nnz && managed) {
     TACOGB_CUDA_TRY(cudaMemcpyAsync(crd, dcrd, (size_t)nnz * 4, cudaMemcpyDefault, st));
     TACOGB_CUDA_TRY(cudaMemcpyAsync(vals, dvals, (size_t)nnz * vb, cudaMemcpyDefault, st));
+  } else if (nnz) {
+    if (int rc = copy_to_fresh_host({{crd, dcrd, (size_t)nnz * 4}, {vals, dvals, (size_t)nnz * vb}},
+                                    st))
+      return rc;
   }
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
   T->indices[1][0] = (uint8_t*)pos;
