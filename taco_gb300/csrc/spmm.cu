@@ -37,8 +37,17 @@ namespace tacogb {
 
 // B64: B as FP64 for the native redo of checked policies (the same array as B unless B was
 // pre-split); bflag (optional): non-zero when B has entries outside the double-float range.
+// CTAs per SM the merge kernel is compiled for: four (64 registers) except the compensated FP32
+// tile four columns wide, which spills there.  Measured against three: FP64 N=64 3.36 -> 3.29
+// ms, BF16 N=64 1.88 -> 1.58 ms, MTTKRP's fiber SpMM 4.01 -> 3.59 ms; FP32 N=256 7.67 -> 8.82
+// ms with four, hence three for that tile.
+template <class P, int VEC>
+constexpr int mm_min_blocks() {
+  return (std::is_same<P, MmComp32>::value && VEC == 4) ? 3 : 4;
+}
+
 template <class P, int VEC, bool STREAM>
-__global__ void __launch_bounds__(kMmBlock, 3)
+__global__ void __launch_bounds__(kMmBlock, mm_min_blocks<P, VEC>())
 spmm_merge_kernel(const int32_t* __restrict__ pos, const int32_t* __restrict__ crd,
                   const typename P::AV* __restrict__ vals, const typename P::BV* __restrict__ B,
                   const double* __restrict__ B64, const int* __restrict__ bflag,
