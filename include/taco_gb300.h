@@ -29,6 +29,13 @@
  * Errors: every function returns 0 on success and a TACOGB_ERR_* code otherwise; the message
  * is available from tacogb_last_error().  Generated taco CUDA exits the process on a CUDA
  * error (src/codegen/codegen_cuda.cpp:58-67); this library never does.
+ *
+ * Threads: the library keeps per-device state (scratch and staging buffers, a small mapped
+ * host mailbox for kernel results, the taco ABI's streams, the last one-pass SpGEMM between
+ * tacogb_spgemm_onepass and _finish).  Calls for one device must not overlap in time from
+ * different host threads — serialise them, as taco's single-threaded compute() does; calls on
+ * different devices may run at the same time.  Device-layer calls on one caller stream are
+ * ordered by that stream like any other work on it.
  */
 #ifndef TACO_GB300_H
 #define TACO_GB300_H
