@@ -536,32 +536,20 @@ __global__ void spmv_carry_fixup(const int32_t* __restrict__ carry_row,
   const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t == 0 && xflag != nullptr) *xflag = 0;
   if (t >= tiles) return;
-  // every load the common case needs is issued before any of them is tested
+  // every load the common case needs is issued before any of them is tested: a run of equal
+  // carry rows almost always ends at the next tile (only rows longer than a tile span more),
+  // so one tile of lookahead, and a loop for the rest
   const int32_t r = carry_row[t];
   const int32_t rp = t > 0 ? carry_row[t - 1] : -1;
   double tot = carry_val[t];
-  int32_t rr[8];
-  double vv[8];
-#pragma unroll
-  for (int j = 0; j < 8; j++) {
-    rr[j] = (t + 1 + j < tiles) ? carry_row[t + 1 + j] : -1;
-    vv[j] = (t + 1 + j < tiles) ? carry_val[t + 1 + j] : 0.0;
-  }
+  int32_t u = t + 1;
+  int32_t ru = u < tiles ? carry_row[u] : -1;
   if (r >= n || rp == r) return;
   const Out y0 = y[r];
-  for (int32_t u = t + 1;; u += 8) {
-    bool more = true;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      more = more && rr[j] == r;
-      if (more) tot += vv[j];
-    }
-    if (!more) break;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      rr[j] = (u + 8 + j < tiles) ? carry_row[u + 8 + j] : -1;
-      vv[j] = (u + 8 + j < tiles) ? carry_val[u + 8 + j] : 0.0;
-    }
+  while (ru == r) {
+    tot += carry_val[u];
+    u++;
+    ru = u < tiles ? carry_row[u] : -1;
   }
   y[r] = (Out)((double)y0 + tot);
 }
