@@ -441,6 +441,7 @@ class SpgemmOp:
         self.args = args
         s = self.spec = W.spgemm_random() if args.workload == "spgemm_random" else W.spgemm_poisson()
         self.pos, self.crd, self.vals = W.generate(s)
+        self.phase_s = {}
         self.rows, self.cols, self.nnz = s.rows, s.cols, len(self.crd)
         lens = np.diff(self.pos).astype(np.int64)
         self.products = int(lens[self.crd].sum())  # sum over A's nonzeros of B's row lengths
@@ -507,7 +508,8 @@ class SpgemmOp:
 
     def _taco_step(self, pattern):
         """One assemble + compute of taco's generated code for `pattern` (a callable that
-        returns nnz(C) and frees C's arrays)."""
+        returns nnz(C) and frees C's arrays); each call's assemble and compute times are
+        appended to self.phase_s[pattern]."""
         import ctypes.util
         from oracle import oracle as O
         from taco_gb300 import taco as T
@@ -515,16 +517,30 @@ class SpgemmOp:
         libc.free.argtypes = [ctypes.c_void_p]
         At = T.csr(self.pos, self.crd, self.vals, [self.rows, self.cols])
         L = O.ref_lib(pattern)
+        times = self.phase_s.setdefault(pattern, {"assemble": [], "compute": []})
 
         def once():
             Ct = T.csr_result([self.rows, self.cols])
+            t0 = time.perf_counter()
             L.assemble(Ct.ptr, At.ptr, At.ptr)
+            t1 = time.perf_counter()
             L.compute(Ct.ptr, At.ptr, At.ptr)
+            t2 = time.perf_counter()
+            times["assemble"].append(t1 - t0)
+            times["compute"].append(t2 - t1)
             nnzC = ctypes.cast(Ct.index(1, 0), ctypes.POINTER(ctypes.c_int32))[self.rows]
             for q in (Ct.index(1, 0), Ct.index(1, 1), Ct.vals_ptr):
                 libc.free(q)
             return nnzC
         return once, At
+
+    def phase_ms(self, pattern):
+        """Medians (ms) of taco's assemble and compute over the timed calls of `pattern`."""
+        t = self.phase_s.get(pattern)
+        if not t or not t["assemble"]:
+            return {}
+        return {"assemble_ms": float(np.median(t["assemble"])) * 1e3,
+                "compute_ms": float(np.median(t["compute"])) * 1e3}
 
     def cpu_serial(self):
         """taco's default (serial) generated SpGEMM, timed beside the scheduled one."""
@@ -547,6 +563,7 @@ class SpgemmOp:
             self.set_nnzC(int(once()))
             self.cpu_sample_desc = ("whole workload, taco's scheduleSpGEMMCPU (parallel two-pass "
                                     "assembly, dense workspace) on all threads")
+            self.cpu_phases = "spgemm_sched"
             return "reference", once, (At,)
         if O.ref_available("spgemm"):
             L = O.ref_lib("spgemm")
@@ -1049,6 +1066,8 @@ def run_reference(args):
            "cpu_baseline": {"value": v, "unit": unit, "cores": ncores, "kind": kind,
                             "sample": sample, "code": code, "work_per_step": work},
            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if getattr(op, "cpu_phases", None):
+        out["cpu_baseline"].update(op.phase_ms(op.cpu_phases))  # assemble, compute separately
     if op.pattern != "batch":
         out["gflops"] = getattr(op, "cpu_work" if op.pattern == "sddmm" else "flops",
                                 op.flops) * steps / dt / 1e9
@@ -1512,6 +1531,8 @@ def main():
                "sample": "%s, median of %d reps" % (getattr(op, "cpu_sample_desc",
                                                             "whole workload"), reps),
                "ms_per_step": t * 1e3}
+        if getattr(op, "cpu_phases", None):
+            cpu.update(op.phase_ms(op.cpu_phases))  # taco's assemble and compute, separately
         serial = op.cpu_serial() if hasattr(op, "cpu_serial") else None
         if serial is not None:
             once, keep_s = serial
@@ -1524,6 +1545,7 @@ def main():
             cpu["serial"] = {"value": cpu_work / float(np.median(ts)) / 1e9, "unit": unit,
                              "cores": 1, "ms_per_step": float(np.median(ts)) * 1e3,
                              "code": "taco's default generated SpGEMM (serial)"}
+            cpu["serial"].update(op.phase_ms("spgemm"))
             del keep_s
 
     if rank == 0:
