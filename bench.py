@@ -18,7 +18,8 @@ Default workload (the headline): FP64 CSR SpMV y(i) = A(i,j) * x(j) on the 4,194
          flags, OpenMP over all host cores), or the C restatement when that is absent
 
 `--impl reference` times taco's generated CPU code alone (rank 0) and prints its line.
-Every working set is larger than L2 (129 MB): no flush between steps.
+Every working set but the 65,536-row SpMV's (labelled L2-resident) is larger than L2 (129 MB):
+no flush between steps.
 """
 import argparse
 import ctypes
@@ -29,7 +30,13 @@ import sys
 import tempfile
 import time
 
-import numpy as np
+# OpenMP placement for the CPU legs (taco's generated code runs OpenMP over all host cores),
+# set before anything loads the OpenMP runtime, which reads it once; the schedule is set to
+# static per call, as taco's module does.  A value already in the environment wins.
+os.environ.setdefault("OMP_PROC_BIND", "close")
+os.environ.setdefault("OMP_PLACES", "cores")
+
+import numpy as np  # noqa: E402
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -965,6 +972,30 @@ class ClockSampler:
 
 # ----------------------------------------------------------------------------- CPU legs
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), or None."""
+    try:
+        r = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                           text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return None
+
+
+def omp_setup():
+    return "OMP_PROC_BIND=%s OMP_PLACES=%s, static schedule" % (
+        os.environ.get("OMP_PROC_BIND"), os.environ.get("OMP_PLACES"))
+
+
 def time_cpu(op, budget_s=8.0, reps=None):
     """Median seconds of one step of taco's generated code (or the port) on all host cores."""
     from oracle import oracle as O
@@ -1064,7 +1095,8 @@ def run_reference(args):
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": workload_config(op, world),
            "cpu_baseline": {"value": v, "unit": unit, "cores": ncores, "kind": kind,
-                            "sample": sample, "code": code, "work_per_step": work},
+                            "sample": sample, "code": code, "work_per_step": work,
+                            "cpu_model": cpu_model(), "omp": omp_setup()},
            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if getattr(op, "cpu_phases", None):
         out["cpu_baseline"].update(op.phase_ms(op.cpu_phases))  # assemble, compute separately
@@ -1530,7 +1562,7 @@ def main():
                "cores": 1 if op.pattern == "pack" else cores, "kind": kind,
                "sample": "%s, median of %d reps" % (getattr(op, "cpu_sample_desc",
                                                             "whole workload"), reps),
-               "ms_per_step": t * 1e3}
+               "ms_per_step": t * 1e3, "cpu_model": cpu_model(), "omp": omp_setup()}
         if getattr(op, "cpu_phases", None):
             cpu.update(op.phase_ms(op.cpu_phases))  # taco's assemble and compute, separately
         serial = op.cpu_serial() if hasattr(op, "cpu_serial") else None
