@@ -914,11 +914,6 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   static_assert(kPipeChunks <= kMaxPublishedChecks, "one published check per chunk");
   const bool check = validation_on();
   TACOGB_CHECK_ARG(cols > 0 || nnz == 0, "%s: %d nonzeros in a matrix of 0 columns", what, nnz);
-  unsigned long long* cnt = nullptr;
-  if (check) {
-    cnt = (unsigned long long*)scratch(5 * sizeof(unsigned long long) * kPipeChunks, 11);
-    if (!cnt) return last_code();
-  }
   int64_t meta[3 * kPipeChunks], coff[kPipeChunks + 1], voff[kPipeChunks + 1];
   int64_t poff = 0, c = 0, v = 0;
   for (int j = 0; j < K; j++) {
@@ -975,8 +970,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     if (check) {
       // a chunk that fails its check is made harmless before its product runs; the verdicts
       // are read once every chunk is done
-      rc = level_check_enqueue(nr, cols, cpos, ccrd, n, cnt + 5 * j, st);
-      if (rc == 0) rc = level_gate_enqueue(nr, cpos, ccrd, n, cnt + 5 * j, st);
+      rc = level_check_enqueue(nr, cols, cpos, ccrd, n, j, true, st);
       if (rc) break;
     }
     rc = prod.run(&cj, ddense, dres + (size_t)rb[j] * res_row_bytes, N, btype, st);
@@ -988,7 +982,6 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
                                       dres + (size_t)rb[j] * res_row_bytes,
                                       (size_t)nr * res_row_bytes, cudaMemcpyDeviceToHost, d2h));
   }
-  if (check && rc == 0) rc = level_checks_publish(cnt, K, st);
   // nothing may still be copying when the call returns, whatever happened
   const cudaError_t e1 = cudaStreamSynchronize(h2d), e2 = cudaStreamSynchronize(st),
                     e3 = cudaStreamSynchronize(d2h);
@@ -1050,7 +1043,8 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
                            0, st, opos, ocrd, &ovals, chk))
     return rc;
   if (int rc = stage_in(ox, x->vals, (size_t)cols * vb, 3, st)) return rc;
-  if (int rc = chk.finish(st, opos.dev, ocrd.dev)) return rc;
+  // staged copies are checked without a wait (a failing one is made harmless on the device)
+  if (int rc = chk.finish_deferred(st, opos.dev, ocrd.dev, opos.staged && ocrd.staged)) return rc;
   void* ydev = y->vals;
   const bool y_staged = !device_accessible(y->vals);
   if (y_staged) {
@@ -1062,6 +1056,7 @@ int tacogb_spmv_compute(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   if (y_staged && rows)
     TACOGB_CUDA_TRY(cudaMemcpyAsync(y->vals, ydev, (size_t)rows * vb, cudaMemcpyDeviceToHost, st));
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (int rc = chk.verdict()) return rc;
   return consume_device_status();
 }
 
@@ -1168,7 +1163,8 @@ int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
                            (size_t)nnz * value_bytes(at), 0, st, opos, ocrd, &ovals, chk))
     return rc;
   if (int rc = stage_in(ob, B->vals, (size_t)cols * N * value_bytes(bt), 3, st)) return rc;
-  if (int rc = chk.finish(st, opos.dev, ocrd.dev)) return rc;
+  // staged copies are checked without a wait (a failing one is made harmless on the device)
+  if (int rc = chk.finish_deferred(st, opos.dev, ocrd.dev, opos.staged && ocrd.staged)) return rc;
   const size_t cbytes = (size_t)rows * N * value_bytes(ct);
   void* cdev = C->vals;
   const bool c_staged = !device_accessible(C->vals);
@@ -1181,6 +1177,7 @@ int tacogb_spmm_compute(taco_tensor_t* C, taco_tensor_t* A, taco_tensor_t* B) {
   if (c_staged && cbytes)
     TACOGB_CUDA_TRY(cudaMemcpyAsync(C->vals, cdev, cbytes, cudaMemcpyDeviceToHost, st));
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  if (int rc = chk.verdict()) return rc;
   return consume_device_status();
 }
 

@@ -12,10 +12,10 @@
 // The check runs on the GPU, on the arrays the kernels will read (the caller's device or managed
 // arrays, or the staged copies of host arrays): one streaming kernel that reads pos and crd
 // once, in bounds (crd at [0, nnz) only, pos at [0, outer]), then one synchronisation to read
-// the verdict before any gathering kernel is launched.  The counters are set and read by
-// kernels (the verdict is published into mapped host memory), so a check issues no copies: in
-// the pipelined products it runs between large copies in flight on the copy engines and does
-// not queue behind them.  When a call cannot reach a GPU at all,
+// the verdict before any gathering kernel is launched.  A check is one launch that also
+// publishes its verdict into mapped host memory, so it issues no copies: in the pipelined
+// products it runs between large copies in flight on the copy engines and does not queue
+// behind them.  When a call cannot reach a GPU at all,
 // host-resident levels are checked on the host instead, so that invalid input is still reported
 // as TACOGB_ERR_ARG rather than as the missing device; tacogb_validate_level_host exposes that
 // host check (multi-threaded for large levels).
@@ -27,6 +27,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -153,44 +154,31 @@ int host_check(const char* what, int64_t outer, int32_t inner, const int32_t* po
   return 0;
 }
 
-// Counters of one check: [0] bits, [1] first bad segment, [2] first bad position, [3] descents,
-// [4] descents at the starts of non-empty segments.
-__global__ void level_check_init(unsigned long long* __restrict__ out) {
-  if (threadIdx.x < 5) out[threadIdx.x] = (threadIdx.x == 1 || threadIdx.x == 2) ? ~0ull : 0ull;
-}
+// Running totals of one check: bits, first bad segment, first bad position, descents, descents
+// at the starts of non-empty segments, and the count of blocks done.  Initialised once per
+// device; the last block of every check puts them back.
+struct CheckState {
+  unsigned long long bits, bad_seg, bad_p, desc, desc_start;
+  unsigned int done;
+};
+constexpr CheckState kCheckInit{0, ~0ull, ~0ull, 0, 0, 0u};
 
-// `count` sets of counters into the host mailbox (plain stores to mapped host memory).
-__global__ void level_check_publish(const unsigned long long* __restrict__ out, int count,
-                                    volatile unsigned long long* box) {
-  for (int i = threadIdx.x; i < 5 * count; i += blockDim.x) box[i] = out[i];
-  __threadfence_system();
-}
-
-// A level whose counters show a violation becomes pos = 0, ..., 0, nnz and crd = 0.
-__global__ void level_gate_kernel(int64_t outer, int32_t* __restrict__ pos,
-                                  int32_t* __restrict__ crd, int64_t nnz,
-                                  const unsigned long long* __restrict__ out) {
-  if (out[0] == 0 && out[3] == out[4]) return;
-  const int64_t n = std::max(outer + 1, nnz);
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-    if (k <= outer) pos[k] = k == outer ? (int32_t)nnz : 0;
-    if (k < nnz && crd) crd[k] = 0;
-  }
-}
-
-// Device check into the counters (set by level_check_init before the launch).
-__global__ void level_check_kernel(int64_t outer, int32_t inner, const int32_t* __restrict__ pos,
-                                   const int32_t* __restrict__ crd, int64_t nnz,
-                                   unsigned long long* __restrict__ out) {
+// One check of a level in one launch.  Every block folds its part into the totals (one atomic
+// per warp and total); the last block to finish publishes the totals into the host mailbox
+// (box[0..4], plain stores to mapped host memory), rewrites the level into a harmless one when
+// `gate` is set and the totals show a violation (pos = 0, ..., 0, nnz; crd = 0), and restores
+// the totals for the next check.  Plain loads: the last block may write what all blocks read.
+__global__ void level_check_fused(int64_t outer, int32_t inner, int32_t* pos, int32_t* crd,
+                                  int64_t nnz, CheckState* cs, volatile unsigned long long* box,
+                                  int gate) {
   unsigned bits = 0;
   unsigned long long bad_seg = ~0ull, bad_p = ~0ull, desc = 0, desc_start = 0;
-  const int64_t n = std::max(outer, nnz);
+  const int64_t n = std::max<int64_t>(std::max(outer, nnz), 1);  // thread 0 reads pos[0]
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-    if (k == 0 && __ldg(pos) != 0) bits |= kBadPos0;
+    if (k == 0 && pos[0] != 0) bits |= kBadPos0;
     if (k < outer) {
-      const int64_t a = __ldg(pos + k), b = __ldg(pos + k + 1);
+      const int64_t a = pos[k], b = pos[k + 1];
       if (b < a) {
         bits |= kBadPosOrder;
         bad_seg = min(bad_seg, (unsigned long long)k);
@@ -198,19 +186,18 @@ __global__ void level_check_kernel(int64_t outer, int32_t inner, const int32_t* 
         bits |= kBadPosEnd;
         bad_seg = min(bad_seg, (unsigned long long)k);
       } else if (crd && a < b && a > 0) {
-        desc_start += __ldg(crd + a) <= __ldg(crd + a - 1);
+        desc_start += crd[a] <= crd[a - 1];
       }
     }
     if (k < nnz && crd) {
-      const int32_t c = __ldg(crd + k);
+      const int32_t c = crd[k];
       if (c < 0 || c >= inner) {
         bits |= kBadCrdRange;
         bad_p = min(bad_p, (unsigned long long)k);
       }
-      if (k > 0) desc += c <= __ldg(crd + k - 1);
+      if (k > 0) desc += c <= crd[k - 1];
     }
   }
-  // one atomic per warp and counter
   const unsigned lane = threadIdx.x & 31;
   bits = __reduce_or_sync(0xffffffffu, bits);
   for (int o = 16; o; o >>= 1) {
@@ -220,49 +207,94 @@ __global__ void level_check_kernel(int64_t outer, int32_t inner, const int32_t* 
     desc_start += __shfl_xor_sync(0xffffffffu, desc_start, o);
   }
   if (lane == 0) {
-    if (bits) atomicOr(out, (unsigned long long)bits);
-    if (bad_seg != ~0ull) atomicMin(out + 1, bad_seg);
-    if (bad_p != ~0ull) atomicMin(out + 2, bad_p);
-    if (desc) atomicAdd(out + 3, desc);
-    if (desc_start) atomicAdd(out + 4, desc_start);
+    if (bits) atomicOr(&cs->bits, (unsigned long long)bits);
+    if (bad_seg != ~0ull) atomicMin(&cs->bad_seg, bad_seg);
+    if (bad_p != ~0ull) atomicMin(&cs->bad_p, bad_p);
+    if (desc) atomicAdd(&cs->desc, desc);
+    if (desc_start) atomicAdd(&cs->desc_start, desc_start);
   }
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // this block's totals before its count
+    last = atomicAdd(&cs->done, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  volatile CheckState* v = cs;
+  const unsigned long long tb = v->bits, ts = v->bad_seg, tp = v->bad_p, td = v->desc,
+                           tds = v->desc_start;
+  if (gate && (tb != 0 || td != tds)) {
+    const int64_t m = std::max(outer + 1, nnz);
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) {
+      if (k <= outer) pos[k] = k == outer ? (int32_t)nnz : 0;
+      if (k < nnz && crd) crd[k] = 0;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    box[0] = tb;
+    box[1] = ts;
+    box[2] = tp;
+    box[3] = td;
+    box[4] = tds;
+    v->bits = kCheckInit.bits;
+    v->bad_seg = kCheckInit.bad_seg;
+    v->bad_p = kCheckInit.bad_p;
+    v->desc = kCheckInit.desc;
+    v->desc_start = kCheckInit.desc_start;
+    __threadfence();
+    v->done = 0u;
+    __threadfence_system();
+  }
+}
+
+std::mutex g_state_mu;
+CheckState* g_state[64] = {};
+
+// This device's check totals (allocated and initialised on first use), or null.
+CheckState* check_state() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    set_error(TACOGB_ERR_CUDA, "validate: no current device");
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lk(g_state_mu);
+  if (!g_state[dev]) {
+    CheckState* p = nullptr;
+    if (cudaMalloc(&p, sizeof(CheckState)) != cudaSuccess ||
+        cudaMemcpy(p, &kCheckInit, sizeof(CheckState), cudaMemcpyHostToDevice) != cudaSuccess) {
+      if (p) cudaFree(p);
+      set_error(TACOGB_ERR_ALLOC, "validate: check state allocation failed");
+      return nullptr;
+    }
+    g_state[dev] = p;
+  }
+  return g_state[dev];
 }
 
 }  // namespace
 
 bool validation_on() { return g_validate.load(std::memory_order_relaxed) != 0; }
 
-int level_check_enqueue(int64_t outer, int32_t inner, const int32_t* pos, const int32_t* crd,
-                        int64_t nnz, unsigned long long* out, cudaStream_t st) {
-  TACOGB_LAUNCH("level_check_init", st, level_check_init<<<1, 32, 0, st>>>(out));
-  if (outer <= 0 && nnz <= 0) return 0;
-  const int64_t n = std::max<int64_t>(std::max(outer, nnz), 1);  // thread 0 reads pos[0]
-  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
-  TACOGB_LAUNCH("level_check_kernel", st,
-                level_check_kernel<<<(unsigned)blocks, 256, 0, st>>>(outer, inner, pos, crd,
-                                                                      nnz, out));
-  return 0;
-}
-
-int level_gate_enqueue(int64_t outer, int32_t* pos, int32_t* crd, int64_t nnz,
-                       const unsigned long long* out, cudaStream_t st) {
-  if (outer <= 0 && nnz <= 0) return 0;
-  const int64_t n = std::max(outer + 1, nnz);
-  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 4);
-  TACOGB_LAUNCH("level_gate_kernel", st,
-                level_gate_kernel<<<(unsigned)blocks, 256, 0, st>>>(outer, pos, crd, nnz, out));
-  return 0;
-}
-
 static_assert(5 * kMaxPublishedChecks <= kMailboxRowLen, "published checks fit the mailbox");
 
-int level_checks_publish(const unsigned long long* out, int count, cudaStream_t st) {
-  TACOGB_CHECK_ARG(count >= 1 && count <= kMaxPublishedChecks, "validate: %d checks to publish",
-                   count);
-  volatile unsigned long long* box = host_mailbox();
+int level_check_enqueue(int64_t outer, int32_t inner, int32_t* pos, int32_t* crd, int64_t nnz,
+                        int box_index, bool gate, cudaStream_t st) {
+  TACOGB_CHECK_ARG(box_index >= 0 && box_index < kMaxPublishedChecks, "validate: check %d",
+                   box_index);
+  TACOGB_CHECK_ARG(pos != nullptr, "validate: null pos");
+  TACOGB_CHECK_ARG(!gate || inner > 0 || nnz == 0, "validate: no columns to gate nonzeros to");
+  CheckState* cs = check_state();
+  if (!cs) return last_code();
+  unsigned long long* box = host_mailbox();
   if (!box) return last_code();
-  TACOGB_LAUNCH("level_check_publish", st,
-                level_check_publish<<<1, 64, 0, st>>>(out, count, (unsigned long long*)box));
+  const int64_t n = std::max<int64_t>(std::max(outer, nnz), 1);
+  const int64_t blocks = std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 8);
+  TACOGB_LAUNCH("level_check_fused", st,
+                level_check_fused<<<(unsigned)blocks, 256, 0, st>>>(
+                    outer, inner, pos, crd, nnz, cs, box + 5 * box_index, gate ? 1 : 0));
   return 0;
 }
 
@@ -288,11 +320,10 @@ int validate_level_device(const char* what, int64_t outer, int32_t inner, const 
                           const int32_t* crd, int64_t nnz, cudaStream_t st) {
   if (outer <= 0 && nnz <= 0) return 0;
   TACOGB_CHECK_ARG(pos != nullptr, "%s: null pos", what);
-  // five counters in the library's scratch arena (slot reserved for the checks)
-  unsigned long long* out = (unsigned long long*)scratch(5 * sizeof(unsigned long long), 11);
-  if (!out) return last_code();
-  if (int rc = level_check_enqueue(outer, inner, pos, crd, nnz, out, st)) return rc;
-  if (int rc = level_checks_publish(out, 1, st)) return rc;
+  // read only (no gate)
+  if (int rc = level_check_enqueue(outer, inner, const_cast<int32_t*>(pos),
+                                   const_cast<int32_t*>(crd), nnz, 0, false, st))
+    return rc;
   TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
   return level_verdict(what, 0, 0, 0);
 }
@@ -307,6 +338,23 @@ void LevelCheck::begin(const char* what, int64_t outer, int32_t inner, const int
   nnz_ = nnz;
   active_ = validation_on() && (outer > 0 || nnz > 0);
   host_ = host_resident;
+}
+
+int LevelCheck::finish_deferred(cudaStream_t st, void* dpos, void* dcrd, bool rewritable) {
+  if (!active_) return 0;
+  if (!rewritable || dpos == nullptr || (inner_ <= 0 && nnz_ > 0)) return finish(st, dpos, dcrd);
+  active_ = false;
+  if (int rc = level_check_enqueue(outer_, inner_, (int32_t*)dpos, (int32_t*)dcrd, nnz_, 0, true,
+                                   st))
+    return rc;
+  pending_ = true;
+  return 0;
+}
+
+int LevelCheck::verdict() {
+  if (!pending_) return 0;
+  pending_ = false;
+  return level_verdict(what_, 0, 0, 0);
 }
 
 int LevelCheck::finish(cudaStream_t st, const void* dpos, const void* dcrd) {

@@ -16,21 +16,17 @@ bool validation_on();
 int validate_level_device(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
                           const int32_t* crd, int64_t nnz, cudaStream_t st);
 
-// The same check without synchronising, for levels checked while copies are in flight (the
-// pipelined products): level_check_enqueue checks a level (device arrays) into five counters at
-// `out` (device memory); level_gate_enqueue then makes the level harmless when its counters
-// show a violation (pos becomes 0, ..., 0, nnz and crd all 0, which every kernel reads in
-// bounds; inner >= 1 is required), so that a kernel launched after it on st never gathers
-// through a bad index; level_checks_publish copies `count` counter sets into the host mailbox
-// (at most kMaxPublishedChecks), and level_verdict reads one published set after the stream
-// has been synchronised: 0, or TACOGB_ERR_ARG with a message whose segment and position are
+// The same check in one launch without synchronising (the pipelined products, deferred checks):
+// level_check_enqueue checks a level (device arrays) on st and publishes its five totals into
+// the host mailbox set `box_index` (< kMaxPublishedChecks); with `gate`, a level that fails is
+// rewritten into a harmless one in the same launch (pos becomes 0, ..., 0, nnz and crd all 0,
+// which every kernel reads in bounds; needs inner >= 1 when nnz > 0), so a kernel launched
+// after it on st never gathers through a bad index.  level_verdict reads a published set after
+// st has been synchronised: 0, or TACOGB_ERR_ARG with a message whose segment and position are
 // offset by seg_base and pos_base (the level's place in the whole operand).
 constexpr int kMaxPublishedChecks = 12;
-int level_check_enqueue(int64_t outer, int32_t inner, const int32_t* pos, const int32_t* crd,
-                        int64_t nnz, unsigned long long* out, cudaStream_t st);
-int level_gate_enqueue(int64_t outer, int32_t* pos, int32_t* crd, int64_t nnz,
-                       const unsigned long long* out, cudaStream_t st);
-int level_checks_publish(const unsigned long long* out, int count, cudaStream_t st);
+int level_check_enqueue(int64_t outer, int32_t inner, int32_t* pos, int32_t* crd, int64_t nnz,
+                        int box_index, bool gate, cudaStream_t st);
 int level_verdict(const char* what, int index, int64_t seg_base, int64_t pos_base);
 
 // One level's check around a call's staging: begin() records the level as the caller passed it;
@@ -43,6 +39,14 @@ class LevelCheck {
   void begin(const char* what, int64_t outer, int32_t inner, const int32_t* pos,
              const int32_t* crd, int64_t nnz, bool host_resident);
   int finish(cudaStream_t st, const void* dpos, const void* dcrd);
+  // The check without waiting for the host, for a level held in the library's own staging
+  // buffers (rewritable): checked and, when it fails, made harmless on the device in one launch
+  // (level_check_enqueue with gate), so the kernels launched after it on st may run; verdict()
+  // after the caller's last synchronisation of st reports it (TACOGB_ERR_ARG with the first
+  // fault; the result's contents are then unspecified).  A level in the caller's memory (not
+  // rewritable), or one with nonzeros but no columns, is checked as finish() does.
+  int finish_deferred(cudaStream_t st, void* dpos, void* dcrd, bool rewritable);
+  int verdict();
 
  private:
   const char* what_ = "";
@@ -50,7 +54,7 @@ class LevelCheck {
   int32_t inner_ = 0;
   const int32_t* pos_ = nullptr;
   const int32_t* crd_ = nullptr;
-  bool active_ = false, host_ = false;
+  bool active_ = false, host_ = false, pending_ = false;
 };
 
 }  // namespace tacogb

@@ -8,7 +8,9 @@
   loop is involved, and the context stays usable, which the tests check by computing after it.
 * Index validation on device-resident operands.  Corrupt levels in device memory are rejected
   by the check kernel before any kernel gathers through them.  Every corruption here keeps
-  pos[rows] equal to the length of crd, so the check kernel's reads stay in bounds.
+  pos[rows] equal to the length of crd, so the check kernel's reads stay in bounds.  Host
+  operands are checked on their staged copies without a wait: a failing level is rewritten
+  into a harmless one before the product, and the verdict is read at the end.
 """
 import ctypes
 import time
@@ -111,6 +113,37 @@ def test_device_operands_are_validated(kind):
     c_.rows, c_.cols, c_.nnz, c_.vtype = len(pos) - 1, cols, len(c), tg.TACOGB_F64
     c_.pos, c_.crd, c_.vals = keep[0].data_ptr(), keep[1].data_ptr(), keep[2].data_ptr()
     assert tg.lib().tacogb_csr_validate(ctypes.byref(c_), _stream()) == ERR_ARG
+
+
+@pytest.mark.parametrize("op", ["spmv", "spmm"])
+@pytest.mark.parametrize("kind", KINDS)
+def test_host_operands_are_validated(op, kind):
+    """Host operands are staged, checked on the device without a wait (a failing level is made
+    harmless before the product) and the verdict read at the end: TACOGB_ERR_ARG with the
+    fault, and the next call with valid operands computes the oracle's result."""
+    pos, crd, vals, cols = _csr()
+    p, c = _corrupt(kind, pos, crd)
+    rows = len(pos) - 1
+    if op == "spmv":
+        x = W.dense(5, cols)
+        y = np.full(rows, np.nan)
+        args = lambda P, C: (T.dense(y, [rows]), T.csr(P, C, vals, [rows, cols]),  # noqa: E731
+                             T.dense(x, [cols]))
+        fn, ref, out = tg.lib().tacogb_spmv_compute, O.spmv(pos, crd, vals, x), y
+    else:
+        N = 8
+        B = np.ascontiguousarray(W.dense(6, cols * N).reshape(cols, N))
+        Cm = np.full((rows, N), np.nan)
+        args = lambda P, C: (T.dense(Cm, [rows, N]), T.csr(P, C, vals, [rows, cols]),  # noqa: E731
+                             T.dense(B, [cols, N]))
+        fn, ref, out = tg.lib().tacogb_spmm_compute, O.spmm(pos, crd, vals, B), Cm
+    Rt, At, Xt = args(p, c)
+    assert fn(Rt.ptr, At.ptr, Xt.ptr) == ERR_ARG
+    err = tg.lib().tacogb_last_error()
+    assert (b"%s operand A" % op.encode()) in err and MESSAGES[kind] in err, err
+    Rt, At, Xt = args(pos, crd)
+    assert fn(Rt.ptr, At.ptr, Xt.ptr) == 0, tg.lib().tacogb_last_error()
+    assert normwise(out, ref) <= 1e-12
 
 
 def test_valid_device_operands_pass_and_compute():
