@@ -78,11 +78,12 @@ int tacogb_device_status(int32_t* status);
  * The check is one kernel reading pos and crd once, on the arrays the kernels will read (the
  * caller's device arrays or the staged copies of host arrays), before any gathering kernel; a
  * call that cannot reach a GPU checks host-resident levels on the host, so invalid input is
- * still reported as TACOGB_ERR_ARG.  tacogb_spmv_compute and tacogb_spmm_compute over host
- * operands of 2^23 nonzeros or more copy, check and multiply A in chunks as the chunks land:
- * there a chunk that fails its check is rewritten on the device into a harmless level before
- * its product runs, the error is returned after the last chunk, and the result's contents are
- * then unspecified.  The device layer (tacogb_spmv
+ * still reported as TACOGB_ERR_ARG.  tacogb_spmv_compute and tacogb_spmm_compute check host
+ * operands on their staged copies without waiting for the verdict: a level that fails is
+ * rewritten on the device into a harmless one before the product runs, the error is returned
+ * when the call ends (over host operands of 2^23 nonzeros or more, which are copied, checked
+ * and multiplied chunk by chunk, with the position in the whole operand), and the result's
+ * contents are then unspecified.  The device layer (tacogb_spmv
  * and the other functions on tacogb_csr) trusts its arguments; tacogb_csr_validate checks a
  * device CSR explicitly (declared with the device layer below).  tacogb_set_validation(0) turns
  * the taco-ABI checks off (and returns the previous setting); they are on by default. */
