@@ -377,6 +377,36 @@ struct HostCopy {
   size_t bytes;
 };
 
+// Maps the pages of [p, p + bytes) of host memory (one write per page, inside the range only)
+// with up to eight threads; for pageable destinations of device -> host copies, before the copy
+// is issued.
+void map_host_pages(void* p, size_t bytes) {
+  if (!bytes) return;
+  const long pg = sysconf(_SC_PAGESIZE);
+  const size_t page = pg > 0 ? (size_t)pg : 4096;
+  const int nt = (int)std::min<size_t>({8, std::max(1u, std::thread::hardware_concurrency()),
+                                        std::max<size_t>(1, bytes >> 22)});
+  auto touch = [=](size_t a, size_t b) {
+    volatile unsigned char* q = (volatile unsigned char*)p;
+    for (size_t o = a; o < b; o = (o / page + 1) * page) q[o] = 0;
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; t++) th.emplace_back(touch, bytes * t / nt, bytes * (t + 1) / nt);
+  touch(0, bytes / nt);
+  for (auto& x : th) x.join();
+}
+
+// True for large results in pageable host memory, whose pages are best mapped before the copy.
+bool wants_page_mapping(const void* dst, size_t bytes) {
+  if (bytes < ((size_t)64 << 20)) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, dst) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return at.type == cudaMemoryTypeUnregistered;
+}
+
 int copy_to_fresh_host(std::initializer_list<HostCopy> copies, cudaStream_t st) {
   constexpr size_t kPipelineBytes = (size_t)64 << 20, kChunk = (size_t)16 << 20;
   size_t total = 0;
@@ -953,6 +983,8 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     }
     TACOGB_CUDA_TRY(cudaEventRecord(ev[j], h2d));
   }
+  // a large pageable result has its pages mapped chunk by chunk before each chunk's return
+  const bool map_pages = wants_page_mapping(result, (size_t)rows * res_row_bytes);
   // chunks' pos rebased once the dense operand and pos are in
   int rc = 0;
   TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[2 * kPipeChunks], 0));
@@ -977,9 +1009,10 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     if (rc) break;
     TACOGB_CUDA_TRY(cudaEventRecord(ev[kPipeChunks + j], st));
     TACOGB_CUDA_TRY(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0));
+    unsigned char* hres = (unsigned char*)result + (size_t)rb[j] * res_row_bytes;
+    if (map_pages) map_host_pages(hres, (size_t)nr * res_row_bytes);
     if (nr)
-      TACOGB_CUDA_TRY(cudaMemcpyAsync((unsigned char*)result + (size_t)rb[j] * res_row_bytes,
-                                      dres + (size_t)rb[j] * res_row_bytes,
+      TACOGB_CUDA_TRY(cudaMemcpyAsync(hres, dres + (size_t)rb[j] * res_row_bytes,
                                       (size_t)nr * res_row_bytes, cudaMemcpyDeviceToHost, d2h));
   }
   // nothing may still be copying when the call returns, whatever happened
