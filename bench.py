@@ -30,11 +30,16 @@ import sys
 import tempfile
 import time
 
-# OpenMP placement for the CPU legs (taco's generated code runs OpenMP over all host cores),
-# set before anything loads the OpenMP runtime, which reads it once; the schedule is set to
-# static per call, as taco's module does.  A value already in the environment wins.
-os.environ.setdefault("OMP_PROC_BIND", "close")
-os.environ.setdefault("OMP_PLACES", "cores")
+# OpenMP placement for the reference arm, a process that runs taco's generated CPU code alone
+# (OpenMP over all host cores): set before anything loads the OpenMP runtime, which reads it
+# once; the schedule is set to static per call, as taco's module does.  A value already in the
+# environment wins.  The GPU arm's process stays unbound: binding pins its main thread to one
+# core, and every thread it starts afterwards (the CUDA driver's, the library's page mapping)
+# inherits that core.
+if "--impl=reference" in sys.argv or any(
+        a == "--impl" and b == "reference" for a, b in zip(sys.argv, sys.argv[1:])):
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_PLACES", "cores")
 
 import numpy as np  # noqa: E402
 
@@ -993,7 +998,7 @@ def cpu_model():
 
 def omp_setup():
     return "OMP_PROC_BIND=%s OMP_PLACES=%s, static schedule" % (
-        os.environ.get("OMP_PROC_BIND"), os.environ.get("OMP_PLACES"))
+        os.environ.get("OMP_PROC_BIND", "unset"), os.environ.get("OMP_PLACES", "unset"))
 
 
 def time_cpu(op, budget_s=8.0, reps=None):
