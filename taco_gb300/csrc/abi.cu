@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "threads.h"
 #include "validate.h"
 
 namespace tacogb {
@@ -391,7 +392,11 @@ void map_host_pages(void* p, size_t bytes) {
     for (size_t o = a; o < b; o = (o / page + 1) * page) q[o] = 0;
   };
   std::vector<std::thread> th;
-  for (int t = 1; t < nt; t++) th.emplace_back(touch, bytes * t / nt, bytes * (t + 1) / nt);
+  for (int t = 1; t < nt; t++)
+    th.emplace_back([=] {
+      spread_thread();
+      touch(bytes * t / nt, bytes * (t + 1) / nt);
+    });
   touch(0, bytes / nt);
   for (auto& x : th) x.join();
 }
@@ -437,6 +442,7 @@ int copy_to_fresh_host(std::initializer_list<HostCopy> copies, cudaStream_t st) 
   std::vector<std::atomic<int>> done(chunks.size());
   for (auto& d : done) d.store(0, std::memory_order_relaxed);
   auto worker = [&](int t) {
+    spread_thread();
     for (size_t k = 0; k < chunks.size(); k++) {
       const HostCopy& c = chunks[k];
       const size_t a = c.bytes * t / nt, b = c.bytes * (t + 1) / nt;

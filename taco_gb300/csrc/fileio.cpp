@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "taco_gb300.h"
+#include "threads.h"
 
 namespace tacogb {
 void set_error(int code, const char* fmt, ...);
@@ -133,6 +134,7 @@ bool parse_parallel(const std::vector<const char*>& lines, int order, int32_t* r
   for (int t = 0; t < T; t++) {
     const size_t a = n * t / T, b = n * (t + 1) / T;
     th.emplace_back([&, t, a, b] {
+      tacogb::spread_thread();
       ok[t] = parse_entries(lines, a, b, order, r + a, c + a, v + a, true, &mx[2 * t]);
     });
   }

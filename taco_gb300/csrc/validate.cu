@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "threads.h"
 #include "validate.h"
 
 namespace tacogb {
@@ -127,6 +128,7 @@ int host_check(const char* what, int64_t outer, int32_t inner, const int32_t* po
   std::vector<HostPart> parts(nt);
   std::atomic<int64_t> next{0};
   auto worker = [&](int t) {
+    if (t > 0) spread_thread();
     for (;;) {
       const int64_t k = next.fetch_add(1);
       if (k >= chunks) break;
