@@ -250,6 +250,32 @@ def test_full_size(which):
         assert cp[-1] == 3397636
 
 
+@pytest.mark.parametrize("where", ["host", "device"])
+def test_abi_evaluate_full_size(where):
+    """tacogb_spgemm_evaluate on the random 262,144^2 matrix: 0.2 GB of results, returned into
+    malloc'd memory by chunked copies whose pages host threads map first (host operands), or
+    written into managed memory populated on the GPU first (device operands); bit-exact."""
+    s = W.spgemm_random()
+    p, c, v = W.generate(s)
+    ref = O.spgemm(p, c, v, p, c, v, s.cols)
+    nnz = int(ref[0][-1])
+    assert nnz * 12 >= 64 << 20
+    arrs = (p, c, v) if where == "host" else tuple(torch.from_numpy(a).cuda() for a in (p, c, v))
+    At = T.csr(*arrs, [s.rows, s.cols])
+    for _ in range(2):
+        Ct = T.csr_result([s.rows, s.cols])
+        assert tg.lib().tacogb_spgemm_evaluate(Ct.ptr, At.ptr, At.ptr) == 0, \
+            tg.lib().tacogb_last_error()
+        if where == "device":
+            torch.cuda.synchronize()
+        P = ctypes.POINTER
+        pos = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 0), P(ctypes.c_int32)), (s.rows + 1,))
+        crd = np.ctypeslib.as_array(ctypes.cast(Ct.index(1, 1), P(ctypes.c_int32)), (nnz,))
+        vals = np.ctypeslib.as_array(ctypes.cast(Ct.vals_ptr, P(ctypes.c_double)), (nnz,))
+        assert np.array_equal(pos, ref[0]) and np.array_equal(crd, ref[1])
+        assert np.array_equal(vals, ref[2])
+
+
 def test_empty_and_degenerate():
     A = (np.zeros(5, np.int32), np.zeros(0, np.int32), np.zeros(0), 7)
     B = (np.zeros(8, np.int32), np.zeros(0, np.int32), np.zeros(0), 3)
