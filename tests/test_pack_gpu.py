@@ -122,6 +122,26 @@ def test_taco_buffer_entry(where):
     assert_same((pos.copy(), crd.copy(), val.copy()), ref)
 
 
+def test_taco_buffer_entry_large_host():
+    """tacogb_pack_taco on a host buffer of the 1,048,576-row power-law matrix's coordinates,
+    shuffled: the results (0.29 GB) come back into malloc'd memory by chunked copies whose pages
+    host threads map first, and pack back to the matrix."""
+    s = W.spmv_powerlaw(rows=1 << 20)
+    pos, crd, vals = W.generate(s)
+    assert len(crd) * 12 >= 64 << 20
+    rows = np.repeat(np.arange(s.rows, dtype=np.int32), np.diff(pos))
+    perm = np.random.default_rng(4).permutation(len(crd))
+    rec = _records(rows[perm], crd[perm], vals[perm])
+    Tt = T.csr_result([s.rows, s.cols])
+    assert tg.lib().tacogb_pack_taco(Tt.ptr, rec.ctypes.data, len(crd)) == 0, \
+        tg.lib().tacogb_last_error()
+    P = ctypes.POINTER
+    got = (np.ctypeslib.as_array(ctypes.cast(Tt.index(1, 0), P(ctypes.c_int32)), (s.rows + 1,)),
+           np.ctypeslib.as_array(ctypes.cast(Tt.index(1, 1), P(ctypes.c_int32)), (len(crd),)),
+           np.ctypeslib.as_array(ctypes.cast(Tt.vals_ptr, P(ctypes.c_double)), (len(crd),)))
+    assert_same(got, (pos, crd, vals))
+
+
 @pytest.mark.parametrize("name", ["read_general.mtx", "read_symmetric.mtx", "read_array.mtx",
                                   "read_plain.tns", "read_rua32.rb"])
 def test_read_csr_matches_taco(name):
