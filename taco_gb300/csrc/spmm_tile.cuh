@@ -154,23 +154,6 @@ struct MmF32 {
   __device__ static double to_double(Acc a) { return (double)a; }
 };
 
-struct MmComp32 : MmF32 {
-  using Acc = DF;
-  __device__ static Acc zero() { return DF{0.f, 0.f}; }
-  __device__ static void madd(Acc& acc, Prep a, BE b, bool&) {
-    DF p;
-    p.h = __fmul_rn(a, b);
-    p.l = __fmaf_rn(a, b, -p.h);
-    acc = df_add(acc, p);
-  }
-  __device__ static Out out(Acc a) { return __fadd_rn(a.h, a.l); }
-  __device__ static double to_double(Acc a) { return (double)a.h + (double)a.l; }
-};
-
-struct MmBF16 : MmF32 {
-  using BV = __nv_bfloat16;
-};
-
 // Running double-float sum with deferred renormalisation: hi sum s and an unnormalised
 // compensation c (the product errors, cross terms and TwoSum errors), renormalised on output
 // and once per 32 nonzeros (so that c's own rounding stays at 2^-48 of the sum for long rows).
@@ -180,6 +163,37 @@ struct DFAcc {
 
 template <class P>
 __device__ __forceinline__ void renorm(typename P::Acc&) {}
+
+// FP32 values and B, compensated: per column the exact TwoProduct and one TwoSum, their errors
+// summed into the unnormalised compensation (ten FP32 instructions; renormalised with the
+// double-float accumulators, once per 32 nonzeros and on output).
+struct MmComp32 : MmF32 {
+  using Acc = DFAcc;
+  __device__ static Acc zero() { return DFAcc{0.f, 0.f}; }
+  __device__ static void madd(Acc& acc, Prep a, BE b, bool&) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);
+    float s1, e;
+    two_sum(acc.s, p, s1, e);
+    acc.c = __fadd_rn(acc.c, __fadd_rn(pe, e));
+    acc.s = s1;
+  }
+  __device__ static Out out(Acc a) { return __fadd_rn(a.s, a.c); }
+  __device__ static double to_double(Acc a) { return (double)a.s + (double)a.c; }
+};
+
+template <>
+__device__ __forceinline__ void renorm<MmComp32>(DFAcc& a) {
+  float s, e;
+  two_sum(a.s, a.c, s, e);
+  a.s = s;
+  a.c = e;
+}
+
+struct MmBF16 : MmF32 {
+  using BV = __nv_bfloat16;
+};
+
 
 // FP64 values, B pre-split into double-float pairs: per column one exact TwoProduct of the hi
 // parts, two cross-term FMAs and one TwoSum (about 12 FP32 instructions); values are split by
