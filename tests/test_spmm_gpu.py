@@ -237,6 +237,19 @@ def test_abi_pipelined_b_outside_double_float_range():
     assert normwise(C2[idx], O.spmm(*sub_rows(pos, crd, vals, idx), B2)) <= F64_TOL
 
 
+def test_abi_pipelined_skewed_rows():
+    """One row with about 60 % of the nonzeros and long runs of empty rows through the pipelined
+    SpMM (empty chunks, one chunk for the big row)."""
+    from tests.test_spmv_gpu import _skewed_pipeline_matrix
+    pos, crd, vals, cols = _skewed_pipeline_matrix()
+    rows, N = len(pos) - 1, 8
+    B = np.ascontiguousarray(W.dense(65, cols * N).reshape(cols, N))
+    C = np.full((rows, N), np.nan)
+    Ct, At, Bt = T.dense(C, [rows, N]), T.csr(pos, crd, vals, [rows, cols]), T.dense(B, [cols, N])
+    assert tg.lib().tacogb_spmm_compute(Ct.ptr, At.ptr, Bt.ptr) == 0, tg.lib().tacogb_last_error()
+    assert normwise(C, O.spmm(pos, crd, vals, B)) <= F64_TOL
+
+
 @pytest.mark.parametrize("kind", ["crd_high", "pos_order"])
 def test_abi_pipelined_rejects_a_corrupt_chunk(kind):
     """A corrupt chunk of the pipelined path: TACOGB_ERR_ARG naming the segment or position in

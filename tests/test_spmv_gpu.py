@@ -306,6 +306,35 @@ def test_abi_pipelined_host_operands(dtype):
         assert normwise(y, ref) <= (F64_TOL if dtype == np.float64 else F32_TOL)
 
 
+def _skewed_pipeline_matrix():
+    """2^23 + nonzeros of which one row holds about 60 %, between long runs of empty rows: the
+    pipeline's chunk boundaries fall on row starts, so several chunks are empty and the big row
+    is one chunk of its own."""
+    rng = np.random.default_rng(11)
+    rows, cols = 200000, 8000000
+    lens = np.zeros(rows, np.int64)
+    live = rng.choice(rows, 20000, replace=False)
+    lens[live] = rng.integers(1, 350, len(live))
+    lens[123457] = 5100000
+    pos = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    crd = np.empty(int(pos[-1]), np.int32)
+    for r in np.flatnonzero(lens):
+        crd[pos[r]:pos[r + 1]] = np.sort(rng.choice(cols, int(lens[r]), replace=False))
+    vals = rng.uniform(-1, 1, len(crd))
+    return pos, crd, vals, cols
+
+
+def test_abi_pipelined_skewed_rows():
+    pos, crd, vals, cols = _skewed_pipeline_matrix()
+    assert len(crd) >= 1 << 23
+    rows = len(pos) - 1
+    x = W.dense(27, cols)
+    y = np.full(rows, np.nan)
+    At, Xt, Yt = T.csr(pos, crd, vals, [rows, cols]), T.dense(x, [cols]), T.dense(y, [rows])
+    assert tg.lib().tacogb_spmv_compute(Yt.ptr, At.ptr, Xt.ptr) == 0, tg.lib().tacogb_last_error()
+    assert normwise(y, O.spmv(pos, crd, vals, x)) <= F64_TOL
+
+
 def test_abi_pipelined_rejects_a_corrupt_late_chunk():
     s = W.spmv_powerlaw(rows=600000)
     pos, crd, vals = W.generate(s)
