@@ -401,9 +401,10 @@ void map_host_pages(void* p, size_t bytes) {
   for (auto& x : th) x.join();
 }
 
-// True for large results in pageable host memory, whose pages are best mapped before the copy.
+// True for results of 4 MB or more in pageable host memory, whose pages are best mapped before
+// the copies into them.
 bool wants_page_mapping(const void* dst, size_t bytes) {
-  if (bytes < ((size_t)64 << 20)) return false;
+  if (bytes < ((size_t)4 << 20)) return false;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, dst) != cudaSuccess) {
     cudaGetLastError();
@@ -989,8 +990,19 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     }
     TACOGB_CUDA_TRY(cudaEventRecord(ev[j], h2d));
   }
-  // a large pageable result has its pages mapped chunk by chunk before each chunk's return
-  const bool map_pages = wants_page_mapping(result, (size_t)rows * res_row_bytes);
+  // A pageable result of up to 64 MB (an evaluate's fresh y) is page-locked for the call, so
+  // that its returns are asynchronous copies like a pinned result's (a copy into pageable memory
+  // completes before cudaMemcpyAsync returns, which holds the chunk loop); a larger one has its
+  // pages mapped by host threads chunk by chunk before each chunk's return.
+  const size_t all_res = (size_t)rows * res_row_bytes;
+  const bool map_pages = wants_page_mapping(result, all_res);
+  bool registered = false;
+  if (map_pages && all_res <= ((size_t)64 << 20)) {
+    registered = cudaHostRegister(result, all_res, cudaHostRegisterDefault) == cudaSuccess;
+    if (!registered) cudaGetLastError();
+  }
+  const bool map_now = map_pages && !registered && all_res <= ((size_t)64 << 20);
+  if (map_now) map_host_pages(result, all_res);
   // chunks' pos rebased once the dense operand and pos are in
   int rc = 0;
   TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[2 * kPipeChunks], 0));
@@ -1016,7 +1028,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     TACOGB_CUDA_TRY(cudaEventRecord(ev[kPipeChunks + j], st));
     TACOGB_CUDA_TRY(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0));
     unsigned char* hres = (unsigned char*)result + (size_t)rb[j] * res_row_bytes;
-    if (map_pages) map_host_pages(hres, (size_t)nr * res_row_bytes);
+    if (map_pages && !map_now && !registered) map_host_pages(hres, (size_t)nr * res_row_bytes);
     if (nr)
       TACOGB_CUDA_TRY(cudaMemcpyAsync(hres, dres + (size_t)rb[j] * res_row_bytes,
                                       (size_t)nr * res_row_bytes, cudaMemcpyDeviceToHost, d2h));
@@ -1024,6 +1036,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   // nothing may still be copying when the call returns, whatever happened
   const cudaError_t e1 = cudaStreamSynchronize(h2d), e2 = cudaStreamSynchronize(st),
                     e3 = cudaStreamSynchronize(d2h);
+  if (registered && cudaHostUnregister(result) != cudaSuccess) cudaGetLastError();
   if (rc) return rc;
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
     set_error(TACOGB_ERR_CUDA, "%s: %s", what,
