@@ -974,22 +974,81 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   int64_t* dmeta = (int64_t*)stage_buffer(8, sizeof(meta));
   if (!dpos || !dposc || !dcrd || !dval || !ddense || !dres || !dmeta) return TACOGB_ERR_ALLOC;
   if (int rc = prod.reserve(cols, N, btype, vt)) return rc;
-  // every copy is issued up front on the host -> device stream
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(dmeta, meta, sizeof(int64_t) * 3 * K, cudaMemcpyHostToDevice, h2d));
-  if (dense_bytes)
-    TACOGB_CUDA_TRY(cudaMemcpyAsync(ddense, dense, dense_bytes, cudaMemcpyHostToDevice, h2d));
-  TACOGB_CUDA_TRY(cudaMemcpyAsync(dpos, pos, ((size_t)rows + 1) * 4, cudaMemcpyHostToDevice, h2d));
-  TACOGB_CUDA_TRY(cudaEventRecord(ev[2 * kPipeChunks], h2d));
-  for (int j = 0; j < K; j++) {
-    const int64_t k0 = pos[rb[j]], n = pos[rb[j + 1]] - k0;
-    if (n) {
-      TACOGB_CUDA_TRY(cudaMemcpyAsync(dcrd + coff[j], crd + k0, (size_t)n * 4,
-                                      cudaMemcpyHostToDevice, h2d));
-      TACOGB_CUDA_TRY(cudaMemcpyAsync(dval + voff[j] * vb, (const unsigned char*)A->vals + k0 * vb,
-                                      (size_t)n * vb, cudaMemcpyHostToDevice, h2d));
+  // Every copy is issued up front on the host -> device stream.  A copy from pageable memory
+  // returns only once it is (nearly) done, so with pageable operands a copier thread issues
+  // them and publishes each chunk's event once it is recorded; the loop below waits for that on
+  // the host before it queues the chunk's wait on the device (a wait queued before the event is
+  // recorded would not wait).  recorded: -2 nothing yet, -1 the dense operand and pos, j the
+  // chunks up to j (K after a failed copy, with copy_err set).
+  std::atomic<int> recorded{-2};
+  std::atomic<int> copy_err{0};
+  auto issue = [&]() {
+    cudaError_t e = cudaMemcpyAsync(dmeta, meta, sizeof(int64_t) * 3 * K, cudaMemcpyHostToDevice,
+                                    h2d);
+    if (e == cudaSuccess && dense_bytes)
+      e = cudaMemcpyAsync(ddense, dense, dense_bytes, cudaMemcpyHostToDevice, h2d);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(dpos, pos, ((size_t)rows + 1) * 4, cudaMemcpyHostToDevice, h2d);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2 * kPipeChunks], h2d);
+    if (e == cudaSuccess) recorded.store(-1, std::memory_order_release);
+    for (int j = 0; j < K && e == cudaSuccess; j++) {
+      const int64_t k0 = pos[rb[j]], n = pos[rb[j + 1]] - k0;
+      if (n) {
+        e = cudaMemcpyAsync(dcrd + coff[j], crd + k0, (size_t)n * 4, cudaMemcpyHostToDevice, h2d);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(dval + voff[j] * vb, (const unsigned char*)A->vals + k0 * vb,
+                              (size_t)n * vb, cudaMemcpyHostToDevice, h2d);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev[j], h2d);
+      if (e == cudaSuccess) recorded.store(j, std::memory_order_release);
     }
-    TACOGB_CUDA_TRY(cudaEventRecord(ev[j], h2d));
-  }
+    if (e != cudaSuccess) {
+      copy_err.store((int)e);
+      recorded.store(K, std::memory_order_release);
+    }
+  };
+  auto pageable = [](const void* p) {
+    cudaPointerAttributes at;
+    if (!p) return false;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+      cudaGetLastError();
+      return true;
+    }
+    return at.type == cudaMemoryTypeUnregistered;
+  };
+  const bool pageable_in = pageable(pos) || pageable(crd) || pageable(A->vals) ||
+                           (dense_bytes && pageable(dense));
+  std::thread copier;
+  int dev = 0;
+  if (pageable_in && cudaGetDevice(&dev) == cudaSuccess)
+    copier = std::thread([&, dev] {
+      spread_thread();
+      if (cudaSetDevice(dev) != cudaSuccess) {  // a new thread starts on device 0
+        copy_err.store((int)cudaErrorInvalidDevice);
+        recorded.store(K, std::memory_order_release);
+        return;
+      }
+      issue();
+    });
+  else
+    issue();
+  int rc = 0;
+  // the host side of a chunk's readiness: its events recorded (or a copy failed)
+  auto wait_recorded = [&](int j) {
+    while (recorded.load(std::memory_order_acquire) < j) std::this_thread::yield();
+    if (const int e = copy_err.load()) {
+      set_error(TACOGB_ERR_CUDA, "%s: copy: %s", what, cudaGetErrorString((cudaError_t)e));
+      rc = TACOGB_ERR_CUDA;
+    }
+    return rc == 0;
+  };
+  auto cu = [&](cudaError_t e) {
+    if (e != cudaSuccess && rc == 0) {
+      set_error(TACOGB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+      rc = TACOGB_ERR_CUDA;
+    }
+    return rc == 0;
+  };
   // A pageable result of up to 64 MB (an evaluate's fresh y) is page-locked for the call, so
   // that its returns are asynchronous copies like a pinned result's (a copy into pageable memory
   // completes before cudaMemcpyAsync returns, which holds the chunk loop); a larger one has its
@@ -1004,16 +1063,16 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   const bool map_now = map_pages && !registered && all_res <= ((size_t)64 << 20);
   if (map_now) map_host_pages(result, all_res);
   // chunks' pos rebased once the dense operand and pos are in
-  int rc = 0;
-  TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[2 * kPipeChunks], 0));
-  count_launch();
-  spmv_rebase_pos<<<dim3(64, K), 256, 0, st>>>(dpos, dmeta, K, dposc);
-  rc = launch_check("spmv_rebase_pos");
-  if (rc == 0) rc = prod.prepare(ddense, cols, N, st);
+  if (wait_recorded(-1) && cu(cudaStreamWaitEvent(st, ev[2 * kPipeChunks], 0))) {
+    count_launch();
+    spmv_rebase_pos<<<dim3(64, K), 256, 0, st>>>(dpos, dmeta, K, dposc);
+    rc = launch_check("spmv_rebase_pos");
+    if (rc == 0) rc = prod.prepare(ddense, cols, N, st);
+  }
   for (int j = 0; j < K && rc == 0; j++) {
     const int32_t nr = (int32_t)meta[3 * j + 1];
     const int32_t n = pos[rb[j + 1]] - pos[rb[j]];
-    TACOGB_CUDA_TRY(cudaStreamWaitEvent(st, ev[j], 0));
+    if (!wait_recorded(j) || !cu(cudaStreamWaitEvent(st, ev[j], 0))) break;
     int32_t* cpos = dposc + meta[3 * j + 2];
     int32_t* ccrd = dcrd + coff[j];
     tacogb_csr cj{nr, cols, n, cpos, ccrd, dval + voff[j] * vb, vt};
@@ -1025,14 +1084,16 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     }
     rc = prod.run(&cj, ddense, dres + (size_t)rb[j] * res_row_bytes, N, btype, st);
     if (rc) break;
-    TACOGB_CUDA_TRY(cudaEventRecord(ev[kPipeChunks + j], st));
-    TACOGB_CUDA_TRY(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0));
+    if (!cu(cudaEventRecord(ev[kPipeChunks + j], st)) ||
+        !cu(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0)))
+      break;
     unsigned char* hres = (unsigned char*)result + (size_t)rb[j] * res_row_bytes;
     if (map_pages && !map_now && !registered) map_host_pages(hres, (size_t)nr * res_row_bytes);
-    if (nr)
-      TACOGB_CUDA_TRY(cudaMemcpyAsync(hres, dres + (size_t)rb[j] * res_row_bytes,
-                                      (size_t)nr * res_row_bytes, cudaMemcpyDeviceToHost, d2h));
+    if (nr && !cu(cudaMemcpyAsync(hres, dres + (size_t)rb[j] * res_row_bytes,
+                                  (size_t)nr * res_row_bytes, cudaMemcpyDeviceToHost, d2h)))
+      break;
   }
+  if (copier.joinable()) copier.join();
   // nothing may still be copying when the call returns, whatever happened
   const cudaError_t e1 = cudaStreamSynchronize(h2d), e2 = cudaStreamSynchronize(st),
                     e3 = cudaStreamSynchronize(d2h);
