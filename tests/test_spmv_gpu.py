@@ -306,6 +306,42 @@ def test_abi_pipelined_host_operands(dtype):
         assert normwise(y, ref) <= (F64_TOL if dtype == np.float64 else F32_TOL)
 
 
+def _off_line(a, pinned, shift=16):
+    """A host copy of a whose first element sits `shift` bytes past a 128-byte boundary, in
+    pinned (torch) or pageable (numpy) memory: large host -> device copies from such addresses
+    go as a short head and a 128-byte-aligned body."""
+    pad = 256 // a.itemsize
+    if pinned:
+        buf = torch.empty(a.size + pad, dtype=torch.from_numpy(a[:0]).dtype).pin_memory()
+        base = buf.data_ptr()
+    else:
+        buf = np.empty(a.size + pad, a.dtype)
+        base = buf.ctypes.data
+    off = ((shift - base) % 128) // a.itemsize
+    view = buf[off:off + a.size]
+    if pinned:
+        view.copy_(torch.from_numpy(a))
+        assert view.data_ptr() % 128 == shift
+    else:
+        view[:] = a
+        assert view.ctypes.data % 128 == shift
+    return view
+
+
+@pytest.mark.parametrize("pinned", [True, False])
+@pytest.mark.parametrize("rows", [100000, 600000])  # staged whole / pipelined (2^23 + nonzeros)
+def test_abi_host_operands_off_line_boundaries(pinned, rows):
+    s = W.spmv_powerlaw(rows=rows)
+    pos, crd, vals = W.generate(s)
+    assert (len(crd) >= 1 << 23) == (rows == 600000) and vals.nbytes >= 4 << 20
+    x = W.dense(26, s.cols)
+    hp, hc, hv, hx = (_off_line(a, pinned) for a in (pos, crd, vals, x))
+    y = np.full(s.rows, np.nan)
+    At, Xt, Yt = T.csr(hp, hc, hv, [s.rows, s.cols]), T.dense(hx, [s.cols]), T.dense(y, [s.rows])
+    assert tg.lib().tacogb_spmv_compute(Yt.ptr, At.ptr, Xt.ptr) == 0, tg.lib().tacogb_last_error()
+    assert normwise(y, O.spmv(pos, crd, vals, x)) <= F64_TOL
+
+
 def _skewed_pipeline_matrix():
     """2^23 + nonzeros of which one row holds about 60 %, between long runs of empty rows: the
     pipeline's chunk boundaries fall on row starts, so several chunks are empty and the big row
