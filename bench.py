@@ -1537,7 +1537,9 @@ def main():
                 "kernel": dom, "kernel_ms": dom_ms, "peak_source": peak_kind,
                 "kernel_share": dom_share}
     if op.pattern == "spmv" and rank == 0:
-        roofline["gather"] = gather_roofline(torch, L, op.nnz, dom_ms)
+        # everything but x goes through L2 as streamed sectors; x is gathered, one per nonzero
+        roofline["gather"] = gather_roofline(torch, L, op.nnz, dom_ms,
+                                             op.bytes - op.cols * ESZ[args.dtype])
     del keep
 
     e2e = None
@@ -1676,15 +1678,22 @@ def gather_ceiling(torch, L, reps=5):
     return n * reps / (e0.elapsed_time(e1) / 1e3), sms
 
 
-def gather_roofline(torch, L, nnz, kernel_ms):
+def gather_roofline(torch, L, nnz, kernel_ms, streamed_bytes):
     """The SpMV kernel's x gathers (one per nonzero) per second against the gather ceiling
-    measured now on this GPU (run after the timed region)."""
+    measured now on this GPU (run after the timed region).  `l2_sectors` counts every 32-byte
+    L2 sector both move: the kernel's gathers plus the operands it streams (crd, values, pos,
+    y), against the probe's gathers plus its index reads (one sector per eight gathers)."""
     ceiling, sms = gather_ceiling(torch, L)
     achieved = nnz / (kernel_ms / 1e3)
+    sectors = (nnz + streamed_bytes / 32) / (kernel_ms / 1e3)
+    probe_sectors = ceiling * (1 + 1 / 8)
     return {"achieved": achieved, "peak": ceiling, "unit": "gathers/s", "frac": achieved / ceiling,
             "floor_ms": nnz / ceiling * 1e3,
             "probe": "tacogb_probe_gather: random 8-byte ld.global.cg from a 32 MiB L2-resident "
-                     "table, 160 KB shared memory held per SM (carveout 70 %), as the kernel"}
+                     "table, 160 KB shared memory held per SM (carveout 70 %), as the kernel",
+            "l2_sectors": {"achieved": sectors, "peak": probe_sectors, "unit": "sectors/s",
+                           "frac": sectors / probe_sectors,
+                           "floor_ms": (nnz + streamed_bytes / 32) / probe_sectors * 1e3}}
 
 
 def main_gather_probe(args, torch, tg, L):
