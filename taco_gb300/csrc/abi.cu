@@ -952,13 +952,28 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     set_error(TACOGB_ERR_CUDA, "%s: no GPU streams", what);
     return TACOGB_ERR_CUDA;
   }
-  // chunk boundaries on the host pos: first row whose start reaches j * nnz / K
+  // chunk boundaries on the host pos: first row whose start reaches the chunk's share of the
+  // nonzeros.  Shares are equal but for the first two and the last two chunks (a quarter and a
+  // half of one, from five chunks on): the products start once the first chunk is in, and the
+  // last chunk's product and return are the part of the call that no copy overlaps.  Measured
+  // against equal shares: SpMV 6.22 -> 6.14 ms (FP64) and 4.21 -> 4.14 ms (FP32) on the
+  // 1.0e8-nonzero power-law matrix, SpMM N=64 unchanged (7.62 ms); small last chunks alone
+  // (4,...,4,2,1) slowed SpMM to 7.77 ms, whose products wait for B and the first chunk.
   const int K = (int)std::min<int64_t>(kPipeChunks, std::max<int64_t>(1, nnz / (kPipeMinNnz / 2)));
   TACOGB_CHECK_ARG(pos[0] == 0, "%s: pos[0] is not 0", what);
+  auto weight_before = [K](int j) -> int64_t {  // in quarters of a full chunk
+    int64_t w = 0;
+    for (int i = 0; i < j; i++) {
+      const int edge = std::min(i, K - 1 - i);  // 0 at either end
+      w += K < 5 || edge >= 2 ? 4 : edge == 1 ? 2 : 1;
+    }
+    return w;
+  };
+  const int64_t weight_all = weight_before(K);
   int32_t rb[kPipeChunks + 1];
   rb[0] = 0;
   for (int j = 1; j < K; j++) {
-    const int64_t target = (int64_t)nnz * j / K;
+    const int64_t target = (int64_t)nnz * weight_before(j) / weight_all;
     int32_t lo = rb[j - 1], hi = rows;
     while (lo < hi) {
       const int32_t mid = lo + (hi - lo) / 2;
