@@ -83,7 +83,9 @@ int tacogb_device_status(int32_t* status);
  * rewritten on the device into a harmless one before the product runs, the error is returned
  * when the call ends (over host operands of 2^23 nonzeros or more, which are copied, checked
  * and multiplied chunk by chunk, with the position in the whole operand), and the result's
- * contents are then unspecified.  The device layer (tacogb_spmv
+ * contents are then unspecified.  tacogb_sddmm_compute does the same over host operands of
+ * 2^23 nonzeros or more with values kept at B's nonzeros and J <= 512 (D copied and
+ * transposed first, then B's rows with their rows of C chunk by chunk).  The device layer (tacogb_spmv
  * and the other functions on tacogb_csr) trusts its arguments; tacogb_csr_validate checks a
  * device CSR explicitly (declared with the device layer below).  tacogb_set_validation(0) turns
  * the taco-ABI checks off (and returns the previous setting); they are on by default. */

@@ -880,8 +880,9 @@ int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
 }
 
 // A CSR product over host operands as a pipeline (SpMV: dense operand x, result y; SpMM: B and
-// C, N values per row): the rows are cut into chunks of about equal nonzeros; one stream copies
-// the dense operand, pos and then every chunk's crd and values to the GPU, the library stream
+// C, N values per row; SDDMM: D, each chunk's rows of C, one value per nonzero): the rows are
+// cut into chunks of about equal nonzeros; one stream copies the dense operand, pos and then
+// every chunk's crd and values (and rows of the row operand) to the GPU, the library stream
 // checks and multiplies each chunk as soon as its copy has landed, and a third stream returns
 // each chunk's rows of the result.  The copies of later chunks overlap the checks, products and
 // returns of earlier ones, so the call takes little more than its copies (the host link bounds
@@ -896,7 +897,8 @@ constexpr int64_t kPipeMinNnz = (int64_t)1 << 23;  // below this, copy then comp
 
 // One kind of product of the pipeline.  reserve() takes any buffers it needs before the copies
 // are issued (an allocation later could wait on them); prepare() runs on the library stream
-// once the dense operand has landed; run() multiplies one chunk.
+// once the dense operand has landed; run() multiplies one chunk (rowop: the chunk's rows of the
+// row operand, when the product has one).
 struct ChunkProduct {
   virtual ~ChunkProduct() = default;
   virtual int reserve(int32_t /*cols*/, int32_t /*N*/, int32_t /*btype*/, int /*vt*/) { return 0; }
@@ -904,11 +906,12 @@ struct ChunkProduct {
     return 0;
   }
   virtual int run(const tacogb_csr* A, const void* dense, void* result, int32_t N, int32_t btype,
-                  cudaStream_t st) = 0;
+                  const void* rowop, cudaStream_t st) = 0;
 };
 
 struct SpmvChunks final : ChunkProduct {
-  int run(const tacogb_csr* A, const void* x, void* y, int32_t, int32_t, cudaStream_t st) override {
+  int run(const tacogb_csr* A, const void* x, void* y, int32_t, int32_t, const void*,
+          cudaStream_t st) override {
     return spmv_run(A, x, y, TACOGB_VARIANT_AUTO, st);
   }
 };
@@ -931,7 +934,7 @@ struct SpmmChunks final : ChunkProduct {
   int prepare(const void* B, int32_t cols, int32_t N, cudaStream_t st) override {
     return bdf ? spmm_split_once((const double*)B, cols, N, bdf, flag, st) : 0;
   }
-  int run(const tacogb_csr* A, const void* B, void* C, int32_t N, int32_t btype,
+  int run(const tacogb_csr* A, const void* B, void* C, int32_t N, int32_t btype, const void*,
           cudaStream_t st) override {
     if (bdf) return spmm_run_presplit(A, N, (const double*)B, bdf, flag, (double*)C, st);
     static const int df = spmm_variant_index("merge_w512_df");
@@ -939,10 +942,32 @@ struct SpmmChunks final : ChunkProduct {
   }
 };
 
+// SDDMM, values at B's nonzeros: the dense operand is D (J x K), transposed once when it lands;
+// the row operand is C (each chunk's rows); the result is one value per nonzero.
+struct SddmmChunks final : ChunkProduct {
+  void* dt = nullptr;
+  int vt = TACOGB_F64;
+  int reserve(int32_t cols, int32_t J, int32_t, int vtype) override {
+    vt = vtype;
+    dt = stage_buffer(61, sddmm_pre_bytes(J, cols, vtype));
+    return dt ? 0 : TACOGB_ERR_ALLOC;
+  }
+  int prepare(const void* D, int32_t cols, int32_t J, cudaStream_t st) override {
+    return sddmm_pre_transpose(D, J, cols, vt, dt, st);
+  }
+  int run(const tacogb_csr* B, const void* D, void* out, int32_t J, int32_t, const void* C,
+          cudaStream_t st) override {
+    return sddmm_pre_run(B, J, C, D, dt, out, st);
+  }
+};
+
+// rowop (optional): a host operand of rowop_row_bytes per row of A, copied chunk by chunk with
+// A's rows.  The result has res_unit_bytes per row of A, or per nonzero of A (res_per_nnz).
 int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int32_t rows,
                           int32_t cols, int32_t nnz, const void* dense, size_t dense_bytes,
-                          int32_t N, int32_t btype, void* result, size_t res_row_bytes,
-                          ChunkProduct& prod) {
+                          int32_t N, int32_t btype, void* result, size_t res_unit_bytes,
+                          ChunkProduct& prod, const void* rowop = nullptr,
+                          size_t rowop_row_bytes = 0, bool res_per_nnz = false) {
   const int32_t* pos = (const int32_t*)A->indices[1][0];
   const int32_t* crd = (const int32_t*)A->indices[1][1];
   const size_t vb = value_bytes(vt);
@@ -1005,9 +1030,14 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   int32_t* dcrd = (int32_t*)stage_buffer(1, (size_t)c * 4 + 64);
   unsigned char* dval = (unsigned char*)stage_buffer(2, (size_t)v * vb + 64);
   void* ddense = stage_buffer(3, dense_bytes + 64);
-  unsigned char* dres = (unsigned char*)stage_buffer(4, (size_t)rows * res_row_bytes + 64);
+  // results per nonzero sit at the chunks' value offsets (16-byte aligned per chunk)
+  unsigned char* dres = (unsigned char*)stage_buffer(
+      4, (res_per_nnz ? (size_t)v : (size_t)rows) * res_unit_bytes + 64);
+  unsigned char* drow =
+      rowop ? (unsigned char*)stage_buffer(9, (size_t)rows * rowop_row_bytes + 64) : nullptr;
   int64_t* dmeta = (int64_t*)stage_buffer(8, sizeof(meta));
-  if (!dpos || !dposc || !dcrd || !dval || !ddense || !dres || !dmeta) return TACOGB_ERR_ALLOC;
+  if (!dpos || !dposc || !dcrd || !dval || !ddense || !dres || !dmeta || (rowop && !drow))
+    return TACOGB_ERR_ALLOC;
   if (int rc = prod.reserve(cols, N, btype, vt)) return rc;
   // Every copy is issued up front on the host -> device stream.  A copy from pageable memory
   // returns only once it is (nearly) done, so with pageable operands a copier thread issues
@@ -1032,6 +1062,10 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
           e = copy_h2d(dval + voff[j] * vb, (const unsigned char*)A->vals + k0 * vb,
                        (size_t)n * vb, h2d);
       }
+      if (e == cudaSuccess && rowop && rb[j + 1] > rb[j])
+        e = copy_h2d(drow + (size_t)rb[j] * rowop_row_bytes,
+                     (const unsigned char*)rowop + (size_t)rb[j] * rowop_row_bytes,
+                     (size_t)(rb[j + 1] - rb[j]) * rowop_row_bytes, h2d);
       if (e == cudaSuccess) e = cudaEventRecord(ev[j], h2d);
       if (e == cudaSuccess) recorded.store(j, std::memory_order_release);
     }
@@ -1086,7 +1120,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   // that its returns are asynchronous copies like a pinned result's (a copy into pageable memory
   // completes before cudaMemcpyAsync returns, which holds the chunk loop); a larger one has its
   // pages mapped by host threads chunk by chunk before each chunk's return.
-  const size_t all_res = (size_t)rows * res_row_bytes;
+  const size_t all_res = (res_per_nnz ? (size_t)nnz : (size_t)rows) * res_unit_bytes;
   const bool map_pages = wants_page_mapping(result, all_res);
   bool registered = false;
   if (map_pages && all_res <= ((size_t)64 << 20)) {
@@ -1115,15 +1149,20 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
       rc = level_check_enqueue(nr, cols, cpos, ccrd, n, j, true, st);
       if (rc) break;
     }
-    rc = prod.run(&cj, ddense, dres + (size_t)rb[j] * res_row_bytes, N, btype, st);
+    // this chunk's result: rows rb[j].., or its nonzeros (at voff[j] here, pos[rb[j]] on the host)
+    const size_t r_dev = res_per_nnz ? (size_t)voff[j] : (size_t)rb[j];
+    const size_t r_host = res_per_nnz ? (size_t)pos[rb[j]] : (size_t)rb[j];
+    const size_t r_cnt = res_per_nnz ? (size_t)n : (size_t)nr;
+    rc = prod.run(&cj, ddense, dres + r_dev * res_unit_bytes, N, btype,
+                  drow ? drow + (size_t)rb[j] * rowop_row_bytes : nullptr, st);
     if (rc) break;
     if (!cu(cudaEventRecord(ev[kPipeChunks + j], st)) ||
         !cu(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0)))
       break;
-    unsigned char* hres = (unsigned char*)result + (size_t)rb[j] * res_row_bytes;
-    if (map_pages && !map_now && !registered) map_host_pages(hres, (size_t)nr * res_row_bytes);
-    if (nr && !cu(cudaMemcpyAsync(hres, dres + (size_t)rb[j] * res_row_bytes,
-                                  (size_t)nr * res_row_bytes, cudaMemcpyDeviceToHost, d2h)))
+    unsigned char* hres = (unsigned char*)result + r_host * res_unit_bytes;
+    if (map_pages && !map_now && !registered) map_host_pages(hres, r_cnt * res_unit_bytes);
+    if (r_cnt && !cu(cudaMemcpyAsync(hres, dres + r_dev * res_unit_bytes, r_cnt * res_unit_bytes,
+                                     cudaMemcpyDeviceToHost, d2h)))
       break;
   }
   if (copier.joinable()) copier.join();
@@ -1676,6 +1715,15 @@ int tacogb_sddmm_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, t
   int32_t nnz = 0;
   if (int rc = read_i32(pos + I, &nnz)) return rc;
   const bool dense = !is_csr_result(A);
+  // large host operands, values at B's nonzeros: D copied and transposed first, then B's rows
+  // with their rows of C copied, checked, multiplied and returned chunk by chunk
+  if (!dense && sddmm_pre_bytes(J, K, vt) > 0 &&
+      pipeline_applies(nnz, {pos, B->indices[1][1], B->vals, C->vals, D->vals, A->vals})) {
+    SddmmChunks chunks;
+    return csr_product_pipelined("sddmm operand B", B, vt, I, K, nnz, D->vals,
+                                 (size_t)J * K * vb, J, vt, A->vals, vb, chunks, C->vals,
+                                 (size_t)J * vb, true);
+  }
   cudaStream_t st = lib_stream();
   Operand opos, ocrd, ovals, oc, od;
   LevelCheck chk;

@@ -55,6 +55,14 @@ int sddmm_variant_count();
 const char* sddmm_variant_name(int v);
 int sddmm_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, void* out,
               int64_t out_ld, int variant, cudaStream_t st);
+// The same product in two steps over one transposed D (J <= 512, the default variant, values at
+// B's nonzeros): D transposed once into Dt (sddmm_pre_bytes of it), then any number of products
+// of row blocks of B (with their rows of C) against it.  sddmm_pre_bytes is 0 for J outside
+// (0, 512].
+size_t sddmm_pre_bytes(int32_t J, int32_t K, int vtype);
+int sddmm_pre_transpose(const void* D, int32_t J, int32_t K, int vtype, void* Dt, cudaStream_t st);
+int sddmm_pre_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, const void* Dt,
+                  void* out, cudaStream_t st);
 
 // Order-3 kernels (tensor3.cu); dense selects taco's dense result form.
 int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, int variant,

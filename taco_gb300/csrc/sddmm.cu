@@ -665,7 +665,96 @@ int sd_run(const tacogb_csr* B, int32_t J, const void* Cv, const void* Dv, void*
   return 0;
 }
 
+// The two-step form: D's transpose (flag cleared, then set by any value the pairs cannot carry)
+// and a product against it, one slab of j.
+template <class P>
+int sd_pre_transpose(const void* Dv, int32_t J, int32_t K, void* Dtv, cudaStream_t st) {
+  using V = typename P::V;
+  using DT = typename P::DT;
+  int JL, CH;
+  sd_shape(J, JL, CH);
+  const int32_t Jp = 32 * JL * CH;
+  int* dflag = nullptr;
+  if constexpr (P::kChecked) {
+    int* status = device_status();
+    if (!status) return last_code();
+    dflag = status + kDFlagWord;
+    TACOGB_CUDA_TRY(cudaMemsetAsync(dflag, 0, sizeof(int), st));
+  }
+  if (K == 0) return 0;
+  const dim3 tgrid((unsigned)((K + 31) / 32), (unsigned)(Jp / 32));
+  TACOGB_LAUNCH("sddmm_transpose", st,
+                (sddmm_transpose<V, DT><<<tgrid, dim3(32, 8), 0, st>>>(
+                    (const V*)Dv, (DT*)Dtv, J, K, K, Jp, dflag)));
+  return 0;
+}
+
+template <class P>
+int sd_pre_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, const void* Dt,
+               void* out, cudaStream_t st) {
+  using V = typename P::V;
+  if (B->nnz == 0) return 0;
+  int JL, CH;
+  sd_shape(J, JL, CH);
+  SdArgs<P> a;
+  a.pos = B->pos;
+  a.crd = B->crd;
+  a.bvals = (const V*)B->vals;
+  a.C = (const V*)C;
+  a.ldc = J;
+  a.Dt = (const typename P::DT*)Dt;
+  a.Jp = 32 * JL * CH;
+  a.D = (const V*)D;
+  a.ldd = B->cols;
+  a.Js = J;
+  a.acc = nullptr;
+  a.acc_in = 0;
+  a.acc_out = 0;
+  a.out = (V*)out;
+  a.out_ld = 0;
+  a.rows = B->rows;
+  a.nnz = B->nnz;
+  a.dflag = nullptr;
+  if constexpr (P::kChecked) {
+    int* status = device_status();
+    if (!status) return last_code();
+    a.dflag = status + kDFlagWord;
+  }
+  return sd_dispatch<P>(a, JL, CH, 0, st);
+}
+
 }  // namespace
+
+size_t sddmm_pre_bytes(int32_t J, int32_t K, int vtype) {
+  if (J <= 0 || J > kSdSlab || K < 0) return 0;
+  int JL, CH;
+  sd_shape(J, JL, CH);
+  const size_t dt = vtype == TACOGB_F32 ? sizeof(float) : sizeof(DF);  // the default policies
+  return ((size_t)K * (size_t)(32 * JL * CH) * dt + 255) & ~(size_t)255;
+}
+
+int sddmm_pre_transpose(const void* D, int32_t J, int32_t K, int vtype, void* Dt,
+                        cudaStream_t st) {
+  TACOGB_CHECK_ARG(J > 0 && J <= kSdSlab && K >= 0, "SDDMM: two-step form needs 0 < J <= %d",
+                   kSdSlab);
+  TACOGB_CHECK_ARG(vtype == TACOGB_F64 || vtype == TACOGB_F32, "SDDMM: unsupported value type %d",
+                   vtype);
+  return vtype == TACOGB_F32 ? sd_pre_transpose<Sd32>(D, J, K, Dt, st)
+                             : sd_pre_transpose<SdDFS>(D, J, K, Dt, st);
+}
+
+int sddmm_pre_run(const tacogb_csr* B, int32_t J, const void* C, const void* D, const void* Dt,
+                  void* out, cudaStream_t st) {
+  TACOGB_CHECK_ARG(B != nullptr && B->rows >= 0 && B->cols >= 0 && B->nnz >= 0,
+                   "SDDMM: bad matrix");
+  TACOGB_CHECK_ARG(J > 0 && J <= kSdSlab, "SDDMM: two-step form needs 0 < J <= %d", kSdSlab);
+  TACOGB_CHECK_ARG(B->vtype == TACOGB_F64 || B->vtype == TACOGB_F32,
+                   "SDDMM: unsupported value type %d", B->vtype);
+  TACOGB_CHECK_ARG(B->nnz == 0 || (B->pos && B->crd && B->vals && C && D && Dt && out),
+                   "SDDMM: null array");
+  return B->vtype == TACOGB_F32 ? sd_pre_run<Sd32>(B, J, C, D, Dt, out, st)
+                                : sd_pre_run<SdDFS>(B, J, C, D, Dt, out, st);
+}
 
 int sddmm_variant_count() { return kNumSddmmVariants; }
 const char* sddmm_variant_name(int v) {

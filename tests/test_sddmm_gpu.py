@@ -243,3 +243,72 @@ def test_dropin_module_shim_compute():
     L._shim_compute.argtypes = [ctypes.c_void_p]
     assert L._shim_compute(args) == 0
     assert np.array_equal(out, A)
+
+
+# ---- the pipelined ABI: host operands of 2^23 nonzeros or more, values at B's nonzeros ----
+
+def _pipelined_case(J, seed, rows=300000):
+    """The SDDMM power-law law (mean 32 per row) at 300,000 rows: 9.6e6 nonzeros."""
+    s = W.spmm_powerlaw(rows=rows)
+    pos, crd, vals = W.generate(s)
+    assert len(crd) >= 1 << 23
+    C = W.dense(seed, s.rows * J).reshape(s.rows, J)
+    D = W.dense(seed + 1, J * s.cols).reshape(J, s.cols)
+    return pos, crd, vals, C, D, s.cols
+
+
+def _abi_sampled(pos, crd, vals, C, D, K, dtype=np.float64):
+    """tacogb_sddmm_compute on host (pageable) arrays into a CSR result with B's pattern."""
+    I, J = C.shape
+    v = vals.astype(dtype)
+    Cc, Dd = np.ascontiguousarray(C.astype(dtype)), np.ascontiguousarray(D.astype(dtype))
+    out = np.full(len(crd), np.nan, dtype)
+    Bt, At = T.csr(pos, crd, v, [I, K]), T.csr(pos, crd, out, [I, K])
+    Ct, Dt = T.dense(Cc, [I, J]), T.dense(Dd, [J, K])
+    return tg.lib().tacogb_sddmm_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr), out
+
+
+@pytest.mark.parametrize("J", [32, 128])
+def test_abi_pipelined_host_operands(J):
+    """D copied and transposed first, then B's rows with their rows of C chunk by chunk: the
+    oracle's values, on two calls in a row."""
+    pos, crd, vals, C, D, K = _pipelined_case(J, 71)
+    ref = O.sddmm_sampled(pos, crd, vals, C, D)
+    for _ in range(2):
+        rc, got = _abi_sampled(pos, crd, vals, C, D, K)
+        assert rc == 0, tg.lib().tacogb_last_error()
+        assert normwise(got, ref) <= F64_TOL
+
+
+def test_abi_pipelined_fp32():
+    pos, crd, vals, C, D, K = _pipelined_case(64, 73)
+    r32 = lambda a: a.astype(np.float32).astype(np.float64)  # noqa: E731
+    ref = O.sddmm_sampled(pos, crd, r32(vals), r32(C), r32(D))
+    rc, got = _abi_sampled(pos, crd, vals, C, D, K, np.float32)
+    assert rc == 0, tg.lib().tacogb_last_error()
+    assert normwise(got.astype(np.float64), ref) <= F32_TOL
+
+
+def test_abi_pipelined_double_float_range():
+    """A D value outside the double-float pairs' range, seen by the one transpose of D, sends
+    every chunk's groups to native FP64."""
+    pos, crd, vals, C, D, K = _pipelined_case(32, 75)
+    D = D.copy()
+    D[3, 1000] = 3e45
+    ref = O.sddmm_sampled(pos, crd, vals, C, D)
+    rc, got = _abi_sampled(pos, crd, vals, C, D, K)
+    assert rc == 0, tg.lib().tacogb_last_error()
+    m = crd == 1000  # the nonzeros that meet the large value, compared on their own
+    assert m.any() and normwise(got[m], ref[m]) <= F64_TOL
+    assert normwise(got[~m], ref[~m]) <= F64_TOL
+
+
+def test_abi_pipelined_rejects_a_corrupt_late_chunk():
+    pos, crd, vals, C, D, K = _pipelined_case(32, 77)
+    bad = crd.copy()
+    bad[len(bad) - 1000] = K + 5  # in the last chunk
+    rc, _ = _abi_sampled(pos, bad, vals, C, D, K)
+    assert rc == 1
+    assert b"out of range at position %d" % (len(bad) - 1000) in tg.lib().tacogb_last_error()
+    rc, got = _abi_sampled(pos, crd, vals, C, D, K)  # usable right after
+    assert rc == 0 and normwise(got, O.sddmm_sampled(pos, crd, vals, C, D)) <= F64_TOL
