@@ -1600,12 +1600,65 @@ int tacogb_pack_taco(taco_tensor_t* T, const void* buffer, int64_t n) {
   int32_t* dcrd = (int32_t*)stage_buffer(15, (size_t)n * 4);
   void* dvals = stage_buffer(16, (size_t)n * vb);
   if (!dr || !dc || !dv || !dpos || !dcrd || !dvals) return TACOGB_ERR_ALLOC;
-  if (int rc = pack_split_records(in.dev, n, vt, dr, dc, dv, st)) return rc;
+  // Large host results (taco frees them) are allocated now at their upper bound, n entries
+  // (duplicates only lower the count), and host threads map their pages while the GPU packs:
+  // the returns then land in mapped memory instead of faulting page by page inside the copies
+  // (1.0e8 coordinates: the pages of the 1.2 GB of results take about 10 ms to map).
+  const bool premap = !managed && (size_t)n * (4 + vb) >= ((size_t)64 << 20);
+  int32_t* pos = nullptr;
+  int32_t* crd = nullptr;
+  void* vals = nullptr;
+  std::thread mapper;
+  if (premap) {
+    pos = (int32_t*)alloc_result(((size_t)rows + 1) * 4, false);
+    crd = (int32_t*)alloc_result((size_t)n * 4, false);
+    vals = alloc_result((size_t)n * vb, false);
+    if (!pos || !crd || !vals) {
+      free(pos);
+      free(crd);
+      free(vals);
+      return TACOGB_ERR_ALLOC;
+    }
+    mapper = std::thread([=] {
+      spread_thread();
+      map_host_pages(pos, ((size_t)rows + 1) * 4);
+      map_host_pages(crd, (size_t)n * 4);
+      map_host_pages(vals, (size_t)n * vb);
+    });
+  }
+  auto fail = [&](int rc) {  // every return after the mapper started
+    if (mapper.joinable()) mapper.join();
+    if (premap) {
+      free(pos);
+      free(crd);
+      free(vals);
+    }
+    return rc;
+  };
   int64_t nnz = 0;
-  if (int rc = pack_csr(rows, cols, n, dr, dc, dv, vt, dpos, dcrd, dvals, &nnz, st)) return rc;
-  int32_t* pos = (int32_t*)alloc_result(((size_t)rows + 1) * 4, managed);
-  int32_t* crd = (int32_t*)alloc_result((size_t)nnz * 4, managed);
-  void* vals = alloc_result((size_t)nnz * vb, managed);
+  if (int rc = pack_split_records(in.dev, n, vt, dr, dc, dv, st)) return fail(rc);
+  if (int rc = pack_csr(rows, cols, n, dr, dc, dv, vt, dpos, dcrd, dvals, &nnz, st))
+    return fail(rc);
+  if (premap) {
+    mapper.join();
+    cudaError_t e = cudaMemcpyAsync(pos, dpos, ((size_t)rows + 1) * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nnz)
+      e = cudaMemcpyAsync(crd, dcrd, (size_t)nnz * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nnz)
+      e = cudaMemcpyAsync(vals, dvals, (size_t)nnz * vb, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      set_error(TACOGB_ERR_CUDA, "pack: %s", cudaGetErrorString(e));
+      return fail(TACOGB_ERR_CUDA);
+    }
+    T->indices[1][0] = (uint8_t*)pos;
+    T->indices[1][1] = (uint8_t*)crd;
+    T->vals = (uint8_t*)vals;
+    return 0;
+  }
+  pos = (int32_t*)alloc_result(((size_t)rows + 1) * 4, managed);
+  crd = (int32_t*)alloc_result((size_t)nnz * 4, managed);
+  vals = alloc_result((size_t)nnz * vb, managed);
   if (!pos || !crd || !vals) return TACOGB_ERR_ALLOC;
   TACOGB_CUDA_TRY(cudaMemcpyAsync(pos, dpos, ((size_t)rows + 1) * 4, cudaMemcpyDefault, st));
   if (nnz && managed) {

@@ -142,6 +142,30 @@ def test_taco_buffer_entry_large_host():
     assert_same(got, (pos, crd, vals))
 
 
+def test_taco_buffer_entry_large_host_duplicates():
+    """Large host results are allocated for every record before the count of distinct ones is
+    known: with many duplicates the arrays are longer than nnz, and pos, crd and values still
+    equal the oracle's (duplicates summed in input order)."""
+    rng = np.random.default_rng(9)
+    rows, cols, n = 200000, 300000, 6000000
+    pool = 2000000
+    pr, pc = rng.integers(0, rows, pool), rng.integers(0, cols, pool)
+    k = rng.integers(0, pool, n)
+    ri, ci, v = pr[k].astype(np.int32), pc[k].astype(np.int32), rng.uniform(-1, 1, n)
+    assert n * 12 >= 64 << 20
+    ref = O.pack_csr(rows, cols, ri, ci, v)
+    nnz = len(ref[1])
+    assert nnz < n
+    rec = _records(ri, ci, v)
+    Tt = T.csr_result([rows, cols])
+    assert tg.lib().tacogb_pack_taco(Tt.ptr, rec.ctypes.data, n) == 0, tg.lib().tacogb_last_error()
+    P = ctypes.POINTER
+    got = (np.ctypeslib.as_array(ctypes.cast(Tt.index(1, 0), P(ctypes.c_int32)), (rows + 1,)),
+           np.ctypeslib.as_array(ctypes.cast(Tt.index(1, 1), P(ctypes.c_int32)), (nnz,)),
+           np.ctypeslib.as_array(ctypes.cast(Tt.vals_ptr, P(ctypes.c_double)), (nnz,)))
+    assert_same(got, ref)
+
+
 @pytest.mark.parametrize("name", ["read_general.mtx", "read_symmetric.mtx", "read_array.mtx",
                                   "read_plain.tns", "read_rua32.rb"])
 def test_read_csr_matches_taco(name):
