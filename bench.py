@@ -1551,13 +1551,18 @@ def main():
         if world > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
+        calls = []  # each call's own time: the host link is shared, so a few calls can stall
         for _ in range(args.e2e_steps):
+            tc = time.perf_counter()
             astep()
+            calls.append(time.perf_counter() - tc)
         e2e_s = max_over_ranks(torch, time.perf_counter() - t0, world)
         e2e = {"value": whole_job_rate(work, args.e2e_steps, world, e2e_s) / 1e9,
                "unit": unit,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "steps": args.e2e_steps, "ms_per_step": e2e_s / args.e2e_steps * 1e3, "api": api}
+               "steps": args.e2e_steps, "ms_per_step": e2e_s / args.e2e_steps * 1e3, "api": api,
+               "call_ms_median": float(np.median(calls)) * 1e3,
+               "call_ms_min": float(min(calls)) * 1e3}
         del akeep
         e2e["link"] = host_link(torch, h2d, d2h)
 

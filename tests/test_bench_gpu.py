@@ -36,6 +36,7 @@ def test_small_spmv_line(graph):
     assert d["gpu_launches"] == steps
     assert ("CUDA-graph" in d["timing"]) == graph
     assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
+    assert 0 < d["e2e"]["call_ms_min"] <= d["e2e"]["call_ms_median"]
     # the gather roofline counts gathers alone and every L2 sector moved; the second is larger
     g = d["roofline"]["gather"]
     assert g["unit"] == "gathers/s" and g["l2_sectors"]["unit"] == "sectors/s"
