@@ -85,7 +85,9 @@ int tacogb_device_status(int32_t* status);
  * and multiplied chunk by chunk, with the position in the whole operand), and the result's
  * contents are then unspecified.  tacogb_sddmm_compute does the same over host operands of
  * 2^23 nonzeros or more with values kept at B's nonzeros and J <= 512 (D copied and
- * transposed first, then B's rows with their rows of C chunk by chunk).  The device layer (tacogb_spmv
+ * transposed first, then B's rows with their rows of C chunk by chunk), and so does
+ * tacogb_mttkrp_compute when B's fiber level holds 2^23 nonzeros or more (that level chunk by
+ * chunk, the upper levels checked after it).  The device layer (tacogb_spmv
  * and the other functions on tacogb_csr) trusts its arguments; tacogb_csr_validate checks a
  * device CSR explicitly (declared with the device layer below).  tacogb_set_validation(0) turns
  * the taco-ABI checks off (and returns the previous setting); they are on by default. */

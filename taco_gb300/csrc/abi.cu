@@ -961,13 +961,26 @@ struct SddmmChunks final : ChunkProduct {
   }
 };
 
+// MTTKRP's fiber product: the fiber level (a CSR of fibers over B's last mode) times D, one row
+// of J values per fiber, kept on the device for the combine.
+struct FiberSpmmChunks final : ChunkProduct {
+  int run(const tacogb_csr* F, const void* D, void* T, int32_t J, int32_t, const void*,
+          cudaStream_t st) override {
+    static const int v = spmm_variant_index("stream_w512_dfs");  // as mttkrp_run
+    return spmm_run(F, J, D, F->vtype, T, v, st);
+  }
+};
+
 // rowop (optional): a host operand of rowop_row_bytes per row of A, copied chunk by chunk with
 // A's rows.  The result has res_unit_bytes per row of A, or per nonzero of A (res_per_nnz).
+// dev_result (optional): a device buffer that keeps the result (rows of A, in order) for a
+// later step on the library stream; nothing is returned to the host then.
 int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int32_t rows,
                           int32_t cols, int32_t nnz, const void* dense, size_t dense_bytes,
                           int32_t N, int32_t btype, void* result, size_t res_unit_bytes,
                           ChunkProduct& prod, const void* rowop = nullptr,
-                          size_t rowop_row_bytes = 0, bool res_per_nnz = false) {
+                          size_t rowop_row_bytes = 0, bool res_per_nnz = false,
+                          void* dev_result = nullptr) {
   const int32_t* pos = (const int32_t*)A->indices[1][0];
   const int32_t* crd = (const int32_t*)A->indices[1][1];
   const size_t vb = value_bytes(vt);
@@ -1031,8 +1044,10 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   unsigned char* dval = (unsigned char*)stage_buffer(2, (size_t)v * vb + 64);
   void* ddense = stage_buffer(3, dense_bytes + 64);
   // results per nonzero sit at the chunks' value offsets (16-byte aligned per chunk)
-  unsigned char* dres = (unsigned char*)stage_buffer(
-      4, (res_per_nnz ? (size_t)v : (size_t)rows) * res_unit_bytes + 64);
+  unsigned char* dres =
+      dev_result ? (unsigned char*)dev_result
+                 : (unsigned char*)stage_buffer(
+                       4, (res_per_nnz ? (size_t)v : (size_t)rows) * res_unit_bytes + 64);
   unsigned char* drow =
       rowop ? (unsigned char*)stage_buffer(9, (size_t)rows * rowop_row_bytes + 64) : nullptr;
   int64_t* dmeta = (int64_t*)stage_buffer(8, sizeof(meta));
@@ -1121,7 +1136,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   // completes before cudaMemcpyAsync returns, which holds the chunk loop); a larger one has its
   // pages mapped by host threads chunk by chunk before each chunk's return.
   const size_t all_res = (res_per_nnz ? (size_t)nnz : (size_t)rows) * res_unit_bytes;
-  const bool map_pages = wants_page_mapping(result, all_res);
+  const bool map_pages = !dev_result && wants_page_mapping(result, all_res);
   bool registered = false;
   if (map_pages && all_res <= ((size_t)64 << 20)) {
     registered = cudaHostRegister(result, all_res, cudaHostRegisterDefault) == cudaSuccess;
@@ -1156,6 +1171,7 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     rc = prod.run(&cj, ddense, dres + r_dev * res_unit_bytes, N, btype,
                   drow ? drow + (size_t)rb[j] * rowop_row_bytes : nullptr, st);
     if (rc) break;
+    if (dev_result) continue;
     if (!cu(cudaEventRecord(ev[kPipeChunks + j], st)) ||
         !cu(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0)))
       break;
@@ -1864,7 +1880,9 @@ int check_dense_order(const taco_tensor_t* t, int order, const char* name) {
 
 // B's arrays as a tacogb_csf3 on the device (host arrays staged in slots base + 1 .. base + 5
 // and base + 60 .. base + 62), each level checked on the way (stage_checked_level).
-int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3& out) {
+// leaf = false stages only levels 0 and 1 (pos2, crd2 and the values stay null in out).
+int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3& out,
+                 bool leaf = true) {
   TACOGB_CHECK_ARG(T != nullptr && T->order == 3 && T->dimensions && T->mode_types && T->indices,
                    "order-3 operand B: expected an order-3 tensor");
   const bool dense0 = T->mode_types[0] == taco_mode_dense;
@@ -1914,15 +1932,17 @@ int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3&
   if (int rc = stage_checked_level("order-3 operand B level 1", b.n0, b.dims[1], b.nfib, pos1,
                                    crd1, nullptr, 0, base + 1, st, op1, oc1, nullptr))
     return rc;
-  if (int rc = stage_checked_level("order-3 operand B level 2", b.nfib, b.dims[2], b.nnz, pos2,
-                                   crd2, T->vals, (size_t)b.nnz * value_bytes(vt), base + 3, st,
-                                   op2, oc2, &ov))
-    return rc;
   b.pos1 = (const int32_t*)op1.dev;
   b.crd1 = (const int32_t*)oc1.dev;
-  b.pos2 = (const int32_t*)op2.dev;
-  b.crd2 = (const int32_t*)oc2.dev;
-  b.vals = ov.dev;
+  if (leaf) {
+    if (int rc = stage_checked_level("order-3 operand B level 2", b.nfib, b.dims[2], b.nnz, pos2,
+                                     crd2, T->vals, (size_t)b.nnz * value_bytes(vt), base + 3, st,
+                                     op2, oc2, &ov))
+      return rc;
+    b.pos2 = (const int32_t*)op2.dev;
+    b.crd2 = (const int32_t*)oc2.dev;
+    b.vals = ov.dev;
+  }
   out = b;
   return 0;
 }
@@ -2060,10 +2080,74 @@ int tacogb_mttkrp_assemble(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C,
   if (int rc = check_mttkrp(A, B, C, D)) return rc;
   return t3_assemble(A, B, (size_t)A->dimensions[0] * A->dimensions[1]);
 }
+// MTTKRP over large host operands: the fiber level (pos2, crd2, values: nearly all of B's
+// bytes) is copied chunk by chunk and multiplied by D as it lands, into fiber rows kept on the
+// device; then B's upper levels and C are staged, the combine runs and A comes back.
+int mttkrp_pipelined(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D,
+                     int32_t J, int vt, bool* applied) {
+  *applied = false;
+  const size_t vb = value_bytes(vt);
+  const bool dense0 = B->mode_types[0] == taco_mode_dense;
+  const int32_t* pos0 = dense0 ? nullptr : (const int32_t*)B->indices[0][0];
+  const int32_t* pos1 = (const int32_t*)B->indices[1][0];
+  const int32_t* pos2 = (const int32_t*)B->indices[2][0];
+  std::initializer_list<const void*> arrays = {
+      pos1, B->indices[1][1], pos2, B->indices[2][1], B->vals, C->vals, D->vals, A->vals,
+      dense0 ? (const void*)B->vals : (const void*)pos0,
+      dense0 ? (const void*)B->vals : (const void*)B->indices[0][1]};
+  for (const void* p : arrays)
+    if (p == nullptr || device_accessible(p)) return 0;
+  const int32_t n0 = dense0 ? B->dimensions[0] : pos0[1];
+  TACOGB_CHECK_ARG(n0 >= 0 && (dense0 || pos0[0] == 0), "order-3 operand B: bad level-0 pos");
+  const int32_t nfib = pos1[n0];
+  TACOGB_CHECK_ARG(nfib >= 0, "order-3 operand B: negative fiber count");
+  const int32_t nnz = pos2[nfib];
+  if (!pipeline_applies(nnz, arrays) || J <= 0) return 0;
+  *applied = true;
+  // the fiber level as a CSR of fibers (rows) over B's last mode
+  int32_t fdims[2] = {nfib, B->dimensions[2]};
+  taco_mode_t ftypes[2] = {taco_mode_dense, taco_mode_sparse};
+  uint8_t* fl1[2] = {B->indices[2][0], B->indices[2][1]};
+  uint8_t** fidx[2] = {nullptr, fl1};
+  taco_tensor_t F{};
+  F.order = 2;
+  F.dimensions = fdims;
+  F.csize = B->csize;
+  F.mode_types = ftypes;
+  F.indices = fidx;
+  F.vals = B->vals;
+  void* T = stage_buffer(40, (size_t)nfib * J * vb + 64);
+  if (!T) return TACOGB_ERR_ALLOC;
+  FiberSpmmChunks fibers;
+  if (int rc = csr_product_pipelined("order-3 operand B level 2", &F, vt, nfib, B->dimensions[2],
+                                     nnz, D->vals, (size_t)B->dimensions[2] * J * vb, J, vt,
+                                     nullptr, (size_t)J * vb, fibers, nullptr, 0, false, T))
+    return rc;
+  cudaStream_t st = lib_stream();
+  tacogb_csf3 b;
+  if (int rc = csf3_operand(B, 30, st, b, false)) return rc;
+  b.nnz = nnz;
+  Operand oc;
+  if (int rc = stage_in(oc, C->vals, (size_t)C->dimensions[0] * J * vb, 37, st)) return rc;
+  const size_t abytes = (size_t)A->dimensions[0] * J * vb;
+  void* adev = stage_buffer(39, abytes + 64);
+  if (!adev) return TACOGB_ERR_ALLOC;
+  if (abytes) TACOGB_CUDA_TRY(cudaMemsetAsync(adev, 0, abytes, st));
+  if (int rc = mttkrp_combine_launch(&b, J, oc.dev, T, adev, st)) return rc;
+  if (abytes) TACOGB_CUDA_TRY(cudaMemcpyAsync(A->vals, adev, abytes, cudaMemcpyDeviceToHost, st));
+  TACOGB_CUDA_TRY(cudaStreamSynchronize(st));
+  return consume_device_status();
+}
+
 int tacogb_mttkrp_compute(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_tensor_t* D) {
   if (int rc = check_mttkrp(A, B, C, D)) return rc;
   const size_t vb = vbytes_of(B);
   const int32_t J = A->dimensions[1];
+  {
+    bool applied = false;
+    const int rc = mttkrp_pipelined(A, B, C, D, J, value_type_of_csize(B->csize), &applied);
+    if (applied || rc) return rc;
+  }
   taco_tensor_t* ops[2] = {C, D};
   const size_t ob[2] = {(size_t)C->dimensions[0] * J * vb, (size_t)D->dimensions[0] * J * vb};
   return t3_compute(A, B, (size_t)A->dimensions[0] * J * vb, 2, ops, ob,

@@ -69,6 +69,10 @@ int ttv_run(const tacogb_csf3* B, const void* c, void* out, bool dense, int vari
             cudaStream_t st);
 int ttm_run(const tacogb_csf3* B, int32_t L, const void* C, void* out, bool dense, int variant,
             cudaStream_t st);
+// MTTKRP's second step alone: A (already zeroed) += C rows times the fiber rows T (nfib x J,
+// the fiber level times D); reads only B's upper levels (crd0, pos1, crd1) and its sizes.
+int mttkrp_combine_launch(const tacogb_csf3* B, int32_t J, const void* C, const void* T, void* A,
+                          cudaStream_t st);
 int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, void* A,
                int variant, cudaStream_t st);
 

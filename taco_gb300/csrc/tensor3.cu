@@ -404,6 +404,12 @@ int mttkrp_run(const tacogb_csf3* B, int32_t J, const void* C, const void* D, vo
   // J = 32: 4.02 ms against 4.42 for the library's SpMM default)
   if (variant < 0) variant = spmm_variant_index("stream_w512_dfs");
   if (int rc = spmm_run(&f, J, D, B->vtype, T, variant, st)) return rc;
+  return mttkrp_combine_launch(B, J, C, T, A, st);
+}
+
+int mttkrp_combine_launch(const tacogb_csf3* B, int32_t J, const void* C, const void* T, void* A,
+                          cudaStream_t st) {
+  if ((int64_t)B->nfib * J == 0 || B->n0 == 0 || B->nnz == 0) return 0;
   const int64_t threads = (((int64_t)B->nfib + kCombFibers - 1) / kCombFibers) * 32;
   if (B->vtype == TACOGB_F64)
     TACOGB_LAUNCH("t3_mttkrp_combine", st,

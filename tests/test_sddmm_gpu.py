@@ -257,25 +257,29 @@ def _pipelined_case(J, seed, rows=300000):
     return pos, crd, vals, C, D, s.cols
 
 
-def _abi_sampled(pos, crd, vals, C, D, K, dtype=np.float64):
-    """tacogb_sddmm_compute on host (pageable) arrays into a CSR result with B's pattern."""
+def _abi_sampled(pos, crd, vals, C, D, K, dtype=np.float64, pinned=False):
+    """tacogb_sddmm_compute on host arrays (pageable numpy, or pinned torch) into a CSR result
+    with B's pattern."""
     I, J = C.shape
-    v = vals.astype(dtype)
-    Cc, Dd = np.ascontiguousarray(C.astype(dtype)), np.ascontiguousarray(D.astype(dtype))
-    out = np.full(len(crd), np.nan, dtype)
-    Bt, At = T.csr(pos, crd, v, [I, K]), T.csr(pos, crd, out, [I, K])
+    host = (lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()) if pinned else (
+        lambda a: np.ascontiguousarray(a))
+    p, c = host(pos), host(crd)
+    v, Cc, Dd = host(vals.astype(dtype)), host(C.astype(dtype)), host(D.astype(dtype))
+    out = host(np.full(len(crd), np.nan, dtype))
+    Bt, At = T.csr(p, c, v, [I, K]), T.csr(p, c, out, [I, K])
     Ct, Dt = T.dense(Cc, [I, J]), T.dense(Dd, [J, K])
-    return tg.lib().tacogb_sddmm_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr), out
+    rc = tg.lib().tacogb_sddmm_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr)
+    return rc, (out.numpy() if pinned else out)
 
 
-@pytest.mark.parametrize("J", [32, 128])
-def test_abi_pipelined_host_operands(J):
+@pytest.mark.parametrize("J,pinned", [(32, False), (128, False), (128, True)])
+def test_abi_pipelined_host_operands(J, pinned):
     """D copied and transposed first, then B's rows with their rows of C chunk by chunk: the
-    oracle's values, on two calls in a row."""
+    oracle's values, on two calls in a row (pageable operands go through the copier thread)."""
     pos, crd, vals, C, D, K = _pipelined_case(J, 71)
     ref = O.sddmm_sampled(pos, crd, vals, C, D)
     for _ in range(2):
-        rc, got = _abi_sampled(pos, crd, vals, C, D, K)
+        rc, got = _abi_sampled(pos, crd, vals, C, D, K, pinned=pinned)
         assert rc == 0, tg.lib().tacogb_last_error()
         assert normwise(got, ref) <= F64_TOL
 

@@ -271,3 +271,65 @@ def test_rejects_bad_shapes():
     Ct, Dt = T.dense(C, list(C.shape)), T.dense(g["D"], list(g["D"].shape))
     At = T.dense_result([g["A"].shape[0], 32])
     assert tg.lib().tacogb_mttkrp_evaluate(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr) != 0
+
+
+# ---- the pipelined ABI: host operands whose fiber level holds 2^23 nonzeros or more ----
+
+def _pipelined_tensor():
+    """The bench tensor's law on smaller modes: 3,000 x 2,000 x 30,000, about 9.6e6 nonzeros."""
+    B = W.tensor3_powerlaw(dims=(3000, 2000, 30000), fib_mean=100.0, leaf_mean=32.0)
+    assert len(B[5]) >= 1 << 23
+    return B
+
+
+def _abi_mttkrp(B, C, D, dtype=np.float64, dense0=False):
+    dims, crd0, pos1, crd1, pos2, crd2, vals = B
+    J = C.shape[1]
+    Bt = taco_csf3_tensor((dims, crd0, pos1, crd1, pos2, crd2, vals.astype(dtype)), dense0=dense0)
+    Cc, Dd = np.ascontiguousarray(C.astype(dtype)), np.ascontiguousarray(D.astype(dtype))
+    Ct, Dt = T.dense(Cc, [dims[1], J]), T.dense(Dd, [dims[2], J])
+    A = np.full((dims[0], J), np.nan, dtype)
+    At = T.dense(A, [dims[0], J])
+    return tg.lib().tacogb_mttkrp_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr), A
+
+
+@pytest.mark.parametrize("J,dense0", [(16, False), (32, False), (32, True)])
+def test_abi_pipelined_mttkrp(J, dense0):
+    """The fiber level copied and multiplied by D chunk by chunk into fiber rows on the device,
+    then the upper levels, C and the combine: the oracle's A, on two calls in a row."""
+    B = _pipelined_tensor()
+    dims = B[0]
+    C = W.dense(81, dims[1] * J).reshape(dims[1], J)
+    D = W.dense(82, dims[2] * J).reshape(dims[2], J)
+    ref = O.mttkrp(B, C, D)
+    for _ in range(2):
+        rc, A = _abi_mttkrp(B, C, D, dense0=dense0)
+        assert rc == 0, tg.lib().tacogb_last_error()
+        assert normwise(A, ref) <= F64_TOL
+
+
+def test_abi_pipelined_mttkrp_fp32():
+    B = _pipelined_tensor()
+    dims, J = B[0], 16
+    r32 = lambda a: a.astype(np.float32).astype(np.float64)  # noqa: E731
+    C = W.dense(83, dims[1] * J).reshape(dims[1], J)
+    D = W.dense(84, dims[2] * J).reshape(dims[2], J)
+    ref = O.mttkrp(B[:6] + (r32(B[6]),), r32(C), r32(D))
+    rc, A = _abi_mttkrp(B, C, D, np.float32)
+    assert rc == 0, tg.lib().tacogb_last_error()
+    assert normwise(A.astype(np.float64), ref) <= F32_TOL
+
+
+def test_abi_pipelined_mttkrp_rejects_a_corrupt_fiber_chunk():
+    B = list(_pipelined_tensor())
+    dims = B[0]
+    crd2 = B[5].copy()
+    crd2[len(crd2) - 700] = dims[2] + 9  # in the last chunk of the fiber level
+    B[5] = crd2
+    J = 16
+    C = W.dense(85, dims[1] * J).reshape(dims[1], J)
+    D = W.dense(86, dims[2] * J).reshape(dims[2], J)
+    rc, _ = _abi_mttkrp(tuple(B), C, D)
+    assert rc == 1
+    err = tg.lib().tacogb_last_error()
+    assert b"level 2" in err and b"out of range at position %d" % (len(crd2) - 700) in err
