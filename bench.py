@@ -1381,6 +1381,10 @@ SECONDARY = [
                            "--e2e-steps", "3"]),
     ("batched_spmv_4096_f32c_learned", ["--workload", "batched_spmv", "--dtype", "f32",
                                         "--select", "learned", "--steps", "5", "--warmup", "3"]),
+    ("sddmm_powerlaw_j128_f64", ["--workload", "sddmm_powerlaw", "--steps", "10", "--warmup", "3",
+                                 "--e2e-steps", "5"]),
+    ("mttkrp_nell2_r32_f64", ["--workload", "mttkrp_nell2", "--steps", "20", "--warmup", "3",
+                              "--e2e-steps", "5"]),
 ]
 
 
