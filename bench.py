@@ -1550,7 +1550,7 @@ def main():
     abi = op.abi(torch, tg, T) if args.e2e_steps > 0 else None
     if abi is not None:
         astep, akeep, h2d, d2h, api = abi
-        for _ in range(2):
+        for _ in range(3):  # untimed, like the device steps' warm-up (first calls allocate)
             astep()
         if world > 1:
             torch.distributed.barrier()
