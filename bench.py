@@ -1694,15 +1694,21 @@ def gather_roofline(torch, L, nnz, kernel_ms, streamed_bytes):
     y), against the probe's gathers plus its index reads (one sector per eight gathers)."""
     ceiling, sms = gather_ceiling(torch, L)
     achieved = nnz / (kernel_ms / 1e3)
-    sectors = (nnz + streamed_bytes / 32) / (kernel_ms / 1e3)
-    probe_sectors = ceiling * (1 + 1 / 8)
     return {"achieved": achieved, "peak": ceiling, "unit": "gathers/s", "frac": achieved / ceiling,
             "floor_ms": nnz / ceiling * 1e3,
             "probe": "tacogb_probe_gather: random 8-byte ld.global.cg from a 32 MiB L2-resident "
                      "table, 160 KB shared memory held per SM (carveout 70 %), as the kernel",
-            "l2_sectors": {"achieved": sectors, "peak": probe_sectors, "unit": "sectors/s",
-                           "frac": sectors / probe_sectors,
-                           "floor_ms": (nnz + streamed_bytes / 32) / probe_sectors * 1e3}}
+            "l2_sectors": l2_sector_roofline(nnz, streamed_bytes, kernel_ms, ceiling)}
+
+
+def l2_sector_roofline(nnz, streamed_bytes, kernel_ms, probe_gathers_per_s):
+    """32-byte L2 sectors per second: the SpMV's one per x gather plus its streamed bytes, against
+    the gather probe's one per gather plus its index reads (eight 4-byte indices per sector)."""
+    sectors = nnz + streamed_bytes / 32
+    achieved = sectors / (kernel_ms / 1e3)
+    peak = probe_gathers_per_s * (1 + 1 / 8)
+    return {"achieved": achieved, "peak": peak, "unit": "sectors/s", "frac": achieved / peak,
+            "floor_ms": sectors / peak * 1e3}
 
 
 def main_gather_probe(args, torch, tg, L):

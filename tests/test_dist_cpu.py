@@ -61,3 +61,4 @@ def test_single_rank_is_identity():
     import bench
     assert bench.max_over_ranks(torch, 3.5, 1) == 3.5
     assert bench.whole_job_rate(10, 2, 1, 0.5) == 40.0
+
