@@ -91,8 +91,10 @@ void prof_after(cudaStream_t st) {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr int kScratchSlots = 14;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3, formats x3,
-                                   // index validation, one-pass SpGEMM x2
+constexpr int kScratchSlots = 15;  // spmv, spmm, spgemm x2, tuner, pack, sddmm, tensor3, formats x3,
+                                   // index validation, one-pass SpGEMM x2, the pipelined SpMM's
+                                   // second product stream
+constexpr int kSpmmLaneSlot = 14;
 
 struct DeviceState {
   int sms = 0;
@@ -102,8 +104,9 @@ struct DeviceState {
   std::vector<void*> stage;
   std::vector<size_t> stage_cap;
   cudaStream_t stream = nullptr;
-  // the pipelined SpMV's copy streams (host -> device, device -> host) and chunk events
-  cudaStream_t h2d = nullptr, d2h = nullptr;
+  // the pipelined products' copy streams (host -> device, device -> host), the two streams of
+  // products that may overlap, and chunk events
+  cudaStream_t h2d = nullptr, d2h = nullptr, lanes[2] = {nullptr, nullptr};
   cudaEvent_t ev[2 * 16 + 1] = {};
   int* status = nullptr;  // device status word (see device_status())
   unsigned long long* mailbox = nullptr;  // mapped pinned host words (see host_mailbox())
@@ -252,7 +255,8 @@ cudaStream_t lib_stream() {
 }
 
 // The pipelined SpMV's two copy streams and its events (created once per device).
-bool pipeline_streams(cudaStream_t* h2d, cudaStream_t* d2h, cudaEvent_t** ev) {
+bool pipeline_streams(cudaStream_t* h2d, cudaStream_t* d2h, cudaStream_t* lanes,
+                      cudaEvent_t** ev) {
   std::lock_guard<std::mutex> lk(g_mu);
   DeviceState* ds = current_device();
   if (!ds) return false;
@@ -260,6 +264,12 @@ bool pipeline_streams(cudaStream_t* h2d, cudaStream_t* d2h, cudaEvent_t** ev) {
     return false;
   if (!ds->d2h && cudaStreamCreateWithFlags(&ds->d2h, cudaStreamNonBlocking) != cudaSuccess)
     return false;
+  for (int l = 0; l < 2; l++) {
+    if (!ds->lanes[l] &&
+        cudaStreamCreateWithFlags(&ds->lanes[l], cudaStreamNonBlocking) != cudaSuccess)
+      return false;
+    lanes[l] = ds->lanes[l];
+  }
   for (cudaEvent_t& e : ds->ev)
     if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return false;
   *h2d = ds->h2d;
@@ -893,24 +903,31 @@ int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
 // up to summation order within merge tiles.
 namespace {
 constexpr int kPipeChunks = 8;
+// chunk events: landed (j), product done (kPipeChunks + j), dense operand and pos in
+// (2 kPipeChunks), checked (2 kPipeChunks + 1 + j)
+static_assert(3 * kPipeChunks + 1 <= (int)(sizeof(DeviceState::ev) / sizeof(cudaEvent_t)),
+              "chunk events");
 constexpr int64_t kPipeMinNnz = (int64_t)1 << 23;  // below this, copy then compute
 
 // One kind of product of the pipeline.  reserve() takes any buffers it needs before the copies
 // are issued (an allocation later could wait on them); prepare() runs on the library stream
 // once the dense operand has landed; run() multiplies one chunk (rowop: the chunk's rows of the
-// row operand, when the product has one).
+// row operand, when the product has one).  A product whose lanes() is true may run two chunks
+// at the same time, on two streams (lane 0 and 1): each launch of a chunk ends in a partly
+// filled last wave, which the next chunk's start then fills.
 struct ChunkProduct {
   virtual ~ChunkProduct() = default;
   virtual int reserve(int32_t /*cols*/, int32_t /*N*/, int32_t /*btype*/, int /*vt*/) { return 0; }
   virtual int prepare(const void* /*dense*/, int32_t /*cols*/, int32_t /*N*/, cudaStream_t) {
     return 0;
   }
+  virtual bool lanes() const { return false; }
   virtual int run(const tacogb_csr* A, const void* dense, void* result, int32_t N, int32_t btype,
-                  const void* rowop, cudaStream_t st) = 0;
+                  const void* rowop, int lane, cudaStream_t st) = 0;
 };
 
-struct SpmvChunks final : ChunkProduct {
-  int run(const tacogb_csr* A, const void* x, void* y, int32_t, int32_t, const void*,
+struct SpmvChunks final : ChunkProduct {  // one lane: the SpMV products share scratch
+  int run(const tacogb_csr* A, const void* x, void* y, int32_t, int32_t, const void*, int,
           cudaStream_t st) override {
     return spmv_run(A, x, y, TACOGB_VARIANT_AUTO, st);
   }
@@ -934,9 +951,13 @@ struct SpmmChunks final : ChunkProduct {
   int prepare(const void* B, int32_t cols, int32_t N, cudaStream_t st) override {
     return bdf ? spmm_split_once((const double*)B, cols, N, bdf, flag, st) : 0;
   }
+  // over the split B the products can overlap: each lane has its own scratch
+  bool lanes() const override { return bdf != nullptr; }
   int run(const tacogb_csr* A, const void* B, void* C, int32_t N, int32_t btype, const void*,
-          cudaStream_t st) override {
-    if (bdf) return spmm_run_presplit(A, N, (const double*)B, bdf, flag, (double*)C, st);
+          int lane, cudaStream_t st) override {
+    if (bdf)
+      return spmm_run_presplit(A, N, (const double*)B, bdf, flag, (double*)C, st,
+                               lane ? kSpmmLaneSlot : 1);
     static const int df = spmm_variant_index("merge_w512_df");
     return spmm_run(A, N, B, btype, C, A->vtype == TACOGB_F64 ? df : TACOGB_VARIANT_AUTO, st);
   }
@@ -955,7 +976,8 @@ struct SddmmChunks final : ChunkProduct {
   int prepare(const void* D, int32_t cols, int32_t J, cudaStream_t st) override {
     return sddmm_pre_transpose(D, J, cols, vt, dt, st);
   }
-  int run(const tacogb_csr* B, const void* D, void* out, int32_t J, int32_t, const void* C,
+  bool lanes() const override { return true; }  // no scratch: chunks may overlap
+  int run(const tacogb_csr* B, const void* D, void* out, int32_t J, int32_t, const void* C, int,
           cudaStream_t st) override {
     return sddmm_pre_run(B, J, C, D, dt, out, st);
   }
@@ -963,8 +985,8 @@ struct SddmmChunks final : ChunkProduct {
 
 // MTTKRP's fiber product: the fiber level (a CSR of fibers over B's last mode) times D, one row
 // of J values per fiber, kept on the device for the combine.
-struct FiberSpmmChunks final : ChunkProduct {
-  int run(const tacogb_csr* F, const void* D, void* T, int32_t J, int32_t, const void*,
+struct FiberSpmmChunks final : ChunkProduct {  // one lane: spmm_run's scratch is shared
+  int run(const tacogb_csr* F, const void* D, void* T, int32_t J, int32_t, const void*, int,
           cudaStream_t st) override {
     static const int v = spmm_variant_index("stream_w512_dfs");  // as mttkrp_run
     return spmm_run(F, J, D, F->vtype, T, v, st);
@@ -984,9 +1006,9 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   const int32_t* pos = (const int32_t*)A->indices[1][0];
   const int32_t* crd = (const int32_t*)A->indices[1][1];
   const size_t vb = value_bytes(vt);
-  cudaStream_t st = lib_stream(), h2d, d2h;
+  cudaStream_t st = lib_stream(), h2d, d2h, lanes[2];
   cudaEvent_t* ev;
-  if (!st || !pipeline_streams(&h2d, &d2h, &ev)) {
+  if (!st || !pipeline_streams(&h2d, &d2h, lanes, &ev)) {
     set_error(TACOGB_ERR_CUDA, "%s: no GPU streams", what);
     return TACOGB_ERR_CUDA;
   }
@@ -1168,11 +1190,20 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
     const size_t r_dev = res_per_nnz ? (size_t)voff[j] : (size_t)rb[j];
     const size_t r_host = res_per_nnz ? (size_t)pos[rb[j]] : (size_t)rb[j];
     const size_t r_cnt = res_per_nnz ? (size_t)n : (size_t)nr;
+    // a product with two lanes runs its chunks on the two lane streams in turn, each after its
+    // chunk's check, so that the checks (in order on the library stream) never wait behind a
+    // product and two products can overlap
+    const bool two = prod.lanes();
+    const int lane = two ? (j & 1) : 0;
+    cudaStream_t ps = two ? lanes[lane] : st;
+    if (two && (!cu(cudaEventRecord(ev[2 * kPipeChunks + 1 + j], st)) ||
+                !cu(cudaStreamWaitEvent(ps, ev[2 * kPipeChunks + 1 + j], 0))))
+      break;
     rc = prod.run(&cj, ddense, dres + r_dev * res_unit_bytes, N, btype,
-                  drow ? drow + (size_t)rb[j] * rowop_row_bytes : nullptr, st);
+                  drow ? drow + (size_t)rb[j] * rowop_row_bytes : nullptr, lane, ps);
     if (rc) break;
-    if (dev_result) continue;
-    if (!cu(cudaEventRecord(ev[kPipeChunks + j], st)) ||
+    if (dev_result) continue;  // every stream is synchronised before the call returns
+    if (!cu(cudaEventRecord(ev[kPipeChunks + j], ps)) ||
         !cu(cudaStreamWaitEvent(d2h, ev[kPipeChunks + j], 0)))
       break;
     unsigned char* hres = (unsigned char*)result + r_host * res_unit_bytes;
@@ -1183,13 +1214,18 @@ int csr_product_pipelined(const char* what, const taco_tensor_t* A, int vt, int3
   }
   if (copier.joinable()) copier.join();
   // nothing may still be copying when the call returns, whatever happened
+  const cudaError_t e0a = cudaStreamSynchronize(lanes[0]), e0b = cudaStreamSynchronize(lanes[1]);
+  const cudaError_t e0 = e0a != cudaSuccess ? e0a : e0b;
   const cudaError_t e1 = cudaStreamSynchronize(h2d), e2 = cudaStreamSynchronize(st),
                     e3 = cudaStreamSynchronize(d2h);
   if (registered && cudaHostUnregister(result) != cudaSuccess) cudaGetLastError();
   if (rc) return rc;
-  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+  if (e0 != cudaSuccess || e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
     set_error(TACOGB_ERR_CUDA, "%s: %s", what,
-              cudaGetErrorString(e1 != cudaSuccess ? e1 : e2 != cudaSuccess ? e2 : e3));
+              cudaGetErrorString(e0 != cudaSuccess   ? e0
+                                 : e1 != cudaSuccess ? e1
+                                 : e2 != cudaSuccess ? e2
+                                                     : e3));
     return TACOGB_ERR_CUDA;
   }
   // the first chunk that failed, with its segment and position in the whole operand

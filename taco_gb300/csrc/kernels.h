@@ -27,12 +27,13 @@ int spmm_variant_index(const char* name);  // -1 when no variant has that name
 // double-float pairs) for several products over it, and the product of one CSR A over that
 // split (the merge_w512_dfs tile; an entry of B outside the double-float range, recorded in
 // *flag by the split, sends every tile to native FP64 over B).  Used by the pipelined taco-ABI
-// SpMM, whose chunks share one B.
+// SpMM, whose chunks share one B; products that may run at the same time on different streams
+// take different scratch slots (the partition and carries live there).
 bool spmm_presplit_applies(const void* B, int32_t N);
 int spmm_split_once(const double* B, int32_t cols, int32_t N, void* bdf, int* flag,
                     cudaStream_t st);
 int spmm_run_presplit(const tacogb_csr* A, int32_t N, const double* B, const void* bdf, int* flag,
-                      double* C, cudaStream_t st);
+                      double* C, cudaStream_t st, int scratch_slot = 1);
 int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,
              cudaStream_t st);
 

@@ -217,7 +217,7 @@ constexpr int kNumSpmmVariants = sizeof(kSpmmVariants) / sizeof(kSpmmVariants[0]
 // by spmm_split_once for several products; the fix-up then leaves the flag alone.
 template <class P, int VEC, bool STREAM, int TMA = 0>
 int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, cudaStream_t st,
-                const void* presplit = nullptr, int* pflag = nullptr) {
+                const void* presplit = nullptr, int* pflag = nullptr, int slot = 1) {
   const int64_t total = (int64_t)A->rows + A->nnz;
   const int64_t tiles64 = (total + W - 1) / W;
   if (tiles64 == 0 || N == 0) return 0;
@@ -229,7 +229,8 @@ int launch_spmm(const tacogb_csr* A, int32_t N, const void* B, void* C, int W, c
   constexpr bool split = std::is_same<P, MmDFS>::value;
   const size_t bdf_bytes =
       split && presplit == nullptr ? (size_t)A->cols * (size_t)N * sizeof(DF) : 0;
-  unsigned char* ws = (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + bdf_bytes, 1);
+  unsigned char* ws =
+      (unsigned char*)scratch(part_bytes + crow_bytes + cval_bytes + bdf_bytes, slot);
   if (!ws) return last_code();
   int2* part = (int2*)ws;
   int32_t* crow = (int32_t*)(ws + part_bytes);
@@ -438,15 +439,16 @@ int spmm_split_once(const double* B, int32_t cols, int32_t N, void* bdf, int* fl
 }
 
 int spmm_run_presplit(const tacogb_csr* A, int32_t N, const double* B, const void* bdf, int* flag,
-                      double* C, cudaStream_t st) {
+                      double* C, cudaStream_t st, int scratch_slot) {
   TACOGB_CHECK_ARG(A != nullptr && A->vtype == TACOGB_F64, "SpMM: pre-split B needs FP64 A");
   TACOGB_CHECK_ARG(A->rows >= 0 && A->cols >= 0 && A->nnz >= 0 && N >= 0, "SpMM: negative size");
   TACOGB_CHECK_ARG((int64_t)A->rows * N <= INT32_MAX,
                    "SpMM: rows*N exceeds taco's int32 dense positions");
   TACOGB_CHECK_ARG(spmm_presplit_applies(B, N), "SpMM: B split needs even N, 16-byte aligned B");
   static const int W = kSpmmVariants[spmm_variant_index("merge_w512_dfs")].tile_items;
-  if (N % 64 == 0) return launch_spmm<MmDFS, 2, false>(A, N, B, C, W, st, bdf, flag);
-  return launch_spmm<MmDFS, 1, false>(A, N, B, C, W, st, bdf, flag);
+  if (N % 64 == 0)
+    return launch_spmm<MmDFS, 2, false>(A, N, B, C, W, st, bdf, flag, scratch_slot);
+  return launch_spmm<MmDFS, 1, false>(A, N, B, C, W, st, bdf, flag, scratch_slot);
 }
 
 int spmm_run(const tacogb_csr* A, int32_t N, const void* B, int32_t btype, void* C, int variant,
