@@ -1372,19 +1372,19 @@ SECONDARY = [
      ["--workload", "spmv_small", "--steps", "500", "--warmup", "20", "--e2e-steps", "10",
       "--graph"]),
     ("spmv_banded_f64", ["--workload", "spmv_banded", "--steps", "50", "--warmup", "5",
-                         "--e2e-steps", "5"]),
+                         "--e2e-steps", "20"]),
     ("spmv_powerlaw_f32c", ["--workload", "spmv_powerlaw", "--dtype", "f32", "--steps", "50",
-                            "--warmup", "5", "--e2e-steps", "5"]),
+                            "--warmup", "5", "--e2e-steps", "20"]),
     ("spmm_powerlaw_n64_f64", ["--workload", "spmm_powerlaw", "--n", "64", "--steps", "20",
-                               "--warmup", "3", "--e2e-steps", "3"]),
+                               "--warmup", "3", "--e2e-steps", "10"]),
     ("spgemm_random_f64", ["--workload", "spgemm_random", "--steps", "20", "--warmup", "3",
-                           "--e2e-steps", "3"]),
+                           "--e2e-steps", "10"]),
     ("batched_spmv_4096_f32c_learned", ["--workload", "batched_spmv", "--dtype", "f32",
                                         "--select", "learned", "--steps", "5", "--warmup", "3"]),
     ("sddmm_powerlaw_j128_f64", ["--workload", "sddmm_powerlaw", "--steps", "10", "--warmup", "3",
-                                 "--e2e-steps", "5"]),
+                                 "--e2e-steps", "10"]),
     ("mttkrp_nell2_r32_f64", ["--workload", "mttkrp_nell2", "--steps", "20", "--warmup", "3",
-                              "--e2e-steps", "5"]),
+                              "--e2e-steps", "10"]),
 ]
 
 
