@@ -890,11 +890,12 @@ int tacogb_spmv_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
 }
 
 // A CSR product over host operands as a pipeline (SpMV: dense operand x, result y; SpMM: B and
-// C, N values per row; SDDMM: D, each chunk's rows of C, one value per nonzero): the rows are
-// cut into chunks of about equal nonzeros; one stream copies the dense operand, pos and then
-// every chunk's crd and values (and rows of the row operand) to the GPU, the library stream
-// checks and multiplies each chunk as soon as its copy has landed, and a third stream returns
-// each chunk's rows of the result.  The copies of later chunks overlap the checks, products and
+// C, N values per row; SDDMM: D, each chunk's rows of C, one value per nonzero; MTTKRP's fiber
+// product: D, fiber rows kept on the device): the rows are cut into chunks by nonzeros (equal
+// shares but smaller first and last chunks, below); one stream copies the dense operand, pos
+// and then every chunk's crd and values (and rows of the row operand) to the GPU, the library
+// stream checks each chunk as soon as its copy has landed and multiplies it (or hands it to one
+// of two lane streams), and a third stream returns each chunk's part of the result.  The copies of later chunks overlap the checks, products and
 // returns of earlier ones, so the call takes little more than its copies (the host link bounds
 // it).  The checks never wait for the host: a chunk that fails is rewritten on the device into
 // a harmless level before its product runs, and the verdicts are read after the last chunk, so
