@@ -1950,7 +1950,8 @@ int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3&
     int32_t p0 = 0;
     if (int rc = read_i32(pos0, &p0)) return rc;
     if (int rc = read_i32(pos0 + 1, &b.n0)) return rc;
-    TACOGB_CHECK_ARG(p0 == 0 && b.n0 >= 0, "operand B: level-0 pos must be {0, n}");
+    TACOGB_CHECK_ARG(p0 == 0 && b.n0 >= 0 && b.n0 <= b.dims[0],
+                     "operand B: level-0 pos must be {0, n} with n <= %d", b.dims[0]);
     crd0 = (const int32_t*)T->indices[0][1];
   }
   const int32_t* pos1 = (const int32_t*)T->indices[1][0];
@@ -2139,7 +2140,10 @@ int mttkrp_pipelined(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_
   for (const void* p : arrays)
     if (p == nullptr || device_accessible(p)) return 0;
   const int32_t n0 = dense0 ? B->dimensions[0] : pos0[1];
-  TACOGB_CHECK_ARG(n0 >= 0 && (dense0 || pos0[0] == 0), "order-3 operand B: bad level-0 pos");
+  // checked before pos1[n0] is read on the host
+  TACOGB_CHECK_ARG(n0 >= 0 && n0 <= B->dimensions[0] && (dense0 || pos0[0] == 0),
+                   "order-3 operand B: level-0 pos must be {0, n} with n <= %d",
+                   B->dimensions[0]);
   const int32_t nfib = pos1[n0];
   TACOGB_CHECK_ARG(nfib >= 0, "order-3 operand B: negative fiber count");
   const int32_t nnz = pos2[nfib];

@@ -146,3 +146,20 @@ def test_batch_plan_rejects_bad_arguments_without_gpu():
     assert L.tacogb_batch_create(2, mats, ptrs, ptrs, 0, None, ctypes.byref(h)) == 1
     assert b"bad size" in L.tacogb_last_error()
     assert L.tacogb_batch_run(None, None) == 1
+
+
+def test_csf_level0_count_checked_without_gpu():
+    """An order-3 operand whose level-0 pos claims more coordinates than B's first mode holds is
+    rejected on the host before pos1 is read at that count (no GPU needed)."""
+    from taco_gb300 import taco as T
+    e = np.zeros(0, np.int32)
+    Bt = T.csf3((5, 6, 7), np.arange(5, dtype=np.int32), np.zeros(6, np.int32), e,
+                np.zeros(1, np.int32), e, np.zeros(0))
+    bad_pos0 = np.array([0, 9], np.int32)  # n0 = 9 > 5
+    Bt.mode_arrays[0][0] = bad_pos0.ctypes.data
+    C, D = np.ones((6, 4)), np.ones((7, 4))
+    A = np.zeros((5, 4))
+    At, Ct, Dt = T.dense(A, [5, 4]), T.dense(C, [6, 4]), T.dense(D, [7, 4])
+    L = tg.lib()
+    assert L.tacogb_mttkrp_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr) == 1
+    assert b"level-0 pos" in L.tacogb_last_error()
