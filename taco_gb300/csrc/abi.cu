@@ -1960,6 +1960,10 @@ int csf3_operand(const taco_tensor_t* T, int base, cudaStream_t st, tacogb_csf3&
   const int32_t* crd2 = (const int32_t*)T->indices[2][1];
   TACOGB_CHECK_ARG(pos1 != nullptr && pos2 != nullptr, "operand B: null pos");
   if (int rc = read_i32(pos1 + b.n0, &b.nfib)) return rc;
+  // checked before pos2 is read at it: a valid level 1 holds at most n0 * dims[1] fibers
+  TACOGB_CHECK_ARG(b.nfib >= 0 && (int64_t)b.nfib <= (int64_t)b.n0 * b.dims[1],
+                   "operand B: level-1 pos ends at %d, more fibers than %d x %d", b.nfib, b.n0,
+                   b.dims[1]);
   int32_t nnz = 0;
   if (int rc = read_i32(pos2 + b.nfib, &nnz)) return rc;
   b.nnz = nnz;
@@ -2145,7 +2149,9 @@ int mttkrp_pipelined(taco_tensor_t* A, taco_tensor_t* B, taco_tensor_t* C, taco_
                    "order-3 operand B: level-0 pos must be {0, n} with n <= %d",
                    B->dimensions[0]);
   const int32_t nfib = pos1[n0];
-  TACOGB_CHECK_ARG(nfib >= 0, "order-3 operand B: negative fiber count");
+  TACOGB_CHECK_ARG(nfib >= 0 && (int64_t)nfib <= (int64_t)n0 * B->dimensions[1],
+                   "order-3 operand B: level-1 pos ends at %d, more fibers than %d x %d", nfib,
+                   n0, B->dimensions[1]);
   const int32_t nnz = pos2[nfib];
   if (!pipeline_applies(nnz, arrays) || J <= 0) return 0;
   *applied = true;

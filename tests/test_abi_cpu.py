@@ -163,3 +163,18 @@ def test_csf_level0_count_checked_without_gpu():
     L = tg.lib()
     assert L.tacogb_mttkrp_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr) == 1
     assert b"level-0 pos" in L.tacogb_last_error()
+
+
+def test_csf_fiber_count_checked_without_gpu():
+    """A level-1 pos whose end claims more fibers than n0 x dims[1] is rejected on the host
+    before pos2 is read at that count."""
+    from taco_gb300 import taco as T
+    e = np.zeros(0, np.int32)
+    pos1 = np.array([0, 0, 0, 0, 0, 1000], np.int32)  # 5 rows of level 0, 1000 > 5 x 6 fibers
+    Bt = T.csf3((5, 6, 7), np.arange(5, dtype=np.int32), pos1, e, np.zeros(1, np.int32), e,
+                np.zeros(0))
+    A, C, D = np.zeros((5, 4)), np.ones((6, 4)), np.ones((7, 4))
+    At, Ct, Dt = T.dense(A, [5, 4]), T.dense(C, [6, 4]), T.dense(D, [7, 4])
+    L = tg.lib()
+    assert L.tacogb_mttkrp_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr) == 1
+    assert b"level-1 pos" in L.tacogb_last_error()
