@@ -751,6 +751,9 @@ int dcsr_operand(const taco_tensor_t* A, int base, cudaStream_t st, tacogb_dcsr&
   d.cols = A->dimensions[1];
   d.vtype = value_type_of_csize(A->csize);
   if (int rc = read_i32(pos0 + 1, &d.n0)) return rc;
+  // checked before pos1 is read at it: at most one stored row per row of A
+  TACOGB_CHECK_ARG(d.n0 >= 0 && d.n0 <= d.rows, "DCSR: level-0 pos ends at %d, beyond %d rows",
+                   d.n0, d.rows);
   const int32_t* pos1 = (const int32_t*)A->indices[1][0];
   TACOGB_CHECK_ARG(pos1 != nullptr, "DCSR: null pos");
   int32_t nnz = 0;
@@ -810,6 +813,8 @@ int spmv_fmt_assemble(taco_tensor_t* y, taco_tensor_t* A, taco_tensor_t* x) {
   }
   int32_t n0 = 0;  // y's pattern: A's stored rows
   if (int rc = read_i32((const int32_t*)A->indices[0][0] + 1, &n0)) return rc;
+  TACOGB_CHECK_ARG(n0 >= 0 && n0 <= A->dimensions[0],
+                   "spmv: A's level-0 pos ends at %d, beyond %d rows", n0, A->dimensions[0]);
   int32_t* pos = (int32_t*)alloc_result(2 * sizeof(int32_t), managed);
   int32_t* crd = (int32_t*)alloc_result((size_t)n0 * 4, managed);
   void* vals = alloc_result((size_t)n0 * value_bytes(vt), managed);
@@ -1462,6 +1467,8 @@ int csr_operand(const char* what, const taco_tensor_t* T, int base, bool with_va
     if (doubly) {
       TACOGB_CHECK_ARG(T->indices[0] && T->indices[0][0], "spgemm: null level-0 pos");
       if (int rc = read_i32((const int32_t*)T->indices[0][0] + 1, &n0)) return rc;
+      TACOGB_CHECK_ARG(n0 >= 0 && n0 <= outer, "spgemm: level-0 pos ends at %d, beyond %d", n0,
+                       outer);
     }
     int32_t nnz = 0;
     if (int rc = read_i32(p1 + n0, &nnz)) return rc;

@@ -178,3 +178,4 @@ def test_csf_fiber_count_checked_without_gpu():
     L = tg.lib()
     assert L.tacogb_mttkrp_compute(At.ptr, Bt.ptr, Ct.ptr, Dt.ptr) == 1
     assert b"level-1 pos" in L.tacogb_last_error()
+
